@@ -1,0 +1,364 @@
+#!/usr/bin/env python
+"""Time-steps/s of the LeachingSim per-time-step hot path on GB300.
+
+Workload (the reference README shape): 338 x 338 x 283 voxels (--xext 338 --yext 338
+--zext 283, i.e. (I, J, K) = (283, 338, 338)), uint8 labels from a seeded Gaussian
+random field (porosity 0.25, correlation length 6, 15% of the solid reactive mineral,
+Air inlet planes i = 0, 1), D = 1, kreac = 1, dt = 1, tmax = 50, nout = 10, csat = 1.
+
+A "step" is one full time step of src/main.cpp:303-432 (props, pressure solve, flux,
+saturation, surface clogging, conc + acid transport, precipitation, dissolution,
+snapshot). `value` times --steps steps after --warmup steps with the state resident
+in HBM; `e2e` runs the whole configured simulation (tmax / dt steps) from a label
+image in pinned host memory, reading every output step's fields back into pinned
+host memory (file writing excluded).
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "time-steps/s at 338x338x283"
+UNIT = "time-steps/s"
+SHAPE = (283, 338, 338)  # (I, J, K) = (zext, yext, xext)
+GEOM = dict(porosity=0.25, corr_len=6.0, mineral_fraction=0.15, seed=0)
+DT, TMAX, NOUT = 1.0, 50.0, 10
+CPU_SAMPLE = (48, 96, 96)  # inlet block of the same geometry for the CPU baseline
+# output arrays of src/Simulation.cpp:1401-1485 (label, frac, 10 float64 fields)
+OUTPUT_FIELDS = ["label", "conc", "pressure", "frac", "flux_x", "flux_y", "flux_z", "saturation",
+                 "cap_pressure", "rel_perm", "permeability", "acid"]
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_geometry(shape):
+    from leachingsim_gb300.geometry import grf_geometry
+    lab, seed = grf_geometry(shape, air_inlet=True, **GEOM)
+    return lab, seed
+
+
+def params(solver):
+    from leachingsim_gb300._abi import PRESS_FP64, PRESS_JACOBI64, PRESS_MIXED, default_params
+    s = {"mixed": PRESS_MIXED, "fp64": PRESS_FP64, "jacobi64": PRESS_JACOBI64}[solver]
+    return default_params(c_sat=1.0, D=1.0, kreac=1.0, press_solver=s)
+
+
+# ---------------------------------------------------------------------------
+# clocks
+
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+class ClockSampler:
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={CLOCK_FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+
+def run_steps(ctx, t0, n0, count, dt):
+    """count accepted steps with the reference's retry manager; returns (t, n, infos)."""
+    t, n = t0, n0
+    infos = []
+    for _ in range(count):
+        cur = dt
+        while True:
+            ok, info = ctx.step(t, cur)
+            if ok:
+                break
+            ctx.rollback()
+            cur *= 0.5
+            if cur < 1e-3:
+                raise RuntimeError("time step shrank below 1 ms")
+        infos.append(info)
+        t += cur
+        n += 1
+    return t, n, infos
+
+
+def roofline(ctx, shape, nsteps):
+    """Roofline of the dominant kernel class, the transport operator apply (k_kry_v and
+    k_kry_t of the BiCGStab). The library accumulates its algorithmic bytes per launch:
+    N x (label 1 + own flux 3x8 + per live right-hand side: input 8 + output 8 + rhat or s 8);
+    one right-hand side is live in a fresh run (the acid field is zero)."""
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peaks = json.load(open(peaks_path)) if os.path.exists(peaks_path) else None
+    ms, cnt = ctx.timing_get("kry_apply")
+    nbytes = ctx.timing_bytes("kry_apply")
+    if cnt == 0 or ms <= 0:
+        return None
+    achieved = nbytes / (ms / 1e3) / 1e9
+    peak, src = (peaks["hbm_gbs"], "measured") if peaks else (6800.0, "fallback")
+    vox = shape[0] * shape[1] * shape[2]
+    return {"bound": "hbm", "kernel": "transport operator apply (k_kry_v, k_kry_t)",
+            "achieved": round(achieved, 1), "peak": peak, "peak_source": src, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": None,
+            "bytes_per_launch": round(nbytes / cnt), "bytes_per_voxel": round(nbytes / cnt / vox, 2),
+            "launches": cnt, "us_per_launch": round(ms * 1e3 / cnt, 2)}
+
+
+def gpu_arm(args, ws, rank, local):
+    import torch
+    from leachingsim_gb300.runtime import Context
+
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else SHAPE
+    t0 = time.time()
+    lab, seed = make_geometry(shape)
+    log(f"[rank {rank}] geometry {shape} seed {seed} in {time.time() - t0:.1f}s")
+    p = params(args.solver)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # ---- resident-state throughput ------------------------------------------------
+    ctx = Context(shape, label_bytes=1, params=p)
+    ctx.upload("label", lab)
+    ctx.init_all()
+    t, n, _ = run_steps(ctx, 0.0, 0, args.warmup, DT)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.timing(True)
+    ctx.timing_reset()
+    barrier()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        w0 = time.perf_counter()
+        t, n, infos = run_steps(ctx, t, n, args.steps, DT)
+        ev1.record(stream)
+        ev1.synchronize()
+        wall = time.perf_counter() - w0
+    barrier()
+    dev_ms = ev0.elapsed_time(ev1)
+    launches = ctx.launches()
+    classes = {k: ctx.timing_get(k) for k in ("props", "press_setup", "press_inner", "press_outer",
+                                              "flux", "saturation", "transport", "precip",
+                                              "dissolve", "snapshot", "kry_apply", "cg_apply")}
+    roof = roofline(ctx, shape, args.steps)
+    ctx.timing(False)
+    mem = ctx.device_bytes()
+    ctx.close()
+    t_max = dev_ms / 1e3
+    if ws > 1:
+        tt = torch.tensor([t_max], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(tt.item())
+
+    # ---- end to end: full configured run from a host image ---------------------------
+    e2e = None
+    if not args.no_e2e:
+        nsteps = int(round(TMAX / DT))
+        pinned_lab = torch.empty(lab.size, dtype=torch.uint8, pin_memory=True)
+        pinned_lab.numpy()[:] = lab.ravel()
+        N = lab.size
+        out_bufs = {}
+        for f in OUTPUT_FIELDS:
+            dt_ = torch.uint8 if f == "label" else (torch.float32 if f == "frac" else torch.float64)
+            out_bufs[f] = torch.empty(N, dtype=dt_, pin_memory=True).numpy()
+        barrier()
+        w0 = time.perf_counter()
+        ctx = Context(shape, label_bytes=1, params=p)
+        ctx.upload("label", pinned_lab.numpy())
+        ctx.init_all()
+        h2d = N
+        d2h = 0
+        te, ne = 0.0, 0
+        for _ in range(nsteps):
+            te, ne, _ = run_steps(ctx, te, ne, 1, DT)
+            if (ne - 1) % NOUT == 0:
+                ctx.props()   # property sync before output (src/main.cpp:491-494)
+                for f in OUTPUT_FIELDS:
+                    ctx.download(f, out=out_bufs[f])
+                    d2h += out_bufs[f].nbytes
+        ctx.synchronize()
+        e2e_wall = time.perf_counter() - w0
+        ctx.close()
+        if ws > 1:
+            tt = torch.tensor([e2e_wall], device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            e2e_wall = float(tt.item())
+        e2e = {"value": round(ws * nsteps / e2e_wall, 4), "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d / nsteps), "d2h_bytes_per_step": int(d2h / nsteps),
+               "steps": nsteps, "wall_s": round(e2e_wall, 3),
+               "note": "fresh run from a pinned host label image, every nout-th step's fields read back to pinned host memory"}
+
+    if rank != 0:
+        return None
+    cpu = None
+    if ws == 1 and not args.no_cpu:
+        cpu = cpu_sample(args.cpu_steps, 1, None)
+    value = ws * args.steps / t_max
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "338x338x283 uint8 GRF geometry (porosity 0.25, corr 6, 15% mineral, "
+                               "Air inlet), dt 1, tmax 50, nout 10, D 1, kreac 1, csat 1",
+                   "shape_ijk": list(shape), "seed": seed, "press_solver": args.solver,
+                   "parallelism": f"replicas{ws}", "l2": "working set > L2 (state %.1f GB)" % (mem / 1e9)},
+        "wall_ms_per_step": round(wall * 1e3 / args.steps, 3),
+        "gpu_launches": launches,
+        "device_bytes": mem,
+        "timers_ms": {k: round(v[0], 3) for k, v in classes.items()},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clk.summary(),
+    }
+    return line
+
+
+# ---------------------------------------------------------------------------
+# CPU: the oracle's reference-algorithm mode (assembled operators, GMRES(30)+Jacobi,
+# rtol 1e-6, two KSPSolve calls per solve) on an inlet block of the same geometry
+
+def cpu_sample(steps, warmup, threads):
+    from oracle import oracle as om
+    full = SHAPE[0] * SHAPE[1] * SHAPE[2]
+    lab, _ = make_geometry(SHAPE)
+    sub = np.ascontiguousarray(lab[:CPU_SAMPLE[0], :CPU_SAMPLE[1], :CPU_SAMPLE[2]])
+    nthreads = threads or os.cpu_count() or 1
+    o = om.Oracle(sub.shape, params=params("fp64"), mode=om.SOLVE_REFERENCE, threads=nthreads)
+    o.set_solver(om.SOLVE_REFERENCE)
+    o.load_labels(sub)
+    o.init_all()
+    t = 0.0
+    for n in range(warmup):
+        o.step(t, DT)
+        t += DT
+    w0 = time.perf_counter()
+    for n in range(steps):
+        ok, _ = o.step(t, DT)
+        if not ok:
+            raise RuntimeError("CPU reference step failed")
+        t += DT
+    wall = time.perf_counter() - w0
+    sample_rate = steps / wall
+    scale = sub.size / full
+    return {"value": round(sample_rate * scale, 6), "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": (f"{steps} warm steps (after {warmup} warm-up) of the {CPU_SAMPLE[0]}x{CPU_SAMPLE[1]}x"
+                       f"{CPU_SAMPLE[2]} inlet block (i,j,k) of the same geometry, oracle reference-"
+                       f"algorithm mode (GMRES(30)+Jacobi rtol 1e-6, KSPSolve twice); sample rate "
+                       f"{sample_rate:.3f} steps/s scaled by voxel count {sub.size}/{full}"),
+            "sample_steps_per_s": round(sample_rate, 4), "wall_s": round(wall, 3)}
+
+
+def reference_arm(args, ws, rank):
+    if rank != 0:
+        return None
+    cpu = cpu_sample(args.steps, args.warmup, None)
+    return {
+        "impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 / cpu["value"], 3) if cpu["value"] else None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "338x338x283 uint8 GRF geometry (porosity 0.25, corr 6, 15% mineral, "
+                               "Air inlet), dt 1, tmax 50, nout 10, D 1, kreac 1, csat 1",
+                   "shape_ijk": list(SHAPE), "parallelism": "host cores"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--solver", default="mixed", choices=["mixed", "fp64", "jacobi64"])
+    ap.add_argument("--shape", default=None, help="override (I,J,K) for quick checks")
+    ap.add_argument("--cpu-steps", type=int, default=20)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if args.warmup < 3 and args.impl == "ours":
+        log("note: fewer than 3 warm-up steps")
+    if args.impl == "reference":
+        line = reference_arm(args, ws, rank)
+    else:
+        line = gpu_arm(args, ws, rank, local)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,264 @@
+/*
+ * leachingsim.h - C-ABI of the GB300 LeachingSim per-time-step hot path.
+ *
+ * One opaque context (ls_ctx) owns every device buffer of one simulation
+ * domain and one CUDA stream. All entry points are plain C: pointers, sizes
+ * and POD structs only, no C++ or torch types. Host pointers passed in are
+ * borrowed for the duration of the call. Every call returns an ls_status and
+ * never throws or aborts; ls_last_error() gives the message of the last
+ * failure on a context.
+ *
+ * Grid and layout (the reference's ZFastest scheme, src/Domain.cpp:107-117,
+ * src/main.cpp:94): extents (I, J, K) = (zext, yext, xext); voxel (i, j, k)
+ * has linear index  k + K*(j + J*i), k fastest, which is also the byte order
+ * of the .raw input (src/MPIRawLoader.h:70).
+ *
+ * Every field lives on the device with (I+1)*J*K "slots": the reference's
+ * padded single-rank array (src/MPIDomain.h:75-97 clips only the lower halo on
+ * rank 0, so one extra top plane remains). Unpadded host transfers cover slots
+ * [0, I*J*K); padded transfers cover all (I+1)*J*K slots, byte-compatible with
+ * the reference's checkpoint arrays (src/Simulation.cpp:2235-2267).
+ *
+ * Label values follow src/compiler_opts.h:70-82: Air=1, Pore=2, Rock=3,
+ * Sulphide=4, Precipitate=5; any other value is carried through with the
+ * reference's semantics for "none of the above".
+ */
+#ifndef LEACHINGSIM_H_
+#define LEACHINGSIM_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LS_ABI_VERSION 1
+
+enum {
+    LS_AIR = 1,
+    LS_PORE = 2,
+    LS_ROCK = 3,
+    LS_SULPHIDE = 4,
+    LS_PRECIPITATE = 5
+};
+
+typedef enum ls_status {
+    LS_OK = 0,
+    LS_NOT_CONVERGED = 1,            /* a linear solve hit its iteration cap */
+    LS_STAGNATED_FALLBACK_USED = 2,  /* accepted, but only after a fallback solver ran */
+    LS_NONFINITE = 3,                /* NaN/Inf met in a residual or a field */
+    LS_BAD_ARG = 4,
+    LS_CUDA_ERROR = 5,
+    LS_TIMEOUT = 6,                  /* a bounded device wait gave up */
+    LS_NO_DEVICE = 7,
+    LS_UNPHYSICAL = 8                /* implicit saturation left [-0.05, 1.05] (src/Simulation.cpp:2008) */
+} ls_status;
+
+/* Field identifiers for upload/download. */
+typedef enum ls_field {
+    LS_F_LABEL = 0,        /* img_data, uint8 or uint16 per label_bytes */
+    LS_F_FRAC = 1,         /* frac, float32 */
+    LS_F_PERMEABILITY = 2, /* float64 from here on */
+    LS_F_VISCOSITY = 3,
+    LS_F_PRESSURE = 4,
+    LS_F_CONC = 5,
+    LS_F_ACID = 6,
+    LS_F_FLUX_X = 7,       /* flux along i (Z, vertical) */
+    LS_F_FLUX_Y = 8,
+    LS_F_FLUX_Z = 9,       /* flux along k (X, fastest) */
+    LS_F_SATURATION = 10,
+    LS_F_CAP_PRESSURE = 11,
+    LS_F_REL_PERM = 12,
+    LS_F_PRECIPITATE = 13,
+    LS_F_COUNT = 14
+} ls_field;
+
+/* Pressure solver variants. */
+typedef enum ls_press_solver {
+    LS_PRESS_MIXED = 0,    /* FP32 MG-PCG inner solves, FP64 iterative refinement outside */
+    LS_PRESS_FP64 = 1,     /* FP64 MG-PCG inner solves (the plain path) */
+    LS_PRESS_JACOBI64 = 2  /* FP64 Jacobi-PCG inner solves (no multigrid; test path) */
+} ls_press_solver;
+
+/*
+ * Physical and numerical parameters. Field names follow Simulation's public
+ * members (src/Simulation.h:75-114) and the CLI (src/main.cpp:39, 69-91).
+ * ls_params_default() fills the CLI defaults.
+ */
+typedef struct ls_params {
+    double D;                 /* --D */
+    double dx;                /* --voxel_size */
+    double Dpore_fac;         /* --Dpore_fac */
+    double kext;              /* --kext (kept for interface parity; unused by the physics) */
+    double kreac;             /* --kreac */
+    double theta;             /* --theta */
+    double c_sat;             /* --csat */
+    double evaporative_flux;  /* --evap_flux */
+    double top_pressure;      /* --top_pressure */
+    double max_cap_grad;      /* --max_cap_grad */
+    double vg_alpha;          /* 1.0, src/main.cpp:90 */
+    double vg_n;              /* 2.0, src/main.cpp:89 */
+    double s_res;             /* 0.05, src/main.cpp:91 */
+    double porosity;          /* --porosity */
+    double time_scalar;       /* --time_scalar */
+    double rock_D_fac;        /* --rock_D_fac (unused by the active transport code) */
+    double alpha_transfer;    /* --alpha_transfer */
+    double solid_density;     /* never initialised by the reference (src/Simulation.h:135); default 1.0 */
+    int use_instant_precipitation; /* --instant_precip */
+    int use_implicit_saturation;   /* --implicit_sat */
+    int enable_microporosity;      /* --enable_microporosity (unused by the active code) */
+    int debug_mode;                /* --debug: enables device NaN audits */
+    int compat_shift;   /* 1 (default): linear-solve results land one i-plane up, as on the
+                           reference's rank 0 (src/Simulation.cpp:808,1247,1975,2173);
+                           0: corrected, results land in their own slots */
+    /* Linear solver controls (the reference: GMRES(30)+Jacobi, rtol 1e-6, max_it 1e4,
+       src/Simulation.cpp:146-157). rtol is on the Jacobi-scaled residual
+       ||D^-1 (b - A x)||_2 / ||D^-1 b||_2, the norm PETSc's left-preconditioned
+       GMRES tests. */
+    double press_rtol;
+    int press_max_it;         /* cap on inner Krylov iterations summed over refinement sweeps */
+    int press_solver;         /* ls_press_solver */
+    double conc_rtol;         /* conc and acid transport solves */
+    int conc_max_it;
+    double sat_rtol;          /* implicit saturation solve */
+    int sat_max_it;
+} ls_params;
+
+/* Result of one linear solve (the reference's log line, src/Simulation.cpp:834-849). */
+typedef struct ls_solve_info {
+    int iterations;           /* inner Krylov iterations */
+    int outer_iterations;     /* refinement sweeps (pressure) */
+    int converged;            /* 1 = the reference's reason > 0 */
+    int reason;               /* >0 converged, <0 diverged (PETSc-style codes: 2 rtol, -3 its, -4 nan) */
+    double rel_residual;      /* final Jacobi-scaled relative residual, FP64 */
+    double min_value;         /* min / max over the solution vector (I*J*K rows) */
+    double max_value;
+} ls_solve_info;
+
+/* Sub-stepping summary (src/Simulation.cpp:455-464, 1770-1779). */
+typedef struct ls_substep_info {
+    double max_rate;          /* max |div q| + evap (saturation) or max fractional rate (leaching) */
+    int num_steps;
+    double dt_sub;
+} ls_substep_info;
+
+/* One full time step (src/main.cpp:303-432). */
+typedef struct ls_step_info {
+    ls_solve_info pressure;
+    ls_substep_info saturation;
+    ls_solve_info saturation_solve;  /* implicit saturation only, last Picard iteration */
+    ls_solve_info conc;
+    ls_solve_info acid;
+    ls_substep_info leaching;
+    int leached;              /* voxels fully leached this step */
+    int picard_iterations;
+    int success;              /* 0 = the retry manager must roll back and halve dt */
+} ls_step_info;
+
+typedef struct ls_ctx ls_ctx;
+
+void ls_params_default(ls_params* p);
+int ls_abi_version(void);
+
+/* Context life cycle. label_bytes is 1 (uint8 images) or 2 (uint16).
+   Replaces Simulation::setupDomain + setupPETSc (src/Simulation.cpp:81-103, 131-159). */
+ls_status ls_create(ls_ctx** out, int I, int J, int K, int label_bytes, const ls_params* params);
+ls_status ls_destroy(ls_ctx* ctx);
+const char* ls_last_error(const ls_ctx* ctx);
+ls_status ls_set_params(ls_ctx* ctx, const ls_params* params);
+ls_status ls_get_params(const ls_ctx* ctx, ls_params* params);
+/* The context's CUDA stream (a cudaStream_t) for event timing by callers. */
+void* ls_stream(ls_ctx* ctx);
+ls_status ls_synchronize(ls_ctx* ctx);
+/* Device bytes held by the context. */
+size_t ls_device_bytes(const ls_ctx* ctx);
+
+/* Host <-> device transfers. n_elems must be I*J*K (padded=0) or (I+1)*J*K (padded=1).
+   The label upload replaces Simulation::readRAW's array (src/Simulation.cpp:68-74). */
+ls_status ls_upload_field(ls_ctx* ctx, ls_field f, const void* host, size_t n_elems, int padded);
+ls_status ls_download_field(ls_ctx* ctx, ls_field f, void* host, size_t n_elems, int padded);
+/* Device-to-device variants (pointers in this process's CUDA context). */
+ls_status ls_upload_field_device(ls_ctx* ctx, ls_field f, const void* dev, size_t n_elems, int padded);
+ls_status ls_download_field_device(ls_ctx* ctx, ls_field f, void* dev, size_t n_elems, int padded);
+
+/* Initialisation (src/Simulation.cpp:165-180, 254-278, 285-310, 1573-1590, 109-125). */
+ls_status ls_init_fields(ls_ctx* ctx);
+ls_status ls_init_frac(ls_ctx* ctx, unsigned long long* initial_sulphide_count);
+ls_status ls_init_saturation(ls_ctx* ctx);
+ls_status ls_init_acid(ls_ctx* ctx);
+
+/* Simulation::updateRelativePermeability + updateCapillaryPressure + initProperties,
+   fused (src/Simulation.cpp:1634-1664, 1596-1628, 187-248). */
+ls_status ls_props(ls_ctx* ctx);
+/* Simulation::setupPressureEqns(t) + solvePressure (src/Simulation.cpp:658-855). */
+ls_status ls_pressure_step(ls_ctx* ctx, double t, ls_solve_info* info);
+/* Simulation::calculateFlux (src/Simulation.cpp:866-953). */
+ls_status ls_flux(ls_ctx* ctx);
+/* Simulation::updateSaturation(dt), explicit sub-stepping (src/Simulation.cpp:1672-1856). */
+ls_status ls_saturation(ls_ctx* ctx, double dt, ls_substep_info* info);
+/* Simulation::setupSaturationEqns(dt) + solveSaturation (src/Simulation.cpp:1858-2053).
+   Returns LS_UNPHYSICAL when the solution leaves [-0.05, 1.05]. */
+ls_status ls_saturation_implicit(ls_ctx* ctx, double dt, ls_solve_info* info);
+/* Simulation::handleSurfaceEffects (src/Simulation.cpp:2063-2103). */
+ls_status ls_surface(ls_ctx* ctx);
+/* Simulation::setupConcentrationEqns + solveConc / solveAcid (src/Simulation.cpp:966-1295,
+   2167-2224). which: bit 0 = conc, bit 1 = acid; both share one matrix and are solved as
+   one two-right-hand-side solve. */
+ls_status ls_transport(ls_ctx* ctx, double dt, int which, ls_solve_info* conc_info,
+                       ls_solve_info* acid_info);
+/* Simulation::handlePrecipitation (src/Simulation.cpp:2114-2165). */
+ls_status ls_precip(ls_ctx* ctx);
+/* Simulation::updateFrac(dt) (src/Simulation.cpp:315-617); *leached = voxels flipped. */
+ls_status ls_dissolve(ls_ctx* ctx, double dt, int* leached, ls_substep_info* info);
+/* Simulation::saveState / restoreState (src/Simulation.cpp:2312-2353); rollback also
+   rebuilds the derived properties like the reference. */
+ls_status ls_snapshot(ls_ctx* ctx);
+ls_status ls_rollback(ls_ctx* ctx);
+/* One attempt of the time step of src/main.cpp:303-432 (no output, no retry):
+   snapshot, Picard loop (props, pressure, flux, saturation), surface effects,
+   conc and acid transport, precipitation, dissolution. info->success==0 means
+   the caller's retry manager must ls_rollback and halve dt. */
+ls_status ls_step(ls_ctx* ctx, double t, double dt, ls_step_info* info);
+
+/* Test hooks. y = A x for the assembled pressure operator of src/Simulation.cpp:674-792
+   (rows of Air/Rock/Sulphide/Precipitate are identity, rows of other non-Pore labels are
+   empty), after ls_pressure_setup(t). x, y are host float64 arrays of I*J*K. */
+ls_status ls_pressure_setup(ls_ctx* ctx, double t);
+ls_status ls_pressure_apply(ls_ctx* ctx, const double* x_host, double* y_host);
+/* Right-hand side b of that system (host float64, I*J*K). */
+ls_status ls_pressure_rhs(ls_ctx* ctx, double* b_host);
+/* y = A x for the transport operator of src/Simulation.cpp:1129-1232 at time step dt. */
+ls_status ls_transport_apply(ls_ctx* ctx, double dt, const double* x_host, double* y_host);
+
+/* Per-kernel-class device timing (CUDA events on the context stream). */
+typedef enum ls_timer {
+    LS_T_PROPS = 0,
+    LS_T_PRESS_SETUP = 1,
+    LS_T_PRESS_INNER = 2,   /* inner PCG iterations incl. the multigrid preconditioner */
+    LS_T_PRESS_OUTER = 3,   /* FP64 residual + refinement update */
+    LS_T_FLUX = 4,
+    LS_T_SATURATION = 5,
+    LS_T_TRANSPORT = 6,
+    LS_T_PRECIP = 7,
+    LS_T_DISSOLVE = 8,
+    LS_T_SNAPSHOT = 9,
+    LS_T_KRY_APPLY = 10,    /* each transport / implicit-saturation operator-apply launch */
+    LS_T_CG_APPLY = 11,     /* each inner pressure operator-apply launch */
+    LS_T_COUNT = 12
+} ls_timer;
+ls_status ls_timing_enable(ls_ctx* ctx, int enable);
+ls_status ls_timing_reset(ls_ctx* ctx);
+/* Total milliseconds and number of timed regions recorded for a class since the last reset. */
+ls_status ls_timing_get(ls_ctx* ctx, ls_timer t, double* total_ms, long long* count);
+/* Algorithmic bytes (compulsory reads + writes) moved by the timed launches of a class
+   since the last reset; defined for LS_T_KRY_APPLY and LS_T_CG_APPLY. */
+ls_status ls_timing_bytes(ls_ctx* ctx, ls_timer t, double* bytes);
+/* Count of kernel launches issued by the library since the last reset. */
+long long ls_kernel_launches(const ls_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LEACHINGSIM_H_ */

@@ -1,0 +1,621 @@
+// ls_api.cu - C-ABI entry points, context life cycle, transfers, snapshot, timing and
+// the time-step orchestration of src/main.cpp:303-432.
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "ls_internal.cuh"
+
+using namespace ls;
+
+namespace ls {
+
+ls_status set_error(ls_ctx* c, ls_status st, const std::string& msg) {
+    if (c) c->err = msg;
+    return st;
+}
+
+ls_status check_cuda(ls_ctx* c, cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    return set_error(c, LS_CUDA_ERROR, m);
+}
+
+ls_status dalloc(ls_ctx* c, void** p, size_t bytes) {
+    if (bytes == 0) bytes = 256;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        char buf[160];
+        snprintf(buf, sizeof(buf), "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+        return set_error(c, LS_CUDA_ERROR, buf);
+    }
+    c->device_bytes += bytes;
+    return LS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// timing
+
+static cudaEvent_t take_event(ls_ctx* c) {
+    if (!c->event_pool.empty()) {
+        cudaEvent_t e = c->event_pool.back();
+        c->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void region_begin(ls_ctx* c, int timer, cudaEvent_t* start) {
+    (void)timer;
+    *start = nullptr;
+    if (!c->timing) return;
+    *start = take_event(c);
+    cudaEventRecord(*start, c->stream);
+}
+
+void region_end(ls_ctx* c, int timer, cudaEvent_t start) {
+    if (!c->timing || !start) return;
+    cudaEvent_t stop = take_event(c);
+    cudaEventRecord(stop, c->stream);
+    c->regions.push_back(TimedRegion{timer, start, stop});
+}
+
+static void resolve_regions(ls_ctx* c) {
+    if (c->regions.empty()) return;
+    cudaStreamSynchronize(c->stream);
+    for (auto& r : c->regions) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, r.start, r.stop);
+        c->timer_ms[r.timer] += ms;
+        c->timer_count[r.timer] += 1;
+        c->event_pool.push_back(r.start);
+        c->event_pool.push_back(r.stop);
+    }
+    c->regions.clear();
+}
+
+// ---------------------------------------------------------------------------
+// reductions
+
+ls_status finalize_sum(ls_ctx* c, int nblocks, int nvals, int out_slot) {
+    LS_LAUNCH(c, k_finalize<false>, 1, 32, 0, c->partials, nblocks, nvals, c->scal + out_slot);
+    return LS_OK;
+}
+
+ls_status finalize_max(ls_ctx* c, int nblocks, int nvals, int out_slot) {
+    LS_LAUNCH(c, k_finalize<true>, 1, 32, 0, c->partials, nblocks, nvals, c->scal + out_slot);
+    return LS_OK;
+}
+
+ls_status read_scalars(ls_ctx* c, int first, int count, double* out) {
+    LS_CUDA(c, cudaMemcpyAsync(c->h_scal + first, c->scal + first, sizeof(double) * count,
+                               cudaMemcpyDeviceToHost, c->stream));
+    LS_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (int q = 0; q < count; ++q) out[q] = c->h_scal[first + q];
+    return LS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// initialisation kernels
+
+// Simulation::initFrac, src/Simulation.cpp:254-278 (the count uses an integer atomic,
+// which is order-independent).
+template <typename L>
+__global__ void k_init_frac(Grid g, const L* __restrict__ label, float* __restrict__ frac,
+                            unsigned long long* __restrict__ count) {
+    unsigned long long local = 0;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        if ((int)label[r] == kSulphide) {
+            frac[r] = 1.0f;
+            local++;
+        } else {
+            frac[r] = 0.0f;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
+}
+
+ls_status init_frac_run(ls_ctx* c, unsigned long long* count) {
+    unsigned long long* d = reinterpret_cast<unsigned long long*>(c->d_int);
+    LS_CUDA(c, cudaMemsetAsync(d, 0, sizeof(unsigned long long), c->stream));
+    int grid = grid_for(c, c->g.N);
+    if (c->label_bytes == 1)
+        LS_LAUNCH(c, k_init_frac<uint8_t>, grid, kBlock, 0, c->g, (const uint8_t*)c->label, c->frac, d);
+    else
+        LS_LAUNCH(c, k_init_frac<uint16_t>, grid, kBlock, 0, c->g, (const uint16_t*)c->label, c->frac, d);
+    unsigned long long h = 0;
+    LS_CUDA(c, cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    LS_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->initial_sulphide_count = h;
+    if (count) *count = h;
+    return LS_OK;
+}
+
+// Simulation::initSaturation, src/Simulation.cpp:1573-1590.
+template <typename L>
+__global__ void k_init_sat(Grid g, const L* __restrict__ label, double* __restrict__ sat) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        int t = (int)label[r];
+        sat[r] = (t == kPore || t == kSulphide) ? 0.1 : 0.0;
+    }
+}
+
+ls_status init_saturation_run(ls_ctx* c) {
+    int grid = grid_for(c, c->g.N);
+    if (c->label_bytes == 1)
+        LS_LAUNCH(c, k_init_sat<uint8_t>, grid, kBlock, 0, c->g, (const uint8_t*)c->label, c->sat);
+    else
+        LS_LAUNCH(c, k_init_sat<uint16_t>, grid, kBlock, 0, c->g, (const uint16_t*)c->label, c->sat);
+    return LS_OK;
+}
+
+}  // namespace ls
+
+// ===========================================================================
+// C-ABI
+
+
+static void* field_ptr(ls_ctx* c, ls_field f, size_t* esz) {
+    switch (f) {
+    case LS_F_LABEL: *esz = (size_t)c->label_bytes; return c->label;
+    case LS_F_FRAC: *esz = 4; return c->frac;
+    case LS_F_PERMEABILITY: *esz = 8; return c->perm;
+    case LS_F_VISCOSITY: *esz = 8; return c->visc;
+    case LS_F_PRESSURE: *esz = 8; return c->P;
+    case LS_F_CONC: *esz = 8; return c->conc;
+    case LS_F_ACID: *esz = 8; return c->acid;
+    case LS_F_FLUX_X: *esz = 8; return c->fx;
+    case LS_F_FLUX_Y: *esz = 8; return c->fy;
+    case LS_F_FLUX_Z: *esz = 8; return c->fz;
+    case LS_F_SATURATION: *esz = 8; return c->sat;
+    case LS_F_CAP_PRESSURE: *esz = 8; return c->pc;
+    case LS_F_REL_PERM: *esz = 8; return c->kr;
+    case LS_F_PRECIPITATE: *esz = 8; return c->precip;
+    default: return nullptr;
+    }
+}
+
+extern "C" {
+
+void ls_params_default(ls_params* p) {
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    // src/main.cpp:39 defaults
+    p->D = 1.0;
+    p->dx = 1.0;
+    p->Dpore_fac = 1.0;
+    p->kext = 1.0;
+    p->kreac = 1.0;
+    p->theta = 1.0;
+    p->c_sat = 0.95;
+    p->evaporative_flux = 0.0;
+    p->top_pressure = 10000.0;
+    p->max_cap_grad = 50000.0;
+    p->porosity = 0.1;
+    p->time_scalar = 1.0;
+    p->rock_D_fac = 1e-4;
+    p->alpha_transfer = 1e-5;
+    // src/main.cpp:89-91
+    p->vg_n = 2.0;
+    p->vg_alpha = 1.0;
+    p->s_res = 0.05;
+    // never set by the reference (src/Simulation.h:135)
+    p->solid_density = 1.0;
+    p->compat_shift = 1;
+    p->press_rtol = 1e-8;
+    p->press_max_it = 10000;
+    p->press_solver = LS_PRESS_MIXED;
+    p->conc_rtol = 1e-10;
+    p->conc_max_it = 10000;
+    p->sat_rtol = 1e-10;
+    p->sat_max_it = 10000;
+}
+
+int ls_abi_version(void) { return LS_ABI_VERSION; }
+
+static ls_status validate_params(ls_ctx* c, const ls_params* p) {
+    if (!(p->dx > 0.0)) return set_error(c, LS_BAD_ARG, "dx (voxel_size) must be > 0");
+    if (!(p->porosity > 0.0)) return set_error(c, LS_BAD_ARG, "porosity must be > 0");
+    if (!(p->vg_n > 1.0)) return set_error(c, LS_BAD_ARG, "vg_n must be > 1");
+    if (p->press_max_it < 1 || p->conc_max_it < 1 || p->sat_max_it < 1)
+        return set_error(c, LS_BAD_ARG, "max_it must be >= 1");
+    if (p->press_solver < LS_PRESS_MIXED || p->press_solver > LS_PRESS_JACOBI64)
+        return set_error(c, LS_BAD_ARG, "unknown press_solver");
+    return LS_OK;
+}
+
+ls_status ls_create(ls_ctx** out, int I, int J, int K, int label_bytes, const ls_params* params) {
+    if (!out) return LS_BAD_ARG;
+    *out = nullptr;
+    if (I < 2 || J < 2 || K < 2) return LS_BAD_ARG;
+    if (label_bytes != 1 && label_bytes != 2) return LS_BAD_ARG;
+    long long JK = (long long)J * K;
+    long long NP = (long long)(I + 1) * JK;
+    if (NP >= (1LL << 31) - 1) return LS_BAD_ARG;  // 32-bit voxel ids in the dissolution lists
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return LS_NO_DEVICE;
+
+    ls_ctx* c = new (std::nothrow) ls_ctx();
+    if (!c) return LS_BAD_ARG;
+    c->g.I = I; c->g.J = J; c->g.K = K;
+    c->g.JK = JK;
+    c->g.N = (long long)I * JK;
+    c->g.NP = NP;
+    c->label_bytes = label_bytes;
+    if (params) c->p = *params; else ls_params_default(&c->p);
+    ls_status st = validate_params(c, &c->p);
+    if (st != LS_OK) { delete c; return st; }
+    cudaGetDevice(&c->device);
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (c->num_sms < 1) c->num_sms = 1;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return LS_CUDA_ERROR;
+    }
+    const size_t np = (size_t)NP, n = (size_t)c->g.N;
+#define ALLOC(ptr, count)                                                     \
+    do {                                                                      \
+        st = dalloc_t(c, &(ptr), (count));                                    \
+        if (st != LS_OK) { ls_destroy(c); return st; }                         \
+        cudaMemsetAsync((ptr), 0, sizeof(*(ptr)) * (count), c->stream);       \
+    } while (0)
+    {
+        uint8_t* lb = nullptr;
+        ALLOC(lb, np * label_bytes);
+        c->label = lb;
+        uint8_t* blb = nullptr;
+        ALLOC(blb, np * label_bytes);
+        c->b_label = blb;
+    }
+    ALLOC(c->frac, np);
+    ALLOC(c->b_frac, np);
+    double** f64[] = {&c->perm, &c->visc, &c->P, &c->conc, &c->acid, &c->fx, &c->fy, &c->fz,
+                      &c->sat, &c->pc, &c->kr, &c->precip, &c->b_precip, &c->b_sat, &c->b_P,
+                      &c->b_conc, &c->b_acid, &c->b_fx, &c->b_fy, &c->b_fz};
+    for (double** q : f64) ALLOC(*q, np);
+    ALLOC(c->pkind, n);
+    ALLOC(c->pdiag, n);
+    ALLOC(c->pb, n);
+    for (int d = 0; d < 3; ++d) ALLOC(c->pface[d], n);
+    ALLOC(c->pisd, n);
+    ALLOC(c->pr, n);
+    ALLOC(c->pdelta, n);
+    ALLOC(c->partials, (size_t)kMaxPartials * 8);
+    ALLOC(c->scal, (size_t)S_COUNT);
+    ALLOC(c->d_int, (size_t)64);
+#undef ALLOC
+    if (cudaMallocHost(&c->h_scal, sizeof(double) * S_COUNT) != cudaSuccess ||
+        cudaMallocHost(&c->h_int, sizeof(int) * 64) != cudaSuccess) {
+        ls_destroy(c);
+        return LS_CUDA_ERROR;
+    }
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        ls_destroy(c);
+        return LS_CUDA_ERROR;
+    }
+    *out = c;
+    return LS_OK;
+}
+
+ls_status ls_destroy(ls_ctx* c) {
+    if (!c) return LS_OK;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    void* ptrs[] = {c->label, c->b_label, c->frac, c->b_frac, c->perm, c->visc, c->P, c->conc,
+                    c->acid, c->fx, c->fy, c->fz, c->sat, c->pc, c->kr, c->precip,
+                    c->b_precip, c->b_sat, c->b_P, c->b_conc, c->b_acid, c->b_fx, c->b_fy,
+                    c->b_fz, c->pkind, c->pdiag, c->pb, c->pface[0], c->pface[1], c->pface[2],
+                    c->pisd, c->pr, c->pdelta, c->w32[0], c->w32[1], c->w32[2], c->w64[0],
+                    c->w64[1], c->w64[2], c->inner[0], c->inner[1], c->inner[2], c->inner[3],
+                    c->inner[4], c->comp, c->cc_flag, c->tdinv, c->s_old, c->dz_list,
+                    c->dz_count, c->dz_level_start, c->partials, c->scal, c->d_int};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    for (double* q : c->tv)
+        if (q) cudaFree(q);
+    for (auto& lv : c->mg) {
+        void* lp[] = {lv.comp, lv.diag, lv.face[0], lv.face[1], lv.face[2], lv.x, lv.b, lv.t};
+        for (void* q : lp)
+            if (q) cudaFree(q);
+    }
+    if (c->h_scal) cudaFreeHost(c->h_scal);
+    if (c->h_int) cudaFreeHost(c->h_int);
+    for (auto& r : c->regions) {
+        cudaEventDestroy(r.start);
+        cudaEventDestroy(r.stop);
+    }
+    for (auto e : c->event_pool) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return LS_OK;
+}
+
+const char* ls_last_error(const ls_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+ls_status ls_set_params(ls_ctx* c, const ls_params* p) {
+    if (!c || !p) return LS_BAD_ARG;
+    LS_TRY(validate_params(c, p));
+    c->p = *p;
+    c->p_ready = 0;
+    return LS_OK;
+}
+
+ls_status ls_get_params(const ls_ctx* c, ls_params* p) {
+    if (!c || !p) return LS_BAD_ARG;
+    *p = c->p;
+    return LS_OK;
+}
+
+void* ls_stream(ls_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+ls_status ls_synchronize(ls_ctx* c) {
+    if (!c) return LS_BAD_ARG;
+    LS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return LS_OK;
+}
+
+size_t ls_device_bytes(const ls_ctx* c) { return c ? c->device_bytes : 0; }
+
+static ls_status transfer(ls_ctx* c, ls_field f, void* host, size_t n, int padded, int up,
+                          cudaMemcpyKind kind) {
+    if (!c || !host) return LS_BAD_ARG;
+    size_t esz = 0;
+    void* dev = field_ptr(c, f, &esz);
+    if (!dev) return set_error(c, LS_BAD_ARG, "unknown field id");
+    size_t want = padded ? (size_t)c->g.NP : (size_t)c->g.N;
+    if (n != want) {
+        char buf[128];
+        snprintf(buf, sizeof(buf), "field transfer: %zu elements given, %zu expected", n, want);
+        return set_error(c, LS_BAD_ARG, buf);
+    }
+    if (up) {
+        LS_CUDA(c, cudaMemcpyAsync(dev, host, n * esz, kind, c->stream));
+        if (f == LS_F_LABEL || f == LS_F_PERMEABILITY || f == LS_F_VISCOSITY) c->p_ready = 0;
+    } else {
+        LS_CUDA(c, cudaMemcpyAsync(host, dev, n * esz, kind, c->stream));
+    }
+    LS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return LS_OK;
+}
+
+ls_status ls_upload_field(ls_ctx* c, ls_field f, const void* host, size_t n, int padded) {
+    return transfer(c, f, const_cast<void*>(host), n, padded, 1, cudaMemcpyHostToDevice);
+}
+ls_status ls_download_field(ls_ctx* c, ls_field f, void* host, size_t n, int padded) {
+    return transfer(c, f, host, n, padded, 0, cudaMemcpyDeviceToHost);
+}
+ls_status ls_upload_field_device(ls_ctx* c, ls_field f, const void* dev, size_t n, int padded) {
+    return transfer(c, f, const_cast<void*>(dev), n, padded, 1, cudaMemcpyDeviceToDevice);
+}
+ls_status ls_download_field_device(ls_ctx* c, ls_field f, void* dev, size_t n, int padded) {
+    return transfer(c, f, dev, n, padded, 0, cudaMemcpyDeviceToDevice);
+}
+
+// Simulation::initFields, src/Simulation.cpp:165-180.
+ls_status ls_init_fields(ls_ctx* c) {
+    if (!c) return LS_BAD_ARG;
+    size_t bytes = sizeof(double) * (size_t)c->g.NP;
+    double* f[] = {c->P, c->conc, c->fx, c->fy, c->fz, c->sat, c->pc, c->kr, c->precip};
+    for (double* q : f) LS_CUDA(c, cudaMemsetAsync(q, 0, bytes, c->stream));
+    c->p_ready = 0;
+    return LS_OK;
+}
+
+ls_status ls_init_frac(ls_ctx* c, unsigned long long* count) {
+    if (!c) return LS_BAD_ARG;
+    return init_frac_run(c, count);
+}
+
+ls_status ls_init_saturation(ls_ctx* c) {
+    if (!c) return LS_BAD_ARG;
+    return init_saturation_run(c);
+}
+
+// Simulation::initAcid, src/Simulation.cpp:285-310.
+ls_status ls_init_acid(ls_ctx* c) {
+    if (!c) return LS_BAD_ARG;
+    LS_CUDA(c, cudaMemsetAsync(c->acid, 0, sizeof(double) * (size_t)c->g.N, c->stream));
+    return LS_OK;
+}
+
+ls_status ls_props(ls_ctx* c) {
+    if (!c) return LS_BAD_ARG;
+    Timed tm(c, LS_T_PROPS);
+    return props_run(c);
+}
+
+ls_status ls_pressure_setup(ls_ctx* c, double t) {
+    if (!c) return LS_BAD_ARG;
+    Timed tm(c, LS_T_PRESS_SETUP);
+    return pressure_setup_run(c, t);
+}
+
+ls_status ls_pressure_step(ls_ctx* c, double t, ls_solve_info* info) {
+    if (!c) return LS_BAD_ARG;
+    {
+        Timed tm(c, LS_T_PRESS_SETUP);
+        LS_TRY(pressure_setup_run(c, t));
+    }
+    return pressure_solve_run(c, info);
+}
+
+ls_status ls_pressure_apply(ls_ctx* c, const double* x, double* y) {
+    if (!c || !x || !y) return LS_BAD_ARG;
+    if (!c->p_ready) return set_error(c, LS_BAD_ARG, "ls_pressure_setup must run first");
+    return pressure_apply_run(c, x, y);
+}
+
+ls_status ls_pressure_rhs(ls_ctx* c, double* b) {
+    if (!c || !b) return LS_BAD_ARG;
+    if (!c->p_ready) return set_error(c, LS_BAD_ARG, "ls_pressure_setup must run first");
+    LS_CUDA(c, cudaMemcpyAsync(b, c->pb, sizeof(double) * (size_t)c->g.N, cudaMemcpyDeviceToHost,
+                               c->stream));
+    LS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return LS_OK;
+}
+
+ls_status ls_flux(ls_ctx* c) {
+    if (!c) return LS_BAD_ARG;
+    Timed tm(c, LS_T_FLUX);
+    return flux_run(c);
+}
+
+ls_status ls_saturation(ls_ctx* c, double dt, ls_substep_info* info) {
+    if (!c || !(dt > 0.0)) return c ? set_error(c, LS_BAD_ARG, "dt must be > 0") : LS_BAD_ARG;
+    Timed tm(c, LS_T_SATURATION);
+    return saturation_run(c, dt, info);
+}
+
+ls_status ls_saturation_implicit(ls_ctx* c, double dt, ls_solve_info* info) {
+    if (!c || !(dt > 0.0)) return c ? set_error(c, LS_BAD_ARG, "dt must be > 0") : LS_BAD_ARG;
+    Timed tm(c, LS_T_SATURATION);
+    return saturation_implicit_run(c, dt, info);
+}
+
+ls_status ls_surface(ls_ctx* c) {
+    if (!c) return LS_BAD_ARG;
+    Timed tm(c, LS_T_PRECIP);
+    return surface_run(c);
+}
+
+ls_status ls_transport(ls_ctx* c, double dt, int which, ls_solve_info* ci, ls_solve_info* ai) {
+    if (!c || !(dt > 0.0)) return c ? set_error(c, LS_BAD_ARG, "dt must be > 0") : LS_BAD_ARG;
+    if (which < 1 || which > 3) return set_error(c, LS_BAD_ARG, "which must be 1, 2 or 3");
+    Timed tm(c, LS_T_TRANSPORT);
+    return transport_run(c, dt, which, ci, ai);
+}
+
+ls_status ls_transport_apply(ls_ctx* c, double dt, const double* x, double* y) {
+    if (!c || !x || !y || !(dt > 0.0)) return LS_BAD_ARG;
+    return transport_apply_run(c, dt, x, y);
+}
+
+ls_status ls_precip(ls_ctx* c) {
+    if (!c) return LS_BAD_ARG;
+    Timed tm(c, LS_T_PRECIP);
+    return precip_run(c);
+}
+
+ls_status ls_dissolve(ls_ctx* c, double dt, int* leached, ls_substep_info* info) {
+    if (!c || !(dt > 0.0)) return c ? set_error(c, LS_BAD_ARG, "dt must be > 0") : LS_BAD_ARG;
+    Timed tm(c, LS_T_DISSOLVE);
+    return dissolve_run(c, dt, leached, info);
+}
+
+// Simulation::saveState, src/Simulation.cpp:2312-2328.
+ls_status ls_snapshot(ls_ctx* c) {
+    if (!c) return LS_BAD_ARG;
+    Timed tm(c, LS_T_SNAPSHOT);
+    size_t np = (size_t)c->g.NP, d8 = np * sizeof(double);
+    cudaStream_t s = c->stream;
+    LS_CUDA(c, cudaMemcpyAsync(c->b_label, c->label, np * c->label_bytes, cudaMemcpyDeviceToDevice, s));
+    LS_CUDA(c, cudaMemcpyAsync(c->b_frac, c->frac, np * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    const std::pair<double*, double*> pairs[] = {
+        {c->b_precip, c->precip}, {c->b_sat, c->sat}, {c->b_P, c->P}, {c->b_conc, c->conc},
+        {c->b_acid, c->acid}, {c->b_fx, c->fx}, {c->b_fy, c->fy}, {c->b_fz, c->fz}};
+    for (auto& pr : pairs) LS_CUDA(c, cudaMemcpyAsync(pr.first, pr.second, d8, cudaMemcpyDeviceToDevice, s));
+    return LS_OK;
+}
+
+// Simulation::restoreState, src/Simulation.cpp:2330-2353 (copy back, rebuild properties).
+ls_status ls_rollback(ls_ctx* c) {
+    if (!c) return LS_BAD_ARG;
+    {
+        Timed tm(c, LS_T_SNAPSHOT);
+        size_t np = (size_t)c->g.NP, d8 = np * sizeof(double);
+        cudaStream_t s = c->stream;
+        LS_CUDA(c, cudaMemcpyAsync(c->label, c->b_label, np * c->label_bytes, cudaMemcpyDeviceToDevice, s));
+        LS_CUDA(c, cudaMemcpyAsync(c->frac, c->b_frac, np * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        const std::pair<double*, double*> pairs[] = {
+            {c->precip, c->b_precip}, {c->sat, c->b_sat}, {c->P, c->b_P}, {c->conc, c->b_conc},
+            {c->acid, c->b_acid}, {c->fx, c->b_fx}, {c->fy, c->b_fy}, {c->fz, c->b_fz}};
+        for (auto& pr : pairs) LS_CUDA(c, cudaMemcpyAsync(pr.first, pr.second, d8, cudaMemcpyDeviceToDevice, s));
+    }
+    c->p_ready = 0;
+    return ls_props(c);
+}
+
+static bool solve_failed(ls_status st) { return st == LS_NOT_CONVERGED || st == LS_NONFINITE; }
+
+// One attempt of src/main.cpp:303-432.
+ls_status ls_step(ls_ctx* c, double t, double dt, ls_step_info* info) {
+    if (!c || !(dt > 0.0)) return c ? set_error(c, LS_BAD_ARG, "dt must be > 0") : LS_BAD_ARG;
+    ls_step_info loc;
+    memset(&loc, 0, sizeof(loc));
+    LS_TRY(ls_snapshot(c));
+    bool ok = true;
+    ls_status st = LS_OK;
+    const int max_picard = c->p.use_implicit_saturation ? 3 : 1;
+    bool physics_valid = true;
+    for (int picard = 0; picard < max_picard; ++picard) {
+        loc.picard_iterations = picard + 1;
+        LS_TRY(ls_props(c));
+        st = ls_pressure_step(c, t, &loc.pressure);
+        if (solve_failed(st)) { ok = false; break; }
+        if (st != LS_OK && st != LS_STAGNATED_FALLBACK_USED) return st;
+        LS_TRY(ls_flux(c));
+        if (c->p.use_implicit_saturation) {
+            st = ls_saturation_implicit(c, dt, &loc.saturation_solve);
+            if (solve_failed(st)) { ok = false; break; }
+            if (st == LS_UNPHYSICAL) physics_valid = false;
+            else { physics_valid = true; if (st != LS_OK) return st; }
+        } else {
+            LS_TRY(ls_saturation(c, dt, &loc.saturation));
+        }
+    }
+    if (ok && c->p.use_implicit_saturation && !physics_valid) ok = false;
+    if (ok) {
+        LS_TRY(ls_surface(c));
+        st = ls_transport(c, dt, 3, &loc.conc, &loc.acid);
+        if (solve_failed(st)) ok = false;
+        else if (st != LS_OK) return st;
+    }
+    if (ok) {
+        LS_TRY(ls_precip(c));
+        LS_TRY(ls_dissolve(c, dt, &loc.leached, &loc.leaching));
+    }
+    loc.success = ok ? 1 : 0;
+    if (info) *info = loc;
+    return LS_OK;
+}
+
+ls_status ls_timing_enable(ls_ctx* c, int enable) {
+    if (!c) return LS_BAD_ARG;
+    if (!enable) resolve_regions(c);
+    c->timing = enable ? 1 : 0;
+    return LS_OK;
+}
+
+ls_status ls_timing_reset(ls_ctx* c) {
+    if (!c) return LS_BAD_ARG;
+    resolve_regions(c);
+    for (int q = 0; q < LS_T_COUNT; ++q) {
+        c->timer_ms[q] = 0.0;
+        c->timer_count[q] = 0;
+        c->timer_bytes[q] = 0.0;
+    }
+    c->launches = 0;
+    return LS_OK;
+}
+
+ls_status ls_timing_get(ls_ctx* c, ls_timer t, double* total_ms, long long* count) {
+    if (!c || t < 0 || t >= LS_T_COUNT) return LS_BAD_ARG;
+    resolve_regions(c);
+    if (total_ms) *total_ms = c->timer_ms[t];
+    if (count) *count = c->timer_count[t];
+    return LS_OK;
+}
+
+ls_status ls_timing_bytes(ls_ctx* c, ls_timer t, double* bytes) {
+    if (!c || t < 0 || t >= LS_T_COUNT || !bytes) return LS_BAD_ARG;
+    *bytes = c->timer_bytes[t];
+    return LS_OK;
+}
+
+long long ls_kernel_launches(const ls_ctx* c) { return c ? c->launches : 0; }
+
+}  // extern "C"

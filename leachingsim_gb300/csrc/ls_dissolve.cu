@@ -1,0 +1,253 @@
+// ls_dissolve.cu - sulphide dissolution of Simulation::updateFrac (src/Simulation.cpp:315-617).
+//
+// The reference sweeps the grid sequentially (k outer, j, i inner) num_steps times; each
+// active mineral voxel (label >= Sulphide, frac > 0) reads the acid and label of its six
+// neighbours, consumes acid from them in place and may turn into Pore. Two active voxels
+// interact only when their Manhattan distance is at most 2. Ordering the voxels by the
+// wavefront index w = i + 2j + 3k respects every such dependence of the sequential sweep
+// (w strictly increases along each of them), and two voxels with equal w are never within
+// distance 2, so processing the levels w = 0, 1, 2, ... in order, each level in parallel,
+// reproduces the sequential result exactly.
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "ls_internal.cuh"
+
+namespace ls {
+
+struct DzConst {
+    double D, dx, kreac, time_scalar, c_sat, dt_sub;
+};
+
+template <typename L>
+__device__ __forceinline__ double dz_surface_flux(const Grid& g, const DzConst& dc,
+                                                  const L* __restrict__ label,
+                                                  const double* __restrict__ acid, bool valid,
+                                                  long long nb) {
+    // calc_surface_flux, src/Simulation.cpp:520-542
+    if (valid) {
+        int n_type = (int)label[nb];
+        if (n_type == kPore || n_type == kRock) {
+            double k_trans = dc.D / dc.dx;
+            double k_eff = 1.0 / ((1.0 / k_trans) + (1.0 / dc.kreac));
+            return k_eff * acid[nb];
+        }
+    }
+    return 0.0;
+}
+
+// Rate pass (src/Simulation.cpp:320-420) plus counters deciding whether the sweeps can
+// change anything: d_int[0] active voxels, [1] active voxels with non-zero flux sum,
+// [2] active voxels already at or below the leaching threshold.
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_dz_rate(Grid g, DzConst dc, const L* __restrict__ label,
+                                                    const double* __restrict__ acid,
+                                                    const float* __restrict__ frac,
+                                                    int* __restrict__ counters,
+                                                    double* __restrict__ partials) {
+    double mx[1] = {0.0};
+    int n_active = 0, n_flux = 0, n_flip = 0;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        const int t = (int)label[r];
+        if (t < kSulphide) continue;
+        int i, j, k;
+        decode(g, r, i, j, k);
+        const long long nbs[6] = {r + g.JK, r - g.JK, r + g.K, r - g.K, r + 1, r - 1};
+        const bool val[6] = {i + 1 < g.I, i > 0, j + 1 < g.J, j > 0, k + 1 < g.K, k > 0};
+        double flux_sum = 0.0;
+#pragma unroll
+        for (int d = 0; d < 6; ++d) flux_sum += dz_surface_flux(g, dc, label, acid, val[d], nbs[d]);
+        if (t == kSulphide) {
+            double area_per_face = dc.dx * dc.dx;
+            double voxel_volume = dc.dx * dc.dx * dc.dx;
+            double vol_rate = flux_sum * area_per_face;
+            double fractional_rate = vol_rate / voxel_volume;
+            if (fractional_rate > mx[0]) mx[0] = fractional_rate;
+        }
+        if (frac[r] > 0.0f) {
+            n_active++;
+            if (flux_sum != 0.0) n_flux++;
+            if ((double)frac[r] <= 1e-4) n_flip++;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        n_active += __shfl_down_sync(0xffffffffu, n_active, o);
+        n_flux += __shfl_down_sync(0xffffffffu, n_flux, o);
+        n_flip += __shfl_down_sync(0xffffffffu, n_flip, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (n_active) atomicAdd(&counters[0], n_active);
+        if (n_flux) atomicAdd(&counters[1], n_flux);
+        if (n_flip) atomicAdd(&counters[2], n_flip);
+    }
+    block_max_store<1>(mx, partials);
+}
+
+__device__ __forceinline__ int dz_level(int i, int j, int k) { return i + 2 * j + 3 * k; }
+
+template <typename L>
+__global__ void k_dz_hist(Grid g, const L* __restrict__ label, const float* __restrict__ frac,
+                          int* __restrict__ hist) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        if ((int)label[r] >= kSulphide && frac[r] > 0.0f) {
+            int i, j, k;
+            decode(g, r, i, j, k);
+            atomicAdd(&hist[dz_level(i, j, k)], 1);
+        }
+    }
+}
+
+template <typename L>
+__global__ void k_dz_scatter(Grid g, const L* __restrict__ label, const float* __restrict__ frac,
+                             const int* __restrict__ start, int* __restrict__ cursor,
+                             int* __restrict__ list) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        if ((int)label[r] >= kSulphide && frac[r] > 0.0f) {
+            int i, j, k;
+            decode(g, r, i, j, k);
+            int w = dz_level(i, j, k);
+            int pos = atomicAdd(&cursor[w], 1);
+            list[start[w] + pos] = (int)r;
+        }
+    }
+}
+
+// One wavefront level of one sub-step (the body of src/Simulation.cpp:475-603).
+template <typename L>
+__global__ void k_dz_level(Grid g, DzConst dc, const int* __restrict__ list, int count,
+                           L* __restrict__ label, float* __restrict__ frac,
+                           double* __restrict__ acid, double* __restrict__ precip,
+                           double* __restrict__ conc, int* __restrict__ leached) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const long long r = list[t];
+    if (!((int)label[r] >= kSulphide && frac[r] > 0.0f)) return;
+    int i, j, k;
+    decode(g, r, i, j, k);
+    const long long nbs[6] = {r + g.JK, r - g.JK, r + g.K, r - g.K, r + 1, r - 1};
+    const bool val[6] = {i + 1 < g.I, i > 0, j + 1 < g.J, j > 0, k + 1 < g.K, k > 0};
+    double f[6];
+#pragma unroll
+    for (int d = 0; d < 6; ++d) f[d] = dz_surface_flux(g, dc, label, acid, val[d], nbs[d]);
+    double flux_sum = f[0] + f[1] + f[2] + f[3] + f[4] + f[5];
+    double area_per_face = dc.dx * dc.dx;
+    double voxel_volume = dc.dx * dc.dx * dc.dx;
+    double mass_loss = flux_sum * area_per_face * dc.dt_sub;
+    double fractional_loss = mass_loss / voxel_volume;
+    float fr = (float)((double)frac[r] - (fractional_loss * dc.time_scalar));
+    frac[r] = fr;
+    if (flux_sum > 0.0) {
+#pragma unroll
+        for (int d = 0; d < 6; ++d)
+            if (val[d]) acid[nbs[d]] -= fractional_loss * (f[d] / flux_sum);
+    }
+    if ((double)fr <= 1e-4) {
+        frac[r] = 0.0f;
+        if ((int)label[r] == kSulphide) {
+            label[r] = (L)kPore;
+            precip[r] = 0.0;
+            conc[r] = dc.c_sat;
+            atomicAdd(leached, 1);
+        }
+    }
+}
+
+template <typename L>
+static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_info* info) {
+    const Grid g = c->g;
+    const int grid = grid_for(c, g.N);
+    DzConst dc;
+    dc.D = c->p.D;
+    dc.dx = c->p.dx;
+    dc.kreac = c->p.kreac;
+    dc.time_scalar = c->p.time_scalar;
+    dc.c_sat = c->p.c_sat;
+    dc.dt_sub = dt;
+    const L* label = (const L*)c->label;
+    LS_CUDA(c, cudaMemsetAsync(c->d_int, 0, sizeof(int) * 4, c->stream));
+    LS_LAUNCH(c, k_dz_rate<L>, grid, kBlock, 0, g, dc, label, (const double*)c->acid,
+              (const float*)c->frac, c->d_int, c->partials);
+    LS_TRY(finalize_max(c, grid, 1, S_RED0));
+    double global_max_rate = 0.0;
+    LS_TRY(read_scalars(c, S_RED0, 1, &global_max_rate));
+    LS_CUDA(c, cudaMemcpyAsync(c->h_int, c->d_int, sizeof(int) * 4, cudaMemcpyDeviceToHost, c->stream));
+    LS_CUDA(c, cudaStreamSynchronize(c->stream));
+    const int n_active = c->h_int[0], n_flux = c->h_int[1], n_flip = c->h_int[2];
+    // sub-step count, src/Simulation.cpp:423-452
+    double effective_fractional_rate = global_max_rate * c->p.time_scalar;
+    double dt_safe = dt;
+    if (effective_fractional_rate > 1e-20) dt_safe = 0.1 / effective_fractional_rate;
+    double calculated_steps = std::ceil(dt / dt_safe);
+    int num_steps = 1;
+    if (calculated_steps > 1000) num_steps = 1000;
+    else if (calculated_steps > 1.0) num_steps = (int)calculated_steps;
+    double dt_sub = dt / num_steps;
+    dc.dt_sub = dt_sub;
+    if (info) {
+        info->max_rate = global_max_rate;
+        info->num_steps = num_steps;
+        info->dt_sub = dt_sub;
+    }
+    if (leached_out) *leached_out = 0;
+    // With no acid reaching any active voxel and none at the threshold, every sweep leaves
+    // every field unchanged (frac -= 0, nothing consumed, nothing flips).
+    if (n_active == 0 || (n_flux == 0 && n_flip == 0)) return LS_OK;
+
+    // active list sorted by wavefront level
+    const int nlev = (g.I - 1) + 2 * (g.J - 1) + 3 * (g.K - 1) + 1;
+    if (c->dz_cap < n_active || !c->dz_list) {
+        if (c->dz_list) { cudaFree(c->dz_list); c->device_bytes -= sizeof(int) * (size_t)c->dz_cap; }
+        c->dz_list = nullptr;
+        LS_TRY(dalloc_t(c, &c->dz_list, (size_t)n_active));
+        c->dz_cap = n_active;
+    }
+    if (!c->dz_level_start) {
+        LS_TRY(dalloc_t(c, &c->dz_level_start, (size_t)nlev + 1));
+        LS_TRY(dalloc_t(c, &c->dz_count, (size_t)nlev + 1));
+    }
+    LS_CUDA(c, cudaMemsetAsync(c->dz_count, 0, sizeof(int) * (nlev + 1), c->stream));
+    LS_LAUNCH(c, k_dz_hist<L>, grid, kBlock, 0, g, label, (const float*)c->frac, c->dz_count);
+    std::vector<int> hist(nlev + 1), start(nlev + 1);
+    LS_CUDA(c, cudaMemcpyAsync(hist.data(), c->dz_count, sizeof(int) * (nlev + 1),
+                               cudaMemcpyDeviceToHost, c->stream));
+    LS_CUDA(c, cudaStreamSynchronize(c->stream));
+    int acc = 0;
+    for (int w = 0; w <= nlev; ++w) {
+        start[w] = acc;
+        acc += hist[w];
+    }
+    if (acc != n_active) return set_error(c, LS_CUDA_ERROR, "dissolution: active list count mismatch");
+    LS_CUDA(c, cudaMemcpyAsync(c->dz_level_start, start.data(), sizeof(int) * (nlev + 1),
+                               cudaMemcpyHostToDevice, c->stream));
+    LS_CUDA(c, cudaMemsetAsync(c->dz_count, 0, sizeof(int) * (nlev + 1), c->stream));
+    LS_LAUNCH(c, k_dz_scatter<L>, grid, kBlock, 0, g, label, (const float*)c->frac,
+              (const int*)c->dz_level_start, c->dz_count, c->dz_list);
+    int* d_leached = c->d_int + 8;
+    LS_CUDA(c, cudaMemsetAsync(d_leached, 0, sizeof(int), c->stream));
+    for (int step = 0; step < num_steps; ++step) {
+        for (int w = 0; w < nlev; ++w) {
+            int n = hist[w];
+            if (n == 0) continue;
+            int blocks = (n + 127) / 128;
+            LS_LAUNCH(c, k_dz_level<L>, blocks, 128, 0, g, dc, (const int*)c->dz_list + start[w], n,
+                      (L*)c->label, c->frac, c->acid, c->precip, c->conc, d_leached);
+        }
+    }
+    int h = 0;
+    LS_CUDA(c, cudaMemcpyAsync(&h, d_leached, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    LS_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (leached_out) *leached_out = h;
+    c->p_ready = 0;
+    return LS_OK;
+}
+
+ls_status dissolve_run(ls_ctx* c, double dt, int* leached, ls_substep_info* info) {
+    if (c->label_bytes == 1) return dissolve_t<uint8_t>(c, dt, leached, info);
+    return dissolve_t<uint16_t>(c, dt, leached, info);
+}
+
+}  // namespace ls

@@ -1,0 +1,266 @@
+// ls_internal.cuh - shared definitions of the GB300 LeachingSim hot path.
+//
+// Device layout: every field has NP = (I+1)*J*K slots, voxel (i,j,k) in slot
+// k + K*(j + J*i) (the reference's padded single-rank array, src/MPIDomain.h:75-97).
+// Linear systems have N = I*J*K rows numbered the same way; with compat_shift the
+// solution of row r is stored in slot r + J*K of its field, as on the reference's
+// rank 0 (src/Simulation.cpp:808,1247,1975,2173).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/leachingsim.h"
+
+namespace ls {
+
+constexpr int kAir = 1, kPore = 2, kRock = 3, kSulphide = 4, kPrecipitate = 5;
+
+// std::min / std::max semantics (NaN handling included): min(a,b) = (b<a)?b:a.
+__host__ __device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
+__host__ __device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
+
+constexpr int kBlock = 256;        // threads per block of the streaming kernels
+constexpr int kMaxPartials = 4096; // per-block partial results of one reduction
+
+struct Grid {
+    int I, J, K;
+    long long JK, N, NP;
+};
+
+__host__ __device__ __forceinline__ void decode(const Grid& g, long long r, int& i, int& j, int& k) {
+    i = (int)(r / g.JK);
+    long long rem = r - (long long)i * g.JK;
+    j = (int)(rem / g.K);
+    k = (int)(rem - (long long)j * g.K);
+}
+
+// Timed region record.
+struct TimedRegion {
+    int timer;
+    cudaEvent_t start, stop;
+};
+
+// Device-side scalar slots (doubles) used by the solvers.
+enum Scalar {
+    S_RED0 = 0,       // generic reduction outputs S_RED0..S_RED0+15
+    S_COUNT = 64
+};
+
+}  // namespace ls
+
+struct ls_ctx {
+    ls::Grid g;
+    int label_bytes;
+    ls_params p;
+    int device;
+    int num_sms;
+    cudaStream_t stream;
+    std::string err;
+
+    // fields, NP slots each
+    void* label;
+    float* frac;
+    double *perm, *visc, *P, *conc, *acid, *fx, *fy, *fz, *sat, *pc, *kr, *precip;
+    // snapshot (src/Simulation.cpp:2312-2328)
+    void* b_label;
+    float* b_frac;
+    double *b_precip, *b_sat, *b_P, *b_conc, *b_acid, *b_fx, *b_fy, *b_fz;
+
+    // pressure system (N rows)
+    int8_t* pkind;      // 0 empty row, 1 identity row, 2 Pore row, 3 Pore row with floored diagonal
+    double* pdiag;      // diagonal of the assembled row
+    double* pb;         // right-hand side (identity rows: the fixed value)
+    double* pface[3];   // link coefficient of the +i, +j, +k face (used by Pore rows)
+    double* pisd;       // 1/sqrt(d) of inner unknowns (normal Pore rows), else 0
+    double* pr;         // FP64 outer residual
+    double* pdelta;     // FP64 correction
+    float* w32[3];      // Jacobi-scaled inner face weights (FP32)
+    double* w64[3];     // Jacobi-scaled inner face weights (FP64)
+    void* inner[5];     // inner PCG vectors x r z p q (FP32 or FP64)
+    int inner_is64;
+    double pscale_den;  // ||D^-1 b|| of the current pressure system
+    double p_t;         // time the pressure system was assembled for
+    int p_ready;
+
+    // multigrid hierarchy (allocated on demand)
+    struct MGLevel {
+        ls::Grid g;
+        int* comp;          // component / unknown id per cell (-1 = not an unknown)
+        void* diag;         // T
+        void* face[3];      // T, + faces
+        void* x;            // T
+        void* b;            // T
+        void* t;            // T
+    };
+    std::vector<MGLevel> mg;
+    int mg_is64;
+    int* comp;            // fine-level strong-component ids (-1 = not an inner unknown)
+    int* cc_flag;         // device flag for the labelling loop
+
+    // transport / implicit saturation Krylov vectors (2 right-hand sides)
+    double* tv[14];
+    double* tdinv;        // inverse diagonal of the transport rows
+    double* s_old;        // saturation before the implicit solve
+
+    // dissolution
+    int* dz_list;         // active mineral voxels sorted by wavefront
+    int* dz_count;
+    int* dz_level_start;
+    int dz_cap;
+
+    // reductions
+    double* partials;     // kMaxPartials * 8 doubles
+    double* scal;         // device scalars
+    double* h_scal;       // pinned host mirror
+    int* d_int;           // device ints (counters, flags)
+    int* h_int;           // pinned host mirror
+
+    // accounting
+    long long launches;
+    int timing;
+    std::vector<ls::TimedRegion> regions;
+    std::vector<cudaEvent_t> event_pool;
+    double timer_ms[LS_T_COUNT];
+    long long timer_count[LS_T_COUNT];
+    double timer_bytes[LS_T_COUNT];
+    unsigned long long initial_sulphide_count;
+    size_t device_bytes;
+};
+
+namespace ls {
+
+// error helpers ------------------------------------------------------------
+ls_status set_error(ls_ctx* c, ls_status st, const std::string& msg);
+ls_status check_cuda(ls_ctx* c, cudaError_t e, const char* what);
+#define LS_CUDA(ctx, call)                                                          \
+    do {                                                                            \
+        cudaError_t e__ = (call);                                                   \
+        if (e__ != cudaSuccess) return ls::check_cuda((ctx), e__, #call);           \
+    } while (0)
+#define LS_TRY(expr)                                                                \
+    do {                                                                            \
+        ls_status s__ = (expr);                                                     \
+        if (s__ != LS_OK) return s__;                                               \
+    } while (0)
+// kernel launch + accounting + launch-error check
+#define LS_LAUNCH(ctx, kernel, grid, block, smem, ...)                              \
+    do {                                                                            \
+        kernel<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);            \
+        (ctx)->launches++;                                                          \
+        cudaError_t e__ = cudaGetLastError();                                       \
+        if (e__ != cudaSuccess) return ls::check_cuda((ctx), e__, #kernel);         \
+    } while (0)
+
+inline int grid_for(const ls_ctx* c, long long n) {
+    long long want = (n + kBlock - 1) / kBlock;
+    long long cap = (long long)c->num_sms * 8;
+    if (want > cap) want = cap;
+    if (want < 1) want = 1;
+    return (int)want;
+}
+
+// timing
+void region_begin(ls_ctx* c, int timer, cudaEvent_t* start);
+void region_end(ls_ctx* c, int timer, cudaEvent_t start);
+struct Timed {
+    ls_ctx* c;
+    int t;
+    cudaEvent_t s;
+    Timed(ls_ctx* ctx, int timer) : c(ctx), t(timer), s(nullptr) { region_begin(c, t, &s); }
+    ~Timed() { region_end(c, t, s); }
+};
+
+// reductions: per-block partials -> device scalar (deterministic order)
+ls_status finalize_sum(ls_ctx* c, int nblocks, int nvals, int out_slot);
+ls_status finalize_max(ls_ctx* c, int nblocks, int nvals, int out_slot);
+ls_status read_scalars(ls_ctx* c, int first, int count, double* out);
+
+// device block reduction of nvals doubles per thread into partials[blockIdx.x*nvals + v]
+template <int NV>
+__device__ __forceinline__ void block_sum_store(double (&v)[NV], double* partials) {
+    __shared__ double sh[NV][kBlock / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        double x = v[q];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sh[q][warp] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double s = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sh[q][w];
+            partials[(size_t)blockIdx.x * NV + q] = s;
+        }
+    }
+}
+
+template <int NV>
+__device__ __forceinline__ void block_max_store(double (&v)[NV], double* partials) {
+    __shared__ double sh[NV][kBlock / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        double x = v[q];
+        for (int o = 16; o > 0; o >>= 1) x = smax(x, __shfl_down_sync(0xffffffffu, x, o));
+        if (lane == 0) sh[q][warp] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double s = sh[q][0];
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w) s = smax(s, sh[q][w]);
+            partials[(size_t)blockIdx.x * NV + q] = s;
+        }
+    }
+}
+
+// one block; thread v reduces value v over the blocks in a fixed order
+template <bool MAX>
+__global__ void k_finalize(const double* __restrict__ partials, int nblocks, int nvals,
+                           double* __restrict__ out) {
+    for (int v = threadIdx.x; v < nvals; v += blockDim.x) {
+        double acc = MAX ? partials[v] : 0.0;
+        for (int b = MAX ? 1 : 0; b < nblocks; ++b) {
+            double x = partials[(size_t)b * nvals + v];
+            acc = MAX ? smax(acc, x) : acc + x;
+        }
+        out[v] = acc;
+    }
+}
+
+// label access
+template <typename L>
+__device__ __forceinline__ int lab(const L* a, long long r) { return (int)a[r]; }
+
+// component-wise entry points implemented in the .cu files
+ls_status props_run(ls_ctx* c);
+ls_status flux_run(ls_ctx* c);
+ls_status saturation_run(ls_ctx* c, double dt, ls_substep_info* info);
+ls_status saturation_implicit_run(ls_ctx* c, double dt, ls_solve_info* info);
+ls_status surface_run(ls_ctx* c);
+ls_status precip_run(ls_ctx* c);
+ls_status pressure_setup_run(ls_ctx* c, double t);
+ls_status pressure_solve_run(ls_ctx* c, ls_solve_info* info);
+ls_status pressure_apply_run(ls_ctx* c, const double* x, double* y);
+ls_status transport_run(ls_ctx* c, double dt, int which, ls_solve_info* ci, ls_solve_info* ai);
+ls_status transport_apply_run(ls_ctx* c, double dt, const double* x, double* y);
+ls_status dissolve_run(ls_ctx* c, double dt, int* leached, ls_substep_info* info);
+ls_status init_frac_run(ls_ctx* c, unsigned long long* count);
+ls_status init_saturation_run(ls_ctx* c);
+
+// allocation helper tracking device bytes
+ls_status dalloc(ls_ctx* c, void** p, size_t bytes);
+template <typename T>
+ls_status dalloc_t(ls_ctx* c, T** p, size_t n) {
+    return dalloc(c, reinterpret_cast<void**>(p), n * sizeof(T));
+}
+
+}  // namespace ls

@@ -1,0 +1,352 @@
+// ls_pointwise.cu - per-voxel and nearest-neighbour kernels of the time step:
+//   props  = updateRelativePermeability + updateCapillaryPressure + initProperties,
+//            fused (src/Simulation.cpp:1634-1664, 1596-1628, 187-248)
+//   flux   = calculateFlux (src/Simulation.cpp:866-953)
+//   saturation = updateSaturation (src/Simulation.cpp:1672-1856)
+//   surface = handleSurfaceEffects (src/Simulation.cpp:2063-2103)
+//   precip  = handlePrecipitation (src/Simulation.cpp:2114-2165)
+// Arithmetic follows the reference expression by expression; the library is built
+// without FMA contraction so each product rounds on its own, as on the reference's host.
+#include <cmath>
+
+#include "ls_internal.cuh"
+
+namespace ls {
+
+struct PropsConst {
+    double m, s_res, vg_n, vg_alpha;
+    double log_k_rock, log_k_pore;
+};
+
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_props(Grid g, PropsConst pc, const L* __restrict__ label,
+                                                  const double* __restrict__ sat,
+                                                  const double* __restrict__ precip,
+                                                  const float* __restrict__ frac,
+                                                  double* __restrict__ kr, double* __restrict__ cap,
+                                                  double* __restrict__ perm, double* __restrict__ visc) {
+    const double pore_permeability = 1.0e-12;
+    const double rock_permeability = 1.0e-18;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        const int t = (int)label[r];
+        const double s = sat[r];
+        double krv = 0.0, pcv = 0.0;
+        if (t == kPore || t == kSulphide) {
+            // relative permeability, src/Simulation.cpp:1643-1657
+            double Se = (s - pc.s_res) / (1.0 - pc.s_res);
+            double Sk = smax(0.0, smin(1.0, Se));
+            if (Sk <= 0.0) {
+                krv = 0.0;
+            } else {
+                double term1 = 1.0 - pow(1.0 - pow(Sk, 1.0 / pc.m), pc.m);
+                krv = sqrt(Sk) * term1 * term1;
+            }
+            // capillary pressure, src/Simulation.cpp:1605-1621
+            double Sc = smax(1e-6, smin(1.0, Se));
+            if (Sc >= 1.0) {
+                pcv = 0.0;
+            } else {
+                double Se_inv_m = pow(Sc, -1.0 / pc.m);
+                pcv = (1.0 / pc.vg_alpha) * pow(Se_inv_m - 1.0, 1.0 / pc.vg_n);
+            }
+        }
+        kr[r] = krv;
+        cap[r] = pcv;
+        // intrinsic permeability and viscosity, src/Simulation.cpp:199-244
+        double K_intrinsic = rock_permeability;
+        if (t == kAir) {
+            K_intrinsic = pore_permeability;
+        } else if (t == kPore) {
+            double p_frac = smax(0.0, smin(1.0, precip[r]));
+            double log_k_eff = (p_frac * pc.log_k_rock) + ((1.0 - p_frac) * pc.log_k_pore);
+            K_intrinsic = pow(10.0, log_k_eff);
+        } else if (t == kSulphide) {
+            double f = (double)frac[r];
+            double log_k_eff = (f * pc.log_k_rock) + ((1.0 - f) * pc.log_k_pore);
+            K_intrinsic = pow(10.0, log_k_eff);
+        }
+        visc[r] = (t == kAir) ? 1.8e-5 : 1.0e-3;
+        perm[r] = K_intrinsic * smax(krv, 1e-15);
+    }
+}
+
+ls_status props_run(ls_ctx* c) {
+    PropsConst pc;
+    pc.m = 1.0 - (1.0 / c->p.vg_n);
+    pc.s_res = c->p.s_res;
+    pc.vg_n = c->p.vg_n;
+    pc.vg_alpha = c->p.vg_alpha;
+    pc.log_k_rock = std::log10(1.0e-18);
+    pc.log_k_pore = std::log10(1.0e-12);
+    int grid = grid_for(c, c->g.N);
+    if (c->label_bytes == 1)
+        LS_LAUNCH(c, k_props<uint8_t>, grid, kBlock, 0, c->g, pc, (const uint8_t*)c->label, c->sat,
+                  c->precip, c->frac, c->kr, c->pc, c->perm, c->visc);
+    else
+        LS_LAUNCH(c, k_props<uint16_t>, grid, kBlock, 0, c->g, pc, (const uint16_t*)c->label, c->sat,
+                  c->precip, c->frac, c->kr, c->pc, c->perm, c->visc);
+    c->p_ready = 0;
+    return LS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// calculateFlux: central differences inside, one-sided on the domain faces (np=1).
+
+__device__ __forceinline__ double grad1(const double* __restrict__ f, long long r, long long off,
+                                        int pos, int ext, double dx) {
+    if (pos == 0) return (f[r + off] - f[r]) / dx;
+    if (pos == ext - 1) return (f[r] - f[r - off]) / dx;
+    return (f[r + off] - f[r - off]) / (2.0 * dx);
+}
+
+__global__ void __launch_bounds__(kBlock) k_flux(Grid g, double dx, double mcg,
+                                                 const double* __restrict__ P,
+                                                 const double* __restrict__ C,
+                                                 const double* __restrict__ perm,
+                                                 const double* __restrict__ visc,
+                                                 double* __restrict__ fx, double* __restrict__ fy,
+                                                 double* __restrict__ fz) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        decode(g, r, i, j, k);
+        double gPx = grad1(P, r, g.JK, i, g.I, dx);
+        double gPy = grad1(P, r, g.K, j, g.J, dx);
+        double gPz = grad1(P, r, 1, k, g.K, dx);
+        double gCx = grad1(C, r, g.JK, i, g.I, dx);
+        double gCy = grad1(C, r, g.K, j, g.J, dx);
+        double gCz = grad1(C, r, 1, k, g.K, dx);
+        gCx = smax(-mcg, smin(mcg, gCx));
+        gCy = smax(-mcg, smin(mcg, gCy));
+        gCz = smax(-mcg, smin(mcg, gCz));
+        double transmissivity = perm[r] / visc[r];
+        const double rho_g = 1000.0 * 9.81;
+        fx[r] = -transmissivity * ((gPx - gCx) - rho_g);
+        fy[r] = -transmissivity * (gPy - gCy);
+        fz[r] = -transmissivity * (gPz - gCz);
+    }
+}
+
+ls_status flux_run(ls_ctx* c) {
+    int grid = grid_for(c, c->g.N);
+    LS_LAUNCH(c, k_flux, grid, kBlock, 0, c->g, c->p.dx, c->p.max_cap_grad, c->P, c->pc, c->perm,
+              c->visc, c->fx, c->fy, c->fz);
+    return LS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// updateSaturation. div q and the evaporative sink of a voxel read only flux and labels,
+// which do not change between sub-steps, so the reference's num_steps full sweeps equal
+// num_steps repetitions of s <- clamp(s - dt_sub/phi*(div q + evap)) per voxel; the
+// repetition stops early once s reaches a fixed point of that map (every later sweep
+// would reproduce it bit for bit).
+
+__device__ __forceinline__ bool sat_inactive(int t) {
+    return t == kAir || t == kRock || t == kSulphide || t == kPrecipitate;
+}
+
+template <typename L>
+__device__ __forceinline__ void sat_rates(const Grid& g, const L* __restrict__ label,
+                                          const double* __restrict__ fx,
+                                          const double* __restrict__ fy,
+                                          const double* __restrict__ fz, long long r, int i,
+                                          int j, int k, int t, double dx, double evap,
+                                          double& div_q, double& evap_sink) {
+    const double fxr = fx[r], fyr = fy[r], fzr = fz[r];
+    double q_xp = (i + 1 < g.I) ? (fxr + fx[r + g.JK]) / 2.0 : 0.0;
+    double q_xm = (i > 0) ? (fxr + fx[r - g.JK]) / 2.0 : 0.0;
+    double q_yp = (j + 1 < g.J) ? (fyr + fy[r + g.K]) / 2.0 : 0.0;
+    double q_ym = (j > 0) ? (fyr + fy[r - g.K]) / 2.0 : 0.0;
+    double q_zp = (k + 1 < g.K) ? (fzr + fz[r + 1]) / 2.0 : 0.0;
+    double q_zm = (k > 0) ? (fzr + fz[r - 1]) / 2.0 : 0.0;
+    div_q = ((q_xp - q_xm) + (q_yp - q_ym) + (q_zp - q_zm)) / dx;
+    evap_sink = 0.0;
+    if (t == kPore) {
+        int air_faces = 0;
+        if (i + 1 < g.I && (int)label[r + g.JK] == kAir) air_faces++;
+        if (i > 0 && (int)label[r - g.JK] == kAir) air_faces++;
+        if (j + 1 < g.J && (int)label[r + g.K] == kAir) air_faces++;
+        if (j > 0 && (int)label[r - g.K] == kAir) air_faces++;
+        if (k + 1 < g.K && (int)label[r + 1] == kAir) air_faces++;
+        if (k > 0 && (int)label[r - 1] == kAir) air_faces++;
+        evap_sink = (air_faces * evap) / dx;
+    }
+}
+
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_sat_rate(Grid g, double dx, double evap,
+                                                     const L* __restrict__ label,
+                                                     const double* __restrict__ fx,
+                                                     const double* __restrict__ fy,
+                                                     const double* __restrict__ fz,
+                                                     double* __restrict__ partials) {
+    double v[1] = {0.0};
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        int t = (int)label[r];
+        if (sat_inactive(t)) continue;
+        int i, j, k;
+        decode(g, r, i, j, k);
+        double div_q, evap_sink;
+        sat_rates(g, label, fx, fy, fz, r, i, j, k, t, dx, evap, div_q, evap_sink);
+        double total_rate = fabs(div_q) + evap_sink;
+        if (total_rate > v[0]) v[0] = total_rate;
+    }
+    block_max_store<1>(v, partials);
+}
+
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_sat_update(Grid g, double dx, double evap,
+                                                       double dt_sub_over_phi, int num_steps,
+                                                       const L* __restrict__ label,
+                                                       const double* __restrict__ fx,
+                                                       const double* __restrict__ fy,
+                                                       const double* __restrict__ fz,
+                                                       double* __restrict__ sat) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.NP;
+         r += (long long)gridDim.x * blockDim.x) {
+        if (r >= g.N) {  // extra top plane of the freshly allocated array
+            sat[r] = 0.0;
+            continue;
+        }
+        int t = (int)label[r];
+        if (sat_inactive(t)) {
+            sat[r] = 0.0;  // never written by the reference's update (indeterminate there)
+            continue;
+        }
+        int i, j, k;
+        decode(g, r, i, j, k);
+        double div_q, evap_sink;
+        sat_rates(g, label, fx, fy, fz, r, i, j, k, t, dx, evap, div_q, evap_sink);
+        double sv = sat[r];
+        for (int step = 0; step < num_steps; ++step) {
+            double new_sat = sv - dt_sub_over_phi * (div_q + evap_sink);
+            double nv = smax(0.0, smin(1.0, new_sat));
+            bool fixed = (nv == sv) || (nv != nv && sv != sv);
+            sv = nv;
+            if (fixed) break;
+        }
+        sat[r] = sv;
+    }
+}
+
+ls_status saturation_run(ls_ctx* c, double dt, ls_substep_info* info) {
+    const double dx = c->p.dx, evap = c->p.evaporative_flux;
+    int grid = grid_for(c, c->g.N);
+    if (c->label_bytes == 1)
+        LS_LAUNCH(c, k_sat_rate<uint8_t>, grid, kBlock, 0, c->g, dx, evap, (const uint8_t*)c->label,
+                  c->fx, c->fy, c->fz, c->partials);
+    else
+        LS_LAUNCH(c, k_sat_rate<uint16_t>, grid, kBlock, 0, c->g, dx, evap, (const uint16_t*)c->label,
+                  c->fx, c->fy, c->fz, c->partials);
+    LS_TRY(finalize_max(c, grid, 1, S_RED0));
+    double max_div_q = 0.0;
+    LS_TRY(read_scalars(c, S_RED0, 1, &max_div_q));
+    // sub-step count, src/Simulation.cpp:1740-1767
+    const double max_dsat = 0.1;
+    double dt_safe = dt;
+    if (max_div_q > 1e-20) dt_safe = (max_dsat * c->p.porosity) / max_div_q;
+    double calculated_steps = std::ceil(dt / dt_safe);
+    int num_steps = 1;
+    if (std::isinf(calculated_steps) || std::isnan(calculated_steps)) num_steps = 1000;
+    else if (calculated_steps > 1000) num_steps = 1000;
+    else if (calculated_steps > 1.0) num_steps = (int)calculated_steps;
+    double dt_sub = dt / num_steps;
+    double dt_sub_over_phi = dt_sub / c->p.porosity;
+    if (info) {
+        info->max_rate = max_div_q;
+        info->num_steps = num_steps;
+        info->dt_sub = dt_sub;
+    }
+    int grid2 = grid_for(c, c->g.NP);
+    if (c->label_bytes == 1)
+        LS_LAUNCH(c, k_sat_update<uint8_t>, grid2, kBlock, 0, c->g, dx, evap, dt_sub_over_phi,
+                  num_steps, (const uint8_t*)c->label, c->fx, c->fy, c->fz, c->sat);
+    else
+        LS_LAUNCH(c, k_sat_update<uint16_t>, grid2, kBlock, 0, c->g, dx, evap, dt_sub_over_phi,
+                  num_steps, (const uint16_t*)c->label, c->fx, c->fy, c->fz, c->sat);
+    return LS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// handleSurfaceEffects: a Pore voxel holding fluid next to Air clogs. Turning Pore into
+// Precipitate never changes whether a neighbour is Air, so the voxels are independent.
+
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_surface(Grid g, L* __restrict__ label,
+                                                    const double* __restrict__ sat,
+                                                    double* __restrict__ conc) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        if ((int)label[r] != kPore || !(sat[r] > 0.0)) continue;
+        int i, j, k;
+        decode(g, r, i, j, k);
+        bool s = (i + 1 < g.I && (int)label[r + g.JK] == kAir) ||
+                 (i > 0 && (int)label[r - g.JK] == kAir) ||
+                 (j + 1 < g.J && (int)label[r + g.K] == kAir) ||
+                 (j > 0 && (int)label[r - g.K] == kAir) ||
+                 (k + 1 < g.K && (int)label[r + 1] == kAir) ||
+                 (k > 0 && (int)label[r - 1] == kAir);
+        if (s) {
+            conc[r] = 1.0;
+            label[r] = (L)kPrecipitate;
+        }
+    }
+}
+
+ls_status surface_run(ls_ctx* c) {
+    int grid = grid_for(c, c->g.N);
+    if (c->label_bytes == 1)
+        LS_LAUNCH(c, k_surface<uint8_t>, grid, kBlock, 0, c->g, (uint8_t*)c->label, c->sat, c->conc);
+    else
+        LS_LAUNCH(c, k_surface<uint16_t>, grid, kBlock, 0, c->g, (uint16_t*)c->label, c->sat, c->conc);
+    c->p_ready = 0;
+    return LS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// handlePrecipitation (pointwise).
+
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_precip(Grid g, double c_sat, int instant,
+                                                   double porosity, double solid_density,
+                                                   double time_scalar, L* __restrict__ label,
+                                                   double* __restrict__ conc,
+                                                   const double* __restrict__ sat,
+                                                   double* __restrict__ precip) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        double cv = conc[r];
+        if ((int)label[r] == kPore && cv > c_sat) {
+            double excess_conc = cv - c_sat;
+            if (instant) {
+                label[r] = (L)kPrecipitate;
+            } else {
+                double fluid_vol_fraction = porosity * sat[r];
+                double precipitated_vol_fraction = (excess_conc * fluid_vol_fraction) / solid_density;
+                double pv = precip[r] + (precipitated_vol_fraction * time_scalar);
+                precip[r] = pv;
+                if (pv > 0.90) label[r] = (L)kPrecipitate;
+            }
+            conc[r] = c_sat;
+        }
+    }
+}
+
+ls_status precip_run(ls_ctx* c) {
+    int grid = grid_for(c, c->g.N);
+    const ls_params& p = c->p;
+    if (c->label_bytes == 1)
+        LS_LAUNCH(c, k_precip<uint8_t>, grid, kBlock, 0, c->g, p.c_sat, p.use_instant_precipitation,
+                  p.porosity, p.solid_density, p.time_scalar, (uint8_t*)c->label, c->conc, c->sat,
+                  c->precip);
+    else
+        LS_LAUNCH(c, k_precip<uint16_t>, grid, kBlock, 0, c->g, p.c_sat, p.use_instant_precipitation,
+                  p.porosity, p.solid_density, p.time_scalar, (uint16_t*)c->label, c->conc, c->sat,
+                  c->precip);
+    c->p_ready = 0;
+    return LS_OK;
+}
+
+}  // namespace ls

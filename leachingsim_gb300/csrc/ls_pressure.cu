@@ -1,0 +1,590 @@
+// ls_pressure.cu - Darcy pressure system of Simulation::setupPressureEqns +
+// solvePressure (src/Simulation.cpp:658-855), matrix-free.
+//
+// Rows (one per voxel, src/Simulation.cpp:674-792):
+//   Air/Rock/Sulphide/Precipitate: identity, value = ramped top pressure on Air voxels
+//     that touch a non-Air voxel, else 0                                   (kind 1)
+//   Pore: sum_n c_n P_n + diag P = b, c_n = harmonic(K)/mu, diag = -sum c_n
+//     (floored to +1e-16 when |diag| < 1e-16: kind 3, else kind 2)
+//   any other label: no entries at all (kind 0); Krylov methods leave such an unknown
+//     at its initial value, so it keeps its current value here.
+//
+// Solver: FP64 iterative refinement on the assembled operator A. Each sweep computes
+// r = b - A x in FP64 and the correction from a block-triangular splitting: floored
+// rows (kind 3) are solved from their diagonal, the normal Pore rows (kind 2) from the
+// symmetric positive definite system M d = A_SQ d_Q - r_S with M = -A_SS, Jacobi-scaled
+// to unit diagonal and solved by an inner PCG in FP32 (LS_PRESS_MIXED) or FP64.
+// Convergence is judged on the FP64 Jacobi-scaled residual ||D^-1 r|| / ||D^-1 b||, the
+// norm PETSc's left-Jacobi GMRES tests in the reference.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "ls_internal.cuh"
+
+namespace ls {
+
+// scalar slots
+enum {
+    SP_NUM = 16,   // sum (r/diag)^2 over rows
+    SP_NAN = 17,
+    SP_DEN = 18,   // sum (b/diag)^2
+    SP_XMAX = 19,
+    SP_XNMAX = 20, // max of -x
+    SP_RZ = 24,    // inner: (r, z)
+    SP_PQ = 25,    // inner: (p, q)
+    SP_RZN = 26,   // inner: new (r, z)
+    SP_RR = 27,    // inner: (r, r)
+    SP_RR0 = 28,
+    SP_RZ_OLD = 29
+};
+
+// ---------------------------------------------------------------------------
+// setup
+
+struct PressConst {
+    double eff_top, evap_dx;
+};
+
+template <typename L>
+__device__ __forceinline__ double link_coeff(const L* __restrict__ label,
+                                             const double* __restrict__ perm,
+                                             const double* __restrict__ visc, long long self,
+                                             long long nb) {
+    // set_neighbor_link of src/Simulation.cpp:730-771 for the Pore voxel `self`
+    double K_neighbor = ((int)label[nb] == kAir) ? 1.0e-9 : perm[nb];
+    double K_self = smax(perm[self], 1e-25);
+    double K_neigh = smax(K_neighbor, 1e-25);
+    double K_avg = (2.0 * K_self * K_neigh) / (K_self + K_neigh);
+    return K_avg / visc[self];
+}
+
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_press_setup(Grid g, PressConst pcst,
+                                                        const L* __restrict__ label,
+                                                        const double* __restrict__ perm,
+                                                        const double* __restrict__ visc,
+                                                        int8_t* __restrict__ kind,
+                                                        double* __restrict__ diag,
+                                                        double* __restrict__ b,
+                                                        double* __restrict__ f0,
+                                                        double* __restrict__ f1,
+                                                        double* __restrict__ f2,
+                                                        double* __restrict__ partials) {
+    double acc[1] = {0.0};  // sum (b/diag)^2
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        decode(g, r, i, j, k);
+        const int t = (int)label[r];
+        // + face coefficients (identical from either side: the harmonic mean is symmetric)
+        double* faces[3] = {f0, f1, f2};
+        const long long offs[3] = {g.JK, g.K, 1};
+        const bool hasp[3] = {i + 1 < g.I, j + 1 < g.J, k + 1 < g.K};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            double cf = 0.0;
+            if (hasp[d]) {
+                long long nb = r + offs[d];
+                int tn = (int)label[nb];
+                if (t == kPore) cf = link_coeff(label, perm, visc, r, nb);
+                else if (tn == kPore) cf = link_coeff(label, perm, visc, nb, r);
+            }
+            faces[d][r] = cf;
+        }
+        int8_t kd = 0;
+        double dg = 0.0, bv = 0.0;
+        if (t == kAir || t == kRock || t == kSulphide || t == kPrecipitate) {
+            kd = 1;
+            dg = 1.0;
+            if (t == kAir) {
+                bool is_surface = (i + 1 < g.I && (int)label[r + g.JK] != kAir) ||
+                                  (i > 0 && (int)label[r - g.JK] != kAir) ||
+                                  (j + 1 < g.J && (int)label[r + g.K] != kAir) ||
+                                  (j > 0 && (int)label[r - g.K] != kAir) ||
+                                  (k + 1 < g.K && (int)label[r + 1] != kAir) ||
+                                  (k > 0 && (int)label[r - 1] != kAir);
+                bv = 0.0 + (is_surface ? pcst.eff_top : 0.0);
+            }
+        } else if (t == kPore) {
+            double diagonal_term = 0.0, source_term = 0.0;
+            const long long nbs[6] = {r + g.JK, r - g.JK, r + g.K, r - g.K, r + 1, r - 1};
+            const bool val[6] = {i + 1 < g.I, i > 0, j + 1 < g.J, j > 0, k + 1 < g.K, k > 0};
+#pragma unroll
+            for (int d = 0; d < 6; ++d) {
+                if (!val[d]) continue;
+                if ((int)label[nbs[d]] == kAir) source_term -= pcst.evap_dx;
+                diagonal_term -= link_coeff(label, perm, visc, r, nbs[d]);
+            }
+            kd = 2;
+            if (fabs(diagonal_term) < 1e-16) {
+                diagonal_term = 1e-16;
+                kd = 3;
+            }
+            dg = diagonal_term;
+            bv = 0.0 + source_term;
+        }
+        kind[r] = kd;
+        diag[r] = dg;
+        b[r] = bv;
+        double di = (dg != 0.0) ? 1.0 / dg : 1.0;
+        double sb = di * bv;
+        acc[0] += sb * sb;
+    }
+    block_sum_store<1>(acc, partials);
+}
+
+// 1/sqrt(d) of the inner unknowns (normal Pore rows).
+__global__ void k_press_isd(Grid g, const int8_t* __restrict__ kind, const double* __restrict__ diag,
+                            double* __restrict__ isd) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x)
+        isd[r] = (kind[r] == 2) ? 1.0 / sqrt(-diag[r]) : 0.0;
+}
+
+// Jacobi-scaled inner weights w = c / sqrt(d_a d_b) between two inner unknowns.
+template <typename T>
+__global__ void k_press_weights(Grid g, const double* __restrict__ isd,
+                                const double* __restrict__ f0, const double* __restrict__ f1,
+                                const double* __restrict__ f2, T* __restrict__ w0,
+                                T* __restrict__ w1, T* __restrict__ w2) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        decode(g, r, i, j, k);
+        double a = isd[r];
+        double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+        if (a != 0.0) {
+            if (i + 1 < g.I) v0 = f0[r] * a * isd[r + g.JK];
+            if (j + 1 < g.J) v1 = f1[r] * a * isd[r + g.K];
+            if (k + 1 < g.K) v2 = f2[r] * a * isd[r + 1];
+        }
+        w0[r] = (T)v0;
+        w1[r] = (T)v1;
+        w2[r] = (T)v2;
+    }
+}
+
+// identity rows take their value; other rows keep the warm start.
+__global__ void k_press_init_x(Grid g, const int8_t* __restrict__ kind, const double* __restrict__ b,
+                               double* __restrict__ x) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x)
+        if (kind[r] == 1) x[r] = b[r];
+}
+
+// (A x)_r for a Pore row: diag x_r + sum_d c_d x_nb, summed in ascending column order.
+__device__ __forceinline__ double press_row_apply(const Grid& g, long long r, int i, int j, int k,
+                                                  double dg, const double* __restrict__ x,
+                                                  const double* __restrict__ f0,
+                                                  const double* __restrict__ f1,
+                                                  const double* __restrict__ f2) {
+    double acc = 0.0;
+    if (i > 0) acc += f0[r - g.JK] * x[r - g.JK];
+    if (j > 0) acc += f1[r - g.K] * x[r - g.K];
+    if (k > 0) acc += f2[r - 1] * x[r - 1];
+    acc += dg * x[r];
+    if (k + 1 < g.K) acc += f2[r] * x[r + 1];
+    if (j + 1 < g.J) acc += f1[r] * x[r + g.K];
+    if (i + 1 < g.I) acc += f0[r] * x[r + g.JK];
+    return acc;
+}
+
+// Full operator y = A x (test hook; identity rows y = x, empty rows y = 0).
+__global__ void k_press_apply_full(Grid g, const int8_t* __restrict__ kind,
+                                   const double* __restrict__ diag, const double* __restrict__ f0,
+                                   const double* __restrict__ f1, const double* __restrict__ f2,
+                                   const double* __restrict__ x, double* __restrict__ y) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        int kd = kind[r];
+        if (kd == 0) { y[r] = 0.0; continue; }
+        if (kd == 1) { y[r] = x[r]; continue; }
+        int i, j, k;
+        decode(g, r, i, j, k);
+        y[r] = press_row_apply(g, r, i, j, k, diag[r], x, f0, f1, f2);
+    }
+}
+
+// Outer residual r = b - A x on Pore rows (0 elsewhere) with the scaled norm, NaN count
+// and the max / -min of x.
+__global__ void __launch_bounds__(kBlock) k_press_residual(Grid g, const int8_t* __restrict__ kind,
+                                                           const double* __restrict__ diag,
+                                                           const double* __restrict__ b,
+                                                           const double* __restrict__ f0,
+                                                           const double* __restrict__ f1,
+                                                           const double* __restrict__ f2,
+                                                           const double* __restrict__ x,
+                                                           double* __restrict__ res,
+                                                           double* __restrict__ partials,
+                                                           double* __restrict__ partials_max,
+                                                           int nblk) {
+    double acc[2] = {0.0, 0.0};
+    double mx[2] = {-INFINITY, -INFINITY};
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        int kd = kind[r];
+        double xv = x[r];
+        mx[0] = smax(mx[0], xv);
+        mx[1] = smax(mx[1], -xv);
+        if (xv != xv) acc[1] += 1.0;
+        double rv = 0.0;
+        if (kd >= 2) {
+            int i, j, k;
+            decode(g, r, i, j, k);
+            double dg = diag[r];
+            rv = b[r] - press_row_apply(g, r, i, j, k, dg, x, f0, f1, f2);
+            double s = rv / dg;
+            acc[0] += s * s;
+            if (rv != rv) acc[1] += 1.0;
+        }
+        res[r] = rv;
+    }
+    block_sum_store<2>(acc, partials);
+    __syncthreads();
+    block_max_store<2>(mx, partials_max);
+    (void)nblk;
+}
+
+// Correction for floored rows and the scaled inner right-hand side
+//   d_Q = r_Q / diag_Q,  g = D^-1/2 (A_SQ d_Q - r_S).
+template <typename T>
+__global__ void k_press_inner_rhs(Grid g, const int8_t* __restrict__ kind,
+                                  const double* __restrict__ diag, const double* __restrict__ isd,
+                                  const double* __restrict__ res, const double* __restrict__ f0,
+                                  const double* __restrict__ f1, const double* __restrict__ f2,
+                                  double* __restrict__ delta, T* __restrict__ rhs) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        int kd = kind[r];
+        double dq = (kd == 3) ? res[r] / diag[r] : 0.0;
+        delta[r] = dq;
+        T gv = (T)0;
+        if (kd == 2) {
+            int i, j, k;
+            decode(g, r, i, j, k);
+            double acc = 0.0;
+            // couplings to floored rows: their correction is d_Q = r_Q / diag_Q
+            if (i > 0 && kind[r - g.JK] == 3) acc += f0[r - g.JK] * (res[r - g.JK] / diag[r - g.JK]);
+            if (j > 0 && kind[r - g.K] == 3) acc += f1[r - g.K] * (res[r - g.K] / diag[r - g.K]);
+            if (k > 0 && kind[r - 1] == 3) acc += f2[r - 1] * (res[r - 1] / diag[r - 1]);
+            if (k + 1 < g.K && kind[r + 1] == 3) acc += f2[r] * (res[r + 1] / diag[r + 1]);
+            if (j + 1 < g.J && kind[r + g.K] == 3) acc += f1[r] * (res[r + g.K] / diag[r + g.K]);
+            if (i + 1 < g.I && kind[r + g.JK] == 3) acc += f0[r] * (res[r + g.JK] / diag[r + g.JK]);
+            gv = (T)(isd[r] * (acc - res[r]));
+        }
+        rhs[r] = gv;
+    }
+}
+
+// x += delta (floored rows) and x += D^-1/2 * inner solution (normal Pore rows), FP64.
+template <typename T>
+__global__ void k_press_accumulate(Grid g, const int8_t* __restrict__ kind,
+                                   const double* __restrict__ isd, const double* __restrict__ delta,
+                                   const T* __restrict__ xin, double* __restrict__ x) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        int kd = kind[r];
+        if (kd == 3) x[r] += delta[r];
+        else if (kd == 2) x[r] += isd[r] * (double)xin[r];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// inner PCG on W = I - L (unit diagonal, L = scaled links between inner unknowns)
+
+template <typename T>
+__device__ __forceinline__ T inner_apply_row(const Grid& g, long long r, int i, int j, int k,
+                                             const T* __restrict__ v, const T* __restrict__ w0,
+                                             const T* __restrict__ w1, const T* __restrict__ w2) {
+    T acc = (T)0;
+    if (i > 0) acc += w0[r - g.JK] * v[r - g.JK];
+    if (j > 0) acc += w1[r - g.K] * v[r - g.K];
+    if (k > 0) acc += w2[r - 1] * v[r - 1];
+    if (k + 1 < g.K) acc += w2[r] * v[r + 1];
+    if (j + 1 < g.J) acc += w1[r] * v[r + g.K];
+    if (i + 1 < g.I) acc += w0[r] * v[r + g.JK];
+    return v[r] - acc;
+}
+
+// q = W p, partial (p, q)
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_cg_apply(Grid g, const T* __restrict__ p,
+                                                     const T* __restrict__ w0,
+                                                     const T* __restrict__ w1,
+                                                     const T* __restrict__ w2, T* __restrict__ q,
+                                                     double* __restrict__ partials) {
+    double acc[1] = {0.0};
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        decode(g, r, i, j, k);
+        T qv = inner_apply_row(g, r, i, j, k, p, w0, w1, w2);
+        q[r] = qv;
+        acc[0] += (double)p[r] * (double)qv;
+    }
+    block_sum_store<1>(acc, partials);
+}
+
+// x += a p, r -= a q with a = (r,z)/(p,q); Jacobi-scaled system: z = r. partial (r, r).
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_cg_update(Grid g, const double* __restrict__ scal,
+                                                      const T* __restrict__ p,
+                                                      const T* __restrict__ q, T* __restrict__ x,
+                                                      T* __restrict__ r_, double* __restrict__ partials) {
+    const double alpha = scal[SP_RZ] / scal[SP_PQ];
+    const T a = (T)alpha;
+    double acc[1] = {0.0};
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        x[r] += a * p[r];
+        T rv = r_[r] - a * q[r];
+        r_[r] = rv;
+        acc[0] += (double)rv * (double)rv;
+    }
+    block_sum_store<1>(acc, partials);
+}
+
+// p = z + b p with b = (r,z)_new / (r,z)_old; z = r here.
+template <typename T>
+__global__ void k_cg_dir(Grid g, const double* __restrict__ scal, const T* __restrict__ z,
+                         T* __restrict__ p) {
+    const T beta = (T)(scal[SP_RZN] / scal[SP_RZ]);
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x)
+        p[r] = z[r] + beta * p[r];
+}
+
+template <typename T>
+__global__ void k_copy_dot(Grid g, const T* __restrict__ a, T* __restrict__ b, T* __restrict__ c,
+                           double* __restrict__ partials) {
+    double acc[1] = {0.0};
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        T v = a[r];
+        b[r] = v;
+        if (c) c[r] = (T)0;
+        acc[0] += (double)v * (double)v;
+    }
+    block_sum_store<1>(acc, partials);
+}
+
+__global__ void k_set_scalar(double* scal, int dst, int src) { scal[dst] = scal[src]; }
+
+template <typename T>
+static ls_status inner_alloc(ls_ctx* c) {
+    const bool is64 = sizeof(T) == 8;
+    if (c->inner[0] && c->inner_is64 == (int)is64) return LS_OK;
+    for (int q = 0; q < 5; ++q) {
+        if (c->inner[q]) { cudaFree(c->inner[q]); c->device_bytes -= sizeof(T) * (size_t)c->g.N; }
+        c->inner[q] = nullptr;
+    }
+    for (int q = 0; q < 5; ++q) LS_TRY(dalloc(c, &c->inner[q], sizeof(T) * (size_t)c->g.N));
+    c->inner_is64 = is64;
+    return LS_OK;
+}
+
+// Inner PCG: solve W x = rhs (rhs held in inner[1] on entry) to relative residual tol.
+// Returns the iterations used in *its.
+template <typename T>
+static ls_status inner_pcg(ls_ctx* c, T* const* w, double tol, int max_it, int* its,
+                           double* rel_out) {
+    T* x = (T*)c->inner[0];
+    T* r = (T*)c->inner[1];
+    T* z = (T*)c->inner[2];
+    T* p = (T*)c->inner[3];
+    T* q = (T*)c->inner[4];
+    const Grid g = c->g;
+    const int grid = grid_for(c, g.N);
+    (void)z;
+    // x = 0, p = r, rz = (r, r)
+    LS_LAUNCH(c, k_copy_dot<T>, grid, kBlock, 0, g, (const T*)r, p, x, c->partials);
+    LS_TRY(finalize_sum(c, grid, 1, SP_RZ));
+    double rr0 = 0.0;
+    LS_TRY(read_scalars(c, SP_RZ, 1, &rr0));
+    *its = 0;
+    *rel_out = 0.0;
+    if (!(rr0 > 0.0)) {
+        if (rr0 != rr0) return set_error(c, LS_NONFINITE, "pressure: NaN in inner right-hand side");
+        return LS_OK;
+    }
+    const double target = tol * tol * rr0;
+    double rr = rr0;
+    for (int it = 0; it < max_it; ++it) {
+        {
+            Timed tm(c, LS_T_CG_APPLY);
+            LS_LAUNCH(c, k_cg_apply<T>, grid, kBlock, 0, g, (const T*)p, (const T*)w[0],
+                      (const T*)w[1], (const T*)w[2], q, c->partials);
+            // p in, three own face weights, q out
+            if (c->timing) c->timer_bytes[LS_T_CG_APPLY] += (double)g.N * 5.0 * sizeof(T);
+        }
+        LS_TRY(finalize_sum(c, grid, 1, SP_PQ));
+        LS_LAUNCH(c, k_cg_update<T>, grid, kBlock, 0, g, (const double*)c->scal, (const T*)p,
+                  (const T*)q, x, r, c->partials);
+        LS_TRY(finalize_sum(c, grid, 1, SP_RZN));
+        *its = it + 1;
+        LS_TRY(read_scalars(c, SP_RZN, 1, &rr));
+        if (rr != rr) return set_error(c, LS_NONFINITE, "pressure: NaN in inner PCG");
+        if (rr <= target) break;
+        LS_LAUNCH(c, k_cg_dir<T>, grid, kBlock, 0, g, (const double*)c->scal, (const T*)r, p);
+        LS_LAUNCH(c, k_set_scalar, 1, 1, 0, c->scal, SP_RZ, SP_RZN);
+    }
+    *rel_out = sqrt(rr / rr0);
+    return LS_OK;
+}
+
+// ---------------------------------------------------------------------------
+
+ls_status pressure_setup_run(ls_ctx* c, double t) {
+    PressConst pcst;
+    const double ramp_duration = 3600.0;
+    double effective_top_pressure = c->p.top_pressure;
+    if (t < ramp_duration)
+        effective_top_pressure = c->p.top_pressure * (t / ramp_duration) + 1e-6;
+    pcst.eff_top = effective_top_pressure;
+    pcst.evap_dx = c->p.evaporative_flux * c->p.dx;
+    const Grid g = c->g;
+    const int grid = grid_for(c, g.N);
+    if (c->label_bytes == 1)
+        LS_LAUNCH(c, k_press_setup<uint8_t>, grid, kBlock, 0, g, pcst, (const uint8_t*)c->label,
+                  c->perm, c->visc, c->pkind, c->pdiag, c->pb, c->pface[0], c->pface[1], c->pface[2],
+                  c->partials);
+    else
+        LS_LAUNCH(c, k_press_setup<uint16_t>, grid, kBlock, 0, g, pcst, (const uint16_t*)c->label,
+                  c->perm, c->visc, c->pkind, c->pdiag, c->pb, c->pface[0], c->pface[1], c->pface[2],
+                  c->partials);
+    LS_TRY(finalize_sum(c, grid, 1, SP_DEN));
+    LS_LAUNCH(c, k_press_isd, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const double*)c->pdiag,
+              c->pisd);
+    c->p_t = t;
+    c->p_ready = 1;
+    return LS_OK;
+}
+
+ls_status pressure_apply_run(ls_ctx* c, const double* xh, double* yh) {
+    const size_t bytes = sizeof(double) * (size_t)c->g.N;
+    LS_CUDA(c, cudaMemcpyAsync(c->pdelta, xh, bytes, cudaMemcpyHostToDevice, c->stream));
+    const int grid = grid_for(c, c->g.N);
+    LS_LAUNCH(c, k_press_apply_full, grid, kBlock, 0, c->g, (const int8_t*)c->pkind,
+              (const double*)c->pdiag, (const double*)c->pface[0], (const double*)c->pface[1],
+              (const double*)c->pface[2], (const double*)c->pdelta, c->pr);
+    LS_CUDA(c, cudaMemcpyAsync(yh, c->pr, bytes, cudaMemcpyDeviceToHost, c->stream));
+    LS_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->p_ready = 1;
+    return LS_OK;
+}
+
+template <typename T>
+static ls_status ensure_weights(ls_ctx* c, T** w) {
+    const bool is64 = sizeof(T) == 8;
+    for (int d = 0; d < 3; ++d) {
+        void** slot = is64 ? (void**)&c->w64[d] : (void**)&c->w32[d];
+        if (!*slot) LS_TRY(dalloc(c, slot, sizeof(T) * (size_t)c->g.N));
+        w[d] = (T*)*slot;
+    }
+    return LS_OK;
+}
+
+template <typename T>
+static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info) {
+    const Grid g = c->g;
+    const int grid = grid_for(c, g.N);
+    double* x = c->P + (c->p.compat_shift ? g.JK : 0);
+    T* w[3];
+    LS_TRY(ensure_weights<T>(c, w));
+    LS_TRY(inner_alloc<T>(c));
+    {
+        Timed tm(c, LS_T_PRESS_SETUP);
+        LS_LAUNCH(c, k_press_weights<T>, grid, kBlock, 0, g, (const double*)c->pisd,
+                  (const double*)c->pface[0], (const double*)c->pface[1],
+                  (const double*)c->pface[2], w[0], w[1], w[2]);
+        LS_LAUNCH(c, k_press_init_x, grid, kBlock, 0, g, (const int8_t*)c->pkind,
+                  (const double*)c->pb, x);
+    }
+    double den = 0.0;
+    LS_TRY(read_scalars(c, SP_DEN, 1, &den));
+    const double rtol = c->p.press_rtol;
+    // inner relative tolerance: enough to reach rtol from the current residual, but not
+    // below what the inner precision resolves
+    const double inner_floor = (sizeof(T) == 4) ? 1e-5 : 1e-13;
+    int total_inner = 0, sweeps = 0;
+    double rel = 0.0;
+    ls_status result = LS_NOT_CONVERGED;
+    double* pmax = c->partials + (size_t)kMaxPartials * 4;
+    double prev_rel = INFINITY;
+    int stagnant = 0;
+    const int max_sweeps = 64;
+    for (;;) {
+        double sc[2] = {0.0, 0.0};
+        {
+            Timed tm(c, LS_T_PRESS_OUTER);
+            LS_LAUNCH(c, k_press_residual, grid, kBlock, 0, g, (const int8_t*)c->pkind,
+                      (const double*)c->pdiag, (const double*)c->pb, (const double*)c->pface[0],
+                      (const double*)c->pface[1], (const double*)c->pface[2], (const double*)x,
+                      c->pr, c->partials, pmax, grid);
+            LS_TRY(finalize_sum(c, grid, 2, SP_NUM));
+        }
+        LS_TRY(read_scalars(c, SP_NUM, 2, sc));
+        if (sc[1] > 0.0 || sc[0] != sc[0]) {
+            result = set_error(c, LS_NONFINITE, "pressure: NaN in the FP64 residual");
+            rel = NAN;
+            break;
+        }
+        rel = (den > 0.0) ? sqrt(sc[0] / den) : sqrt(sc[0]);
+        if (rel <= rtol || (den == 0.0 && sc[0] == 0.0)) { result = LS_OK; break; }
+        if (total_inner >= c->p.press_max_it || sweeps >= max_sweeps) break;
+        if (rel > 0.5 * prev_rel) {
+            if (++stagnant >= 8) break;
+        } else {
+            stagnant = 0;
+        }
+        prev_rel = rel;
+        sweeps++;
+        int its = 0;
+        double irel = 0.0;
+        {
+            Timed tm(c, LS_T_PRESS_INNER);
+            LS_LAUNCH(c, k_press_inner_rhs<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind,
+                      (const double*)c->pdiag, (const double*)c->pisd, (const double*)c->pr,
+                      (const double*)c->pface[0], (const double*)c->pface[1],
+                      (const double*)c->pface[2], c->pdelta, (T*)c->inner[1]);
+            double tol = std::max(inner_floor, 0.2 * rtol / std::max(rel, 1e-300));
+            tol = std::min(tol, 0.5);
+            ls_status st = inner_pcg<T>(c, w, tol, c->p.press_max_it - total_inner, &its, &irel);
+            if (st != LS_OK) { result = st; break; }
+            LS_LAUNCH(c, k_press_accumulate<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind,
+                      (const double*)c->pisd, (const double*)c->pdelta, (const T*)c->inner[0], x);
+        }
+        total_inner += its;
+    }
+    // min / max of the solution vector for the log line
+    double mm[2] = {0.0, 0.0};
+    // k_press_residual left the block maxima of x and -x in pmax
+    LS_LAUNCH(c, k_finalize<true>, 1, 32, 0, pmax, grid, 2, c->scal + SP_XMAX);
+    LS_TRY(read_scalars(c, SP_XMAX, 2, mm));
+    if (info) {
+        info->iterations = total_inner;
+        info->outer_iterations = sweeps;
+        info->converged = (result == LS_OK) ? 1 : 0;
+        info->reason = (result == LS_OK) ? 2 : (result == LS_NONFINITE ? -4 : -3);
+        info->rel_residual = rel;
+        info->max_value = mm[0];
+        info->min_value = -mm[1];
+    }
+    if (result == LS_NOT_CONVERGED) {
+        char buf[160];
+        snprintf(buf, sizeof(buf), "pressure: not converged (rel %.3e after %d inner its, %d sweeps)",
+                 rel, total_inner, sweeps);
+        set_error(c, LS_NOT_CONVERGED, buf);
+    }
+    return result;
+}
+
+ls_status pressure_solve_run(ls_ctx* c, ls_solve_info* info) {
+    if (!c->p_ready) return set_error(c, LS_BAD_ARG, "pressure system not assembled");
+    if (c->p.press_solver == LS_PRESS_MIXED) return pressure_solve_t<float>(c, info);
+    return pressure_solve_t<double>(c, info);
+}
+
+}  // namespace ls

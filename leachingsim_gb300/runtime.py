@@ -1,0 +1,311 @@
+"""ctypes binding of libleachingsim_gb300.so (the C-ABI of include/leachingsim.h).
+
+There is no fallback: if the CUDA library cannot be loaded, or no GPU is
+present, creating a Context raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import FIELDS, LsParams, LsSolveInfo, LsStepInfo, LsSubstepInfo, TIMERS
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libleachingsim_gb300.so")
+
+SYMBOLS = {
+    # name: (restype, argtypes)
+    "ls_params_default": (None, [C.POINTER(LsParams)]),
+    "ls_abi_version": (C.c_int, []),
+    "ls_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int, C.c_int,
+                            C.POINTER(LsParams)]),
+    "ls_destroy": (C.c_int, [C.c_void_p]),
+    "ls_last_error": (C.c_char_p, [C.c_void_p]),
+    "ls_set_params": (C.c_int, [C.c_void_p, C.POINTER(LsParams)]),
+    "ls_get_params": (C.c_int, [C.c_void_p, C.POINTER(LsParams)]),
+    "ls_stream": (C.c_void_p, [C.c_void_p]),
+    "ls_synchronize": (C.c_int, [C.c_void_p]),
+    "ls_device_bytes": (C.c_size_t, [C.c_void_p]),
+    "ls_upload_field": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_int]),
+    "ls_download_field": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_int]),
+    "ls_upload_field_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_int]),
+    "ls_download_field_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_int]),
+    "ls_init_fields": (C.c_int, [C.c_void_p]),
+    "ls_init_frac": (C.c_int, [C.c_void_p, C.POINTER(C.c_ulonglong)]),
+    "ls_init_saturation": (C.c_int, [C.c_void_p]),
+    "ls_init_acid": (C.c_int, [C.c_void_p]),
+    "ls_props": (C.c_int, [C.c_void_p]),
+    "ls_pressure_step": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(LsSolveInfo)]),
+    "ls_flux": (C.c_int, [C.c_void_p]),
+    "ls_saturation": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(LsSubstepInfo)]),
+    "ls_saturation_implicit": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(LsSolveInfo)]),
+    "ls_surface": (C.c_int, [C.c_void_p]),
+    "ls_transport": (C.c_int, [C.c_void_p, C.c_double, C.c_int, C.POINTER(LsSolveInfo),
+                               C.POINTER(LsSolveInfo)]),
+    "ls_precip": (C.c_int, [C.c_void_p]),
+    "ls_dissolve": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_int),
+                              C.POINTER(LsSubstepInfo)]),
+    "ls_snapshot": (C.c_int, [C.c_void_p]),
+    "ls_rollback": (C.c_int, [C.c_void_p]),
+    "ls_step": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.POINTER(LsStepInfo)]),
+    "ls_pressure_setup": (C.c_int, [C.c_void_p, C.c_double]),
+    "ls_pressure_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ls_pressure_rhs": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ls_transport_apply": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]),
+    "ls_timing_enable": (C.c_int, [C.c_void_p, C.c_int]),
+    "ls_timing_reset": (C.c_int, [C.c_void_p]),
+    "ls_timing_get": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double),
+                                C.POINTER(C.c_longlong)]),
+    "ls_timing_bytes": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
+    "ls_kernel_launches": (C.c_longlong, [C.c_void_p]),
+}
+
+_lib = None
+
+
+def load(build_if_missing=True):
+    """Load the CUDA library (building it in-tree first when it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH) and build_if_missing:
+        from . import build
+        build.build()
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run python -m leachingsim_gb300.build")
+    L = C.CDLL(LIB_PATH)
+    for name, (res, args) in SYMBOLS.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+class LsError(RuntimeError):
+    def __init__(self, status, message):
+        self.status = status
+        super().__init__(f"{_abi.STATUS_NAMES.get(status, status)}: {message}")
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """One simulation domain on the GPU (owns an ls_ctx)."""
+
+    def __init__(self, shape, label_bytes=1, params=None):
+        L = load()
+        self.shape = tuple(int(v) for v in shape)
+        self.I, self.J, self.K = self.shape
+        self.N = self.I * self.J * self.K
+        self.NP = (self.I + 1) * self.J * self.K
+        self.label_bytes = int(label_bytes)
+        self.params = params if params is not None else _abi.default_params()
+        h = C.c_void_p()
+        st = L.ls_create(C.byref(h), self.I, self.J, self.K, self.label_bytes, C.byref(self.params))
+        if st != 0:
+            raise LsError(st, "ls_create failed")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().ls_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st, allowed=(0,)):
+        if st not in allowed:
+            msg = load().ls_last_error(self.h)
+            raise LsError(st, msg.decode() if msg else "")
+        return st
+
+    # parameters -----------------------------------------------------------
+    def set_params(self, params):
+        self.params = params
+        self._check(load().ls_set_params(self.h, C.byref(params)))
+
+    # transfers --------------------------------------------------------------
+    def _dtype(self, fid):
+        if fid == 0:
+            return np.uint8 if self.label_bytes == 1 else np.uint16
+        if fid == 1:
+            return np.float32
+        return np.float64
+
+    def upload(self, name, arr, padded=False):
+        fid = FIELDS[name]
+        a = np.ascontiguousarray(np.asarray(arr).reshape(-1), dtype=self._dtype(fid))
+        self._check(load().ls_upload_field(self.h, fid, _p(a), a.size, int(padded)))
+
+    def download(self, name, padded=False, out=None):
+        fid = FIELDS[name]
+        n = self.NP if padded else self.N
+        if out is None:
+            out = np.empty(n, dtype=self._dtype(fid))
+        self._check(load().ls_download_field(self.h, fid, _p(out), n, int(padded)))
+        return out.reshape((self.I + (1 if padded else 0), self.J, self.K))
+
+    # initialisation ---------------------------------------------------------
+    def init_all(self):
+        """Fresh start of src/main.cpp:189-206; returns the initial sulphide count."""
+        L = load()
+        self._check(L.ls_init_fields(self.h))
+        cnt = C.c_ulonglong(0)
+        self._check(L.ls_init_frac(self.h, C.byref(cnt)))
+        self._check(L.ls_init_saturation(self.h))
+        self._check(L.ls_init_acid(self.h))
+        self._check(L.ls_props(self.h))
+        return int(cnt.value)
+
+    def init_fields(self):
+        self._check(load().ls_init_fields(self.h))
+
+    def init_frac(self):
+        cnt = C.c_ulonglong(0)
+        self._check(load().ls_init_frac(self.h, C.byref(cnt)))
+        return int(cnt.value)
+
+    def init_saturation(self):
+        self._check(load().ls_init_saturation(self.h))
+
+    def init_acid(self):
+        self._check(load().ls_init_acid(self.h))
+
+    # hot path ---------------------------------------------------------------
+    def props(self):
+        self._check(load().ls_props(self.h))
+
+    def pressure(self, t):
+        info = LsSolveInfo()
+        st = self._check(load().ls_pressure_step(self.h, float(t), C.byref(info)), (0, 1, 2, 3))
+        return st in (0, 2), info.as_dict()
+
+    def flux(self):
+        self._check(load().ls_flux(self.h))
+
+    def saturation(self, dt):
+        info = LsSubstepInfo()
+        self._check(load().ls_saturation(self.h, float(dt), C.byref(info)))
+        return info.as_dict()
+
+    def saturation_implicit(self, dt):
+        info = LsSolveInfo()
+        st = self._check(load().ls_saturation_implicit(self.h, float(dt), C.byref(info)), (0, 1, 3, 8))
+        return st == 0, st != 8, info.as_dict()
+
+    def surface(self):
+        self._check(load().ls_surface(self.h))
+
+    def transport(self, dt, which=3):
+        ci, ai = LsSolveInfo(), LsSolveInfo()
+        st = self._check(load().ls_transport(self.h, float(dt), int(which), C.byref(ci), C.byref(ai)),
+                         (0, 1, 3))
+        return st == 0, ci.as_dict(), ai.as_dict()
+
+    def precip(self):
+        self._check(load().ls_precip(self.h))
+
+    def dissolve(self, dt):
+        n = C.c_int(0)
+        info = LsSubstepInfo()
+        self._check(load().ls_dissolve(self.h, float(dt), C.byref(n), C.byref(info)))
+        return int(n.value), info.as_dict()
+
+    def snapshot(self):
+        self._check(load().ls_snapshot(self.h))
+
+    def rollback(self):
+        self._check(load().ls_rollback(self.h))
+
+    def step(self, t, dt):
+        info = LsStepInfo()
+        self._check(load().ls_step(self.h, float(t), float(dt), C.byref(info)))
+        d = info.as_dict()
+        return bool(d["success"]), d
+
+    def synchronize(self):
+        self._check(load().ls_synchronize(self.h))
+
+    def stream(self):
+        return load().ls_stream(self.h)
+
+    def device_bytes(self):
+        return int(load().ls_device_bytes(self.h))
+
+    # test hooks -------------------------------------------------------------
+    def pressure_setup(self, t):
+        self._check(load().ls_pressure_setup(self.h, float(t)))
+
+    def pressure_apply(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1)
+        y = np.empty_like(x)
+        self._check(load().ls_pressure_apply(self.h, _p(x), _p(y)))
+        return y
+
+    def pressure_rhs(self):
+        b = np.empty(self.N)
+        self._check(load().ls_pressure_rhs(self.h, _p(b)))
+        return b
+
+    def transport_apply(self, dt, x):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1)
+        y = np.empty_like(x)
+        self._check(load().ls_transport_apply(self.h, float(dt), _p(x), _p(y)))
+        return y
+
+    # timing -----------------------------------------------------------------
+    def timing(self, enable=True):
+        self._check(load().ls_timing_enable(self.h, int(bool(enable))))
+
+    def timing_reset(self):
+        self._check(load().ls_timing_reset(self.h))
+
+    def timing_get(self, name):
+        ms = C.c_double(0.0)
+        cnt = C.c_longlong(0)
+        self._check(load().ls_timing_get(self.h, TIMERS[name], C.byref(ms), C.byref(cnt)))
+        return float(ms.value), int(cnt.value)
+
+    def timing_bytes(self, name):
+        b = C.c_double(0.0)
+        self._check(load().ls_timing_bytes(self.h, TIMERS[name], C.byref(b)))
+        return float(b.value)
+
+    def launches(self):
+        return int(load().ls_kernel_launches(self.h))
+
+    # time loop --------------------------------------------------------------
+    def run(self, tmax, dt, t0=0.0, n0=0, on_step=None, max_steps=None):
+        """Time loop of src/main.cpp:293-558 (retry manager, dt ramp; no files)."""
+        t, n = t0, n0
+        dt_target = dt
+        current_dt = min(60.0, dt_target) if n0 == 0 else dt_target
+        log = []
+        while True:
+            while True:
+                ok, info = self.step(t, current_dt)
+                if ok:
+                    break
+                self.rollback()
+                current_dt *= 0.5
+                if current_dt < 1e-3:
+                    raise RuntimeError("time step shrank below 1 ms")
+            info["t"], info["n"], info["dt"] = t, n, current_dt
+            log.append(info)
+            if on_step is not None:
+                on_step(n, t, self)
+            t += current_dt
+            n += 1
+            if current_dt < dt_target:
+                current_dt = min(current_dt * 1.5, dt_target)
+            if not (t < tmax) or (max_steps is not None and len(log) >= max_steps):
+                break
+        return log
