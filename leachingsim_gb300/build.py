@@ -18,6 +18,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libleachingsim_gb300.so")
+HOST = os.path.join(HERE, "host")
+CLI = os.path.join(HERE, "leachingsim")
+HOST_SOURCES = ["Simulation.cpp", "vtk_writer.cpp", "main.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["ls_api.cu", "ls_pointwise.cu", "ls_pressure.cu", "ls_mg.cu", "ls_transport.cu",
            "ls_dissolve.cu"]
@@ -40,6 +43,7 @@ def _flags(extra=()):
 
 def _deps():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    files += [os.path.join(HOST, f) for f in os.listdir(HOST)]
     files.append(os.path.join(ROOT, "include", "leachingsim.h"))
     files.append(os.path.abspath(__file__))
     return files
@@ -61,9 +65,23 @@ def _compile(src, extra=()):
     return obj, res.stderr
 
 
+def build_cli():
+    """The command-line driver (host C++ over the C-ABI), linked to the library in-tree."""
+    cxx = shutil.which("g++") or "g++"
+    srcs = [os.path.join(HOST, s) for s in HOST_SOURCES]
+    tmp = CLI + ".tmp"
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I" + os.path.join(ROOT, "include"), "-I" + HOST,
+           *srcs, "-o", tmp, "-L" + HERE, "-lleachingsim_gb300", "-Wl,-rpath,$ORIGIN"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"host build failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, CLI)
+    return CLI
+
+
 def build(force=False, verbose=False, extra=()):
     deps = _deps()
-    if not force and not _stale(LIB, deps):
+    if not force and not _stale(LIB, deps) and not _stale(CLI, deps):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     srcs = [os.path.join(CSRC, s) for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
@@ -80,6 +98,7 @@ def build(force=False, verbose=False, extra=()):
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, LIB)
+    build_cli()
     return LIB
 
 

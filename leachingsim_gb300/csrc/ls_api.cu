@@ -311,12 +311,19 @@ ls_status ls_destroy(ls_ctx* c) {
                     c->b_fz, c->pkind, c->pdiag, c->pb, c->pface[0], c->pface[1], c->pface[2],
                     c->pisd, c->pr, c->pdelta, c->w32[0], c->w32[1], c->w32[2], c->w64[0],
                     c->w64[1], c->w64[2], c->inner[0], c->inner[1], c->inner[2], c->inner[3],
-                    c->inner[4], c->comp, c->cc_flag, c->tdinv, c->s_old, c->dz_list,
+                    c->inner[4], c->comp, c->cc_flag, c->tkind, c->dz_list,
                     c->dz_count, c->dz_level_start, c->partials, c->scal, c->d_int};
     for (void* q : ptrs)
         if (q) cudaFree(q);
-    for (double* q : c->tv)
+    for (double* q : c->tc)
         if (q) cudaFree(q);
+    for (double* q : c->tb)
+        if (q) cudaFree(q);
+    for (float* q : c->to)
+        if (q) cudaFree(q);
+    for (auto& v : c->tf)
+        for (float* q : v)
+            if (q) cudaFree(q);
     for (auto& lv : c->mg) {
         void* lp[] = {lv.comp, lv.diag, lv.face[0], lv.face[1], lv.face[2], lv.x, lv.b, lv.t};
         for (void* q : lp)

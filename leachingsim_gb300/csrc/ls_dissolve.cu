@@ -18,6 +18,7 @@ namespace ls {
 
 struct DzConst {
     double D, dx, kreac, time_scalar, c_sat, dt_sub;
+    double k_eff;  // 1/((1/(D/dx)) + (1/kreac)), the same expression as per neighbour
 };
 
 template <typename L>
@@ -28,11 +29,7 @@ __device__ __forceinline__ double dz_surface_flux(const Grid& g, const DzConst& 
     // calc_surface_flux, src/Simulation.cpp:520-542
     if (valid) {
         int n_type = (int)label[nb];
-        if (n_type == kPore || n_type == kRock) {
-            double k_trans = dc.D / dc.dx;
-            double k_eff = 1.0 / ((1.0 / k_trans) + (1.0 / dc.kreac));
-            return k_eff * acid[nb];
-        }
+        if (n_type == kPore || n_type == kRock) return dc.k_eff * acid[nb];
     }
     return 0.0;
 }
@@ -167,6 +164,10 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
     dc.time_scalar = c->p.time_scalar;
     dc.c_sat = c->p.c_sat;
     dc.dt_sub = dt;
+    {
+        double k_trans = dc.D / dc.dx;
+        dc.k_eff = 1.0 / ((1.0 / k_trans) + (1.0 / dc.kreac));
+    }
     const L* label = (const L*)c->label;
     LS_CUDA(c, cudaMemsetAsync(c->d_int, 0, sizeof(int) * 4, c->stream));
     LS_LAUNCH(c, k_dz_rate<L>, grid, kBlock, 0, g, dc, label, (const double*)c->acid,

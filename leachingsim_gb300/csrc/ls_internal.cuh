@@ -101,10 +101,12 @@ struct ls_ctx {
     int* comp;            // fine-level strong-component ids (-1 = not an inner unknown)
     int* cc_flag;         // device flag for the labelling loop
 
-    // transport / implicit saturation Krylov vectors (2 right-hand sides)
-    double* tv[14];
-    double* tdinv;        // inverse diagonal of the transport rows
-    double* s_old;        // saturation before the implicit solve
+    // transport / implicit saturation (2 right-hand sides)
+    double* tc[7];        // FP64 row coefficients: diagonal, then +i,-i,+j,-j,+k,-k
+    double* tb[2];        // FP64 right-hand sides
+    float* to[6];         // FP32 off-diagonals scaled by the row diagonal
+    float* tf[2][8];      // FP32 inner vectors per right-hand side: rhs r rh p v s t d
+    int8_t* tkind;        // 1 identity row, 2 coupled row
 
     // dissolution
     int* dz_list;         // active mineral voxels sorted by wavefront

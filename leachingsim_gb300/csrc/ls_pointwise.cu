@@ -14,8 +14,11 @@
 namespace ls {
 
 struct PropsConst {
-    double m, s_res, vg_n, vg_alpha;
+    double m, s_res, vg_n, vg_alpha, inv_alpha;
     double log_k_rock, log_k_pore;
+    double k_clean_pore;     // pow(10, 0*log_k_rock + 1*log_k_pore), precipitate fraction 0
+    double k_clogged_pore;   // pow(10, 1*log_k_rock + 0*log_k_pore), precipitate fraction 1
+    int vg_n_is_2;           // m = 1/2: Se^(1/m) = Se*Se, (.)^m = sqrt, Se^(-1/m) = 1/(Se*Se)
 };
 
 template <typename L>
@@ -30,25 +33,28 @@ __global__ void __launch_bounds__(kBlock) k_props(Grid g, PropsConst pc, const L
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
         const int t = (int)label[r];
-        const double s = sat[r];
         double krv = 0.0, pcv = 0.0;
         if (t == kPore || t == kSulphide) {
+            const double s = sat[r];
             // relative permeability, src/Simulation.cpp:1643-1657
             double Se = (s - pc.s_res) / (1.0 - pc.s_res);
             double Sk = smax(0.0, smin(1.0, Se));
             if (Sk <= 0.0) {
                 krv = 0.0;
             } else {
-                double term1 = 1.0 - pow(1.0 - pow(Sk, 1.0 / pc.m), pc.m);
+                double term1 = pc.vg_n_is_2 ? 1.0 - sqrt(1.0 - Sk * Sk)
+                                            : 1.0 - pow(1.0 - pow(Sk, 1.0 / pc.m), pc.m);
                 krv = sqrt(Sk) * term1 * term1;
             }
             // capillary pressure, src/Simulation.cpp:1605-1621
             double Sc = smax(1e-6, smin(1.0, Se));
             if (Sc >= 1.0) {
                 pcv = 0.0;
+            } else if (pc.vg_n_is_2) {
+                pcv = pc.inv_alpha * sqrt(1.0 / (Sc * Sc) - 1.0);
             } else {
                 double Se_inv_m = pow(Sc, -1.0 / pc.m);
-                pcv = (1.0 / pc.vg_alpha) * pow(Se_inv_m - 1.0, 1.0 / pc.vg_n);
+                pcv = pc.inv_alpha * pow(Se_inv_m - 1.0, 1.0 / pc.vg_n);
             }
         }
         kr[r] = krv;
@@ -59,12 +65,14 @@ __global__ void __launch_bounds__(kBlock) k_props(Grid g, PropsConst pc, const L
             K_intrinsic = pore_permeability;
         } else if (t == kPore) {
             double p_frac = smax(0.0, smin(1.0, precip[r]));
-            double log_k_eff = (p_frac * pc.log_k_rock) + ((1.0 - p_frac) * pc.log_k_pore);
-            K_intrinsic = pow(10.0, log_k_eff);
+            if (p_frac == 0.0) K_intrinsic = pc.k_clean_pore;
+            else if (p_frac == 1.0) K_intrinsic = pc.k_clogged_pore;
+            else K_intrinsic = pow(10.0, (p_frac * pc.log_k_rock) + ((1.0 - p_frac) * pc.log_k_pore));
         } else if (t == kSulphide) {
             double f = (double)frac[r];
-            double log_k_eff = (f * pc.log_k_rock) + ((1.0 - f) * pc.log_k_pore);
-            K_intrinsic = pow(10.0, log_k_eff);
+            if (f == 1.0) K_intrinsic = pc.k_clogged_pore;
+            else if (f == 0.0) K_intrinsic = pc.k_clean_pore;
+            else K_intrinsic = pow(10.0, (f * pc.log_k_rock) + ((1.0 - f) * pc.log_k_pore));
         }
         visc[r] = (t == kAir) ? 1.8e-5 : 1.0e-3;
         perm[r] = K_intrinsic * smax(krv, 1e-15);
@@ -77,8 +85,12 @@ ls_status props_run(ls_ctx* c) {
     pc.s_res = c->p.s_res;
     pc.vg_n = c->p.vg_n;
     pc.vg_alpha = c->p.vg_alpha;
+    pc.inv_alpha = 1.0 / c->p.vg_alpha;
     pc.log_k_rock = std::log10(1.0e-18);
     pc.log_k_pore = std::log10(1.0e-12);
+    pc.k_clean_pore = std::pow(10.0, (0.0 * pc.log_k_rock) + ((1.0 - 0.0) * pc.log_k_pore));
+    pc.k_clogged_pore = std::pow(10.0, (1.0 * pc.log_k_rock) + ((1.0 - 1.0) * pc.log_k_pore));
+    pc.vg_n_is_2 = (c->p.vg_n == 2.0) ? 1 : 0;
     int grid = grid_for(c, c->g.N);
     if (c->label_bytes == 1)
         LS_LAUNCH(c, k_props<uint8_t>, grid, kBlock, 0, c->g, pc, (const uint8_t*)c->label, c->sat,
@@ -90,17 +102,37 @@ ls_status props_run(ls_ctx* c) {
     return LS_OK;
 }
 
+// Division by dx: when dx is a power of two, multiplying by its reciprocal gives the same
+// double as dividing (both are exact scalings), without an FP64 division.
+struct DxDiv {
+    double dx, inv_dx;
+    int pow2;
+    __device__ __forceinline__ double div(double a) const { return pow2 ? a * inv_dx : a / dx; }
+};
+
+static DxDiv make_dxdiv(double dx) {
+    DxDiv d;
+    d.dx = dx;
+    d.inv_dx = 1.0 / dx;
+    int e = 0;
+    double m = std::frexp(dx, &e);
+    d.pow2 = (m == 0.5) ? 1 : 0;
+    return d;
+}
+
 // ---------------------------------------------------------------------------
 // calculateFlux: central differences inside, one-sided on the domain faces (np=1).
 
 __device__ __forceinline__ double grad1(const double* __restrict__ f, long long r, long long off,
-                                        int pos, int ext, double dx) {
-    if (pos == 0) return (f[r + off] - f[r]) / dx;
-    if (pos == ext - 1) return (f[r] - f[r - off]) / dx;
-    return (f[r + off] - f[r - off]) / (2.0 * dx);
+                                        int pos, int ext, const DxDiv& dd) {
+    if (pos == 0) return dd.div(f[r + off] - f[r]);
+    if (pos == ext - 1) return dd.div(f[r] - f[r - off]);
+    // (a - b) / (2 dx): with dx a power of two this is (a - b) * (0.5 / dx) exactly
+    double d = f[r + off] - f[r - off];
+    return dd.pow2 ? d * (0.5 * dd.inv_dx) : d / (2.0 * dd.dx);
 }
 
-__global__ void __launch_bounds__(kBlock) k_flux(Grid g, double dx, double mcg,
+__global__ void __launch_bounds__(kBlock) k_flux(Grid g, DxDiv dd, double mcg,
                                                  const double* __restrict__ P,
                                                  const double* __restrict__ C,
                                                  const double* __restrict__ perm,
@@ -111,12 +143,12 @@ __global__ void __launch_bounds__(kBlock) k_flux(Grid g, double dx, double mcg,
          r += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         decode(g, r, i, j, k);
-        double gPx = grad1(P, r, g.JK, i, g.I, dx);
-        double gPy = grad1(P, r, g.K, j, g.J, dx);
-        double gPz = grad1(P, r, 1, k, g.K, dx);
-        double gCx = grad1(C, r, g.JK, i, g.I, dx);
-        double gCy = grad1(C, r, g.K, j, g.J, dx);
-        double gCz = grad1(C, r, 1, k, g.K, dx);
+        double gPx = grad1(P, r, g.JK, i, g.I, dd);
+        double gPy = grad1(P, r, g.K, j, g.J, dd);
+        double gPz = grad1(P, r, 1, k, g.K, dd);
+        double gCx = grad1(C, r, g.JK, i, g.I, dd);
+        double gCy = grad1(C, r, g.K, j, g.J, dd);
+        double gCz = grad1(C, r, 1, k, g.K, dd);
         gCx = smax(-mcg, smin(mcg, gCx));
         gCy = smax(-mcg, smin(mcg, gCy));
         gCz = smax(-mcg, smin(mcg, gCz));
@@ -130,8 +162,8 @@ __global__ void __launch_bounds__(kBlock) k_flux(Grid g, double dx, double mcg,
 
 ls_status flux_run(ls_ctx* c) {
     int grid = grid_for(c, c->g.N);
-    LS_LAUNCH(c, k_flux, grid, kBlock, 0, c->g, c->p.dx, c->p.max_cap_grad, c->P, c->pc, c->perm,
-              c->visc, c->fx, c->fy, c->fz);
+    LS_LAUNCH(c, k_flux, grid, kBlock, 0, c->g, make_dxdiv(c->p.dx), c->p.max_cap_grad, c->P, c->pc,
+              c->perm, c->visc, c->fx, c->fy, c->fz);
     return LS_OK;
 }
 
@@ -151,16 +183,17 @@ __device__ __forceinline__ void sat_rates(const Grid& g, const L* __restrict__ l
                                           const double* __restrict__ fx,
                                           const double* __restrict__ fy,
                                           const double* __restrict__ fz, long long r, int i,
-                                          int j, int k, int t, double dx, double evap,
+                                          int j, int k, int t, const DxDiv& dd, double evap,
                                           double& div_q, double& evap_sink) {
+    // (a + b) / 2.0 == (a + b) * 0.5 exactly
     const double fxr = fx[r], fyr = fy[r], fzr = fz[r];
-    double q_xp = (i + 1 < g.I) ? (fxr + fx[r + g.JK]) / 2.0 : 0.0;
-    double q_xm = (i > 0) ? (fxr + fx[r - g.JK]) / 2.0 : 0.0;
-    double q_yp = (j + 1 < g.J) ? (fyr + fy[r + g.K]) / 2.0 : 0.0;
-    double q_ym = (j > 0) ? (fyr + fy[r - g.K]) / 2.0 : 0.0;
-    double q_zp = (k + 1 < g.K) ? (fzr + fz[r + 1]) / 2.0 : 0.0;
-    double q_zm = (k > 0) ? (fzr + fz[r - 1]) / 2.0 : 0.0;
-    div_q = ((q_xp - q_xm) + (q_yp - q_ym) + (q_zp - q_zm)) / dx;
+    double q_xp = (i + 1 < g.I) ? (fxr + fx[r + g.JK]) * 0.5 : 0.0;
+    double q_xm = (i > 0) ? (fxr + fx[r - g.JK]) * 0.5 : 0.0;
+    double q_yp = (j + 1 < g.J) ? (fyr + fy[r + g.K]) * 0.5 : 0.0;
+    double q_ym = (j > 0) ? (fyr + fy[r - g.K]) * 0.5 : 0.0;
+    double q_zp = (k + 1 < g.K) ? (fzr + fz[r + 1]) * 0.5 : 0.0;
+    double q_zm = (k > 0) ? (fzr + fz[r - 1]) * 0.5 : 0.0;
+    div_q = dd.div((q_xp - q_xm) + (q_yp - q_ym) + (q_zp - q_zm));
     evap_sink = 0.0;
     if (t == kPore) {
         int air_faces = 0;
@@ -170,12 +203,12 @@ __device__ __forceinline__ void sat_rates(const Grid& g, const L* __restrict__ l
         if (j > 0 && (int)label[r - g.K] == kAir) air_faces++;
         if (k + 1 < g.K && (int)label[r + 1] == kAir) air_faces++;
         if (k > 0 && (int)label[r - 1] == kAir) air_faces++;
-        evap_sink = (air_faces * evap) / dx;
+        evap_sink = dd.div(air_faces * evap);
     }
 }
 
 template <typename L>
-__global__ void __launch_bounds__(kBlock) k_sat_rate(Grid g, double dx, double evap,
+__global__ void __launch_bounds__(kBlock) k_sat_rate(Grid g, DxDiv dd, double evap,
                                                      const L* __restrict__ label,
                                                      const double* __restrict__ fx,
                                                      const double* __restrict__ fy,
@@ -189,7 +222,7 @@ __global__ void __launch_bounds__(kBlock) k_sat_rate(Grid g, double dx, double e
         int i, j, k;
         decode(g, r, i, j, k);
         double div_q, evap_sink;
-        sat_rates(g, label, fx, fy, fz, r, i, j, k, t, dx, evap, div_q, evap_sink);
+        sat_rates(g, label, fx, fy, fz, r, i, j, k, t, dd, evap, div_q, evap_sink);
         double total_rate = fabs(div_q) + evap_sink;
         if (total_rate > v[0]) v[0] = total_rate;
     }
@@ -197,7 +230,7 @@ __global__ void __launch_bounds__(kBlock) k_sat_rate(Grid g, double dx, double e
 }
 
 template <typename L>
-__global__ void __launch_bounds__(kBlock) k_sat_update(Grid g, double dx, double evap,
+__global__ void __launch_bounds__(kBlock) k_sat_update(Grid g, DxDiv dd, double evap,
                                                        double dt_sub_over_phi, int num_steps,
                                                        const L* __restrict__ label,
                                                        const double* __restrict__ fx,
@@ -218,7 +251,7 @@ __global__ void __launch_bounds__(kBlock) k_sat_update(Grid g, double dx, double
         int i, j, k;
         decode(g, r, i, j, k);
         double div_q, evap_sink;
-        sat_rates(g, label, fx, fy, fz, r, i, j, k, t, dx, evap, div_q, evap_sink);
+        sat_rates(g, label, fx, fy, fz, r, i, j, k, t, dd, evap, div_q, evap_sink);
         double sv = sat[r];
         for (int step = 0; step < num_steps; ++step) {
             double new_sat = sv - dt_sub_over_phi * (div_q + evap_sink);
@@ -232,7 +265,8 @@ __global__ void __launch_bounds__(kBlock) k_sat_update(Grid g, double dx, double
 }
 
 ls_status saturation_run(ls_ctx* c, double dt, ls_substep_info* info) {
-    const double dx = c->p.dx, evap = c->p.evaporative_flux;
+    const DxDiv dx = make_dxdiv(c->p.dx);
+    const double evap = c->p.evaporative_flux;
     int grid = grid_for(c, c->g.N);
     if (c->label_bytes == 1)
         LS_LAUNCH(c, k_sat_rate<uint8_t>, grid, kBlock, 0, c->g, dx, evap, (const uint8_t*)c->label,

@@ -25,6 +25,11 @@
 
 namespace ls {
 
+template <typename T>
+ls_status mg_setup(ls_ctx* c, T* const* w);
+template <typename T>
+ls_status mg_apply(ls_ctx* c, const T* r, T* z, int* nblocks_out);
+
 // scalar slots
 enum {
     SP_NUM = 16,   // sum (r/diag)^2 over rows
@@ -60,25 +65,21 @@ __device__ __forceinline__ double link_coeff(const L* __restrict__ label,
     return K_avg / visc[self];
 }
 
+// Face coefficients of the +i, +j, +k faces (kernel 1 of 2). A face is used only by the
+// Pore rows on its two sides and gives the same value from either side (the harmonic mean
+// is symmetric bit for bit: (2a)b == (2b)a, a+b == b+a), so it is computed once.
 template <typename L>
-__global__ void __launch_bounds__(kBlock) k_press_setup(Grid g, PressConst pcst,
-                                                        const L* __restrict__ label,
+__global__ void __launch_bounds__(kBlock) k_press_faces(Grid g, const L* __restrict__ label,
                                                         const double* __restrict__ perm,
                                                         const double* __restrict__ visc,
-                                                        int8_t* __restrict__ kind,
-                                                        double* __restrict__ diag,
-                                                        double* __restrict__ b,
                                                         double* __restrict__ f0,
                                                         double* __restrict__ f1,
-                                                        double* __restrict__ f2,
-                                                        double* __restrict__ partials) {
-    double acc[1] = {0.0};  // sum (b/diag)^2
+                                                        double* __restrict__ f2) {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         decode(g, r, i, j, k);
         const int t = (int)label[r];
-        // + face coefficients (identical from either side: the harmonic mean is symmetric)
         double* faces[3] = {f0, f1, f2};
         const long long offs[3] = {g.JK, g.K, 1};
         const bool hasp[3] = {i + 1 < g.I, j + 1 < g.J, k + 1 < g.K};
@@ -93,6 +94,28 @@ __global__ void __launch_bounds__(kBlock) k_press_setup(Grid g, PressConst pcst,
             }
             faces[d][r] = cf;
         }
+    }
+}
+
+// Rows (kernel 2 of 2): kind, diagonal and right-hand side of src/Simulation.cpp:674-792.
+// The diagonal subtracts the six link coefficients in the reference's order
+// (+i, -i, +j, -j, +k, -k), read from the stored faces.
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_press_setup(Grid g, PressConst pcst,
+                                                        const L* __restrict__ label,
+                                                        int8_t* __restrict__ kind,
+                                                        double* __restrict__ diag,
+                                                        double* __restrict__ b,
+                                                        const double* __restrict__ f0,
+                                                        const double* __restrict__ f1,
+                                                        const double* __restrict__ f2,
+                                                        double* __restrict__ partials) {
+    double acc[1] = {0.0};  // sum (b/diag)^2
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        decode(g, r, i, j, k);
+        const int t = (int)label[r];
         int8_t kd = 0;
         double dg = 0.0, bv = 0.0;
         if (t == kAir || t == kRock || t == kSulphide || t == kPrecipitate) {
@@ -111,11 +134,14 @@ __global__ void __launch_bounds__(kBlock) k_press_setup(Grid g, PressConst pcst,
             double diagonal_term = 0.0, source_term = 0.0;
             const long long nbs[6] = {r + g.JK, r - g.JK, r + g.K, r - g.K, r + 1, r - 1};
             const bool val[6] = {i + 1 < g.I, i > 0, j + 1 < g.J, j > 0, k + 1 < g.K, k > 0};
+            const double cf[6] = {val[0] ? f0[r] : 0.0, val[1] ? f0[r - g.JK] : 0.0,
+                                  val[2] ? f1[r] : 0.0, val[3] ? f1[r - g.K] : 0.0,
+                                  val[4] ? f2[r] : 0.0, val[5] ? f2[r - 1] : 0.0};
 #pragma unroll
             for (int d = 0; d < 6; ++d) {
                 if (!val[d]) continue;
                 if ((int)label[nbs[d]] == kAir) source_term -= pcst.evap_dx;
-                diagonal_term -= link_coeff(label, perm, visc, r, nbs[d]);
+                diagonal_term -= cf[d];
             }
             kd = 2;
             if (fabs(diagonal_term) < 1e-16) {
@@ -128,8 +154,7 @@ __global__ void __launch_bounds__(kBlock) k_press_setup(Grid g, PressConst pcst,
         kind[r] = kd;
         diag[r] = dg;
         b[r] = bv;
-        double di = (dg != 0.0) ? 1.0 / dg : 1.0;
-        double sb = di * bv;
+        double sb = (dg != 0.0) ? bv / dg : bv;
         acc[0] += sb * sb;
     }
     block_sum_store<1>(acc, partials);
@@ -211,6 +236,7 @@ __global__ void k_press_apply_full(Grid g, const int8_t* __restrict__ kind,
 // and the max / -min of x.
 __global__ void __launch_bounds__(kBlock) k_press_residual(Grid g, const int8_t* __restrict__ kind,
                                                            const double* __restrict__ diag,
+                                                           const double* __restrict__ isd,
                                                            const double* __restrict__ b,
                                                            const double* __restrict__ f0,
                                                            const double* __restrict__ f1,
@@ -235,8 +261,9 @@ __global__ void __launch_bounds__(kBlock) k_press_residual(Grid g, const int8_t*
             decode(g, r, i, j, k);
             double dg = diag[r];
             rv = b[r] - press_row_apply(g, r, i, j, k, dg, x, f0, f1, f2);
-            double s = rv / dg;
-            acc[0] += s * s;
+            // (r / diag)^2 without an FP64 division: 1/diag^2 = isd^4 for normal rows
+            double id2 = (kd == 2) ? isd[r] * isd[r] : 1e16;  // floored rows: diag = 1e-16
+            acc[0] += rv * rv * (id2 * id2);
             if (rv != rv) acc[1] += 1.0;
         }
         res[r] = rv;
@@ -315,15 +342,16 @@ __global__ void __launch_bounds__(kBlock) k_cg_apply(Grid g, const T* __restrict
                                                      const T* __restrict__ w1,
                                                      const T* __restrict__ w2, T* __restrict__ q,
                                                      double* __restrict__ partials) {
-    double acc[1] = {0.0};
+    T a = (T)0;  // per-thread partial in the inner precision
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         decode(g, r, i, j, k);
         T qv = inner_apply_row(g, r, i, j, k, p, w0, w1, w2);
         q[r] = qv;
-        acc[0] += (double)p[r] * (double)qv;
+        a += p[r] * qv;
     }
+    double acc[1] = {(double)a};
     block_sum_store<1>(acc, partials);
 }
 
@@ -335,14 +363,15 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(Grid g, const double* __re
                                                       T* __restrict__ r_, double* __restrict__ partials) {
     const double alpha = scal[SP_RZ] / scal[SP_PQ];
     const T a = (T)alpha;
-    double acc[1] = {0.0};
+    T s = (T)0;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
         x[r] += a * p[r];
         T rv = r_[r] - a * q[r];
         r_[r] = rv;
-        acc[0] += (double)rv * (double)rv;
+        s += rv * rv;
     }
+    double acc[1] = {(double)s};
     block_sum_store<1>(acc, partials);
 }
 
@@ -373,6 +402,15 @@ __global__ void k_copy_dot(Grid g, const T* __restrict__ a, T* __restrict__ b, T
 __global__ void k_set_scalar(double* scal, int dst, int src) { scal[dst] = scal[src]; }
 
 template <typename T>
+__global__ void k_copy_zero(Grid g, const T* __restrict__ a, T* __restrict__ b, T* __restrict__ z) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        b[r] = a[r];
+        z[r] = (T)0;
+    }
+}
+
+template <typename T>
 static ls_status inner_alloc(ls_ctx* c) {
     const bool is64 = sizeof(T) == 8;
     if (c->inner[0] && c->inner_is64 == (int)is64) return LS_OK;
@@ -385,10 +423,11 @@ static ls_status inner_alloc(ls_ctx* c) {
     return LS_OK;
 }
 
-// Inner PCG: solve W x = rhs (rhs held in inner[1] on entry) to relative residual tol.
+// Inner PCG: solve W x = rhs (rhs held in inner[1] on entry) to relative residual tol,
+// preconditioned by one multigrid V-cycle (use_mg) or by the unit diagonal.
 // Returns the iterations used in *its.
 template <typename T>
-static ls_status inner_pcg(ls_ctx* c, T* const* w, double tol, int max_it, int* its,
+static ls_status inner_pcg(ls_ctx* c, T* const* w, bool use_mg, double tol, int max_it, int* its,
                            double* rel_out) {
     T* x = (T*)c->inner[0];
     T* r = (T*)c->inner[1];
@@ -397,17 +436,25 @@ static ls_status inner_pcg(ls_ctx* c, T* const* w, double tol, int max_it, int* 
     T* q = (T*)c->inner[4];
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
-    (void)z;
-    // x = 0, p = r, rz = (r, r)
+    // (r, r) for the stopping test, x = 0
     LS_LAUNCH(c, k_copy_dot<T>, grid, kBlock, 0, g, (const T*)r, p, x, c->partials);
-    LS_TRY(finalize_sum(c, grid, 1, SP_RZ));
+    LS_TRY(finalize_sum(c, grid, 1, SP_RR0));
     double rr0 = 0.0;
-    LS_TRY(read_scalars(c, SP_RZ, 1, &rr0));
+    LS_TRY(read_scalars(c, SP_RR0, 1, &rr0));
     *its = 0;
     *rel_out = 0.0;
     if (!(rr0 > 0.0)) {
         if (rr0 != rr0) return set_error(c, LS_NONFINITE, "pressure: NaN in inner right-hand side");
         return LS_OK;
+    }
+    if (use_mg) {
+        // z = B r, p = z, rz = (r, z)
+        int nb = 0;
+        LS_TRY(mg_apply<T>(c, (const T*)r, z, &nb));
+        LS_TRY(finalize_sum(c, nb, 1, SP_RZ));
+        LS_LAUNCH(c, k_copy_zero<T>, grid, kBlock, 0, g, (const T*)z, p, x);
+    } else {
+        LS_LAUNCH(c, k_set_scalar, 1, 1, 0, c->scal, SP_RZ, SP_RR0);
     }
     const double target = tol * tol * rr0;
     double rr = rr0;
@@ -422,12 +469,20 @@ static ls_status inner_pcg(ls_ctx* c, T* const* w, double tol, int max_it, int* 
         LS_TRY(finalize_sum(c, grid, 1, SP_PQ));
         LS_LAUNCH(c, k_cg_update<T>, grid, kBlock, 0, g, (const double*)c->scal, (const T*)p,
                   (const T*)q, x, r, c->partials);
-        LS_TRY(finalize_sum(c, grid, 1, SP_RZN));
+        LS_TRY(finalize_sum(c, grid, 1, SP_RR));
         *its = it + 1;
-        LS_TRY(read_scalars(c, SP_RZN, 1, &rr));
+        LS_TRY(read_scalars(c, SP_RR, 1, &rr));
         if (rr != rr) return set_error(c, LS_NONFINITE, "pressure: NaN in inner PCG");
         if (rr <= target) break;
-        LS_LAUNCH(c, k_cg_dir<T>, grid, kBlock, 0, g, (const double*)c->scal, (const T*)r, p);
+        if (use_mg) {
+            int nb = 0;
+            LS_TRY(mg_apply<T>(c, (const T*)r, z, &nb));
+            LS_TRY(finalize_sum(c, nb, 1, SP_RZN));
+            LS_LAUNCH(c, k_cg_dir<T>, grid, kBlock, 0, g, (const double*)c->scal, (const T*)z, p);
+        } else {
+            LS_LAUNCH(c, k_set_scalar, 1, 1, 0, c->scal, SP_RZN, SP_RR);
+            LS_LAUNCH(c, k_cg_dir<T>, grid, kBlock, 0, g, (const double*)c->scal, (const T*)r, p);
+        }
         LS_LAUNCH(c, k_set_scalar, 1, 1, 0, c->scal, SP_RZ, SP_RZN);
     }
     *rel_out = sqrt(rr / rr0);
@@ -446,14 +501,17 @@ ls_status pressure_setup_run(ls_ctx* c, double t) {
     pcst.evap_dx = c->p.evaporative_flux * c->p.dx;
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
-    if (c->label_bytes == 1)
+    if (c->label_bytes == 1) {
+        LS_LAUNCH(c, k_press_faces<uint8_t>, grid, kBlock, 0, g, (const uint8_t*)c->label, c->perm,
+                  c->visc, c->pface[0], c->pface[1], c->pface[2]);
         LS_LAUNCH(c, k_press_setup<uint8_t>, grid, kBlock, 0, g, pcst, (const uint8_t*)c->label,
-                  c->perm, c->visc, c->pkind, c->pdiag, c->pb, c->pface[0], c->pface[1], c->pface[2],
-                  c->partials);
-    else
+                  c->pkind, c->pdiag, c->pb, c->pface[0], c->pface[1], c->pface[2], c->partials);
+    } else {
+        LS_LAUNCH(c, k_press_faces<uint16_t>, grid, kBlock, 0, g, (const uint16_t*)c->label, c->perm,
+                  c->visc, c->pface[0], c->pface[1], c->pface[2]);
         LS_LAUNCH(c, k_press_setup<uint16_t>, grid, kBlock, 0, g, pcst, (const uint16_t*)c->label,
-                  c->perm, c->visc, c->pkind, c->pdiag, c->pb, c->pface[0], c->pface[1], c->pface[2],
-                  c->partials);
+                  c->pkind, c->pdiag, c->pb, c->pface[0], c->pface[1], c->pface[2], c->partials);
+    }
     LS_TRY(finalize_sum(c, grid, 1, SP_DEN));
     LS_LAUNCH(c, k_press_isd, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const double*)c->pdiag,
               c->pisd);
@@ -502,6 +560,11 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info) {
         LS_LAUNCH(c, k_press_init_x, grid, kBlock, 0, g, (const int8_t*)c->pkind,
                   (const double*)c->pb, x);
     }
+    const bool use_mg = c->p.press_solver != LS_PRESS_JACOBI64;
+    if (use_mg) {
+        Timed tm(c, LS_T_PRESS_SETUP);
+        LS_TRY(mg_setup<T>(c, w));
+    }
     double den = 0.0;
     LS_TRY(read_scalars(c, SP_DEN, 1, &den));
     const double rtol = c->p.press_rtol;
@@ -520,7 +583,7 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info) {
         {
             Timed tm(c, LS_T_PRESS_OUTER);
             LS_LAUNCH(c, k_press_residual, grid, kBlock, 0, g, (const int8_t*)c->pkind,
-                      (const double*)c->pdiag, (const double*)c->pb, (const double*)c->pface[0],
+                      (const double*)c->pdiag, (const double*)c->pisd, (const double*)c->pb, (const double*)c->pface[0],
                       (const double*)c->pface[1], (const double*)c->pface[2], (const double*)x,
                       c->pr, c->partials, pmax, grid);
             LS_TRY(finalize_sum(c, grid, 2, SP_NUM));
@@ -551,7 +614,8 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info) {
                       (const double*)c->pface[2], c->pdelta, (T*)c->inner[1]);
             double tol = std::max(inner_floor, 0.2 * rtol / std::max(rel, 1e-300));
             tol = std::min(tol, 0.5);
-            ls_status st = inner_pcg<T>(c, w, tol, c->p.press_max_it - total_inner, &its, &irel);
+            ls_status st = inner_pcg<T>(c, w, use_mg, tol, c->p.press_max_it - total_inner, &its,
+                                        &irel);
             if (st != LS_OK) { result = st; break; }
             LS_LAUNCH(c, k_press_accumulate<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind,
                       (const double*)c->pisd, (const double*)c->pdelta, (const T*)c->inner[0], x);

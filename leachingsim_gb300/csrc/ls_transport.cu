@@ -12,8 +12,14 @@
 //     faces (zero next to Precipitate/Sulphide); explicit (1-theta) part on the RHS.
 //   Links to neighbours outside the domain are skipped.
 // conc and acid share the matrix (labels and flux are the same for both solves) and are
-// solved together by one two-right-hand-side BiCGStab on the Jacobi-scaled system; the
-// convergence test ||D^-1 r|| / ||D^-1 b|| is the one PETSc applies to left-Jacobi GMRES.
+// solved together, two right-hand sides per pass.
+//
+// Solver (GB300 has little FP64 throughput, so FP64 divisions and FP64 Krylov sweeps are
+// kept out of the iteration): the FP64 row coefficients and right-hand sides are computed
+// once per solve, exactly as the reference assembles them; an FP64 refinement loop forms
+// the true residual r = b - A x and its Jacobi-scaled norm ||D^-1 r|| / ||D^-1 b|| (the
+// test PETSc applies to left-Jacobi GMRES); each correction comes from an FP32 BiCGStab on
+// the unit-diagonal system (D^-1 A) d = D^-1 r with FP32 scaled off-diagonals.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -168,66 +174,30 @@ __device__ __forceinline__ int sat_row(const Grid& g, const SatConst& sc,
     return 2;
 }
 
-// Operator descriptor handed to the Krylov kernels.
+
+// ---------------------------------------------------------------------------
+// setup: FP64 coefficients, right-hand sides, FP32 scaled off-diagonals
+
 template <typename L>
-struct Op {
+struct Rows {
     int mode;  // 0 transport, 1 implicit saturation
     Grid g;
     TransConst tc;
     SatConst sc;
     const L* label;
     const double *fx, *fy, *fz, *s;
-
-    __device__ __forceinline__ int row(long long r, int i, int j, int k, double& diag,
-                                       double off[6]) const {
-        if (mode == 0)
-            return trans_row(g, tc, label, fx, fy, fz, r, i, j, k, diag, off, nullptr, nullptr,
-                             nullptr);
-        return sat_row(g, sc, label, fx, fy, fz, s, r, i, j, k, diag, off, nullptr);
-    }
 };
 
-// y_q = D^-1 A x_q (or A x_q when unscaled) for nrhs vectors; summed in ascending column
-// order.
-template <typename L>
-__device__ __forceinline__ void op_apply_row(const Op<L>& op, long long r, int i, int j, int k,
-                                             const double* const* x, double* yv, int nrhs,
-                                             bool unscaled = false, int mask = 3) {
-    double dg, off[6];
-    op.row(r, i, j, k, dg, off);
-    const Grid& g = op.g;
-    for (int q = 0; q < nrhs; ++q) {
-        if (!((mask >> q) & 1)) continue;
-        const double* xv = x[q];
-        double acc = 0.0;
-        if (i > 0) acc += off[1] * xv[r - g.JK];
-        if (j > 0) acc += off[3] * xv[r - g.K];
-        if (k > 0) acc += off[5] * xv[r - 1];
-        acc += dg * xv[r];
-        if (k + 1 < g.K) acc += off[4] * xv[r + 1];
-        if (j + 1 < g.J) acc += off[2] * xv[r + g.K];
-        if (i + 1 < g.I) acc += off[0] * xv[r + g.JK];
-        yv[q] = unscaled ? acc : acc / dg;
-    }
-}
-
-struct KVec {
+struct TBuf {
+    double* c[7];
     double* b[2];
-    double* x[2];
-    double* r[2];
-    double* rh[2];
-    double* p[2];
-    double* v[2];
-    double* s[2];
-    double* t[2];
+    float* o[6];
+    int8_t* kind;
 };
 
-// setup: scaled right-hand sides b~ = D^-1 b and their squared norms. Reads the fields
-// only; x is written by k_kry_xid afterwards (with compat_shift x aliases field slots).
 template <typename L>
-__global__ void __launch_bounds__(kBlock) k_kry_setup(Op<L> op, KVec kv, int nrhs,
-                                                      const double* f0, const double* f1,
-                                                      double* __restrict__ partials) {
+__global__ void __launch_bounds__(kBlock) k_t_setup(Rows<L> op, TBuf tb, int nrhs, const double* f0,
+                                                    const double* f1, double* __restrict__ partials) {
     double acc[2] = {0.0, 0.0};
     const Grid& g = op.g;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
@@ -235,174 +205,211 @@ __global__ void __launch_bounds__(kBlock) k_kry_setup(Op<L> op, KVec kv, int nrh
         int i, j, k;
         decode(g, r, i, j, k);
         double dg, off[6], rhs[2] = {0.0, 0.0};
+        int kind;
         if (op.mode == 0)
-            trans_row(g, op.tc, op.label, op.fx, op.fy, op.fz, r, i, j, k, dg, off, f0, f1, rhs);
+            kind = trans_row(g, op.tc, op.label, op.fx, op.fy, op.fz, r, i, j, k, dg, off, f0, f1, rhs);
         else
-            sat_row(g, op.sc, op.label, op.fx, op.fy, op.fz, op.s, r, i, j, k, dg, off, rhs);
+            kind = sat_row(g, op.sc, op.label, op.fx, op.fy, op.fz, op.s, r, i, j, k, dg, off, rhs);
+        tb.c[0][r] = dg;
+#pragma unroll
+        for (int d = 0; d < 6; ++d) {
+            tb.c[1 + d][r] = off[d];
+            tb.o[d][r] = (float)(off[d] / dg);
+        }
+        tb.kind[r] = (int8_t)kind;
         for (int q = 0; q < nrhs; ++q) {
+            tb.b[q][r] = rhs[q];
             double bt = rhs[q] / dg;
-            kv.b[q][r] = bt;
             acc[q] += bt * bt;
         }
     }
     block_sum_store<2>(acc, partials);
 }
 
-// identity rows take their value: x = b~ (Precipitate for transport, inactive labels for
-// the implicit saturation)
-template <typename L>
-__global__ void k_kry_xid(Op<L> op, KVec kv, int nrhs) {
-    const Grid& g = op.g;
+// identity rows take their value
+__global__ void k_t_xid(Grid g, TBuf tb, double* x0, double* x1, int nrhs) {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
-        int t = (int)op.label[r];
-        bool ident = (op.mode == 0) ? (t == kPrecipitate)
-                                    : (t == kAir || t == kRock || t == kSulphide || t == kPrecipitate);
-        if (ident)
-            for (int q = 0; q < nrhs; ++q) kv.x[q][r] = kv.b[q][r];
+        if (tb.kind[r] != 1) continue;
+        x0[r] = tb.b[0][r];
+        if (nrhs > 1) x1[r] = tb.b[1][r];
     }
 }
 
-// zero the flux of Rock and Precipitate voxels (src/Simulation.cpp:1134-1149), after the
-// solve; no transport row uses the flux of such a voxel
-template <typename L>
-__global__ void k_zero_solid_flux(Grid g, const L* __restrict__ label, double* __restrict__ fx,
-                                  double* __restrict__ fy, double* __restrict__ fz) {
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x) {
-        int t = (int)label[r];
-        if (t == kRock || t == kPrecipitate) { fx[r] = 0.0; fy[r] = 0.0; fz[r] = 0.0; }
-    }
+// FP64 A x with the stored coefficients, ascending column order
+__device__ __forceinline__ double t_row_apply(const Grid& g, const TBuf& tb, long long r, int i, int j,
+                                              int k, const double* __restrict__ x) {
+    double acc = 0.0;
+    if (i > 0) acc = __fma_rn(tb.c[2][r], x[r - g.JK], acc);
+    if (j > 0) acc = __fma_rn(tb.c[4][r], x[r - g.K], acc);
+    if (k > 0) acc = __fma_rn(tb.c[6][r], x[r - 1], acc);
+    acc = __fma_rn(tb.c[0][r], x[r], acc);
+    if (k + 1 < g.K) acc = __fma_rn(tb.c[5][r], x[r + 1], acc);
+    if (j + 1 < g.J) acc = __fma_rn(tb.c[3][r], x[r + g.K], acc);
+    if (i + 1 < g.I) acc = __fma_rn(tb.c[1][r], x[r + g.JK], acc);
+    return acc;
 }
 
-// r = b~ - A~ x, rhat = r, p = v = 0; partial (r, r)
-template <typename L>
-__global__ void __launch_bounds__(kBlock) k_kry_init(Op<L> op, KVec kv, int nrhs,
-                                                     double* __restrict__ partials) {
-    double acc[2] = {0.0, 0.0};
-    const Grid& g = op.g;
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x) {
-        int i, j, k;
-        decode(g, r, i, j, k);
-        double y[2];
-        const double* xs[2] = {kv.x[0], kv.x[1]};
-        op_apply_row(op, r, i, j, k, xs, y, nrhs);
-        for (int q = 0; q < nrhs; ++q) {
-            double rv = kv.b[q][r] - y[q];
-            kv.r[q][r] = rv;
-            kv.rh[q][r] = rv;
-            kv.p[q][r] = 0.0;
-            kv.v[q][r] = 0.0;
-            acc[q] += rv * rv;
-        }
-    }
-    block_sum_store<2>(acc, partials);
-}
-
-// p = r + beta (p - omega v), beta = (rho/rho_old)(alpha/omega)
-__global__ void k_kry_p(Grid g, KVec kv, int nrhs, int mask, const double* __restrict__ scal) {
-    double beta[2], omega[2];
-    bool act[2];
-    for (int q = 0; q < nrhs; ++q) {
-        act[q] = (mask >> q) & 1;
-        omega[q] = scal[sslot(q, ST_OMEGA)];
-        beta[q] = (scal[sslot(q, ST_RHO)] / scal[sslot(q, ST_RHO_OLD)]) *
-                  (scal[sslot(q, ST_ALPHA)] / omega[q]);
-    }
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x)
-        for (int q = 0; q < nrhs; ++q)
-            if (act[q]) kv.p[q][r] = kv.r[q][r] + beta[q] * (kv.p[q][r] - omega[q] * kv.v[q][r]);
-}
-
-// v = A~ p; partial (rhat, v)
-template <typename L>
-__global__ void __launch_bounds__(kBlock) k_kry_v(Op<L> op, KVec kv, int nrhs, int mask,
-                                                  double* __restrict__ partials) {
-    double acc[2] = {0.0, 0.0};
-    const Grid& g = op.g;
-    bool act[2] = {(mask & 1) != 0, (mask & 2) != 0};
-    const double* ps[2] = {kv.p[0], kv.p[1]};
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x) {
-        int i, j, k;
-        decode(g, r, i, j, k);
-        double y[2];
-        op_apply_row(op, r, i, j, k, ps, y, nrhs, false, mask);
-        for (int q = 0; q < nrhs; ++q) {
-            if (!act[q]) continue;
-            kv.v[q][r] = y[q];
-            acc[q] += kv.rh[q][r] * y[q];
-        }
-    }
-    block_sum_store<2>(acc, partials);
-}
-
-// s = r - alpha v (alpha = rho / (rhat, v)), written by this kernel for its own rows.
-__global__ void k_kry_s(Grid g, KVec kv, int nrhs, int mask, const double* __restrict__ scal) {
-    double alpha[2];
-    bool act[2];
-    for (int q = 0; q < nrhs; ++q) {
-        act[q] = (mask >> q) & 1;
-        alpha[q] = scal[sslot(q, ST_RHO)] / scal[sslot(q, ST_RV)];
-    }
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x)
-        for (int q = 0; q < nrhs; ++q)
-            if (act[q]) kv.s[q][r] = kv.r[q][r] - alpha[q] * kv.v[q][r];
-}
-
-// t = A~ s; partials (t, s), (t, t)
-template <typename L>
-__global__ void __launch_bounds__(kBlock) k_kry_t(Op<L> op, KVec kv, int nrhs, int mask,
-                                                  double* __restrict__ partials) {
+// outer residual: rhs32 = D^-1 (b - A x) in FP32; partials sum (D^-1 r)^2 and NaN count
+__global__ void __launch_bounds__(kBlock) k_t_resid(Grid g, TBuf tb, double* x0, double* x1,
+                                                    float* r0, float* r1, int mask,
+                                                    double* __restrict__ partials) {
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    const Grid& g = op.g;
-    bool act[2] = {(mask & 1) != 0, (mask & 2) != 0};
-    const double* ss[2] = {kv.s[0], kv.s[1]};
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         decode(g, r, i, j, k);
-        double y[2];
-        op_apply_row(op, r, i, j, k, ss, y, nrhs, false, mask);
-        for (int q = 0; q < nrhs; ++q) {
-            if (!act[q]) continue;
-            kv.t[q][r] = y[q];
-            acc[2 * q] += y[q] * kv.s[q][r];
-            acc[2 * q + 1] += y[q] * y[q];
+        const double dg = tb.c[0][r];
+        if (mask & 1) {
+            double rv = (tb.b[0][r] - t_row_apply(g, tb, r, i, j, k, x0)) / dg;
+            r0[r] = (float)rv;
+            acc[0] += rv * rv;
+            if (rv != rv) acc[2] += 1.0;
+        }
+        if (mask & 2) {
+            double rv = (tb.b[1][r] - t_row_apply(g, tb, r, i, j, k, x1)) / dg;
+            r1[r] = (float)rv;
+            acc[1] += rv * rv;
+            if (rv != rv) acc[3] += 1.0;
         }
     }
     block_sum_store<4>(acc, partials);
 }
 
-// x += alpha p + omega s; r = s - omega t; partials (rhat, r), (r, r)
-__global__ void __launch_bounds__(kBlock) k_kry_x(Grid g, KVec kv, int nrhs, int mask,
-                                                  const double* __restrict__ scal,
-                                                  double* __restrict__ partials) {
-    double alpha[2], omega[2];
-    bool act[2] = {false, false};
-    for (int q = 0; q < nrhs; ++q) {
-        act[q] = (mask >> q) & 1;
-        alpha[q] = scal[sslot(q, ST_RHO)] / scal[sslot(q, ST_RV)];
+// ---------------------------------------------------------------------------
+// inner FP32 BiCGStab on A^ = I + O (O: scaled off-diagonals), per right-hand side q:
+// vectors tf[q] = {rhs, r, rh, p, v, s, t, d}
+
+struct IVec {
+    float* v[2][8];
+};
+enum { IV_RHS = 0, IV_R, IV_RH, IV_P, IV_V, IV_S, IV_T, IV_D };
+
+__device__ __forceinline__ float i_apply(const Grid& g, const TBuf& tb, long long r, int i, int j,
+                                         int k, const float* __restrict__ v) {
+    float acc = v[r];
+    if (i > 0) acc = __fmaf_rn(tb.o[1][r], v[r - g.JK], acc);
+    if (j > 0) acc = __fmaf_rn(tb.o[3][r], v[r - g.K], acc);
+    if (k > 0) acc = __fmaf_rn(tb.o[5][r], v[r - 1], acc);
+    if (k + 1 < g.K) acc = __fmaf_rn(tb.o[4][r], v[r + 1], acc);
+    if (j + 1 < g.J) acc = __fmaf_rn(tb.o[2][r], v[r + g.K], acc);
+    if (i + 1 < g.I) acc = __fmaf_rn(tb.o[0][r], v[r + g.JK], acc);
+    return acc;
+}
+
+// start: r = rh = rhs, p = v = d = 0; partial (r, r)
+__global__ void __launch_bounds__(kBlock) k_i_init(Grid g, IVec iv, int mask, double* __restrict__ partials) {
+    float acc[2] = {0.f, 0.f};
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        for (int q = 0; q < 2; ++q) {
+            if (!((mask >> q) & 1)) continue;
+            float rv = iv.v[q][IV_RHS][r];
+            iv.v[q][IV_R][r] = rv;
+            iv.v[q][IV_RH][r] = rv;
+            iv.v[q][IV_P][r] = 0.f;
+            iv.v[q][IV_V][r] = 0.f;
+            iv.v[q][IV_D][r] = 0.f;
+            acc[q] = __fmaf_rn(rv, rv, acc[q]);
+        }
+    }
+    double a[2] = {acc[0], acc[1]};
+    block_sum_store<2>(a, partials);
+}
+
+// p = r + beta (p - omega v)
+__global__ void k_i_p(Grid g, IVec iv, int mask, const double* __restrict__ scal) {
+    float beta[2] = {0.f, 0.f}, omega[2] = {0.f, 0.f};
+    for (int q = 0; q < 2; ++q) {
+        if (!((mask >> q) & 1)) continue;
+        double om = scal[sslot(q, ST_OMEGA)];
+        omega[q] = (float)om;
+        beta[q] = (float)((scal[sslot(q, ST_RHO)] / scal[sslot(q, ST_RHO_OLD)]) * (scal[sslot(q, ST_ALPHA)] / om));
+    }
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x)
+        for (int q = 0; q < 2; ++q)
+            if ((mask >> q) & 1)
+                iv.v[q][IV_P][r] = __fmaf_rn(beta[q], __fmaf_rn(-omega[q], iv.v[q][IV_V][r], iv.v[q][IV_P][r]),
+                                             iv.v[q][IV_R][r]);
+}
+
+// v = A^ p; partial (rh, v)
+__global__ void __launch_bounds__(kBlock) k_i_v(Grid g, TBuf tb, IVec iv, int mask,
+                                                double* __restrict__ partials) {
+    float acc[2] = {0.f, 0.f};
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        decode(g, r, i, j, k);
+        for (int q = 0; q < 2; ++q) {
+            if (!((mask >> q) & 1)) continue;
+            float y = i_apply(g, tb, r, i, j, k, iv.v[q][IV_P]);
+            iv.v[q][IV_V][r] = y;
+            acc[q] = __fmaf_rn(iv.v[q][IV_RH][r], y, acc[q]);
+        }
+    }
+    double a[2] = {acc[0], acc[1]};
+    block_sum_store<2>(a, partials);
+}
+
+// s = r - alpha v
+__global__ void k_i_s(Grid g, IVec iv, int mask, const double* __restrict__ scal) {
+    float alpha[2] = {0.f, 0.f};
+    for (int q = 0; q < 2; ++q)
+        if ((mask >> q) & 1) alpha[q] = (float)(scal[sslot(q, ST_RHO)] / scal[sslot(q, ST_RV)]);
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x)
+        for (int q = 0; q < 2; ++q)
+            if ((mask >> q) & 1)
+                iv.v[q][IV_S][r] = __fmaf_rn(-alpha[q], iv.v[q][IV_V][r], iv.v[q][IV_R][r]);
+}
+
+// t = A^ s; partials (t, s), (t, t)
+__global__ void __launch_bounds__(kBlock) k_i_t(Grid g, TBuf tb, IVec iv, int mask,
+                                                double* __restrict__ partials) {
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        decode(g, r, i, j, k);
+        for (int q = 0; q < 2; ++q) {
+            if (!((mask >> q) & 1)) continue;
+            float y = i_apply(g, tb, r, i, j, k, iv.v[q][IV_S]);
+            iv.v[q][IV_T][r] = y;
+            acc[2 * q] = __fmaf_rn(y, iv.v[q][IV_S][r], acc[2 * q]);
+            acc[2 * q + 1] = __fmaf_rn(y, y, acc[2 * q + 1]);
+        }
+    }
+    double a[4] = {acc[0], acc[1], acc[2], acc[3]};
+    block_sum_store<4>(a, partials);
+}
+
+// d += alpha p + omega s; r = s - omega t; partials (rh, r), (r, r)
+__global__ void __launch_bounds__(kBlock) k_i_x(Grid g, IVec iv, int mask, const double* __restrict__ scal,
+                                                double* __restrict__ partials) {
+    float alpha[2] = {0.f, 0.f}, omega[2] = {0.f, 0.f};
+    for (int q = 0; q < 2; ++q) {
+        if (!((mask >> q) & 1)) continue;
+        alpha[q] = (float)(scal[sslot(q, ST_RHO)] / scal[sslot(q, ST_RV)]);
         double tt = scal[sslot(q, ST_TT)];
-        omega[q] = (tt > 0.0) ? scal[sslot(q, ST_TS)] / tt : 0.0;
+        omega[q] = (float)((tt > 0.0) ? scal[sslot(q, ST_TS)] / tt : 0.0);
     }
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
-        for (int q = 0; q < nrhs; ++q) {
-            if (!act[q]) continue;
-            double sv = kv.s[q][r];
-            kv.x[q][r] += alpha[q] * kv.p[q][r] + omega[q] * sv;
-            double rv = sv - omega[q] * kv.t[q][r];
-            kv.r[q][r] = rv;
-            acc[2 * q] += kv.rh[q][r] * rv;
-            acc[2 * q + 1] += rv * rv;
+        for (int q = 0; q < 2; ++q) {
+            if (!((mask >> q) & 1)) continue;
+            float sv = iv.v[q][IV_S][r];
+            iv.v[q][IV_D][r] = __fmaf_rn(alpha[q], iv.v[q][IV_P][r], __fmaf_rn(omega[q], sv, iv.v[q][IV_D][r]));
+            float rv = __fmaf_rn(-omega[q], iv.v[q][IV_T][r], sv);
+            iv.v[q][IV_R][r] = rv;
+            acc[2 * q] = __fmaf_rn(iv.v[q][IV_RH][r], rv, acc[2 * q]);
+            acc[2 * q + 1] = __fmaf_rn(rv, rv, acc[2 * q + 1]);
         }
     }
-    block_sum_store<4>(acc, partials);
+    double a[4] = {acc[0], acc[1], acc[2], acc[3]};
+    block_sum_store<4>(a, partials);
 }
 
 // Scalar bookkeeping between kernels (one thread).
@@ -411,10 +418,12 @@ __global__ void __launch_bounds__(kBlock) k_kry_x(Grid g, KVec kv, int nrhs, int
 // phase 3: after t: (t, s), (t, t) from generic slots 12+2q, 13+2q
 // phase 2: after x: alpha, omega kept for the next p update; rho_old = rho;
 //          rho, (r, r) from generic slots 2q, 2q+1
-__global__ void k_kry_scalars(double* scal, int nrhs, int phase) {
-    for (int q = 0; q < nrhs; ++q) {
+__global__ void k_kry_scalars(double* scal, int mask, int phase) {
+    for (int q = 0; q < 2; ++q) {
+        if (!((mask >> q) & 1)) continue;
         if (phase == 0) {
-            scal[sslot(q, ST_RHO)] = scal[sslot(q, ST_RR)];
+            scal[sslot(q, ST_RHO)] = scal[S_RED0 + q];
+            scal[sslot(q, ST_RR)] = scal[S_RED0 + q];
             scal[sslot(q, ST_RHO_OLD)] = 1.0;
             scal[sslot(q, ST_ALPHA)] = 1.0;
             scal[sslot(q, ST_OMEGA)] = 1.0;
@@ -424,7 +433,6 @@ __global__ void k_kry_scalars(double* scal, int nrhs, int phase) {
             scal[sslot(q, ST_TS)] = scal[S_RED0 + 12 + 2 * q];
             scal[sslot(q, ST_TT)] = scal[S_RED0 + 13 + 2 * q];
         } else if (phase == 2) {
-            if (scal[aslot(q)] == 0.0) continue;
             double alpha = scal[sslot(q, ST_RHO)] / scal[sslot(q, ST_RV)];
             double tt = scal[sslot(q, ST_TT)];
             double omega = (tt > 0.0) ? scal[sslot(q, ST_TS)] / tt : 0.0;
@@ -434,6 +442,16 @@ __global__ void k_kry_scalars(double* scal, int nrhs, int phase) {
             scal[sslot(q, ST_RHO)] = scal[S_RED0 + 2 * q];
             scal[sslot(q, ST_RR)] = scal[S_RED0 + 2 * q + 1];
         }
+    }
+}
+
+// x += d (FP64 accumulation of the FP32 correction)
+__global__ void k_t_accum(Grid g, const float* __restrict__ d0, const float* __restrict__ d1,
+                          double* __restrict__ x0, double* __restrict__ x1, int mask) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        if (mask & 1) x0[r] += (double)d0[r];
+        if (mask & 2) x1[r] += (double)d1[r];
     }
 }
 
@@ -450,174 +468,180 @@ __global__ void __launch_bounds__(kBlock) k_minmax(Grid g, const double* __restr
     block_max_store<2>(m, partials);
 }
 
-// Scaled residual of x: sum (b~ - A~ x)^2 (diagnostic, once per solve)
+// zero the flux of Rock and Precipitate voxels (src/Simulation.cpp:1134-1149), after the
+// solve; no transport row uses the flux of such a voxel
 template <typename L>
-__global__ void __launch_bounds__(kBlock) k_kry_resid(Op<L> op, KVec kv, int nrhs,
-                                                      double* __restrict__ partials) {
-    double acc[2] = {0.0, 0.0};
-    const Grid& g = op.g;
-    const double* xs[2] = {kv.x[0], kv.x[1]};
+__global__ void k_zero_solid_flux(Grid g, const L* __restrict__ label, double* __restrict__ fx,
+                                  double* __restrict__ fy, double* __restrict__ fz) {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
-        int i, j, k;
-        decode(g, r, i, j, k);
-        double y[2];
-        op_apply_row(op, r, i, j, k, xs, y, nrhs);
-        for (int q = 0; q < nrhs; ++q) {
-            double rv = kv.b[q][r] - y[q];
-            acc[q] += rv * rv;
-        }
+        int t = (int)label[r];
+        if (t == kRock || t == kPrecipitate) { fx[r] = 0.0; fy[r] = 0.0; fz[r] = 0.0; }
     }
-    block_sum_store<2>(acc, partials);
 }
 
-static ls_status kry_alloc(ls_ctx* c) {
-    for (int q = 0; q < 14; ++q)
-        if (!c->tv[q]) LS_TRY(dalloc_t(c, &c->tv[q], (size_t)c->g.N));
+static ls_status t_alloc(ls_ctx* c) {
+    const size_t n = (size_t)c->g.N;
+    for (int q = 0; q < 7; ++q)
+        if (!c->tc[q]) LS_TRY(dalloc_t(c, &c->tc[q], n));
+    for (int q = 0; q < 2; ++q)
+        if (!c->tb[q]) LS_TRY(dalloc_t(c, &c->tb[q], n));
+    for (int q = 0; q < 6; ++q)
+        if (!c->to[q]) LS_TRY(dalloc_t(c, &c->to[q], n));
+    for (int q = 0; q < 2; ++q)
+        for (int v = 0; v < 8; ++v)
+            if (!c->tf[q][v]) LS_TRY(dalloc_t(c, &c->tf[q][v], n));
+    if (!c->tkind) LS_TRY(dalloc_t(c, &c->tkind, n));
     return LS_OK;
 }
 
-static ls_status set_scalars(ls_ctx* c, int first, const double* v, int n) {
-    for (int q = 0; q < n; ++q) c->h_scal[first + q] = v[q];
-    LS_CUDA(c, cudaMemcpyAsync(c->scal + first, c->h_scal + first, sizeof(double) * n,
-                               cudaMemcpyHostToDevice, c->stream));
-    return LS_OK;
+static TBuf make_tbuf(ls_ctx* c) {
+    TBuf tb;
+    for (int q = 0; q < 7; ++q) tb.c[q] = c->tc[q];
+    for (int q = 0; q < 2; ++q) tb.b[q] = c->tb[q];
+    for (int q = 0; q < 6; ++q) tb.o[q] = c->to[q];
+    tb.kind = c->tkind;
+    return tb;
 }
 
-// BiCGStab on D^-1 A x = D^-1 b for nrhs right-hand sides (x warm-started in place).
-template <typename L>
-static ls_status bicgstab(ls_ctx* c, const Op<L>& op, KVec& kv, int nrhs, const double* f0,
-                          const double* f1, double rtol, int max_it, ls_solve_info* info[2]) {
+static IVec make_ivec(ls_ctx* c) {
+    IVec iv;
+    for (int q = 0; q < 2; ++q)
+        for (int v = 0; v < 8; ++v) iv.v[q][v] = c->tf[q][v];
+    return iv;
+}
+
+// Inner FP32 BiCGStab for the right-hand sides in mask; each stops at its own relative
+// tolerance tol[q] or on breakdown. Returns the iterations of each.
+static ls_status inner_bicgstab(ls_ctx* c, const TBuf& tb, const IVec& iv, int mask, const double tol[2],
+                                int max_it, int its[2]) {
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
-    LS_LAUNCH(c, k_kry_setup<L>, grid, kBlock, 0, op, kv, nrhs, f0, f1, c->partials);
-    LS_TRY(finalize_sum(c, grid, 2, S_RED0 + 4));
-    LS_LAUNCH(c, k_kry_xid<L>, grid, kBlock, 0, op, kv, nrhs);
-    LS_LAUNCH(c, k_kry_init<L>, grid, kBlock, 0, op, kv, nrhs, c->partials);
+    its[0] = its[1] = 0;
+    LS_LAUNCH(c, k_i_init, grid, kBlock, 0, g, iv, mask, c->partials);
     LS_TRY(finalize_sum(c, grid, 2, S_RED0));
-    double h[8];
-    LS_TRY(read_scalars(c, S_RED0, 6, h));
-    double bn2[2] = {h[4], h[5]}, rr[2] = {h[0], h[1]};
-    double act[2] = {0.0, 0.0};
-    int its[2] = {0, 0};
-    int reason[2] = {0, 0};
-    int restarts[2] = {0, 0};
-    for (int q = 0; q < nrhs; ++q) {
-        if (rr[q] != rr[q] || bn2[q] != bn2[q]) { reason[q] = -4; continue; }
-        double tgt = rtol * rtol * bn2[q];
-        if (rr[q] <= tgt || rr[q] == 0.0) reason[q] = 2;
-        else act[q] = 1.0;
-    }
-    LS_TRY(set_scalars(c, aslot(0), act, 2));
-    double init_rr[2];
-    for (int q = 0; q < nrhs; ++q) {
-        init_rr[q] = rr[q];
-        c->h_scal[sslot(q, ST_RR)] = rr[q];
-        LS_CUDA(c, cudaMemcpyAsync(c->scal + sslot(q, ST_RR), c->h_scal + sslot(q, ST_RR),
-                                   sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    }
-    LS_LAUNCH(c, k_kry_scalars, 1, 1, 0, c->scal, nrhs, 0);
+    LS_LAUNCH(c, k_kry_scalars, 1, 1, 0, c->scal, mask, 0);
+    double rr0[2];
+    LS_TRY(read_scalars(c, S_RED0, 2, rr0));
+    int act = 0;
+    for (int q = 0; q < 2; ++q)
+        if (((mask >> q) & 1) && rr0[q] > 0.0 && rr0[q] == rr0[q]) act |= 1 << q;
+    const double apply_bytes_per_rhs = (double)g.N * 4.0 * (1 + 1 + 1);  // in, out, rh or s
     int it = 0;
-    while ((act[0] != 0.0 || act[1] != 0.0) && it < max_it) {
-        const int mask = (act[0] != 0.0 ? 1 : 0) | (act[1] != 0.0 ? 2 : 0);
-        const int nact = (mask & 1) + ((mask >> 1) & 1);
-        // label 1 + own flux 3x8 + per live vector: input 8, output 8, rhat (or s) 8
-        const double apply_bytes = (double)g.N * (1.0 + 24.0 + 24.0 * nact);
-        LS_LAUNCH(c, k_kry_p, grid, kBlock, 0, g, kv, nrhs, mask, (const double*)c->scal);
+    while (act && it < max_it) {
+        const int nact = (act & 1) + ((act >> 1) & 1);
+        // scaled off-diagonals 6x4 per row + per live vector: input, output, rhat/s
+        const double apply_bytes = (double)g.N * 24.0 + apply_bytes_per_rhs * nact;
+        LS_LAUNCH(c, k_i_p, grid, kBlock, 0, g, iv, act, (const double*)c->scal);
         {
             Timed tm(c, LS_T_KRY_APPLY);
-            LS_LAUNCH(c, k_kry_v<L>, grid, kBlock, 0, op, kv, nrhs, mask, c->partials);
-            c->timer_bytes[LS_T_KRY_APPLY] += c->timing ? apply_bytes : 0.0;
+            LS_LAUNCH(c, k_i_v, grid, kBlock, 0, g, tb, iv, act, c->partials);
+            if (c->timing) c->timer_bytes[LS_T_KRY_APPLY] += apply_bytes;
         }
         LS_TRY(finalize_sum(c, grid, 2, S_RED0 + 10));
-        LS_LAUNCH(c, k_kry_scalars, 1, 1, 0, c->scal, nrhs, 1);
-        LS_LAUNCH(c, k_kry_s, grid, kBlock, 0, g, kv, nrhs, mask, (const double*)c->scal);
+        LS_LAUNCH(c, k_kry_scalars, 1, 1, 0, c->scal, act, 1);
+        LS_LAUNCH(c, k_i_s, grid, kBlock, 0, g, iv, act, (const double*)c->scal);
         {
             Timed tm(c, LS_T_KRY_APPLY);
-            LS_LAUNCH(c, k_kry_t<L>, grid, kBlock, 0, op, kv, nrhs, mask, c->partials);
-            c->timer_bytes[LS_T_KRY_APPLY] += c->timing ? apply_bytes : 0.0;
+            LS_LAUNCH(c, k_i_t, grid, kBlock, 0, g, tb, iv, act, c->partials);
+            if (c->timing) c->timer_bytes[LS_T_KRY_APPLY] += apply_bytes;
         }
         LS_TRY(finalize_sum(c, grid, 4, S_RED0 + 12));
-        LS_LAUNCH(c, k_kry_scalars, 1, 1, 0, c->scal, nrhs, 3);
-        LS_LAUNCH(c, k_kry_x, grid, kBlock, 0, g, kv, nrhs, mask, (const double*)c->scal, c->partials);
+        LS_LAUNCH(c, k_kry_scalars, 1, 1, 0, c->scal, act, 3);
+        LS_LAUNCH(c, k_i_x, grid, kBlock, 0, g, iv, act, (const double*)c->scal, c->partials);
         LS_TRY(finalize_sum(c, grid, 4, S_RED0));
-        LS_LAUNCH(c, k_kry_scalars, 1, 1, 0, c->scal, nrhs, 2);
+        LS_LAUNCH(c, k_kry_scalars, 1, 1, 0, c->scal, act, 2);
         it++;
-        double sc[32];
+        double sc[16];
         LS_TRY(read_scalars(c, ST_BASE, 16, sc));
-        bool changed = false;
-        for (int q = 0; q < nrhs; ++q) {
-            if (act[q] == 0.0) continue;
+        for (int q = 0; q < 2; ++q) {
+            if (!((act >> q) & 1)) continue;
             its[q] = it;
             double rho = sc[8 * q + ST_RHO], r2 = sc[8 * q + ST_RR], om = sc[8 * q + ST_OMEGA];
-            if (r2 != r2 || rho != rho) { reason[q] = -4; act[q] = 0.0; changed = true; continue; }
-            if (r2 <= rtol * rtol * bn2[q]) { reason[q] = 2; act[q] = 0.0; changed = true; continue; }
-            // breakdown: restart with rhat = r
-            if (rho == 0.0 || om == 0.0 || fabs(rho) < 1e-30 * r2) {
-                if (++restarts[q] > 20) { reason[q] = -5; act[q] = 0.0; changed = true; continue; }
-                reason[q] = 1;  // marker: restart requested
-            }
-        }
-        bool need_restart = false;
-        for (int q = 0; q < nrhs; ++q)
-            if (reason[q] == 1) { need_restart = true; reason[q] = 0; }
-        if (changed) LS_TRY(set_scalars(c, aslot(0), act, 2));
-        if (need_restart) {
-            LS_LAUNCH(c, k_kry_init<L>, grid, kBlock, 0, op, kv, nrhs, c->partials);
-            LS_TRY(finalize_sum(c, grid, 2, S_RED0));
-            for (int q = 0; q < nrhs; ++q)
-                LS_CUDA(c, cudaMemcpyAsync(c->scal + sslot(q, ST_RR), c->scal + S_RED0 + q,
-                                           sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
-            LS_LAUNCH(c, k_kry_scalars, 1, 1, 0, c->scal, nrhs, 0);
+            bool done = (r2 <= tol[q] * tol[q] * rr0[q]) || r2 != r2 || rho != rho || rho == 0.0 ||
+                        om == 0.0;
+            if (done) act &= ~(1 << q);
         }
     }
-    for (int q = 0; q < nrhs; ++q)
-        if (act[q] != 0.0) reason[q] = -3;
-    // final scaled residual and min/max per right-hand side
-    LS_LAUNCH(c, k_kry_resid<L>, grid, kBlock, 0, op, kv, nrhs, c->partials);
-    LS_TRY(finalize_sum(c, grid, 2, S_RED0));
-    double fr[2];
-    LS_TRY(read_scalars(c, S_RED0, 2, fr));
+    return LS_OK;
+}
+
+// Mixed-precision solve of the rows in `rows` for nrhs right-hand sides (x warm-started in
+// place), fields f0/f1 supplying the right-hand sides.
+template <typename L>
+static ls_status mixed_solve(ls_ctx* c, const Rows<L>& rows, int nrhs, const double* f0, const double* f1,
+                             double* x0, double* x1, double rtol, int max_it, ls_solve_info* info[2]) {
+    LS_TRY(t_alloc(c));
+    const Grid g = c->g;
+    const int grid = grid_for(c, g.N);
+    TBuf tb = make_tbuf(c);
+    IVec iv = make_ivec(c);
+    LS_LAUNCH(c, k_t_setup<L>, grid, kBlock, 0, rows, tb, nrhs, f0, f1, c->partials);
+    LS_TRY(finalize_sum(c, grid, 2, S_RED0 + 4));
+    LS_LAUNCH(c, k_t_xid, grid, kBlock, 0, g, tb, x0, x1, nrhs);
+    double den[2];
+    LS_TRY(read_scalars(c, S_RED0 + 4, 2, den));
+    int mask = nrhs > 1 ? 3 : 1;
+    int its[2] = {0, 0}, sweeps[2] = {0, 0}, reason[2] = {0, 0};
+    double rel[2] = {0.0, 0.0}, prev[2] = {INFINITY, INFINITY};
+    int stagnant[2] = {0, 0};
+    const int max_sweeps = 40;
+    while (mask) {
+        LS_LAUNCH(c, k_t_resid, grid, kBlock, 0, g, tb, x0, x1, iv.v[0][IV_RHS], iv.v[1][IV_RHS], mask,
+                  c->partials);
+        LS_TRY(finalize_sum(c, grid, 4, S_RED0));
+        double h[4];
+        LS_TRY(read_scalars(c, S_RED0, 4, h));
+        int solve_mask = 0;
+        double tol[2] = {0.5, 0.5};
+        for (int q = 0; q < nrhs; ++q) {
+            if (!((mask >> q) & 1)) continue;
+            if (h[2 + q] > 0.0 || h[q] != h[q]) { reason[q] = -4; rel[q] = NAN; mask &= ~(1 << q); continue; }
+            rel[q] = den[q] > 0.0 ? sqrt(h[q] / den[q]) : sqrt(h[q]);
+            if (rel[q] <= rtol || h[q] == 0.0) { reason[q] = 2; mask &= ~(1 << q); continue; }
+            if (its[q] >= max_it || sweeps[q] >= max_sweeps) { reason[q] = -3; mask &= ~(1 << q); continue; }
+            if (rel[q] > 0.5 * prev[q]) {
+                if (++stagnant[q] >= 6) { reason[q] = -3; mask &= ~(1 << q); continue; }
+            } else {
+                stagnant[q] = 0;
+            }
+            prev[q] = rel[q];
+            tol[q] = std::min(0.5, std::max(1e-5, 0.2 * rtol / std::max(rel[q], 1e-300)));
+            solve_mask |= 1 << q;
+        }
+        if (!solve_mask) break;
+        int iits[2] = {0, 0};
+        int budget = max_it - std::max(its[0], its[1]);
+        LS_TRY(inner_bicgstab(c, tb, iv, solve_mask, tol, std::max(budget, 1), iits));
+        for (int q = 0; q < 2; ++q)
+            if ((solve_mask >> q) & 1) { its[q] += iits[q]; sweeps[q]++; }
+        LS_LAUNCH(c, k_t_accum, grid, kBlock, 0, g, iv.v[0][IV_D], iv.v[1][IV_D], x0, x1, solve_mask);
+    }
     ls_status st = LS_OK;
+    double* xs[2] = {x0, x1};
     for (int q = 0; q < nrhs; ++q) {
-        LS_LAUNCH(c, k_minmax, grid, kBlock, 0, g, (const double*)kv.x[q], c->partials);
+        double mm[2] = {0.0, 0.0};
+        LS_LAUNCH(c, k_minmax, grid, kBlock, 0, g, (const double*)xs[q], c->partials);
         LS_TRY(finalize_max(c, grid, 2, S_RED0 + 2));
-        double mm[2];
         LS_TRY(read_scalars(c, S_RED0 + 2, 2, mm));
         if (info[q]) {
             info[q]->iterations = its[q];
-            info[q]->outer_iterations = restarts[q] + 1;
+            info[q]->outer_iterations = sweeps[q];
             info[q]->converged = reason[q] > 0;
             info[q]->reason = reason[q];
-            info[q]->rel_residual = bn2[q] > 0.0 ? sqrt(fr[q] / bn2[q]) : sqrt(fr[q]);
+            info[q]->rel_residual = rel[q];
             info[q]->max_value = mm[0];
             info[q]->min_value = -mm[1];
         }
-        (void)init_rr;
         if (reason[q] == -4) st = set_error(c, LS_NONFINITE, "Krylov solve met NaN/Inf");
         else if (reason[q] <= 0 && st == LS_OK) {
-            char buf[128];
-            snprintf(buf, sizeof(buf), "Krylov solve not converged in %d iterations", its[q]);
+            char buf[160];
+            snprintf(buf, sizeof(buf), "Krylov solve not converged (rel %.3e after %d its, %d sweeps)",
+                     rel[q], its[q], sweeps[q]);
             st = set_error(c, LS_NOT_CONVERGED, buf);
         }
     }
     return st;
-}
-
-static KVec make_kvec(ls_ctx* c, double* x0, double* x1) {
-    KVec kv;
-    for (int q = 0; q < 2; ++q) {
-        kv.b[q] = c->tv[7 * q + 0];
-        kv.r[q] = c->tv[7 * q + 1];
-        kv.rh[q] = c->tv[7 * q + 2];
-        kv.p[q] = c->tv[7 * q + 3];
-        kv.v[q] = c->tv[7 * q + 4];
-        kv.s[q] = c->tv[7 * q + 5];
-        kv.t[q] = c->tv[7 * q + 6];
-    }
-    kv.x[0] = x0;
-    kv.x[1] = x1;
-    return kv;
 }
 
 static TransConst trans_const(const ls_ctx* c, double dt) {
@@ -633,24 +657,29 @@ static TransConst trans_const(const ls_ctx* c, double dt) {
 }
 
 template <typename L>
+static Rows<L> trans_rows(ls_ctx* c, double dt) {
+    Rows<L> rows;
+    rows.mode = 0;
+    rows.g = c->g;
+    rows.tc = trans_const(c, dt);
+    rows.sc = SatConst{0.0, 1.0, 0.0};
+    rows.label = (const L*)c->label;
+    rows.fx = c->fx; rows.fy = c->fy; rows.fz = c->fz; rows.s = nullptr;
+    return rows;
+}
+
+template <typename L>
 static ls_status transport_t(ls_ctx* c, double dt, int which, ls_solve_info* ci, ls_solve_info* ai) {
-    LS_TRY(kry_alloc(c));
-    Op<L> op;
-    op.mode = 0;
-    op.g = c->g;
-    op.tc = trans_const(c, dt);
-    op.label = (const L*)c->label;
-    op.fx = c->fx; op.fy = c->fy; op.fz = c->fz; op.s = nullptr;
+    Rows<L> rows = trans_rows<L>(c, dt);
     const long long sh = c->p.compat_shift ? c->g.JK : 0;
     double* fields[2] = {c->conc, c->acid};
-    double* f[2];
-    ls_solve_info* inf[2];
+    double* f[2] = {nullptr, nullptr};
+    ls_solve_info* inf[2] = {nullptr, nullptr};
     int n = 0;
     if (which & 1) { f[n] = fields[0]; inf[n] = ci; n++; }
     if (which & 2) { f[n] = fields[1]; inf[n] = ai; n++; }
-    KVec kv = make_kvec(c, f[0] + sh, n > 1 ? f[1] + sh : nullptr);
-    ls_status st = bicgstab<L>(c, op, kv, n, f[0], n > 1 ? f[1] : nullptr, c->p.conc_rtol,
-                               c->p.conc_max_it, inf);
+    ls_status st = mixed_solve<L>(c, rows, n, f[0], f[1], f[0] + sh, n > 1 ? f[1] + sh : nullptr,
+                                  c->p.conc_rtol, c->p.conc_max_it, inf);
     if (st != LS_OK && st != LS_NOT_CONVERGED && st != LS_NONFINITE) return st;
     LS_LAUNCH(c, k_zero_solid_flux<L>, grid_for(c, c->g.N), kBlock, 0, c->g, (const L*)c->label,
               c->fx, c->fy, c->fz);
@@ -662,34 +691,37 @@ ls_status transport_run(ls_ctx* c, double dt, int which, ls_solve_info* ci, ls_s
     return transport_t<uint16_t>(c, dt, which, ci, ai);
 }
 
-// test hook: y = A x (unscaled) for the transport operator at dt
+// test hook: y = A x (unscaled, separate multiply and add like an assembled matrix)
 template <typename L>
-__global__ void k_trans_apply_full(Op<L> op, const double* __restrict__ x, double* __restrict__ y) {
+__global__ void k_trans_apply_full(Rows<L> op, const double* __restrict__ x, double* __restrict__ y) {
     const Grid& g = op.g;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         decode(g, r, i, j, k);
-        double yv[1];
-        const double* xs[1] = {x};
-        op_apply_row(op, r, i, j, k, xs, yv, 1, true);
-        y[r] = yv[0];
+        double dg, off[6];
+        trans_row(g, op.tc, op.label, op.fx, op.fy, op.fz, r, i, j, k, dg, off, nullptr, nullptr, nullptr);
+        double acc = 0.0;
+        if (i > 0) acc += off[1] * x[r - g.JK];
+        if (j > 0) acc += off[3] * x[r - g.K];
+        if (k > 0) acc += off[5] * x[r - 1];
+        acc += dg * x[r];
+        if (k + 1 < g.K) acc += off[4] * x[r + 1];
+        if (j + 1 < g.J) acc += off[2] * x[r + g.K];
+        if (i + 1 < g.I) acc += off[0] * x[r + g.JK];
+        y[r] = acc;
     }
 }
 
 template <typename L>
 static ls_status transport_apply_t(ls_ctx* c, double dt, const double* xh, double* yh) {
-    LS_TRY(kry_alloc(c));
-    Op<L> op;
-    op.mode = 0;
-    op.g = c->g;
-    op.tc = trans_const(c, dt);
-    op.label = (const L*)c->label;
-    op.fx = c->fx; op.fy = c->fy; op.fz = c->fz; op.s = nullptr;
+    LS_TRY(t_alloc(c));
+    Rows<L> rows = trans_rows<L>(c, dt);
     const size_t bytes = sizeof(double) * (size_t)c->g.N;
-    LS_CUDA(c, cudaMemcpyAsync(c->tv[0], xh, bytes, cudaMemcpyHostToDevice, c->stream));
-    LS_LAUNCH(c, k_trans_apply_full<L>, grid_for(c, c->g.N), kBlock, 0, op, (const double*)c->tv[0], c->tv[1]);
-    LS_CUDA(c, cudaMemcpyAsync(yh, c->tv[1], bytes, cudaMemcpyDeviceToHost, c->stream));
+    LS_CUDA(c, cudaMemcpyAsync(c->tc[0], xh, bytes, cudaMemcpyHostToDevice, c->stream));
+    LS_LAUNCH(c, k_trans_apply_full<L>, grid_for(c, c->g.N), kBlock, 0, rows, (const double*)c->tc[0],
+              c->tc[1]);
+    LS_CUDA(c, cudaMemcpyAsync(yh, c->tc[1], bytes, cudaMemcpyDeviceToHost, c->stream));
     LS_CUDA(c, cudaStreamSynchronize(c->stream));
     return LS_OK;
 }
@@ -700,7 +732,8 @@ ls_status transport_apply_run(ls_ctx* c, double dt, const double* x, double* y) 
 }
 
 // ---------------------------------------------------------------------------
-// implicit saturation
+// implicit saturation: the coefficients are taken from the saturation before the solve
+// (the setup kernel reads every slot before any solution slot is written)
 
 __global__ void k_clamp_sat(Grid g, double* __restrict__ s) {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
@@ -710,23 +743,20 @@ __global__ void k_clamp_sat(Grid g, double* __restrict__ s) {
 
 template <typename L>
 static ls_status sat_implicit_t(ls_ctx* c, double dt, ls_solve_info* info) {
-    LS_TRY(kry_alloc(c));
-    if (!c->s_old) LS_TRY(dalloc_t(c, &c->s_old, (size_t)c->g.NP));
-    LS_CUDA(c, cudaMemcpyAsync(c->s_old, c->sat, sizeof(double) * (size_t)c->g.NP,
-                               cudaMemcpyDeviceToDevice, c->stream));
-    Op<L> op;
-    op.mode = 1;
-    op.g = c->g;
-    op.sc.phi_dt = c->p.porosity * (1.0 / dt);
-    op.sc.dx = c->p.dx;
-    op.sc.evap = c->p.evaporative_flux;
-    op.label = (const L*)c->label;
-    op.fx = c->fx; op.fy = c->fy; op.fz = c->fz; op.s = c->s_old;
+    Rows<L> rows;
+    rows.mode = 1;
+    rows.g = c->g;
+    rows.tc = trans_const(c, 1.0);
+    rows.sc.phi_dt = c->p.porosity * (1.0 / dt);
+    rows.sc.dx = c->p.dx;
+    rows.sc.evap = c->p.evaporative_flux;
+    rows.label = (const L*)c->label;
+    rows.fx = c->fx; rows.fy = c->fy; rows.fz = c->fz; rows.s = c->sat;
     const long long sh = c->p.compat_shift ? c->g.JK : 0;
-    KVec kv = make_kvec(c, c->sat + sh, nullptr);
     ls_solve_info loc;
     ls_solve_info* inf[2] = {&loc, nullptr};
-    ls_status st = bicgstab<L>(c, op, kv, 1, nullptr, nullptr, c->p.sat_rtol, c->p.sat_max_it, inf);
+    ls_status st = mixed_solve<L>(c, rows, 1, nullptr, nullptr, c->sat + sh, nullptr, c->p.sat_rtol,
+                                  c->p.sat_max_it, inf);
     if (info) *info = loc;
     if (st != LS_OK && st != LS_NOT_CONVERGED) return st;
     // physics check and clamp over the voxel slots (src/Simulation.cpp:2007-2047)

@@ -3,7 +3,8 @@
 Each kernel is isolated by uploading the oracle's inputs, so that arithmetic
 without transcendental functions can be required to match bit for bit.
 Tolerances, where not exact:
-  * props (pow/log10/sqrt of CUDA vs glibc): 1e-14 relative
+  * props (CUDA pow/sqrt against glibc pow; the n = 2 van Genuchten exponents are
+    evaluated with sqrt and products): 1e-13 relative
   * pressure solutions: the Pore system is conditioned near 1e18; rel-L2 1e-7 for
     the full field against a direct solve, 1e-8 Jacobi-scaled residual
   * transport solutions: rel-L2 1e-9 against a direct solve
@@ -65,7 +66,7 @@ def test_props(oracle_mod, name, geom, lb):
     lab = geom()
     o, g = pair(oracle_mod, lab, params(), lb, seed=11)
     for f in ("rel_perm", "cap_pressure", "permeability"):
-        np.testing.assert_allclose(g.download(f), o.get(f), rtol=1e-14, atol=0, err_msg=f)
+        np.testing.assert_allclose(g.download(f), o.get(f), rtol=1e-13, atol=0, err_msg=f)
     np.testing.assert_array_equal(g.download("viscosity"), o.get("viscosity"))
     g.close()
 
