@@ -240,8 +240,11 @@ ls_status ls_create(ls_ctx** out, int I, int J, int K, int label_bytes, const ls
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return LS_NO_DEVICE;
 
+    cudaGetLastError();  // a context starts without an error left pending by other code
     ls_ctx* c = new (std::nothrow) ls_ctx();
     if (!c) return LS_BAD_ARG;
+    c->inner_is64 = -1;
+    c->mg_is64 = -1;
     c->g.I = I; c->g.J = J; c->g.K = K;
     c->g.JK = JK;
     c->g.N = (long long)I * JK;
@@ -262,7 +265,10 @@ ls_status ls_create(ls_ctx** out, int I, int J, int K, int label_bytes, const ls
     do {                                                                      \
         st = dalloc_t(c, &(ptr), (count));                                    \
         if (st != LS_OK) { ls_destroy(c); return st; }                         \
-        cudaMemsetAsync((ptr), 0, sizeof(*(ptr)) * (count), c->stream);       \
+        if (cudaMemsetAsync((ptr), 0, sizeof(*(ptr)) * (count), c->stream) != cudaSuccess) { \
+            ls_destroy(c);                                                     \
+            return LS_CUDA_ERROR;                                              \
+        }                                                                      \
     } while (0)
     {
         uint8_t* lb = nullptr;
@@ -309,9 +315,9 @@ ls_status ls_destroy(ls_ctx* c) {
                     c->acid, c->fx, c->fy, c->fz, c->sat, c->pc, c->kr, c->precip,
                     c->b_precip, c->b_sat, c->b_P, c->b_conc, c->b_acid, c->b_fx, c->b_fy,
                     c->b_fz, c->pkind, c->pdiag, c->pb, c->pface[0], c->pface[1], c->pface[2],
-                    c->pisd, c->pr, c->pdelta, c->w32[0], c->w32[1], c->w32[2], c->w64[0],
-                    c->w64[1], c->w64[2], c->inner[0], c->inner[1], c->inner[2], c->inner[3],
-                    c->inner[4], c->comp, c->cc_flag, c->tkind, c->dz_list,
+                    c->pisd, c->pr, c->pdelta, c->ie, c->iface[0], c->iface[1], c->iface[2],
+                    c->iinvd, c->inner[0], c->inner[1], c->inner[2], c->inner[3],
+                    c->inner[4], c->mg0_x, c->mg0_t, c->comp, c->cc_flag, c->tkind, c->dz_list,
                     c->dz_count, c->dz_level_start, c->partials, c->scal, c->d_int};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -325,7 +331,7 @@ ls_status ls_destroy(ls_ctx* c) {
         for (float* q : v)
             if (q) cudaFree(q);
     for (auto& lv : c->mg) {
-        void* lp[] = {lv.comp, lv.diag, lv.face[0], lv.face[1], lv.face[2], lv.x, lv.b, lv.t};
+        void* lp[] = {lv.comp, lv.e, lv.face[0], lv.face[1], lv.face[2], lv.invd, lv.x, lv.b, lv.t};
         for (void* q : lp)
             if (q) cudaFree(q);
     }
@@ -338,6 +344,7 @@ ls_status ls_destroy(ls_ctx* c) {
     for (auto e : c->event_pool) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
+    cudaGetLastError();  // leave no error of the teardown pending for the next context
     return LS_OK;
 }
 

@@ -78,26 +78,33 @@ struct ls_ctx {
     double* pisd;       // 1/sqrt(d) of inner unknowns (normal Pore rows), else 0
     double* pr;         // FP64 outer residual
     double* pdelta;     // FP64 correction
-    float* w32[3];      // Jacobi-scaled inner face weights (FP32)
-    double* w64[3];     // Jacobi-scaled inner face weights (FP64)
-    void* inner[5];     // inner PCG vectors x r z p q (FP32 or FP64)
-    int inner_is64;
+    // inner pressure system on the normal Pore rows, sigma-scaled, in "excess + graph
+    // Laplacian" form: (M x)_i = e_i x_i + sum_links c_ij (x_i - x_j). T = float or double.
+    void* ie;           // excess e (links to rows that are not inner unknowns), T
+    void* iface[3];     // link coefficients of the +i, +j, +k faces between two unknowns, T
+    void* iinvd;        // 1 / (e + sum of the six links), T
+    void* inner[5];     // inner PCG vectors x r z p q, T
+    int inner_is64;     // -1 = not allocated
     double pscale_den;  // ||D^-1 b|| of the current pressure system
     double p_t;         // time the pressure system was assembled for
     int p_ready;
 
-    // multigrid hierarchy (allocated on demand)
+    // multigrid: the finest level is the inner system above (vectors mg0_x, mg0_t);
+    // mg[l] are the coarse levels, each owning its arrays
     struct MGLevel {
         ls::Grid g;
-        int* comp;          // component / unknown id per cell (-1 = not an unknown)
-        void* diag;         // T
-        void* face[3];      // T, + faces
+        int* comp;          // owning component of the cell (-1 = no unknown)
+        void* e;            // excess, T
+        void* face[3];      // + face links, T
+        void* invd;         // 1 / diagonal, T
         void* x;            // T
         void* b;            // T
         void* t;            // T
     };
     std::vector<MGLevel> mg;
-    int mg_is64;
+    void* mg0_x;
+    void* mg0_t;
+    int mg_is64;          // -1 = not allocated
     int* comp;            // fine-level strong-component ids (-1 = not an inner unknown)
     int* cc_flag;         // device flag for the labelling loop
 

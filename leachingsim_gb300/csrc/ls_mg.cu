@@ -1,21 +1,25 @@
 // ls_mg.cu - geometric multigrid preconditioner of the inner pressure PCG.
 //
-// The inner system is W = I - L on the Pore unknowns (Jacobi-scaled, unit diagonal; L
-// holds the positive scaled link weights of the +i, +j, +k faces). The Pore network is
-// masked by Dirichlet voxels everywhere and its links span ~13 orders of magnitude, so
-// plain 2x2x2 aggregation would hand coarse corrections to Pore clusters that merely share
-// a block with the main network while being joined to it by no strong link. Such a
-// cluster's own near-null mode then absorbs the correction and keeps it (the residual
-// there is ~1e-13 of the error). The hierarchy therefore works per strong component:
-//   * components: connected pieces of the unknowns over links with w > kStrong
-//     (union-find on the device);
+// Every level holds its operator in "excess + graph Laplacian" form,
+//     (M x)_i = e_i x_i + sum_{links ij} c_ij (x_i - x_j),   e_i >= 0, c_ij >= 0,
+// so M is symmetric positive (semi)definite for any rounding of e and c: the FP32 copy of
+// the finest operator cannot turn indefinite, and the Galerkin coarse operators are sums of
+// positive terms (no cancellation). The finest level is the inner system itself (excess =
+// links of a Pore row to rows that are not inner unknowns).
+//
+// The Pore network is masked by Dirichlet voxels everywhere and its links span ~13 orders
+// of magnitude, so plain 2x2x2 aggregation would hand coarse corrections to Pore clusters
+// that merely share a block with the main network while being joined to it by no strong
+// link; such a cluster's near-null mode then keeps the correction (its residual is ~1e-13
+// of the error). The hierarchy therefore works per strong component:
+//   * components: connected pieces of the unknowns over links with
+//     c_ij / sqrt(d_i d_j) > kStrong (union-find on the device);
 //   * aggregation: each 2x2x2 block becomes one coarse cell owned by the component with
-//     most members in the block; only those members are restricted to / prolongated from
-//     it (piecewise-constant interpolation), the rest are left to the smoother;
-//   * coarse operators: Galerkin P^T W P, again a 7-point stencil (diag + 3 face weights);
-//   * V-cycle: nu damped-Jacobi sweeps before and after (symmetric), a fixed number of
-//     Jacobi sweeps by one CTA on the coarsest level, so the cycle is a symmetric operator
-//     usable inside CG.
+//     most members in the block; only its members are restricted to / prolongated from it
+//     (piecewise-constant interpolation); links from members to non-members become excess;
+//   * V-cycle: two damped-Jacobi sweeps before and after the coarse correction, a fixed
+//     number of Jacobi sweeps by one CTA on the coarsest level, so the cycle is a symmetric
+//     operator usable inside CG.
 #include <algorithm>
 #include <cstdio>
 
@@ -23,12 +27,56 @@
 
 namespace ls {
 
-constexpr double kStrong = 1e-3;   // scaled link weight below which a link does not join components
-// two damped-Jacobi sweeps before and two after the coarse correction (mg_apply)
+constexpr double kStrong = 1e-3;   // scaled link weight below which a link joins no components
 constexpr double kOmega = 2.0 / 3.0;
 constexpr int kCoarsestCells = 4096;
 constexpr int kCoarseSweeps = 48;
 constexpr int kUnionSpin = 1 << 20;  // bound on the union-find retry loop
+
+__device__ __forceinline__ long long lidx(const Grid& g, int i, int j, int k) {
+    return (long long)k + (long long)g.K * ((long long)j + (long long)g.J * i);
+}
+
+// (M x)_r in difference form (links on the six faces; f0/f1/f2 hold the + faces)
+template <typename T>
+__device__ __forceinline__ T m_apply(const Grid& g, long long r, int i, int j, int k, const T* __restrict__ e,
+                                     const T* __restrict__ f0, const T* __restrict__ f1,
+                                     const T* __restrict__ f2, const T* __restrict__ x) {
+    const T xr = x[r];
+    T acc = e[r] * xr;
+    if (i > 0) acc += f0[r - g.JK] * (xr - x[r - g.JK]);
+    if (j > 0) acc += f1[r - g.K] * (xr - x[r - g.K]);
+    if (k > 0) acc += f2[r - 1] * (xr - x[r - 1]);
+    if (k + 1 < g.K) acc += f2[r] * (xr - x[r + 1]);
+    if (j + 1 < g.J) acc += f1[r] * (xr - x[r + g.K]);
+    if (i + 1 < g.I) acc += f0[r] * (xr - x[r + g.JK]);
+    return acc;
+}
+
+// 1 / (e + sum of the six links) of live cells, 1 elsewhere
+template <typename T>
+__global__ void k_level_invd(Grid g, const int* __restrict__ comp, const int8_t* __restrict__ kind,
+                             const T* __restrict__ e, const T* __restrict__ f0, const T* __restrict__ f1,
+                             const T* __restrict__ f2, T* __restrict__ invd) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        T out = (T)1;
+        bool live = comp ? comp[r] >= 0 : kind[r] == 2;
+        if (live) {
+            int i, j, k;
+            decode(g, r, i, j, k);
+            T d = e[r];
+            if (i > 0) d += f0[r - g.JK];
+            if (j > 0) d += f1[r - g.K];
+            if (k > 0) d += f2[r - 1];
+            if (k + 1 < g.K) d += f2[r];
+            if (j + 1 < g.J) d += f1[r];
+            if (i + 1 < g.I) d += f0[r];
+            out = (d > (T)0) ? (T)1 / d : (T)1;
+        }
+        invd[r] = out;
+    }
+}
 
 // ---------------------------------------------------------------------------
 // strong components (union-find with path halving; ids are voxel indices, the root is the
@@ -46,24 +94,29 @@ __device__ __forceinline__ int cc_find(int* parent, int x) {
     return x;
 }
 
-__global__ void k_cc_init(Grid g, const double* __restrict__ isd, int* __restrict__ parent) {
+__global__ void k_cc_init(Grid g, const int8_t* __restrict__ kind, int* __restrict__ parent) {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x)
-        parent[r] = (isd[r] != 0.0) ? (int)r : -1;
+        parent[r] = (kind[r] == 2) ? (int)r : -1;
 }
 
 template <typename T>
-__global__ void k_cc_hook(Grid g, const T* __restrict__ w0, const T* __restrict__ w1,
-                          const T* __restrict__ w2, int* parent, int* __restrict__ err) {
+__global__ void k_cc_hook(Grid g, const T* __restrict__ f0, const T* __restrict__ f1,
+                          const T* __restrict__ f2, const T* __restrict__ invd, int* parent,
+                          int* __restrict__ err) {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
         if (parent[r] < 0) continue;
-        const T* ws[3] = {w0, w1, w2};
+        const T* fs[3] = {f0, f1, f2};
         const long long offs[3] = {g.JK, g.K, 1};
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            if (!((double)ws[d][r] > kStrong)) continue;  // w > 0 only between two unknowns
-            int a = (int)r, b = (int)(r + offs[d]);
+            T c = fs[d][r];
+            if (!(c > (T)0)) continue;  // c > 0 only between two unknowns
+            long long nb = r + offs[d];
+            double w = (double)c * sqrt((double)invd[r] * (double)invd[nb]);
+            if (!(w > kStrong)) continue;
+            int a = (int)r, b = (int)nb;
             int spins = 0;
             while (true) {
                 int ra = cc_find(parent, a), rb = cc_find(parent, b);
@@ -86,10 +139,6 @@ __global__ void k_cc_compress(Grid g, int* parent) {
 
 // ---------------------------------------------------------------------------
 // hierarchy construction
-
-__device__ __forceinline__ long long lidx(const Grid& g, int i, int j, int k) {
-    return (long long)k + (long long)g.K * ((long long)j + (long long)g.J * i);
-}
 
 // dominant component of each 2x2x2 block (most members; ties: smallest id)
 __global__ void k_mg_dom(Grid f, Grid cg, const int* __restrict__ fcomp, int* __restrict__ ccomp) {
@@ -117,20 +166,27 @@ __global__ void k_mg_dom(Grid f, Grid cg, const int* __restrict__ fcomp, int* __
     }
 }
 
-// Galerkin coarse operator P^T W P for piecewise-constant P restricted to the members of
-// the owning component. fdiag == nullptr means unit diagonal (the finest level).
+// is fine cell (i,j,k) a member of its own block's owner?
+__device__ __forceinline__ bool is_member(const Grid& f, const Grid& cg, const int* fcomp, const int* ccomp,
+                                          int i, int j, int k) {
+    int id = fcomp[lidx(f, i, j, k)];
+    return id >= 0 && ccomp[lidx(cg, i >> 1, j >> 1, k >> 1)] == id;
+}
+
+// Galerkin coarse operator P^T M P for piecewise-constant P restricted to the members of
+// each block's owner: coarse excess = member excess + member links to non-members;
+// coarse + face link = member-to-member links crossing the block's + face.
 template <typename T>
-__global__ void k_mg_coarse_op(Grid f, Grid cg, const int* __restrict__ fcomp,
-                               const int* __restrict__ ccomp, const T* __restrict__ fdiag,
-                               const T* __restrict__ fw0, const T* __restrict__ fw1,
-                               const T* __restrict__ fw2, T* __restrict__ cdiag,
-                               T* __restrict__ cw0, T* __restrict__ cw1, T* __restrict__ cw2) {
+__global__ void k_mg_coarse_op(Grid f, Grid cg, const int* __restrict__ fcomp, const int* __restrict__ ccomp,
+                               const T* __restrict__ fe, const T* __restrict__ f0, const T* __restrict__ f1,
+                               const T* __restrict__ f2, T* __restrict__ ce, T* __restrict__ c0,
+                               T* __restrict__ c1, T* __restrict__ c2) {
     for (long long R = blockIdx.x * (long long)blockDim.x + threadIdx.x; R < cg.N;
          R += (long long)gridDim.x * blockDim.x) {
         int I, J, K;
         decode(cg, R, I, J, K);
         const int own = ccomp[R];
-        double dg = 0.0, e0 = 0.0, e1 = 0.0, e2 = 0.0;
+        double ex = 0.0, e0 = 0.0, e1 = 0.0, e2 = 0.0;
         if (own >= 0) {
             for (int a = 0; a < 2; ++a)
                 for (int b = 0; b < 2; ++b)
@@ -139,65 +195,55 @@ __global__ void k_mg_coarse_op(Grid f, Grid cg, const int* __restrict__ fcomp,
                         if (i >= f.I || j >= f.J || k >= f.K) continue;
                         long long fr = lidx(f, i, j, k);
                         if (fcomp[fr] != own) continue;
-                        dg += fdiag ? (double)fdiag[fr] : 1.0;
-                        // + face links of this fine cell
-                        if (i + 1 < f.I) {
-                            long long nb = fr + f.JK;
-                            if (a == 0) { if (fcomp[nb] == own) dg -= 2.0 * (double)fw0[fr]; }
-                            else if (I + 1 < cg.I && fcomp[nb] == ccomp[R + cg.JK]) e0 += (double)fw0[fr];
-                        }
-                        if (j + 1 < f.J) {
-                            long long nb = fr + f.K;
-                            if (b == 0) { if (fcomp[nb] == own) dg -= 2.0 * (double)fw1[fr]; }
-                            else if (J + 1 < cg.J && fcomp[nb] == ccomp[R + cg.K]) e1 += (double)fw1[fr];
-                        }
-                        if (k + 1 < f.K) {
-                            long long nb = fr + 1;
-                            if (c == 0) { if (fcomp[nb] == own) dg -= 2.0 * (double)fw2[fr]; }
-                            else if (K + 1 < cg.K && fcomp[nb] == ccomp[R + 1]) e2 += (double)fw2[fr];
+                        ex += (double)fe[fr];
+                        // the six links of this member
+                        const int di[6] = {1, -1, 0, 0, 0, 0}, dj[6] = {0, 0, 1, -1, 0, 0},
+                                  dk[6] = {0, 0, 0, 0, 1, -1};
+                        for (int d = 0; d < 6; ++d) {
+                            int ni = i + di[d], nj = j + dj[d], nk = k + dk[d];
+                            if (ni < 0 || nj < 0 || nk < 0 || ni >= f.I || nj >= f.J || nk >= f.K) continue;
+                            long long nr = lidx(f, ni, nj, nk);
+                            double cl;
+                            switch (d) {
+                            case 0: cl = (double)f0[fr]; break;
+                            case 1: cl = (double)f0[nr]; break;
+                            case 2: cl = (double)f1[fr]; break;
+                            case 3: cl = (double)f1[nr]; break;
+                            case 4: cl = (double)f2[fr]; break;
+                            default: cl = (double)f2[nr]; break;
+                            }
+                            if (cl == 0.0) continue;
+                            bool nmem = is_member(f, cg, fcomp, ccomp, ni, nj, nk);
+                            bool same_block = (ni >> 1) == I && (nj >> 1) == J && (nk >> 1) == K;
+                            if (!nmem) { ex += cl; continue; }  // P = 0 on the other end
+                            if (same_block) continue;           // internal link
+                            // member of another block: a coarse link (stored on + faces)
+                            if (d == 0) e0 += cl;
+                            else if (d == 2) e1 += cl;
+                            else if (d == 4) e2 += cl;
                         }
                     }
         }
-        // the coarse neighbour must also be a live cell
-        if (own < 0) { e0 = e1 = e2 = 0.0; dg = 1.0; }
-        cdiag[R] = (T)dg;
-        cw0[R] = (T)e0;
-        cw1[R] = (T)e1;
-        cw2[R] = (T)e2;
+        ce[R] = (T)(own >= 0 ? ex : 1.0);
+        c0[R] = (T)e0;
+        c1[R] = (T)e1;
+        c2[R] = (T)e2;
     }
 }
 
 // ---------------------------------------------------------------------------
 // V-cycle kernels
 
+// x_out = x + omega invd (b - M x); x == nullptr means x = 0. With dotv, the per-block
+// partial of (dotv, x_out) is stored (the (r, z) of the PCG).
 template <typename T>
-__device__ __forceinline__ T offsum(const Grid& g, long long r, int i, int j, int k,
-                                    const T* __restrict__ v, const T* __restrict__ w0,
-                                    const T* __restrict__ w1, const T* __restrict__ w2) {
-    T acc = (T)0;
-    if (i > 0) acc += w0[r - g.JK] * v[r - g.JK];
-    if (j > 0) acc += w1[r - g.K] * v[r - g.K];
-    if (k > 0) acc += w2[r - 1] * v[r - 1];
-    if (k + 1 < g.K) acc += w2[r] * v[r + 1];
-    if (j + 1 < g.J) acc += w1[r] * v[r + g.K];
-    if (i + 1 < g.I) acc += w0[r] * v[r + g.JK];
-    return acc;
-}
-
-// x_out = x + omega D^-1 (b - (D x - L x)); x == nullptr means x = 0.
-// When dot != nullptr the per-block partial of (dotv, x_out) is stored (for (r, z)).
-template <typename T>
-__global__ void __launch_bounds__(kBlock) k_mg_smooth(Grid g, const int* __restrict__ comp,
-                                                      const T* __restrict__ diag,
-                                                      const T* __restrict__ w0,
-                                                      const T* __restrict__ w1,
-                                                      const T* __restrict__ w2,
-                                                      const T* __restrict__ b,
-                                                      const T* __restrict__ x,
-                                                      T* __restrict__ xo,
-                                                      const T* __restrict__ dotv,
+__global__ void __launch_bounds__(kBlock) k_mg_smooth(Grid g, const int* __restrict__ comp, const T* __restrict__ e,
+                                                      const T* __restrict__ f0, const T* __restrict__ f1,
+                                                      const T* __restrict__ f2, const T* __restrict__ invd,
+                                                      const T* __restrict__ b, const T* __restrict__ x,
+                                                      T* __restrict__ xo, const T* __restrict__ dotv,
                                                       double* __restrict__ partials) {
-    double acc[1] = {0.0};
+    T acc = (T)0;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
         T out = (T)0;
@@ -206,38 +252,33 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth(Grid g, const int* __restr
             if (x) {
                 int i, j, k;
                 decode(g, r, i, j, k);
-                T xv = x[r];
-                if (diag) {
-                    T dg = diag[r];
-                    T res = bv - (dg * xv - offsum(g, r, i, j, k, x, w0, w1, w2));
-                    out = xv + (T)kOmega * res / dg;
-                } else {  // unit diagonal (finest level)
-                    T res = bv - (xv - offsum(g, r, i, j, k, x, w0, w1, w2));
-                    out = xv + (T)kOmega * res;
-                }
+                T res = bv - m_apply(g, r, i, j, k, e, f0, f1, f2, x);
+                out = x[r] + (T)kOmega * invd[r] * res;
             } else {
-                out = diag ? (T)kOmega * bv / diag[r] : (T)kOmega * bv;
+                out = (T)kOmega * invd[r] * bv;
             }
         }
         xo[r] = out;
-        if (dotv) acc[0] += (double)dotv[r] * (double)out;
+        if (dotv) acc += dotv[r] * out;
     }
-    if (dotv) block_sum_store<1>(acc, partials);
+    if (dotv) {
+        double a[1] = {(double)acc};
+        block_sum_store<1>(a, partials);
+    }
 }
 
-// coarse right-hand side: b_c(R) = sum over owned members of (b - W x)
+// coarse right-hand side: b_c(R) = sum over owned members of (b - M x)
 template <typename T>
-__global__ void k_mg_restrict(Grid f, Grid cg, const int* __restrict__ fcomp,
-                              const int* __restrict__ ccomp, const T* __restrict__ fdiag,
-                              const T* __restrict__ w0, const T* __restrict__ w1,
-                              const T* __restrict__ w2, const T* __restrict__ fb,
-                              const T* __restrict__ fx, T* __restrict__ cb) {
+__global__ void k_mg_restrict(Grid f, Grid cg, const int* __restrict__ fcomp, const int* __restrict__ ccomp,
+                              const T* __restrict__ e, const T* __restrict__ f0, const T* __restrict__ f1,
+                              const T* __restrict__ f2, const T* __restrict__ fb, const T* __restrict__ fx,
+                              T* __restrict__ cb) {
     for (long long R = blockIdx.x * (long long)blockDim.x + threadIdx.x; R < cg.N;
          R += (long long)gridDim.x * blockDim.x) {
         int I, J, K;
         decode(cg, R, I, J, K);
         const int own = ccomp[R];
-        double acc = 0.0;
+        T acc = (T)0;
         if (own >= 0) {
             for (int a = 0; a < 2; ++a)
                 for (int b = 0; b < 2; ++b)
@@ -246,20 +287,17 @@ __global__ void k_mg_restrict(Grid f, Grid cg, const int* __restrict__ fcomp,
                         if (i >= f.I || j >= f.J || k >= f.K) continue;
                         long long fr = lidx(f, i, j, k);
                         if (fcomp[fr] != own) continue;
-                        T dg = fdiag ? fdiag[fr] : (T)1;
-                        T res = fb[fr] - (dg * fx[fr] - offsum(f, fr, i, j, k, fx, w0, w1, w2));
-                        acc += (double)res;
+                        acc += fb[fr] - m_apply(f, fr, i, j, k, e, f0, f1, f2, fx);
                     }
         }
-        cb[R] = (T)acc;
+        cb[R] = acc;
     }
 }
 
 // x_f += x_c(block) for owned members
 template <typename T>
-__global__ void k_mg_prolong(Grid f, Grid cg, const int* __restrict__ fcomp,
-                             const int* __restrict__ ccomp, const T* __restrict__ cx,
-                             T* __restrict__ fx) {
+__global__ void k_mg_prolong(Grid f, Grid cg, const int* __restrict__ fcomp, const int* __restrict__ ccomp,
+                             const T* __restrict__ cx, T* __restrict__ fx) {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < f.N;
          r += (long long)gridDim.x * blockDim.x) {
         int id = fcomp[r];
@@ -271,14 +309,13 @@ __global__ void k_mg_prolong(Grid f, Grid cg, const int* __restrict__ fcomp,
     }
 }
 
-// coarsest level: fixed number of damped Jacobi sweeps from zero by one CTA
+// coarsest level: a fixed number of damped Jacobi sweeps from zero by one CTA
 template <typename T>
-__global__ void k_mg_coarsest(Grid g, const int* __restrict__ comp, const T* __restrict__ diag,
-                              const T* __restrict__ w0, const T* __restrict__ w1,
-                              const T* __restrict__ w2, const T* __restrict__ b, T* x, T* t,
-                              int sweeps) {
+__global__ void k_mg_coarsest(Grid g, const int* __restrict__ comp, const T* __restrict__ e,
+                              const T* __restrict__ f0, const T* __restrict__ f1, const T* __restrict__ f2,
+                              const T* __restrict__ invd, const T* __restrict__ b, T* x, T* t, int sweeps) {
     for (long long r = threadIdx.x; r < g.N; r += blockDim.x)
-        x[r] = (comp[r] >= 0) ? (T)kOmega * b[r] / diag[r] : (T)0;
+        x[r] = (comp[r] >= 0) ? (T)kOmega * invd[r] * b[r] : (T)0;
     __syncthreads();
     for (int s = 1; s < sweeps; ++s) {
         for (long long r = threadIdx.x; r < g.N; r += blockDim.x) {
@@ -286,9 +323,8 @@ __global__ void k_mg_coarsest(Grid g, const int* __restrict__ comp, const T* __r
             if (comp[r] >= 0) {
                 int i, j, k;
                 decode(g, r, i, j, k);
-                T dg = diag[r];
-                T res = b[r] - (dg * x[r] - offsum(g, r, i, j, k, x, w0, w1, w2));
-                out = x[r] + (T)kOmega * res / dg;
+                T res = b[r] - m_apply(g, r, i, j, k, e, f0, f1, f2, x);
+                out = x[r] + (T)kOmega * invd[r] * res;
             }
             t[r] = out;
         }
@@ -311,38 +347,37 @@ static Grid coarse_of(const Grid& f) {
     return c;
 }
 
-template <typename T>
-static ls_status mg_alloc(ls_ctx* c) {
-    const int is64 = sizeof(T) == 8;
-    if (!c->mg.empty() && c->mg_is64 == is64) return LS_OK;
+void mg_free(ls_ctx* c) {
     for (auto& lv : c->mg) {
-        void* lp[] = {lv.comp, lv.diag, lv.face[0], lv.face[1], lv.face[2], lv.x, lv.b, lv.t};
+        void* lp[] = {lv.comp, lv.e, lv.face[0], lv.face[1], lv.face[2], lv.invd, lv.x, lv.b, lv.t};
         for (void* q : lp)
             if (q) cudaFree(q);
     }
     c->mg.clear();
+    if (c->mg0_x) cudaFree(c->mg0_x);
+    if (c->mg0_t) cudaFree(c->mg0_t);
+    c->mg0_x = c->mg0_t = nullptr;
+    c->mg_is64 = -1;
+}
+
+template <typename T>
+static ls_status mg_alloc(ls_ctx* c) {
+    const int is64 = sizeof(T) == 8;
+    if (c->mg_is64 == is64) return LS_OK;
+    mg_free(c);
     if (!c->comp) LS_TRY(dalloc_t(c, &c->comp, (size_t)c->g.N));
     if (!c->cc_flag) LS_TRY(dalloc_t(c, &c->cc_flag, (size_t)4));
-    // level 0 is the fine grid itself: comp = c->comp, unit diagonal, weights w32/w64; its
-    // x/b/t vectors are allocated here
-    ls_ctx::MGLevel l0 = {};
-    l0.g = c->g;
-    l0.g.NP = l0.g.N;
-    l0.comp = c->comp;
-    LS_TRY(dalloc(c, &l0.x, sizeof(T) * (size_t)l0.g.N));
-    LS_TRY(dalloc(c, &l0.t, sizeof(T) * (size_t)l0.g.N));
-    c->mg.push_back(l0);
+    LS_TRY(dalloc(c, &c->mg0_x, sizeof(T) * (size_t)c->g.N));
+    LS_TRY(dalloc(c, &c->mg0_t, sizeof(T) * (size_t)c->g.N));
     Grid g = c->g;
-    while ((c->mg.size() < 2 || g.N > kCoarsestCells) && (g.I > 1 || g.J > 1 || g.K > 1)) {
+    g.NP = g.N;
+    while ((c->mg.empty() || g.N > kCoarsestCells) && (g.I > 1 || g.J > 1 || g.K > 1)) {
         Grid cg = coarse_of(g);
         ls_ctx::MGLevel lv = {};
         lv.g = cg;
         LS_TRY(dalloc_t(c, &lv.comp, (size_t)cg.N));
-        LS_TRY(dalloc(c, &lv.diag, sizeof(T) * (size_t)cg.N));
-        for (int d = 0; d < 3; ++d) LS_TRY(dalloc(c, &lv.face[d], sizeof(T) * (size_t)cg.N));
-        LS_TRY(dalloc(c, &lv.x, sizeof(T) * (size_t)cg.N));
-        LS_TRY(dalloc(c, &lv.b, sizeof(T) * (size_t)cg.N));
-        LS_TRY(dalloc(c, &lv.t, sizeof(T) * (size_t)cg.N));
+        void** arrs[] = {&lv.e, &lv.face[0], &lv.face[1], &lv.face[2], &lv.invd, &lv.x, &lv.b, &lv.t};
+        for (void** q : arrs) LS_TRY(dalloc(c, q, sizeof(T) * (size_t)cg.N));
         c->mg.push_back(lv);
         g = cg;
     }
@@ -350,28 +385,46 @@ static ls_status mg_alloc(ls_ctx* c) {
     return LS_OK;
 }
 
-// Build components and coarse operators for the current fine weights.
+// 1/diagonal of the finest inner operator (rows of kind 2 live)
 template <typename T>
-ls_status mg_setup(ls_ctx* c, T* const* w) {
+ls_status inner_invd(ls_ctx* c) {
+    LS_LAUNCH(c, k_level_invd<T>, grid_for(c, c->g.N), kBlock, 0, c->g, (const int*)nullptr,
+              (const int8_t*)c->pkind, (const T*)c->ie, (const T*)c->iface[0], (const T*)c->iface[1],
+              (const T*)c->iface[2], (T*)c->iinvd);
+    return LS_OK;
+}
+
+// Components and coarse operators for the current fine inner operator (c->ie, c->iface,
+// c->iinvd, precision T).
+template <typename T>
+ls_status mg_setup(ls_ctx* c) {
     LS_TRY(mg_alloc<T>(c));
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
     LS_CUDA(c, cudaMemsetAsync(c->cc_flag, 0, sizeof(int), c->stream));
-    LS_LAUNCH(c, k_cc_init, grid, kBlock, 0, g, (const double*)c->pisd, c->comp);
-    LS_LAUNCH(c, k_cc_hook<T>, grid, kBlock, 0, g, (const T*)w[0], (const T*)w[1], (const T*)w[2],
-              c->comp, c->cc_flag);
+    LS_LAUNCH(c, k_cc_init, grid, kBlock, 0, g, (const int8_t*)c->pkind, c->comp);
+    LS_LAUNCH(c, k_cc_hook<T>, grid, kBlock, 0, g, (const T*)c->iface[0], (const T*)c->iface[1],
+              (const T*)c->iface[2], (const T*)c->iinvd, c->comp, c->cc_flag);
     LS_LAUNCH(c, k_cc_compress, grid, kBlock, 0, g, c->comp);
-    c->mg[0].face[0] = w[0];
-    c->mg[0].face[1] = w[1];
-    c->mg[0].face[2] = w[2];
-    for (size_t l = 1; l < c->mg.size(); ++l) {
-        auto& f = c->mg[l - 1];
+    Grid fg = g;
+    const int* fcomp = c->comp;
+    const T* fe = (const T*)c->ie;
+    const T* ff[3] = {(const T*)c->iface[0], (const T*)c->iface[1], (const T*)c->iface[2]};
+    for (size_t l = 0; l < c->mg.size(); ++l) {
         auto& cl = c->mg[l];
         const int cgd = grid_for(c, cl.g.N);
-        LS_LAUNCH(c, k_mg_dom, cgd, kBlock, 0, f.g, cl.g, (const int*)f.comp, cl.comp);
-        LS_LAUNCH(c, k_mg_coarse_op<T>, cgd, kBlock, 0, f.g, cl.g, (const int*)f.comp,
-                  (const int*)cl.comp, (const T*)f.diag, (const T*)f.face[0], (const T*)f.face[1],
-                  (const T*)f.face[2], (T*)cl.diag, (T*)cl.face[0], (T*)cl.face[1], (T*)cl.face[2]);
+        LS_LAUNCH(c, k_mg_dom, cgd, kBlock, 0, fg, cl.g, fcomp, cl.comp);
+        LS_LAUNCH(c, k_mg_coarse_op<T>, cgd, kBlock, 0, fg, cl.g, fcomp, (const int*)cl.comp, fe, ff[0], ff[1],
+                  ff[2], (T*)cl.e, (T*)cl.face[0], (T*)cl.face[1], (T*)cl.face[2]);
+        LS_LAUNCH(c, k_level_invd<T>, cgd, kBlock, 0, cl.g, (const int*)cl.comp, (const int8_t*)nullptr,
+                  (const T*)cl.e, (const T*)cl.face[0], (const T*)cl.face[1], (const T*)cl.face[2],
+                  (T*)cl.invd);
+        fg = cl.g;
+        fcomp = cl.comp;
+        fe = (const T*)cl.e;
+        ff[0] = (const T*)cl.face[0];
+        ff[1] = (const T*)cl.face[1];
+        ff[2] = (const T*)cl.face[2];
     }
     int flag = 0;
     LS_CUDA(c, cudaMemcpyAsync(&flag, c->cc_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -380,60 +433,66 @@ ls_status mg_setup(ls_ctx* c, T* const* w) {
     return LS_OK;
 }
 
-// z = B r (one V-cycle); the partial sums of (r, z) are left in c->partials for the caller.
+// z = B r (one V-cycle); the per-block partials of (r, z) are left in c->partials and
+// their count in *nblocks_out.
 template <typename T>
 ls_status mg_apply(ls_ctx* c, const T* r, T* z, int* nblocks_out) {
-    const size_t L = c->mg.size();
-    // descending leg: level l solves W_l e = b_l; b_0 = r
-    for (size_t l = 0; l + 1 < L; ++l) {
-        auto& lv = c->mg[l];
-        const T* b = (l == 0) ? r : (const T*)lv.b;
-        T* x = (T*)lv.x;
-        T* t = (T*)lv.t;
-        const int gd = grid_for(c, lv.g.N);
-        // nu sweeps from zero, ending in x
-        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, lv.g, (const int*)lv.comp, (const T*)lv.diag,
-                  (const T*)lv.face[0], (const T*)lv.face[1], (const T*)lv.face[2], b, (const T*)nullptr,
-                  t, (const T*)nullptr, (double*)nullptr);
-        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, lv.g, (const int*)lv.comp, (const T*)lv.diag,
-                  (const T*)lv.face[0], (const T*)lv.face[1], (const T*)lv.face[2], b, (const T*)t,
-                  x, (const T*)nullptr, (double*)nullptr);
-        auto& cl = c->mg[l + 1];
-        LS_LAUNCH(c, k_mg_restrict<T>, grid_for(c, cl.g.N), kBlock, 0, lv.g, cl.g,
-                  (const int*)lv.comp, (const int*)cl.comp, (const T*)lv.diag, (const T*)lv.face[0],
-                  (const T*)lv.face[1], (const T*)lv.face[2], b, (const T*)x, (T*)cl.b);
+    const size_t L = c->mg.size();  // coarse levels
+    if (L == 0) return set_error(c, LS_BAD_ARG, "multigrid hierarchy missing");
+    struct Lv {
+        Grid g;
+        const int* comp;
+        const T *e, *f0, *f1, *f2, *invd;
+        T *x, *b, *t;
+    };
+    std::vector<Lv> lv(L + 1);
+    lv[0] = {c->g, c->comp, (const T*)c->ie, (const T*)c->iface[0], (const T*)c->iface[1], (const T*)c->iface[2],
+             (const T*)c->iinvd, (T*)c->mg0_x, nullptr, (T*)c->mg0_t};
+    for (size_t l = 0; l < L; ++l) {
+        auto& m = c->mg[l];
+        lv[l + 1] = {m.g, m.comp, (const T*)m.e, (const T*)m.face[0], (const T*)m.face[1], (const T*)m.face[2],
+                     (const T*)m.invd, (T*)m.x, (T*)m.b, (T*)m.t};
+    }
+    // descending leg
+    for (size_t l = 0; l < L; ++l) {
+        Lv& a = lv[l];
+        Lv& cl = lv[l + 1];
+        const T* b = (l == 0) ? r : a.b;
+        const int gd = grid_for(c, a.g.N);
+        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, a.invd, b,
+                  (const T*)nullptr, a.t, (const T*)nullptr, (double*)nullptr);
+        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, a.invd, b,
+                  (const T*)a.t, a.x, (const T*)nullptr, (double*)nullptr);
+        LS_LAUNCH(c, k_mg_restrict<T>, grid_for(c, cl.g.N), kBlock, 0, a.g, cl.g, a.comp, cl.comp, a.e, a.f0,
+                  a.f1, a.f2, b, (const T*)a.x, cl.b);
     }
     {
-        auto& lv = c->mg[L - 1];
-        if (L == 1) return set_error(c, LS_BAD_ARG, "multigrid needs at least two levels");
-        LS_LAUNCH(c, k_mg_coarsest<T>, 1, 1024, 0, lv.g, (const int*)lv.comp, (const T*)lv.diag,
-                  (const T*)lv.face[0], (const T*)lv.face[1], (const T*)lv.face[2],
-                  (const T*)lv.b, (T*)lv.x, (T*)lv.t, kCoarseSweeps);
+        Lv& a = lv[L];
+        LS_LAUNCH(c, k_mg_coarsest<T>, 1, 1024, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, a.invd,
+                  (const T*)a.b, a.x, a.t, kCoarseSweeps);
     }
     // ascending leg
-    for (size_t l = L - 1; l-- > 0;) {
-        auto& lv = c->mg[l];
-        auto& cl = c->mg[l + 1];
-        const T* b = (l == 0) ? r : (const T*)lv.b;
-        T* x = (T*)lv.x;
-        T* t = (T*)lv.t;
-        const int gd = grid_for(c, lv.g.N);
-        LS_LAUNCH(c, k_mg_prolong<T>, gd, kBlock, 0, lv.g, cl.g, (const int*)lv.comp,
-                  (const int*)cl.comp, (const T*)cl.x, x);
-        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, lv.g, (const int*)lv.comp, (const T*)lv.diag,
-                  (const T*)lv.face[0], (const T*)lv.face[1], (const T*)lv.face[2], b, (const T*)x,
-                  t, (const T*)nullptr, (double*)nullptr);
-        T* out = (l == 0) ? z : x;
-        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, lv.g, (const int*)lv.comp, (const T*)lv.diag,
-                  (const T*)lv.face[0], (const T*)lv.face[1], (const T*)lv.face[2], b, (const T*)t,
-                  out, (l == 0) ? r : (const T*)nullptr, (l == 0) ? c->partials : (double*)nullptr);
+    for (size_t l = L; l-- > 0;) {
+        Lv& a = lv[l];
+        Lv& cl = lv[l + 1];
+        const T* b = (l == 0) ? r : a.b;
+        const int gd = grid_for(c, a.g.N);
+        LS_LAUNCH(c, k_mg_prolong<T>, gd, kBlock, 0, a.g, cl.g, a.comp, cl.comp, (const T*)cl.x, a.x);
+        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, a.invd, b,
+                  (const T*)a.x, a.t, (const T*)nullptr, (double*)nullptr);
+        T* out = (l == 0) ? z : a.x;
+        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, a.invd, b,
+                  (const T*)a.t, out, (l == 0) ? r : (const T*)nullptr,
+                  (l == 0) ? c->partials : (double*)nullptr);
         if (l == 0 && nblocks_out) *nblocks_out = gd;
     }
     return LS_OK;
 }
 
-template ls_status mg_setup<float>(ls_ctx*, float* const*);
-template ls_status mg_setup<double>(ls_ctx*, double* const*);
+template ls_status inner_invd<float>(ls_ctx*);
+template ls_status inner_invd<double>(ls_ctx*);
+template ls_status mg_setup<float>(ls_ctx*);
+template ls_status mg_setup<double>(ls_ctx*);
 template ls_status mg_apply<float>(ls_ctx*, const float*, float*, int*);
 template ls_status mg_apply<double>(ls_ctx*, const double*, double*, int*);
 

@@ -12,8 +12,11 @@
 // Solver: FP64 iterative refinement on the assembled operator A. Each sweep computes
 // r = b - A x in FP64 and the correction from a block-triangular splitting: floored
 // rows (kind 3) are solved from their diagonal, the normal Pore rows (kind 2) from the
-// symmetric positive definite system M d = A_SQ d_Q - r_S with M = -A_SS, Jacobi-scaled
-// to unit diagonal and solved by an inner PCG in FP32 (LS_PRESS_MIXED) or FP64.
+// symmetric positive definite system M d = A_SQ d_Q - r_S with M = -A_SS, solved by an
+// inner PCG in FP32 (LS_PRESS_MIXED) or FP64, preconditioned by multigrid (or Jacobi for
+// LS_PRESS_JACOBI64). M is scaled by sigma = 1/max(diagonal) and held as
+// e_i x_i + sum_links c_ij (x_i - x_j) with e_i = links to rows that are not unknowns,
+// which stays positive definite under FP32 rounding.
 // Convergence is judged on the FP64 Jacobi-scaled residual ||D^-1 r|| / ||D^-1 b||, the
 // norm PETSc's left-Jacobi GMRES tests in the reference.
 #include <algorithm>
@@ -26,9 +29,11 @@
 namespace ls {
 
 template <typename T>
-ls_status mg_setup(ls_ctx* c, T* const* w);
+ls_status mg_setup(ls_ctx* c);
 template <typename T>
 ls_status mg_apply(ls_ctx* c, const T* r, T* z, int* nblocks_out);
+template <typename T>
+ls_status inner_invd(ls_ctx* c);
 
 // scalar slots
 enum {
@@ -168,26 +173,43 @@ __global__ void k_press_isd(Grid g, const int8_t* __restrict__ kind, const doubl
         isd[r] = (kind[r] == 2) ? 1.0 / sqrt(-diag[r]) : 0.0;
 }
 
-// Jacobi-scaled inner weights w = c / sqrt(d_a d_b) between two inner unknowns.
+// largest diagonal magnitude of the normal Pore rows (for the inner scaling sigma)
+__global__ void __launch_bounds__(kBlock) k_press_maxd(Grid g, const int8_t* __restrict__ kind,
+                                                       const double* __restrict__ diag,
+                                                       double* __restrict__ partials) {
+    double m[1] = {0.0};
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x)
+        if (kind[r] == 2) m[0] = smax(m[0], -diag[r]);
+    block_max_store<1>(m, partials);
+}
+
+// Inner operator sigma*M in excess + Laplacian form: e_i = sigma * (links of row i to rows
+// that are not normal Pore rows), face c = sigma * link between two normal Pore rows.
+// Rows that are not unknowns get e = 1 and no links.
 template <typename T>
-__global__ void k_press_weights(Grid g, const double* __restrict__ isd,
-                                const double* __restrict__ f0, const double* __restrict__ f1,
-                                const double* __restrict__ f2, T* __restrict__ w0,
-                                T* __restrict__ w1, T* __restrict__ w2) {
+__global__ void k_inner_setup(Grid g, double sigma, const int8_t* __restrict__ kind,
+                              const double* __restrict__ f0, const double* __restrict__ f1,
+                              const double* __restrict__ f2, T* __restrict__ e, T* __restrict__ o0,
+                              T* __restrict__ o1, T* __restrict__ o2) {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         decode(g, r, i, j, k);
-        double a = isd[r];
-        double v0 = 0.0, v1 = 0.0, v2 = 0.0;
-        if (a != 0.0) {
-            if (i + 1 < g.I) v0 = f0[r] * a * isd[r + g.JK];
-            if (j + 1 < g.J) v1 = f1[r] * a * isd[r + g.K];
-            if (k + 1 < g.K) v2 = f2[r] * a * isd[r + 1];
+        const bool u = kind[r] == 2;
+        double ex = 0.0;
+        if (u) {
+            if (i > 0 && kind[r - g.JK] != 2) ex += f0[r - g.JK];
+            if (j > 0 && kind[r - g.K] != 2) ex += f1[r - g.K];
+            if (k > 0 && kind[r - 1] != 2) ex += f2[r - 1];
+            if (k + 1 < g.K && kind[r + 1] != 2) ex += f2[r];
+            if (j + 1 < g.J && kind[r + g.K] != 2) ex += f1[r];
+            if (i + 1 < g.I && kind[r + g.JK] != 2) ex += f0[r];
         }
-        w0[r] = (T)v0;
-        w1[r] = (T)v1;
-        w2[r] = (T)v2;
+        e[r] = u ? (T)(sigma * ex) : (T)1;
+        o0[r] = (u && i + 1 < g.I && kind[r + g.JK] == 2) ? (T)(sigma * f0[r]) : (T)0;
+        o1[r] = (u && j + 1 < g.J && kind[r + g.K] == 2) ? (T)(sigma * f1[r]) : (T)0;
+        o2[r] = (u && k + 1 < g.K && kind[r + 1] == 2) ? (T)(sigma * f2[r]) : (T)0;
     }
 }
 
@@ -274,11 +296,11 @@ __global__ void __launch_bounds__(kBlock) k_press_residual(Grid g, const int8_t*
     (void)nblk;
 }
 
-// Correction for floored rows and the scaled inner right-hand side
-//   d_Q = r_Q / diag_Q,  g = D^-1/2 (A_SQ d_Q - r_S).
+// Correction for floored rows and the inner right-hand side
+//   d_Q = r_Q / diag_Q,  g = sigma (A_SQ d_Q - r_S).
 template <typename T>
-__global__ void k_press_inner_rhs(Grid g, const int8_t* __restrict__ kind,
-                                  const double* __restrict__ diag, const double* __restrict__ isd,
+__global__ void k_press_inner_rhs(Grid g, double sigma, const int8_t* __restrict__ kind,
+                                  const double* __restrict__ diag,
                                   const double* __restrict__ res, const double* __restrict__ f0,
                                   const double* __restrict__ f1, const double* __restrict__ f2,
                                   double* __restrict__ delta, T* __restrict__ rhs) {
@@ -299,45 +321,48 @@ __global__ void k_press_inner_rhs(Grid g, const int8_t* __restrict__ kind,
             if (k + 1 < g.K && kind[r + 1] == 3) acc += f2[r] * (res[r + 1] / diag[r + 1]);
             if (j + 1 < g.J && kind[r + g.K] == 3) acc += f1[r] * (res[r + g.K] / diag[r + g.K]);
             if (i + 1 < g.I && kind[r + g.JK] == 3) acc += f0[r] * (res[r + g.JK] / diag[r + g.JK]);
-            gv = (T)(isd[r] * (acc - res[r]));
+            gv = (T)(sigma * (acc - res[r]));
         }
         rhs[r] = gv;
     }
 }
 
-// x += delta (floored rows) and x += D^-1/2 * inner solution (normal Pore rows), FP64.
+// x += delta (floored rows) and x += inner solution (normal Pore rows), FP64.
 template <typename T>
 __global__ void k_press_accumulate(Grid g, const int8_t* __restrict__ kind,
-                                   const double* __restrict__ isd, const double* __restrict__ delta,
-                                   const T* __restrict__ xin, double* __restrict__ x) {
+                                   const double* __restrict__ delta, const T* __restrict__ xin,
+                                   double* __restrict__ x) {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
         int kd = kind[r];
         if (kd == 3) x[r] += delta[r];
-        else if (kd == 2) x[r] += isd[r] * (double)xin[r];
+        else if (kd == 2) x[r] += (double)xin[r];
     }
 }
 
 // ---------------------------------------------------------------------------
-// inner PCG on W = I - L (unit diagonal, L = scaled links between inner unknowns)
+// inner PCG on sigma*M (excess + Laplacian form)
 
 template <typename T>
 __device__ __forceinline__ T inner_apply_row(const Grid& g, long long r, int i, int j, int k,
-                                             const T* __restrict__ v, const T* __restrict__ w0,
-                                             const T* __restrict__ w1, const T* __restrict__ w2) {
-    T acc = (T)0;
-    if (i > 0) acc += w0[r - g.JK] * v[r - g.JK];
-    if (j > 0) acc += w1[r - g.K] * v[r - g.K];
-    if (k > 0) acc += w2[r - 1] * v[r - 1];
-    if (k + 1 < g.K) acc += w2[r] * v[r + 1];
-    if (j + 1 < g.J) acc += w1[r] * v[r + g.K];
-    if (i + 1 < g.I) acc += w0[r] * v[r + g.JK];
-    return v[r] - acc;
+                                             const T* __restrict__ v, const T* __restrict__ e,
+                                             const T* __restrict__ w0, const T* __restrict__ w1,
+                                             const T* __restrict__ w2) {
+    const T vr = v[r];
+    T acc = e[r] * vr;
+    if (i > 0) acc += w0[r - g.JK] * (vr - v[r - g.JK]);
+    if (j > 0) acc += w1[r - g.K] * (vr - v[r - g.K]);
+    if (k > 0) acc += w2[r - 1] * (vr - v[r - 1]);
+    if (k + 1 < g.K) acc += w2[r] * (vr - v[r + 1]);
+    if (j + 1 < g.J) acc += w1[r] * (vr - v[r + g.K]);
+    if (i + 1 < g.I) acc += w0[r] * (vr - v[r + g.JK]);
+    return acc;
 }
 
-// q = W p, partial (p, q)
+// q = M p, partial (p, q)
 template <typename T>
 __global__ void __launch_bounds__(kBlock) k_cg_apply(Grid g, const T* __restrict__ p,
+                                                     const T* __restrict__ e,
                                                      const T* __restrict__ w0,
                                                      const T* __restrict__ w1,
                                                      const T* __restrict__ w2, T* __restrict__ q,
@@ -347,7 +372,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_apply(Grid g, const T* __restrict
          r += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         decode(g, r, i, j, k);
-        T qv = inner_apply_row(g, r, i, j, k, p, w0, w1, w2);
+        T qv = inner_apply_row(g, r, i, j, k, p, e, w0, w1, w2);
         q[r] = qv;
         a += p[r] * qv;
     }
@@ -355,27 +380,37 @@ __global__ void __launch_bounds__(kBlock) k_cg_apply(Grid g, const T* __restrict
     block_sum_store<1>(acc, partials);
 }
 
-// x += a p, r -= a q with a = (r,z)/(p,q); Jacobi-scaled system: z = r. partial (r, r).
+// x += a p, r -= a q with a = (r,z)/(p,q) (0 when (p,q) <= 0)
 template <typename T>
-__global__ void __launch_bounds__(kBlock) k_cg_update(Grid g, const double* __restrict__ scal,
-                                                      const T* __restrict__ p,
-                                                      const T* __restrict__ q, T* __restrict__ x,
-                                                      T* __restrict__ r_, double* __restrict__ partials) {
-    const double alpha = scal[SP_RZ] / scal[SP_PQ];
-    const T a = (T)alpha;
-    T s = (T)0;
+__global__ void k_cg_update(Grid g, const double* __restrict__ scal, const T* __restrict__ p,
+                            const T* __restrict__ q, T* __restrict__ x, T* __restrict__ r_) {
+    const double pq = scal[SP_PQ];
+    const T a = (T)((pq > 0.0) ? scal[SP_RZ] / pq : 0.0);
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
         x[r] += a * p[r];
-        T rv = r_[r] - a * q[r];
-        r_[r] = rv;
-        s += rv * rv;
+        r_[r] -= a * q[r];
     }
-    double acc[1] = {(double)s};
+}
+
+// Jacobi preconditioner: z = r / diag, partial (r, z)
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_cg_jacobi(Grid g, const T* __restrict__ invd,
+                                                      const T* __restrict__ r_, T* __restrict__ z,
+                                                      double* __restrict__ partials) {
+    T a = (T)0;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        T rv = r_[r];
+        T zv = invd[r] * rv;
+        z[r] = zv;
+        a += rv * zv;
+    }
+    double acc[1] = {(double)a};
     block_sum_store<1>(acc, partials);
 }
 
-// p = z + b p with b = (r,z)_new / (r,z)_old; z = r here.
+// p = z + b p with b = (r,z)_new / (r,z)_old
 template <typename T>
 __global__ void k_cg_dir(Grid g, const double* __restrict__ scal, const T* __restrict__ z,
                          T* __restrict__ p) {
@@ -385,22 +420,7 @@ __global__ void k_cg_dir(Grid g, const double* __restrict__ scal, const T* __res
         p[r] = z[r] + beta * p[r];
 }
 
-template <typename T>
-__global__ void k_copy_dot(Grid g, const T* __restrict__ a, T* __restrict__ b, T* __restrict__ c,
-                           double* __restrict__ partials) {
-    double acc[1] = {0.0};
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x) {
-        T v = a[r];
-        b[r] = v;
-        if (c) c[r] = (T)0;
-        acc[0] += (double)v * (double)v;
-    }
-    block_sum_store<1>(acc, partials);
-}
-
-__global__ void k_set_scalar(double* scal, int dst, int src) { scal[dst] = scal[src]; }
-
+// p = z, x = 0
 template <typename T>
 __global__ void k_copy_zero(Grid g, const T* __restrict__ a, T* __restrict__ b, T* __restrict__ z) {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
@@ -410,82 +430,86 @@ __global__ void k_copy_zero(Grid g, const T* __restrict__ a, T* __restrict__ b, 
     }
 }
 
+__global__ void k_set_scalar(double* scal, int dst, int src) { scal[dst] = scal[src]; }
+
 template <typename T>
 static ls_status inner_alloc(ls_ctx* c) {
-    const bool is64 = sizeof(T) == 8;
-    if (c->inner[0] && c->inner_is64 == (int)is64) return LS_OK;
-    for (int q = 0; q < 5; ++q) {
-        if (c->inner[q]) { cudaFree(c->inner[q]); c->device_bytes -= sizeof(T) * (size_t)c->g.N; }
-        c->inner[q] = nullptr;
+    const int is64 = sizeof(T) == 8;
+    if (c->inner_is64 == is64) return LS_OK;
+    void** arrs[] = {&c->ie, &c->iface[0], &c->iface[1], &c->iface[2], &c->iinvd, &c->inner[0],
+                     &c->inner[1], &c->inner[2], &c->inner[3], &c->inner[4]};
+    const size_t old_bytes = (c->inner_is64 == 1 ? 8 : 4) * (size_t)c->g.N;
+    for (void** q : arrs) {
+        if (*q) { cudaFree(*q); c->device_bytes -= old_bytes; }
+        *q = nullptr;
     }
-    for (int q = 0; q < 5; ++q) LS_TRY(dalloc(c, &c->inner[q], sizeof(T) * (size_t)c->g.N));
+    c->inner_is64 = -1;
+    for (void** q : arrs) LS_TRY(dalloc(c, q, sizeof(T) * (size_t)c->g.N));
     c->inner_is64 = is64;
     return LS_OK;
 }
 
-// Inner PCG: solve W x = rhs (rhs held in inner[1] on entry) to relative residual tol,
-// preconditioned by one multigrid V-cycle (use_mg) or by the unit diagonal.
-// Returns the iterations used in *its.
+// Inner PCG: solve sigma*M x = rhs (rhs in inner[1] on entry) until the preconditioned
+// residual (r, z) has dropped by tol^2, preconditioned by one multigrid V-cycle (use_mg)
+// or by Jacobi. Returns the iterations used in *its.
 template <typename T>
-static ls_status inner_pcg(ls_ctx* c, T* const* w, bool use_mg, double tol, int max_it, int* its,
+static ls_status inner_pcg(ls_ctx* c, bool use_mg, double tol, int max_it, int* its,
                            double* rel_out) {
     T* x = (T*)c->inner[0];
     T* r = (T*)c->inner[1];
     T* z = (T*)c->inner[2];
     T* p = (T*)c->inner[3];
     T* q = (T*)c->inner[4];
+    const T* e = (const T*)c->ie;
+    const T* w0 = (const T*)c->iface[0];
+    const T* w1 = (const T*)c->iface[1];
+    const T* w2 = (const T*)c->iface[2];
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
-    // (r, r) for the stopping test, x = 0
-    LS_LAUNCH(c, k_copy_dot<T>, grid, kBlock, 0, g, (const T*)r, p, x, c->partials);
-    LS_TRY(finalize_sum(c, grid, 1, SP_RR0));
-    double rr0 = 0.0;
-    LS_TRY(read_scalars(c, SP_RR0, 1, &rr0));
-    *its = 0;
-    *rel_out = 0.0;
-    if (!(rr0 > 0.0)) {
-        if (rr0 != rr0) return set_error(c, LS_NONFINITE, "pressure: NaN in inner right-hand side");
-        return LS_OK;
-    }
-    if (use_mg) {
-        // z = B r, p = z, rz = (r, z)
-        int nb = 0;
-        LS_TRY(mg_apply<T>(c, (const T*)r, z, &nb));
-        LS_TRY(finalize_sum(c, nb, 1, SP_RZ));
-        LS_LAUNCH(c, k_copy_zero<T>, grid, kBlock, 0, g, (const T*)z, p, x);
-    } else {
-        LS_LAUNCH(c, k_set_scalar, 1, 1, 0, c->scal, SP_RZ, SP_RR0);
-    }
-    const double target = tol * tol * rr0;
-    double rr = rr0;
-    for (int it = 0; it < max_it; ++it) {
-        {
-            Timed tm(c, LS_T_CG_APPLY);
-            LS_LAUNCH(c, k_cg_apply<T>, grid, kBlock, 0, g, (const T*)p, (const T*)w[0],
-                      (const T*)w[1], (const T*)w[2], q, c->partials);
-            // p in, three own face weights, q out
-            if (c->timing) c->timer_bytes[LS_T_CG_APPLY] += (double)g.N * 5.0 * sizeof(T);
-        }
-        LS_TRY(finalize_sum(c, grid, 1, SP_PQ));
-        LS_LAUNCH(c, k_cg_update<T>, grid, kBlock, 0, g, (const double*)c->scal, (const T*)p,
-                  (const T*)q, x, r, c->partials);
-        LS_TRY(finalize_sum(c, grid, 1, SP_RR));
-        *its = it + 1;
-        LS_TRY(read_scalars(c, SP_RR, 1, &rr));
-        if (rr != rr) return set_error(c, LS_NONFINITE, "pressure: NaN in inner PCG");
-        if (rr <= target) break;
+    auto precondition = [&](int slot) -> ls_status {
         if (use_mg) {
             int nb = 0;
             LS_TRY(mg_apply<T>(c, (const T*)r, z, &nb));
-            LS_TRY(finalize_sum(c, nb, 1, SP_RZN));
-            LS_LAUNCH(c, k_cg_dir<T>, grid, kBlock, 0, g, (const double*)c->scal, (const T*)z, p);
-        } else {
-            LS_LAUNCH(c, k_set_scalar, 1, 1, 0, c->scal, SP_RZN, SP_RR);
-            LS_LAUNCH(c, k_cg_dir<T>, grid, kBlock, 0, g, (const double*)c->scal, (const T*)r, p);
+            return finalize_sum(c, nb, 1, slot);
         }
+        LS_LAUNCH(c, k_cg_jacobi<T>, grid, kBlock, 0, g, (const T*)c->iinvd, (const T*)r, z, c->partials);
+        return finalize_sum(c, grid, 1, slot);
+    };
+    *its = 0;
+    *rel_out = 0.0;
+    LS_TRY(precondition(SP_RZ));
+    double rz0 = 0.0;
+    LS_TRY(read_scalars(c, SP_RZ, 1, &rz0));
+    if (rz0 != rz0) return set_error(c, LS_NONFINITE, "pressure: NaN in the inner right-hand side");
+    if (!(rz0 > 0.0)) {
+        LS_CUDA(c, cudaMemsetAsync(x, 0, sizeof(T) * (size_t)g.N, c->stream));
+        return LS_OK;
+    }
+    LS_LAUNCH(c, k_copy_zero<T>, grid, kBlock, 0, g, (const T*)z, p, x);
+    const double target = tol * tol * rz0;
+    double rz = rz0;
+    for (int it = 0; it < max_it; ++it) {
+        {
+            Timed tm(c, LS_T_CG_APPLY);
+            LS_LAUNCH(c, k_cg_apply<T>, grid, kBlock, 0, g, (const T*)p, e, w0, w1, w2, q, c->partials);
+            // p in, excess and three own face links, q out
+            if (c->timing) c->timer_bytes[LS_T_CG_APPLY] += (double)g.N * 6.0 * sizeof(T);
+        }
+        LS_TRY(finalize_sum(c, grid, 1, SP_PQ));
+        LS_LAUNCH(c, k_cg_update<T>, grid, kBlock, 0, g, (const double*)c->scal, (const T*)p,
+                  (const T*)q, x, r);
+        LS_TRY(precondition(SP_RZN));
+        *its = it + 1;
+        double sc[3];
+        LS_TRY(read_scalars(c, SP_PQ, 2, sc));  // (p, q) and the new (r, z)
+        double pq = sc[0];
+        rz = sc[1];
+        if (rz != rz) return set_error(c, LS_NONFINITE, "pressure: NaN in inner PCG");
+        if (rz <= target || !(pq > 0.0) || rz < 0.0) break;
+        LS_LAUNCH(c, k_cg_dir<T>, grid, kBlock, 0, g, (const double*)c->scal, (const T*)z, p);
         LS_LAUNCH(c, k_set_scalar, 1, 1, 0, c->scal, SP_RZ, SP_RZN);
     }
-    *rel_out = sqrt(rr / rr0);
+    *rel_out = sqrt(std::max(rz, 0.0) / rz0);
     return LS_OK;
 }
 
@@ -534,36 +558,28 @@ ls_status pressure_apply_run(ls_ctx* c, const double* xh, double* yh) {
 }
 
 template <typename T>
-static ls_status ensure_weights(ls_ctx* c, T** w) {
-    const bool is64 = sizeof(T) == 8;
-    for (int d = 0; d < 3; ++d) {
-        void** slot = is64 ? (void**)&c->w64[d] : (void**)&c->w32[d];
-        if (!*slot) LS_TRY(dalloc(c, slot, sizeof(T) * (size_t)c->g.N));
-        w[d] = (T*)*slot;
-    }
-    return LS_OK;
-}
-
-template <typename T>
 static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info) {
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
     double* x = c->P + (c->p.compat_shift ? g.JK : 0);
-    T* w[3];
-    LS_TRY(ensure_weights<T>(c, w));
     LS_TRY(inner_alloc<T>(c));
+    const bool use_mg = c->p.press_solver != LS_PRESS_JACOBI64;
+    double sigma = 1.0;
     {
         Timed tm(c, LS_T_PRESS_SETUP);
-        LS_LAUNCH(c, k_press_weights<T>, grid, kBlock, 0, g, (const double*)c->pisd,
-                  (const double*)c->pface[0], (const double*)c->pface[1],
-                  (const double*)c->pface[2], w[0], w[1], w[2]);
         LS_LAUNCH(c, k_press_init_x, grid, kBlock, 0, g, (const int8_t*)c->pkind,
                   (const double*)c->pb, x);
-    }
-    const bool use_mg = c->p.press_solver != LS_PRESS_JACOBI64;
-    if (use_mg) {
-        Timed tm(c, LS_T_PRESS_SETUP);
-        LS_TRY(mg_setup<T>(c, w));
+        LS_LAUNCH(c, k_press_maxd, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const double*)c->pdiag,
+                  c->partials);
+        LS_TRY(finalize_max(c, grid, 1, S_RED0));
+        double maxd = 0.0;
+        LS_TRY(read_scalars(c, S_RED0, 1, &maxd));
+        sigma = (maxd > 0.0) ? 1.0 / maxd : 1.0;
+        LS_LAUNCH(c, k_inner_setup<T>, grid, kBlock, 0, g, sigma, (const int8_t*)c->pkind,
+                  (const double*)c->pface[0], (const double*)c->pface[1], (const double*)c->pface[2],
+                  (T*)c->ie, (T*)c->iface[0], (T*)c->iface[1], (T*)c->iface[2]);
+        LS_TRY(inner_invd<T>(c));
+        if (use_mg) LS_TRY(mg_setup<T>(c));
     }
     double den = 0.0;
     LS_TRY(read_scalars(c, SP_DEN, 1, &den));
@@ -608,17 +624,16 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info) {
         double irel = 0.0;
         {
             Timed tm(c, LS_T_PRESS_INNER);
-            LS_LAUNCH(c, k_press_inner_rhs<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind,
-                      (const double*)c->pdiag, (const double*)c->pisd, (const double*)c->pr,
+            LS_LAUNCH(c, k_press_inner_rhs<T>, grid, kBlock, 0, g, sigma, (const int8_t*)c->pkind,
+                      (const double*)c->pdiag, (const double*)c->pr,
                       (const double*)c->pface[0], (const double*)c->pface[1],
                       (const double*)c->pface[2], c->pdelta, (T*)c->inner[1]);
             double tol = std::max(inner_floor, 0.2 * rtol / std::max(rel, 1e-300));
             tol = std::min(tol, 0.5);
-            ls_status st = inner_pcg<T>(c, w, use_mg, tol, c->p.press_max_it - total_inner, &its,
-                                        &irel);
+            ls_status st = inner_pcg<T>(c, use_mg, tol, c->p.press_max_it - total_inner, &its, &irel);
             if (st != LS_OK) { result = st; break; }
             LS_LAUNCH(c, k_press_accumulate<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind,
-                      (const double*)c->pisd, (const double*)c->pdelta, (const T*)c->inner[0], x);
+                      (const double*)c->pdelta, (const T*)c->inner[0], x);
         }
         total_inner += its;
     }
