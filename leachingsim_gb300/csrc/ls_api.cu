@@ -80,12 +80,14 @@ static void resolve_regions(ls_ctx* c) {
 // reductions
 
 ls_status finalize_sum(ls_ctx* c, int nblocks, int nvals, int out_slot) {
-    LS_LAUNCH(c, k_finalize<false>, 1, 32, 0, c->partials, nblocks, nvals, c->scal + out_slot);
+    LS_LAUNCH(c, k_finalize<false>, nvals, kFinalizeThreads, 0, c->partials, nblocks, nvals,
+              c->scal + out_slot);
     return LS_OK;
 }
 
 ls_status finalize_max(ls_ctx* c, int nblocks, int nvals, int out_slot) {
-    LS_LAUNCH(c, k_finalize<true>, 1, 32, 0, c->partials, nblocks, nvals, c->scal + out_slot);
+    LS_LAUNCH(c, k_finalize<true>, nvals, kFinalizeThreads, 0, c->partials, nblocks, nvals,
+              c->scal + out_slot);
     return LS_OK;
 }
 
@@ -249,6 +251,7 @@ ls_status ls_create(ls_ctx** out, int I, int J, int K, int label_bytes, const ls
     c->g.JK = JK;
     c->g.N = (long long)I * JK;
     c->g.NP = NP;
+    grid_init_div(c->g);
     c->label_bytes = label_bytes;
     if (params) c->p = *params; else ls_params_default(&c->p);
     ls_status st = validate_params(c, &c->p);
@@ -317,7 +320,7 @@ ls_status ls_destroy(ls_ctx* c) {
                     c->b_fz, c->pkind, c->pdiag, c->pb, c->pface[0], c->pface[1], c->pface[2],
                     c->pisd, c->pr, c->pdelta, c->ie, c->iface[0], c->iface[1], c->iface[2],
                     c->iinvd, c->inner[0], c->inner[1], c->inner[2], c->inner[3],
-                    c->inner[4], c->mg0_x, c->mg0_t, c->comp, c->cc_flag, c->tkind, c->dz_list,
+                    c->inner[4], c->mg0_x, c->mg0_t, c->comp, c->cc_flag, c->tkind, c->tinv, c->dz_list,
                     c->dz_count, c->dz_level_start, c->partials, c->scal, c->d_int};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -389,6 +392,7 @@ static ls_status transfer(ls_ctx* c, ls_field f, void* host, size_t n, int padde
     if (up) {
         LS_CUDA(c, cudaMemcpyAsync(dev, host, n * esz, kind, c->stream));
         if (f == LS_F_LABEL || f == LS_F_PERMEABILITY || f == LS_F_VISCOSITY) c->p_ready = 0;
+        if (f == LS_F_PRESSURE) c->p_eff_prev = 0.0;
     } else {
         LS_CUDA(c, cudaMemcpyAsync(host, dev, n * esz, kind, c->stream));
     }
@@ -416,6 +420,7 @@ ls_status ls_init_fields(ls_ctx* c) {
     double* f[] = {c->P, c->conc, c->fx, c->fy, c->fz, c->sat, c->pc, c->kr, c->precip};
     for (double* q : f) LS_CUDA(c, cudaMemsetAsync(q, 0, bytes, c->stream));
     c->p_ready = 0;
+    c->p_eff_prev = 0.0;
     return LS_OK;
 }
 
@@ -550,6 +555,7 @@ ls_status ls_rollback(ls_ctx* c) {
         for (auto& pr : pairs) LS_CUDA(c, cudaMemcpyAsync(pr.first, pr.second, d8, cudaMemcpyDeviceToDevice, s));
     }
     c->p_ready = 0;
+    c->p_eff_prev = 0.0;
     return ls_props(c);
 }
 

@@ -8,6 +8,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 
 #include <string>
@@ -26,16 +27,70 @@ __host__ __device__ __forceinline__ double smax(double a, double b) { return (a 
 constexpr int kBlock = 256;        // threads per block of the streaming kernels
 constexpr int kMaxPartials = 4096; // per-block partial results of one reduction
 
+// Division of a 32-bit index by a fixed divisor through a multiply-high and a shift
+// (Granlund-Montgomery): q = umulhi(n, m) >> s, exact for every n < 2^31.
+struct FastDiv {
+    unsigned int d, m, s;
+};
+
+inline FastDiv make_fastdiv(unsigned int d) {
+    FastDiv f;
+    f.d = d;
+    unsigned int s = 0;
+    while ((1ull << s) < d) ++s;  // s = ceil(log2 d)
+    // m = ceil(2^(32+s) / d) - 2^32, valid for n < 2^31 with the add-back form below
+    unsigned long long m = ((1ull << (32 + s)) + d - 1) / d;
+    f.m = (unsigned int)(m - (1ull << 32));
+    f.s = s;
+    return f;
+}
+
+__host__ __device__ __forceinline__ unsigned int fdiv(const FastDiv& f, unsigned int n) {
+#ifdef __CUDA_ARCH__
+    unsigned int t = __umulhi(n, f.m);
+#else
+    unsigned int t = (unsigned int)(((unsigned long long)n * f.m) >> 32);
+#endif
+    return (unsigned int)(((unsigned long long)t + n) >> f.s);
+}
+
 struct Grid {
     int I, J, K;
     long long JK, N, NP;
+    FastDiv div_jk, div_k;
 };
 
+inline void grid_init_div(Grid& g) {
+    g.div_jk = make_fastdiv((unsigned int)g.JK);
+    g.div_k = make_fastdiv((unsigned int)g.K);
+}
+
 __host__ __device__ __forceinline__ void decode(const Grid& g, long long r, int& i, int& j, int& k) {
-    i = (int)(r / g.JK);
-    long long rem = r - (long long)i * g.JK;
-    j = (int)(rem / g.K);
-    k = (int)(rem - (long long)j * g.K);
+    const unsigned int rr = (unsigned int)r;
+    const unsigned int ii = fdiv(g.div_jk, rr);
+    const unsigned int rem = rr - ii * (unsigned int)g.JK;
+    const unsigned int jj = fdiv(g.div_k, rem);
+    i = (int)ii;
+    j = (int)jj;
+    k = (int)(rem - jj * (unsigned int)g.K);
+}
+
+// Division by dx: when dx is a power of two, multiplying by its reciprocal gives the same
+// double as dividing (both are exact scalings), without an FP64 division.
+struct DxDiv {
+    double dx, inv_dx;
+    int pow2;
+    __host__ __device__ __forceinline__ double div(double a) const { return pow2 ? a * inv_dx : a / dx; }
+};
+
+inline DxDiv make_dxdiv(double dx) {
+    DxDiv d;
+    d.dx = dx;
+    d.inv_dx = 1.0 / dx;
+    int e = 0;
+    double m = frexp(dx, &e);
+    d.pow2 = (m == 0.5) ? 1 : 0;
+    return d;
 }
 
 // Timed region record.
@@ -87,6 +142,8 @@ struct ls_ctx {
     int inner_is64;     // -1 = not allocated
     double pscale_den;  // ||D^-1 b|| of the current pressure system
     double p_t;         // time the pressure system was assembled for
+    double p_eff;       // ramped top pressure of the assembled system
+    double p_eff_prev;  // ... of the previous solve (0 = none)
     int p_ready;
 
     // multigrid: the finest level is the inner system above (vectors mg0_x, mg0_t);
@@ -112,6 +169,7 @@ struct ls_ctx {
     double* tc[7];        // FP64 row coefficients: diagonal, then +i,-i,+j,-j,+k,-k
     double* tb[2];        // FP64 right-hand sides
     float* to[6];         // FP32 off-diagonals scaled by the row diagonal
+    double* tinv;         // FP64 1 / row diagonal
     float* tf[2][8];      // FP32 inner vectors per right-hand side: rhs r rh p v s t d
     int8_t* tkind;        // 1 identity row, 2 coupled row
 
@@ -231,18 +289,30 @@ __device__ __forceinline__ void block_max_store(double (&v)[NV], double* partial
     }
 }
 
-// one block; thread v reduces value v over the blocks in a fixed order
+// One block per value: a fixed-order tree reduction of the per-block partials (the
+// result does not depend on timing).
+constexpr int kFinalizeThreads = 256;
 template <bool MAX>
-__global__ void k_finalize(const double* __restrict__ partials, int nblocks, int nvals,
-                           double* __restrict__ out) {
-    for (int v = threadIdx.x; v < nvals; v += blockDim.x) {
-        double acc = MAX ? partials[v] : 0.0;
-        for (int b = MAX ? 1 : 0; b < nblocks; ++b) {
-            double x = partials[(size_t)b * nvals + v];
-            acc = MAX ? smax(acc, x) : acc + x;
-        }
-        out[v] = acc;
+__global__ void __launch_bounds__(kFinalizeThreads) k_finalize(const double* __restrict__ partials,
+                                                               int nblocks, int nvals,
+                                                               double* __restrict__ out) {
+    __shared__ double sh[kFinalizeThreads];
+    const int v = blockIdx.x;
+    double acc = MAX ? -INFINITY : 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+        double x = partials[(size_t)b * nvals + v];
+        acc = MAX ? smax(acc, x) : acc + x;
     }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = kFinalizeThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            double o = sh[threadIdx.x + w];
+            sh[threadIdx.x] = MAX ? smax(sh[threadIdx.x], o) : sh[threadIdx.x] + o;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[v] = sh[0];
 }
 
 // label access

@@ -344,6 +344,7 @@ static Grid coarse_of(const Grid& f) {
     c.JK = (long long)c.J * c.K;
     c.N = (long long)c.I * c.JK;
     c.NP = c.N;
+    grid_init_div(c);
     return c;
 }
 

@@ -102,24 +102,6 @@ ls_status props_run(ls_ctx* c) {
     return LS_OK;
 }
 
-// Division by dx: when dx is a power of two, multiplying by its reciprocal gives the same
-// double as dividing (both are exact scalings), without an FP64 division.
-struct DxDiv {
-    double dx, inv_dx;
-    int pow2;
-    __device__ __forceinline__ double div(double a) const { return pow2 ? a * inv_dx : a / dx; }
-};
-
-static DxDiv make_dxdiv(double dx) {
-    DxDiv d;
-    d.dx = dx;
-    d.inv_dx = 1.0 / dx;
-    int e = 0;
-    double m = std::frexp(dx, &e);
-    d.pow2 = (m == 0.5) ? 1 : 0;
-    return d;
-}
-
 // ---------------------------------------------------------------------------
 // calculateFlux: central differences inside, one-sided on the domain faces (np=1).
 

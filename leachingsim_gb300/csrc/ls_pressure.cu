@@ -213,6 +213,18 @@ __global__ void k_inner_setup(Grid g, double sigma, const int8_t* __restrict__ k
     }
 }
 
+// Pore rows of the initial guess scaled by the ratio of the ramped boundary pressures of
+// this solve and the previous one: without evaporative sources the solution is
+// proportional to the boundary pressure, so the previous solution scaled is the best
+// available starting point (the converged result does not depend on the starting point
+// beyond the tolerance).
+__global__ void k_press_scale_x(Grid g, const int8_t* __restrict__ kind, double ratio,
+                                double* __restrict__ x) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x)
+        if (kind[r] >= 2) x[r] *= ratio;
+}
+
 // identity rows take their value; other rows keep the warm start.
 __global__ void k_press_init_x(Grid g, const int8_t* __restrict__ kind, const double* __restrict__ b,
                                double* __restrict__ x) {
@@ -522,6 +534,7 @@ ls_status pressure_setup_run(ls_ctx* c, double t) {
     if (t < ramp_duration)
         effective_top_pressure = c->p.top_pressure * (t / ramp_duration) + 1e-6;
     pcst.eff_top = effective_top_pressure;
+    c->p_eff = effective_top_pressure;
     pcst.evap_dx = c->p.evaporative_flux * c->p.dx;
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
@@ -565,10 +578,19 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info) {
     LS_TRY(inner_alloc<T>(c));
     const bool use_mg = c->p.press_solver != LS_PRESS_JACOBI64;
     double sigma = 1.0;
+    bool inner_ready = false;
     {
         Timed tm(c, LS_T_PRESS_SETUP);
+        if (c->p.evaporative_flux == 0.0 && c->p_eff_prev > 0.0 && c->p_eff != c->p_eff_prev)
+            LS_LAUNCH(c, k_press_scale_x, grid, kBlock, 0, g, (const int8_t*)c->pkind,
+                      c->p_eff / c->p_eff_prev, x);
         LS_LAUNCH(c, k_press_init_x, grid, kBlock, 0, g, (const int8_t*)c->pkind,
                   (const double*)c->pb, x);
+    }
+    // the inner operator and the multigrid hierarchy, built on the first sweep that needs
+    // them
+    auto build_inner = [&]() -> ls_status {
+        Timed tm(c, LS_T_PRESS_SETUP);
         LS_LAUNCH(c, k_press_maxd, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const double*)c->pdiag,
                   c->partials);
         LS_TRY(finalize_max(c, grid, 1, S_RED0));
@@ -580,7 +602,8 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info) {
                   (T*)c->ie, (T*)c->iface[0], (T*)c->iface[1], (T*)c->iface[2]);
         LS_TRY(inner_invd<T>(c));
         if (use_mg) LS_TRY(mg_setup<T>(c));
-    }
+        return LS_OK;
+    };
     double den = 0.0;
     LS_TRY(read_scalars(c, SP_DEN, 1, &den));
     const double rtol = c->p.press_rtol;
@@ -622,6 +645,11 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info) {
         sweeps++;
         int its = 0;
         double irel = 0.0;
+        if (!inner_ready) {
+            ls_status st = build_inner();
+            if (st != LS_OK) { result = st; break; }
+            inner_ready = true;
+        }
         {
             Timed tm(c, LS_T_PRESS_INNER);
             LS_LAUNCH(c, k_press_inner_rhs<T>, grid, kBlock, 0, g, sigma, (const int8_t*)c->pkind,
@@ -640,8 +668,9 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info) {
     // min / max of the solution vector for the log line
     double mm[2] = {0.0, 0.0};
     // k_press_residual left the block maxima of x and -x in pmax
-    LS_LAUNCH(c, k_finalize<true>, 1, 32, 0, pmax, grid, 2, c->scal + SP_XMAX);
+    LS_LAUNCH(c, k_finalize<true>, 2, kFinalizeThreads, 0, pmax, grid, 2, c->scal + SP_XMAX);
     LS_TRY(read_scalars(c, SP_XMAX, 2, mm));
+    if (result == LS_OK) c->p_eff_prev = c->p_eff;
     if (info) {
         info->iterations = total_inner;
         info->outer_iterations = sweeps;

@@ -46,6 +46,8 @@ __host__ __device__ __forceinline__ int aslot(int q) { return S_RED0 + 8 + q; }
 
 struct TransConst {
     double inv_dt, theta, alpha, D, Dpore, dx2, dx;
+    double dc_pore, dc_other;  // -D_eff / dx^2 for a Pore neighbour / any other neighbour
+    DxDiv dd;
 };
 
 // Coefficients of one transport row: diag, off[6] (+i,-i,+j,-j,+k,-k) and the explicit
@@ -107,11 +109,11 @@ __device__ __forceinline__ int trans_row(const Grid& g, const TransConst& tc,
         default: q_face = -fz[nb]; break;
         }
         double actual_q_face = (nt == kPrecipitate || nt == kSulphide) ? 0.0 : q_face;
-        double D_eff = (nt == kPore) ? tc.Dpore : tc.D;
-        double diffusion_coeff = -D_eff / tc.dx2;
+        // -D_eff / dx^2 takes one of two values, evaluated once on the host
+        double diffusion_coeff = (nt == kPore) ? tc.dc_pore : tc.dc_other;
         double coeff_neighbor = diffusion_coeff;
         double coeff_self = -diffusion_coeff;
-        double adv_coeff = actual_q_face / tc.dx;
+        double adv_coeff = tc.dd.div(actual_q_face);
         if (adv_coeff > 0) coeff_self += adv_coeff;
         else coeff_neighbor -= adv_coeff;
         off[d] = tc.theta * coeff_neighbor;
@@ -125,6 +127,7 @@ __device__ __forceinline__ int trans_row(const Grid& g, const TransConst& tc,
 
 struct SatConst {
     double phi_dt, dx, evap;
+    DxDiv dd;
 };
 
 // Coefficients of one implicit-saturation row (src/Simulation.cpp:1877-1958), from the
@@ -151,7 +154,7 @@ __device__ __forceinline__ int sat_row(const Grid& g, const SatConst& sc,
 #pragma unroll
     for (int d = 0; d < 6; ++d)
         if (val[d] && (int)label[nbs[d]] == kAir) air_faces++;
-    double evap_sink = (air_faces * sc.evap) / sc.dx;
+    double evap_sink = sc.dd.div(air_faces * sc.evap);
     const double sr = s[r];
     double coeff_self = sc.phi_dt;
     if (rhs) *rhs = 0.0 + ((sc.phi_dt * sr) - evap_sink);
@@ -164,10 +167,10 @@ __device__ __forceinline__ int sat_row(const Grid& g, const SatConst& sc,
         double q_face_outward = (d & 1) ? -q : q;
         if (q_face_outward > 0) {
             double v_eff = q_face_outward / smax(sr, 1e-6);
-            coeff_self += v_eff / sc.dx;
+            coeff_self += sc.dd.div(v_eff);
         } else {
             double v_eff = q_face_outward / smax(s[nbs[d]], 1e-6);
-            off[d] = v_eff / sc.dx;
+            off[d] = sc.dd.div(v_eff);
         }
     }
     diag = coeff_self;
@@ -192,6 +195,7 @@ struct TBuf {
     double* c[7];
     double* b[2];
     float* o[6];
+    double* inv;
     int8_t* kind;
 };
 
@@ -210,16 +214,18 @@ __global__ void __launch_bounds__(kBlock) k_t_setup(Rows<L> op, TBuf tb, int nrh
             kind = trans_row(g, op.tc, op.label, op.fx, op.fy, op.fz, r, i, j, k, dg, off, f0, f1, rhs);
         else
             kind = sat_row(g, op.sc, op.label, op.fx, op.fy, op.fz, op.s, r, i, j, k, dg, off, rhs);
+        const double inv = 1.0 / dg;  // the one FP64 division of the row
         tb.c[0][r] = dg;
+        tb.inv[r] = inv;
 #pragma unroll
         for (int d = 0; d < 6; ++d) {
             tb.c[1 + d][r] = off[d];
-            tb.o[d][r] = (float)(off[d] / dg);
+            tb.o[d][r] = (float)(off[d] * inv);
         }
         tb.kind[r] = (int8_t)kind;
         for (int q = 0; q < nrhs; ++q) {
             tb.b[q][r] = rhs[q];
-            double bt = rhs[q] / dg;
+            double bt = rhs[q] * inv;
             acc[q] += bt * bt;
         }
     }
@@ -259,15 +265,15 @@ __global__ void __launch_bounds__(kBlock) k_t_resid(Grid g, TBuf tb, double* x0,
          r += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         decode(g, r, i, j, k);
-        const double dg = tb.c[0][r];
+        const double inv = tb.inv[r];
         if (mask & 1) {
-            double rv = (tb.b[0][r] - t_row_apply(g, tb, r, i, j, k, x0)) / dg;
+            double rv = (tb.b[0][r] - t_row_apply(g, tb, r, i, j, k, x0)) * inv;
             r0[r] = (float)rv;
             acc[0] += rv * rv;
             if (rv != rv) acc[2] += 1.0;
         }
         if (mask & 2) {
-            double rv = (tb.b[1][r] - t_row_apply(g, tb, r, i, j, k, x1)) / dg;
+            double rv = (tb.b[1][r] - t_row_apply(g, tb, r, i, j, k, x1)) * inv;
             r1[r] = (float)rv;
             acc[1] += rv * rv;
             if (rv != rv) acc[3] += 1.0;
@@ -492,6 +498,7 @@ static ls_status t_alloc(ls_ctx* c) {
         for (int v = 0; v < 8; ++v)
             if (!c->tf[q][v]) LS_TRY(dalloc_t(c, &c->tf[q][v], n));
     if (!c->tkind) LS_TRY(dalloc_t(c, &c->tkind, n));
+    if (!c->tinv) LS_TRY(dalloc_t(c, &c->tinv, n));
     return LS_OK;
 }
 
@@ -500,6 +507,7 @@ static TBuf make_tbuf(ls_ctx* c) {
     for (int q = 0; q < 7; ++q) tb.c[q] = c->tc[q];
     for (int q = 0; q < 2; ++q) tb.b[q] = c->tb[q];
     for (int q = 0; q < 6; ++q) tb.o[q] = c->to[q];
+    tb.inv = c->tinv;
     tb.kind = c->tkind;
     return tb;
 }
@@ -653,6 +661,9 @@ static TransConst trans_const(const ls_ctx* c, double dt) {
     tc.Dpore = c->p.D * c->p.Dpore_fac;
     tc.dx = c->p.dx;
     tc.dx2 = c->p.dx * c->p.dx;
+    tc.dc_pore = -tc.Dpore / tc.dx2;
+    tc.dc_other = -tc.D / tc.dx2;
+    tc.dd = make_dxdiv(c->p.dx);
     return tc;
 }
 
@@ -662,7 +673,7 @@ static Rows<L> trans_rows(ls_ctx* c, double dt) {
     rows.mode = 0;
     rows.g = c->g;
     rows.tc = trans_const(c, dt);
-    rows.sc = SatConst{0.0, 1.0, 0.0};
+    rows.sc = SatConst{0.0, 1.0, 0.0, make_dxdiv(1.0)};
     rows.label = (const L*)c->label;
     rows.fx = c->fx; rows.fy = c->fy; rows.fz = c->fz; rows.s = nullptr;
     return rows;
@@ -750,6 +761,7 @@ static ls_status sat_implicit_t(ls_ctx* c, double dt, ls_solve_info* info) {
     rows.sc.phi_dt = c->p.porosity * (1.0 / dt);
     rows.sc.dx = c->p.dx;
     rows.sc.evap = c->p.evaporative_flux;
+    rows.sc.dd = make_dxdiv(c->p.dx);
     rows.label = (const L*)c->label;
     rows.fx = c->fx; rows.fy = c->fy; rows.fz = c->fz; rows.s = c->sat;
     const long long sh = c->p.compat_shift ? c->g.JK : 0;

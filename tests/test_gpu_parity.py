@@ -205,11 +205,15 @@ def test_dissolve_no_acid_is_identity(oracle_mod):
     g.close()
 
 
+# Pressure tolerance per inner precision: the FP64 residual meets rtol either way, but
+# components of the error in near-null modes (clusters anchored only by weak links) are
+# invisible to it and sit at the inner solver's precision.
+@pytest.mark.parametrize("solver,ptol", [(_abi.PRESS_MIXED, 1e-6), (_abi.PRESS_FP64, 1e-7)])
 @pytest.mark.parametrize("shift", [1, 0])
 @pytest.mark.parametrize("name,geom,lb", GEOMS[2:])
-def test_steps_against_twin(oracle_mod, name, geom, lb, shift):
+def test_steps_against_twin(oracle_mod, name, geom, lb, shift, solver, ptol):
     lab = geom()
-    p = params(compat_shift=shift, press_rtol=1e-11, conc_rtol=1e-13)
+    p = params(compat_shift=shift, press_rtol=1e-11, conc_rtol=1e-13, press_solver=solver)
     g = Context(lab.shape, label_bytes=lb, params=p)
     g.upload("label", lab)
     g.init_all()
@@ -220,7 +224,7 @@ def test_steps_against_twin(oracle_mod, name, geom, lb, shift):
         assert ok, info
         tw.step(float(n), 1.0)
         np.testing.assert_array_equal(g.download("label"), tw.label[:lab.shape[0]])
-        assert rel_l2(g.download("pressure", padded=True), tw.P) < 1e-7
+        assert rel_l2(g.download("pressure", padded=True), tw.P) < ptol
         assert rel_l2(g.download("saturation", padded=True), tw.sat) < 1e-9
         assert rel_l2(g.download("conc", padded=True), tw.conc) < 1e-9
     g.close()
