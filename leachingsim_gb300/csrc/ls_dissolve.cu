@@ -18,7 +18,8 @@ namespace ls {
 
 struct DzConst {
     double D, dx, kreac, time_scalar, c_sat, dt_sub;
-    double k_eff;  // 1/((1/(D/dx)) + (1/kreac)), the same expression as per neighbour
+    double k_eff;      // 1/((1/(D/dx)) + (1/kreac)), the same expression as per neighbour
+    DxDiv vol;         // division by the voxel volume dx*dx*dx (exact reciprocal when a power of two)
 };
 
 template <typename L>
@@ -60,7 +61,8 @@ __global__ void __launch_bounds__(kBlock) k_dz_rate(Grid g, DzConst dc, const L*
             double area_per_face = dc.dx * dc.dx;
             double voxel_volume = dc.dx * dc.dx * dc.dx;
             double vol_rate = flux_sum * area_per_face;
-            double fractional_rate = vol_rate / voxel_volume;
+            double fractional_rate = dc.vol.div(vol_rate);
+            (void)voxel_volume;
             if (fractional_rate > mx[0]) mx[0] = fractional_rate;
         }
         if (frac[r] > 0.0f) {
@@ -134,7 +136,8 @@ __global__ void k_dz_level(Grid g, DzConst dc, const int* __restrict__ list, int
     double area_per_face = dc.dx * dc.dx;
     double voxel_volume = dc.dx * dc.dx * dc.dx;
     double mass_loss = flux_sum * area_per_face * dc.dt_sub;
-    double fractional_loss = mass_loss / voxel_volume;
+    double fractional_loss = dc.vol.div(mass_loss);
+    (void)voxel_volume;
     float fr = (float)((double)frac[r] - (fractional_loss * dc.time_scalar));
     frac[r] = fr;
     if (flux_sum > 0.0) {
@@ -167,6 +170,7 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
     {
         double k_trans = dc.D / dc.dx;
         dc.k_eff = 1.0 / ((1.0 / k_trans) + (1.0 / dc.kreac));
+        dc.vol = make_dxdiv(dc.dx * dc.dx * dc.dx);
     }
     const L* label = (const L*)c->label;
     LS_CUDA(c, cudaMemsetAsync(c->d_int, 0, sizeof(int) * 4, c->stream));

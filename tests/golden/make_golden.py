@@ -1,0 +1,76 @@
+"""Generate the golden fixtures of tests/golden/ from the CPU oracle (tight solves).
+
+Cases: the reference's two generate_input.py recipes scaled to 20^3 (Air slabs at both
+ends) and a small seeded Gaussian-random-field geometry, each run from a fresh start for
+4 steps of dt = 1 (csat = 1, like the reference's job scripts), plus one restart-style
+case with acid present so the dissolution sweep is exercised. Saved per case: the inputs,
+the parameters, the per-step solver/sub-step summaries and the final fields (padded
+(I+1)*J*K arrays, the reference's np=1 layout).
+
+Run:  python tests/golden/make_golden.py
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from leachingsim_gb300._abi import default_params  # noqa: E402
+from leachingsim_gb300.geometry import grf_geometry, reference_case  # noqa: E402
+from oracle import oracle as om  # noqa: E402
+
+FIELDS = ["label", "frac", "pressure", "conc", "acid", "flux_x", "flux_y", "flux_z", "saturation",
+          "cap_pressure", "rel_perm", "permeability", "precipitate"]
+
+
+def cases():
+    yield "case0_20", reference_case(0, n=20), dict(c_sat=1.0), None
+    yield "case1_20", reference_case(1, n=20), dict(c_sat=1.0), None
+    lab, _ = grf_geometry((18, 16, 14), porosity=0.32, corr_len=2.0, mineral_fraction=0.2, seed=7)
+    yield "grf_18x16x14", lab, dict(c_sat=1.0), None
+    acid = np.random.default_rng(11).uniform(0.0, 1.0, lab.shape)
+    yield "grf_acid_18x16x14", lab, dict(c_sat=1.0, kreac=5.0, time_scalar=100.0), acid
+
+
+def run_case(lab, pover, acid, steps=4):
+    p = default_params(press_rtol=1e-13, conc_rtol=1e-13, **pover)
+    o = om.Oracle(lab.shape, params=p, mode=om.SOLVE_TIGHT, rtol=1e-14, restart=200, max_it=200000)
+    o.load_labels(lab)
+    o.init_all()
+    if acid is not None:
+        o.set("acid", acid)
+    infos = []
+    for n in range(steps):
+        ok, info = o.step(float(n), 1.0)
+        assert ok, info
+        infos.append({"leached": info["leached"], "sat_steps": info["saturation"]["num_steps"],
+                      "sat_max_rate": info["saturation"]["max_rate"],
+                      "leach_steps": info["leaching"]["num_steps"],
+                      "leach_max_rate": info["leaching"]["max_rate"]})
+    out = {f: o.get(f, padded=True) for f in FIELDS}
+    return p, infos, out
+
+
+def main():
+    manifest = {}
+    for name, lab, pover, acid in cases():
+        p, infos, out = run_case(lab, pover, acid)
+        arrays = {"in_label": lab}
+        if acid is not None:
+            arrays["in_acid"] = acid
+        for f, v in out.items():
+            arrays[f] = v
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrays)
+        manifest[name] = {"shape": list(lab.shape), "params": {k: v for k, v in p.as_dict().items()},
+                          "steps": len(infos), "infos": infos}
+        print(name, lab.shape, [i["leached"] for i in infos])
+    with open(os.path.join(HERE, "manifest.json"), "w") as fh:
+        json.dump(manifest, fh, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,79 @@
+"""Golden fixtures (tests/golden/, made by tests/golden/make_golden.py from the oracle).
+
+CPU: the oracle still reproduces them. GPU: the CUDA path reproduces them through the C-ABI:
+labels exactly, fields within the stated tolerances (pressure per the conditioning note of
+test_gpu_parity.py)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from helpers import rel_l2
+from leachingsim_gb300._abi import LsParams
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+MANIFEST = json.load(open(os.path.join(HERE, "manifest.json")))
+NAMES = sorted(MANIFEST)
+
+
+def load(name):
+    d = np.load(os.path.join(HERE, f"{name}.npz"))
+    m = MANIFEST[name]
+    p = LsParams()
+    for k, v in m["params"].items():
+        setattr(p, k, v)
+    return d, m, p
+
+
+def check(name, get, ptol, ftol):
+    d, m, _ = load(name)
+    np.testing.assert_array_equal(get("label").astype(np.int64), d["label"].astype(np.int64))
+    np.testing.assert_array_equal(get("frac"), d["frac"])
+    assert rel_l2(get("pressure"), d["pressure"]) < ptol
+    for f in ("saturation", "flux_x", "flux_y", "flux_z"):
+        assert rel_l2(get(f), d[f]) < ftol, f
+    for f in ("conc", "acid", "precipitate"):
+        assert rel_l2(get(f) + 1.0, d[f] + 1.0) < ftol, f
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_reproduces_golden(oracle_mod, name):
+    d, m, p = load(name)
+    lab = d["in_label"]
+    o = oracle_mod.Oracle(lab.shape, params=p, mode=oracle_mod.SOLVE_TIGHT, rtol=1e-14, restart=200,
+                          max_it=200000)
+    o.load_labels(lab)
+    o.init_all()
+    if "in_acid" in d:
+        o.set("acid", d["in_acid"])
+    for n in range(m["steps"]):
+        ok, info = o.step(float(n), 1.0)
+        assert ok
+        assert info["leached"] == m["infos"][n]["leached"]
+        assert info["saturation"]["num_steps"] == m["infos"][n]["sat_steps"]
+    check(name, lambda f: o.get(f, padded=True), 1e-9, 1e-10)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("solver,ptol", [(0, 1e-6), (1, 1e-7)])
+@pytest.mark.parametrize("name", NAMES)
+def test_gpu_reproduces_golden(name, solver, ptol):
+    from leachingsim_gb300.runtime import Context
+    d, m, p = load(name)
+    p.press_solver = solver
+    p.press_rtol = 1e-11
+    p.conc_rtol = 1e-13
+    lab = d["in_label"].astype(np.uint8)
+    g = Context(lab.shape, params=p)
+    g.upload("label", lab)
+    g.init_all()
+    if "in_acid" in d:
+        g.upload("acid", d["in_acid"])
+    for n in range(m["steps"]):
+        ok, info = g.step(float(n), 1.0)
+        assert ok, info
+        assert info["leached"] == m["infos"][n]["leached"]
+        assert info["saturation"]["num_steps"] == m["infos"][n]["sat_steps"]
+    check(name, lambda f: g.download(f, padded=True), ptol, 1e-8)
+    g.close()
