@@ -200,6 +200,26 @@ ls_status ls_saturation(ls_ctx* ctx, double dt, ls_substep_info* info);
 /* Simulation::setupSaturationEqns(dt) + solveSaturation (src/Simulation.cpp:1858-2053).
    Returns LS_UNPHYSICAL when the solution leaves [-0.05, 1.05]. */
 ls_status ls_saturation_implicit(ls_ctx* ctx, double dt, ls_solve_info* info);
+/* Explicit saturation update of ls_saturation on caller-owned device buffers that allocates
+   no device memory. No counterpart in the reference: it is for callers that cannot let this
+   library call cudaMalloc, such as hosts that own all device memory through their own pool
+   (preallocated work arrays, a fixed device-memory budget) or stepping loops that cannot
+   take the device-wide synchronisation an allocation may imply. Its reduction scratch is a
+   fixed device array (LS_NOALLOC_SAT_SCRATCH_BYTES) held by every GPU that loads the
+   library until the process exits; the first call on a device looks up that array's
+   address, so it should come before any stream capture. All calls share the array: calls
+   that overlap on the GPU race. Domains above LS_NOALLOC_SAT_MAX_VOXELS (512^3) are
+   rejected with LS_BAD_ARG and a message in err (if given).
+   Device pointers: label (I*J*K, uint8 or uint16 per label_bytes), flux_x/y/z (I*J*K
+   float64), saturation ((I+1)*J*K float64, updated in place like the context's field).
+   stream: a cudaStream_t, or NULL for the default stream. */
+#define LS_NOALLOC_SAT_MAX_VOXELS 134217728LL
+#define LS_NOALLOC_SAT_SCRATCH_BYTES ((16384 + 32) * 8)
+ls_status ls_saturation_noalloc(int I, int J, int K, int label_bytes, const void* label,
+                                const double* flux_x, const double* flux_y, const double* flux_z,
+                                double* saturation, double dt, double dx, double porosity,
+                                double evaporative_flux, void* stream, ls_substep_info* info,
+                                char* err, size_t err_len);
 /* Simulation::handleSurfaceEffects (src/Simulation.cpp:2063-2103). */
 ls_status ls_surface(ls_ctx* ctx);
 /* Simulation::setupConcentrationEqns + solveConc / solveAcid (src/Simulation.cpp:966-1295,

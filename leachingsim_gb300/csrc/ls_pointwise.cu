@@ -7,7 +7,10 @@
 //   precip  = handlePrecipitation (src/Simulation.cpp:2114-2165)
 // Arithmetic follows the reference expression by expression; the library is built
 // without FMA contraction so each product rounds on its own, as on the reference's host.
+#include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <mutex>
 
 #include "ls_internal.cuh"
 
@@ -366,3 +369,169 @@ ls_status precip_run(ls_ctx* c) {
 }
 
 }  // namespace ls
+
+// ===========================================================================
+// Explicit saturation update on caller-owned device buffers, allocating nothing.
+//
+// Some callers cannot let this library call cudaMalloc: hosts that own all device memory
+// through their own pool (a solver framework handing out preallocated work arrays, or a
+// process run under a fixed device-memory budget), and time-stepping loops that must not
+// pay for the device-wide synchronisation cudaMalloc/cudaFree may imply. For them the
+// reduction scratch of this update lives in a file-scope device array of fixed size,
+// loaded with the library and held on every GPU that loads it until the process exits.
+// The first call on a device looks up the array's device address (cudaGetSymbolAddress,
+// with that device current) and caches it, so that first call should come before any
+// stream capture. Every call uses the same array: two calls that overlap on the GPU (on
+// different streams or host threads) race on it. Each call writes every slot it later
+// reads (no accumulation), so nothing has to be cleared; the previous call's contents stay
+// until overwritten.
+
+namespace ls {
+
+constexpr int kNoAllocVoxelsPerThread = 32;
+constexpr int kNoAllocSlots = 16384;  // one block maximum per 256*32 voxels, + result slot
+static __device__ __align__(256) double g_noalloc_sat_scratch[kNoAllocSlots + 32];
+
+// block maxima of |div q| + evaporative sink over the active voxels of one chunk
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_noalloc_sat_rate(Grid g, DxDiv dd, double evap,
+                                                             const L* __restrict__ label,
+                                                             const double* __restrict__ fx,
+                                                             const double* __restrict__ fy,
+                                                             const double* __restrict__ fz,
+                                                             double* __restrict__ scratch) {
+    double v[1] = {0.0};
+    const long long base = (long long)blockIdx.x * kBlock * kNoAllocVoxelsPerThread;
+    for (int q = 0; q < kNoAllocVoxelsPerThread; ++q) {
+        long long r = base + (long long)q * kBlock + threadIdx.x;
+        if (r >= g.N) break;
+        int t = (int)label[r];
+        if (sat_inactive(t)) continue;
+        int i, j, k;
+        decode(g, r, i, j, k);
+        double div_q, evap_sink;
+        sat_rates(g, label, fx, fy, fz, r, i, j, k, t, dd, evap, div_q, evap_sink);
+        double total_rate = fabs(div_q) + evap_sink;
+        if (total_rate > v[0]) v[0] = total_rate;
+    }
+    block_max_store<1>(v, scratch);
+}
+
+// max of the block maxima into the result slot
+__global__ void __launch_bounds__(kFinalizeThreads) k_noalloc_sat_final(int nblocks, double* __restrict__ scratch) {
+    __shared__ double sh[kFinalizeThreads];
+    double acc = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) acc = smax(acc, scratch[b]);
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = kFinalizeThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] = smax(sh[threadIdx.x], sh[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) scratch[kNoAllocSlots] = sh[0];
+}
+
+static double* noalloc_scratch_address(int device, cudaError_t* err) {
+    static std::mutex mu;
+    static double* addr[128] = {nullptr};
+    *err = cudaSuccess;
+    if (device < 0 || device >= 128) {
+        *err = cudaErrorInvalidDevice;
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_sat_scratch);
+        if (e != cudaSuccess) {
+            *err = e;
+            return nullptr;
+        }
+        addr[device] = (double*)p;
+    }
+    return addr[device];
+}
+
+}  // namespace ls
+
+static ls_status noalloc_fail(ls_status st, char* err, size_t len, const char* msg) {
+    if (err && len) snprintf(err, len, "%s", msg);
+    return st;
+}
+
+extern "C" ls_status ls_saturation_noalloc(int I, int J, int K, int label_bytes, const void* label,
+                                           const double* flux_x, const double* flux_y,
+                                           const double* flux_z, double* saturation, double dt,
+                                           double dx, double porosity, double evaporative_flux,
+                                           void* stream, ls_substep_info* info, char* err,
+                                           size_t err_len) {
+    using namespace ls;
+    if (err && err_len) err[0] = '\0';
+    if (I < 2 || J < 2 || K < 2 || (label_bytes != 1 && label_bytes != 2))
+        return noalloc_fail(LS_BAD_ARG, err, err_len, "ls_saturation_noalloc: bad extents or label_bytes");
+    if (!label || !flux_x || !flux_y || !flux_z || !saturation)
+        return noalloc_fail(LS_BAD_ARG, err, err_len, "ls_saturation_noalloc: null device pointer");
+    if (!(dt > 0.0) || !(dx > 0.0) || !(porosity > 0.0))
+        return noalloc_fail(LS_BAD_ARG, err, err_len, "ls_saturation_noalloc: dt, dx and porosity must be > 0");
+    const long long N = (long long)I * J * K;
+    if (N > LS_NOALLOC_SAT_MAX_VOXELS) {
+        char buf[200];
+        snprintf(buf, sizeof(buf),
+                 "ls_saturation_noalloc: %lld voxels exceed the fixed scratch limit of %lld voxels "
+                 "(use ls_saturation on a context instead)", N, (long long)LS_NOALLOC_SAT_MAX_VOXELS);
+        return noalloc_fail(LS_BAD_ARG, err, err_len, buf);
+    }
+    Grid g;
+    g.I = I; g.J = J; g.K = K;
+    g.JK = (long long)J * K;
+    g.N = N;
+    g.NP = N + g.JK;
+    grid_init_div(g);
+    int device = 0;
+    cudaError_t ce = cudaGetDevice(&device);
+    if (ce != cudaSuccess) return noalloc_fail(LS_CUDA_ERROR, err, err_len, cudaGetErrorString(ce));
+    double* scratch = noalloc_scratch_address(device, &ce);
+    if (!scratch) return noalloc_fail(LS_CUDA_ERROR, err, err_len, cudaGetErrorString(ce));
+    cudaStream_t s = (cudaStream_t)stream;
+    const DxDiv dd = make_dxdiv(dx);
+    const int nblocks = (int)((N + (long long)kBlock * kNoAllocVoxelsPerThread - 1) /
+                              ((long long)kBlock * kNoAllocVoxelsPerThread));
+    if (label_bytes == 1)
+        k_noalloc_sat_rate<uint8_t><<<nblocks, kBlock, 0, s>>>(g, dd, evaporative_flux, (const uint8_t*)label,
+                                                              flux_x, flux_y, flux_z, scratch);
+    else
+        k_noalloc_sat_rate<uint16_t><<<nblocks, kBlock, 0, s>>>(g, dd, evaporative_flux, (const uint16_t*)label,
+                                                               flux_x, flux_y, flux_z, scratch);
+    k_noalloc_sat_final<<<1, kFinalizeThreads, 0, s>>>(nblocks, scratch);
+    double max_div_q = 0.0;
+    ce = cudaMemcpyAsync(&max_div_q, scratch + kNoAllocSlots, sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+    if (ce == cudaSuccess) ce = cudaGetLastError();
+    if (ce != cudaSuccess) return noalloc_fail(LS_CUDA_ERROR, err, err_len, cudaGetErrorString(ce));
+    // sub-step count, src/Simulation.cpp:1740-1767
+    const double max_dsat = 0.1;
+    double dt_safe = dt;
+    if (max_div_q > 1e-20) dt_safe = (max_dsat * porosity) / max_div_q;
+    double calculated_steps = std::ceil(dt / dt_safe);
+    int num_steps = 1;
+    if (std::isinf(calculated_steps) || std::isnan(calculated_steps)) num_steps = 1000;
+    else if (calculated_steps > 1000) num_steps = 1000;
+    else if (calculated_steps > 1.0) num_steps = (int)calculated_steps;
+    double dt_sub = dt / num_steps;
+    double dt_sub_over_phi = dt_sub / porosity;
+    if (info) {
+        info->max_rate = max_div_q;
+        info->num_steps = num_steps;
+        info->dt_sub = dt_sub;
+    }
+    const int grid2 = (int)std::min<long long>((g.NP + kBlock - 1) / kBlock, 152LL * 8);
+    if (label_bytes == 1)
+        k_sat_update<uint8_t><<<grid2, kBlock, 0, s>>>(g, dd, evaporative_flux, dt_sub_over_phi, num_steps,
+                                                       (const uint8_t*)label, flux_x, flux_y, flux_z, saturation);
+    else
+        k_sat_update<uint16_t><<<grid2, kBlock, 0, s>>>(g, dd, evaporative_flux, dt_sub_over_phi, num_steps,
+                                                        (const uint16_t*)label, flux_x, flux_y, flux_z, saturation);
+    ce = cudaGetLastError();
+    if (ce != cudaSuccess) return noalloc_fail(LS_CUDA_ERROR, err, err_len, cudaGetErrorString(ce));
+    return LS_OK;
+}

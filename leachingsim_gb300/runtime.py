@@ -40,6 +40,10 @@ SYMBOLS = {
     "ls_flux": (C.c_int, [C.c_void_p]),
     "ls_saturation": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(LsSubstepInfo)]),
     "ls_saturation_implicit": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(LsSolveInfo)]),
+    "ls_saturation_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
+                                        C.c_double, C.c_double, C.c_void_p, C.POINTER(LsSubstepInfo),
+                                        C.c_char_p, C.c_size_t]),
     "ls_surface": (C.c_int, [C.c_void_p]),
     "ls_transport": (C.c_int, [C.c_void_p, C.c_double, C.c_int, C.POINTER(LsSolveInfo),
                                C.POINTER(LsSolveInfo)]),
