@@ -238,7 +238,9 @@ ls_status ls_create(ls_ctx** out, int I, int J, int K, int label_bytes, const ls
     if (label_bytes != 1 && label_bytes != 2) return LS_BAD_ARG;
     long long JK = (long long)J * K;
     long long NP = (long long)(I + 1) * JK;
-    if (NP >= (1LL << 31) - 1) return LS_BAD_ARG;  // 32-bit voxel ids in the dissolution lists
+    // 32-bit voxel ids (dissolution lists) and 32-bit row indices with a plane of padding on
+    // each side and a grid stride of headroom (transport inner vectors)
+    if (NP + J * (long long)K + (1LL << 22) >= (1LL << 31)) return LS_BAD_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return LS_NO_DEVICE;
 
@@ -330,9 +332,10 @@ ls_status ls_destroy(ls_ctx* c) {
         if (q) cudaFree(q);
     for (float* q : c->to)
         if (q) cudaFree(q);
-    for (auto& v : c->tf)
-        for (float* q : v)
-            if (q) cudaFree(q);
+    for (float* q : c->trhs)
+        if (q) cudaFree(q);
+    if (c->ti) cudaFree(c->ti);
+    if (c->tcount) cudaFree(c->tcount);
     for (auto& lv : c->mg) {
         void* lp[] = {lv.comp, lv.e, lv.face[0], lv.face[1], lv.face[2], lv.invd, lv.x, lv.b, lv.t};
         for (void* q : lp)

@@ -102,7 +102,7 @@ struct TimedRegion {
 // Device-side scalar slots (doubles) used by the solvers.
 enum Scalar {
     S_RED0 = 0,       // generic reduction outputs S_RED0..S_RED0+15
-    S_COUNT = 64
+    S_COUNT = 128
 };
 
 }  // namespace ls
@@ -170,7 +170,10 @@ struct ls_ctx {
     double* tb[2];        // FP64 right-hand sides
     float* to[6];         // FP32 off-diagonals scaled by the row diagonal
     double* tinv;         // FP64 1 / row diagonal
-    float* tf[2][8];      // FP32 inner vectors per right-hand side: rhs r rh p v s t d
+    float* trhs[2];       // FP32 D^-1 (b - A x) per right-hand side
+    float* ti;            // FP32 inner vectors r rh p v s t d, padded, float or float2 rows
+    long long ti_pad, ti_stride;  // zero elements around each vector; floats per vector
+    unsigned int* tcount; // blocks done in the current transport reduction
     int8_t* tkind;        // 1 identity row, 2 coupled row
 
     // dissolution

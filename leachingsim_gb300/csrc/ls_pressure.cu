@@ -225,6 +225,48 @@ __global__ void k_press_scale_x(Grid g, const int8_t* __restrict__ kind, double 
         if (kind[r] >= 2) x[r] *= ratio;
 }
 
+// Minimal-residual scaling of the warm start: with u = b - A x_fixed and y = A x_free on the
+// Pore rows (x_fixed: identity and empty rows, x_free: Pore rows), the partials of the
+// weighted dots (u,u), (u,y), (y,y) in the norm of the outer residual test; s = (u,y)/(y,y)
+// minimises ||D^-1 (b - A (x_fixed + s x_free))||.
+__global__ void __launch_bounds__(kBlock) k_press_guess_dots(Grid g, const int8_t* __restrict__ kind,
+                                                             const double* __restrict__ diag,
+                                                             const double* __restrict__ isd,
+                                                             const double* __restrict__ b,
+                                                             const double* __restrict__ f0,
+                                                             const double* __restrict__ f1,
+                                                             const double* __restrict__ f2,
+                                                             const double* __restrict__ x,
+                                                             double* __restrict__ partials) {
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        const int kd = kind[r];
+        if (kd < 2) continue;
+        int i, j, k;
+        decode(g, r, i, j, k);
+        double fixed = 0.0, free = diag[r] * x[r];
+        const long long nb[6] = {r - g.JK, r - g.K, r - 1, r + 1, r + g.K, r + g.JK};
+        const bool val[6] = {i > 0, j > 0, k > 0, k + 1 < g.K, j + 1 < g.J, i + 1 < g.I};
+        const double cf[6] = {val[0] ? f0[nb[0]] : 0.0, val[1] ? f1[nb[1]] : 0.0, val[2] ? f2[nb[2]] : 0.0,
+                              val[3] ? f2[r] : 0.0, val[4] ? f1[r] : 0.0, val[5] ? f0[r] : 0.0};
+#pragma unroll
+        for (int d = 0; d < 6; ++d) {
+            if (!val[d]) continue;
+            const double t = cf[d] * x[nb[d]];
+            if (kind[nb[d]] >= 2) free += t;
+            else fixed += t;
+        }
+        const double u = b[r] - fixed;
+        const double id2 = (kd == 2) ? isd[r] * isd[r] : 1e16;
+        const double w = id2 * id2;
+        acc[0] += u * u * w;
+        acc[1] += u * free * w;
+        acc[2] += free * free * w;
+    }
+    block_sum_store<3>(acc, partials);
+}
+
 // identity rows take their value; other rows keep the warm start.
 __global__ void k_press_init_x(Grid g, const int8_t* __restrict__ kind, const double* __restrict__ b,
                                double* __restrict__ x) {
@@ -617,6 +659,10 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info) {
     double prev_rel = INFINITY;
     int stagnant = 0;
     const int max_sweeps = 64;
+    // A warm start that misses the tolerance is first rescaled by the minimal-residual
+    // factor (it recovers the exact solution when only the boundary pressure changed, and
+    // drops a start that no longer fits after the labels changed).
+    bool rescaled = false;
     for (;;) {
         double sc[2] = {0.0, 0.0};
         {
@@ -635,6 +681,29 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info) {
         }
         rel = (den > 0.0) ? sqrt(sc[0] / den) : sqrt(sc[0]);
         if (rel <= rtol || (den == 0.0 && sc[0] == 0.0)) { result = LS_OK; break; }
+        if (!rescaled && sweeps == 0) {
+            rescaled = true;
+            double dots[3] = {0.0, 0.0, 0.0};
+            {
+                Timed tm(c, LS_T_PRESS_OUTER);
+                LS_LAUNCH(c, k_press_guess_dots, grid, kBlock, 0, g, (const int8_t*)c->pkind,
+                          (const double*)c->pdiag, (const double*)c->pisd, (const double*)c->pb,
+                          (const double*)c->pface[0], (const double*)c->pface[1], (const double*)c->pface[2],
+                          (const double*)x, c->partials);
+                LS_TRY(finalize_sum(c, grid, 3, S_RED0));
+            }
+            LS_TRY(read_scalars(c, S_RED0, 3, dots));
+            if (dots[2] > 0.0 && std::isfinite(dots[1] / dots[2])) {
+                const double scale = dots[1] / dots[2];
+                // keep the start unless the rescaled one has a smaller residual:
+                // ||u - s y||^2 = (u,u) - (u,y)^2/(y,y)
+                const double rr_scaled = std::max(dots[0] - dots[1] * scale, 0.0);
+                if (rr_scaled < sc[0] && scale != 1.0) {
+                    LS_LAUNCH(c, k_press_scale_x, grid, kBlock, 0, g, (const int8_t*)c->pkind, scale, x);
+                    continue;
+                }
+            }
+        }
         if (total_inner >= c->p.press_max_it || sweeps >= max_sweeps) break;
         if (rel > 0.5 * prev_rel) {
             if (++stagnant >= 8) break;

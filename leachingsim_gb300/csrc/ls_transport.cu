@@ -28,22 +28,6 @@
 
 namespace ls {
 
-enum {
-    ST_BASE = 32,  // per right-hand side q: ST_BASE + 8*q + ...
-    ST_RHO = 0,    // (rhat, r)
-    ST_RHO_OLD = 1,
-    ST_ALPHA = 2,
-    ST_OMEGA = 3,
-    ST_RV = 4,     // (rhat, v)
-    ST_TS = 5,     // (t, s)
-    ST_TT = 6,     // (t, t)
-    ST_RR = 7      // (r, r)
-};
-// slot of value v for right-hand side q
-__host__ __device__ __forceinline__ int sslot(int q, int v) { return ST_BASE + 8 * q + v; }
-// 0/1 activity flags of the right-hand sides live in scal[S_RED0 + 8 + q]
-__host__ __device__ __forceinline__ int aslot(int q) { return S_RED0 + 8 + q; }
-
 struct TransConst {
     double inv_dt, theta, alpha, D, Dpore, dx2, dx;
     double dc_pore, dc_other;  // -D_eff / dx^2 for a Pore neighbour / any other neighbour
@@ -283,181 +267,364 @@ __global__ void __launch_bounds__(kBlock) k_t_resid(Grid g, TBuf tb, double* x0,
 }
 
 // ---------------------------------------------------------------------------
-// inner FP32 BiCGStab on A^ = I + O (O: scaled off-diagonals), per right-hand side q:
-// vectors tf[q] = {rhs, r, rh, p, v, s, t, d}
+// Inner FP32 BiCGStab on A^ = I + O (O: FP32 off-diagonals scaled by the row diagonal), for
+// NQ right-hand sides at once. With NQ = 2 both share the off-diagonal loads: each vector
+// element is a float2 with one lane per right-hand side. Every vector has `pad` zero
+// elements before and after its N rows, so the stencil needs no bounds tests (a link that
+// leaves the domain has a zero coefficient, and 0 * 0 adds nothing).
+//
+// Iteration n, with the per-lane scalars a (alpha), w (omega), b (beta) on the device:
+//   XP (n > 0): r = s - w t;  d += a p + w s;  p = r + b (p - w v)
+//   V         : v = A^ p (n = 0: p = r);              dots (rh, v)
+//   ST        : s = r - a v;  t = A^ s;               dots (t,s) (t,t) (rh,s) (rh,t) (s,s)
+// ST recomputes s at the six neighbours from r and v instead of reading a stored s. The
+// next rho = (rh, r) = (rh,s) - w (rh,t) and ||r||^2 = (s,s) - 2w (t,s) + w^2 (t,t) come from
+// the ST dots, so one iteration takes two reductions. Each reduction's last block updates
+// the scalars on the device; kernels return at once when no lane is active, so the host
+// launches iterations in batches and reads the state once per batch. The update a p + w s
+// still pending after the last iteration goes into the FP64 solution with d.
 
-struct IVec {
-    float* v[2][8];
+enum {
+    TI_BASE = 64,    // lane l: TI_BASE + TI_STRIDE * l + TI_*
+    TI_STRIDE = 16,
+    TI_RHO = 0,
+    TI_ALPHA,
+    TI_OMEGA,
+    TI_BETA,
+    TI_R2,           // ||r||^2 after the last iteration
+    TI_RR0,          // ||r0||^2
+    TI_TOL2,         // (relative tolerance)^2
+    TI_ACT,          // 1 while the lane iterates
+    TI_ITS,
+    TI_REASON,       // 1 converged, -1 breakdown, -4 NaN/Inf
+    TI_ANY = 100,    // 1 while some lane iterates
+    TI_RED = 104     // reduced dots of the last reduction (up to 10)
 };
-enum { IV_RHS = 0, IV_R, IV_RH, IV_P, IV_V, IV_S, IV_T, IV_D };
+__host__ __device__ __forceinline__ int tslot(int l, int v) { return TI_BASE + TI_STRIDE * l + v; }
+static_assert(TI_RED + 10 <= S_COUNT, "transport scalars exceed the scalar block");
 
-__device__ __forceinline__ float i_apply(const Grid& g, const TBuf& tb, long long r, int i, int j,
-                                         int k, const float* __restrict__ v) {
-    float acc = v[r];
-    if (i > 0) acc = __fmaf_rn(tb.o[1][r], v[r - g.JK], acc);
-    if (j > 0) acc = __fmaf_rn(tb.o[3][r], v[r - g.K], acc);
-    if (k > 0) acc = __fmaf_rn(tb.o[5][r], v[r - 1], acc);
-    if (k + 1 < g.K) acc = __fmaf_rn(tb.o[4][r], v[r + 1], acc);
-    if (j + 1 < g.J) acc = __fmaf_rn(tb.o[2][r], v[r + g.K], acc);
-    if (i + 1 < g.I) acc = __fmaf_rn(tb.o[0][r], v[r + g.JK], acc);
+enum { PH_INIT = 0, PH_V = 1, PH_ST = 2 };
+
+template <int NQ>
+struct Lanes;
+template <>
+struct Lanes<1> {
+    using V = float;
+    static __device__ __forceinline__ V zero() { return 0.f; }
+    static __device__ __forceinline__ V fma_s(float a, V x, V y) { return __fmaf_rn(a, x, y); }
+    static __device__ __forceinline__ V fma_l(V a, V x, V y) { return __fmaf_rn(a, x, y); }
+    static __device__ __forceinline__ float lane(V v, int) { return v; }
+    static __device__ __forceinline__ V scal(const double* s, int v, float sign) {
+        return sign * (float)s[tslot(0, v)];
+    }
+    static __device__ __forceinline__ V gather(const float* const* f, int r) { return f[0][r]; }
+};
+template <>
+struct Lanes<2> {
+    using V = float2;
+    static __device__ __forceinline__ V zero() { return make_float2(0.f, 0.f); }
+    static __device__ __forceinline__ V fma_s(float a, V x, V y) {
+        return make_float2(__fmaf_rn(a, x.x, y.x), __fmaf_rn(a, x.y, y.y));
+    }
+    static __device__ __forceinline__ V fma_l(V a, V x, V y) {
+        return make_float2(__fmaf_rn(a.x, x.x, y.x), __fmaf_rn(a.y, x.y, y.y));
+    }
+    static __device__ __forceinline__ float lane(V v, int q) { return q ? v.y : v.x; }
+    static __device__ __forceinline__ V scal(const double* s, int v, float sign) {
+        return make_float2(sign * (float)s[tslot(0, v)], sign * (float)s[tslot(1, v)]);
+    }
+    static __device__ __forceinline__ V gather(const float* const* f, int r) {
+        return make_float2(f[0][r], f[1][r]);
+    }
+};
+
+// inner vectors: element pointers of row 0 in the active layout (float or float2)
+struct TIVec {
+    float *r, *rh, *p, *v, *s, *t, *d;
+    const float* rhs[2];  // FP32 D^-1 (b - A x) per lane, unpadded
+};
+
+struct TOff {
+    const float* o[6];  // +i,-i,+j,-j,+k,-k
+};
+
+// y = x + sum_d o_d x_nb, neighbours in the order -i, -j, -k, +k, +j, +i
+template <int NQ>
+__device__ __forceinline__ typename Lanes<NQ>::V ti_apply(const TOff& op, int r, int JK, int K,
+                                                          const typename Lanes<NQ>::V* __restrict__ x) {
+    using L = Lanes<NQ>;
+    typename L::V acc = x[r];
+    acc = L::fma_s(__ldg(op.o[1] + r), x[r - JK], acc);
+    acc = L::fma_s(__ldg(op.o[3] + r), x[r - K], acc);
+    acc = L::fma_s(__ldg(op.o[5] + r), x[r - 1], acc);
+    acc = L::fma_s(__ldg(op.o[4] + r), x[r + 1], acc);
+    acc = L::fma_s(__ldg(op.o[2] + r), x[r + K], acc);
+    acc = L::fma_s(__ldg(op.o[0] + r), x[r + JK], acc);
     return acc;
 }
 
-// start: r = rh = rhs, p = v = d = 0; partial (r, r)
-__global__ void __launch_bounds__(kBlock) k_i_init(Grid g, IVec iv, int mask, double* __restrict__ partials) {
-    float acc[2] = {0.f, 0.f};
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x) {
-        for (int q = 0; q < 2; ++q) {
-            if (!((mask >> q) & 1)) continue;
-            float rv = iv.v[q][IV_RHS][r];
-            iv.v[q][IV_R][r] = rv;
-            iv.v[q][IV_RH][r] = rv;
-            iv.v[q][IV_P][r] = 0.f;
-            iv.v[q][IV_V][r] = 0.f;
-            iv.v[q][IV_D][r] = 0.f;
-            acc[q] = __fmaf_rn(rv, rv, acc[q]);
+// r = rh = rhs, d = 0, zero halos of r, p, v; dots (r, r)
+template <int NQ>
+__global__ void __launch_bounds__(kBlock) k_ti_init(int N, int pad, TIVec iv, double* __restrict__ partials) {
+    using L = Lanes<NQ>;
+    using V = typename L::V;
+    V* __restrict__ R = reinterpret_cast<V*>(iv.r);
+    V* __restrict__ RH = reinterpret_cast<V*>(iv.rh);
+    V* __restrict__ D = reinterpret_cast<V*>(iv.d);
+    V* __restrict__ P = reinterpret_cast<V*>(iv.p);
+    V* __restrict__ VV = reinterpret_cast<V*>(iv.v);
+    float acc[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) acc[q] = 0.f;
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int r = t0; r < N; r += stride) {
+        V x = L::gather(iv.rhs, r);
+        R[r] = x;
+        RH[r] = x;
+        D[r] = L::zero();
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) acc[q] = __fmaf_rn(L::lane(x, q), L::lane(x, q), acc[q]);
+    }
+    for (int h = t0; h < pad; h += stride) {
+        R[-1 - h] = L::zero(); R[N + h] = L::zero();
+        P[-1 - h] = L::zero(); P[N + h] = L::zero();
+        VV[-1 - h] = L::zero(); VV[N + h] = L::zero();
+    }
+    double a[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) a[q] = acc[q];
+    block_sum_store<NQ>(a, partials);
+}
+
+// v = A^ p (FIRST: p = r, stored); dots (rh, v)
+template <int NQ, bool FIRST>
+__global__ void __launch_bounds__(kBlock) k_ti_v(int N, int JK, int K, TOff op, TIVec iv,
+                                                 const double* __restrict__ scal,
+                                                 double* __restrict__ partials) {
+    if (scal[TI_ANY] == 0.0) return;
+    using L = Lanes<NQ>;
+    using V = typename L::V;
+    const V* __restrict__ X = reinterpret_cast<const V*>(FIRST ? iv.r : iv.p);
+    const V* __restrict__ RH = reinterpret_cast<const V*>(iv.rh);
+    V* __restrict__ VV = reinterpret_cast<V*>(iv.v);
+    V* __restrict__ P = reinterpret_cast<V*>(iv.p);
+    float acc[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) acc[q] = 0.f;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x) {
+        const V y = ti_apply<NQ>(op, r, JK, K, X);
+        VV[r] = y;
+        if (FIRST) P[r] = X[r];
+        const V h = RH[r];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) acc[q] = __fmaf_rn(L::lane(h, q), L::lane(y, q), acc[q]);
+    }
+    double a[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) a[q] = acc[q];
+    block_sum_store<NQ>(a, partials);
+}
+
+// s = r - a v (at the row and, recomputed, at its neighbours); t = A^ s;
+// dots (t,s) (t,t) (rh,s) (rh,t) (s,s) per lane
+template <int NQ>
+__global__ void __launch_bounds__(kBlock) k_ti_st(int N, int JK, int K, TOff op, TIVec iv,
+                                                  const double* __restrict__ scal,
+                                                  double* __restrict__ partials) {
+    if (scal[TI_ANY] == 0.0) return;
+    using L = Lanes<NQ>;
+    using V = typename L::V;
+    const V* __restrict__ R = reinterpret_cast<const V*>(iv.r);
+    const V* __restrict__ VV = reinterpret_cast<const V*>(iv.v);
+    const V* __restrict__ RH = reinterpret_cast<const V*>(iv.rh);
+    V* __restrict__ S = reinterpret_cast<V*>(iv.s);
+    V* __restrict__ T = reinterpret_cast<V*>(iv.t);
+    const V na = L::scal(scal, TI_ALPHA, -1.f);
+    float acc[5 * NQ];
+#pragma unroll
+    for (int q = 0; q < 5 * NQ; ++q) acc[q] = 0.f;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x) {
+        const V s = L::fma_l(na, VV[r], R[r]);
+        V t = s;
+        t = L::fma_s(__ldg(op.o[1] + r), L::fma_l(na, VV[r - JK], R[r - JK]), t);
+        t = L::fma_s(__ldg(op.o[3] + r), L::fma_l(na, VV[r - K], R[r - K]), t);
+        t = L::fma_s(__ldg(op.o[5] + r), L::fma_l(na, VV[r - 1], R[r - 1]), t);
+        t = L::fma_s(__ldg(op.o[4] + r), L::fma_l(na, VV[r + 1], R[r + 1]), t);
+        t = L::fma_s(__ldg(op.o[2] + r), L::fma_l(na, VV[r + K], R[r + K]), t);
+        t = L::fma_s(__ldg(op.o[0] + r), L::fma_l(na, VV[r + JK], R[r + JK]), t);
+        S[r] = s;
+        T[r] = t;
+        const V h = RH[r];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            const float sq = L::lane(s, q), tq = L::lane(t, q), hq = L::lane(h, q);
+            acc[5 * q + 0] = __fmaf_rn(tq, sq, acc[5 * q + 0]);
+            acc[5 * q + 1] = __fmaf_rn(tq, tq, acc[5 * q + 1]);
+            acc[5 * q + 2] = __fmaf_rn(hq, sq, acc[5 * q + 2]);
+            acc[5 * q + 3] = __fmaf_rn(hq, tq, acc[5 * q + 3]);
+            acc[5 * q + 4] = __fmaf_rn(sq, sq, acc[5 * q + 4]);
         }
     }
-    double a[2] = {acc[0], acc[1]};
-    block_sum_store<2>(a, partials);
+    double a[5 * NQ];
+#pragma unroll
+    for (int q = 0; q < 5 * NQ; ++q) a[q] = acc[q];
+    block_sum_store<5 * NQ>(a, partials);
 }
 
-// p = r + beta (p - omega v)
-__global__ void k_i_p(Grid g, IVec iv, int mask, const double* __restrict__ scal) {
-    float beta[2] = {0.f, 0.f}, omega[2] = {0.f, 0.f};
-    for (int q = 0; q < 2; ++q) {
-        if (!((mask >> q) & 1)) continue;
-        double om = scal[sslot(q, ST_OMEGA)];
-        omega[q] = (float)om;
-        beta[q] = (float)((scal[sslot(q, ST_RHO)] / scal[sslot(q, ST_RHO_OLD)]) * (scal[sslot(q, ST_ALPHA)] / om));
+// r = s - w t; d += a p + w s; p = r + b (p - w v)
+template <int NQ>
+__global__ void __launch_bounds__(kBlock) k_ti_xp(int N, TIVec iv, const double* __restrict__ scal) {
+    if (scal[TI_ANY] == 0.0) return;
+    using L = Lanes<NQ>;
+    using V = typename L::V;
+    const V* __restrict__ S = reinterpret_cast<const V*>(iv.s);
+    const V* __restrict__ T = reinterpret_cast<const V*>(iv.t);
+    const V* __restrict__ VV = reinterpret_cast<const V*>(iv.v);
+    V* __restrict__ R = reinterpret_cast<V*>(iv.r);
+    V* __restrict__ P = reinterpret_cast<V*>(iv.p);
+    V* __restrict__ D = reinterpret_cast<V*>(iv.d);
+    const V a = L::scal(scal, TI_ALPHA, 1.f);
+    const V w = L::scal(scal, TI_OMEGA, 1.f);
+    const V nw = L::scal(scal, TI_OMEGA, -1.f);
+    const V b = L::scal(scal, TI_BETA, 1.f);
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x) {
+        const V s = S[r], t = T[r], p = P[r], v = VV[r];
+        const V rn = L::fma_l(nw, t, s);
+        D[r] = L::fma_l(a, p, L::fma_l(w, s, D[r]));
+        R[r] = rn;
+        P[r] = L::fma_l(b, L::fma_l(nw, v, p), rn);
     }
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x)
-        for (int q = 0; q < 2; ++q)
-            if ((mask >> q) & 1)
-                iv.v[q][IV_P][r] = __fmaf_rn(beta[q], __fmaf_rn(-omega[q], iv.v[q][IV_V][r], iv.v[q][IV_P][r]),
-                                             iv.v[q][IV_R][r]);
 }
 
-// v = A^ p; partial (rh, v)
-__global__ void __launch_bounds__(kBlock) k_i_v(Grid g, TBuf tb, IVec iv, int mask,
-                                                double* __restrict__ partials) {
-    float acc[2] = {0.f, 0.f};
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x) {
-        int i, j, k;
-        decode(g, r, i, j, k);
-        for (int q = 0; q < 2; ++q) {
-            if (!((mask >> q) & 1)) continue;
-            float y = i_apply(g, tb, r, i, j, k, iv.v[q][IV_P]);
-            iv.v[q][IV_V][r] = y;
-            acc[q] = __fmaf_rn(iv.v[q][IV_RH][r], y, acc[q]);
-        }
+// x_lane += d + a p + w s (the pending update of the last iteration)
+template <int NQ>
+__global__ void k_ti_accum(int N, TIVec iv, const double* __restrict__ scal, double* __restrict__ x0,
+                           double* __restrict__ x1) {
+    using L = Lanes<NQ>;
+    using V = typename L::V;
+    const V* __restrict__ S = reinterpret_cast<const V*>(iv.s);
+    const V* __restrict__ P = reinterpret_cast<const V*>(iv.p);
+    const V* __restrict__ D = reinterpret_cast<const V*>(iv.d);
+    float a[NQ], w[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        a[q] = (float)scal[tslot(q, TI_ALPHA)];
+        w[q] = (float)scal[tslot(q, TI_OMEGA)];
     }
-    double a[2] = {acc[0], acc[1]};
-    block_sum_store<2>(a, partials);
-}
-
-// s = r - alpha v
-__global__ void k_i_s(Grid g, IVec iv, int mask, const double* __restrict__ scal) {
-    float alpha[2] = {0.f, 0.f};
-    for (int q = 0; q < 2; ++q)
-        if ((mask >> q) & 1) alpha[q] = (float)(scal[sslot(q, ST_RHO)] / scal[sslot(q, ST_RV)]);
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x)
-        for (int q = 0; q < 2; ++q)
-            if ((mask >> q) & 1)
-                iv.v[q][IV_S][r] = __fmaf_rn(-alpha[q], iv.v[q][IV_V][r], iv.v[q][IV_R][r]);
-}
-
-// t = A^ s; partials (t, s), (t, t)
-__global__ void __launch_bounds__(kBlock) k_i_t(Grid g, TBuf tb, IVec iv, int mask,
-                                                double* __restrict__ partials) {
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x) {
-        int i, j, k;
-        decode(g, r, i, j, k);
-        for (int q = 0; q < 2; ++q) {
-            if (!((mask >> q) & 1)) continue;
-            float y = i_apply(g, tb, r, i, j, k, iv.v[q][IV_S]);
-            iv.v[q][IV_T][r] = y;
-            acc[2 * q] = __fmaf_rn(y, iv.v[q][IV_S][r], acc[2 * q]);
-            acc[2 * q + 1] = __fmaf_rn(y, y, acc[2 * q + 1]);
-        }
-    }
-    double a[4] = {acc[0], acc[1], acc[2], acc[3]};
-    block_sum_store<4>(a, partials);
-}
-
-// d += alpha p + omega s; r = s - omega t; partials (rh, r), (r, r)
-__global__ void __launch_bounds__(kBlock) k_i_x(Grid g, IVec iv, int mask, const double* __restrict__ scal,
-                                                double* __restrict__ partials) {
-    float alpha[2] = {0.f, 0.f}, omega[2] = {0.f, 0.f};
-    for (int q = 0; q < 2; ++q) {
-        if (!((mask >> q) & 1)) continue;
-        alpha[q] = (float)(scal[sslot(q, ST_RHO)] / scal[sslot(q, ST_RV)]);
-        double tt = scal[sslot(q, ST_TT)];
-        omega[q] = (float)((tt > 0.0) ? scal[sslot(q, ST_TS)] / tt : 0.0);
-    }
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x) {
-        for (int q = 0; q < 2; ++q) {
-            if (!((mask >> q) & 1)) continue;
-            float sv = iv.v[q][IV_S][r];
-            iv.v[q][IV_D][r] = __fmaf_rn(alpha[q], iv.v[q][IV_P][r], __fmaf_rn(omega[q], sv, iv.v[q][IV_D][r]));
-            float rv = __fmaf_rn(-omega[q], iv.v[q][IV_T][r], sv);
-            iv.v[q][IV_R][r] = rv;
-            acc[2 * q] = __fmaf_rn(iv.v[q][IV_RH][r], rv, acc[2 * q]);
-            acc[2 * q + 1] = __fmaf_rn(rv, rv, acc[2 * q + 1]);
-        }
-    }
-    double a[4] = {acc[0], acc[1], acc[2], acc[3]};
-    block_sum_store<4>(a, partials);
-}
-
-// Scalar bookkeeping between kernels (one thread).
-// phase 0: after init: rho = (r,r) (rhat = r), rho_old = alpha = omega = 1
-// phase 1: after v: (rhat, v) from generic slots 10+q
-// phase 3: after t: (t, s), (t, t) from generic slots 12+2q, 13+2q
-// phase 2: after x: alpha, omega kept for the next p update; rho_old = rho;
-//          rho, (r, r) from generic slots 2q, 2q+1
-__global__ void k_kry_scalars(double* scal, int mask, int phase) {
-    for (int q = 0; q < 2; ++q) {
-        if (!((mask >> q) & 1)) continue;
-        if (phase == 0) {
-            scal[sslot(q, ST_RHO)] = scal[S_RED0 + q];
-            scal[sslot(q, ST_RR)] = scal[S_RED0 + q];
-            scal[sslot(q, ST_RHO_OLD)] = 1.0;
-            scal[sslot(q, ST_ALPHA)] = 1.0;
-            scal[sslot(q, ST_OMEGA)] = 1.0;
-        } else if (phase == 1) {
-            scal[sslot(q, ST_RV)] = scal[S_RED0 + 10 + q];
-        } else if (phase == 3) {
-            scal[sslot(q, ST_TS)] = scal[S_RED0 + 12 + 2 * q];
-            scal[sslot(q, ST_TT)] = scal[S_RED0 + 13 + 2 * q];
-        } else if (phase == 2) {
-            double alpha = scal[sslot(q, ST_RHO)] / scal[sslot(q, ST_RV)];
-            double tt = scal[sslot(q, ST_TT)];
-            double omega = (tt > 0.0) ? scal[sslot(q, ST_TS)] / tt : 0.0;
-            scal[sslot(q, ST_ALPHA)] = alpha;
-            scal[sslot(q, ST_OMEGA)] = omega;
-            scal[sslot(q, ST_RHO_OLD)] = scal[sslot(q, ST_RHO)];
-            scal[sslot(q, ST_RHO)] = scal[S_RED0 + 2 * q];
-            scal[sslot(q, ST_RR)] = scal[S_RED0 + 2 * q + 1];
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x) {
+        const V d = D[r];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            float inc = L::lane(d, q);
+            if (w[q] != 0.f) inc = __fmaf_rn(w[q], L::lane(S[r], q), inc);
+            if (a[q] != 0.f) inc = __fmaf_rn(a[q], L::lane(P[r], q), inc);
+            double* x = q ? x1 : x0;
+            x[r] += (double)inc;
         }
     }
 }
 
-// x += d (FP64 accumulation of the FP32 correction)
-__global__ void k_t_accum(Grid g, const float* __restrict__ d0, const float* __restrict__ d1,
-                          double* __restrict__ x0, double* __restrict__ x1, int mask) {
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x) {
-        if (mask & 1) x0[r] += (double)d0[r];
-        if (mask & 2) x1[r] += (double)d1[r];
+__device__ __forceinline__ bool finite_d(double v) { return v == v && fabs(v) < INFINITY; }
+
+// scalar update after a reduction (one thread)
+template <int PH, int NQ>
+__device__ void ti_phase(double* scal, const double* red, double tol2_0, double tol2_1) {
+    int any = 0;
+#pragma unroll
+    for (int l = 0; l < NQ; ++l) {
+        double* s = scal + tslot(l, 0);
+        if (PH == PH_INIT) {
+            const double rr = red[l];
+            s[TI_RR0] = rr;
+            s[TI_RHO] = rr;
+            s[TI_R2] = rr;
+            s[TI_TOL2] = l ? tol2_1 : tol2_0;
+            s[TI_ALPHA] = s[TI_OMEGA] = s[TI_BETA] = 0.0;
+            s[TI_ITS] = 0.0;
+            const bool ok = finite_d(rr) && rr > 0.0;
+            s[TI_ACT] = ok ? 1.0 : 0.0;
+            s[TI_REASON] = ok ? 0.0 : (finite_d(rr) ? 1.0 : -4.0);
+        } else if (PH == PH_V) {
+            if (s[TI_ACT] != 0.0) {
+                const double rv = red[l];
+                if (rv != 0.0 && finite_d(rv)) {
+                    s[TI_ALPHA] = s[TI_RHO] / rv;
+                } else {
+                    s[TI_ACT] = 0.0;
+                    s[TI_REASON] = finite_d(rv) ? -1.0 : -4.0;
+                    s[TI_ALPHA] = s[TI_OMEGA] = s[TI_BETA] = 0.0;
+                }
+            } else {
+                s[TI_ALPHA] = s[TI_OMEGA] = s[TI_BETA] = 0.0;
+            }
+        } else {  // PH_ST
+            if (s[TI_ACT] != 0.0) {
+                const double ts = red[5 * l + 0], tt = red[5 * l + 1], hs = red[5 * l + 2],
+                             ht = red[5 * l + 3], ss = red[5 * l + 4];
+                const double w = (tt > 0.0) ? ts / tt : 0.0;
+                const double rho = hs - w * ht;
+                const double r2 = fmax(ss - 2.0 * w * ts + w * w * tt, 0.0);
+                s[TI_ITS] += 1.0;
+                s[TI_OMEGA] = w;
+                s[TI_R2] = r2;
+                if (!(finite_d(w) && finite_d(rho) && finite_d(r2) && finite_d(s[TI_ALPHA]))) {
+                    s[TI_ACT] = 0.0;
+                    s[TI_REASON] = -4.0;
+                    s[TI_ALPHA] = s[TI_OMEGA] = s[TI_BETA] = 0.0;
+                } else if (r2 <= s[TI_TOL2] * s[TI_RR0]) {
+                    s[TI_ACT] = 0.0;
+                    s[TI_REASON] = 1.0;
+                    s[TI_BETA] = 0.0;
+                } else if (w == 0.0 || rho == 0.0) {
+                    s[TI_ACT] = 0.0;
+                    s[TI_REASON] = -1.0;
+                    s[TI_BETA] = 0.0;
+                } else {
+                    s[TI_BETA] = (rho / s[TI_RHO]) * (s[TI_ALPHA] / w);
+                    s[TI_RHO] = rho;
+                }
+            } else {
+                s[TI_ALPHA] = s[TI_OMEGA] = s[TI_BETA] = 0.0;
+            }
+        }
+        if (s[TI_ACT] != 0.0) any = 1;
+    }
+    scal[TI_ANY] = any ? 1.0 : 0.0;
+}
+
+// Fixed-order reduction of the per-block partials, one block per value (as k_finalize);
+// the last block to finish applies the scalar update of phase PH.
+template <int PH, int NQ>
+__global__ void __launch_bounds__(kFinalizeThreads) k_ti_fin(const double* __restrict__ partials, int nblocks,
+                                                             double* scal, unsigned int* counter,
+                                                             double tol2_0, double tol2_1) {
+    if (PH != PH_INIT && scal[TI_ANY] == 0.0) return;
+    constexpr int NV = (PH == PH_ST) ? 5 * NQ : NQ;
+    __shared__ double sh[kFinalizeThreads];
+    __shared__ bool last;
+    const int v = blockIdx.x;
+    double acc = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) acc += partials[(size_t)b * NV + v];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = kFinalizeThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        scal[TI_RED + v] = sh[0];
+        __threadfence();
+        last = (atomicAdd(counter, 1u) == (unsigned int)(NV - 1));
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        double red[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) red[q] = __ldcg(scal + TI_RED + q);
+        ti_phase<PH, NQ>(scal, red, tol2_0, tol2_1);
+        *counter = 0u;
     }
 }
 
@@ -495,10 +662,20 @@ static ls_status t_alloc(ls_ctx* c) {
     for (int q = 0; q < 6; ++q)
         if (!c->to[q]) LS_TRY(dalloc_t(c, &c->to[q], n));
     for (int q = 0; q < 2; ++q)
-        for (int v = 0; v < 8; ++v)
-            if (!c->tf[q][v]) LS_TRY(dalloc_t(c, &c->tf[q][v], n));
+        if (!c->trhs[q]) LS_TRY(dalloc_t(c, &c->trhs[q], n));
     if (!c->tkind) LS_TRY(dalloc_t(c, &c->tkind, n));
     if (!c->tinv) LS_TRY(dalloc_t(c, &c->tinv, n));
+    if (!c->ti) {
+        // 7 inner vectors of up to N float2 each, with `pad` elements on both sides
+        c->ti_pad = ((c->g.JK + 31) / 32) * 32;
+        c->ti_stride = ((2 * (c->g.N + 2 * c->ti_pad) + 63) / 64) * 64;
+        LS_TRY(dalloc_t(c, &c->ti, (size_t)c->ti_stride * 7));
+        LS_CUDA(c, cudaMemsetAsync(c->ti, 0, sizeof(float) * (size_t)c->ti_stride * 7, c->stream));
+    }
+    if (!c->tcount) {
+        LS_TRY(dalloc_t(c, &c->tcount, 1));
+        LS_CUDA(c, cudaMemsetAsync(c->tcount, 0, sizeof(unsigned int), c->stream));
+    }
     return LS_OK;
 }
 
@@ -512,65 +689,74 @@ static TBuf make_tbuf(ls_ctx* c) {
     return tb;
 }
 
-static IVec make_ivec(ls_ctx* c) {
-    IVec iv;
-    for (int q = 0; q < 2; ++q)
-        for (int v = 0; v < 8; ++v) iv.v[q][v] = c->tf[q][v];
-    return iv;
-}
-
-// Inner FP32 BiCGStab for the right-hand sides in mask; each stops at its own relative
-// tolerance tol[q] or on breakdown. Returns the iterations of each.
-static ls_status inner_bicgstab(ls_ctx* c, const TBuf& tb, const IVec& iv, int mask, const double tol[2],
-                                int max_it, int its[2]) {
+// Inner solve of the right-hand sides lane_q[0..NQ-1] (indices into trhs / x), each to its
+// relative tolerance tol[l]; the correction is added to x[lane_q[l]]. Returns the
+// iterations of each lane.
+template <int NQ>
+static ls_status inner_solve(ls_ctx* c, const TBuf& tb, const int lane_q[NQ], const double tol[NQ],
+                             int max_it, double* x[2], int its[NQ]) {
     const Grid g = c->g;
+    const int N = (int)g.N, JK = (int)g.JK, K = g.K;
     const int grid = grid_for(c, g.N);
-    its[0] = its[1] = 0;
-    LS_LAUNCH(c, k_i_init, grid, kBlock, 0, g, iv, mask, c->partials);
-    LS_TRY(finalize_sum(c, grid, 2, S_RED0));
-    LS_LAUNCH(c, k_kry_scalars, 1, 1, 0, c->scal, mask, 0);
-    double rr0[2];
-    LS_TRY(read_scalars(c, S_RED0, 2, rr0));
-    int act = 0;
-    for (int q = 0; q < 2; ++q)
-        if (((mask >> q) & 1) && rr0[q] > 0.0 && rr0[q] == rr0[q]) act |= 1 << q;
-    const double apply_bytes_per_rhs = (double)g.N * 4.0 * (1 + 1 + 1);  // in, out, rh or s
-    int it = 0;
-    while (act && it < max_it) {
-        const int nact = (act & 1) + ((act >> 1) & 1);
-        // scaled off-diagonals 6x4 per row + per live vector: input, output, rhat/s
-        const double apply_bytes = (double)g.N * 24.0 + apply_bytes_per_rhs * nact;
-        LS_LAUNCH(c, k_i_p, grid, kBlock, 0, g, iv, act, (const double*)c->scal);
-        {
-            Timed tm(c, LS_T_KRY_APPLY);
-            LS_LAUNCH(c, k_i_v, grid, kBlock, 0, g, tb, iv, act, c->partials);
-            if (c->timing) c->timer_bytes[LS_T_KRY_APPLY] += apply_bytes;
+    TIVec iv;
+    float** vecs[7] = {&iv.r, &iv.rh, &iv.p, &iv.v, &iv.s, &iv.t, &iv.d};
+    for (int v = 0; v < 7; ++v) *vecs[v] = c->ti + (size_t)v * c->ti_stride + 2 * c->ti_pad;
+    iv.rhs[0] = c->trhs[lane_q[0]];
+    iv.rhs[1] = c->trhs[NQ > 1 ? lane_q[1] : lane_q[0]];
+    TOff op;
+    for (int d = 0; d < 6; ++d) op.o[d] = tb.o[d];
+    const double t0 = tol[0] * tol[0], t1 = NQ > 1 ? tol[1] * tol[1] : 0.0;
+    LS_LAUNCH(c, k_ti_init<NQ>, grid, kBlock, 0, N, (int)c->ti_pad, iv, c->partials);
+    LS_LAUNCH(c, (k_ti_fin<PH_INIT, NQ>), NQ, kFinalizeThreads, 0, (const double*)c->partials, grid, c->scal,
+              c->tcount, t0, t1);
+    // algorithmic bytes of the two operator applications: FP32 off-diagonals (24 per row)
+    // plus per lane 4 bytes for each vector read or written once
+    const double v_bytes = (double)g.N * (24.0 + 12.0 * NQ);
+    const double st_bytes = (double)g.N * (24.0 + 20.0 * NQ);
+    int it = 0, batch = 4;
+    double sc[TI_STRIDE * 2 + 8];
+    while (it < max_it) {
+        const int nb = std::min(batch, max_it - it);
+        for (int b = 0; b < nb; ++b, ++it) {
+            if (it > 0) LS_LAUNCH(c, k_ti_xp<NQ>, grid, kBlock, 0, N, iv, (const double*)c->scal);
+            {
+                Timed tm(c, LS_T_KRY_APPLY);
+                if (it == 0)
+                    LS_LAUNCH(c, (k_ti_v<NQ, true>), grid, kBlock, 0, N, JK, K, op, iv, (const double*)c->scal,
+                              c->partials);
+                else
+                    LS_LAUNCH(c, (k_ti_v<NQ, false>), grid, kBlock, 0, N, JK, K, op, iv, (const double*)c->scal,
+                              c->partials);
+                if (c->timing) c->timer_bytes[LS_T_KRY_APPLY] += v_bytes + (it == 0 ? 4.0 * NQ * g.N : 0.0);
+            }
+            LS_LAUNCH(c, (k_ti_fin<PH_V, NQ>), NQ, kFinalizeThreads, 0, (const double*)c->partials, grid,
+                      c->scal, c->tcount, 0.0, 0.0);
+            {
+                Timed tm(c, LS_T_KRY_APPLY);
+                LS_LAUNCH(c, k_ti_st<NQ>, grid, kBlock, 0, N, JK, K, op, iv, (const double*)c->scal, c->partials);
+                if (c->timing) c->timer_bytes[LS_T_KRY_APPLY] += st_bytes;
+            }
+            LS_LAUNCH(c, (k_ti_fin<PH_ST, NQ>), 5 * NQ, kFinalizeThreads, 0, (const double*)c->partials, grid,
+                      c->scal, c->tcount, 0.0, 0.0);
         }
-        LS_TRY(finalize_sum(c, grid, 2, S_RED0 + 10));
-        LS_LAUNCH(c, k_kry_scalars, 1, 1, 0, c->scal, act, 1);
-        LS_LAUNCH(c, k_i_s, grid, kBlock, 0, g, iv, act, (const double*)c->scal);
-        {
-            Timed tm(c, LS_T_KRY_APPLY);
-            LS_LAUNCH(c, k_i_t, grid, kBlock, 0, g, tb, iv, act, c->partials);
-            if (c->timing) c->timer_bytes[LS_T_KRY_APPLY] += apply_bytes;
-        }
-        LS_TRY(finalize_sum(c, grid, 4, S_RED0 + 12));
-        LS_LAUNCH(c, k_kry_scalars, 1, 1, 0, c->scal, act, 3);
-        LS_LAUNCH(c, k_i_x, grid, kBlock, 0, g, iv, act, (const double*)c->scal, c->partials);
-        LS_TRY(finalize_sum(c, grid, 4, S_RED0));
-        LS_LAUNCH(c, k_kry_scalars, 1, 1, 0, c->scal, act, 2);
-        it++;
-        double sc[16];
-        LS_TRY(read_scalars(c, ST_BASE, 16, sc));
-        for (int q = 0; q < 2; ++q) {
-            if (!((act >> q) & 1)) continue;
-            its[q] = it;
-            double rho = sc[8 * q + ST_RHO], r2 = sc[8 * q + ST_RR], om = sc[8 * q + ST_OMEGA];
-            bool done = (r2 <= tol[q] * tol[q] * rr0[q]) || r2 != r2 || rho != rho || rho == 0.0 ||
-                        om == 0.0;
-            if (done) act &= ~(1 << q);
+        LS_TRY(read_scalars(c, TI_BASE, TI_ANY - TI_BASE + 1, sc));
+        if (sc[TI_ANY - TI_BASE] == 0.0) break;
+        // next batch: the iterations the observed convergence rate still needs (at least 1)
+        batch = 1;
+        for (int l = 0; l < NQ; ++l) {
+            const double* s = sc + TI_STRIDE * l;
+            if (s[TI_ACT] == 0.0 || !(s[TI_R2] > 0.0) || !(s[TI_RR0] > 0.0) || s[TI_ITS] < 1.0) continue;
+            const double red = s[TI_R2] / s[TI_RR0];
+            const double per_it = log(red) / s[TI_ITS];
+            if (per_it < 0.0) {
+                const double need = log(s[TI_TOL2]) / per_it - s[TI_ITS];
+                batch = std::max(batch, (int)std::min(16.0, std::max(1.0, ceil(need))));
+            }
         }
     }
+    LS_LAUNCH(c, k_ti_accum<NQ>, grid, kBlock, 0, N, iv, (const double*)c->scal, x[lane_q[0]],
+              NQ > 1 ? x[lane_q[1]] : (double*)nullptr);
+    for (int l = 0; l < NQ; ++l) its[l] = (int)sc[TI_STRIDE * l + TI_ITS];
     return LS_OK;
 }
 
@@ -583,7 +769,6 @@ static ls_status mixed_solve(ls_ctx* c, const Rows<L>& rows, int nrhs, const dou
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
     TBuf tb = make_tbuf(c);
-    IVec iv = make_ivec(c);
     LS_LAUNCH(c, k_t_setup<L>, grid, kBlock, 0, rows, tb, nrhs, f0, f1, c->partials);
     LS_TRY(finalize_sum(c, grid, 2, S_RED0 + 4));
     LS_LAUNCH(c, k_t_xid, grid, kBlock, 0, g, tb, x0, x1, nrhs);
@@ -595,7 +780,7 @@ static ls_status mixed_solve(ls_ctx* c, const Rows<L>& rows, int nrhs, const dou
     int stagnant[2] = {0, 0};
     const int max_sweeps = 40;
     while (mask) {
-        LS_LAUNCH(c, k_t_resid, grid, kBlock, 0, g, tb, x0, x1, iv.v[0][IV_RHS], iv.v[1][IV_RHS], mask,
+        LS_LAUNCH(c, k_t_resid, grid, kBlock, 0, g, tb, x0, x1, c->trhs[0], c->trhs[1], mask,
                   c->partials);
         LS_TRY(finalize_sum(c, grid, 4, S_RED0));
         double h[4];
@@ -618,12 +803,16 @@ static ls_status mixed_solve(ls_ctx* c, const Rows<L>& rows, int nrhs, const dou
             solve_mask |= 1 << q;
         }
         if (!solve_mask) break;
-        int iits[2] = {0, 0};
-        int budget = max_it - std::max(its[0], its[1]);
-        LS_TRY(inner_bicgstab(c, tb, iv, solve_mask, tol, std::max(budget, 1), iits));
+        int lane_q[2] = {0, 0}, nq = 0;
         for (int q = 0; q < 2; ++q)
-            if ((solve_mask >> q) & 1) { its[q] += iits[q]; sweeps[q]++; }
-        LS_LAUNCH(c, k_t_accum, grid, kBlock, 0, g, iv.v[0][IV_D], iv.v[1][IV_D], x0, x1, solve_mask);
+            if ((solve_mask >> q) & 1) lane_q[nq++] = q;
+        const double ltol[2] = {tol[lane_q[0]], tol[lane_q[nq - 1]]};
+        int lits[2] = {0, 0};
+        const int budget = std::max(1, max_it - std::max(its[0], its[1]));
+        double* xs[2] = {x0, x1};
+        if (nq == 2) LS_TRY(inner_solve<2>(c, tb, lane_q, ltol, budget, xs, lits));
+        else LS_TRY(inner_solve<1>(c, tb, lane_q, ltol, budget, xs, lits));
+        for (int l = 0; l < nq; ++l) { its[lane_q[l]] += lits[l]; sweeps[lane_q[l]]++; }
     }
     ls_status st = LS_OK;
     double* xs[2] = {x0, x1};
