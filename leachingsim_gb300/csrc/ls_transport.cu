@@ -36,7 +36,10 @@ struct TransConst {
 
 // Coefficients of one transport row: diag, off[6] (+i,-i,+j,-j,+k,-k) and the explicit
 // right-hand-side part for field f (f may be null). kind: 1 identity, 2 coupled.
-template <typename L>
+// EXPL = false is the fully implicit case theta = 1: the theta factors are 1 and the
+// explicit part (1 - theta) * (...) adds zero to the right-hand side (for finite fields), so
+// both are left out, which takes most of the FP64 work out of the row.
+template <typename L, bool EXPL = true>
 __device__ __forceinline__ int trans_row(const Grid& g, const TransConst& tc,
                                          const L* __restrict__ label,
                                          const double* __restrict__ fx,
@@ -100,10 +103,15 @@ __device__ __forceinline__ int trans_row(const Grid& g, const TransConst& tc,
         double adv_coeff = tc.dd.div(actual_q_face);
         if (adv_coeff > 0) coeff_self += adv_coeff;
         else coeff_neighbor -= adv_coeff;
-        off[d] = tc.theta * coeff_neighbor;
-        dg += tc.theta * coeff_self;
-        if (f0) rhs[0] += (1.0 - tc.theta) * (-(coeff_self * fr0 + coeff_neighbor * f0[nb]));
-        if (f1) rhs[1] += (1.0 - tc.theta) * (-(coeff_self * fr1 + coeff_neighbor * f1[nb]));
+        if (EXPL) {
+            off[d] = tc.theta * coeff_neighbor;
+            dg += tc.theta * coeff_self;
+            if (f0) rhs[0] += (1.0 - tc.theta) * (-(coeff_self * fr0 + coeff_neighbor * f0[nb]));
+            if (f1) rhs[1] += (1.0 - tc.theta) * (-(coeff_self * fr1 + coeff_neighbor * f1[nb]));
+        } else {
+            off[d] = coeff_neighbor;
+            dg += coeff_self;
+        }
     }
     diag = dg;
     return 2;
@@ -183,7 +191,18 @@ struct TBuf {
     int8_t* kind;
 };
 
-template <typename L>
+// 1/d for d > 0 (a positive diagonal sum) without an FP64 division: an FP32 reciprocal
+// refined by two Newton-Raphson steps y <- y + y (1 - d y), accurate to about 1 ulp. The
+// reciprocal only scales the inner system and the residual norm.
+__device__ __forceinline__ double recip_nr(double d) {
+    double y = (double)__frcp_rn((float)d);
+    double e = __fma_rn(-d, y, 1.0);
+    y = __fma_rn(y, e, y);
+    e = __fma_rn(-d, y, 1.0);
+    return __fma_rn(y, e, y);
+}
+
+template <typename L, bool EXPL>
 __global__ void __launch_bounds__(kBlock) k_t_setup(Rows<L> op, TBuf tb, int nrhs, const double* f0,
                                                     const double* f1, double* __restrict__ partials) {
     double acc[2] = {0.0, 0.0};
@@ -195,16 +214,17 @@ __global__ void __launch_bounds__(kBlock) k_t_setup(Rows<L> op, TBuf tb, int nrh
         double dg, off[6], rhs[2] = {0.0, 0.0};
         int kind;
         if (op.mode == 0)
-            kind = trans_row(g, op.tc, op.label, op.fx, op.fy, op.fz, r, i, j, k, dg, off, f0, f1, rhs);
+            kind = trans_row<L, EXPL>(g, op.tc, op.label, op.fx, op.fy, op.fz, r, i, j, k, dg, off, f0, f1, rhs);
         else
             kind = sat_row(g, op.sc, op.label, op.fx, op.fy, op.fz, op.s, r, i, j, k, dg, off, rhs);
-        const double inv = 1.0 / dg;  // the one FP64 division of the row
+        const double inv = (dg > 1e-30 && dg < 1e30) ? recip_nr(dg) : 1.0 / dg;
+        const float inv32 = (float)inv;
         tb.c[0][r] = dg;
         tb.inv[r] = inv;
 #pragma unroll
         for (int d = 0; d < 6; ++d) {
             tb.c[1 + d][r] = off[d];
-            tb.o[d][r] = (float)(off[d] * inv);
+            tb.o[d][r] = (float)off[d] * inv32;
         }
         tb.kind[r] = (int8_t)kind;
         for (int q = 0; q < nrhs; ++q) {
@@ -769,7 +789,10 @@ static ls_status mixed_solve(ls_ctx* c, const Rows<L>& rows, int nrhs, const dou
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
     TBuf tb = make_tbuf(c);
-    LS_LAUNCH(c, k_t_setup<L>, grid, kBlock, 0, rows, tb, nrhs, f0, f1, c->partials);
+    if (rows.mode == 0 && rows.tc.theta != 1.0)
+        LS_LAUNCH(c, (k_t_setup<L, true>), grid, kBlock, 0, rows, tb, nrhs, f0, f1, c->partials);
+    else
+        LS_LAUNCH(c, (k_t_setup<L, false>), grid, kBlock, 0, rows, tb, nrhs, f0, f1, c->partials);
     LS_TRY(finalize_sum(c, grid, 2, S_RED0 + 4));
     LS_LAUNCH(c, k_t_xid, grid, kBlock, 0, g, tb, x0, x1, nrhs);
     double den[2];
