@@ -147,10 +147,12 @@ def run_steps(ctx, t0, n0, count, dt):
 
 
 def roofline(ctx, shape, nsteps):
-    """Roofline of the dominant kernel class, the transport operator apply (k_kry_v and
-    k_kry_t of the BiCGStab). The library accumulates its algorithmic bytes per launch:
-    N x (label 1 + own flux 3x8 + per live right-hand side: input 8 + output 8 + rhat or s 8);
-    one right-hand side is live in a fresh run (the acid field is zero)."""
+    """Roofline of the dominant kernel class, the transport operator applications of the
+    inner BiCGStab (k_ti_v and k_ti_st). The library accumulates their algorithmic bytes per
+    launch: N x (six FP32 scaled off-diagonals 24 + per live right-hand side 4 bytes for each
+    vector read or written once: 12 for v = A p (p in, rhat in, v out; 16 on the first
+    iteration, which also stores p = r), 20 for s = r - alpha v, t = A s (r, v, rhat in; s, t
+    out)); one right-hand side is live in this workload (the acid field is zero)."""
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peaks = json.load(open(peaks_path)) if os.path.exists(peaks_path) else None
     ms, cnt = ctx.timing_get("kry_apply")
@@ -160,7 +162,7 @@ def roofline(ctx, shape, nsteps):
     achieved = nbytes / (ms / 1e3) / 1e9
     peak, src = (peaks["hbm_gbs"], "measured") if peaks else (6800.0, "fallback")
     vox = shape[0] * shape[1] * shape[2]
-    return {"bound": "hbm", "kernel": "transport operator apply (k_kry_v, k_kry_t)",
+    return {"bound": "hbm", "kernel": "transport operator apply (k_ti_v, k_ti_st)",
             "achieved": round(achieved, 1), "peak": peak, "peak_source": src, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": None,
             "bytes_per_launch": round(nbytes / cnt), "bytes_per_voxel": round(nbytes / cnt / vox, 2),
@@ -197,12 +199,16 @@ def gpu_arm(args, ws, rank, local):
     ctx.timing_reset()
     barrier()
     with ClockSampler(local) as clk:
+        if args.nvtx:
+            torch.cuda.nvtx.range_push("timed")
         ev0.record(stream)
         w0 = time.perf_counter()
         t, n, infos = run_steps(ctx, t, n, args.steps, DT)
         ev1.record(stream)
         ev1.synchronize()
         wall = time.perf_counter() - w0
+        if args.nvtx:
+            torch.cuda.nvtx.range_pop()
     barrier()
     dev_ms = ev0.elapsed_time(ev1)
     launches = ctx.launches()
@@ -348,6 +354,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--nvtx", action="store_true",
+                    help="wrap the timed steps in an NVTX range 'timed' (for ncu --nvtx-include timed/)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.warmup < 3 and args.impl == "ours":

@@ -93,6 +93,49 @@ inline DxDiv make_dxdiv(double dx) {
     return d;
 }
 
+// FP64 tests and narrowing on the integer pipe. GB300 issues FP64 compares and FP64 <->
+// FP32 conversions on its FP64 pipe (2 operations per clock per SM, the cost of an FMA),
+// which bounds the per-voxel FP64 kernels; these give the same results as the FP64
+// instructions (NaN included) from the bit patterns.
+__device__ __forceinline__ bool disnan(double x) {
+    return (__double_as_longlong(x) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+}
+__device__ __forceinline__ bool dpos(double x) {  // x > 0
+    const long long b = __double_as_longlong(x);
+    return b > 0 && b <= 0x7ff0000000000000ll;
+}
+
+// double -> float rounded toward zero (|x| < 2^-126 -> +-0, |x| >= 2^128 -> +-Inf, NaN ->
+// NaN); for FP32 copies whose rounding does not matter.
+__device__ __forceinline__ float d2f_rz(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7ff) - 1023;
+    const unsigned int mant = (unsigned int)((b >> 29) & 0x7fffffu);
+    unsigned int out = sign | ((unsigned int)(e + 127) << 23) | mant;
+    if (e < -126) out = sign;
+    if (e > 127) out = sign | 0x7f800000u;
+    if (e == 1024) out = sign | 0x7f800000u | ((b & 0xfffffffffffffull) ? 0x400000u : 0u);
+    return __uint_as_float(out);
+}
+
+// 1/d for positive d in [2^-125, 2^126) (others: the FP64 division), within about an ulp:
+// the FP32 reciprocal of the truncated significand, moved to FP64 on the integer pipe,
+// then two Newton-Raphson steps y <- y + y (1 - d y). For scalings, not reference values.
+__device__ __forceinline__ double drcp_nr(double d) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023;
+    if ((b >> 63) || e < -125 || e > 125) return 1.0 / d;
+    const float f = __uint_as_float(((unsigned int)(e + 127) << 23) | (unsigned int)((b >> 29) & 0x7fffffu));
+    float yf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(f));
+    const unsigned int yb = __float_as_uint(yf);
+    double y = __longlong_as_double((long long)(((unsigned long long)(((yb >> 23) & 0xffu) - 127 + 1023) << 52) |
+                                                ((unsigned long long)(yb & 0x7fffffu) << 29)));
+    y = __fma_rn(y, __fma_rn(-d, y, 1.0), y);
+    return __fma_rn(y, __fma_rn(-d, y, 1.0), y);
+}
+
 // Timed region record.
 struct TimedRegion {
     int timer;

@@ -72,10 +72,13 @@ __global__ void __launch_bounds__(kBlock) k_props(Grid g, PropsConst pc, const L
             else if (p_frac == 1.0) K_intrinsic = pc.k_clogged_pore;
             else K_intrinsic = pow(10.0, (p_frac * pc.log_k_rock) + ((1.0 - p_frac) * pc.log_k_pore));
         } else if (t == kSulphide) {
-            double f = (double)frac[r];
-            if (f == 1.0) K_intrinsic = pc.k_clogged_pore;
-            else if (f == 0.0) K_intrinsic = pc.k_clean_pore;
-            else K_intrinsic = pow(10.0, (f * pc.log_k_rock) + ((1.0 - f) * pc.log_k_pore));
+            const float ff = frac[r];
+            if (ff == 1.0f) K_intrinsic = pc.k_clogged_pore;
+            else if (ff == 0.0f) K_intrinsic = pc.k_clean_pore;
+            else {
+                const double f = (double)ff;
+                K_intrinsic = pow(10.0, (f * pc.log_k_rock) + ((1.0 - f) * pc.log_k_pore));
+            }
         }
         visc[r] = (t == kAir) ? 1.8e-5 : 1.0e-3;
         perm[r] = K_intrinsic * smax(krv, 1e-15);
@@ -188,7 +191,8 @@ __device__ __forceinline__ void sat_rates(const Grid& g, const L* __restrict__ l
         if (j > 0 && (int)label[r - g.K] == kAir) air_faces++;
         if (k + 1 < g.K && (int)label[r + 1] == kAir) air_faces++;
         if (k > 0 && (int)label[r - 1] == kAir) air_faces++;
-        evap_sink = dd.div(air_faces * evap);
+        // with evap = +0 the sink is air_faces * +0 = +0
+        evap_sink = (__double_as_longlong(evap) == 0) ? 0.0 : dd.div(air_faces * evap);
     }
 }
 

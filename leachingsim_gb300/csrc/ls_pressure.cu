@@ -165,12 +165,12 @@ __global__ void __launch_bounds__(kBlock) k_press_setup(Grid g, PressConst pcst,
     block_sum_store<1>(acc, partials);
 }
 
-// 1/sqrt(d) of the inner unknowns (normal Pore rows).
+// 1/|d| of the normal Pore rows (weights of the scaled residual norm).
 __global__ void k_press_isd(Grid g, const int8_t* __restrict__ kind, const double* __restrict__ diag,
                             double* __restrict__ isd) {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x)
-        isd[r] = (kind[r] == 2) ? 1.0 / sqrt(-diag[r]) : 0.0;
+        isd[r] = (kind[r] == 2) ? drcp_nr(-diag[r]) : 0.0;
 }
 
 // largest diagonal magnitude of the normal Pore rows (for the inner scaling sigma)
@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(kBlock) k_press_guess_dots(Grid g, const int8_
             else fixed += t;
         }
         const double u = b[r] - fixed;
-        const double id2 = (kd == 2) ? isd[r] * isd[r] : 1e16;
+        const double id2 = (kd == 2) ? isd[r] : 1e16;
         const double w = id2 * id2;
         acc[0] += u * u * w;
         acc[1] += u * free * w;
@@ -289,6 +289,23 @@ __device__ __forceinline__ double press_row_apply(const Grid& g, long long r, in
     if (k + 1 < g.K) acc += f2[r] * x[r + 1];
     if (j + 1 < g.J) acc += f1[r] * x[r + g.K];
     if (i + 1 < g.I) acc += f0[r] * x[r + g.JK];
+    return acc;
+}
+
+// The same row product with fused multiply-adds, for the residual of the iterative solve
+// (one FP64 operation per term instead of two; the residual is not a reference value).
+__device__ __forceinline__ double press_row_apply_fma(const Grid& g, long long r, int i, int j, int k,
+                                                      double dg, const double* __restrict__ x,
+                                                      const double* __restrict__ f0,
+                                                      const double* __restrict__ f1,
+                                                      const double* __restrict__ f2) {
+    double acc = dg * x[r];
+    if (i > 0) acc = __fma_rn(f0[r - g.JK], x[r - g.JK], acc);
+    if (j > 0) acc = __fma_rn(f1[r - g.K], x[r - g.K], acc);
+    if (k > 0) acc = __fma_rn(f2[r - 1], x[r - 1], acc);
+    if (k + 1 < g.K) acc = __fma_rn(f2[r], x[r + 1], acc);
+    if (j + 1 < g.J) acc = __fma_rn(f1[r], x[r + g.K], acc);
+    if (i + 1 < g.I) acc = __fma_rn(f0[r], x[r + g.JK], acc);
     return acc;
 }
 
@@ -330,17 +347,18 @@ __global__ void __launch_bounds__(kBlock) k_press_residual(Grid g, const int8_t*
         double xv = x[r];
         mx[0] = smax(mx[0], xv);
         mx[1] = smax(mx[1], -xv);
-        if (xv != xv) acc[1] += 1.0;
+        if (disnan(xv)) acc[1] += 1.0;
         double rv = 0.0;
         if (kd >= 2) {
             int i, j, k;
             decode(g, r, i, j, k);
             double dg = diag[r];
-            rv = b[r] - press_row_apply(g, r, i, j, k, dg, x, f0, f1, f2);
+            rv = b[r] - press_row_apply_fma(g, r, i, j, k, dg, x, f0, f1, f2);
             // (r / diag)^2 without an FP64 division: 1/diag^2 = isd^4 for normal rows
-            double id2 = (kd == 2) ? isd[r] * isd[r] : 1e16;  // floored rows: diag = 1e-16
-            acc[0] += rv * rv * (id2 * id2);
-            if (rv != rv) acc[1] += 1.0;
+            double id2 = (kd == 2) ? isd[r] : 1e16;  // 1/|diag|; floored rows: diag = 1e-16
+            const double wr = rv * id2;
+            acc[0] = __fma_rn(wr, wr, acc[0]);
+            if (disnan(rv)) acc[1] += 1.0;
         }
         res[r] = rv;
     }

@@ -101,7 +101,7 @@ __device__ __forceinline__ int trans_row(const Grid& g, const TransConst& tc,
         double coeff_neighbor = diffusion_coeff;
         double coeff_self = -diffusion_coeff;
         double adv_coeff = tc.dd.div(actual_q_face);
-        if (adv_coeff > 0) coeff_self += adv_coeff;
+        if (dpos(adv_coeff)) coeff_self += adv_coeff;
         else coeff_neighbor -= adv_coeff;
         if (EXPL) {
             off[d] = tc.theta * coeff_neighbor;
@@ -191,17 +191,6 @@ struct TBuf {
     int8_t* kind;
 };
 
-// 1/d for d > 0 (a positive diagonal sum) without an FP64 division: an FP32 reciprocal
-// refined by two Newton-Raphson steps y <- y + y (1 - d y), accurate to about 1 ulp. The
-// reciprocal only scales the inner system and the residual norm.
-__device__ __forceinline__ double recip_nr(double d) {
-    double y = (double)__frcp_rn((float)d);
-    double e = __fma_rn(-d, y, 1.0);
-    y = __fma_rn(y, e, y);
-    e = __fma_rn(-d, y, 1.0);
-    return __fma_rn(y, e, y);
-}
-
 template <typename L, bool EXPL>
 __global__ void __launch_bounds__(kBlock) k_t_setup(Rows<L> op, TBuf tb, int nrhs, const double* f0,
                                                     const double* f1, double* __restrict__ partials) {
@@ -217,14 +206,15 @@ __global__ void __launch_bounds__(kBlock) k_t_setup(Rows<L> op, TBuf tb, int nrh
             kind = trans_row<L, EXPL>(g, op.tc, op.label, op.fx, op.fy, op.fz, r, i, j, k, dg, off, f0, f1, rhs);
         else
             kind = sat_row(g, op.sc, op.label, op.fx, op.fy, op.fz, op.s, r, i, j, k, dg, off, rhs);
-        const double inv = (dg > 1e-30 && dg < 1e30) ? recip_nr(dg) : 1.0 / dg;
-        const float inv32 = (float)inv;
+        // the row scaling (not a reference value): reciprocal without an FP64 division
+        const double inv = drcp_nr(dg);
+        const float inv32 = d2f_rz(inv);
         tb.c[0][r] = dg;
         tb.inv[r] = inv;
 #pragma unroll
         for (int d = 0; d < 6; ++d) {
             tb.c[1 + d][r] = off[d];
-            tb.o[d][r] = (float)off[d] * inv32;
+            tb.o[d][r] = d2f_rz(off[d]) * inv32;
         }
         tb.kind[r] = (int8_t)kind;
         for (int q = 0; q < nrhs; ++q) {
@@ -273,14 +263,14 @@ __global__ void __launch_bounds__(kBlock) k_t_resid(Grid g, TBuf tb, double* x0,
         if (mask & 1) {
             double rv = (tb.b[0][r] - t_row_apply(g, tb, r, i, j, k, x0)) * inv;
             r0[r] = (float)rv;
-            acc[0] += rv * rv;
-            if (rv != rv) acc[2] += 1.0;
+            acc[0] = __fma_rn(rv, rv, acc[0]);
+            if (disnan(rv)) acc[2] += 1.0;
         }
         if (mask & 2) {
             double rv = (tb.b[1][r] - t_row_apply(g, tb, r, i, j, k, x1)) * inv;
             r1[r] = (float)rv;
-            acc[1] += rv * rv;
-            if (rv != rv) acc[3] += 1.0;
+            acc[1] = __fma_rn(rv, rv, acc[1]);
+            if (disnan(rv)) acc[3] += 1.0;
         }
     }
     block_sum_store<4>(acc, partials);
