@@ -507,6 +507,124 @@ __global__ void __launch_bounds__(kBlock) k_ti_xp(int N, TIVec iv, const double*
     }
 }
 
+// Single right-hand side with an even row length K: each thread takes a pair of rows
+// (r, r+1), r even, with 8-byte loads (the +-j and +-i neighbours of an even row are even as
+// K and J*K are even; the -k neighbour of r and the +k neighbour of r+1 are single loads).
+// Same arithmetic per row as k_ti_v / k_ti_st / k_ti_xp, half the load instructions.
+
+__device__ __forceinline__ float2 ti_apply_pair(const TOff& op, int t, int JK2, int K2,
+                                                const float* __restrict__ x) {
+    const float2* __restrict__ x2 = reinterpret_cast<const float2*>(x);
+    const int r = 2 * t;
+    const float2 xc = x2[t], xim = x2[t - JK2], xjm = x2[t - K2], xjp = x2[t + K2], xip = x2[t + JK2];
+    const float xkm = x[r - 1], xkp = x[r + 2];
+    const float2 o0 = __ldg(reinterpret_cast<const float2*>(op.o[0]) + t);
+    const float2 o1 = __ldg(reinterpret_cast<const float2*>(op.o[1]) + t);
+    const float2 o2 = __ldg(reinterpret_cast<const float2*>(op.o[2]) + t);
+    const float2 o3 = __ldg(reinterpret_cast<const float2*>(op.o[3]) + t);
+    const float2 o4 = __ldg(reinterpret_cast<const float2*>(op.o[4]) + t);
+    const float2 o5 = __ldg(reinterpret_cast<const float2*>(op.o[5]) + t);
+    float y0 = xc.x, y1 = xc.y;
+    y0 = __fmaf_rn(o1.x, xim.x, y0); y1 = __fmaf_rn(o1.y, xim.y, y1);
+    y0 = __fmaf_rn(o3.x, xjm.x, y0); y1 = __fmaf_rn(o3.y, xjm.y, y1);
+    y0 = __fmaf_rn(o5.x, xkm, y0);   y1 = __fmaf_rn(o5.y, xc.x, y1);
+    y0 = __fmaf_rn(o4.x, xc.y, y0);  y1 = __fmaf_rn(o4.y, xkp, y1);
+    y0 = __fmaf_rn(o2.x, xjp.x, y0); y1 = __fmaf_rn(o2.y, xjp.y, y1);
+    y0 = __fmaf_rn(o0.x, xip.x, y0); y1 = __fmaf_rn(o0.y, xip.y, y1);
+    return make_float2(y0, y1);
+}
+
+template <bool FIRST>
+__global__ void __launch_bounds__(kBlock) k_ti_v_pair(int N2, int JK2, int K2, TOff op, TIVec iv,
+                                                      const double* __restrict__ scal,
+                                                      double* __restrict__ partials) {
+    if (scal[TI_ANY] == 0.0) return;
+    const float* __restrict__ X = FIRST ? iv.r : iv.p;
+    const float2* __restrict__ RH = reinterpret_cast<const float2*>(iv.rh);
+    float2* __restrict__ VV = reinterpret_cast<float2*>(iv.v);
+    float2* __restrict__ P = reinterpret_cast<float2*>(iv.p);
+    float acc = 0.f;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N2; t += gridDim.x * blockDim.x) {
+        const float2 y = ti_apply_pair(op, t, JK2, K2, X);
+        VV[t] = y;
+        if (FIRST) P[t] = reinterpret_cast<const float2*>(X)[t];
+        const float2 h = RH[t];
+        acc = __fmaf_rn(h.x, y.x, acc);
+        acc = __fmaf_rn(h.y, y.y, acc);
+    }
+    double a[1] = {acc};
+    block_sum_store<1>(a, partials);
+}
+
+__global__ void __launch_bounds__(kBlock) k_ti_st_pair(int N2, int JK2, int K2, TOff op, TIVec iv,
+                                                       const double* __restrict__ scal,
+                                                       double* __restrict__ partials) {
+    if (scal[TI_ANY] == 0.0) return;
+    const float* __restrict__ R = iv.r;
+    const float* __restrict__ VV = iv.v;
+    const float2* __restrict__ R2 = reinterpret_cast<const float2*>(iv.r);
+    const float2* __restrict__ V2 = reinterpret_cast<const float2*>(iv.v);
+    const float2* __restrict__ RH = reinterpret_cast<const float2*>(iv.rh);
+    float2* __restrict__ S = reinterpret_cast<float2*>(iv.s);
+    float2* __restrict__ T = reinterpret_cast<float2*>(iv.t);
+    const float na = -(float)scal[tslot(0, TI_ALPHA)];
+    float acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N2; t += gridDim.x * blockDim.x) {
+        const int r = 2 * t;
+        auto s2 = [&](int u) {
+            const float2 rv = R2[u], vv = V2[u];
+            return make_float2(__fmaf_rn(na, vv.x, rv.x), __fmaf_rn(na, vv.y, rv.y));
+        };
+        const float2 sc = s2(t), sim = s2(t - JK2), sjm = s2(t - K2), sjp = s2(t + K2), sip = s2(t + JK2);
+        const float skm = __fmaf_rn(na, VV[r - 1], R[r - 1]);
+        const float skp = __fmaf_rn(na, VV[r + 2], R[r + 2]);
+        const float2 o0 = __ldg(reinterpret_cast<const float2*>(op.o[0]) + t);
+        const float2 o1 = __ldg(reinterpret_cast<const float2*>(op.o[1]) + t);
+        const float2 o2 = __ldg(reinterpret_cast<const float2*>(op.o[2]) + t);
+        const float2 o3 = __ldg(reinterpret_cast<const float2*>(op.o[3]) + t);
+        const float2 o4 = __ldg(reinterpret_cast<const float2*>(op.o[4]) + t);
+        const float2 o5 = __ldg(reinterpret_cast<const float2*>(op.o[5]) + t);
+        float t0 = sc.x, t1 = sc.y;
+        t0 = __fmaf_rn(o1.x, sim.x, t0); t1 = __fmaf_rn(o1.y, sim.y, t1);
+        t0 = __fmaf_rn(o3.x, sjm.x, t0); t1 = __fmaf_rn(o3.y, sjm.y, t1);
+        t0 = __fmaf_rn(o5.x, skm, t0);   t1 = __fmaf_rn(o5.y, sc.x, t1);
+        t0 = __fmaf_rn(o4.x, sc.y, t0);  t1 = __fmaf_rn(o4.y, skp, t1);
+        t0 = __fmaf_rn(o2.x, sjp.x, t0); t1 = __fmaf_rn(o2.y, sjp.y, t1);
+        t0 = __fmaf_rn(o0.x, sip.x, t0); t1 = __fmaf_rn(o0.y, sip.y, t1);
+        S[t] = sc;
+        T[t] = make_float2(t0, t1);
+        const float2 h = RH[t];
+        acc[0] = __fmaf_rn(t0, sc.x, acc[0]); acc[0] = __fmaf_rn(t1, sc.y, acc[0]);
+        acc[1] = __fmaf_rn(t0, t0, acc[1]);   acc[1] = __fmaf_rn(t1, t1, acc[1]);
+        acc[2] = __fmaf_rn(h.x, sc.x, acc[2]); acc[2] = __fmaf_rn(h.y, sc.y, acc[2]);
+        acc[3] = __fmaf_rn(h.x, t0, acc[3]);  acc[3] = __fmaf_rn(h.y, t1, acc[3]);
+        acc[4] = __fmaf_rn(sc.x, sc.x, acc[4]); acc[4] = __fmaf_rn(sc.y, sc.y, acc[4]);
+    }
+    double a[5] = {acc[0], acc[1], acc[2], acc[3], acc[4]};
+    block_sum_store<5>(a, partials);
+}
+
+// k_ti_xp on pairs of rows (8-byte loads and stores)
+__global__ void __launch_bounds__(kBlock) k_ti_xp_pair(int N2, TIVec iv, const double* __restrict__ scal) {
+    if (scal[TI_ANY] == 0.0) return;
+    const float2* __restrict__ S = reinterpret_cast<const float2*>(iv.s);
+    const float2* __restrict__ T = reinterpret_cast<const float2*>(iv.t);
+    const float2* __restrict__ VV = reinterpret_cast<const float2*>(iv.v);
+    float2* __restrict__ R = reinterpret_cast<float2*>(iv.r);
+    float2* __restrict__ P = reinterpret_cast<float2*>(iv.p);
+    float2* __restrict__ D = reinterpret_cast<float2*>(iv.d);
+    const float a = (float)scal[tslot(0, TI_ALPHA)];
+    const float w = (float)scal[tslot(0, TI_OMEGA)];
+    const float b = (float)scal[tslot(0, TI_BETA)];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N2; t += gridDim.x * blockDim.x) {
+        const float2 s = S[t], tt = T[t], p = P[t], v = VV[t], d = D[t];
+        const float2 rn = make_float2(__fmaf_rn(-w, tt.x, s.x), __fmaf_rn(-w, tt.y, s.y));
+        D[t] = make_float2(__fmaf_rn(a, p.x, __fmaf_rn(w, s.x, d.x)), __fmaf_rn(a, p.y, __fmaf_rn(w, s.y, d.y)));
+        R[t] = rn;
+        P[t] = make_float2(__fmaf_rn(b, __fmaf_rn(-w, v.x, p.x), rn.x), __fmaf_rn(b, __fmaf_rn(-w, v.y, p.y), rn.y));
+    }
+}
+
 // x_lane += d + a p + w s (the pending update of the last iteration)
 template <int NQ>
 __global__ void k_ti_accum(int N, TIVec iv, const double* __restrict__ scal, double* __restrict__ x0,
@@ -725,28 +843,48 @@ static ls_status inner_solve(ls_ctx* c, const TBuf& tb, const int lane_q[NQ], co
     const double st_bytes = (double)g.N * (24.0 + 20.0 * NQ);
     int it = 0, batch = 4;
     double sc[TI_STRIDE * 2 + 8];
+    // one right-hand side and an even row length: paired-row kernels
+    const bool pair = (NQ == 1) && (K % 2 == 0);
+    const int N2 = N / 2, JK2 = JK / 2, K2 = K / 2;
+    const int kgrid = pair ? grid_for(c, N2) : grid;
     while (it < max_it) {
         const int nb = std::min(batch, max_it - it);
         for (int b = 0; b < nb; ++b, ++it) {
-            if (it > 0) LS_LAUNCH(c, k_ti_xp<NQ>, grid, kBlock, 0, N, iv, (const double*)c->scal);
+            if (it > 0) {
+                if (pair) LS_LAUNCH(c, k_ti_xp_pair, kgrid, kBlock, 0, N2, iv, (const double*)c->scal);
+                else LS_LAUNCH(c, k_ti_xp<NQ>, grid, kBlock, 0, N, iv, (const double*)c->scal);
+            }
             {
                 Timed tm(c, LS_T_KRY_APPLY);
-                if (it == 0)
+                if (pair) {
+                    if (it == 0)
+                        LS_LAUNCH(c, k_ti_v_pair<true>, kgrid, kBlock, 0, N2, JK2, K2, op, iv,
+                                  (const double*)c->scal, c->partials);
+                    else
+                        LS_LAUNCH(c, k_ti_v_pair<false>, kgrid, kBlock, 0, N2, JK2, K2, op, iv,
+                                  (const double*)c->scal, c->partials);
+                } else if (it == 0) {
                     LS_LAUNCH(c, (k_ti_v<NQ, true>), grid, kBlock, 0, N, JK, K, op, iv, (const double*)c->scal,
                               c->partials);
-                else
+                } else {
                     LS_LAUNCH(c, (k_ti_v<NQ, false>), grid, kBlock, 0, N, JK, K, op, iv, (const double*)c->scal,
                               c->partials);
+                }
                 if (c->timing) c->timer_bytes[LS_T_KRY_APPLY] += v_bytes + (it == 0 ? 4.0 * NQ * g.N : 0.0);
             }
-            LS_LAUNCH(c, (k_ti_fin<PH_V, NQ>), NQ, kFinalizeThreads, 0, (const double*)c->partials, grid,
+            LS_LAUNCH(c, (k_ti_fin<PH_V, NQ>), NQ, kFinalizeThreads, 0, (const double*)c->partials, kgrid,
                       c->scal, c->tcount, 0.0, 0.0);
             {
                 Timed tm(c, LS_T_KRY_APPLY);
-                LS_LAUNCH(c, k_ti_st<NQ>, grid, kBlock, 0, N, JK, K, op, iv, (const double*)c->scal, c->partials);
+                if (pair)
+                    LS_LAUNCH(c, k_ti_st_pair, kgrid, kBlock, 0, N2, JK2, K2, op, iv, (const double*)c->scal,
+                              c->partials);
+                else
+                    LS_LAUNCH(c, k_ti_st<NQ>, grid, kBlock, 0, N, JK, K, op, iv, (const double*)c->scal,
+                              c->partials);
                 if (c->timing) c->timer_bytes[LS_T_KRY_APPLY] += st_bytes;
             }
-            LS_LAUNCH(c, (k_ti_fin<PH_ST, NQ>), 5 * NQ, kFinalizeThreads, 0, (const double*)c->partials, grid,
+            LS_LAUNCH(c, (k_ti_fin<PH_ST, NQ>), 5 * NQ, kFinalizeThreads, 0, (const double*)c->partials, kgrid,
                       c->scal, c->tcount, 0.0, 0.0);
         }
         LS_TRY(read_scalars(c, TI_BASE, TI_ANY - TI_BASE + 1, sc));
