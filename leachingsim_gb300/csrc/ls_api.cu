@@ -79,6 +79,15 @@ static void resolve_regions(ls_ctx* c) {
 // ---------------------------------------------------------------------------
 // reductions
 
+ls_status wlist_reset(ls_ctx* c) {
+    const size_t n = (size_t)c->g.N;
+    if (!c->wlist) LS_TRY(dalloc_t(c, &c->wlist, n));
+    if (!c->wcount) LS_TRY(dalloc_t(c, &c->wcount, 4));
+    if (!c->dirty) LS_TRY(dalloc_t(c, &c->dirty, n));
+    LS_CUDA(c, cudaMemsetAsync(c->wcount, 0, sizeof(unsigned int), c->stream));
+    return LS_OK;
+}
+
 ls_status finalize_sum(ls_ctx* c, int nblocks, int nvals, int out_slot) {
     LS_LAUNCH(c, k_finalize<false>, nvals, kFinalizeThreads, 0, c->partials, nblocks, nvals,
               c->scal + out_slot);
@@ -323,7 +332,11 @@ ls_status ls_destroy(ls_ctx* c) {
                     c->pisd, c->pr, c->pdelta, c->ie, c->iface[0], c->iface[1], c->iface[2],
                     c->iinvd, c->inner[0], c->inner[1], c->inner[2], c->inner[3],
                     c->inner[4], c->mg0_x, c->mg0_t, c->comp, c->cc_flag, c->tkind, c->tinv, c->dz_list,
-                    c->dz_count, c->dz_level_start, c->partials, c->scal, c->d_int};
+                    c->dz_count, c->dz_level_start, c->partials, c->scal, c->d_int,
+                    c->sh_label, c->sh_sat, c->sh_precip, c->sh_frac, c->shf_label, c->shf_perm,
+                    c->shf_visc, c->dirty, c->sht_label, c->sht_fx, c->sht_fy, c->sht_fz,
+                    c->shq_P, c->shq_C, c->shq_K, c->shq_V, c->shq_fx, c->shq_fy, c->shq_fz,
+                    c->wlist, c->wcount};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     for (double* q : c->tc)
@@ -361,6 +374,7 @@ ls_status ls_set_params(ls_ctx* c, const ls_params* p) {
     LS_TRY(validate_params(c, p));
     c->p = *p;
     c->p_ready = 0;
+    c->props_force = 1;  // the property constants may have changed
     return LS_OK;
 }
 
@@ -395,6 +409,9 @@ static ls_status transfer(ls_ctx* c, ls_field f, void* host, size_t n, int padde
     if (up) {
         LS_CUDA(c, cudaMemcpyAsync(dev, host, n * esz, kind, c->stream));
         if (f == LS_F_LABEL || f == LS_F_PERMEABILITY || f == LS_F_VISCOSITY) c->p_ready = 0;
+        // outputs of the property kernel written from outside: re-evaluate every voxel
+        if (f == LS_F_PERMEABILITY || f == LS_F_VISCOSITY || f == LS_F_CAP_PRESSURE || f == LS_F_REL_PERM)
+            c->props_force = 1;
         if (f == LS_F_PRESSURE) c->p_eff_prev = 0.0;
     } else {
         LS_CUDA(c, cudaMemcpyAsync(host, dev, n * esz, kind, c->stream));
@@ -424,6 +441,7 @@ ls_status ls_init_fields(ls_ctx* c) {
     for (double* q : f) LS_CUDA(c, cudaMemsetAsync(q, 0, bytes, c->stream));
     c->p_ready = 0;
     c->p_eff_prev = 0.0;
+    c->props_force = 1;  // kr and Pc were cleared
     return LS_OK;
 }
 

@@ -136,6 +136,20 @@ __device__ __forceinline__ double drcp_nr(double d) {
     return __fma_rn(y, __fma_rn(-d, y, 1.0), y);
 }
 
+// Append `value` to list[] for every lane with pred set: one atomic per warp (warp-aggregated);
+// the order of the entries is unspecified, so list consumers must not depend on it.
+__device__ __forceinline__ void warp_append(bool pred, int value, int* list, unsigned int* count) {
+    const unsigned int mask = __activemask();
+    const unsigned int ballot = __ballot_sync(mask, pred);
+    if (ballot == 0u) return;
+    const int lane = (int)(threadIdx.x & 31u);
+    const int leader = __ffs(ballot) - 1;
+    unsigned int base = 0u;
+    if (lane == leader) base = atomicAdd(count, (unsigned int)__popc(ballot));
+    base = __shfl_sync(mask, base, leader);
+    if (pred) list[base + (unsigned int)__popc(ballot & ((1u << lane) - 1u))] = value;
+}
+
 // Timed region record.
 struct TimedRegion {
     int timer;
@@ -188,6 +202,29 @@ struct ls_ctx {
     double p_eff;       // ramped top pressure of the assembled system
     double p_eff_prev;  // ... of the previous solve (0 = none)
     int p_ready;
+
+    // change tracking: the per-voxel property and face kernels keep shadow copies of their
+    // inputs and recompute only voxels whose inputs changed bitwise since their last
+    // evaluation (their results are pure functions of those inputs, so reuse is exact)
+    void* sh_label;       // props inputs at the last evaluation of each voxel
+    double* sh_sat;
+    double* sh_precip;
+    float* sh_frac;
+    void* shf_label;      // pressure-face inputs at the last evaluation
+    double* shf_perm;
+    double* shf_visc;
+    uint8_t* dirty;       // per-voxel scratch flag of the two-pass change tests
+    int* wlist;           // voxel work list of the change-tracked kernels (N entries)
+    unsigned int* wcount; // its length
+    int props_force, faces_force;  // recompute every voxel on the next call
+    void* sht_label;      // transport-row inputs at the last evaluation (fully implicit rows)
+    double *sht_fx, *sht_fy, *sht_fz;
+    int t_valid;          // the stored transport rows are fully implicit rows for t_consts
+    double t_consts[8];
+    double *shq_P, *shq_C, *shq_K, *shq_V;  // flux inputs at the last evaluation
+    double *shq_fx, *shq_fy, *shq_fz;       // the fluxes last computed
+    int flux_valid;
+    double flux_consts[2];
 
     // multigrid: the finest level is the inner system above (vectors mg0_x, mg0_t);
     // mg[l] are the coarse levels, each owning its arrays
@@ -383,6 +420,8 @@ ls_status init_saturation_run(ls_ctx* c);
 
 // allocation helper tracking device bytes
 ls_status dalloc(ls_ctx* c, void** p, size_t bytes);
+// the work list, its counter and the dirty flags, allocated on first use; resets the counter
+ls_status wlist_reset(ls_ctx* c);
 template <typename T>
 ls_status dalloc_t(ls_ctx* c, T** p, size_t n) {
     return dalloc(c, reinterpret_cast<void**>(p), n * sizeof(T));

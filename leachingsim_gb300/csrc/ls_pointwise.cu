@@ -24,64 +24,105 @@ struct PropsConst {
     int vg_n_is_2;           // m = 1/2: Se^(1/m) = Se*Se, (.)^m = sqrt, Se^(-1/m) = 1/(Se*Se)
 };
 
+// updateRelativePermeability / updateCapillaryPressure / initProperties for one voxel from
+// its label t, saturation s, precipitate fraction and mineral fraction.
+__device__ __forceinline__ void props_eval(const PropsConst& pc, int t, double s, double precip_v,
+                                           float ff, double& krv, double& pcv, double& permv,
+                                           double& viscv) {
+    const double pore_permeability = 1.0e-12;
+    const double rock_permeability = 1.0e-18;
+    krv = 0.0;
+    pcv = 0.0;
+    if (t == kPore || t == kSulphide) {
+        // relative permeability, src/Simulation.cpp:1643-1657
+        double Se = (s - pc.s_res) / (1.0 - pc.s_res);
+        double Sk = smax(0.0, smin(1.0, Se));
+        if (Sk <= 0.0) {
+            krv = 0.0;
+        } else {
+            double term1 = pc.vg_n_is_2 ? 1.0 - sqrt(1.0 - Sk * Sk)
+                                        : 1.0 - pow(1.0 - pow(Sk, 1.0 / pc.m), pc.m);
+            krv = sqrt(Sk) * term1 * term1;
+        }
+        // capillary pressure, src/Simulation.cpp:1605-1621
+        double Sc = smax(1e-6, smin(1.0, Se));
+        if (Sc >= 1.0) {
+            pcv = 0.0;
+        } else if (pc.vg_n_is_2) {
+            pcv = pc.inv_alpha * sqrt(1.0 / (Sc * Sc) - 1.0);
+        } else {
+            double Se_inv_m = pow(Sc, -1.0 / pc.m);
+            pcv = pc.inv_alpha * pow(Se_inv_m - 1.0, 1.0 / pc.vg_n);
+        }
+    }
+    // intrinsic permeability and viscosity, src/Simulation.cpp:199-244
+    double K_intrinsic = rock_permeability;
+    if (t == kAir) {
+        K_intrinsic = pore_permeability;
+    } else if (t == kPore) {
+        double p_frac = smax(0.0, smin(1.0, precip_v));
+        if (p_frac == 0.0) K_intrinsic = pc.k_clean_pore;
+        else if (p_frac == 1.0) K_intrinsic = pc.k_clogged_pore;
+        else K_intrinsic = pow(10.0, (p_frac * pc.log_k_rock) + ((1.0 - p_frac) * pc.log_k_pore));
+    } else if (t == kSulphide) {
+        if (ff == 1.0f) K_intrinsic = pc.k_clogged_pore;
+        else if (ff == 0.0f) K_intrinsic = pc.k_clean_pore;
+        else {
+            const double f = (double)ff;
+            K_intrinsic = pow(10.0, (f * pc.log_k_rock) + ((1.0 - f) * pc.log_k_pore));
+        }
+    }
+    viscv = (t == kAir) ? 1.8e-5 : 1.0e-3;
+    permv = K_intrinsic * smax(krv, 1e-15);
+}
+
+// Pass 1: voxels whose label, s, precip or frac differ bitwise from their values at the last
+// evaluation (all voxels when forced) go to the work list, with their new inputs recorded;
+// the others keep their properties, which are a pure function of those inputs.
 template <typename L>
-__global__ void __launch_bounds__(kBlock) k_props(Grid g, PropsConst pc, const L* __restrict__ label,
+__global__ void __launch_bounds__(kBlock) k_props_scan(Grid g, const L* __restrict__ label,
+                                                       const double* __restrict__ sat,
+                                                       const double* __restrict__ precip,
+                                                       const float* __restrict__ frac, L* __restrict__ sl,
+                                                       double* __restrict__ ss, double* __restrict__ sp,
+                                                       float* __restrict__ sf, int force,
+                                                       int* __restrict__ list, unsigned int* __restrict__ count) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < (int)g.N; r += gridDim.x * blockDim.x) {
+        const L lab = label[r];
+        const long long sb = __double_as_longlong(sat[r]);
+        const long long pb = __double_as_longlong(precip[r]);
+        const unsigned int fb = __float_as_uint(frac[r]);
+        const bool d = force || lab != sl[r] || sb != __double_as_longlong(ss[r]) ||
+                       pb != __double_as_longlong(sp[r]) || fb != __float_as_uint(sf[r]);
+        if (d) {
+            sl[r] = lab;
+            ss[r] = __longlong_as_double(sb);
+            sp[r] = __longlong_as_double(pb);
+            sf[r] = __uint_as_float(fb);
+        }
+        warp_append(d, r, list, count);
+    }
+}
+
+// Pass 2: the properties of the listed voxels (dense: every lane has work).
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_props(PropsConst pc, const L* __restrict__ label,
                                                   const double* __restrict__ sat,
                                                   const double* __restrict__ precip,
                                                   const float* __restrict__ frac,
                                                   double* __restrict__ kr, double* __restrict__ cap,
-                                                  double* __restrict__ perm, double* __restrict__ visc) {
-    const double pore_permeability = 1.0e-12;
-    const double rock_permeability = 1.0e-18;
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x) {
-        const int t = (int)label[r];
-        double krv = 0.0, pcv = 0.0;
-        if (t == kPore || t == kSulphide) {
-            const double s = sat[r];
-            // relative permeability, src/Simulation.cpp:1643-1657
-            double Se = (s - pc.s_res) / (1.0 - pc.s_res);
-            double Sk = smax(0.0, smin(1.0, Se));
-            if (Sk <= 0.0) {
-                krv = 0.0;
-            } else {
-                double term1 = pc.vg_n_is_2 ? 1.0 - sqrt(1.0 - Sk * Sk)
-                                            : 1.0 - pow(1.0 - pow(Sk, 1.0 / pc.m), pc.m);
-                krv = sqrt(Sk) * term1 * term1;
-            }
-            // capillary pressure, src/Simulation.cpp:1605-1621
-            double Sc = smax(1e-6, smin(1.0, Se));
-            if (Sc >= 1.0) {
-                pcv = 0.0;
-            } else if (pc.vg_n_is_2) {
-                pcv = pc.inv_alpha * sqrt(1.0 / (Sc * Sc) - 1.0);
-            } else {
-                double Se_inv_m = pow(Sc, -1.0 / pc.m);
-                pcv = pc.inv_alpha * pow(Se_inv_m - 1.0, 1.0 / pc.vg_n);
-            }
-        }
+                                                  double* __restrict__ perm, double* __restrict__ visc,
+                                                  const int* __restrict__ list,
+                                                  const unsigned int* __restrict__ count) {
+    const int n = (int)*count;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int r = list[q];
+        double krv, pcv, pv, vv;
+        props_eval(pc, (int)label[r], sat[r], precip[r], frac[r], krv, pcv, pv, vv);
         kr[r] = krv;
         cap[r] = pcv;
-        // intrinsic permeability and viscosity, src/Simulation.cpp:199-244
-        double K_intrinsic = rock_permeability;
-        if (t == kAir) {
-            K_intrinsic = pore_permeability;
-        } else if (t == kPore) {
-            double p_frac = smax(0.0, smin(1.0, precip[r]));
-            if (p_frac == 0.0) K_intrinsic = pc.k_clean_pore;
-            else if (p_frac == 1.0) K_intrinsic = pc.k_clogged_pore;
-            else K_intrinsic = pow(10.0, (p_frac * pc.log_k_rock) + ((1.0 - p_frac) * pc.log_k_pore));
-        } else if (t == kSulphide) {
-            const float ff = frac[r];
-            if (ff == 1.0f) K_intrinsic = pc.k_clogged_pore;
-            else if (ff == 0.0f) K_intrinsic = pc.k_clean_pore;
-            else {
-                const double f = (double)ff;
-                K_intrinsic = pow(10.0, (f * pc.log_k_rock) + ((1.0 - f) * pc.log_k_pore));
-            }
-        }
-        visc[r] = (t == kAir) ? 1.8e-5 : 1.0e-3;
-        perm[r] = K_intrinsic * smax(krv, 1e-15);
+        perm[r] = pv;
+        visc[r] = vv;
     }
 }
 
@@ -97,13 +138,30 @@ ls_status props_run(ls_ctx* c) {
     pc.k_clean_pore = std::pow(10.0, (0.0 * pc.log_k_rock) + ((1.0 - 0.0) * pc.log_k_pore));
     pc.k_clogged_pore = std::pow(10.0, (1.0 * pc.log_k_rock) + ((1.0 - 1.0) * pc.log_k_pore));
     pc.vg_n_is_2 = (c->p.vg_n == 2.0) ? 1 : 0;
+    const size_t n = (size_t)c->g.N;
+    if (!c->sh_sat) {
+        LS_TRY(dalloc(c, &c->sh_label, n * c->label_bytes));
+        LS_TRY(dalloc_t(c, &c->sh_sat, n));
+        LS_TRY(dalloc_t(c, &c->sh_precip, n));
+        LS_TRY(dalloc_t(c, &c->sh_frac, n));
+        c->props_force = 1;
+    }
+    const int force = c->props_force;
+    c->props_force = 0;
     int grid = grid_for(c, c->g.N);
-    if (c->label_bytes == 1)
-        LS_LAUNCH(c, k_props<uint8_t>, grid, kBlock, 0, c->g, pc, (const uint8_t*)c->label, c->sat,
-                  c->precip, c->frac, c->kr, c->pc, c->perm, c->visc);
-    else
-        LS_LAUNCH(c, k_props<uint16_t>, grid, kBlock, 0, c->g, pc, (const uint16_t*)c->label, c->sat,
-                  c->precip, c->frac, c->kr, c->pc, c->perm, c->visc);
+    LS_TRY(wlist_reset(c));
+    if (c->label_bytes == 1) {
+        LS_LAUNCH(c, k_props_scan<uint8_t>, grid, kBlock, 0, c->g, (const uint8_t*)c->label, c->sat, c->precip,
+                  c->frac, (uint8_t*)c->sh_label, c->sh_sat, c->sh_precip, c->sh_frac, force, c->wlist, c->wcount);
+        LS_LAUNCH(c, k_props<uint8_t>, grid, kBlock, 0, pc, (const uint8_t*)c->label, c->sat, c->precip,
+                  c->frac, c->kr, c->pc, c->perm, c->visc, (const int*)c->wlist, (const unsigned int*)c->wcount);
+    } else {
+        LS_LAUNCH(c, k_props_scan<uint16_t>, grid, kBlock, 0, c->g, (const uint16_t*)c->label, c->sat, c->precip,
+                  c->frac, (uint16_t*)c->sh_label, c->sh_sat, c->sh_precip, c->sh_frac, force, c->wlist,
+                  c->wcount);
+        LS_LAUNCH(c, k_props<uint16_t>, grid, kBlock, 0, pc, (const uint16_t*)c->label, c->sat, c->precip,
+                  c->frac, c->kr, c->pc, c->perm, c->visc, (const int*)c->wlist, (const unsigned int*)c->wcount);
+    }
     c->p_ready = 0;
     return LS_OK;
 }
@@ -120,15 +178,70 @@ __device__ __forceinline__ double grad1(const double* __restrict__ f, long long 
     return dd.pow2 ? d * (0.5 * dd.inv_dx) : d / (2.0 * dd.dx);
 }
 
-__global__ void __launch_bounds__(kBlock) k_flux(Grid g, DxDiv dd, double mcg,
-                                                 const double* __restrict__ P,
-                                                 const double* __restrict__ C,
-                                                 const double* __restrict__ perm,
-                                                 const double* __restrict__ visc,
-                                                 double* __restrict__ fx, double* __restrict__ fy,
-                                                 double* __restrict__ fz) {
+// Change test of the flux inputs (pass 1): bit 0 = P or Pc of the voxel changed (they
+// enter the gradients of its neighbours too), bit 1 = its permeability or viscosity changed,
+// bitwise against the values at the last flux evaluation.
+__global__ void __launch_bounds__(kBlock) k_flux_dirty(Grid g, const double* __restrict__ P,
+                                                       const double* __restrict__ C,
+                                                       const double* __restrict__ perm,
+                                                       const double* __restrict__ visc,
+                                                       double* __restrict__ sP, double* __restrict__ sC,
+                                                       double* __restrict__ sK, double* __restrict__ sV,
+                                                       uint8_t* __restrict__ dirty, int force) {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
+        const long long pb = __double_as_longlong(P[r]), cb = __double_as_longlong(C[r]);
+        const long long kb = __double_as_longlong(perm[r]), vb = __double_as_longlong(visc[r]);
+        const bool d0 = force || pb != __double_as_longlong(sP[r]) || cb != __double_as_longlong(sC[r]);
+        const bool d1 = force || kb != __double_as_longlong(sK[r]) || vb != __double_as_longlong(sV[r]);
+        if (d0) {
+            sP[r] = __longlong_as_double(pb);
+            sC[r] = __longlong_as_double(cb);
+        }
+        if (d1) {
+            sK[r] = __longlong_as_double(kb);
+            sV[r] = __longlong_as_double(vb);
+        }
+        dirty[r] = (d0 ? 1 : 0) | (d1 ? 2 : 0);
+    }
+}
+
+// Pass 2: the flux of a voxel is a pure function of P and Pc at the voxel and its six
+// neighbours and of its own permeability and viscosity. Voxels where one of those changed go
+// to the work list; the others get their last computed flux back (the transport solve zeroes
+// the flux of Rock and Precipitate voxels after use).
+__global__ void __launch_bounds__(kBlock) k_flux_scan(Grid g, const uint8_t* __restrict__ dirty,
+                                                      double* __restrict__ fx, double* __restrict__ fy,
+                                                      double* __restrict__ fz, const double* __restrict__ sfx,
+                                                      const double* __restrict__ sfy,
+                                                      const double* __restrict__ sfz, int* __restrict__ list,
+                                                      unsigned int* __restrict__ count) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < (int)g.N; r += gridDim.x * blockDim.x) {
+        int i, j, k;
+        decode(g, r, i, j, k);
+        const bool d = dirty[r] || (i > 0 && (dirty[r - g.JK] & 1)) || (i + 1 < g.I && (dirty[r + g.JK] & 1)) ||
+                       (j > 0 && (dirty[r - g.K] & 1)) || (j + 1 < g.J && (dirty[r + g.K] & 1)) ||
+                       (k > 0 && (dirty[r - 1] & 1)) || (k + 1 < g.K && (dirty[r + 1] & 1));
+        if (!d) {
+            fx[r] = sfx[r];
+            fy[r] = sfy[r];
+            fz[r] = sfz[r];
+        }
+        warp_append(d, r, list, count);
+    }
+}
+
+// Pass 3: calculateFlux at the listed voxels.
+__global__ void __launch_bounds__(kBlock) k_flux(Grid g, DxDiv dd, double mcg, const double* __restrict__ P,
+                                                 const double* __restrict__ C, const double* __restrict__ perm,
+                                                 const double* __restrict__ visc, double* __restrict__ fx,
+                                                 double* __restrict__ fy, double* __restrict__ fz,
+                                                 double* __restrict__ sfx, double* __restrict__ sfy,
+                                                 double* __restrict__ sfz, const int* __restrict__ list,
+                                                 const unsigned int* __restrict__ count) {
+    const int n = (int)*count;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int r = list[q];
         int i, j, k;
         decode(g, r, i, j, k);
         double gPx = grad1(P, r, g.JK, i, g.I, dd);
@@ -142,16 +255,35 @@ __global__ void __launch_bounds__(kBlock) k_flux(Grid g, DxDiv dd, double mcg,
         gCz = smax(-mcg, smin(mcg, gCz));
         double transmissivity = perm[r] / visc[r];
         const double rho_g = 1000.0 * 9.81;
-        fx[r] = -transmissivity * ((gPx - gCx) - rho_g);
-        fy[r] = -transmissivity * (gPy - gCy);
-        fz[r] = -transmissivity * (gPz - gCz);
+        const double qx = -transmissivity * ((gPx - gCx) - rho_g);
+        const double qy = -transmissivity * (gPy - gCy);
+        const double qz = -transmissivity * (gPz - gCz);
+        fx[r] = qx; fy[r] = qy; fz[r] = qz;
+        sfx[r] = qx; sfy[r] = qy; sfz[r] = qz;
     }
 }
 
 ls_status flux_run(ls_ctx* c) {
     int grid = grid_for(c, c->g.N);
+    const size_t n = (size_t)c->g.N;
+    if (!c->shq_P) {
+        double** arrs[] = {&c->shq_P, &c->shq_C, &c->shq_K, &c->shq_V, &c->shq_fx, &c->shq_fy, &c->shq_fz};
+        for (double** q : arrs) LS_TRY(dalloc_t(c, q, n));
+        c->flux_valid = 0;
+    }
+    const int force = (!c->flux_valid || c->flux_consts[0] != c->p.dx ||
+                       c->flux_consts[1] != c->p.max_cap_grad) ? 1 : 0;
+    LS_TRY(wlist_reset(c));
+    LS_LAUNCH(c, k_flux_dirty, grid, kBlock, 0, c->g, c->P, c->pc, c->perm, c->visc, c->shq_P, c->shq_C,
+              c->shq_K, c->shq_V, c->dirty, force);
+    LS_LAUNCH(c, k_flux_scan, grid, kBlock, 0, c->g, (const uint8_t*)c->dirty, c->fx, c->fy, c->fz,
+              (const double*)c->shq_fx, (const double*)c->shq_fy, (const double*)c->shq_fz, c->wlist, c->wcount);
     LS_LAUNCH(c, k_flux, grid, kBlock, 0, c->g, make_dxdiv(c->p.dx), c->p.max_cap_grad, c->P, c->pc,
-              c->perm, c->visc, c->fx, c->fy, c->fz);
+              c->perm, c->visc, c->fx, c->fy, c->fz, c->shq_fx, c->shq_fy, c->shq_fz, (const int*)c->wlist,
+              (const unsigned int*)c->wcount);
+    c->flux_consts[0] = c->p.dx;
+    c->flux_consts[1] = c->p.max_cap_grad;
+    c->flux_valid = 1;
     return LS_OK;
 }
 

@@ -70,18 +70,60 @@ __device__ __forceinline__ double link_coeff(const L* __restrict__ label,
     return K_avg / visc[self];
 }
 
-// Face coefficients of the +i, +j, +k faces (kernel 1 of 2). A face is used only by the
-// Pore rows on its two sides and gives the same value from either side (the harmonic mean
-// is symmetric bit for bit: (2a)b == (2b)a, a+b == b+a), so it is computed once.
+// Change test of the face inputs (pass 1 of the faces): dirty[r] = label, permeability or
+// viscosity of voxel r differ bitwise from their values at the last face evaluation.
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_faces_dirty(Grid g, const L* __restrict__ label,
+                                                        const double* __restrict__ perm,
+                                                        const double* __restrict__ visc,
+                                                        L* __restrict__ sl, double* __restrict__ sp,
+                                                        double* __restrict__ sv,
+                                                        uint8_t* __restrict__ dirty, int force) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        const L lab = label[r];
+        const long long pb = __double_as_longlong(perm[r]);
+        const long long vb = __double_as_longlong(visc[r]);
+        const bool d = force || lab != sl[r] || pb != __double_as_longlong(sp[r]) ||
+                       vb != __double_as_longlong(sv[r]);
+        if (d) {
+            sl[r] = lab;
+            sp[r] = __longlong_as_double(pb);
+            sv[r] = __longlong_as_double(vb);
+        }
+        dirty[r] = d ? 1 : 0;
+    }
+}
+
+// Pass 2: voxels holding a face (their +i, +j, +k faces) with a dirty voxel on either side.
+__global__ void __launch_bounds__(kBlock) k_faces_scan(Grid g, const uint8_t* __restrict__ dirty,
+                                                       int* __restrict__ list, unsigned int* __restrict__ count) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < (int)g.N; r += gridDim.x * blockDim.x) {
+        int i, j, k;
+        decode(g, r, i, j, k);
+        const bool need = dirty[r] || (i + 1 < g.I && dirty[r + g.JK]) || (j + 1 < g.J && dirty[r + g.K]) ||
+                          (k + 1 < g.K && dirty[r + 1]);
+        warp_append(need, r, list, count);
+    }
+}
+
+// Pass 3: face coefficients of the +i, +j, +k faces of the listed voxels. A face is used
+// only by the Pore rows on its two sides and gives the same value from either side (the
+// harmonic mean is symmetric bit for bit: (2a)b == (2b)a, a+b == b+a), so it is computed
+// once; it is a pure function of the labels, permeabilities and viscosities of its two
+// voxels, so faces between clean voxels keep their stored values.
 template <typename L>
 __global__ void __launch_bounds__(kBlock) k_press_faces(Grid g, const L* __restrict__ label,
                                                         const double* __restrict__ perm,
                                                         const double* __restrict__ visc,
                                                         double* __restrict__ f0,
                                                         double* __restrict__ f1,
-                                                        double* __restrict__ f2) {
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x) {
+                                                        double* __restrict__ f2,
+                                                        const int* __restrict__ list,
+                                                        const unsigned int* __restrict__ count) {
+    const int n = (int)*count;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int r = list[q];
         int i, j, k;
         decode(g, r, i, j, k);
         const int t = (int)label[r];
@@ -92,8 +134,8 @@ __global__ void __launch_bounds__(kBlock) k_press_faces(Grid g, const L* __restr
         for (int d = 0; d < 3; ++d) {
             double cf = 0.0;
             if (hasp[d]) {
-                long long nb = r + offs[d];
-                int tn = (int)label[nb];
+                const long long nb = r + offs[d];
+                const int tn = (int)label[nb];
                 if (t == kPore) cf = link_coeff(label, perm, visc, r, nb);
                 else if (tn == kPore) cf = link_coeff(label, perm, visc, nb, r);
             }
@@ -598,14 +640,33 @@ ls_status pressure_setup_run(ls_ctx* c, double t) {
     pcst.evap_dx = c->p.evaporative_flux * c->p.dx;
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
+    const size_t n = (size_t)g.N;
+    if (!c->shf_perm) {
+        LS_TRY(dalloc(c, &c->shf_label, n * c->label_bytes));
+        LS_TRY(dalloc_t(c, &c->shf_perm, n));
+        LS_TRY(dalloc_t(c, &c->shf_visc, n));
+        c->faces_force = 1;
+    }
+    const int faces_force = c->faces_force;
+    c->faces_force = 0;
+    LS_TRY(wlist_reset(c));
+    if (c->label_bytes == 1)
+        LS_LAUNCH(c, k_faces_dirty<uint8_t>, grid, kBlock, 0, g, (const uint8_t*)c->label, c->perm, c->visc,
+                  (uint8_t*)c->shf_label, c->shf_perm, c->shf_visc, c->dirty, faces_force);
+    else
+        LS_LAUNCH(c, k_faces_dirty<uint16_t>, grid, kBlock, 0, g, (const uint16_t*)c->label, c->perm, c->visc,
+                  (uint16_t*)c->shf_label, c->shf_perm, c->shf_visc, c->dirty, faces_force);
+    LS_LAUNCH(c, k_faces_scan, grid, kBlock, 0, g, (const uint8_t*)c->dirty, c->wlist, c->wcount);
     if (c->label_bytes == 1) {
         LS_LAUNCH(c, k_press_faces<uint8_t>, grid, kBlock, 0, g, (const uint8_t*)c->label, c->perm,
-                  c->visc, c->pface[0], c->pface[1], c->pface[2]);
+                  c->visc, c->pface[0], c->pface[1], c->pface[2], (const int*)c->wlist,
+                  (const unsigned int*)c->wcount);
         LS_LAUNCH(c, k_press_setup<uint8_t>, grid, kBlock, 0, g, pcst, (const uint8_t*)c->label,
                   c->pkind, c->pdiag, c->pb, c->pface[0], c->pface[1], c->pface[2], c->partials);
     } else {
         LS_LAUNCH(c, k_press_faces<uint16_t>, grid, kBlock, 0, g, (const uint16_t*)c->label, c->perm,
-                  c->visc, c->pface[0], c->pface[1], c->pface[2]);
+                  c->visc, c->pface[0], c->pface[1], c->pface[2], (const int*)c->wlist,
+                  (const unsigned int*)c->wcount);
         LS_LAUNCH(c, k_press_setup<uint16_t>, grid, kBlock, 0, g, pcst, (const uint16_t*)c->label,
                   c->pkind, c->pdiag, c->pb, c->pface[0], c->pface[1], c->pface[2], c->partials);
     }

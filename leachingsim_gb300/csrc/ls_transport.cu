@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 
 #include "ls_internal.cuh"
 
@@ -220,6 +221,94 @@ __global__ void __launch_bounds__(kBlock) k_t_setup(Rows<L> op, TBuf tb, int nrh
         for (int q = 0; q < nrhs; ++q) {
             tb.b[q][r] = rhs[q];
             double bt = rhs[q] * inv;
+            acc[q] += bt * bt;
+        }
+    }
+    block_sum_store<2>(acc, partials);
+}
+
+// Change test of the transport-row inputs (pass 1 of the fully implicit setup): dirty[r] =
+// label or own face fluxes of voxel r differ bitwise from their values at the last setup.
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_t_dirty(Grid g, const L* __restrict__ label,
+                                                    const double* __restrict__ fx,
+                                                    const double* __restrict__ fy,
+                                                    const double* __restrict__ fz,
+                                                    L* __restrict__ sl, double* __restrict__ sx,
+                                                    double* __restrict__ sy, double* __restrict__ sz,
+                                                    uint8_t* __restrict__ dirty, int force) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        const L lab = label[r];
+        const long long xb = __double_as_longlong(fx[r]), yb = __double_as_longlong(fy[r]),
+                        zb = __double_as_longlong(fz[r]);
+        const bool d = force || lab != sl[r] || xb != __double_as_longlong(sx[r]) ||
+                       yb != __double_as_longlong(sy[r]) || zb != __double_as_longlong(sz[r]);
+        if (d) {
+            sl[r] = lab;
+            sx[r] = __longlong_as_double(xb);
+            sy[r] = __longlong_as_double(yb);
+            sz[r] = __longlong_as_double(zb);
+        }
+        dirty[r] = d ? 1 : 0;
+    }
+}
+
+// Fully implicit (theta = 1) transport setup. A row is a pure function of its own and its
+// six neighbours' labels and of its own and its lower neighbours' face fluxes; pass 2 lists
+// the rows with a dirty voxel among those, pass 3 recomputes their coefficients, pass 4
+// forms the right-hand sides of every row (old value over dt, or the old value on identity
+// rows) and the partial norms in a fixed order.
+__global__ void __launch_bounds__(kBlock) k_t_scan(Grid g, const uint8_t* __restrict__ dirty,
+                                                   int* __restrict__ list, unsigned int* __restrict__ count) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < (int)g.N; r += gridDim.x * blockDim.x) {
+        int i, j, k;
+        decode(g, r, i, j, k);
+        const bool d = dirty[r] || (i > 0 && dirty[r - g.JK]) || (i + 1 < g.I && dirty[r + g.JK]) ||
+                       (j > 0 && dirty[r - g.K]) || (j + 1 < g.J && dirty[r + g.K]) ||
+                       (k > 0 && dirty[r - 1]) || (k + 1 < g.K && dirty[r + 1]);
+        warp_append(d, r, list, count);
+    }
+}
+
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_t_rows(Rows<L> op, TBuf tb, const int* __restrict__ list,
+                                                   const unsigned int* __restrict__ count) {
+    const Grid& g = op.g;
+    const int n = (int)*count;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int r = list[q];
+        int i, j, k;
+        decode(g, r, i, j, k);
+        double dg, off[6], unused[2];
+        const int kind = trans_row<L, false>(g, op.tc, op.label, op.fx, op.fy, op.fz, r, i, j, k, dg, off,
+                                             nullptr, nullptr, unused);
+        const double inv = drcp_nr(dg);
+        const float inv32 = d2f_rz(inv);
+        tb.c[0][r] = dg;
+        tb.inv[r] = inv;
+#pragma unroll
+        for (int d = 0; d < 6; ++d) {
+            tb.c[1 + d][r] = off[d];
+            tb.o[d][r] = d2f_rz(off[d]) * inv32;
+        }
+        tb.kind[r] = (int8_t)kind;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_t_rhs(Grid g, double inv_dt, TBuf tb, int nrhs, const double* f0,
+                                                  const double* f1, double* __restrict__ partials) {
+    double acc[2] = {0.0, 0.0};
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < (int)g.N; r += gridDim.x * blockDim.x) {
+        const int kind = tb.kind[r];
+        const double inv = tb.inv[r];
+        for (int q = 0; q < nrhs; ++q) {
+            const double fv = (q ? f1 : f0)[r];
+            // trans_row's right-hand side at theta = 1: 0.0 + c_old on Precipitate rows,
+            // 0.0 + c_old * (1/dt) on every other row
+            const double rhs = (kind == 1) ? 0.0 + fv : 0.0 + fv * inv_dt;
+            tb.b[q][r] = rhs;
+            double bt = rhs * inv;
             acc[q] += bt * bt;
         }
     }
@@ -917,10 +1006,35 @@ static ls_status mixed_solve(ls_ctx* c, const Rows<L>& rows, int nrhs, const dou
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
     TBuf tb = make_tbuf(c);
-    if (rows.mode == 0 && rows.tc.theta != 1.0)
-        LS_LAUNCH(c, (k_t_setup<L, true>), grid, kBlock, 0, rows, tb, nrhs, f0, f1, c->partials);
-    else
-        LS_LAUNCH(c, (k_t_setup<L, false>), grid, kBlock, 0, rows, tb, nrhs, f0, f1, c->partials);
+    if (rows.mode == 0 && rows.tc.theta == 1.0) {
+        // fully implicit transport rows: recompute only the rows whose inputs changed
+        const TransConst& tc = rows.tc;
+        const double consts[8] = {tc.inv_dt, tc.alpha, tc.D, tc.Dpore, tc.dx, tc.dc_pore, tc.dc_other,
+                                  (double)tc.dd.pow2};
+        if (!c->sht_fx) {
+            const size_t n = (size_t)g.N;
+            LS_TRY(dalloc(c, &c->sht_label, n * c->label_bytes));
+            LS_TRY(dalloc_t(c, &c->sht_fx, n));
+            LS_TRY(dalloc_t(c, &c->sht_fy, n));
+            LS_TRY(dalloc_t(c, &c->sht_fz, n));
+            c->t_valid = 0;
+        }
+        const int force = (!c->t_valid || memcmp(consts, c->t_consts, sizeof(consts)) != 0) ? 1 : 0;
+        LS_TRY(wlist_reset(c));
+        LS_LAUNCH(c, k_t_dirty<L>, grid, kBlock, 0, g, rows.label, rows.fx, rows.fy, rows.fz,
+                  (L*)c->sht_label, c->sht_fx, c->sht_fy, c->sht_fz, c->dirty, force);
+        LS_LAUNCH(c, k_t_scan, grid, kBlock, 0, g, (const uint8_t*)c->dirty, c->wlist, c->wcount);
+        LS_LAUNCH(c, k_t_rows<L>, grid, kBlock, 0, rows, tb, (const int*)c->wlist, (const unsigned int*)c->wcount);
+        LS_LAUNCH(c, k_t_rhs, grid, kBlock, 0, g, rows.tc.inv_dt, tb, nrhs, f0, f1, c->partials);
+        memcpy(c->t_consts, consts, sizeof(consts));
+        c->t_valid = 1;
+    } else {
+        if (rows.mode == 0)
+            LS_LAUNCH(c, (k_t_setup<L, true>), grid, kBlock, 0, rows, tb, nrhs, f0, f1, c->partials);
+        else
+            LS_LAUNCH(c, (k_t_setup<L, false>), grid, kBlock, 0, rows, tb, nrhs, f0, f1, c->partials);
+        c->t_valid = 0;  // the row buffers now hold other rows
+    }
     LS_TRY(finalize_sum(c, grid, 2, S_RED0 + 4));
     LS_LAUNCH(c, k_t_xid, grid, kBlock, 0, g, tb, x0, x1, nrhs);
     double den[2];
@@ -1067,6 +1181,7 @@ __global__ void k_trans_apply_full(Rows<L> op, const double* __restrict__ x, dou
 template <typename L>
 static ls_status transport_apply_t(ls_ctx* c, double dt, const double* xh, double* yh) {
     LS_TRY(t_alloc(c));
+    c->t_valid = 0;  // tc[0] and tc[1] serve as scratch below
     Rows<L> rows = trans_rows<L>(c, dt);
     const size_t bytes = sizeof(double) * (size_t)c->g.N;
     LS_CUDA(c, cudaMemcpyAsync(c->tc[0], xh, bytes, cudaMemcpyHostToDevice, c->stream));
