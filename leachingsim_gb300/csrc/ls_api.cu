@@ -83,7 +83,10 @@ ls_status wlist_reset(ls_ctx* c) {
     const size_t n = (size_t)c->g.N;
     if (!c->wlist) LS_TRY(dalloc_t(c, &c->wlist, n));
     if (!c->wcount) LS_TRY(dalloc_t(c, &c->wcount, 4));
-    if (!c->dirty) LS_TRY(dalloc_t(c, &c->dirty, n));
+    if (!c->dbits) {
+        c->dwords = (long long)((n + 31) / 32);
+        LS_TRY(dalloc_t(c, &c->dbits, 2 * (size_t)c->dwords));
+    }
     LS_CUDA(c, cudaMemsetAsync(c->wcount, 0, sizeof(unsigned int), c->stream));
     return LS_OK;
 }
@@ -334,7 +337,7 @@ ls_status ls_destroy(ls_ctx* c) {
                     c->inner[4], c->mg0_x, c->mg0_t, c->comp, c->cc_flag, c->tkind, c->tinv, c->dz_list,
                     c->dz_count, c->dz_level_start, c->partials, c->scal, c->d_int,
                     c->sh_label, c->sh_sat, c->sh_precip, c->sh_frac, c->shf_label, c->shf_perm,
-                    c->shf_visc, c->dirty, c->sht_label, c->sht_fx, c->sht_fy, c->sht_fz,
+                    c->shf_visc, c->psb2, c->sat_q, c->dbits, c->sht_label, c->sht_fx, c->sht_fy, c->sht_fz,
                     c->shq_P, c->shq_C, c->shq_K, c->shq_V, c->shq_fx, c->shq_fy, c->shq_fz,
                     c->wlist, c->wcount};
     for (void* q : ptrs)

@@ -136,18 +136,43 @@ __device__ __forceinline__ double drcp_nr(double d) {
     return __fma_rn(y, __fma_rn(-d, y, 1.0), y);
 }
 
-// Append `value` to list[] for every lane with pred set: one atomic per warp (warp-aggregated);
-// the order of the entries is unspecified, so list consumers must not depend on it.
-__device__ __forceinline__ void warp_append(bool pred, int value, int* list, unsigned int* count) {
-    const unsigned int mask = __activemask();
-    const unsigned int ballot = __ballot_sync(mask, pred);
-    if (ballot == 0u) return;
-    const int lane = (int)(threadIdx.x & 31u);
-    const int leader = __ffs(ballot) - 1;
-    unsigned int base = 0u;
-    if (lane == leader) base = atomicAdd(count, (unsigned int)__popc(ballot));
-    base = __shfl_sync(mask, base, leader);
-    if (pred) list[base + (unsigned int)__popc(ballot & ((1u << lane) - 1u))] = value;
+// Dirty bits of the change-tracked kernels: one bit per voxel, word w holds voxels 32w ..
+// 32w+31. The change tests run warp-aligned (a warp covers voxels r0 .. r0+31, r0 a multiple
+// of 32) and store one ballot word per warp; the scans read windows of 32 neighbours' bits.
+__device__ __forceinline__ unsigned int dwin(const unsigned int* __restrict__ bits, long long nwords,
+                                             long long s) {
+    // bits of voxels s .. s+31, 0 outside [0, N)
+    const long long w = s >> 5;
+    const int sh = (int)(s & 31);
+    const unsigned int lo = (w >= 0 && w < nwords) ? __ldg(bits + w) : 0u;
+    const unsigned int hi = (w + 1 >= 0 && w + 1 < nwords) ? __ldg(bits + w + 1) : 0u;
+    return __funnelshift_r(lo, hi, sh);
+}
+__device__ __forceinline__ bool dbit(unsigned int window, int lane) { return (window >> lane) & 1u; }
+
+// Append `value` to list[] for every thread of the block with pred set: one atomic per block
+// (a single global counter takes ~one atomic per clock, so per-warp atomics over ~10^6 warps
+// would serialise); every thread of the block must call it, the same number of times. The
+// order of the entries is unspecified, so list consumers must not depend on it.
+__device__ __forceinline__ void block_append(bool pred, int value, int* list, unsigned int* count) {
+    __shared__ unsigned int warp_off[kBlock / 32];
+    __shared__ unsigned int base;
+    const int lane = (int)(threadIdx.x & 31u), warp = (int)(threadIdx.x >> 5);
+    const unsigned int ballot = __ballot_sync(0xffffffffu, pred);
+    if (lane == 0) warp_off[warp] = (unsigned int)__popc(ballot);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int tot = 0u;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            const unsigned int c = warp_off[w];
+            warp_off[w] = tot;
+            tot += c;
+        }
+        base = tot ? atomicAdd(count, tot) : 0u;
+    }
+    __syncthreads();
+    if (pred) list[base + warp_off[warp] + (unsigned int)__popc(ballot & ((1u << lane) - 1u))] = value;
+    __syncthreads();
 }
 
 // Timed region record.
@@ -213,7 +238,11 @@ struct ls_ctx {
     void* shf_label;      // pressure-face inputs at the last evaluation
     double* shf_perm;
     double* shf_visc;
-    uint8_t* dirty;       // per-voxel scratch flag of the two-pass change tests
+    double* psb2;         // (b/diag)^2 of each pressure row, for the norm of the residual test
+    double rows_evap_dx;  // evaporation constant the stored pressure rows were built with
+    double* sat_q;        // div q + evaporative sink of each active voxel (saturation update)
+    unsigned int* dbits;  // dirty bits of the change tests: two planes of dwords words
+    long long dwords;     // ceil(N / 32)
     int* wlist;           // voxel work list of the change-tracked kernels (N entries)
     unsigned int* wcount; // its length
     int props_force, faces_force;  // recompute every voxel on the next call

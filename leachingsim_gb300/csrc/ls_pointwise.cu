@@ -87,20 +87,25 @@ __global__ void __launch_bounds__(kBlock) k_props_scan(Grid g, const L* __restri
                                                        double* __restrict__ ss, double* __restrict__ sp,
                                                        float* __restrict__ sf, int force,
                                                        int* __restrict__ list, unsigned int* __restrict__ count) {
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < (int)g.N; r += gridDim.x * blockDim.x) {
-        const L lab = label[r];
-        const long long sb = __double_as_longlong(sat[r]);
-        const long long pb = __double_as_longlong(precip[r]);
-        const unsigned int fb = __float_as_uint(frac[r]);
-        const bool d = force || lab != sl[r] || sb != __double_as_longlong(ss[r]) ||
-                       pb != __double_as_longlong(sp[r]) || fb != __float_as_uint(sf[r]);
-        if (d) {
-            sl[r] = lab;
-            ss[r] = __longlong_as_double(sb);
-            sp[r] = __longlong_as_double(pb);
-            sf[r] = __uint_as_float(fb);
+    // block-uniform trip count (block_append is called by every thread of the block)
+    for (int b0 = blockIdx.x * blockDim.x; b0 < (int)g.N; b0 += gridDim.x * blockDim.x) {
+        const int r = b0 + (int)threadIdx.x;
+        bool d = false;
+        if (r < (int)g.N) {
+            const L lab = label[r];
+            const long long sb = __double_as_longlong(sat[r]);
+            const long long pb = __double_as_longlong(precip[r]);
+            const unsigned int fb = __float_as_uint(frac[r]);
+            d = force || lab != sl[r] || sb != __double_as_longlong(ss[r]) || pb != __double_as_longlong(sp[r]) ||
+                fb != __float_as_uint(sf[r]);
+            if (d) {
+                sl[r] = lab;
+                ss[r] = __longlong_as_double(sb);
+                sp[r] = __longlong_as_double(pb);
+                sf[r] = __uint_as_float(fb);
+            }
         }
-        warp_append(d, r, list, count);
+        block_append(d, r, list, count);
     }
 }
 
@@ -178,31 +183,40 @@ __device__ __forceinline__ double grad1(const double* __restrict__ f, long long 
     return dd.pow2 ? d * (0.5 * dd.inv_dx) : d / (2.0 * dd.dx);
 }
 
-// Change test of the flux inputs (pass 1): bit 0 = P or Pc of the voxel changed (they
-// enter the gradients of its neighbours too), bit 1 = its permeability or viscosity changed,
-// bitwise against the values at the last flux evaluation.
+// Change test of the flux inputs (pass 1), against the values at the last flux evaluation:
+// plane 0 bit = P or Pc of the voxel changed (they enter its neighbours' gradients too),
+// plane 1 bit = its permeability or viscosity changed.
 __global__ void __launch_bounds__(kBlock) k_flux_dirty(Grid g, const double* __restrict__ P,
                                                        const double* __restrict__ C,
                                                        const double* __restrict__ perm,
                                                        const double* __restrict__ visc,
                                                        double* __restrict__ sP, double* __restrict__ sC,
                                                        double* __restrict__ sK, double* __restrict__ sV,
-                                                       uint8_t* __restrict__ dirty, int force) {
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x) {
-        const long long pb = __double_as_longlong(P[r]), cb = __double_as_longlong(C[r]);
-        const long long kb = __double_as_longlong(perm[r]), vb = __double_as_longlong(visc[r]);
-        const bool d0 = force || pb != __double_as_longlong(sP[r]) || cb != __double_as_longlong(sC[r]);
-        const bool d1 = force || kb != __double_as_longlong(sK[r]) || vb != __double_as_longlong(sV[r]);
-        if (d0) {
-            sP[r] = __longlong_as_double(pb);
-            sC[r] = __longlong_as_double(cb);
+                                                       unsigned int* __restrict__ bits, long long nw, int force) {
+    for (long long r0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); r0 < g.N;
+         r0 += (long long)gridDim.x * blockDim.x) {
+        const long long r = r0 + (threadIdx.x & 31u);
+        bool d0 = false, d1 = false;
+        if (r < g.N) {
+            const long long pb = __double_as_longlong(P[r]), cb = __double_as_longlong(C[r]);
+            const long long kb = __double_as_longlong(perm[r]), vb = __double_as_longlong(visc[r]);
+            d0 = force || pb != __double_as_longlong(sP[r]) || cb != __double_as_longlong(sC[r]);
+            d1 = force || kb != __double_as_longlong(sK[r]) || vb != __double_as_longlong(sV[r]);
+            if (d0) {
+                sP[r] = __longlong_as_double(pb);
+                sC[r] = __longlong_as_double(cb);
+            }
+            if (d1) {
+                sK[r] = __longlong_as_double(kb);
+                sV[r] = __longlong_as_double(vb);
+            }
         }
-        if (d1) {
-            sK[r] = __longlong_as_double(kb);
-            sV[r] = __longlong_as_double(vb);
+        const unsigned int w0 = __ballot_sync(0xffffffffu, d0);
+        const unsigned int w1 = __ballot_sync(0xffffffffu, d1);
+        if ((threadIdx.x & 31u) == 0u) {
+            bits[r0 >> 5] = w0;
+            bits[nw + (r0 >> 5)] = w1;
         }
-        dirty[r] = (d0 ? 1 : 0) | (d1 ? 2 : 0);
     }
 }
 
@@ -210,24 +224,35 @@ __global__ void __launch_bounds__(kBlock) k_flux_dirty(Grid g, const double* __r
 // neighbours and of its own permeability and viscosity. Voxels where one of those changed go
 // to the work list; the others get their last computed flux back (the transport solve zeroes
 // the flux of Rock and Precipitate voxels after use).
-__global__ void __launch_bounds__(kBlock) k_flux_scan(Grid g, const uint8_t* __restrict__ dirty,
+__global__ void __launch_bounds__(kBlock) k_flux_scan(Grid g, const unsigned int* __restrict__ bits, long long nw,
                                                       double* __restrict__ fx, double* __restrict__ fy,
                                                       double* __restrict__ fz, const double* __restrict__ sfx,
                                                       const double* __restrict__ sfy,
                                                       const double* __restrict__ sfz, int* __restrict__ list,
                                                       unsigned int* __restrict__ count) {
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < (int)g.N; r += gridDim.x * blockDim.x) {
-        int i, j, k;
-        decode(g, r, i, j, k);
-        const bool d = dirty[r] || (i > 0 && (dirty[r - g.JK] & 1)) || (i + 1 < g.I && (dirty[r + g.JK] & 1)) ||
-                       (j > 0 && (dirty[r - g.K] & 1)) || (j + 1 < g.J && (dirty[r + g.K] & 1)) ||
-                       (k > 0 && (dirty[r - 1] & 1)) || (k + 1 < g.K && (dirty[r + 1] & 1));
-        if (!d) {
-            fx[r] = sfx[r];
-            fy[r] = sfy[r];
-            fz[r] = sfz[r];
+    const int lane = (int)(threadIdx.x & 31u);
+    // block-uniform trip count (block_append is called by every thread of the block)
+    for (long long b0 = (long long)blockIdx.x * blockDim.x; b0 < g.N; b0 += (long long)gridDim.x * blockDim.x) {
+        const long long r0 = b0 + (threadIdx.x & ~31u);
+        const long long r = r0 + lane;
+        const unsigned int own = dwin(bits, nw, r0) | dwin(bits + nw, nw, r0);
+        const unsigned int km = dwin(bits, nw, r0 - 1), kp = dwin(bits, nw, r0 + 1);
+        const unsigned int jm = dwin(bits, nw, r0 - g.K), jp = dwin(bits, nw, r0 + g.K);
+        const unsigned int im = dwin(bits, nw, r0 - g.JK), ip = dwin(bits, nw, r0 + g.JK);
+        bool d = false;
+        if (r < g.N) {
+            int i, j, k;
+            decode(g, r, i, j, k);
+            d = dbit(own, lane) || (i > 0 && dbit(im, lane)) || (i + 1 < g.I && dbit(ip, lane)) ||
+                (j > 0 && dbit(jm, lane)) || (j + 1 < g.J && dbit(jp, lane)) || (k > 0 && dbit(km, lane)) ||
+                (k + 1 < g.K && dbit(kp, lane));
+            if (!d) {
+                fx[r] = sfx[r];
+                fy[r] = sfy[r];
+                fz[r] = sfz[r];
+            }
         }
-        warp_append(d, r, list, count);
+        block_append(d, (int)r, list, count);
     }
 }
 
@@ -275,8 +300,8 @@ ls_status flux_run(ls_ctx* c) {
                        c->flux_consts[1] != c->p.max_cap_grad) ? 1 : 0;
     LS_TRY(wlist_reset(c));
     LS_LAUNCH(c, k_flux_dirty, grid, kBlock, 0, c->g, c->P, c->pc, c->perm, c->visc, c->shq_P, c->shq_C,
-              c->shq_K, c->shq_V, c->dirty, force);
-    LS_LAUNCH(c, k_flux_scan, grid, kBlock, 0, c->g, (const uint8_t*)c->dirty, c->fx, c->fy, c->fz,
+              c->shq_K, c->shq_V, c->dbits, c->dwords, force);
+    LS_LAUNCH(c, k_flux_scan, grid, kBlock, 0, c->g, (const unsigned int*)c->dbits, c->dwords, c->fx, c->fy, c->fz,
               (const double*)c->shq_fx, (const double*)c->shq_fy, (const double*)c->shq_fz, c->wlist, c->wcount);
     LS_LAUNCH(c, k_flux, grid, kBlock, 0, c->g, make_dxdiv(c->p.dx), c->p.max_cap_grad, c->P, c->pc,
               c->perm, c->visc, c->fx, c->fy, c->fz, c->shq_fx, c->shq_fy, c->shq_fz, (const int*)c->wlist,
@@ -329,28 +354,6 @@ __device__ __forceinline__ void sat_rates(const Grid& g, const L* __restrict__ l
 }
 
 template <typename L>
-__global__ void __launch_bounds__(kBlock) k_sat_rate(Grid g, DxDiv dd, double evap,
-                                                     const L* __restrict__ label,
-                                                     const double* __restrict__ fx,
-                                                     const double* __restrict__ fy,
-                                                     const double* __restrict__ fz,
-                                                     double* __restrict__ partials) {
-    double v[1] = {0.0};
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x) {
-        int t = (int)label[r];
-        if (sat_inactive(t)) continue;
-        int i, j, k;
-        decode(g, r, i, j, k);
-        double div_q, evap_sink;
-        sat_rates(g, label, fx, fy, fz, r, i, j, k, t, dd, evap, div_q, evap_sink);
-        double total_rate = fabs(div_q) + evap_sink;
-        if (total_rate > v[0]) v[0] = total_rate;
-    }
-    block_max_store<1>(v, partials);
-}
-
-template <typename L>
 __global__ void __launch_bounds__(kBlock) k_sat_update(Grid g, DxDiv dd, double evap,
                                                        double dt_sub_over_phi, int num_steps,
                                                        const L* __restrict__ label,
@@ -385,16 +388,72 @@ __global__ void __launch_bounds__(kBlock) k_sat_update(Grid g, DxDiv dd, double 
     }
 }
 
+// The context path of the update: the rate pass stores div q + evaporative sink of every
+// active voxel (the update applies that same sum in every sub-step), so the update pass does
+// no flux arithmetic.
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_sat_rate_st(Grid g, DxDiv dd, double evap,
+                                                        const L* __restrict__ label,
+                                                        const double* __restrict__ fx,
+                                                        const double* __restrict__ fy,
+                                                        const double* __restrict__ fz,
+                                                        double* __restrict__ qsum,
+                                                        double* __restrict__ partials) {
+    double v[1] = {0.0};
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        int t = (int)label[r];
+        if (sat_inactive(t)) continue;
+        int i, j, k;
+        decode(g, r, i, j, k);
+        double div_q, evap_sink;
+        sat_rates(g, label, fx, fy, fz, r, i, j, k, t, dd, evap, div_q, evap_sink);
+        qsum[r] = div_q + evap_sink;
+        double total_rate = fabs(div_q) + evap_sink;
+        if (total_rate > v[0]) v[0] = total_rate;
+    }
+    block_max_store<1>(v, partials);
+}
+
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_sat_update_st(Grid g, double dt_sub_over_phi, int num_steps,
+                                                          const L* __restrict__ label,
+                                                          const double* __restrict__ qsum,
+                                                          double* __restrict__ sat) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.NP;
+         r += (long long)gridDim.x * blockDim.x) {
+        if (r >= g.N) {  // extra top plane of the freshly allocated array
+            sat[r] = 0.0;
+            continue;
+        }
+        if (sat_inactive((int)label[r])) {
+            sat[r] = 0.0;  // never written by the reference's update (indeterminate there)
+            continue;
+        }
+        const double q = qsum[r];
+        double sv = sat[r];
+        for (int step = 0; step < num_steps; ++step) {
+            double new_sat = sv - dt_sub_over_phi * q;
+            double nv = smax(0.0, smin(1.0, new_sat));
+            bool fixed = (nv == sv) || (nv != nv && sv != sv);
+            sv = nv;
+            if (fixed) break;
+        }
+        sat[r] = sv;
+    }
+}
+
 ls_status saturation_run(ls_ctx* c, double dt, ls_substep_info* info) {
     const DxDiv dx = make_dxdiv(c->p.dx);
     const double evap = c->p.evaporative_flux;
     int grid = grid_for(c, c->g.N);
+    if (!c->sat_q) LS_TRY(dalloc_t(c, &c->sat_q, (size_t)c->g.N));
     if (c->label_bytes == 1)
-        LS_LAUNCH(c, k_sat_rate<uint8_t>, grid, kBlock, 0, c->g, dx, evap, (const uint8_t*)c->label,
-                  c->fx, c->fy, c->fz, c->partials);
+        LS_LAUNCH(c, k_sat_rate_st<uint8_t>, grid, kBlock, 0, c->g, dx, evap, (const uint8_t*)c->label,
+                  c->fx, c->fy, c->fz, c->sat_q, c->partials);
     else
-        LS_LAUNCH(c, k_sat_rate<uint16_t>, grid, kBlock, 0, c->g, dx, evap, (const uint16_t*)c->label,
-                  c->fx, c->fy, c->fz, c->partials);
+        LS_LAUNCH(c, k_sat_rate_st<uint16_t>, grid, kBlock, 0, c->g, dx, evap, (const uint16_t*)c->label,
+                  c->fx, c->fy, c->fz, c->sat_q, c->partials);
     LS_TRY(finalize_max(c, grid, 1, S_RED0));
     double max_div_q = 0.0;
     LS_TRY(read_scalars(c, S_RED0, 1, &max_div_q));
@@ -416,11 +475,11 @@ ls_status saturation_run(ls_ctx* c, double dt, ls_substep_info* info) {
     }
     int grid2 = grid_for(c, c->g.NP);
     if (c->label_bytes == 1)
-        LS_LAUNCH(c, k_sat_update<uint8_t>, grid2, kBlock, 0, c->g, dx, evap, dt_sub_over_phi,
-                  num_steps, (const uint8_t*)c->label, c->fx, c->fy, c->fz, c->sat);
+        LS_LAUNCH(c, k_sat_update_st<uint8_t>, grid2, kBlock, 0, c->g, dt_sub_over_phi, num_steps,
+                  (const uint8_t*)c->label, (const double*)c->sat_q, c->sat);
     else
-        LS_LAUNCH(c, k_sat_update<uint16_t>, grid2, kBlock, 0, c->g, dx, evap, dt_sub_over_phi,
-                  num_steps, (const uint16_t*)c->label, c->fx, c->fy, c->fz, c->sat);
+        LS_LAUNCH(c, k_sat_update_st<uint16_t>, grid2, kBlock, 0, c->g, dt_sub_over_phi, num_steps,
+                  (const uint16_t*)c->label, (const double*)c->sat_q, c->sat);
     return LS_OK;
 }
 

@@ -70,40 +70,55 @@ __device__ __forceinline__ double link_coeff(const L* __restrict__ label,
     return K_avg / visc[self];
 }
 
-// Change test of the face inputs (pass 1 of the faces): dirty[r] = label, permeability or
-// viscosity of voxel r differ bitwise from their values at the last face evaluation.
+// Change test of the face inputs (pass 1 of the faces): the dirty bit of voxel r is set when
+// its label, permeability or viscosity differ bitwise from the values at the last face
+// evaluation.
 template <typename L>
 __global__ void __launch_bounds__(kBlock) k_faces_dirty(Grid g, const L* __restrict__ label,
                                                         const double* __restrict__ perm,
                                                         const double* __restrict__ visc,
                                                         L* __restrict__ sl, double* __restrict__ sp,
                                                         double* __restrict__ sv,
-                                                        uint8_t* __restrict__ dirty, int force) {
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x) {
-        const L lab = label[r];
-        const long long pb = __double_as_longlong(perm[r]);
-        const long long vb = __double_as_longlong(visc[r]);
-        const bool d = force || lab != sl[r] || pb != __double_as_longlong(sp[r]) ||
-                       vb != __double_as_longlong(sv[r]);
-        if (d) {
-            sl[r] = lab;
-            sp[r] = __longlong_as_double(pb);
-            sv[r] = __longlong_as_double(vb);
+                                                        unsigned int* __restrict__ bits, int force) {
+    for (long long r0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); r0 < g.N;
+         r0 += (long long)gridDim.x * blockDim.x) {
+        const long long r = r0 + (threadIdx.x & 31u);
+        bool d = false;
+        if (r < g.N) {
+            const L lab = label[r];
+            const long long pb = __double_as_longlong(perm[r]);
+            const long long vb = __double_as_longlong(visc[r]);
+            d = force || lab != sl[r] || pb != __double_as_longlong(sp[r]) || vb != __double_as_longlong(sv[r]);
+            if (d) {
+                sl[r] = lab;
+                sp[r] = __longlong_as_double(pb);
+                sv[r] = __longlong_as_double(vb);
+            }
         }
-        dirty[r] = d ? 1 : 0;
+        const unsigned int w = __ballot_sync(0xffffffffu, d);
+        if ((threadIdx.x & 31u) == 0u) bits[r0 >> 5] = w;
     }
 }
 
 // Pass 2: voxels holding a face (their +i, +j, +k faces) with a dirty voxel on either side.
-__global__ void __launch_bounds__(kBlock) k_faces_scan(Grid g, const uint8_t* __restrict__ dirty,
-                                                       int* __restrict__ list, unsigned int* __restrict__ count) {
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < (int)g.N; r += gridDim.x * blockDim.x) {
-        int i, j, k;
-        decode(g, r, i, j, k);
-        const bool need = dirty[r] || (i + 1 < g.I && dirty[r + g.JK]) || (j + 1 < g.J && dirty[r + g.K]) ||
-                          (k + 1 < g.K && dirty[r + 1]);
-        warp_append(need, r, list, count);
+__global__ void __launch_bounds__(kBlock) k_faces_scan(Grid g, const unsigned int* __restrict__ bits,
+                                                       long long nw, int* __restrict__ list,
+                                                       unsigned int* __restrict__ count) {
+    const int lane = (int)(threadIdx.x & 31u);
+    // block-uniform trip count (block_append is called by every thread of the block)
+    for (long long b0 = (long long)blockIdx.x * blockDim.x; b0 < g.N; b0 += (long long)gridDim.x * blockDim.x) {
+        const long long r0 = b0 + (threadIdx.x & ~31u);
+        const long long r = r0 + lane;
+        const unsigned int own = dwin(bits, nw, r0), kp = dwin(bits, nw, r0 + 1),
+                           jp = dwin(bits, nw, r0 + g.K), ip = dwin(bits, nw, r0 + g.JK);
+        bool need = false;
+        if (r < g.N) {
+            int i, j, k;
+            decode(g, r, i, j, k);
+            need = dbit(own, lane) || (i + 1 < g.I && dbit(ip, lane)) || (j + 1 < g.J && dbit(jp, lane)) ||
+                   (k + 1 < g.K && dbit(kp, lane));
+        }
+        block_append(need, (int)r, list, count);
     }
 }
 
@@ -144,75 +159,119 @@ __global__ void __launch_bounds__(kBlock) k_press_faces(Grid g, const L* __restr
     }
 }
 
-// Rows (kernel 2 of 2): kind, diagonal and right-hand side of src/Simulation.cpp:674-792.
-// The diagonal subtracts the six link coefficients in the reference's order
-// (+i, -i, +j, -j, +k, -k), read from the stored faces.
+// One row of src/Simulation.cpp:674-792: kind, diagonal and right-hand side. The diagonal
+// subtracts the six link coefficients in the reference's order (+i, -i, +j, -j, +k, -k),
+// read from the stored faces.
 template <typename L>
-__global__ void __launch_bounds__(kBlock) k_press_setup(Grid g, PressConst pcst,
-                                                        const L* __restrict__ label,
-                                                        int8_t* __restrict__ kind,
-                                                        double* __restrict__ diag,
-                                                        double* __restrict__ b,
+__device__ __forceinline__ void press_row_eval(const Grid& g, const PressConst& pcst, const L* __restrict__ label,
+                                               const double* __restrict__ f0, const double* __restrict__ f1,
+                                               const double* __restrict__ f2, long long r, int i, int j, int k,
+                                               int8_t& kd, double& dg, double& bv) {
+    const int t = (int)label[r];
+    kd = 0;
+    dg = 0.0;
+    bv = 0.0;
+    if (t == kAir || t == kRock || t == kSulphide || t == kPrecipitate) {
+        kd = 1;
+        dg = 1.0;
+        if (t == kAir) {
+            bool is_surface = (i + 1 < g.I && (int)label[r + g.JK] != kAir) ||
+                              (i > 0 && (int)label[r - g.JK] != kAir) ||
+                              (j + 1 < g.J && (int)label[r + g.K] != kAir) ||
+                              (j > 0 && (int)label[r - g.K] != kAir) ||
+                              (k + 1 < g.K && (int)label[r + 1] != kAir) ||
+                              (k > 0 && (int)label[r - 1] != kAir);
+            bv = 0.0 + (is_surface ? pcst.eff_top : 0.0);
+        }
+    } else if (t == kPore) {
+        double diagonal_term = 0.0, source_term = 0.0;
+        const long long nbs[6] = {r + g.JK, r - g.JK, r + g.K, r - g.K, r + 1, r - 1};
+        const bool val[6] = {i + 1 < g.I, i > 0, j + 1 < g.J, j > 0, k + 1 < g.K, k > 0};
+        const double cf[6] = {val[0] ? f0[r] : 0.0, val[1] ? f0[r - g.JK] : 0.0,
+                              val[2] ? f1[r] : 0.0, val[3] ? f1[r - g.K] : 0.0,
+                              val[4] ? f2[r] : 0.0, val[5] ? f2[r - 1] : 0.0};
+#pragma unroll
+        for (int d = 0; d < 6; ++d) {
+            if (!val[d]) continue;
+            if ((int)label[nbs[d]] == kAir) source_term -= pcst.evap_dx;
+            diagonal_term -= cf[d];
+        }
+        kd = 2;
+        if (fabs(diagonal_term) < 1e-16) {
+            diagonal_term = 1e-16;
+            kd = 3;
+        }
+        dg = diagonal_term;
+        bv = 0.0 + source_term;
+    }
+}
+
+// Rows pass 1: a row is a pure function of the labels of its voxel and six neighbours, of
+// its six faces and of the evaporation constant, plus the ramped boundary pressure on Air
+// rows; rows with a dirty voxel in that stencil (face change bits) and all Air rows are listed.
+__global__ void __launch_bounds__(kBlock) k_rows_scan(Grid g, const unsigned int* __restrict__ bits, long long nw,
+                                                      const uint8_t* __restrict__ label8,
+                                                      const uint16_t* __restrict__ label16, int force,
+                                                      int* __restrict__ list, unsigned int* __restrict__ count) {
+    const int lane = (int)(threadIdx.x & 31u);
+    // block-uniform trip count (block_append is called by every thread of the block)
+    for (long long b0 = (long long)blockIdx.x * blockDim.x; b0 < g.N; b0 += (long long)gridDim.x * blockDim.x) {
+        const long long r0 = b0 + (threadIdx.x & ~31u);
+        const long long r = r0 + lane;
+        const unsigned int own = dwin(bits, nw, r0);
+        const unsigned int km = dwin(bits, nw, r0 - 1), kp = dwin(bits, nw, r0 + 1);
+        const unsigned int jm = dwin(bits, nw, r0 - g.K), jp = dwin(bits, nw, r0 + g.K);
+        const unsigned int im = dwin(bits, nw, r0 - g.JK), ip = dwin(bits, nw, r0 + g.JK);
+        bool d = false;
+        if (r < g.N) {
+            int i, j, k;
+            decode(g, r, i, j, k);
+            const int t = label8 ? (int)label8[r] : (int)label16[r];
+            d = force || t == kAir || dbit(own, lane) || (i > 0 && dbit(im, lane)) ||
+                (i + 1 < g.I && dbit(ip, lane)) || (j > 0 && dbit(jm, lane)) || (j + 1 < g.J && dbit(jp, lane)) ||
+                (k > 0 && dbit(km, lane)) || (k + 1 < g.K && dbit(kp, lane));
+        }
+        block_append(d, (int)r, list, count);
+    }
+}
+
+// Rows pass 2: the listed rows, their (b/diag)^2 for the norm of the relative residual test
+// and 1/|diag| of normal Pore rows (the weights of the scaled residual norm).
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_press_setup(Grid g, PressConst pcst, const L* __restrict__ label,
+                                                        int8_t* __restrict__ kind, double* __restrict__ diag,
+                                                        double* __restrict__ b, double* __restrict__ sb2,
+                                                        double* __restrict__ isd,
                                                         const double* __restrict__ f0,
                                                         const double* __restrict__ f1,
                                                         const double* __restrict__ f2,
-                                                        double* __restrict__ partials) {
-    double acc[1] = {0.0};  // sum (b/diag)^2
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x) {
+                                                        const int* __restrict__ list,
+                                                        const unsigned int* __restrict__ count) {
+    const int n = (int)*count;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int r = list[q];
         int i, j, k;
         decode(g, r, i, j, k);
-        const int t = (int)label[r];
-        int8_t kd = 0;
-        double dg = 0.0, bv = 0.0;
-        if (t == kAir || t == kRock || t == kSulphide || t == kPrecipitate) {
-            kd = 1;
-            dg = 1.0;
-            if (t == kAir) {
-                bool is_surface = (i + 1 < g.I && (int)label[r + g.JK] != kAir) ||
-                                  (i > 0 && (int)label[r - g.JK] != kAir) ||
-                                  (j + 1 < g.J && (int)label[r + g.K] != kAir) ||
-                                  (j > 0 && (int)label[r - g.K] != kAir) ||
-                                  (k + 1 < g.K && (int)label[r + 1] != kAir) ||
-                                  (k > 0 && (int)label[r - 1] != kAir);
-                bv = 0.0 + (is_surface ? pcst.eff_top : 0.0);
-            }
-        } else if (t == kPore) {
-            double diagonal_term = 0.0, source_term = 0.0;
-            const long long nbs[6] = {r + g.JK, r - g.JK, r + g.K, r - g.K, r + 1, r - 1};
-            const bool val[6] = {i + 1 < g.I, i > 0, j + 1 < g.J, j > 0, k + 1 < g.K, k > 0};
-            const double cf[6] = {val[0] ? f0[r] : 0.0, val[1] ? f0[r - g.JK] : 0.0,
-                                  val[2] ? f1[r] : 0.0, val[3] ? f1[r - g.K] : 0.0,
-                                  val[4] ? f2[r] : 0.0, val[5] ? f2[r - 1] : 0.0};
-#pragma unroll
-            for (int d = 0; d < 6; ++d) {
-                if (!val[d]) continue;
-                if ((int)label[nbs[d]] == kAir) source_term -= pcst.evap_dx;
-                diagonal_term -= cf[d];
-            }
-            kd = 2;
-            if (fabs(diagonal_term) < 1e-16) {
-                diagonal_term = 1e-16;
-                kd = 3;
-            }
-            dg = diagonal_term;
-            bv = 0.0 + source_term;
-        }
+        int8_t kd;
+        double dg, bv;
+        press_row_eval(g, pcst, label, f0, f1, f2, r, i, j, k, kd, dg, bv);
         kind[r] = kd;
         diag[r] = dg;
         b[r] = bv;
         double sb = (dg != 0.0) ? bv / dg : bv;
-        acc[0] += sb * sb;
+        sb2[r] = sb * sb;
+        isd[r] = (kd == 2) ? drcp_nr(-dg) : 0.0;
     }
-    block_sum_store<1>(acc, partials);
 }
 
-// 1/|d| of the normal Pore rows (weights of the scaled residual norm).
-__global__ void k_press_isd(Grid g, const int8_t* __restrict__ kind, const double* __restrict__ diag,
-                            double* __restrict__ isd) {
+// Rows pass 3: partial sums of (b/diag)^2 over all rows, in a fixed order.
+__global__ void __launch_bounds__(kBlock) k_press_den(Grid g, const double* __restrict__ sb2,
+                                                      double* __restrict__ partials) {
+    double acc[1] = {0.0};
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x)
-        isd[r] = (kind[r] == 2) ? drcp_nr(-diag[r]) : 0.0;
+        acc[0] += sb2[r];
+    block_sum_store<1>(acc, partials);
 }
 
 // largest diagonal magnitude of the normal Pore rows (for the inner scaling sigma)
@@ -645,34 +704,46 @@ ls_status pressure_setup_run(ls_ctx* c, double t) {
         LS_TRY(dalloc(c, &c->shf_label, n * c->label_bytes));
         LS_TRY(dalloc_t(c, &c->shf_perm, n));
         LS_TRY(dalloc_t(c, &c->shf_visc, n));
+        LS_TRY(dalloc_t(c, &c->psb2, n));
         c->faces_force = 1;
     }
     const int faces_force = c->faces_force;
     c->faces_force = 0;
+    const int rows_force = (faces_force || c->rows_evap_dx != pcst.evap_dx) ? 1 : 0;
     LS_TRY(wlist_reset(c));
     if (c->label_bytes == 1)
         LS_LAUNCH(c, k_faces_dirty<uint8_t>, grid, kBlock, 0, g, (const uint8_t*)c->label, c->perm, c->visc,
-                  (uint8_t*)c->shf_label, c->shf_perm, c->shf_visc, c->dirty, faces_force);
+                  (uint8_t*)c->shf_label, c->shf_perm, c->shf_visc, c->dbits, faces_force);
     else
         LS_LAUNCH(c, k_faces_dirty<uint16_t>, grid, kBlock, 0, g, (const uint16_t*)c->label, c->perm, c->visc,
-                  (uint16_t*)c->shf_label, c->shf_perm, c->shf_visc, c->dirty, faces_force);
-    LS_LAUNCH(c, k_faces_scan, grid, kBlock, 0, g, (const uint8_t*)c->dirty, c->wlist, c->wcount);
-    if (c->label_bytes == 1) {
+                  (uint16_t*)c->shf_label, c->shf_perm, c->shf_visc, c->dbits, faces_force);
+    LS_LAUNCH(c, k_faces_scan, grid, kBlock, 0, g, (const unsigned int*)c->dbits, c->dwords, c->wlist,
+              c->wcount);
+    if (c->label_bytes == 1)
         LS_LAUNCH(c, k_press_faces<uint8_t>, grid, kBlock, 0, g, (const uint8_t*)c->label, c->perm,
                   c->visc, c->pface[0], c->pface[1], c->pface[2], (const int*)c->wlist,
                   (const unsigned int*)c->wcount);
-        LS_LAUNCH(c, k_press_setup<uint8_t>, grid, kBlock, 0, g, pcst, (const uint8_t*)c->label,
-                  c->pkind, c->pdiag, c->pb, c->pface[0], c->pface[1], c->pface[2], c->partials);
-    } else {
+    else
         LS_LAUNCH(c, k_press_faces<uint16_t>, grid, kBlock, 0, g, (const uint16_t*)c->label, c->perm,
                   c->visc, c->pface[0], c->pface[1], c->pface[2], (const int*)c->wlist,
                   (const unsigned int*)c->wcount);
-        LS_LAUNCH(c, k_press_setup<uint16_t>, grid, kBlock, 0, g, pcst, (const uint16_t*)c->label,
-                  c->pkind, c->pdiag, c->pb, c->pface[0], c->pface[1], c->pface[2], c->partials);
-    }
+    // rows: the same change bits (labels, faces), plus every Air row (boundary pressure)
+    LS_CUDA(c, cudaMemsetAsync(c->wcount, 0, sizeof(unsigned int), c->stream));
+    LS_LAUNCH(c, k_rows_scan, grid, kBlock, 0, g, (const unsigned int*)c->dbits, c->dwords,
+              c->label_bytes == 1 ? (const uint8_t*)c->label : (const uint8_t*)nullptr,
+              c->label_bytes == 2 ? (const uint16_t*)c->label : (const uint16_t*)nullptr, rows_force, c->wlist,
+              c->wcount);
+    if (c->label_bytes == 1)
+        LS_LAUNCH(c, k_press_setup<uint8_t>, grid, kBlock, 0, g, pcst, (const uint8_t*)c->label, c->pkind,
+                  c->pdiag, c->pb, c->psb2, c->pisd, (const double*)c->pface[0], (const double*)c->pface[1],
+                  (const double*)c->pface[2], (const int*)c->wlist, (const unsigned int*)c->wcount);
+    else
+        LS_LAUNCH(c, k_press_setup<uint16_t>, grid, kBlock, 0, g, pcst, (const uint16_t*)c->label, c->pkind,
+                  c->pdiag, c->pb, c->psb2, c->pisd, (const double*)c->pface[0], (const double*)c->pface[1],
+                  (const double*)c->pface[2], (const int*)c->wlist, (const unsigned int*)c->wcount);
+    c->rows_evap_dx = pcst.evap_dx;
+    LS_LAUNCH(c, k_press_den, grid, kBlock, 0, g, (const double*)c->psb2, c->partials);
     LS_TRY(finalize_sum(c, grid, 1, SP_DEN));
-    LS_LAUNCH(c, k_press_isd, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const double*)c->pdiag,
-              c->pisd);
     c->p_t = t;
     c->p_ready = 1;
     return LS_OK;

@@ -227,8 +227,9 @@ __global__ void __launch_bounds__(kBlock) k_t_setup(Rows<L> op, TBuf tb, int nrh
     block_sum_store<2>(acc, partials);
 }
 
-// Change test of the transport-row inputs (pass 1 of the fully implicit setup): dirty[r] =
-// label or own face fluxes of voxel r differ bitwise from their values at the last setup.
+// Change test of the transport-row inputs (pass 1 of the fully implicit setup): the dirty
+// bit of voxel r is set when its label or own face fluxes differ bitwise from their values at
+// the last setup.
 template <typename L>
 __global__ void __launch_bounds__(kBlock) k_t_dirty(Grid g, const L* __restrict__ label,
                                                     const double* __restrict__ fx,
@@ -236,21 +237,26 @@ __global__ void __launch_bounds__(kBlock) k_t_dirty(Grid g, const L* __restrict_
                                                     const double* __restrict__ fz,
                                                     L* __restrict__ sl, double* __restrict__ sx,
                                                     double* __restrict__ sy, double* __restrict__ sz,
-                                                    uint8_t* __restrict__ dirty, int force) {
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x) {
-        const L lab = label[r];
-        const long long xb = __double_as_longlong(fx[r]), yb = __double_as_longlong(fy[r]),
-                        zb = __double_as_longlong(fz[r]);
-        const bool d = force || lab != sl[r] || xb != __double_as_longlong(sx[r]) ||
-                       yb != __double_as_longlong(sy[r]) || zb != __double_as_longlong(sz[r]);
-        if (d) {
-            sl[r] = lab;
-            sx[r] = __longlong_as_double(xb);
-            sy[r] = __longlong_as_double(yb);
-            sz[r] = __longlong_as_double(zb);
+                                                    unsigned int* __restrict__ bits, int force) {
+    for (long long r0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); r0 < g.N;
+         r0 += (long long)gridDim.x * blockDim.x) {
+        const long long r = r0 + (threadIdx.x & 31u);
+        bool d = false;
+        if (r < g.N) {
+            const L lab = label[r];
+            const long long xb = __double_as_longlong(fx[r]), yb = __double_as_longlong(fy[r]),
+                            zb = __double_as_longlong(fz[r]);
+            d = force || lab != sl[r] || xb != __double_as_longlong(sx[r]) || yb != __double_as_longlong(sy[r]) ||
+                zb != __double_as_longlong(sz[r]);
+            if (d) {
+                sl[r] = lab;
+                sx[r] = __longlong_as_double(xb);
+                sy[r] = __longlong_as_double(yb);
+                sz[r] = __longlong_as_double(zb);
+            }
         }
-        dirty[r] = d ? 1 : 0;
+        const unsigned int w = __ballot_sync(0xffffffffu, d);
+        if ((threadIdx.x & 31u) == 0u) bits[r0 >> 5] = w;
     }
 }
 
@@ -259,15 +265,26 @@ __global__ void __launch_bounds__(kBlock) k_t_dirty(Grid g, const L* __restrict_
 // the rows with a dirty voxel among those, pass 3 recomputes their coefficients, pass 4
 // forms the right-hand sides of every row (old value over dt, or the old value on identity
 // rows) and the partial norms in a fixed order.
-__global__ void __launch_bounds__(kBlock) k_t_scan(Grid g, const uint8_t* __restrict__ dirty,
+__global__ void __launch_bounds__(kBlock) k_t_scan(Grid g, const unsigned int* __restrict__ bits, long long nw,
                                                    int* __restrict__ list, unsigned int* __restrict__ count) {
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < (int)g.N; r += gridDim.x * blockDim.x) {
-        int i, j, k;
-        decode(g, r, i, j, k);
-        const bool d = dirty[r] || (i > 0 && dirty[r - g.JK]) || (i + 1 < g.I && dirty[r + g.JK]) ||
-                       (j > 0 && dirty[r - g.K]) || (j + 1 < g.J && dirty[r + g.K]) ||
-                       (k > 0 && dirty[r - 1]) || (k + 1 < g.K && dirty[r + 1]);
-        warp_append(d, r, list, count);
+    const int lane = (int)(threadIdx.x & 31u);
+    // block-uniform trip count (block_append is called by every thread of the block)
+    for (long long b0 = (long long)blockIdx.x * blockDim.x; b0 < g.N; b0 += (long long)gridDim.x * blockDim.x) {
+        const long long r0 = b0 + (threadIdx.x & ~31u);
+        const long long r = r0 + lane;
+        const unsigned int own = dwin(bits, nw, r0);
+        const unsigned int km = dwin(bits, nw, r0 - 1), kp = dwin(bits, nw, r0 + 1);
+        const unsigned int jm = dwin(bits, nw, r0 - g.K), jp = dwin(bits, nw, r0 + g.K);
+        const unsigned int im = dwin(bits, nw, r0 - g.JK), ip = dwin(bits, nw, r0 + g.JK);
+        bool d = false;
+        if (r < g.N) {
+            int i, j, k;
+            decode(g, r, i, j, k);
+            d = dbit(own, lane) || (i > 0 && dbit(im, lane)) || (i + 1 < g.I && dbit(ip, lane)) ||
+                (j > 0 && dbit(jm, lane)) || (j + 1 < g.J && dbit(jp, lane)) || (k > 0 && dbit(km, lane)) ||
+                (k + 1 < g.K && dbit(kp, lane));
+        }
+        block_append(d, (int)r, list, count);
     }
 }
 
@@ -296,9 +313,13 @@ __global__ void __launch_bounds__(kBlock) k_t_rows(Rows<L> op, TBuf tb, const in
     }
 }
 
+// Also counts, per right-hand side, the rows where b or the solution after k_t_xid (b on
+// identity rows) is nonzero: a system with none has the exact solution x = 0 already.
 __global__ void __launch_bounds__(kBlock) k_t_rhs(Grid g, double inv_dt, TBuf tb, int nrhs, const double* f0,
-                                                  const double* f1, double* __restrict__ partials) {
-    double acc[2] = {0.0, 0.0};
+                                                  const double* f1, const double* __restrict__ x0,
+                                                  const double* __restrict__ x1, double* __restrict__ partials) {
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    unsigned int nz[2] = {0u, 0u};
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < (int)g.N; r += gridDim.x * blockDim.x) {
         const int kind = tb.kind[r];
         const double inv = tb.inv[r];
@@ -310,10 +331,17 @@ __global__ void __launch_bounds__(kBlock) k_t_rhs(Grid g, double inv_dt, TBuf tb
             tb.b[q][r] = rhs;
             double bt = rhs * inv;
             acc[q] += bt * bt;
+            const double xv = (kind == 1) ? rhs : (q ? x1 : x0)[r];
+            const long long m = 0x7fffffffffffffffll;
+            if ((__double_as_longlong(rhs) & m) != 0 || (__double_as_longlong(xv) & m) != 0) nz[q]++;
         }
     }
-    block_sum_store<2>(acc, partials);
+    acc[2] = (double)nz[0];
+    acc[3] = (double)nz[1];
+    block_sum_store<4>(acc, partials);
 }
+
+__global__ void k_set_ones(double* v) { v[threadIdx.x] = 1.0; }
 
 // identity rows take their value
 __global__ void k_t_xid(Grid g, TBuf tb, double* x0, double* x1, int nrhs) {
@@ -1022,10 +1050,12 @@ static ls_status mixed_solve(ls_ctx* c, const Rows<L>& rows, int nrhs, const dou
         const int force = (!c->t_valid || memcmp(consts, c->t_consts, sizeof(consts)) != 0) ? 1 : 0;
         LS_TRY(wlist_reset(c));
         LS_LAUNCH(c, k_t_dirty<L>, grid, kBlock, 0, g, rows.label, rows.fx, rows.fy, rows.fz,
-                  (L*)c->sht_label, c->sht_fx, c->sht_fy, c->sht_fz, c->dirty, force);
-        LS_LAUNCH(c, k_t_scan, grid, kBlock, 0, g, (const uint8_t*)c->dirty, c->wlist, c->wcount);
+                  (L*)c->sht_label, c->sht_fx, c->sht_fy, c->sht_fz, c->dbits, force);
+        LS_LAUNCH(c, k_t_scan, grid, kBlock, 0, g, (const unsigned int*)c->dbits, c->dwords, c->wlist, c->wcount);
         LS_LAUNCH(c, k_t_rows<L>, grid, kBlock, 0, rows, tb, (const int*)c->wlist, (const unsigned int*)c->wcount);
-        LS_LAUNCH(c, k_t_rhs, grid, kBlock, 0, g, rows.tc.inv_dt, tb, nrhs, f0, f1, c->partials);
+        LS_LAUNCH(c, k_t_rhs, grid, kBlock, 0, g, rows.tc.inv_dt, tb, nrhs, f0, f1, (const double*)x0,
+                  (const double*)x1, c->partials);
+        LS_TRY(finalize_sum(c, grid, 4, S_RED0 + 4));
         memcpy(c->t_consts, consts, sizeof(consts));
         c->t_valid = 1;
     } else {
@@ -1033,14 +1063,18 @@ static ls_status mixed_solve(ls_ctx* c, const Rows<L>& rows, int nrhs, const dou
             LS_LAUNCH(c, (k_t_setup<L, true>), grid, kBlock, 0, rows, tb, nrhs, f0, f1, c->partials);
         else
             LS_LAUNCH(c, (k_t_setup<L, false>), grid, kBlock, 0, rows, tb, nrhs, f0, f1, c->partials);
+        LS_TRY(finalize_sum(c, grid, 2, S_RED0 + 4));
+        LS_LAUNCH(c, k_set_ones, 1, 2, 0, c->scal + S_RED0 + 6);
         c->t_valid = 0;  // the row buffers now hold other rows
     }
-    LS_TRY(finalize_sum(c, grid, 2, S_RED0 + 4));
     LS_LAUNCH(c, k_t_xid, grid, kBlock, 0, g, tb, x0, x1, nrhs);
-    double den[2];
-    LS_TRY(read_scalars(c, S_RED0 + 4, 2, den));
+    double den[4];
+    LS_TRY(read_scalars(c, S_RED0 + 4, 4, den));
     int mask = nrhs > 1 ? 3 : 1;
     int its[2] = {0, 0}, sweeps[2] = {0, 0}, reason[2] = {0, 0};
+    // a system with b = 0 and x = 0 on every row is solved exactly: no residual pass
+    for (int q = 0; q < nrhs; ++q)
+        if (den[2 + q] == 0.0) { reason[q] = 2; mask &= ~(1 << q); }
     double rel[2] = {0.0, 0.0}, prev[2] = {INFINITY, INFINITY};
     int stagnant[2] = {0, 0};
     const int max_sweeps = 40;
@@ -1082,10 +1116,12 @@ static ls_status mixed_solve(ls_ctx* c, const Rows<L>& rows, int nrhs, const dou
     ls_status st = LS_OK;
     double* xs[2] = {x0, x1};
     for (int q = 0; q < nrhs; ++q) {
-        double mm[2] = {0.0, 0.0};
-        LS_LAUNCH(c, k_minmax, grid, kBlock, 0, g, (const double*)xs[q], c->partials);
-        LS_TRY(finalize_max(c, grid, 2, S_RED0 + 2));
-        LS_TRY(read_scalars(c, S_RED0 + 2, 2, mm));
+        double mm[2] = {0.0, -0.0};  // max x, max -x
+        if (den[2 + q] != 0.0) {  // otherwise x = 0 on every row
+            LS_LAUNCH(c, k_minmax, grid, kBlock, 0, g, (const double*)xs[q], c->partials);
+            LS_TRY(finalize_max(c, grid, 2, S_RED0 + 2));
+            LS_TRY(read_scalars(c, S_RED0 + 2, 2, mm));
+        }
         if (info[q]) {
             info[q]->iterations = its[q];
             info[q]->outer_iterations = sweeps[q];
