@@ -237,8 +237,12 @@ __global__ void k_mg_coarse_op(Grid f, Grid cg, const int* __restrict__ fcomp, c
 
 // x_out = x + omega invd (b - M x); x == nullptr means x = 0. With dotv, the per-block
 // partial of (dotv, x_out) is stored (the (r, z) of the PCG).
+// Cells that are not members keep 0 in every level vector: the buffers are cleared when
+// allocated and nothing writes them there, so the smoother skips them (membership from the
+// 1-byte kind on the finest level, the component id on coarse levels).
 template <typename T>
-__global__ void __launch_bounds__(kBlock) k_mg_smooth(Grid g, const int* __restrict__ comp, const T* __restrict__ e,
+__global__ void __launch_bounds__(kBlock) k_mg_smooth(Grid g, const int* __restrict__ comp,
+                                                      const int8_t* __restrict__ kind0, const T* __restrict__ e,
                                                       const T* __restrict__ f0, const T* __restrict__ f1,
                                                       const T* __restrict__ f2, const T* __restrict__ invd,
                                                       const T* __restrict__ b, const T* __restrict__ x,
@@ -247,17 +251,17 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth(Grid g, const int* __restr
     T acc = (T)0;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
-        T out = (T)0;
-        if (comp[r] >= 0) {
-            T bv = b[r];
-            if (x) {
-                int i, j, k;
-                decode(g, r, i, j, k);
-                T res = bv - m_apply(g, r, i, j, k, e, f0, f1, f2, x);
-                out = x[r] + (T)kOmega * invd[r] * res;
-            } else {
-                out = (T)kOmega * invd[r] * bv;
-            }
+        const bool live = kind0 ? kind0[r] == 2 : comp[r] >= 0;
+        if (!live) continue;
+        T out;
+        T bv = b[r];
+        if (x) {
+            int i, j, k;
+            decode(g, r, i, j, k);
+            T res = bv - m_apply(g, r, i, j, k, e, f0, f1, f2, x);
+            out = x[r] + (T)kOmega * invd[r] * res;
+        } else {
+            out = (T)kOmega * invd[r] * bv;
         }
         xo[r] = out;
         if (dotv) acc += dotv[r] * out;
@@ -373,6 +377,8 @@ static ls_status mg_alloc(ls_ctx* c) {
     if (!c->cc_flag) LS_TRY(dalloc_t(c, &c->cc_flag, (size_t)4));
     LS_TRY(dalloc(c, &c->mg0_x, sizeof(T) * (size_t)c->g.N));
     LS_TRY(dalloc(c, &c->mg0_t, sizeof(T) * (size_t)c->g.N));
+    LS_CUDA(c, cudaMemsetAsync(c->mg0_x, 0, sizeof(T) * (size_t)c->g.N, c->stream));
+    LS_CUDA(c, cudaMemsetAsync(c->mg0_t, 0, sizeof(T) * (size_t)c->g.N, c->stream));
     Grid g = c->g;
     g.NP = g.N;
     while ((c->mg.empty() || g.N > kCoarsestCells) && (g.I > 1 || g.J > 1 || g.K > 1)) {
@@ -381,7 +387,10 @@ static ls_status mg_alloc(ls_ctx* c) {
         lv.g = cg;
         LS_TRY(dalloc_t(c, &lv.comp, (size_t)cg.N));
         void** arrs[] = {&lv.e, &lv.face[0], &lv.face[1], &lv.face[2], &lv.invd, &lv.x, &lv.b, &lv.t};
-        for (void** q : arrs) LS_TRY(dalloc(c, q, sizeof(T) * (size_t)cg.N));
+        for (void** q : arrs) {
+            LS_TRY(dalloc(c, q, sizeof(T) * (size_t)cg.N));
+            LS_CUDA(c, cudaMemsetAsync(*q, 0, sizeof(T) * (size_t)cg.N, c->stream));
+        }
         c->mg.push_back(lv);
         g = cg;
     }
@@ -437,6 +446,20 @@ ls_status mg_setup(ls_ctx* c) {
     return LS_OK;
 }
 
+// Zero every level vector (the smoother and the PCG skip non-member cells, which must hold 0).
+template <typename T>
+ls_status mg_clear(ls_ctx* c) {
+    LS_CUDA(c, cudaMemsetAsync(c->mg0_x, 0, sizeof(T) * (size_t)c->g.N, c->stream));
+    LS_CUDA(c, cudaMemsetAsync(c->mg0_t, 0, sizeof(T) * (size_t)c->g.N, c->stream));
+    for (auto& lv : c->mg) {
+        const size_t b = sizeof(T) * (size_t)lv.g.N;
+        LS_CUDA(c, cudaMemsetAsync(lv.x, 0, b, c->stream));
+        LS_CUDA(c, cudaMemsetAsync(lv.b, 0, b, c->stream));
+        LS_CUDA(c, cudaMemsetAsync(lv.t, 0, b, c->stream));
+    }
+    return LS_OK;
+}
+
 // z = B r (one V-cycle); the per-block partials of (r, z) are left in c->partials and
 // their count in *nblocks_out.
 template <typename T>
@@ -463,9 +486,9 @@ ls_status mg_apply(ls_ctx* c, const T* r, T* z, int* nblocks_out) {
         Lv& cl = lv[l + 1];
         const T* b = (l == 0) ? r : a.b;
         const int gd = grid_for(c, a.g.N);
-        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, a.invd, b,
+        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp, l == 0 ? (const int8_t*)c->pkind : (const int8_t*)nullptr, a.e, a.f0, a.f1, a.f2, a.invd, b,
                   (const T*)nullptr, a.t, (const T*)nullptr, (double*)nullptr);
-        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, a.invd, b,
+        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp, l == 0 ? (const int8_t*)c->pkind : (const int8_t*)nullptr, a.e, a.f0, a.f1, a.f2, a.invd, b,
                   (const T*)a.t, a.x, (const T*)nullptr, (double*)nullptr);
         LS_LAUNCH(c, k_mg_restrict<T>, grid_for(c, cl.g.N), kBlock, 0, a.g, cl.g, a.comp, cl.comp, a.e, a.f0,
                   a.f1, a.f2, b, (const T*)a.x, cl.b);
@@ -482,10 +505,10 @@ ls_status mg_apply(ls_ctx* c, const T* r, T* z, int* nblocks_out) {
         const T* b = (l == 0) ? r : a.b;
         const int gd = grid_for(c, a.g.N);
         LS_LAUNCH(c, k_mg_prolong<T>, gd, kBlock, 0, a.g, cl.g, a.comp, cl.comp, (const T*)cl.x, a.x);
-        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, a.invd, b,
+        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp, l == 0 ? (const int8_t*)c->pkind : (const int8_t*)nullptr, a.e, a.f0, a.f1, a.f2, a.invd, b,
                   (const T*)a.x, a.t, (const T*)nullptr, (double*)nullptr);
         T* out = (l == 0) ? z : a.x;
-        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, a.invd, b,
+        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp, l == 0 ? (const int8_t*)c->pkind : (const int8_t*)nullptr, a.e, a.f0, a.f1, a.f2, a.invd, b,
                   (const T*)a.t, out, (l == 0) ? r : (const T*)nullptr,
                   (l == 0) ? c->partials : (double*)nullptr);
         if (l == 0 && nblocks_out) *nblocks_out = gd;
@@ -497,6 +520,8 @@ template ls_status inner_invd<float>(ls_ctx*);
 template ls_status inner_invd<double>(ls_ctx*);
 template ls_status mg_setup<float>(ls_ctx*);
 template ls_status mg_setup<double>(ls_ctx*);
+template ls_status mg_clear<float>(ls_ctx*);
+template ls_status mg_clear<double>(ls_ctx*);
 template ls_status mg_apply<float>(ls_ctx*, const float*, float*, int*);
 template ls_status mg_apply<double>(ls_ctx*, const double*, double*, int*);
 

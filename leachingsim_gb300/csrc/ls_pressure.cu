@@ -31,6 +31,8 @@ namespace ls {
 template <typename T>
 ls_status mg_setup(ls_ctx* c);
 template <typename T>
+ls_status mg_clear(ls_ctx* c);
+template <typename T>
 ls_status mg_apply(ls_ctx* c, const T* r, T* z, int* nblocks_out);
 template <typename T>
 ls_status inner_invd(ls_ctx* c);
@@ -532,9 +534,14 @@ __device__ __forceinline__ T inner_apply_row(const Grid& g, long long r, int i, 
     return acc;
 }
 
+// The inner vectors are zero on voxels that are not inner unknowns (kind != 2) and no
+// kernel writes them there (the buffers are cleared when allocated), so the inner PCG
+// kernels skip those voxels: ~3/4 of the box in a porosity-0.25 medium.
+
 // q = M p, partial (p, q)
 template <typename T>
-__global__ void __launch_bounds__(kBlock) k_cg_apply(Grid g, const T* __restrict__ p,
+__global__ void __launch_bounds__(kBlock) k_cg_apply(Grid g, const int8_t* __restrict__ kind,
+                                                     const T* __restrict__ p,
                                                      const T* __restrict__ e,
                                                      const T* __restrict__ w0,
                                                      const T* __restrict__ w1,
@@ -543,6 +550,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_apply(Grid g, const T* __restrict
     T a = (T)0;  // per-thread partial in the inner precision
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
+        if (kind[r] != 2) continue;
         int i, j, k;
         decode(g, r, i, j, k);
         T qv = inner_apply_row(g, r, i, j, k, p, e, w0, w1, w2);
@@ -555,12 +563,14 @@ __global__ void __launch_bounds__(kBlock) k_cg_apply(Grid g, const T* __restrict
 
 // x += a p, r -= a q with a = (r,z)/(p,q) (0 when (p,q) <= 0)
 template <typename T>
-__global__ void k_cg_update(Grid g, const double* __restrict__ scal, const T* __restrict__ p,
-                            const T* __restrict__ q, T* __restrict__ x, T* __restrict__ r_) {
+__global__ void k_cg_update(Grid g, const int8_t* __restrict__ kind, const double* __restrict__ scal,
+                            const T* __restrict__ p, const T* __restrict__ q, T* __restrict__ x,
+                            T* __restrict__ r_) {
     const double pq = scal[SP_PQ];
     const T a = (T)((pq > 0.0) ? scal[SP_RZ] / pq : 0.0);
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
+        if (kind[r] != 2) continue;
         x[r] += a * p[r];
         r_[r] -= a * q[r];
     }
@@ -585,12 +595,12 @@ __global__ void __launch_bounds__(kBlock) k_cg_jacobi(Grid g, const T* __restric
 
 // p = z + b p with b = (r,z)_new / (r,z)_old
 template <typename T>
-__global__ void k_cg_dir(Grid g, const double* __restrict__ scal, const T* __restrict__ z,
-                         T* __restrict__ p) {
+__global__ void k_cg_dir(Grid g, const int8_t* __restrict__ kind, const double* __restrict__ scal,
+                         const T* __restrict__ z, T* __restrict__ p) {
     const T beta = (T)(scal[SP_RZN] / scal[SP_RZ]);
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x)
-        p[r] = z[r] + beta * p[r];
+        if (kind[r] == 2) p[r] = z[r] + beta * p[r];
 }
 
 // p = z, x = 0
@@ -617,7 +627,10 @@ static ls_status inner_alloc(ls_ctx* c) {
         *q = nullptr;
     }
     c->inner_is64 = -1;
-    for (void** q : arrs) LS_TRY(dalloc(c, q, sizeof(T) * (size_t)c->g.N));
+    for (void** q : arrs) {
+        LS_TRY(dalloc(c, q, sizeof(T) * (size_t)c->g.N));
+        LS_CUDA(c, cudaMemsetAsync(*q, 0, sizeof(T) * (size_t)c->g.N, c->stream));
+    }
     c->inner_is64 = is64;
     return LS_OK;
 }
@@ -664,13 +677,14 @@ static ls_status inner_pcg(ls_ctx* c, bool use_mg, double tol, int max_it, int* 
     for (int it = 0; it < max_it; ++it) {
         {
             Timed tm(c, LS_T_CG_APPLY);
-            LS_LAUNCH(c, k_cg_apply<T>, grid, kBlock, 0, g, (const T*)p, e, w0, w1, w2, q, c->partials);
+            LS_LAUNCH(c, k_cg_apply<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const T*)p, e, w0, w1, w2,
+                      q, c->partials);
             // p in, excess and three own face links, q out
             if (c->timing) c->timer_bytes[LS_T_CG_APPLY] += (double)g.N * 6.0 * sizeof(T);
         }
         LS_TRY(finalize_sum(c, grid, 1, SP_PQ));
-        LS_LAUNCH(c, k_cg_update<T>, grid, kBlock, 0, g, (const double*)c->scal, (const T*)p,
-                  (const T*)q, x, r);
+        LS_LAUNCH(c, k_cg_update<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const double*)c->scal,
+                  (const T*)p, (const T*)q, x, r);
         LS_TRY(precondition(SP_RZN));
         *its = it + 1;
         double sc[3];
@@ -679,7 +693,8 @@ static ls_status inner_pcg(ls_ctx* c, bool use_mg, double tol, int max_it, int* 
         rz = sc[1];
         if (rz != rz) return set_error(c, LS_NONFINITE, "pressure: NaN in inner PCG");
         if (rz <= target || !(pq > 0.0) || rz < 0.0) break;
-        LS_LAUNCH(c, k_cg_dir<T>, grid, kBlock, 0, g, (const double*)c->scal, (const T*)z, p);
+        LS_LAUNCH(c, k_cg_dir<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const double*)c->scal,
+                  (const T*)z, p);
         LS_LAUNCH(c, k_set_scalar, 1, 1, 0, c->scal, SP_RZ, SP_RZN);
     }
     *rel_out = sqrt(std::max(rz, 0.0) / rz0);
@@ -794,6 +809,11 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info) {
                   (T*)c->ie, (T*)c->iface[0], (T*)c->iface[1], (T*)c->iface[2]);
         LS_TRY(inner_invd<T>(c));
         if (use_mg) LS_TRY(mg_setup<T>(c));
+        // the PCG and multigrid kernels skip voxels that are not inner unknowns, which must
+        // hold 0 there: clear what earlier solves (with other unknowns) left behind
+        for (int v = 0; v < 5; ++v)
+            LS_CUDA(c, cudaMemsetAsync(c->inner[v], 0, sizeof(T) * (size_t)g.N, c->stream));
+        if (use_mg) LS_TRY(mg_clear<T>(c));
         return LS_OK;
     };
     double den = 0.0;
