@@ -79,6 +79,26 @@ static void resolve_regions(ls_ctx* c) {
 // ---------------------------------------------------------------------------
 // reductions
 
+ls_status l0_alloc(ls_ctx* c, int slot, size_t esize, void** out) {
+    if (c->l0pad == 0) c->l0pad = ((c->g.JK + 31) / 32) * 32;
+    const size_t bytes = esize * ((size_t)c->g.N + 2 * (size_t)c->l0pad);
+    LS_TRY(dalloc(c, &c->l0base[slot], bytes));
+    c->l0bytes[slot] = bytes;
+    LS_CUDA(c, cudaMemsetAsync(c->l0base[slot], 0, bytes, c->stream));
+    *out = (char*)c->l0base[slot] + esize * (size_t)c->l0pad;
+    return LS_OK;
+}
+
+void l0_free(ls_ctx* c, int slot, void** p) {
+    if (c->l0base[slot]) {
+        cudaFree(c->l0base[slot]);
+        c->device_bytes -= c->l0bytes[slot];
+    }
+    c->l0base[slot] = nullptr;
+    c->l0bytes[slot] = 0;
+    *p = nullptr;
+}
+
 ls_status wlist_reset(ls_ctx* c) {
     const size_t n = (size_t)c->g.N;
     if (!c->wlist) LS_TRY(dalloc_t(c, &c->wlist, n));
@@ -332,15 +352,15 @@ ls_status ls_destroy(ls_ctx* c) {
                     c->acid, c->fx, c->fy, c->fz, c->sat, c->pc, c->kr, c->precip,
                     c->b_precip, c->b_sat, c->b_P, c->b_conc, c->b_acid, c->b_fx, c->b_fy,
                     c->b_fz, c->pkind, c->pdiag, c->pb, c->pface[0], c->pface[1], c->pface[2],
-                    c->pisd, c->pr, c->pdelta, c->ie, c->iface[0], c->iface[1], c->iface[2],
-                    c->iinvd, c->inner[0], c->inner[1], c->inner[2], c->inner[3],
-                    c->inner[4], c->mg0_x, c->mg0_t, c->comp, c->cc_flag, c->tkind, c->tinv, c->dz_list,
+                    c->pisd, c->pr, c->pdelta, c->comp, c->cc_flag, c->tkind, c->tinv, c->dz_list,
                     c->dz_count, c->dz_level_start, c->partials, c->scal, c->d_int,
                     c->sh_label, c->sh_sat, c->sh_precip, c->sh_frac, c->shf_label, c->shf_perm,
                     c->shf_visc, c->psb2, c->sat_q, c->dbits, c->sht_label, c->sht_fx, c->sht_fy, c->sht_fz,
                     c->shq_P, c->shq_C, c->shq_K, c->shq_V, c->shq_fx, c->shq_fy, c->shq_fz,
                     c->wlist, c->wcount};
     for (void* q : ptrs)
+        if (q) cudaFree(q);
+    for (void* q : c->l0base)
         if (q) cudaFree(q);
     for (double* q : c->tc)
         if (q) cudaFree(q);

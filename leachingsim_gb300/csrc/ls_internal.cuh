@@ -175,6 +175,41 @@ __device__ __forceinline__ void block_append(bool pred, int value, int* list, un
     __syncthreads();
 }
 
+// Finest level of the inner pressure system, FP32, even row length K: (M x) for the pair of
+// cells (r, r+1), r = 2t even, in the excess + Laplacian form
+//   (M x)_r = e_r x_r + sum over the six faces c (x_r - x_nb),
+// with the terms in the order -i, -j, -k, +k, +j, +i and separate multiply and add, as the
+// per-cell kernels evaluate it. The arrays are padded (l0pad zero elements on both sides) and
+// faces leaving the domain are zero, so no bounds tests are needed: such terms add 0 * (...).
+__device__ __forceinline__ float2 m0_apply_pair(int t, int JK2, int K2, const float* __restrict__ e,
+                                                const float* __restrict__ f0, const float* __restrict__ f1,
+                                                const float* __restrict__ f2, const float* __restrict__ x) {
+    const int r = 2 * t;
+    const float2 ec = reinterpret_cast<const float2*>(e)[t];
+    const float2 f0c = reinterpret_cast<const float2*>(f0)[t], f0m = reinterpret_cast<const float2*>(f0)[t - JK2];
+    const float2 f1c = reinterpret_cast<const float2*>(f1)[t], f1m = reinterpret_cast<const float2*>(f1)[t - K2];
+    const float2 f2c = reinterpret_cast<const float2*>(f2)[t];
+    const float f2m = f2[r - 1];
+    const float2* x2 = reinterpret_cast<const float2*>(x);
+    const float2 xc = x2[t], xim = x2[t - JK2], xip = x2[t + JK2], xjm = x2[t - K2], xjp = x2[t + K2];
+    const float xkm = x[r - 1], xkp = x[r + 2];
+    float a0 = ec.x * xc.x;
+    a0 += f0m.x * (xc.x - xim.x);
+    a0 += f1m.x * (xc.x - xjm.x);
+    a0 += f2m * (xc.x - xkm);
+    a0 += f2c.x * (xc.x - xc.y);
+    a0 += f1c.x * (xc.x - xjp.x);
+    a0 += f0c.x * (xc.x - xip.x);
+    float a1 = ec.y * xc.y;
+    a1 += f0m.y * (xc.y - xim.y);
+    a1 += f1m.y * (xc.y - xjm.y);
+    a1 += f2c.x * (xc.y - xc.x);
+    a1 += f2c.y * (xc.y - xkp);
+    a1 += f1c.y * (xc.y - xjp.y);
+    a1 += f0c.y * (xc.y - xip.y);
+    return make_float2(a0, a1);
+}
+
 // Timed region record.
 struct TimedRegion {
     int timer;
@@ -221,6 +256,12 @@ struct ls_ctx {
     void* iface[3];     // link coefficients of the +i, +j, +k faces between two unknowns, T
     void* iinvd;        // 1 / (e + sum of the six links), T
     void* inner[5];     // inner PCG vectors x r z p q, T
+    // the finest-level arrays (ie, iface, iinvd, inner, mg0_x, mg0_t) carry l0pad zero
+    // elements on both sides, so stencil loads need no bounds tests; l0base holds the
+    // allocations (slots: 0 ie, 1-3 iface, 4 iinvd, 5-9 inner, 10 mg0_x, 11 mg0_t)
+    void* l0base[12];
+    size_t l0bytes[12];
+    long long l0pad;
     int inner_is64;     // -1 = not allocated
     double pscale_den;  // ||D^-1 b|| of the current pressure system
     double p_t;         // time the pressure system was assembled for
@@ -451,6 +492,10 @@ ls_status init_saturation_run(ls_ctx* c);
 ls_status dalloc(ls_ctx* c, void** p, size_t bytes);
 // the work list, its counter and the dirty flags, allocated on first use; resets the counter
 ls_status wlist_reset(ls_ctx* c);
+// finest-level array in slot `slot`: N elements of `esize` bytes with l0pad zero elements on
+// both sides (cleared); *out points at element 0
+ls_status l0_alloc(ls_ctx* c, int slot, size_t esize, void** out);
+void l0_free(ls_ctx* c, int slot, void** p);
 template <typename T>
 ls_status dalloc_t(ls_ctx* c, T** p, size_t n) {
     return dalloc(c, reinterpret_cast<void**>(p), n * sizeof(T));

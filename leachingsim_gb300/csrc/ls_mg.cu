@@ -21,6 +21,7 @@
 //     number of Jacobi sweeps by one CTA on the coarsest level, so the cycle is a symmetric
 //     operator usable inside CG.
 #include <algorithm>
+#include <type_traits>
 #include <cstdio>
 
 #include "ls_internal.cuh"
@@ -272,6 +273,46 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth(Grid g, const int* __restr
     }
 }
 
+// The finest-level smoother on pairs of cells (FP32, K even, padded arrays; see
+// m0_apply_pair): the same sweep as k_mg_smooth for kind-2 cells.
+__global__ void __launch_bounds__(kBlock) k_mg_smooth0_pair(int N2, int JK2, int K2,
+                                                            const int8_t* __restrict__ kind,
+                                                            const float* __restrict__ e, const float* __restrict__ f0,
+                                                            const float* __restrict__ f1, const float* __restrict__ f2,
+                                                            const float* __restrict__ invd, const float* __restrict__ b,
+                                                            const float* __restrict__ x, float* __restrict__ xo,
+                                                            const float* __restrict__ dotv,
+                                                            double* __restrict__ partials) {
+    float acc = 0.f;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N2; t += gridDim.x * blockDim.x) {
+        const char2 kd = reinterpret_cast<const char2*>(kind)[t];
+        const bool l0 = kd.x == 2, l1 = kd.y == 2;
+        if (!l0 && !l1) continue;
+        const float2 bv = reinterpret_cast<const float2*>(b)[t];
+        const float2 iv = reinterpret_cast<const float2*>(invd)[t];
+        float o0, o1;
+        if (x) {
+            const float2 m = m0_apply_pair(t, JK2, K2, e, f0, f1, f2, x);
+            const float2 xv = reinterpret_cast<const float2*>(x)[t];
+            o0 = xv.x + (float)kOmega * iv.x * (bv.x - m.x);
+            o1 = xv.y + (float)kOmega * iv.y * (bv.y - m.y);
+        } else {
+            o0 = (float)kOmega * iv.x * bv.x;
+            o1 = (float)kOmega * iv.y * bv.y;
+        }
+        if (l0) xo[2 * t] = o0;
+        if (l1) xo[2 * t + 1] = o1;
+        if (dotv) {
+            if (l0) acc += dotv[2 * t] * o0;
+            if (l1) acc += dotv[2 * t + 1] * o1;
+        }
+    }
+    if (dotv) {
+        double a[1] = {(double)acc};
+        block_sum_store<1>(a, partials);
+    }
+}
+
 // coarse right-hand side: b_c(R) = sum over owned members of (b - M x)
 template <typename T>
 __global__ void k_mg_restrict(Grid f, Grid cg, const int* __restrict__ fcomp, const int* __restrict__ ccomp,
@@ -362,9 +403,8 @@ void mg_free(ls_ctx* c) {
             if (q) cudaFree(q);
     }
     c->mg.clear();
-    if (c->mg0_x) cudaFree(c->mg0_x);
-    if (c->mg0_t) cudaFree(c->mg0_t);
-    c->mg0_x = c->mg0_t = nullptr;
+    l0_free(c, 10, &c->mg0_x);
+    l0_free(c, 11, &c->mg0_t);
     c->mg_is64 = -1;
 }
 
@@ -375,10 +415,8 @@ static ls_status mg_alloc(ls_ctx* c) {
     mg_free(c);
     if (!c->comp) LS_TRY(dalloc_t(c, &c->comp, (size_t)c->g.N));
     if (!c->cc_flag) LS_TRY(dalloc_t(c, &c->cc_flag, (size_t)4));
-    LS_TRY(dalloc(c, &c->mg0_x, sizeof(T) * (size_t)c->g.N));
-    LS_TRY(dalloc(c, &c->mg0_t, sizeof(T) * (size_t)c->g.N));
-    LS_CUDA(c, cudaMemsetAsync(c->mg0_x, 0, sizeof(T) * (size_t)c->g.N, c->stream));
-    LS_CUDA(c, cudaMemsetAsync(c->mg0_t, 0, sizeof(T) * (size_t)c->g.N, c->stream));
+    LS_TRY(l0_alloc(c, 10, sizeof(T), &c->mg0_x));
+    LS_TRY(l0_alloc(c, 11, sizeof(T), &c->mg0_t));
     Grid g = c->g;
     g.NP = g.N;
     while ((c->mg.empty() || g.N > kCoarsestCells) && (g.I > 1 || g.J > 1 || g.K > 1)) {
@@ -480,16 +518,35 @@ ls_status mg_apply(ls_ctx* c, const T* r, T* z, int* nblocks_out) {
         lv[l + 1] = {m.g, m.comp, (const T*)m.e, (const T*)m.face[0], (const T*)m.face[1], (const T*)m.face[2],
                      (const T*)m.invd, (T*)m.x, (T*)m.b, (T*)m.t};
     }
+    // one damped-Jacobi sweep on level l (paired finest-level kernel for FP32 and even K)
+    const bool pair0 = std::is_same<T, float>::value && (c->g.K % 2 == 0);
+    auto smooth = [&](size_t l, const T* b, const T* x, T* xo, const T* dotv, double* partials,
+                      int* nb) -> ls_status {
+        Lv& a = lv[l];
+        if (l == 0 && pair0) {
+            const int N2 = (int)(a.g.N / 2);
+            const int gd = grid_for(c, N2);
+            LS_LAUNCH(c, k_mg_smooth0_pair, gd, kBlock, 0, N2, (int)(a.g.JK / 2), a.g.K / 2,
+                      (const int8_t*)c->pkind, (const float*)a.e, (const float*)a.f0, (const float*)a.f1,
+                      (const float*)a.f2, (const float*)a.invd, (const float*)b, (const float*)x, (float*)xo,
+                      (const float*)dotv, partials);
+            if (nb) *nb = gd;
+            return LS_OK;
+        }
+        const int gd = grid_for(c, a.g.N);
+        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp,
+                  l == 0 ? (const int8_t*)c->pkind : (const int8_t*)nullptr, a.e, a.f0, a.f1, a.f2, a.invd, b, x,
+                  xo, dotv, partials);
+        if (nb) *nb = gd;
+        return LS_OK;
+    };
     // descending leg
     for (size_t l = 0; l < L; ++l) {
         Lv& a = lv[l];
         Lv& cl = lv[l + 1];
         const T* b = (l == 0) ? r : a.b;
-        const int gd = grid_for(c, a.g.N);
-        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp, l == 0 ? (const int8_t*)c->pkind : (const int8_t*)nullptr, a.e, a.f0, a.f1, a.f2, a.invd, b,
-                  (const T*)nullptr, a.t, (const T*)nullptr, (double*)nullptr);
-        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp, l == 0 ? (const int8_t*)c->pkind : (const int8_t*)nullptr, a.e, a.f0, a.f1, a.f2, a.invd, b,
-                  (const T*)a.t, a.x, (const T*)nullptr, (double*)nullptr);
+        LS_TRY(smooth(l, b, (const T*)nullptr, a.t, (const T*)nullptr, (double*)nullptr, nullptr));
+        LS_TRY(smooth(l, b, (const T*)a.t, a.x, (const T*)nullptr, (double*)nullptr, nullptr));
         LS_LAUNCH(c, k_mg_restrict<T>, grid_for(c, cl.g.N), kBlock, 0, a.g, cl.g, a.comp, cl.comp, a.e, a.f0,
                   a.f1, a.f2, b, (const T*)a.x, cl.b);
     }
@@ -505,13 +562,10 @@ ls_status mg_apply(ls_ctx* c, const T* r, T* z, int* nblocks_out) {
         const T* b = (l == 0) ? r : a.b;
         const int gd = grid_for(c, a.g.N);
         LS_LAUNCH(c, k_mg_prolong<T>, gd, kBlock, 0, a.g, cl.g, a.comp, cl.comp, (const T*)cl.x, a.x);
-        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp, l == 0 ? (const int8_t*)c->pkind : (const int8_t*)nullptr, a.e, a.f0, a.f1, a.f2, a.invd, b,
-                  (const T*)a.x, a.t, (const T*)nullptr, (double*)nullptr);
+        LS_TRY(smooth(l, b, (const T*)a.x, a.t, (const T*)nullptr, (double*)nullptr, nullptr));
         T* out = (l == 0) ? z : a.x;
-        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp, l == 0 ? (const int8_t*)c->pkind : (const int8_t*)nullptr, a.e, a.f0, a.f1, a.f2, a.invd, b,
-                  (const T*)a.t, out, (l == 0) ? r : (const T*)nullptr,
-                  (l == 0) ? c->partials : (double*)nullptr);
-        if (l == 0 && nblocks_out) *nblocks_out = gd;
+        LS_TRY(smooth(l, b, (const T*)a.t, out, (l == 0) ? r : (const T*)nullptr,
+                      (l == 0) ? c->partials : (double*)nullptr, (l == 0) ? nblocks_out : nullptr));
     }
     return LS_OK;
 }

@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 
 #include "ls_internal.cuh"
 
@@ -561,6 +562,26 @@ __global__ void __launch_bounds__(kBlock) k_cg_apply(Grid g, const int8_t* __res
     block_sum_store<1>(acc, partials);
 }
 
+// k_cg_apply on pairs of cells (FP32, K even, padded finest-level arrays)
+__global__ void __launch_bounds__(kBlock) k_cg_apply0_pair(int N2, int JK2, int K2, const int8_t* __restrict__ kind,
+                                                           const float* __restrict__ p, const float* __restrict__ e,
+                                                           const float* __restrict__ w0, const float* __restrict__ w1,
+                                                           const float* __restrict__ w2, float* __restrict__ q,
+                                                           double* __restrict__ partials) {
+    float a = 0.f;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N2; t += gridDim.x * blockDim.x) {
+        const char2 kd = reinterpret_cast<const char2*>(kind)[t];
+        const bool l0 = kd.x == 2, l1 = kd.y == 2;
+        if (!l0 && !l1) continue;
+        const float2 qv = m0_apply_pair(t, JK2, K2, e, w0, w1, w2, p);
+        const float2 pv = reinterpret_cast<const float2*>(p)[t];
+        if (l0) { q[2 * t] = qv.x; a += pv.x * qv.x; }
+        if (l1) { q[2 * t + 1] = qv.y; a += pv.y * qv.y; }
+    }
+    double acc[1] = {(double)a};
+    block_sum_store<1>(acc, partials);
+}
+
 // x += a p, r -= a q with a = (r,z)/(p,q) (0 when (p,q) <= 0)
 template <typename T>
 __global__ void k_cg_update(Grid g, const int8_t* __restrict__ kind, const double* __restrict__ scal,
@@ -621,16 +642,9 @@ static ls_status inner_alloc(ls_ctx* c) {
     if (c->inner_is64 == is64) return LS_OK;
     void** arrs[] = {&c->ie, &c->iface[0], &c->iface[1], &c->iface[2], &c->iinvd, &c->inner[0],
                      &c->inner[1], &c->inner[2], &c->inner[3], &c->inner[4]};
-    const size_t old_bytes = (c->inner_is64 == 1 ? 8 : 4) * (size_t)c->g.N;
-    for (void** q : arrs) {
-        if (*q) { cudaFree(*q); c->device_bytes -= old_bytes; }
-        *q = nullptr;
-    }
+    for (int q = 0; q < 10; ++q) l0_free(c, q, arrs[q]);
     c->inner_is64 = -1;
-    for (void** q : arrs) {
-        LS_TRY(dalloc(c, q, sizeof(T) * (size_t)c->g.N));
-        LS_CUDA(c, cudaMemsetAsync(*q, 0, sizeof(T) * (size_t)c->g.N, c->stream));
-    }
+    for (int q = 0; q < 10; ++q) LS_TRY(l0_alloc(c, q, sizeof(T), arrs[q]));
     c->inner_is64 = is64;
     return LS_OK;
 }
@@ -652,6 +666,7 @@ static ls_status inner_pcg(ls_ctx* c, bool use_mg, double tol, int max_it, int* 
     const T* w2 = (const T*)c->iface[2];
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
+    const int pgrid = grid_for(c, g.N / 2);
     auto precondition = [&](int slot) -> ls_status {
         if (use_mg) {
             int nb = 0;
@@ -677,12 +692,17 @@ static ls_status inner_pcg(ls_ctx* c, bool use_mg, double tol, int max_it, int* 
     for (int it = 0; it < max_it; ++it) {
         {
             Timed tm(c, LS_T_CG_APPLY);
-            LS_LAUNCH(c, k_cg_apply<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const T*)p, e, w0, w1, w2,
-                      q, c->partials);
+            if (std::is_same<T, float>::value && g.K % 2 == 0)
+                LS_LAUNCH(c, k_cg_apply0_pair, pgrid, kBlock, 0, (int)(g.N / 2), (int)(g.JK / 2), g.K / 2,
+                          (const int8_t*)c->pkind, (const float*)p, (const float*)e, (const float*)w0,
+                          (const float*)w1, (const float*)w2, (float*)q, c->partials);
+            else
+                LS_LAUNCH(c, k_cg_apply<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const T*)p, e, w0, w1,
+                          w2, q, c->partials);
             // p in, excess and three own face links, q out
             if (c->timing) c->timer_bytes[LS_T_CG_APPLY] += (double)g.N * 6.0 * sizeof(T);
         }
-        LS_TRY(finalize_sum(c, grid, 1, SP_PQ));
+        LS_TRY(finalize_sum(c, (std::is_same<T, float>::value && g.K % 2 == 0) ? pgrid : grid, 1, SP_PQ));
         LS_LAUNCH(c, k_cg_update<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const double*)c->scal,
                   (const T*)p, (const T*)q, x, r);
         LS_TRY(precondition(SP_RZN));
