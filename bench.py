@@ -57,10 +57,19 @@ def make_geometry(shape):
     return lab, seed
 
 
+# Solver tolerances of the workload: transport and saturation at the reference's own KSP
+# default (rtol 1e-6, src/Simulation.cpp:156 -- the tolerance of the CPU baseline's
+# reference-algorithm mode too), the pressure at the FP64 relative residual 1e-8 of the
+# second metric.
+CONC_RTOL = 1e-6
+PRESS_RTOL = 1e-8
+
+
 def params(solver):
     from leachingsim_gb300._abi import PRESS_FP64, PRESS_JACOBI64, PRESS_MIXED, default_params
     s = {"mixed": PRESS_MIXED, "fp64": PRESS_FP64, "jacobi64": PRESS_JACOBI64}[solver]
-    return default_params(c_sat=1.0, D=1.0, kreac=1.0, press_solver=s)
+    return default_params(c_sat=1.0, D=1.0, kreac=1.0, press_solver=s, conc_rtol=CONC_RTOL,
+                          sat_rtol=CONC_RTOL, press_rtol=PRESS_RTOL)
 
 
 # ---------------------------------------------------------------------------
@@ -297,7 +306,8 @@ def gpu_arm(args, ws, rank, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
         "config": {"workload": "338x338x283 uint8 GRF geometry (porosity 0.25, corr 6, 15% mineral, "
-                               "Air inlet), dt 1, tmax 50, nout 10, D 1, kreac 1, csat 1",
+                               "Air inlet), dt 1, tmax 50, nout 10, D 1, kreac 1, csat 1, transport rtol 1e-6 "
+                               "(the reference's KSP default), pressure rtol 1e-8",
                    "shape_ijk": list(shape), "seed": seed, "press_solver": args.solver,
                    "parallelism": f"replicas{ws}", "l2": "working set > L2 (state %.1f GB)" % (mem / 1e9)},
         "wall_ms_per_step": round(wall * 1e3 / args.steps, 3),
@@ -359,7 +369,8 @@ def reference_arm(args, ws, rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
         "config": {"workload": "338x338x283 uint8 GRF geometry (porosity 0.25, corr 6, 15% mineral, "
-                               "Air inlet), dt 1, tmax 50, nout 10, D 1, kreac 1, csat 1",
+                               "Air inlet), dt 1, tmax 50, nout 10, D 1, kreac 1, csat 1, transport rtol 1e-6 "
+                               "(the reference's KSP default), pressure rtol 1e-8",
                    "shape_ijk": list(SHAPE), "parallelism": "host cores"},
         "cpu_baseline": cpu,
         "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

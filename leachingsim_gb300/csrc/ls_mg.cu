@@ -313,6 +313,50 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth0_pair(int N2, int JK2, int
     }
 }
 
+// Finest-level residual b - M x of kind-2 cells on pairs (FP32, K even, padded arrays), for
+// the restriction: each fine residual is formed once, by a coalesced fine-cell pass.
+__global__ void __launch_bounds__(kBlock) k_mg_resid0_pair(int N2, int JK2, int K2, const int8_t* __restrict__ kind,
+                                                           const float* __restrict__ e, const float* __restrict__ f0,
+                                                           const float* __restrict__ f1, const float* __restrict__ f2,
+                                                           const float* __restrict__ b, const float* __restrict__ x,
+                                                           float* __restrict__ res) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N2; t += gridDim.x * blockDim.x) {
+        const char2 kd = reinterpret_cast<const char2*>(kind)[t];
+        const bool l0 = kd.x == 2, l1 = kd.y == 2;
+        if (!l0 && !l1) continue;
+        const float2 m = m0_apply_pair(t, JK2, K2, e, f0, f1, f2, x);
+        const float2 bv = reinterpret_cast<const float2*>(b)[t];
+        if (l0) res[2 * t] = bv.x - m.x;
+        if (l1) res[2 * t + 1] = bv.y - m.y;
+    }
+}
+
+// coarse right-hand side from stored fine residuals: b_c(R) = sum over owned members, in
+// the child order of k_mg_restrict
+template <typename T>
+__global__ void k_mg_restrict_gather(Grid f, Grid cg, const int* __restrict__ fcomp, const int* __restrict__ ccomp,
+                                     const T* __restrict__ res, T* __restrict__ cb) {
+    for (long long R = blockIdx.x * (long long)blockDim.x + threadIdx.x; R < cg.N;
+         R += (long long)gridDim.x * blockDim.x) {
+        int I, J, K;
+        decode(cg, R, I, J, K);
+        const int own = ccomp[R];
+        T acc = (T)0;
+        if (own >= 0) {
+            for (int a = 0; a < 2; ++a)
+                for (int b = 0; b < 2; ++b)
+                    for (int c = 0; c < 2; ++c) {
+                        int i = 2 * I + a, j = 2 * J + b, k = 2 * K + c;
+                        if (i >= f.I || j >= f.J || k >= f.K) continue;
+                        long long fr = lidx(f, i, j, k);
+                        if (fcomp[fr] != own) continue;
+                        acc += res[fr];
+                    }
+        }
+        cb[R] = acc;
+    }
+}
+
 // coarse right-hand side: b_c(R) = sum over owned members of (b - M x)
 template <typename T>
 __global__ void k_mg_restrict(Grid f, Grid cg, const int* __restrict__ fcomp, const int* __restrict__ ccomp,
@@ -547,8 +591,18 @@ ls_status mg_apply(ls_ctx* c, const T* r, T* z, int* nblocks_out) {
         const T* b = (l == 0) ? r : a.b;
         LS_TRY(smooth(l, b, (const T*)nullptr, a.t, (const T*)nullptr, (double*)nullptr, nullptr));
         LS_TRY(smooth(l, b, (const T*)a.t, a.x, (const T*)nullptr, (double*)nullptr, nullptr));
-        LS_LAUNCH(c, k_mg_restrict<T>, grid_for(c, cl.g.N), kBlock, 0, a.g, cl.g, a.comp, cl.comp, a.e, a.f0,
-                  a.f1, a.f2, b, (const T*)a.x, cl.b);
+        if (l == 0 && pair0) {
+            // residual into the free ping-pong buffer, then the per-block sums
+            const int N2 = (int)(a.g.N / 2);
+            LS_LAUNCH(c, k_mg_resid0_pair, grid_for(c, N2), kBlock, 0, N2, (int)(a.g.JK / 2), a.g.K / 2,
+                      (const int8_t*)c->pkind, (const float*)a.e, (const float*)a.f0, (const float*)a.f1,
+                      (const float*)a.f2, (const float*)b, (const float*)a.x, (float*)a.t);
+            LS_LAUNCH(c, k_mg_restrict_gather<T>, grid_for(c, cl.g.N), kBlock, 0, a.g, cl.g, a.comp, cl.comp,
+                      (const T*)a.t, cl.b);
+        } else {
+            LS_LAUNCH(c, k_mg_restrict<T>, grid_for(c, cl.g.N), kBlock, 0, a.g, cl.g, a.comp, cl.comp, a.e, a.f0,
+                      a.f1, a.f2, b, (const T*)a.x, cl.b);
+        }
     }
     {
         Lv& a = lv[L];
