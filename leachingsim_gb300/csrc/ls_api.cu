@@ -376,6 +376,8 @@ ls_status ls_destroy(ls_ctx* c) {
         void* lp[] = {lv.comp, lv.e, lv.face[0], lv.face[1], lv.face[2], lv.invd, lv.x, lv.b, lv.t};
         for (void* q : lp)
             if (q) cudaFree(q);
+        for (void* q : lv.kv)
+            if (q) cudaFree(q);
     }
     if (c->h_scal) cudaFreeHost(c->h_scal);
     if (c->h_int) cudaFreeHost(c->h_int);

@@ -307,6 +307,7 @@ struct ls_ctx {
         void* x;            // T
         void* b;            // T
         void* t;            // T
+        void* kv[7];        // K-cycle vectors on this level (rr, za, zb, pd, q0, q1, e), T, or null
     };
     std::vector<MGLevel> mg;
     void* mg0_x;

@@ -21,6 +21,7 @@
 //     number of Jacobi sweeps by one CTA on the coarsest level, so the cycle is a symmetric
 //     operator usable inside CG.
 #include <algorithm>
+#include <functional>
 #include <type_traits>
 #include <cstdio>
 
@@ -33,6 +34,8 @@ constexpr double kOmega = 2.0 / 3.0;
 constexpr int kCoarsestCells = 512;
 constexpr int kCoarseSweeps = 48;
 constexpr double kProlongScale = 1.8;
+constexpr int kKLevels = 2;   // levels 1..kKLevels take a K-cycle coarse correction
+constexpr int kKSlot0 = 32;   // device scalar slots of the K-cycle FCG (5 per level)
 constexpr int kUnionSpin = 1 << 20;  // bound on the union-find retry loop
 
 __device__ __forceinline__ long long lidx(const Grid& g, int i, int j, int k) {
@@ -84,14 +87,28 @@ __global__ void k_level_invd(Grid g, const int* __restrict__ comp, const int8_t*
 // strong components (union-find with path halving; ids are voxel indices, the root is the
 // smallest voxel of the component)
 
+// find with path halving (hooking): each store points a non-root at one of its ancestors;
+// loads bypass L1, which is not coherent across SMs, so roots hooked elsewhere are seen
 __device__ __forceinline__ int cc_find(int* parent, int x) {
-    int p = parent[x];
+    int p = __ldcg(parent + x);
     int guard = 0;
     while (p != x && guard++ < kUnionSpin) {
-        int gp = parent[p];
-        parent[x] = gp;  // path halving; benign race
+        int gp = __ldcg(parent + p);
+        parent[x] = gp;
         x = p;
         p = gp;
+    }
+    return x;
+}
+
+// read-only find (compression): a path-halving store from a stale parent value could
+// otherwise overwrite a cell's final root with an intermediate ancestor
+__device__ __forceinline__ int cc_find_ro(const int* parent, int x) {
+    int p = __ldcg(parent + x);
+    int guard = 0;
+    while (p != x && guard++ < kUnionSpin) {
+        x = p;
+        p = __ldcg(parent + x);
     }
     return x;
 }
@@ -135,7 +152,7 @@ __global__ void k_cc_compress(Grid g, int* parent) {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
         if (parent[r] < 0) continue;
-        parent[r] = cc_find(parent, (int)r);
+        parent[r] = cc_find_ro(parent, (int)r);
     }
 }
 
@@ -248,8 +265,8 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth(Grid g, const int* __restr
                                                       const T* __restrict__ f2, const T* __restrict__ invd,
                                                       const T* __restrict__ b, const T* __restrict__ x,
                                                       T* __restrict__ xo, const T* __restrict__ dotv,
-                                                      double* __restrict__ partials) {
-    T acc = (T)0;
+                                                      const T* __restrict__ dotv2, double* __restrict__ partials) {
+    T acc = (T)0, acc2 = (T)0;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
         const bool live = kind0 ? kind0[r] == 2 : comp[r] >= 0;
@@ -266,10 +283,11 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth(Grid g, const int* __restr
         }
         xo[r] = out;
         if (dotv) acc += dotv[r] * out;
+        if (dotv2) acc2 += dotv2[r] * out;
     }
     if (dotv) {
-        double a[1] = {(double)acc};
-        block_sum_store<1>(a, partials);
+        double a[2] = {(double)acc, (double)acc2};
+        block_sum_store<2>(a, partials);
     }
 }
 
@@ -282,8 +300,9 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth0_pair(int N2, int JK2, int
                                                             const float* __restrict__ invd, const float* __restrict__ b,
                                                             const float* __restrict__ x, float* __restrict__ xo,
                                                             const float* __restrict__ dotv,
+                                                            const float* __restrict__ dotv2,
                                                             double* __restrict__ partials) {
-    float acc = 0.f;
+    float acc = 0.f, acc2 = 0.f;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N2; t += gridDim.x * blockDim.x) {
         const char2 kd = reinterpret_cast<const char2*>(kind)[t];
         const bool l0 = kd.x == 2, l1 = kd.y == 2;
@@ -306,10 +325,14 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth0_pair(int N2, int JK2, int
             if (l0) acc += dotv[2 * t] * o0;
             if (l1) acc += dotv[2 * t + 1] * o1;
         }
+        if (dotv2) {
+            if (l0) acc2 += dotv2[2 * t] * o0;
+            if (l1) acc2 += dotv2[2 * t + 1] * o1;
+        }
     }
     if (dotv) {
-        double a[1] = {(double)acc};
-        block_sum_store<1>(a, partials);
+        double a[2] = {(double)acc, (double)acc2};
+        block_sum_store<2>(a, partials);
     }
 }
 
@@ -389,7 +412,7 @@ __global__ void k_mg_restrict(Grid f, Grid cg, const int* __restrict__ fcomp, co
 // PCG iterations on these pore-space operators (33 instead of 71 on a 96^3 porosity-0.25 field).
 template <typename T>
 __global__ void k_mg_prolong(Grid f, Grid cg, const int* __restrict__ fcomp, const int* __restrict__ ccomp,
-                             const T* __restrict__ cx, T* __restrict__ fx) {
+                             const T* __restrict__ cx, T* __restrict__ fx, T scale) {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < f.N;
          r += (long long)gridDim.x * blockDim.x) {
         int id = fcomp[r];
@@ -397,8 +420,70 @@ __global__ void k_mg_prolong(Grid f, Grid cg, const int* __restrict__ fcomp, con
         int i, j, k;
         decode(f, r, i, j, k);
         long long R = lidx(cg, i >> 1, j >> 1, k >> 1);
-        if (ccomp[R] == id) fx[r] += (T)kProlongScale * cx[R];
+        if (ccomp[R] == id) fx[r] += scale * cx[R];
     }
+}
+
+// ---------------------------------------------------------------------------
+// K-cycle (Notay-Vassilevski): on the levels 1..kKLevels the coarse correction is two
+// flexible-CG iterations on that level, preconditioned by the cycle from that level down,
+// instead of one cycle. The scalars of each level's FCG live on the device (slots kKSlot0 +
+// 5 (level - 1) + {pq0, prr0, zq0, pq1, prr1}), so no host synchronisation is needed.
+
+// q = M pd and the partial dots (pd, q), (pd, rr) over member cells
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_kc_apply(Grid g, const int* __restrict__ comp, const T* __restrict__ e,
+                                                     const T* __restrict__ f0, const T* __restrict__ f1,
+                                                     const T* __restrict__ f2, const T* __restrict__ pd,
+                                                     const T* __restrict__ rr, T* __restrict__ q,
+                                                     double* __restrict__ partials) {
+    T a0 = (T)0, a1 = (T)0;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        if (comp[r] < 0) continue;
+        int i, j, k;
+        decode(g, r, i, j, k);
+        const T qv = m_apply(g, r, i, j, k, e, f0, f1, f2, pd);
+        q[r] = qv;
+        a0 += pd[r] * qv;
+        a1 += pd[r] * rr[r];
+    }
+    double a[2] = {(double)a0, (double)a1};
+    block_sum_store<2>(a, partials);
+}
+
+// first iteration: e = alpha pd, rr -= alpha q with alpha = (pd, rr) / (pd, q)
+template <typename T>
+__global__ void k_kc_first(Grid g, const int* __restrict__ comp, const double* __restrict__ s,
+                           const T* __restrict__ pd, const T* __restrict__ q, T* __restrict__ e,
+                           T* __restrict__ rr) {
+    const T a = (T)((s[0] > 0.0) ? s[1] / s[0] : 0.0);
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        if (comp[r] < 0) continue;
+        e[r] = a * pd[r];
+        rr[r] -= a * q[r];
+    }
+}
+
+// second direction: pd1 = z - ((z, q0) / (pd0, q0)) pd0
+template <typename T>
+__global__ void k_kc_dir(Grid g, const int* __restrict__ comp, const double* __restrict__ s,
+                         const T* __restrict__ z, const T* __restrict__ pd0, T* __restrict__ pd1) {
+    const T b = (T)((s[0] > 0.0) ? -s[2] / s[0] : 0.0);
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x)
+        if (comp[r] >= 0) pd1[r] = z[r] + b * pd0[r];
+}
+
+// second iteration: e += alpha1 pd1, alpha1 = (pd1, rr) / (pd1, q1)
+template <typename T>
+__global__ void k_kc_second(Grid g, const int* __restrict__ comp, const double* __restrict__ s,
+                            const T* __restrict__ pd1, T* __restrict__ e) {
+    const T a = (T)((s[3] > 0.0) ? s[4] / s[3] : 0.0);
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x)
+        if (comp[r] >= 0) e[r] += a * pd1[r];
 }
 
 // coarsest level: a fixed number of damped Jacobi sweeps from zero by one CTA
@@ -445,6 +530,8 @@ void mg_free(ls_ctx* c) {
         void* lp[] = {lv.comp, lv.e, lv.face[0], lv.face[1], lv.face[2], lv.invd, lv.x, lv.b, lv.t};
         for (void* q : lp)
             if (q) cudaFree(q);
+        for (void* q : lv.kv)
+            if (q) cudaFree(q);
     }
     c->mg.clear();
     l0_free(c, 10, &c->mg0_x);
@@ -475,6 +562,14 @@ static ls_status mg_alloc(ls_ctx* c) {
         }
         c->mg.push_back(lv);
         g = cg;
+    }
+    // K-cycle vectors on the levels 1..kKLevels that have a coarser level below them
+    for (size_t m = 1; m <= (size_t)kKLevels && m < c->mg.size(); ++m) {
+        auto& lv = c->mg[m - 1];
+        for (void*& q : lv.kv) {
+            LS_TRY(dalloc(c, &q, sizeof(T) * (size_t)lv.g.N));
+            LS_CUDA(c, cudaMemsetAsync(q, 0, sizeof(T) * (size_t)lv.g.N, c->stream));
+        }
     }
     c->mg_is64 = is64;
     return LS_OK;
@@ -538,14 +633,17 @@ ls_status mg_clear(ls_ctx* c) {
         LS_CUDA(c, cudaMemsetAsync(lv.x, 0, b, c->stream));
         LS_CUDA(c, cudaMemsetAsync(lv.b, 0, b, c->stream));
         LS_CUDA(c, cudaMemsetAsync(lv.t, 0, b, c->stream));
+        for (void* q : lv.kv)
+            if (q) LS_CUDA(c, cudaMemsetAsync(q, 0, b, c->stream));
     }
     return LS_OK;
 }
 
-// z = B r (one V-cycle); the per-block partials of (r, z) are left in c->partials and
-// their count in *nblocks_out.
+// z = B r: one K-cycle (levels 1..kKLevels take the two-iteration FCG coarse correction,
+// deeper levels a plain V-cycle). The per-block partials of (r, z) and (dotv2, z) are left in
+// c->partials (two values per block, dotv2 may be null) and their count in *nblocks_out.
 template <typename T>
-ls_status mg_apply(ls_ctx* c, const T* r, T* z, int* nblocks_out) {
+ls_status mg_apply(ls_ctx* c, const T* r, T* z, const T* dotv2, int* nblocks_out) {
     const size_t L = c->mg.size();  // coarse levels
     if (L == 0) return set_error(c, LS_BAD_ARG, "multigrid hierarchy missing");
     struct Lv {
@@ -553,44 +651,75 @@ ls_status mg_apply(ls_ctx* c, const T* r, T* z, int* nblocks_out) {
         const int* comp;
         const T *e, *f0, *f1, *f2, *invd;
         T *x, *b, *t;
+        T* kv[7];
     };
     std::vector<Lv> lv(L + 1);
     lv[0] = {c->g, c->comp, (const T*)c->ie, (const T*)c->iface[0], (const T*)c->iface[1], (const T*)c->iface[2],
-             (const T*)c->iinvd, (T*)c->mg0_x, nullptr, (T*)c->mg0_t};
+             (const T*)c->iinvd, (T*)c->mg0_x, nullptr, (T*)c->mg0_t, {}};
     for (size_t l = 0; l < L; ++l) {
         auto& m = c->mg[l];
         lv[l + 1] = {m.g, m.comp, (const T*)m.e, (const T*)m.face[0], (const T*)m.face[1], (const T*)m.face[2],
-                     (const T*)m.invd, (T*)m.x, (T*)m.b, (T*)m.t};
+                     (const T*)m.invd, (T*)m.x, (T*)m.b, (T*)m.t, {}};
+        for (int q = 0; q < 7; ++q) lv[l + 1].kv[q] = (T*)m.kv[q];
     }
     // one damped-Jacobi sweep on level l (paired finest-level kernel for FP32 and even K)
     const bool pair0 = std::is_same<T, float>::value && (c->g.K % 2 == 0);
-    auto smooth = [&](size_t l, const T* b, const T* x, T* xo, const T* dotv, double* partials,
-                      int* nb) -> ls_status {
+    auto smooth = [&](size_t l, const T* b, const T* x, T* xo, const T* dv, const T* dv2, int* nb) -> ls_status {
         Lv& a = lv[l];
+        double* partials = dv ? c->partials : (double*)nullptr;
         if (l == 0 && pair0) {
             const int N2 = (int)(a.g.N / 2);
             const int gd = grid_for(c, N2);
             LS_LAUNCH(c, k_mg_smooth0_pair, gd, kBlock, 0, N2, (int)(a.g.JK / 2), a.g.K / 2,
                       (const int8_t*)c->pkind, (const float*)a.e, (const float*)a.f0, (const float*)a.f1,
                       (const float*)a.f2, (const float*)a.invd, (const float*)b, (const float*)x, (float*)xo,
-                      (const float*)dotv, partials);
+                      (const float*)dv, (const float*)dv2, partials);
             if (nb) *nb = gd;
             return LS_OK;
         }
         const int gd = grid_for(c, a.g.N);
         LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp,
                   l == 0 ? (const int8_t*)c->pkind : (const int8_t*)nullptr, a.e, a.f0, a.f1, a.f2, a.invd, b, x,
-                  xo, dotv, partials);
+                  xo, dv, dv2, partials);
         if (nb) *nb = gd;
         return LS_OK;
     };
-    // descending leg
-    for (size_t l = 0; l < L; ++l) {
+    // cycle(l, b, out): out = B_l b; with dv non-null the final sweep leaves the partial dots
+    // (dv, out), (dv2, out) and their block count in *nb. Level l's x and t are its scratch.
+    std::function<ls_status(size_t, const T*, T*, const T*, const T*, int*)> cycle;
+    // kfcg(m): two FCG iterations on level m for M_m e = b_m (m's b), result in kv[6]
+    auto kfcg = [&](size_t m) -> ls_status {
+        Lv& a = lv[m];
+        T *rr = a.kv[0], *za = a.kv[1], *zb = a.kv[2], *pd = a.kv[3], *q0 = a.kv[4], *q1 = a.kv[5], *e = a.kv[6];
+        const int slot = kKSlot0 + 5 * ((int)m - 1);
+        const double* s = c->scal + slot;
+        const int gd = grid_for(c, a.g.N);
+        LS_CUDA(c, cudaMemcpyAsync(rr, a.b, sizeof(T) * (size_t)a.g.N, cudaMemcpyDeviceToDevice, c->stream));
+        LS_TRY(cycle(m, (const T*)rr, za, nullptr, nullptr, nullptr));
+        LS_LAUNCH(c, k_kc_apply<T>, gd, kBlock, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, (const T*)za,
+                  (const T*)rr, q0, c->partials);
+        LS_TRY(finalize_sum(c, gd, 2, slot));  // (za, q0), (za, rr)
+        LS_LAUNCH(c, k_kc_first<T>, gd, kBlock, 0, a.g, a.comp, s, (const T*)za, (const T*)q0, e, rr);
+        int nb = 0;
+        LS_TRY(cycle(m, (const T*)rr, zb, (const T*)q0, nullptr, &nb));
+        LS_TRY(finalize_sum(c, nb, 2, slot + 2));  // (zb, q0)
+        LS_LAUNCH(c, k_kc_dir<T>, gd, kBlock, 0, a.g, a.comp, s, (const T*)zb, (const T*)za, pd);
+        LS_LAUNCH(c, k_kc_apply<T>, gd, kBlock, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, (const T*)pd,
+                  (const T*)rr, q1, c->partials);
+        LS_TRY(finalize_sum(c, gd, 2, slot + 3));  // (pd, q1), (pd, rr)
+        LS_LAUNCH(c, k_kc_second<T>, gd, kBlock, 0, a.g, a.comp, s, (const T*)pd, e);
+        return LS_OK;
+    };
+    cycle = [&](size_t l, const T* b, T* out, const T* dv, const T* dv2, int* nb) -> ls_status {
         Lv& a = lv[l];
+        if (l == L) {
+            LS_LAUNCH(c, k_mg_coarsest<T>, 1, 1024, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, a.invd, b, out, a.t,
+                      kCoarseSweeps);
+            return LS_OK;
+        }
         Lv& cl = lv[l + 1];
-        const T* b = (l == 0) ? r : a.b;
-        LS_TRY(smooth(l, b, (const T*)nullptr, a.t, (const T*)nullptr, (double*)nullptr, nullptr));
-        LS_TRY(smooth(l, b, (const T*)a.t, a.x, (const T*)nullptr, (double*)nullptr, nullptr));
+        LS_TRY(smooth(l, b, (const T*)nullptr, a.t, nullptr, nullptr, nullptr));
+        LS_TRY(smooth(l, b, (const T*)a.t, a.x, nullptr, nullptr, nullptr));
         if (l == 0 && pair0) {
             // residual into the free ping-pong buffer, then the per-block sums
             const int N2 = (int)(a.g.N / 2);
@@ -603,25 +732,23 @@ ls_status mg_apply(ls_ctx* c, const T* r, T* z, int* nblocks_out) {
             LS_LAUNCH(c, k_mg_restrict<T>, grid_for(c, cl.g.N), kBlock, 0, a.g, cl.g, a.comp, cl.comp, a.e, a.f0,
                       a.f1, a.f2, b, (const T*)a.x, cl.b);
         }
-    }
-    {
-        Lv& a = lv[L];
-        LS_LAUNCH(c, k_mg_coarsest<T>, 1, 1024, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, a.invd,
-                  (const T*)a.b, a.x, a.t, kCoarseSweeps);
-    }
-    // ascending leg
-    for (size_t l = L; l-- > 0;) {
-        Lv& a = lv[l];
-        Lv& cl = lv[l + 1];
-        const T* b = (l == 0) ? r : a.b;
-        const int gd = grid_for(c, a.g.N);
-        LS_LAUNCH(c, k_mg_prolong<T>, gd, kBlock, 0, a.g, cl.g, a.comp, cl.comp, (const T*)cl.x, a.x);
-        LS_TRY(smooth(l, b, (const T*)a.x, a.t, (const T*)nullptr, (double*)nullptr, nullptr));
-        T* out = (l == 0) ? z : a.x;
-        LS_TRY(smooth(l, b, (const T*)a.t, out, (l == 0) ? r : (const T*)nullptr,
-                      (l == 0) ? c->partials : (double*)nullptr, (l == 0) ? nblocks_out : nullptr));
-    }
-    return LS_OK;
+        const T* corr;
+        T scale;
+        if (l + 1 <= (size_t)kKLevels && l + 1 < L) {
+            LS_TRY(kfcg(l + 1));
+            corr = cl.kv[6];
+            scale = (T)1;  // the FCG steps carry the optimal scaling
+        } else {
+            LS_TRY(cycle(l + 1, (const T*)cl.b, cl.x, nullptr, nullptr, nullptr));
+            corr = cl.x;
+            scale = (T)kProlongScale;
+        }
+        LS_LAUNCH(c, k_mg_prolong<T>, grid_for(c, a.g.N), kBlock, 0, a.g, cl.g, a.comp, cl.comp, corr, a.x,
+                  scale);
+        LS_TRY(smooth(l, b, (const T*)a.x, a.t, nullptr, nullptr, nullptr));
+        return smooth(l, b, (const T*)a.t, out, dv, dv2, nb);
+    };
+    return cycle(0, r, z, r, dotv2, nblocks_out);
 }
 
 template ls_status inner_invd<float>(ls_ctx*);
@@ -630,7 +757,7 @@ template ls_status mg_setup<float>(ls_ctx*);
 template ls_status mg_setup<double>(ls_ctx*);
 template ls_status mg_clear<float>(ls_ctx*);
 template ls_status mg_clear<double>(ls_ctx*);
-template ls_status mg_apply<float>(ls_ctx*, const float*, float*, int*);
-template ls_status mg_apply<double>(ls_ctx*, const double*, double*, int*);
+template ls_status mg_apply<float>(ls_ctx*, const float*, float*, const float*, int*);
+template ls_status mg_apply<double>(ls_ctx*, const double*, double*, const double*, int*);
 
 }  // namespace ls

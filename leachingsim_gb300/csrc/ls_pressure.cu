@@ -34,7 +34,7 @@ ls_status mg_setup(ls_ctx* c);
 template <typename T>
 ls_status mg_clear(ls_ctx* c);
 template <typename T>
-ls_status mg_apply(ls_ctx* c, const T* r, T* z, int* nblocks_out);
+ls_status mg_apply(ls_ctx* c, const T* r, T* z, const T* dotv2, int* nblocks_out);
 template <typename T>
 ls_status inner_invd(ls_ctx* c);
 
@@ -48,9 +48,7 @@ enum {
     SP_RZ = 24,    // inner: (r, z)
     SP_PQ = 25,    // inner: (p, q)
     SP_RZN = 26,   // inner: new (r, z)
-    SP_RR = 27,    // inner: (r, r)
-    SP_RR0 = 28,
-    SP_RZ_OLD = 29
+    SP_ZQ = 27     // inner: (z_new, q), the flexible-CG direction term
 };
 
 // ---------------------------------------------------------------------------
@@ -614,11 +612,13 @@ __global__ void __launch_bounds__(kBlock) k_cg_jacobi(Grid g, const T* __restric
     block_sum_store<1>(acc, partials);
 }
 
-// p = z + b p with b = (r,z)_new / (r,z)_old
+// p = z + b p with b = (r,z)_new / (r,z)_old (fixed preconditioner) or, for the flexible CG
+// that the K-cycle needs, b = -(z_new, q) / (p, q) (Notay's FCG(1))
 template <typename T>
 __global__ void k_cg_dir(Grid g, const int8_t* __restrict__ kind, const double* __restrict__ scal,
-                         const T* __restrict__ z, T* __restrict__ p) {
-    const T beta = (T)(scal[SP_RZN] / scal[SP_RZ]);
+                         const T* __restrict__ z, T* __restrict__ p, int flexible) {
+    const T beta = (T)(flexible ? ((scal[SP_PQ] > 0.0) ? -scal[SP_ZQ] / scal[SP_PQ] : 0.0)
+                                : scal[SP_RZN] / scal[SP_RZ]);
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x)
         if (kind[r] == 2) p[r] = z[r] + beta * p[r];
@@ -650,8 +650,9 @@ static ls_status inner_alloc(ls_ctx* c) {
 }
 
 // Inner PCG: solve sigma*M x = rhs (rhs in inner[1] on entry) until the preconditioned
-// residual (r, z) has dropped by tol^2, preconditioned by one multigrid V-cycle (use_mg)
-// or by Jacobi. Returns the iterations used in *its.
+// residual (r, z) has dropped by tol^2, preconditioned by one multigrid K-cycle (use_mg; the
+// cycle is not a fixed linear operator, so the directions follow the flexible CG) or by
+// Jacobi. Returns the iterations used in *its.
 template <typename T>
 static ls_status inner_pcg(ls_ctx* c, bool use_mg, double tol, int max_it, int* its,
                            double* rel_out) {
@@ -667,18 +668,19 @@ static ls_status inner_pcg(ls_ctx* c, bool use_mg, double tol, int max_it, int* 
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
     const int pgrid = grid_for(c, g.N / 2);
-    auto precondition = [&](int slot) -> ls_status {
+    // z = B r and (r, z) into slot; with the multigrid, also (qv, z) into slot + 1
+    auto precondition = [&](int slot, const T* qv) -> ls_status {
         if (use_mg) {
             int nb = 0;
-            LS_TRY(mg_apply<T>(c, (const T*)r, z, &nb));
-            return finalize_sum(c, nb, 1, slot);
+            LS_TRY(mg_apply<T>(c, (const T*)r, z, qv, &nb));
+            return finalize_sum(c, nb, 2, slot);
         }
         LS_LAUNCH(c, k_cg_jacobi<T>, grid, kBlock, 0, g, (const T*)c->iinvd, (const T*)r, z, c->partials);
         return finalize_sum(c, grid, 1, slot);
     };
     *its = 0;
     *rel_out = 0.0;
-    LS_TRY(precondition(SP_RZ));
+    LS_TRY(precondition(SP_RZ, nullptr));
     double rz0 = 0.0;
     LS_TRY(read_scalars(c, SP_RZ, 1, &rz0));
     if (rz0 != rz0) return set_error(c, LS_NONFINITE, "pressure: NaN in the inner right-hand side");
@@ -705,7 +707,7 @@ static ls_status inner_pcg(ls_ctx* c, bool use_mg, double tol, int max_it, int* 
         LS_TRY(finalize_sum(c, (std::is_same<T, float>::value && g.K % 2 == 0) ? pgrid : grid, 1, SP_PQ));
         LS_LAUNCH(c, k_cg_update<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const double*)c->scal,
                   (const T*)p, (const T*)q, x, r);
-        LS_TRY(precondition(SP_RZN));
+        LS_TRY(precondition(SP_RZN, (const T*)q));
         *its = it + 1;
         double sc[3];
         LS_TRY(read_scalars(c, SP_PQ, 2, sc));  // (p, q) and the new (r, z)
@@ -714,7 +716,7 @@ static ls_status inner_pcg(ls_ctx* c, bool use_mg, double tol, int max_it, int* 
         if (rz != rz) return set_error(c, LS_NONFINITE, "pressure: NaN in inner PCG");
         if (rz <= target || !(pq > 0.0) || rz < 0.0) break;
         LS_LAUNCH(c, k_cg_dir<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const double*)c->scal,
-                  (const T*)z, p);
+                  (const T*)z, p, use_mg ? 1 : 0);
         LS_LAUNCH(c, k_set_scalar, 1, 1, 0, c->scal, SP_RZ, SP_RZN);
     }
     *rel_out = sqrt(std::max(rz, 0.0) / rz0);
