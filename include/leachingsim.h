@@ -251,6 +251,32 @@ ls_status ls_pressure_rhs(ls_ctx* ctx, double* b_host);
 /* y = A x for the transport operator of src/Simulation.cpp:1129-1232 at time step dt. */
 ls_status ls_transport_apply(ls_ctx* ctx, double dt, const double* x_host, double* y_host);
 
+/* Geometry pre-processing of label images (host buffers, (z, y, x) order, no context; each
+   call allocates its device scratch on the current device and returns when done).
+   ls_geom_coarsen replaces coarsen_grid.py:20-62: 2x2x2 ranked priority voting (Sulphide >
+   Air > Pore > Rock) into ((I+1)/2, J/2, K/2), an odd I padded with one Air plane; J and K
+   must be even. ls_geom_clean replaces clean_micro_ct.py:33-114 in place: opening of the
+   Pore mask (6-neighbour erosion then dilation), 6-connected pore components, and every Pore
+   voxel outside the components reached from the ambient Air (mode 0, 'agglomerate': the
+   one-voxel dilation of the largest Air component) or from the x = 0 face (mode 1,
+   'core_sample') becomes Rock; *changed receives the number of such voxels.
+   ls_geom_fracture replaces micro_fracture.py:21-93 in place: from every Sulphide voxel with
+   no Pore face neighbour a centre line runs to its nearest Pore voxel (exact Euclidean
+   feature transform, ties as scipy.ndimage.distance_transform_edt), sampled at
+   ceil(distance) + 1 points as numpy.linspace + round; the Rock voxels on the lines, dilated
+   by the full 3x3x3 element, become Pore. *drilled receives their number, *encapsulated the
+   number of encapsulated Sulphide voxels; an image without Pore voxels is LS_BAD_ARG.
+   ls_geom_classify labels a uint16 grey-level image: out = labels[i], i the number of the
+   (ascending, at most 16) thresholds <= the grey value; labels has n_thresholds + 1 entries. */
+ls_status ls_geom_coarsen(int I, int J, int K, int label_bytes, const void* in_host, void* out_host);
+ls_status ls_geom_clean(int I, int J, int K, int label_bytes, void* labels_host, int mode,
+                        long long* changed);
+ls_status ls_geom_fracture(int I, int J, int K, int label_bytes, void* labels_host, long long* drilled,
+                           long long* encapsulated);
+ls_status ls_geom_classify(int I, int J, int K, const uint16_t* grey_host, int n_thresholds,
+                           const uint16_t* thresholds, const int* labels, int label_bytes,
+                           void* out_host);
+
 /* Per-kernel-class device timing (CUDA events on the context stream). */
 typedef enum ls_timer {
     LS_T_PROPS = 0,

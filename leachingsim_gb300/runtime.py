@@ -57,6 +57,11 @@ SYMBOLS = {
     "ls_pressure_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "ls_pressure_rhs": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ls_transport_apply": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]),
+    "ls_geom_coarsen": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
+    "ls_geom_clean": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p]),
+    "ls_geom_fracture": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ls_geom_classify": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                   C.c_int, C.c_void_p]),
     "ls_timing_enable": (C.c_int, [C.c_void_p, C.c_int]),
     "ls_timing_reset": (C.c_int, [C.c_void_p]),
     "ls_timing_get": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double),
@@ -95,6 +100,71 @@ class LsError(RuntimeError):
 
 def _p(a):
     return a.ctypes.data_as(C.c_void_p)
+
+
+_LABEL_DTYPES = {1: np.uint8, 2: np.uint16}
+
+
+def _geom_check(st, what):
+    if st != 0:
+        raise RuntimeError(f"{what} failed with status {st}")
+
+
+def geom_coarsen(labels):
+    """coarsen_grid.py on the GPU: 2x2x2 ranked priority voting (Sulphide > Air > Pore >
+    Rock); an odd slowest extent is padded with one Air plane."""
+    lab = np.ascontiguousarray(labels)
+    if lab.dtype not in (np.uint8, np.uint16) or lab.ndim != 3:
+        raise ValueError("labels must be a 3-D uint8 or uint16 array")
+    I, J, K = lab.shape
+    if J % 2 or K % 2:
+        raise ValueError("coarsening needs even y and x extents")
+    out = np.empty(((I + 1) // 2, J // 2, K // 2), dtype=lab.dtype)
+    _geom_check(load().ls_geom_coarsen(I, J, K, lab.itemsize, _p(lab), _p(out)), "ls_geom_coarsen")
+    return out
+
+
+def geom_clean(labels, mode="agglomerate"):
+    """clean_micro_ct.py on the GPU; returns (cleaned labels, number of Pore voxels turned to
+    Rock). mode: 'agglomerate' or 'core_sample'."""
+    modes = {"agglomerate": 0, "core_sample": 1}
+    if mode not in modes:
+        raise ValueError(f"mode must be one of {sorted(modes)}")
+    lab = np.array(labels, copy=True, order="C")
+    if lab.dtype not in (np.uint8, np.uint16) or lab.ndim != 3:
+        raise ValueError("labels must be a 3-D uint8 or uint16 array")
+    n = C.c_longlong(0)
+    _geom_check(load().ls_geom_clean(*lab.shape, lab.itemsize, _p(lab), modes[mode], C.byref(n)),
+                "ls_geom_clean")
+    return lab, int(n.value)
+
+
+def geom_fracture(labels):
+    """micro_fracture.py on the GPU; returns (labels after drilling, number of Rock voxels
+    turned to Pore, number of encapsulated Sulphide voxels)."""
+    lab = np.array(labels, copy=True, order="C")
+    if lab.dtype not in (np.uint8, np.uint16) or lab.ndim != 3:
+        raise ValueError("labels must be a 3-D uint8 or uint16 array")
+    n, ne = C.c_longlong(0), C.c_longlong(0)
+    _geom_check(load().ls_geom_fracture(*lab.shape, lab.itemsize, _p(lab), C.byref(n), C.byref(ne)),
+                "ls_geom_fracture")
+    return lab, int(n.value), int(ne.value)
+
+
+def geom_classify(grey, thresholds, labels, label_bytes=1):
+    """Threshold classification of a uint16 grey-level image on the GPU: label = labels[i],
+    i = the number of the ascending thresholds <= the grey value."""
+    g = np.ascontiguousarray(grey, dtype=np.uint16)
+    if g.ndim != 3:
+        raise ValueError("grey must be a 3-D array")
+    t = np.ascontiguousarray(thresholds, dtype=np.uint16)
+    lb = np.ascontiguousarray(labels, dtype=np.int32)
+    if lb.size != t.size + 1:
+        raise ValueError("labels needs one entry more than thresholds")
+    out = np.empty(g.shape, dtype=_LABEL_DTYPES[label_bytes])
+    _geom_check(load().ls_geom_classify(*g.shape, _p(g), t.size, _p(t) if t.size else None, _p(lb),
+                                        label_bytes, _p(out)), "ls_geom_classify")
+    return out
 
 
 class Context:
