@@ -86,13 +86,16 @@ __global__ void k_morph6(Dims d, const uint8_t* __restrict__ in, uint8_t* __rest
 
 // union-find over 6-connected mask voxels; the root of a component is its smallest voxel.
 // Hooking phase: find with path halving. Every store points a non-root at one of its
-// ancestors, so the races between threads are benign; loads bypass L1, which is not coherent
-// across SMs, so that a root hooked by another SM is seen on the retry.
+// ancestors, and a value read from a stale L1 line (L1 is not coherent across SMs) is a
+// former ancestor, so the races between threads are benign. A stale line can show a root
+// that another SM has hooked since: the CAS then fails, and the retry uses FRESH loads that
+// bypass L1.
+template <bool FRESH>
 __device__ __forceinline__ int gfind(int* parent, int x) {
-    int p = __ldcg(parent + x);
+    int p = FRESH ? __ldcg(parent + x) : parent[x];
     int guard = 0;
     while (p != x && guard++ < kGeoSpin) {
-        const int gp = __ldcg(parent + p);
+        const int gp = FRESH ? __ldcg(parent + p) : parent[p];
         parent[x] = gp;
         x = p;
         p = gp;
@@ -104,11 +107,11 @@ __device__ __forceinline__ int gfind(int* parent, int x) {
 // parent value could overwrite a voxel's final root with an intermediate ancestor after the
 // voxel's own thread had stored the root.
 __device__ __forceinline__ int gfind_ro(const int* parent, int x) {
-    int p = __ldcg(parent + x);
+    int p = parent[x];
     int guard = 0;
     while (p != x && guard++ < kGeoSpin) {
         x = p;
-        p = __ldcg(parent + x);
+        p = parent[x];
     }
     return x;
 }
@@ -132,7 +135,8 @@ __global__ void k_uf_hook(Dims d, const uint8_t* __restrict__ m, int* parent, in
             int a = (int)r, b = (int)(r + off[q]);
             int spins = 0;
             while (true) {
-                const int ra = gfind(parent, a), rb = gfind(parent, b);
+                const int ra = spins ? gfind<true>(parent, a) : gfind<false>(parent, a);
+                const int rb = spins ? gfind<true>(parent, b) : gfind<false>(parent, b);
                 if (ra == rb) break;
                 const int lo = ra < rb ? ra : rb, hi = ra < rb ? rb : ra;
                 if (atomicCAS(&parent[hi], hi, lo) == hi) break;

@@ -87,13 +87,16 @@ __global__ void k_level_invd(Grid g, const int* __restrict__ comp, const int8_t*
 // strong components (union-find with path halving; ids are voxel indices, the root is the
 // smallest voxel of the component)
 
-// find with path halving (hooking): each store points a non-root at one of its ancestors;
-// loads bypass L1, which is not coherent across SMs, so roots hooked elsewhere are seen
+// find with path halving (hooking). Each store points a non-root at one of its ancestors,
+// and a parent value read from a stale L1 line (L1 is not coherent across SMs) is a former
+// ancestor, so still an ancestor. A stale line can however show a root that another SM has
+// hooked since; the CAS then fails, and the retry reads with FRESH loads that bypass L1.
+template <bool FRESH>
 __device__ __forceinline__ int cc_find(int* parent, int x) {
-    int p = __ldcg(parent + x);
+    int p = FRESH ? __ldcg(parent + x) : parent[x];
     int guard = 0;
     while (p != x && guard++ < kUnionSpin) {
-        int gp = __ldcg(parent + p);
+        int gp = FRESH ? __ldcg(parent + p) : parent[p];
         parent[x] = gp;
         x = p;
         p = gp;
@@ -104,11 +107,11 @@ __device__ __forceinline__ int cc_find(int* parent, int x) {
 // read-only find (compression): a path-halving store from a stale parent value could
 // otherwise overwrite a cell's final root with an intermediate ancestor
 __device__ __forceinline__ int cc_find_ro(const int* parent, int x) {
-    int p = __ldcg(parent + x);
+    int p = parent[x];
     int guard = 0;
     while (p != x && guard++ < kUnionSpin) {
         x = p;
-        p = __ldcg(parent + x);
+        p = parent[x];
     }
     return x;
 }
@@ -138,7 +141,8 @@ __global__ void k_cc_hook(Grid g, const T* __restrict__ f0, const T* __restrict_
             int a = (int)r, b = (int)nb;
             int spins = 0;
             while (true) {
-                int ra = cc_find(parent, a), rb = cc_find(parent, b);
+                int ra = spins ? cc_find<true>(parent, a) : cc_find<false>(parent, a);
+                int rb = spins ? cc_find<true>(parent, b) : cc_find<false>(parent, b);
                 if (ra == rb) break;
                 int lo = ra < rb ? ra : rb, hi = ra < rb ? rb : ra;
                 if (atomicCAS(&parent[hi], hi, lo) == hi) break;

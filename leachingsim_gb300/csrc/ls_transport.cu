@@ -1098,7 +1098,9 @@ static ls_status mixed_solve(ls_ctx* c, const Rows<L>& rows, int nrhs, const dou
                 stagnant[q] = 0;
             }
             prev[q] = rel[q];
-            tol[q] = std::min(0.5, std::max(1e-5, 0.2 * rtol / std::max(rel[q], 1e-300)));
+            // inner tolerance: what reaches rtol from here (with a margin), floored at what
+            // the FP32 inner system still resolves (a relative 1e-6 is ~17 FP32 ulps)
+            tol[q] = std::min(0.5, std::max(1e-6, 0.2 * rtol / std::max(rel[q], 1e-300)));
             solve_mask |= 1 << q;
         }
         if (!solve_mask) break;
