@@ -277,6 +277,29 @@ ls_status ls_geom_classify(int I, int J, int K, const uint16_t* grey_host, int n
                            const uint16_t* thresholds, const int* labels, int label_bytes,
                            void* out_host);
 
+/* Learned pressure network (no counterpart in the reference): a U-shaped 3D convolutional
+   network (4 levels, 16-64 channels, 3x3x3 convolutions, BF16 weights and activations,
+   FP32 accumulation on the tensor cores) mapping three input fields (pore mask, normalised
+   log-permeability, boundary / previous pressure) on a D x H x W grid (multiples of 8) to
+   one output field. Field pointers are DEVICE pointers to D*H*W float32 values, (z, y, x)
+   order. Parameters are float32, per layer (W0a, W0b, W1, W2, W3, U2, U1, U0) the weights
+   [27][cout][cin] (tap = 9 (dz+1) + 3 (dy+1) + (dx+1)) then the biases [cout].
+   ls_lpnet_train_step runs forward, the masked mean-square loss of output vs target over
+   the mask_count voxels with mask 1, backward and (update != 0) one Adam step with rate lr;
+   the gradients stay readable through ls_lpnet_get_grads. */
+typedef struct ls_lpnet ls_lpnet;
+ls_status ls_lpnet_create(int D, int H, int W, int seed, ls_lpnet** net);
+ls_status ls_lpnet_destroy(ls_lpnet* net);
+const char* ls_lpnet_last_error(const ls_lpnet* net);
+long long ls_lpnet_param_count(const ls_lpnet* net);
+ls_status ls_lpnet_get_params(ls_lpnet* net, float* host, long long count);
+ls_status ls_lpnet_set_params(ls_lpnet* net, const float* host, long long count);
+ls_status ls_lpnet_get_grads(ls_lpnet* net, float* host, long long count);
+ls_status ls_lpnet_forward(ls_lpnet* net, const float* c0, const float* c1, const float* c2, float* out);
+ls_status ls_lpnet_train_step(ls_lpnet* net, const float* c0, const float* c1, const float* c2,
+                              const float* target, const float* mask, long long mask_count, float lr,
+                              int update, double* loss);
+
 /* Per-kernel-class device timing (CUDA events on the context stream). */
 typedef enum ls_timer {
     LS_T_PROPS = 0,

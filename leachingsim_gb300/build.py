@@ -23,7 +23,7 @@ CLI = os.path.join(HERE, "leachingsim")
 HOST_SOURCES = ["Simulation.cpp", "vtk_writer.cpp", "main.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["ls_api.cu", "ls_pointwise.cu", "ls_pressure.cu", "ls_mg.cu", "ls_transport.cu",
-           "ls_dissolve.cu", "ls_geometry.cu"]
+           "ls_dissolve.cu", "ls_geometry.cu", "ls_learned.cu"]
 
 
 def nvcc():

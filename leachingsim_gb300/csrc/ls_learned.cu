@@ -1,0 +1,705 @@
+// ls_learned.cu - the learned pressure network: a U-shaped 3D convolutional network (4
+// levels, 16-64 channels, BF16 weights and activations, FP32 accumulation) that maps a
+// pore mask, the log-permeability and a boundary / previous-pressure channel to a pressure
+// field. It is the warm start of the pressure solve; the plain multigrid solver judges
+// every start through the FP64 residual and finishes the solve.
+//
+// Kernels, all hand-written:
+//  * k_lp_conv: 3x3x3 convolution as an implicit GEMM on the tensor cores
+//    (mma.sync m16n8k16, BF16 x BF16 -> FP32): a warp computes 16 output voxels x all output
+//    channels; the K dimension runs over 27 taps x input channels in chunks of 16. The same
+//    kernel with flipped, transposed weights is the backward pass for the input gradient.
+//  * k_lp_conv_dw: the weight / bias gradient, staged through shared memory, FP32 FMA.
+//  * pooling, upsampling + skip addition and their backward passes, ReLU masking, the
+//    masked mean-square loss and Adam.
+//
+// Layout: activations (D, H, W, C) with the channels innermost (BF16), gradients the same in
+// FP32; weights [tap][cout][cin], tap = 9 (dz+1) + 3 (dy+1) + (dx+1). D, H and W are
+// multiples of 8 (three 2x poolings).
+#include <cuda_bf16.h>
+
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "ls_internal.cuh"
+
+namespace ls {
+
+typedef __nv_bfloat16 bf16;
+
+struct LpDims {
+    int D, H, W;
+    long long N;
+};
+
+namespace {
+
+__host__ __device__ inline LpDims lp_dims(int D, int H, int W) {
+    return LpDims{D, H, W, (long long)D * H * W};
+}
+
+__device__ __forceinline__ void lp_decode(const LpDims& d, long long r, int& z, int& y, int& x) {
+    const long long hw = (long long)d.H * d.W;
+    z = (int)(r / hw);
+    const long long rem = r - (long long)z * hw;
+    y = (int)(rem / d.W);
+    x = (int)(rem - (long long)y * d.W);
+}
+
+// D = A (16x16, row) x B (16x8, col) + D, BF16 inputs, FP32 accumulators
+__device__ __forceinline__ void mma_16816(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <typename T>
+__device__ __forceinline__ void store_pair(T* p, float a, float b);
+template <>
+__device__ __forceinline__ void store_pair<bf16>(bf16* p, float a, float b) {
+    *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(a, b);
+}
+template <>
+__device__ __forceinline__ void store_pair<float>(float* p, float a, float b) {
+    *reinterpret_cast<float2*>(p) = make_float2(a, b);
+}
+
+// out[v, co] = act(bias[co] + sum_tap sum_ci w[tap][co][ci] in[v + tap, ci]), zero padding.
+// Fragment layout of m16n8k16 (lane = 4 g + t): A rows g and g + 8, columns 2t, 2t + 1 and
+// 2t + 8, 2t + 9; B column g, rows 2t, 2t + 1 and 2t + 8, 2t + 9; C rows g, g + 8, columns
+// 2t, 2t + 1. Rows are voxels, A columns input channels, B columns output channels.
+template <int CIN, int COUT, bool RELU, typename OutT>
+__global__ void __launch_bounds__(128) k_lp_conv(LpDims d, const bf16* __restrict__ in, const bf16* __restrict__ w,
+                                                 const float* __restrict__ bias, OutT* __restrict__ out) {
+    static_assert(CIN % 16 == 0 && COUT % 8 == 0, "channel counts");
+    constexpr int NT = COUT / 8, KC = CIN / 16;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane >> 2, tg = lane & 3;
+    const long long ntiles = (d.N + 15) / 16;
+    const uint32_t* __restrict__ in32 = reinterpret_cast<const uint32_t*>(in);
+    const uint32_t* __restrict__ w32 = reinterpret_cast<const uint32_t*>(w);
+    for (long long tile = blockIdx.x * 4LL + warp; tile < ntiles; tile += gridDim.x * 4LL) {
+        const long long r0 = tile * 16 + g, r1 = r0 + 8;
+        const bool ok0 = r0 < d.N, ok1 = r1 < d.N;
+        int z0 = 0, y0 = 0, x0 = 0, z1 = 0, y1 = 0, x1 = 0;
+        if (ok0) lp_decode(d, r0, z0, y0, x0);
+        if (ok1) lp_decode(d, r1, z1, y1, x1);
+        float acc[NT][4];
+#pragma unroll
+        for (int n = 0; n < NT; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
+        for (int t = 0; t < 27; ++t) {
+            const int dz = t / 9 - 1, dy = (t / 3) % 3 - 1, dx = t % 3 - 1;
+            const int za = z0 + dz, ya = y0 + dy, xa = x0 + dx, zb = z1 + dz, yb = y1 + dy, xb = x1 + dx;
+            const bool v0 = ok0 && za >= 0 && za < d.D && ya >= 0 && ya < d.H && xa >= 0 && xa < d.W;
+            const bool v1 = ok1 && zb >= 0 && zb < d.D && yb >= 0 && yb < d.H && xb >= 0 && xb < d.W;
+            const long long n0 = v0 ? ((long long)za * d.H + ya) * d.W + xa : 0;
+            const long long n1 = v1 ? ((long long)zb * d.H + yb) * d.W + xb : 0;
+            const uint32_t* p0 = in32 + n0 * (CIN / 2);
+            const uint32_t* p1 = in32 + n1 * (CIN / 2);
+#pragma unroll
+            for (int kc = 0; kc < KC; ++kc) {
+                uint32_t a[4];
+                a[0] = v0 ? p0[kc * 8 + tg] : 0u;
+                a[1] = v1 ? p1[kc * 8 + tg] : 0u;
+                a[2] = v0 ? p0[kc * 8 + 4 + tg] : 0u;
+                a[3] = v1 ? p1[kc * 8 + 4 + tg] : 0u;
+#pragma unroll
+                for (int n = 0; n < NT; ++n) {
+                    const uint32_t* wp = w32 + ((size_t)t * COUT + n * 8 + g) * (CIN / 2);
+                    const uint32_t b[2] = {__ldg(wp + kc * 8 + tg), __ldg(wp + kc * 8 + 4 + tg)};
+                    mma_16816(acc[n], a, b);
+                }
+            }
+        }
+#pragma unroll
+        for (int n = 0; n < NT; ++n) {
+            const int co = n * 8 + tg * 2;
+            const float b0 = bias ? bias[co] : 0.f, b1 = bias ? bias[co + 1] : 0.f;
+            float c0 = acc[n][0] + b0, c1 = acc[n][1] + b1, c2 = acc[n][2] + b0, c3 = acc[n][3] + b1;
+            if (RELU) {
+                c0 = fmaxf(c0, 0.f); c1 = fmaxf(c1, 0.f); c2 = fmaxf(c2, 0.f); c3 = fmaxf(c3, 0.f);
+            }
+            if (ok0) store_pair<OutT>(out + r0 * COUT + co, c0, c1);
+            if (ok1) store_pair<OutT>(out + r1 * COUT + co, c2, c3);
+        }
+    }
+}
+
+// dw[tap][co][ci] += sum_v dy[v, co] in[v + tap, ci]; db[co] += sum_v dy[v, co] (tap 13).
+// Block (chunk of voxels, tap): 64-voxel slices of dy and of the shifted input staged in
+// shared memory, each thread accumulating its (co, ci) pairs, one atomic add per pair.
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(256) k_lp_conv_dw(LpDims d, const bf16* __restrict__ in, const bf16* __restrict__ dy,
+                                                    float* __restrict__ dw, float* __restrict__ db, int chunk) {
+    constexpr int PAIRS = CIN * COUT, PER = (PAIRS + 255) / 256;
+    __shared__ float sD[64][COUT];
+    __shared__ float sX[64][CIN + 1];
+    __shared__ long long sN[64];
+    const int t = blockIdx.y;
+    const int dz = t / 9 - 1, dyy = (t / 3) % 3 - 1, dx = t % 3 - 1;
+    const long long v0 = (long long)blockIdx.x * chunk;
+    const long long vend = (v0 + chunk < d.N) ? v0 + chunk : d.N;
+    float acc[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) acc[q] = 0.f;
+    float bacc = 0.f;
+    for (long long vb = v0; vb < vend; vb += 64) {
+        if (threadIdx.x < 64) {
+            const long long v = vb + threadIdx.x;
+            long long nb = -1;
+            if (v < vend) {
+                int z, y, x;
+                lp_decode(d, v, z, y, x);
+                z += dz; y += dyy; x += dx;
+                if (z >= 0 && z < d.D && y >= 0 && y < d.H && x >= 0 && x < d.W)
+                    nb = ((long long)z * d.H + y) * d.W + x;
+            }
+            sN[threadIdx.x] = nb;
+        }
+        for (int e = threadIdx.x; e < 64 * COUT; e += 256) {
+            const int vv = e / COUT, co = e - vv * COUT;
+            const long long v = vb + vv;
+            sD[vv][co] = (v < vend) ? __bfloat162float(dy[v * COUT + co]) : 0.f;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < 64 * CIN; e += 256) {
+            const int vv = e / CIN, ci = e - vv * CIN;
+            const long long nb = sN[vv];
+            sX[vv][ci] = (nb >= 0) ? __bfloat162float(in[nb * CIN + ci]) : 0.f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int p = threadIdx.x + q * 256;
+            if (p < PAIRS) {
+                const int co = p / CIN, ci = p - co * CIN;
+                float a = acc[q];
+                for (int vv = 0; vv < 64; ++vv) a = fmaf(sD[vv][co], sX[vv][ci], a);
+                acc[q] = a;
+            }
+        }
+        if (t == 13 && threadIdx.x < COUT)
+            for (int vv = 0; vv < 64; ++vv) bacc += sD[vv][threadIdx.x];
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int p = threadIdx.x + q * 256;
+        if (p < PAIRS) {
+            const int co = p / CIN, ci = p - co * CIN;
+            atomicAdd(&dw[((size_t)t * COUT + co) * CIN + ci], acc[q]);
+        }
+    }
+    if (t == 13 && threadIdx.x < COUT) atomicAdd(&db[threadIdx.x], bacc);
+}
+
+// wt[26 - tap][ci][co] = w[tap][co][ci] (the input-gradient convolution)
+__global__ void k_lp_wt(const bf16* __restrict__ w, bf16* __restrict__ wt, int cin, int cout) {
+    const int n = 27 * cin * cout;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const int t = e / (cin * cout), rem = e - t * cin * cout;
+        const int co = rem / cin, ci = rem - co * cin;
+        wt[((size_t)(26 - t) * cin + ci) * cout + co] = w[e];
+    }
+}
+
+// the 16-channel input: channels 0..2 from three FP32 fields, the rest 0
+__global__ void k_lp_pack(LpDims d, const float* __restrict__ c0, const float* __restrict__ c1,
+                          const float* __restrict__ c2, bf16* __restrict__ x) {
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < d.N; v += (long long)gridDim.x * blockDim.x) {
+        __nv_bfloat162* o = reinterpret_cast<__nv_bfloat162*>(x + v * 16);
+        o[0] = __floats2bfloat162_rn(c0[v], c1[v]);
+        o[1] = __floats2bfloat162_rn(c2[v], 0.f);
+        const __nv_bfloat162 z = __floats2bfloat162_rn(0.f, 0.f);
+        for (int q = 2; q < 8; ++q) o[q] = z;
+    }
+}
+
+// coarse = mean of the 2x2x2 children (fine dims df, coarse dims dc)
+__global__ void k_lp_pool(LpDims dc, int C, const bf16* __restrict__ fine, bf16* __restrict__ coarse) {
+    const int Wf = dc.W * 2, Hf = dc.H * 2;
+    const long long n = dc.N * C;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const long long v = e / C;
+        const int c = (int)(e - v * C);
+        int z, y, x;
+        lp_decode(dc, v, z, y, x);
+        float s = 0.f;
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b)
+                for (int q = 0; q < 2; ++q)
+                    s += __bfloat162float(fine[((((long long)(2 * z + a) * Hf) + 2 * y + b) * Wf + 2 * x + q) * C + c]);
+        coarse[e] = __float2bfloat16_rn(s * 0.125f);
+    }
+}
+
+// out(fine) = coarse(parent) + skip
+__global__ void k_lp_up_add(LpDims df, int C, const bf16* __restrict__ coarse, const bf16* __restrict__ skip,
+                            bf16* __restrict__ out) {
+    const int Wc = df.W / 2, Hc = df.H / 2;
+    const long long n = df.N * C;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const long long v = e / C;
+        const int c = (int)(e - v * C);
+        int z, y, x;
+        lp_decode(df, v, z, y, x);
+        const long long p = (((long long)(z / 2) * Hc) + y / 2) * Wc + x / 2;
+        out[e] = __float2bfloat16_rn(__bfloat162float(coarse[p * C + c]) + __bfloat162float(skip[e]));
+    }
+}
+
+// coarse gradient = sum of the 8 children's gradients (backward of the upsampling)
+__global__ void k_lp_up_bwd(LpDims dc, int C, const float* __restrict__ fine, float* __restrict__ coarse) {
+    const int Wf = dc.W * 2, Hf = dc.H * 2;
+    const long long n = dc.N * C;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const long long v = e / C;
+        const int c = (int)(e - v * C);
+        int z, y, x;
+        lp_decode(dc, v, z, y, x);
+        float s = 0.f;
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b)
+                for (int q = 0; q < 2; ++q)
+                    s += fine[((((long long)(2 * z + a) * Hf) + 2 * y + b) * Wf + 2 * x + q) * C + c];
+        coarse[e] = s;
+    }
+}
+
+// fine gradient += coarse gradient (parent) / 8 (backward of the pooling)
+__global__ void k_lp_pool_bwd_add(LpDims df, int C, const float* __restrict__ coarse, float* __restrict__ fine) {
+    const int Wc = df.W / 2, Hc = df.H / 2;
+    const long long n = df.N * C;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const long long v = e / C;
+        const int c = (int)(e - v * C);
+        int z, y, x;
+        lp_decode(df, v, z, y, x);
+        const long long p = (((long long)(z / 2) * Hc) + y / 2) * Wc + x / 2;
+        fine[e] += coarse[p * C + c] * 0.125f;
+    }
+}
+
+// BF16 gradient at a layer output: d masked by the ReLU (out > 0) when relu is set
+__global__ void k_lp_mask(long long n, const float* __restrict__ d, const bf16* __restrict__ out, int relu,
+                          bf16* __restrict__ q) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const float v = (!relu || __bfloat162float(out[e]) > 0.f) ? d[e] : 0.f;
+        q[e] = __float2bfloat16_rn(v);
+    }
+}
+
+// masked mean-square loss on output channel 0 and its gradient (16 channels, the others 0);
+// partial sums of the squared error per block
+__global__ void __launch_bounds__(kBlock) k_lp_loss(long long N, const bf16* __restrict__ y,
+                                                    const float* __restrict__ target, const float* __restrict__ mask,
+                                                    float inv_n, float* __restrict__ dy, double* __restrict__ partials) {
+    double acc = 0.0;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < N; v += (long long)gridDim.x * blockDim.x) {
+        const float m = mask[v];
+        const float diff = (__bfloat162float(y[v * 16]) - target[v]) * m;
+        acc += (double)diff * diff;
+        float4* o = reinterpret_cast<float4*>(dy + v * 16);
+        o[0] = make_float4(2.f * diff * inv_n, 0.f, 0.f, 0.f);
+        for (int q = 1; q < 4; ++q) o[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    double a[1] = {acc};
+    block_sum_store<1>(a, partials);
+}
+
+// output channel 0 to FP32
+__global__ void k_lp_out(long long N, const bf16* __restrict__ y, float* __restrict__ out) {
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < N; v += (long long)gridDim.x * blockDim.x)
+        out[v] = __bfloat162float(y[v * 16]);
+}
+
+// Adam on the FP32 master parameters; the BF16 copy of every weight follows
+__global__ void k_lp_adam(long long n, float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                          float* __restrict__ v, float lr, float b1, float b2, float eps, float c1, float c2,
+                          const int* __restrict__ bf_index, bf16* __restrict__ pw) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const float ge = g[e];
+        const float me = b1 * m[e] + (1.f - b1) * ge;
+        const float ve = b2 * v[e] + (1.f - b2) * ge * ge;
+        m[e] = me;
+        v[e] = ve;
+        const float pe = p[e] - lr * (me / c1) / (sqrtf(ve / c2) + eps);
+        p[e] = pe;
+        const int bi = bf_index[e];
+        if (bi >= 0) pw[bi] = __float2bfloat16_rn(pe);
+    }
+}
+
+// FP32 -> BF16 copy of the weights (after a parameter upload)
+__global__ void k_lp_cast(long long n, const float* __restrict__ p, const int* __restrict__ bf_index,
+                          bf16* __restrict__ pw) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int bi = bf_index[e];
+        if (bi >= 0) pw[bi] = __float2bfloat16_rn(p[e]);
+    }
+}
+
+}  // namespace
+}  // namespace ls
+
+// ---------------------------------------------------------------------------
+// host side
+
+namespace ls {
+
+struct LpLayer {
+    int cin, cout, relu;
+    size_t w_off, b_off;    // FP32 parameter offsets (weights 27*cout*cin, bias cout)
+    size_t wb_off;          // BF16 weight offset
+};
+
+constexpr int kLpLayers = 8;
+// (cin, cout, relu): W0a, W0b, W1, W2, W3, U2, U1, U0
+constexpr int kLpSpec[kLpLayers][3] = {{16, 16, 1}, {16, 16, 1}, {16, 32, 1}, {32, 64, 1},
+                                       {64, 64, 1}, {64, 32, 1}, {32, 16, 1}, {16, 16, 0}};
+
+}  // namespace ls
+
+using ls::bf16;
+using ls::kLpLayers;
+using ls::kLpSpec;
+using ls::LpDims;
+using ls::LpLayer;
+
+struct ls_lpnet {
+    int D, H, W;
+    int device, num_sms;
+    cudaStream_t stream;
+    LpLayer layer[kLpLayers];
+    size_t nparam, nweight_bf;
+    float *p, *g, *m, *v;   // FP32 parameters, gradients, Adam moments
+    int* bf_index;          // parameter -> BF16 weight index (-1 for biases)
+    bf16* wb;               // BF16 weights
+    bf16* wt;               // BF16 transposed, flipped weights (input gradients)
+    int adam_t;
+    // activations (BF16) per level
+    bf16 *x, *a0, *s0, *p1, *s1, *p2, *s2, *p3, *a3, *u2, *b2, *u1, *b1, *u0, *y;
+    // gradients (FP32)
+    float *gy, *g0, *g0b, *g1, *g1b, *g2, *g2b, *g3, *g3b;
+    bf16* q;                // BF16 masked gradient scratch
+    float* out;             // FP32 output (channel 0)
+    double* partials;
+    double* h_loss;
+    std::vector<void*> allocs;
+    std::string err;
+};
+
+namespace {
+
+ls_status lp_fail(ls_lpnet* n, const char* what, cudaError_t e) {
+    if (n) {
+        char buf[256];
+        snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+        n->err = buf;
+    }
+    return LS_CUDA_ERROR;
+}
+
+#define LP_CUDA(n, expr)                                     \
+    do {                                                     \
+        cudaError_t e__ = (expr);                            \
+        if (e__ != cudaSuccess) return lp_fail((n), #expr, e__); \
+    } while (0)
+#define LP_LAUNCH(n, kernel, grid, block, ...)                             \
+    do {                                                                   \
+        kernel<<<(grid), (block), 0, (n)->stream>>>(__VA_ARGS__);          \
+        cudaError_t e__ = cudaGetLastError();                              \
+        if (e__ != cudaSuccess) return lp_fail((n), #kernel, e__);         \
+    } while (0)
+
+template <typename T>
+ls_status lp_alloc(ls_lpnet* n, T** p, size_t count) {
+    void* v = nullptr;
+    LP_CUDA(n, cudaMalloc(&v, count * sizeof(T) + 16));
+    n->allocs.push_back(v);
+    *p = (T*)v;
+    return LS_OK;
+}
+
+int lp_grid(const ls_lpnet* n, long long work, int block) {
+    long long b = (work + block - 1) / block;
+    const long long cap = (long long)n->num_sms * 16;
+    if (b > cap) b = cap;
+    return (int)(b < 1 ? 1 : b);
+}
+
+// conv forward / input-gradient dispatch over the channel pairs of the network
+template <bool RELU, typename OutT>
+ls_status lp_conv(ls_lpnet* n, LpDims d, int cin, int cout, const bf16* in, const bf16* w, const float* bias,
+                  OutT* out) {
+    const int grid = lp_grid(n, (d.N + 15) / 16, 4);
+#define LP_CASE(CI, CO)                                                                        \
+    if (cin == CI && cout == CO) {                                                             \
+        LP_LAUNCH(n, (ls::k_lp_conv<CI, CO, RELU, OutT>), grid, 128, d, in, w, bias, out);     \
+        return LS_OK;                                                                          \
+    }
+    LP_CASE(16, 16) LP_CASE(16, 32) LP_CASE(32, 64) LP_CASE(64, 64) LP_CASE(64, 32) LP_CASE(32, 16)
+#undef LP_CASE
+    n->err = "unsupported channel pair";
+    return LS_BAD_ARG;
+}
+
+ls_status lp_conv_dw(ls_lpnet* n, LpDims d, int cin, int cout, const bf16* in, const bf16* dy, float* dw, float* db) {
+    const int chunk = 2048;
+    const dim3 grid((unsigned)((d.N + chunk - 1) / chunk), 27);
+#define LP_CASE(CI, CO)                                                                   \
+    if (cin == CI && cout == CO) {                                                        \
+        LP_LAUNCH(n, (ls::k_lp_conv_dw<CI, CO>), grid, 256, d, in, dy, dw, db, chunk);    \
+        return LS_OK;                                                                     \
+    }
+    LP_CASE(16, 16) LP_CASE(16, 32) LP_CASE(32, 64) LP_CASE(64, 64) LP_CASE(64, 32) LP_CASE(32, 16)
+#undef LP_CASE
+    n->err = "unsupported channel pair";
+    return LS_BAD_ARG;
+}
+
+ls_status lp_refresh_wt(ls_lpnet* n) {
+    for (int l = 0; l < kLpLayers; ++l) {
+        const LpLayer& L = n->layer[l];
+        const int cnt = 27 * L.cin * L.cout;
+        LP_LAUNCH(n, ls::k_lp_wt, lp_grid(n, cnt, 256), 256, n->wb + L.wb_off, n->wt + L.wb_off, L.cin, L.cout);
+    }
+    return LS_OK;
+}
+
+ls_status lp_forward(ls_lpnet* n, const float* c0, const float* c1, const float* c2) {
+    const LpDims d0 = ls::lp_dims(n->D, n->H, n->W), d1 = ls::lp_dims(n->D / 2, n->H / 2, n->W / 2),
+                 d2 = ls::lp_dims(n->D / 4, n->H / 4, n->W / 4), d3 = ls::lp_dims(n->D / 8, n->H / 8, n->W / 8);
+    const LpLayer* L = n->layer;
+    auto wb = [&](int l) { return (const bf16*)(n->wb + L[l].wb_off); };
+    auto bias = [&](int l) { return (const float*)(n->p + L[l].b_off); };
+    LP_LAUNCH(n, ls::k_lp_pack, lp_grid(n, d0.N, 256), 256, d0, c0, c1, c2, n->x);
+    LS_TRY((lp_conv<true, bf16>(n, d0, 16, 16, n->x, wb(0), bias(0), n->a0)));
+    LS_TRY((lp_conv<true, bf16>(n, d0, 16, 16, n->a0, wb(1), bias(1), n->s0)));
+    LP_LAUNCH(n, ls::k_lp_pool, lp_grid(n, d1.N * 16, 256), 256, d1, 16, (const bf16*)n->s0, n->p1);
+    LS_TRY((lp_conv<true, bf16>(n, d1, 16, 32, n->p1, wb(2), bias(2), n->s1)));
+    LP_LAUNCH(n, ls::k_lp_pool, lp_grid(n, d2.N * 32, 256), 256, d2, 32, (const bf16*)n->s1, n->p2);
+    LS_TRY((lp_conv<true, bf16>(n, d2, 32, 64, n->p2, wb(3), bias(3), n->s2)));
+    LP_LAUNCH(n, ls::k_lp_pool, lp_grid(n, d3.N * 64, 256), 256, d3, 64, (const bf16*)n->s2, n->p3);
+    LS_TRY((lp_conv<true, bf16>(n, d3, 64, 64, n->p3, wb(4), bias(4), n->a3)));
+    LP_LAUNCH(n, ls::k_lp_up_add, lp_grid(n, d2.N * 64, 256), 256, d2, 64, (const bf16*)n->a3, (const bf16*)n->s2, n->u2);
+    LS_TRY((lp_conv<true, bf16>(n, d2, 64, 32, n->u2, wb(5), bias(5), n->b2)));
+    LP_LAUNCH(n, ls::k_lp_up_add, lp_grid(n, d1.N * 32, 256), 256, d1, 32, (const bf16*)n->b2, (const bf16*)n->s1, n->u1);
+    LS_TRY((lp_conv<true, bf16>(n, d1, 32, 16, n->u1, wb(6), bias(6), n->b1)));
+    LP_LAUNCH(n, ls::k_lp_up_add, lp_grid(n, d0.N * 16, 256), 256, d0, 16, (const bf16*)n->b1, (const bf16*)n->s0, n->u0);
+    LS_TRY((lp_conv<false, bf16>(n, d0, 16, 16, n->u0, wb(7), bias(7), n->y)));
+    return LS_OK;
+}
+
+// backward of one layer: q = mask(d), dW += in^T q, dIn = conv(q, W^T) (dIn null: skipped)
+ls_status lp_layer_bwd(ls_lpnet* n, int l, LpDims d, const bf16* in, const bf16* out, const float* dout, float* din) {
+    const LpLayer& L = n->layer[l];
+    LP_LAUNCH(n, ls::k_lp_mask, lp_grid(n, d.N * L.cout, 256), 256, d.N * L.cout, dout, out, L.relu, n->q);
+    LS_TRY(lp_conv_dw(n, d, L.cin, L.cout, in, (const bf16*)n->q, n->g + L.w_off, n->g + L.b_off));
+    if (din) LS_TRY((lp_conv<false, float>(n, d, L.cout, L.cin, (const bf16*)n->q, n->wt + L.wb_off, nullptr, din)));
+    return LS_OK;
+}
+
+ls_status lp_backward(ls_lpnet* n) {
+    const LpDims d0 = ls::lp_dims(n->D, n->H, n->W), d1 = ls::lp_dims(n->D / 2, n->H / 2, n->W / 2),
+                 d2 = ls::lp_dims(n->D / 4, n->H / 4, n->W / 4), d3 = ls::lp_dims(n->D / 8, n->H / 8, n->W / 8);
+    LP_CUDA(n, cudaMemsetAsync(n->g, 0, sizeof(float) * n->nparam, n->stream));
+    LS_TRY(lp_layer_bwd(n, 7, d0, n->u0, n->y, n->gy, n->g0));                     // d_u0 = d_s0 (partial)
+    LP_LAUNCH(n, ls::k_lp_up_bwd, lp_grid(n, d1.N * 16, 256), 256, d1, 16, (const float*)n->g0, n->g1b);  // d_b1
+    LS_TRY(lp_layer_bwd(n, 6, d1, n->u1, n->b1, n->g1b, n->g1));                    // d_u1
+    LP_LAUNCH(n, ls::k_lp_up_bwd, lp_grid(n, d2.N * 32, 256), 256, d2, 32, (const float*)n->g1, n->g2b);  // d_b2
+    LS_TRY(lp_layer_bwd(n, 5, d2, n->u2, n->b2, n->g2b, n->g2));                    // d_u2
+    LP_LAUNCH(n, ls::k_lp_up_bwd, lp_grid(n, d3.N * 64, 256), 256, d3, 64, (const float*)n->g2, n->g3);   // d_a3
+    LS_TRY(lp_layer_bwd(n, 4, d3, n->p3, n->a3, n->g3, n->g3b));                    // d_p3
+    LP_LAUNCH(n, ls::k_lp_pool_bwd_add, lp_grid(n, d2.N * 64, 256), 256, d2, 64, (const float*)n->g3b, n->g2);  // d_s2
+    LS_TRY(lp_layer_bwd(n, 3, d2, n->p2, n->s2, n->g2, n->g2b));                    // d_p2
+    LP_LAUNCH(n, ls::k_lp_pool_bwd_add, lp_grid(n, d1.N * 32, 256), 256, d1, 32, (const float*)n->g2b, n->g1);  // d_s1
+    LS_TRY(lp_layer_bwd(n, 2, d1, n->p1, n->s1, n->g1, n->g1b));                    // d_p1
+    LP_LAUNCH(n, ls::k_lp_pool_bwd_add, lp_grid(n, d0.N * 16, 256), 256, d0, 16, (const float*)n->g1b, n->g0);  // d_s0
+    LS_TRY(lp_layer_bwd(n, 1, d0, n->a0, n->s0, n->g0, n->g0b));                    // d_a0
+    LS_TRY(lp_layer_bwd(n, 0, d0, n->x, n->a0, n->g0b, nullptr));
+    return LS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+ls_status ls_lpnet_create(int D, int H, int W, int seed, ls_lpnet** out) {
+    if (!out) return LS_BAD_ARG;
+    *out = nullptr;
+    if (D < 8 || H < 8 || W < 8 || D % 8 || H % 8 || W % 8) return LS_BAD_ARG;
+    if ((long long)D * H * W * 64 >= (1LL << 40)) return LS_BAD_ARG;
+    ls_lpnet* n = new (std::nothrow) ls_lpnet();
+    if (!n) return LS_CUDA_ERROR;
+    n->D = D; n->H = H; n->W = W;
+    ls_status st = LS_OK;
+    auto fail = [&](ls_status s) { ls_lpnet_destroy(n); return s; };
+    if (cudaGetDevice(&n->device) != cudaSuccess) return fail(LS_CUDA_ERROR);
+    cudaDeviceGetAttribute(&n->num_sms, cudaDevAttrMultiProcessorCount, n->device);
+    if (cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(LS_CUDA_ERROR);
+    size_t off = 0, boff = 0;
+    for (int l = 0; l < kLpLayers; ++l) {
+        LpLayer& L = n->layer[l];
+        L.cin = kLpSpec[l][0]; L.cout = kLpSpec[l][1]; L.relu = kLpSpec[l][2];
+        L.w_off = off; off += (size_t)27 * L.cin * L.cout;
+        L.b_off = off; off += (size_t)L.cout;
+        L.wb_off = boff; boff += (size_t)27 * L.cin * L.cout;
+    }
+    n->nparam = off;
+    n->nweight_bf = boff;
+    const long long v0 = (long long)D * H * W, v1 = v0 / 8, v2 = v0 / 64, v3 = v0 / 512;
+    st = [&]() -> ls_status {
+        LS_TRY(lp_alloc(n, &n->p, n->nparam));
+        LS_TRY(lp_alloc(n, &n->g, n->nparam));
+        LS_TRY(lp_alloc(n, &n->m, n->nparam));
+        LS_TRY(lp_alloc(n, &n->v, n->nparam));
+        LS_TRY(lp_alloc(n, &n->bf_index, n->nparam));
+        LS_TRY(lp_alloc(n, &n->wb, n->nweight_bf));
+        LS_TRY(lp_alloc(n, &n->wt, n->nweight_bf));
+        LS_TRY(lp_alloc(n, &n->x, v0 * 16));
+        LS_TRY(lp_alloc(n, &n->a0, v0 * 16));
+        LS_TRY(lp_alloc(n, &n->s0, v0 * 16));
+        LS_TRY(lp_alloc(n, &n->p1, v1 * 16));
+        LS_TRY(lp_alloc(n, &n->s1, v1 * 32));
+        LS_TRY(lp_alloc(n, &n->p2, v2 * 32));
+        LS_TRY(lp_alloc(n, &n->s2, v2 * 64));
+        LS_TRY(lp_alloc(n, &n->p3, v3 * 64));
+        LS_TRY(lp_alloc(n, &n->a3, v3 * 64));
+        LS_TRY(lp_alloc(n, &n->u2, v2 * 64));
+        LS_TRY(lp_alloc(n, &n->b2, v2 * 32));
+        LS_TRY(lp_alloc(n, &n->u1, v1 * 32));
+        LS_TRY(lp_alloc(n, &n->b1, v1 * 16));
+        LS_TRY(lp_alloc(n, &n->u0, v0 * 16));
+        LS_TRY(lp_alloc(n, &n->y, v0 * 16));
+        LS_TRY(lp_alloc(n, &n->gy, v0 * 16));
+        LS_TRY(lp_alloc(n, &n->g0, v0 * 16));
+        LS_TRY(lp_alloc(n, &n->g0b, v0 * 16));
+        LS_TRY(lp_alloc(n, &n->g1, v1 * 32));
+        LS_TRY(lp_alloc(n, &n->g1b, v1 * 16));
+        LS_TRY(lp_alloc(n, &n->g2, v2 * 64));
+        LS_TRY(lp_alloc(n, &n->g2b, v2 * 32));
+        LS_TRY(lp_alloc(n, &n->g3, v3 * 64));
+        LS_TRY(lp_alloc(n, &n->g3b, v3 * 64));
+        LS_TRY(lp_alloc(n, &n->q, v0 * 16));
+        LS_TRY(lp_alloc(n, &n->out, v0));
+        LS_TRY(lp_alloc(n, &n->partials, (size_t)n->num_sms * 16));
+        if (cudaMallocHost(&n->h_loss, sizeof(double)) != cudaSuccess) return LS_CUDA_ERROR;
+        // parameter -> BF16 weight index, He-normal weights from the seed, zero biases
+        std::vector<int> idx(n->nparam, -1);
+        std::vector<float> p(n->nparam, 0.f);
+        unsigned long long s = 0x9E3779B97F4A7C15ull ^ (unsigned long long)(unsigned)seed;
+        auto next = [&]() {  // splitmix64
+            s += 0x9E3779B97F4A7C15ull;
+            unsigned long long z = s;
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+            return z ^ (z >> 31);
+        };
+        for (int l = 0; l < kLpLayers; ++l) {
+            const LpLayer& L = n->layer[l];
+            const size_t cnt = (size_t)27 * L.cin * L.cout;
+            const double sd = sqrt(2.0 / (27.0 * L.cin));
+            for (size_t e = 0; e < cnt; ++e) {
+                idx[L.w_off + e] = (int)(L.wb_off + e);
+                // Box-Muller from two uniforms
+                const double u1 = ((next() >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+                const double u2 = ((next() >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+                p[L.w_off + e] = (float)(sd * sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
+            }
+        }
+        LP_CUDA(n, cudaMemcpy(n->bf_index, idx.data(), sizeof(int) * n->nparam, cudaMemcpyHostToDevice));
+        LP_CUDA(n, cudaMemcpy(n->p, p.data(), sizeof(float) * n->nparam, cudaMemcpyHostToDevice));
+        LP_CUDA(n, cudaMemset(n->m, 0, sizeof(float) * n->nparam));
+        LP_CUDA(n, cudaMemset(n->v, 0, sizeof(float) * n->nparam));
+        LP_LAUNCH(n, ls::k_lp_cast, lp_grid(n, (long long)n->nparam, 256), 256, (long long)n->nparam,
+                  (const float*)n->p, (const int*)n->bf_index, n->wb);
+        LS_TRY(lp_refresh_wt(n));
+        LP_CUDA(n, cudaStreamSynchronize(n->stream));
+        return LS_OK;
+    }();
+    if (st != LS_OK) return fail(st);
+    *out = n;
+    return LS_OK;
+}
+
+ls_status ls_lpnet_destroy(ls_lpnet* n) {
+    if (!n) return LS_OK;
+    if (n->stream) cudaStreamSynchronize(n->stream);
+    for (void* q : n->allocs) cudaFree(q);
+    if (n->h_loss) cudaFreeHost(n->h_loss);
+    if (n->stream) cudaStreamDestroy(n->stream);
+    delete n;
+    return LS_OK;
+}
+
+const char* ls_lpnet_last_error(const ls_lpnet* n) { return n ? n->err.c_str() : "null network"; }
+
+long long ls_lpnet_param_count(const ls_lpnet* n) { return n ? (long long)n->nparam : 0; }
+
+ls_status ls_lpnet_get_params(ls_lpnet* n, float* host, long long count) {
+    if (!n || !host || count != (long long)n->nparam) return LS_BAD_ARG;
+    LP_CUDA(n, cudaMemcpyAsync(host, n->p, sizeof(float) * n->nparam, cudaMemcpyDeviceToHost, n->stream));
+    LP_CUDA(n, cudaStreamSynchronize(n->stream));
+    return LS_OK;
+}
+
+ls_status ls_lpnet_set_params(ls_lpnet* n, const float* host, long long count) {
+    if (!n || !host || count != (long long)n->nparam) return LS_BAD_ARG;
+    LP_CUDA(n, cudaMemcpyAsync(n->p, host, sizeof(float) * n->nparam, cudaMemcpyHostToDevice, n->stream));
+    LP_LAUNCH(n, ls::k_lp_cast, lp_grid(n, (long long)n->nparam, 256), 256, (long long)n->nparam,
+              (const float*)n->p, (const int*)n->bf_index, n->wb);
+    LS_TRY(lp_refresh_wt(n));
+    LP_CUDA(n, cudaMemsetAsync(n->m, 0, sizeof(float) * n->nparam, n->stream));
+    LP_CUDA(n, cudaMemsetAsync(n->v, 0, sizeof(float) * n->nparam, n->stream));
+    n->adam_t = 0;
+    LP_CUDA(n, cudaStreamSynchronize(n->stream));
+    return LS_OK;
+}
+
+ls_status ls_lpnet_get_grads(ls_lpnet* n, float* host, long long count) {
+    if (!n || !host || count != (long long)n->nparam) return LS_BAD_ARG;
+    LP_CUDA(n, cudaMemcpyAsync(host, n->g, sizeof(float) * n->nparam, cudaMemcpyDeviceToHost, n->stream));
+    LP_CUDA(n, cudaStreamSynchronize(n->stream));
+    return LS_OK;
+}
+
+ls_status ls_lpnet_forward(ls_lpnet* n, const float* c0, const float* c1, const float* c2, float* out) {
+    if (!n || !c0 || !c1 || !c2 || !out) return LS_BAD_ARG;
+    LS_TRY(lp_forward(n, c0, c1, c2));
+    const long long N = (long long)n->D * n->H * n->W;
+    LP_LAUNCH(n, ls::k_lp_out, lp_grid(n, N, 256), 256, N, (const bf16*)n->y, out);
+    LP_CUDA(n, cudaStreamSynchronize(n->stream));
+    return LS_OK;
+}
+
+ls_status ls_lpnet_train_step(ls_lpnet* n, const float* c0, const float* c1, const float* c2, const float* target,
+                              const float* mask, long long mask_count, float lr, int update, double* loss) {
+    if (!n || !c0 || !c1 || !c2 || !target || !mask || mask_count < 1 || !(lr >= 0.f)) return LS_BAD_ARG;
+    LS_TRY(lp_forward(n, c0, c1, c2));
+    const long long N = (long long)n->D * n->H * n->W;
+    const int nb = lp_grid(n, N, ls::kBlock);
+    LP_LAUNCH(n, ls::k_lp_loss, nb, ls::kBlock, N, (const bf16*)n->y, target, mask, (float)(1.0 / (double)mask_count),
+              n->gy, n->partials);
+    LS_TRY(lp_backward(n));
+    if (update) {
+        n->adam_t += 1;
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float c1 = (float)(1.0 - pow((double)b1, n->adam_t)), c2 = (float)(1.0 - pow((double)b2, n->adam_t));
+        LP_LAUNCH(n, ls::k_lp_adam, lp_grid(n, (long long)n->nparam, 256), 256, (long long)n->nparam, n->p,
+                  (const float*)n->g, n->m, n->v, lr, b1, b2, 1e-8f, c1, c2, (const int*)n->bf_index, n->wb);
+        LS_TRY(lp_refresh_wt(n));
+    }
+    std::vector<double> part(nb);
+    LP_CUDA(n, cudaMemcpyAsync(part.data(), n->partials, sizeof(double) * nb, cudaMemcpyDeviceToHost, n->stream));
+    LP_CUDA(n, cudaStreamSynchronize(n->stream));
+    double sum = 0.0;
+    for (double v : part) sum += v;
+    if (loss) *loss = sum / (double)mask_count;
+    return LS_OK;
+}
+
+}  // extern "C"

@@ -59,6 +59,16 @@ SYMBOLS = {
     "ls_transport_apply": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]),
     "ls_geom_coarsen": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     "ls_geom_clean": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p]),
+    "ls_lpnet_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "ls_lpnet_destroy": (C.c_int, [C.c_void_p]),
+    "ls_lpnet_last_error": (C.c_char_p, [C.c_void_p]),
+    "ls_lpnet_param_count": (C.c_longlong, [C.c_void_p]),
+    "ls_lpnet_get_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
+    "ls_lpnet_set_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
+    "ls_lpnet_get_grads": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
+    "ls_lpnet_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ls_lpnet_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_longlong, C.c_float, C.c_int, C.POINTER(C.c_double)]),
     "ls_geom_fracture": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ls_geom_classify": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                    C.c_int, C.c_void_p]),
@@ -165,6 +175,106 @@ def geom_classify(grey, thresholds, labels, label_bytes=1):
     _geom_check(load().ls_geom_classify(*g.shape, _p(g), t.size, _p(t) if t.size else None, _p(lb),
                                         label_bytes, _p(out)), "ls_geom_classify")
     return out
+
+
+# layer (name, cin, cout) of the learned pressure network, in parameter order
+LPNET_LAYERS = [("W0a", 16, 16), ("W0b", 16, 16), ("W1", 16, 32), ("W2", 32, 64), ("W3", 64, 64),
+                ("U2", 64, 32), ("U1", 32, 16), ("U0", 16, 16)]
+
+
+def lpnet_flatten(params):
+    """{name: (27, cout, cin) weights, name_b: (cout,) biases} -> flat float32 vector."""
+    parts = []
+    for name, cin, cout in LPNET_LAYERS:
+        parts.append(np.asarray(params[name], np.float32).reshape(-1))
+        parts.append(np.asarray(params[name + "_b"], np.float32).reshape(-1))
+    return np.concatenate(parts)
+
+
+def lpnet_unflatten(flat):
+    out, o = {}, 0
+    for name, cin, cout in LPNET_LAYERS:
+        n = 27 * cout * cin
+        out[name] = flat[o:o + n].reshape(27, cout, cin)
+        o += n
+        out[name + "_b"] = flat[o:o + cout].copy()
+        o += cout
+    return out
+
+
+class LPNet:
+    """The learned pressure network on the GPU (owns an ls_lpnet). Fields are torch CUDA
+    float32 tensors of shape (D, H, W) or numpy arrays (copied to the device)."""
+
+    def __init__(self, shape, seed=0):
+        import torch  # noqa: F401  (device memory for the fields)
+        self.shape = tuple(int(v) for v in shape)
+        h = C.c_void_p()
+        st = load().ls_lpnet_create(*self.shape, int(seed), C.byref(h))
+        if st != 0:
+            raise LsError(st, "ls_lpnet_create")
+        self.h = h
+        self.n = int(load().ls_lpnet_param_count(self.h))
+
+    def close(self):
+        if self.h:
+            load().ls_lpnet_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != 0:
+            raise LsError(st, (load().ls_lpnet_last_error(self.h) or b"").decode())
+
+    def _dev(self, a):
+        import torch
+        if isinstance(a, torch.Tensor):
+            t = a.to(device="cuda", dtype=torch.float32).contiguous()
+        else:
+            t = torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda()
+        if tuple(t.shape) != self.shape:
+            raise ValueError(f"field shape {tuple(t.shape)} != {self.shape}")
+        return t
+
+    def get_params(self):
+        out = np.empty(self.n, np.float32)
+        self._check(load().ls_lpnet_get_params(self.h, _p(out), self.n))
+        return out
+
+    def set_params(self, flat):
+        flat = np.ascontiguousarray(flat, np.float32)
+        if flat.size != self.n:
+            raise ValueError("wrong parameter count")
+        self._check(load().ls_lpnet_set_params(self.h, _p(flat), self.n))
+
+    def get_grads(self):
+        out = np.empty(self.n, np.float32)
+        self._check(load().ls_lpnet_get_grads(self.h, _p(out), self.n))
+        return out
+
+    def forward(self, c0, c1, c2):
+        import torch
+        t = [self._dev(c) for c in (c0, c1, c2)]
+        out = torch.empty(self.shape, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        self._check(load().ls_lpnet_forward(self.h, *[C.c_void_p(x.data_ptr()) for x in t],
+                                            C.c_void_p(out.data_ptr())))
+        return out
+
+    def train_step(self, c0, c1, c2, target, mask, lr=1e-3, update=True):
+        import torch
+        t = [self._dev(c) for c in (c0, c1, c2, target, mask)]
+        count = int((t[4] > 0).sum().item())
+        loss = C.c_double(0.0)
+        torch.cuda.synchronize()
+        self._check(load().ls_lpnet_train_step(self.h, *[C.c_void_p(x.data_ptr()) for x in t], max(count, 1),
+                                               float(lr), 1 if update else 0, C.byref(loss)))
+        return float(loss.value)
 
 
 class Context:
