@@ -183,6 +183,56 @@ def roofline(ctx, shape, nsteps):
             "launches": cnt, "us_per_launch": round(ms * 1e3 / cnt, 2)}
 
 
+def cold_pressure_solves(ctx, shape, solver, reps=2):
+    """The second metric: cold solves of the first step's pressure system (t = 0, zero
+    start, rtol 1e-8 on the Jacobi-scaled FP64 residual) with the plain FP64 multigrid-PCG,
+    with the mixed-precision K-cycle FCG, and with the mixed solver from the learned start
+    (when trained weights exist). Each: assembly + [network inference] + solve, wall time
+    with the device idle on both sides, the last of `reps` runs (the first pays the buffer
+    allocations of a precision switch). The P slots are zeroed around every solve, so the
+    run that follows starts from the same state."""
+    import torch
+    from leachingsim_gb300 import learned as L
+    from leachingsim_gb300._abi import PRESS_FP64, PRESS_MIXED
+    zeros_p = np.zeros(ctx.NP)
+    zeros = torch.zeros(shape, dtype=torch.float32, device="cuda")
+    weights = L.load_weights()
+    ls = L.LearnedStart(shape, weights) if weights is not None else None
+    variants = [("plain_fp64", PRESS_FP64, None), ("plain", PRESS_MIXED, None)]
+    if ls is not None:
+        variants.append(("learned", PRESS_MIXED, ls))
+    ctx.props()
+    out = {}
+    for name, s, start in variants:
+        base = params("fp64" if s == PRESS_FP64 else "mixed")
+        ctx.set_params(base)
+        for _ in range(reps):
+            ctx.upload("pressure", zeros_p, padded=True)
+            ctx.synchronize()
+            torch.cuda.synchronize()
+            w0 = time.perf_counter()
+            ctx.pressure_setup(0.0)
+            w1 = time.perf_counter()
+            x0 = start.start(ctx) if start is not None else zeros
+            torch.cuda.synchronize()
+            w2 = time.perf_counter()
+            ok, info = ctx.pressure_solve_start(x0, 1.0 if start is not None else 0.0)
+            ctx.synchronize()
+            w3 = time.perf_counter()
+        out[name] = {"solver": "fp64" if s == PRESS_FP64 else "mixed", "ms": round((w3 - w0) * 1e3, 3),
+                     "setup_ms": round((w1 - w0) * 1e3, 3), "solve_ms": round((w3 - w2) * 1e3, 3),
+                     "iterations": info["iterations"], "outer": info["outer_iterations"],
+                     "scaled_rel_residual": info["rel_residual"], "converged": bool(ok)}
+        if start is not None:
+            out[name]["inference_ms"] = round((w2 - w1) * 1e3, 3)
+    if ls is not None:
+        ls.close()
+    ctx.set_params(params(solver))
+    ctx.upload("pressure", zeros_p, padded=True)
+    ctx.synchronize()
+    return out
+
+
 def gpu_arm(args, ws, rank, local):
     import torch
     from leachingsim_gb300.runtime import Context
@@ -208,9 +258,10 @@ def gpu_arm(args, ws, rank, local):
     ctx.init_all()
     stream = torch.cuda.ExternalStream(ctx.stream())
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    # second metric: the first step's pressure solve is a cold solve (zero start) of the
-    # plain multigrid-PCG to rtol 1e-8; its assembly + setup + solve time from the library's
-    # CUDA-event timers on the context stream
+    # second metric: cold pressure solves of the first step's system (plain FP64, mixed,
+    # learned start), then the run's own first step, whose pressure solve is a cold solve
+    # too (assembly + setup + solve from the library's CUDA-event timers)
+    cold = cold_pressure_solves(ctx, shape, args.solver) if not args.no_cold else {}
     ctx.timing(True)
     ctx.timing_reset()
     if args.nvtx:
@@ -221,13 +272,15 @@ def gpu_arm(args, ws, rank, local):
         torch.cuda.nvtx.range_pop()
     pinfo = first[0]["pressure"]
     psolve_ms = sum(ctx.timing_get(k)[0] for k in ("press_setup", "press_inner", "press_outer"))
-    psolve = {"plain": {"solver": args.solver, "ms": round(psolve_ms, 3), "iterations": pinfo["iterations"],
-                        "outer": pinfo["outer_iterations"], "scaled_rel_residual": pinfo["rel_residual"],
-                        "converged": bool(pinfo["converged"])},
-              "learned": None,
-              "note": "first step of the run: cold start (zero pressure), t = 0, rtol 1e-8 on the "
-                      "Jacobi-scaled FP64 residual, assembly + multigrid setup + solve; learned FCG "
-                      "preconditioner not built"}
+    psolve = dict(cold)
+    psolve["first_step"] = {"solver": args.solver, "ms": round(psolve_ms, 3), "iterations": pinfo["iterations"],
+                            "outer": pinfo["outer_iterations"], "scaled_rel_residual": pinfo["rel_residual"],
+                            "converged": bool(pinfo["converged"])}
+    psolve.setdefault("learned", None)
+    psolve["note"] = ("cold solves of the first step's pressure system: t = 0, zero start (learned: the "
+                      "network's start), rtol 1e-8 on the Jacobi-scaled FP64 residual; ms = assembly + "
+                      "[inference] + multigrid setup + solve; first_step = the run's own first step "
+                      "(device timers)")
     ctx.timing(False)
     t, n, _ = run_steps(ctx, t, n, max(args.warmup - 1, 0), DT)
     ctx.timing(True)
@@ -468,6 +521,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cold", action="store_true", help="skip the separate cold pressure solves")
     ap.add_argument("--nvtx", action="store_true",
                     help="wrap the first (cold) step in an NVTX range 'cold' and the timed steps in "
                          "'timed' (for ncu --nvtx-include cold/ or timed/)")

@@ -193,6 +193,16 @@ ls_status ls_init_acid(ls_ctx* ctx);
 ls_status ls_props(ls_ctx* ctx);
 /* Simulation::setupPressureEqns(t) + solvePressure (src/Simulation.cpp:658-855). */
 ls_status ls_pressure_step(ls_ctx* ctx, double t, ls_solve_info* info);
+/* The learned start of the pressure solve (no counterpart in the reference), on the system
+   assembled by ls_pressure_setup(t): ls_pressure_learned_inputs writes the network's input
+   fields to DEVICE float32 arrays of I*J*K values: the Pore-row mask (0/1), the
+   log-permeability (log10 K + 15) / 3, and the identity-row values over the effective top
+   pressure. ls_pressure_solve_start solves the assembled system from x = scale * p_top *
+   start (start: DEVICE float32, I*J*K; p_top: the effective top pressure) on the Pore rows
+   instead of the stored pressure; the FP64 refinement judges and finishes the solve
+   exactly as in ls_pressure_step. */
+ls_status ls_pressure_learned_inputs(ls_ctx* ctx, float* mask, float* logk, float* bc);
+ls_status ls_pressure_solve_start(ls_ctx* ctx, const float* start, double scale, ls_solve_info* info);
 /* Simulation::calculateFlux (src/Simulation.cpp:866-953). */
 ls_status ls_flux(ls_ctx* ctx);
 /* Simulation::updateSaturation(dt), explicit sub-stepping (src/Simulation.cpp:1672-1856). */

@@ -371,6 +371,7 @@ ls_status ls_destroy(ls_ctx* c) {
     for (float* q : c->trhs)
         if (q) cudaFree(q);
     if (c->ti) cudaFree(c->ti);
+    if (c->start_anchor) cudaFree(c->start_anchor);
     if (c->tcount) cudaFree(c->tcount);
     for (auto& lv : c->mg) {
         void* lp[] = {lv.comp, lv.e, lv.face[0], lv.face[1], lv.face[2], lv.invd, lv.x, lv.b, lv.t};
@@ -506,6 +507,16 @@ ls_status ls_pressure_step(ls_ctx* c, double t, ls_solve_info* info) {
         LS_TRY(pressure_setup_run(c, t));
     }
     return pressure_solve_run(c, info);
+}
+
+ls_status ls_pressure_learned_inputs(ls_ctx* c, float* mask, float* logk, float* bc) {
+    if (!c || !mask || !logk || !bc) return LS_BAD_ARG;
+    return pressure_learned_inputs_run(c, mask, logk, bc);
+}
+
+ls_status ls_pressure_solve_start(ls_ctx* c, const float* start, double scale, ls_solve_info* info) {
+    if (!c || !start || !(scale == scale)) return LS_BAD_ARG;
+    return pressure_solve_run(c, info, start, scale);
 }
 
 ls_status ls_pressure_apply(ls_ctx* c, const double* x, double* y) {

@@ -314,6 +314,7 @@ struct ls_ctx {
     void* mg0_t;
     int mg_is64;          // -1 = not allocated
     int* comp;            // fine-level strong-component ids (-1 = not an inner unknown)
+    uint8_t* start_anchor; // per component root: anchored to fixed values (supplied starts)
     int* cc_flag;         // device flag for the labelling loop
 
     // transport / implicit saturation (2 right-hand sides)
@@ -481,7 +482,9 @@ ls_status saturation_implicit_run(ls_ctx* c, double dt, ls_solve_info* info);
 ls_status surface_run(ls_ctx* c);
 ls_status precip_run(ls_ctx* c);
 ls_status pressure_setup_run(ls_ctx* c, double t);
-ls_status pressure_solve_run(ls_ctx* c, ls_solve_info* info);
+ls_status pressure_solve_run(ls_ctx* c, ls_solve_info* info, const float* start = nullptr,
+                             double start_scale = 0.0);
+ls_status pressure_learned_inputs_run(ls_ctx* c, float* mask, float* logk, float* bc);
 ls_status pressure_apply_run(ls_ctx* c, const double* x, double* y);
 ls_status transport_run(ls_ctx* c, double dt, int which, ls_solve_info* ci, ls_solve_info* ai);
 ls_status transport_apply_run(ls_ctx* c, double dt, const double* x, double* y);

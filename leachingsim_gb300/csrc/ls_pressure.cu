@@ -377,6 +377,62 @@ __global__ void k_press_init_x(Grid g, const int8_t* __restrict__ kind, const do
         if (kind[r] == 1) x[r] = b[r];
 }
 
+// a supplied start on the Pore rows: x = scale * start
+__global__ void k_press_start_x(Grid g, const int8_t* __restrict__ kind, const float* __restrict__ start,
+                                double scale, double* __restrict__ x) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x)
+        if (kind[r] >= 2) x[r] = scale * (double)start[r];
+}
+
+// A supplied start is kept only on the strong components (the multigrid's labelling) that
+// are anchored to fixed values: a component none of whose cells has a significant excess
+// (coupling to identity rows, e > 1e-3 of the row's diagonal) floats on links of ~1e-22 at
+// most. Its rows get 0, the value a zero start gives them and the solve leaves there when
+// their right-hand side is 0; a start that is not constant on such a component would have
+// to be smoothed out through its near-null modes.
+template <typename T>
+__global__ void k_start_anchor(Grid g, const int* __restrict__ comp, const T* __restrict__ e,
+                               const T* __restrict__ w0, const T* __restrict__ w1, const T* __restrict__ w2,
+                               uint8_t* __restrict__ anchored) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        const int id = comp[r];
+        if (id < 0) continue;
+        // the finest-level link arrays carry zero padding, so r - JK etc. are readable
+        const double links = (double)w0[r] + (double)w0[r - g.JK] + (double)w1[r] + (double)w1[r - g.K] +
+                             (double)w2[r] + (double)w2[r - 1];
+        const double ev = (double)e[r];
+        if (ev > 1e-3 * (ev + links)) anchored[id] = 1;
+    }
+}
+
+__global__ void k_start_unanchored(Grid g, const int8_t* __restrict__ kind, const int* __restrict__ comp,
+                                   const uint8_t* __restrict__ anchored, double* __restrict__ x) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        if (kind[r] < 2) continue;
+        const int id = comp[r];
+        if (id < 0 || !anchored[id]) x[r] = 0.0;
+    }
+}
+
+// Input fields of the learned start for the assembled system: the Pore-row mask, the
+// log-permeability (log10 K + 15) / 3, and the fixed values of the identity rows relative
+// to the effective top pressure (1 on the Air voxels that carry it, 0 elsewhere)
+__global__ void k_press_learned_inputs(Grid g, const int8_t* __restrict__ kind, const double* __restrict__ perm,
+                                       const double* __restrict__ b, double inv_top, float* __restrict__ mask,
+                                       float* __restrict__ logk, float* __restrict__ bc) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        const int kd = kind[r];
+        mask[r] = kd >= 2 ? 1.f : 0.f;
+        const double k = perm[r] > 1e-30 ? perm[r] : 1e-30;
+        logk[r] = (float)((log10(k) + 15.0) / 3.0);
+        bc[r] = kd == 1 ? (float)(b[r] * inv_top) : 0.f;
+    }
+}
+
 // (A x)_r for a Pore row: diag x_r + sum_d c_d x_nb, summed in ascending column order.
 __device__ __forceinline__ double press_row_apply(const Grid& g, long long r, int i, int j, int k,
                                                   double dg, const double* __restrict__ x,
@@ -800,7 +856,7 @@ ls_status pressure_apply_run(ls_ctx* c, const double* xh, double* yh) {
 }
 
 template <typename T>
-static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info) {
+static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info, const float* start, double start_scale) {
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
     double* x = c->P + (c->p.compat_shift ? g.JK : 0);
@@ -810,7 +866,9 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info) {
     bool inner_ready = false;
     {
         Timed tm(c, LS_T_PRESS_SETUP);
-        if (c->p.evaporative_flux == 0.0 && c->p_eff_prev > 0.0 && c->p_eff != c->p_eff_prev)
+        if (start)
+            LS_LAUNCH(c, k_press_start_x, grid, kBlock, 0, g, (const int8_t*)c->pkind, start, start_scale, x);
+        else if (c->p.evaporative_flux == 0.0 && c->p_eff_prev > 0.0 && c->p_eff != c->p_eff_prev)
             LS_LAUNCH(c, k_press_scale_x, grid, kBlock, 0, g, (const int8_t*)c->pkind,
                       c->p_eff / c->p_eff_prev, x);
         LS_LAUNCH(c, k_press_init_x, grid, kBlock, 0, g, (const int8_t*)c->pkind,
@@ -838,6 +896,18 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info) {
         if (use_mg) LS_TRY(mg_clear<T>(c));
         return LS_OK;
     };
+    if (start && use_mg) {
+        // build the inner operator and the components now, and keep the start only on the
+        // anchored components
+        LS_TRY(build_inner());
+        inner_ready = true;
+        if (!c->start_anchor) LS_TRY(dalloc_t(c, &c->start_anchor, (size_t)g.N));
+        LS_CUDA(c, cudaMemsetAsync(c->start_anchor, 0, (size_t)g.N, c->stream));
+        LS_LAUNCH(c, k_start_anchor<T>, grid, kBlock, 0, g, (const int*)c->comp, (const T*)c->ie,
+                  (const T*)c->iface[0], (const T*)c->iface[1], (const T*)c->iface[2], c->start_anchor);
+        LS_LAUNCH(c, k_start_unanchored, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const int*)c->comp,
+                  (const uint8_t*)c->start_anchor, x);
+    }
     double den = 0.0;
     LS_TRY(read_scalars(c, SP_DEN, 1, &den));
     const double rtol = c->p.press_rtol;
@@ -950,10 +1020,21 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info) {
     return result;
 }
 
-ls_status pressure_solve_run(ls_ctx* c, ls_solve_info* info) {
+ls_status pressure_solve_run(ls_ctx* c, ls_solve_info* info, const float* start, double start_scale) {
     if (!c->p_ready) return set_error(c, LS_BAD_ARG, "pressure system not assembled");
-    if (c->p.press_solver == LS_PRESS_MIXED) return pressure_solve_t<float>(c, info);
-    return pressure_solve_t<double>(c, info);
+    // a supplied start is relative to the effective (ramped) top pressure
+    const double sc = start ? start_scale * (c->p_eff > 0.0 ? c->p_eff : 1.0) : 0.0;
+    if (c->p.press_solver == LS_PRESS_MIXED) return pressure_solve_t<float>(c, info, start, sc);
+    return pressure_solve_t<double>(c, info, start, sc);
+}
+
+ls_status pressure_learned_inputs_run(ls_ctx* c, float* mask, float* logk, float* bc) {
+    if (!c->p_ready) return set_error(c, LS_BAD_ARG, "pressure system not assembled");
+    const double top = c->p_eff > 0.0 ? c->p_eff : 1.0;
+    LS_LAUNCH(c, k_press_learned_inputs, grid_for(c, c->g.N), kBlock, 0, c->g, (const int8_t*)c->pkind,
+              (const double*)c->perm, (const double*)c->pb, 1.0 / top, mask, logk, bc);
+    LS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return LS_OK;
 }
 
 }  // namespace ls

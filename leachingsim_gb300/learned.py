@@ -1,0 +1,204 @@
+"""The learned warm start of the pressure solve.
+
+The network (the U-shaped 3D convolutional network of ls_lpnet_*, hand-written CUDA
+kernels for its forward and backward passes and Adam) maps three fields of an assembled
+pressure system to a start for the solve:
+
+    mask  - 1 on the Pore rows (the unknowns), 0 elsewhere
+    logk  - (log10 K + 15) / 3
+    bc    - the fixed values of the identity rows over the effective top pressure
+
+and predicts the deviation of the pressure from the top pressure, d = 100 (1 - P / p_top),
+on the Pore rows (the start is P / p_top = 1 - d / 100). The pressure of the Pore space
+that the Air inlet reaches sits within a few percent of p_top, so this scaling gives the
+network targets of order one. The loss covers the Pore voxels of the components anchored
+to the inlet only: elsewhere the system is singular or nearly so, the solver keeps the
+zero start's value, and what the network says there is discarded (the solver zeroes a
+supplied start on unanchored components). It is trained only on solutions of the plain
+solver (mixed-precision multigrid FCG with FP64 refinement) on seeded synthetic
+geometries, 96^3 patches with porosity 0.15-0.40, correlation length 2-10 and mineral
+fraction 0.05-0.30, Air inlet planes as in the workload. At use, the start goes through
+ls_pressure_solve_start: the FP64 refinement rescales it once by its minimal-residual
+factor when that lowers the residual, judges it by the FP64 residual and finishes the
+solve with the plain solver, so a poor start costs iterations, never accuracy.
+
+    python -m leachingsim_gb300.learned train --samples 256 --epochs 16 --lr 2e-3 --seed 0
+
+writes lpnet_weights.npy beside this file (the weights shipped here were made so).
+"""
+import argparse
+import json
+import math
+import os
+import sys
+import time
+
+import numpy as np
+
+from . import _abi
+from .geometry import grf_geometry
+
+PATCH = (96, 96, 96)
+DEV_SCALE = 100.0  # network output d = DEV_SCALE (1 - P / p_top)
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lpnet_weights.npy")
+RAMP = 3600.0  # the top-pressure ramp of src/Simulation.cpp:662-670
+
+
+def pad8(shape):
+    return tuple(((int(v) + 7) // 8) * 8 for v in shape)
+
+
+def top_pressure(params, t):
+    """The effective (ramped) top pressure of the system assembled at time t."""
+    top = params.top_pressure
+    return top * (t / RAMP) + 1e-6 if t < RAMP else top
+
+
+def solver_params(**kw):
+    base = dict(c_sat=1.0, press_solver=_abi.PRESS_MIXED, press_rtol=1e-8)
+    base.update(kw)
+    return _abi.default_params(**base)
+
+
+def patch_geometry(seed, shape=PATCH):
+    """A seeded percolating patch with random porosity, correlation length and mineral
+    fraction (parameters redrawn while a draw finds no percolating field)."""
+    rng = np.random.default_rng(seed)
+    for _ in range(32):
+        por = rng.uniform(0.15, 0.40)
+        corr = rng.uniform(2.0, 10.0)
+        mineral = rng.uniform(0.05, 0.30)
+        try:
+            lab, used = grf_geometry(shape, porosity=por, corr_len=corr, mineral_fraction=mineral,
+                                     seed=int(rng.integers(1 << 30)), air_inlet=True, max_tries=8)
+        except RuntimeError:
+            continue
+        return lab, {"porosity": por, "corr_len": corr, "mineral_fraction": mineral, "seed": used}
+    raise RuntimeError(f"no percolating patch from seed {seed}")
+
+
+def _solution(ctx):
+    """x of the last pressure solve (the P slots, shifted by one plane in the reference's
+    write-back convention)."""
+    Pp = ctx.download("pressure", padded=True).ravel()
+    sh = ctx.J * ctx.K if ctx.params.compat_shift else 0
+    return Pp[sh:sh + ctx.N].reshape(ctx.shape)
+
+
+def make_sample(seed, shape=PATCH, t=RAMP, params=None):
+    """One training sample from the plain solver: the inputs (3 fields), the target
+    d = DEV_SCALE (1 - P / p_top) and the loss mask (the anchored Pore voxels)."""
+    import torch
+    from .runtime import Context
+    params = params or solver_params()
+    lab, meta = patch_geometry(seed, shape)
+    ctx = Context(shape, params=params)
+    try:
+        ctx.upload("label", lab)
+        ctx.init_all()
+        ctx.props()
+        ctx.pressure_setup(t)
+        m, k, b = ctx.pressure_learned_inputs()
+        ok, info = ctx.pressure_solve_start(torch.zeros(shape, dtype=torch.float32, device="cuda"), 0.0)
+        if not ok:
+            raise RuntimeError(f"plain solve failed on sample {seed}: {info}")
+        tau = torch.from_numpy(np.ascontiguousarray(_solution(ctx) / top_pressure(params, t),
+                                                    dtype=np.float32)).cuda()
+        # the components anchored to the inlet: Pore voxels the solution lifted off the zero
+        # start (the others keep 0)
+        anchored = m * (tau > 0.5).float()
+        target = DEV_SCALE * (1.0 - tau) * anchored
+    finally:
+        ctx.close()
+    return (m, k, b, target, anchored), dict(meta, iterations=info["iterations"],
+                                             anchored=float(anchored.sum() / max(float(m.sum()), 1.0)))
+
+
+def _pad(t, shape):
+    import torch
+    if tuple(t.shape) == tuple(shape):
+        return t.contiguous()
+    out = torch.zeros(shape, dtype=t.dtype, device=t.device)
+    out[:t.shape[0], :t.shape[1], :t.shape[2]] = t
+    return out
+
+
+class LearnedStart:
+    """A trained network sized for one grid (padded to multiples of 8)."""
+
+    def __init__(self, shape, params_flat):
+        from .runtime import LPNet
+        self.shape = tuple(shape)
+        self.net = LPNet(pad8(shape))
+        self.net.set_params(params_flat)
+
+    def start(self, ctx):
+        """The start (a torch CUDA float32 tensor of ctx's shape) for the system that
+        ctx.pressure_setup(t) assembled."""
+        m, k, b = ctx.pressure_learned_inputs()
+        ps = self.net.shape
+        out = self.net.forward(_pad(m, ps), _pad(k, ps), _pad(b, ps))
+        I, J, K = self.shape
+        return ((1.0 - out[:I, :J, :K] / DEV_SCALE) * m).contiguous()
+
+    def close(self):
+        self.net.close()
+
+
+def load_weights(path=WEIGHTS):
+    return np.load(path) if os.path.exists(path) else None
+
+
+def train(samples=256, epochs=16, lr=2e-3, seed=0, shape=PATCH, log=print):
+    """Generate samples with the plain solver and train a network on them; returns
+    (flat parameters, history)."""
+    from .runtime import LPNet
+    t0 = time.time()
+    data, metas = [], []
+    for s in range(samples):
+        d, meta = make_sample(seed * 100003 + s, shape)
+        data.append(d)
+        metas.append(meta)
+    gen_s = time.time() - t0
+    log(f"generated {samples} samples in {gen_s:.1f}s "
+        f"(mean plain iterations {np.mean([m['iterations'] for m in metas]):.1f})")
+    net = LPNet(shape, seed=seed)
+    rng = np.random.default_rng(seed)
+    hist = []
+    t1 = time.time()
+    steps = epochs * samples
+    for ep in range(epochs):
+        order = rng.permutation(samples)
+        losses = []
+        for q, i in enumerate(order):
+            step = ep * samples + q
+            rate = lr * 0.5 * (1.0 + math.cos(math.pi * step / steps))  # cosine decay
+            m, k, b, tgt, anchored = data[i]
+            losses.append(net.train_step(m, k, b, tgt, anchored, lr=rate))
+        hist.append(float(np.mean(losses)))
+        log(f"epoch {ep}: mean loss {hist[-1]:.3e}")
+    train_s = time.time() - t1
+    flat = net.get_params()
+    net.close()
+    return flat, {"samples": samples, "epochs": epochs, "lr": lr, "generate_s": round(gen_s, 1),
+                  "train_s": round(train_s, 1), "loss": hist}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    tr = sub.add_parser("train")
+    tr.add_argument("--samples", type=int, default=256)
+    tr.add_argument("--epochs", type=int, default=16)
+    tr.add_argument("--lr", type=float, default=2e-3)
+    tr.add_argument("--seed", type=int, default=0)
+    tr.add_argument("--out", default=WEIGHTS)
+    a = ap.parse_args(argv)
+    if a.cmd == "train":
+        flat, hist = train(a.samples, a.epochs, a.lr, a.seed, log=lambda *x: print(*x, file=sys.stderr, flush=True))
+        np.save(a.out, flat)
+        print(json.dumps(hist))
+
+
+if __name__ == "__main__":
+    main()

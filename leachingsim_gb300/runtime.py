@@ -69,6 +69,8 @@ SYMBOLS = {
     "ls_lpnet_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ls_lpnet_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_longlong, C.c_float, C.c_int, C.POINTER(C.c_double)]),
+    "ls_pressure_learned_inputs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ls_pressure_solve_start": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.POINTER(LsSolveInfo)]),
     "ls_geom_fracture": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ls_geom_classify": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                    C.c_int, C.c_void_p]),
@@ -370,6 +372,29 @@ class Context:
     def pressure(self, t):
         info = LsSolveInfo()
         st = self._check(load().ls_pressure_step(self.h, float(t), C.byref(info)), (0, 1, 2, 3))
+        return st in (0, 2), info.as_dict()
+
+    def pressure_learned_inputs(self):
+        """The learned start's input fields for the system assembled by pressure_setup(t):
+        (Pore-row mask, (log10 K + 15) / 3, identity-row values / top pressure), torch CUDA
+        float32 tensors of the grid's shape."""
+        import torch
+        out = [torch.empty(self.shape, dtype=torch.float32, device="cuda") for _ in range(3)]
+        torch.cuda.synchronize()
+        self._check(load().ls_pressure_learned_inputs(self.h, *[C.c_void_p(t.data_ptr()) for t in out]))
+        return tuple(out)
+
+    def pressure_solve_start(self, start, scale=1.0):
+        """Solve the assembled pressure system from x = scale * top pressure * start on the
+        Pore rows (start: torch CUDA float32 tensor of the grid's shape)."""
+        import torch
+        if tuple(start.shape) != self.shape or start.dtype != torch.float32 or not start.is_cuda:
+            raise ValueError("start must be a CUDA float32 tensor of the grid's shape")
+        start = start.contiguous()
+        info = LsSolveInfo()
+        torch.cuda.synchronize()
+        st = self._check(load().ls_pressure_solve_start(self.h, C.c_void_p(start.data_ptr()), float(scale),
+                                                        C.byref(info)), (0, 1, 2, 3))
         return st in (0, 2), info.as_dict()
 
     def flux(self):

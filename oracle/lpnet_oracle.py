@@ -8,7 +8,8 @@ this module's gradients by finite differences and the GPU kernels against this m
 
 Layout and arithmetic, as on the GPU:
 * activations are (D, H, W, C) arrays (channels innermost), stored as bfloat16 between
-  layers (`bf16` rounds float32 to the nearest bfloat16, ties to even);
+  layers (`bf16` rounds float32 to the nearest bfloat16, ties to even); the output layer
+  is float32;
 * a convolution is 3x3x3, stride 1, zero padding: out[z,y,x,co] = b[co] +
   sum_tap sum_ci w[tap,co,ci] in[z+dz,y+dy,x+dx,ci], tap = 9 (dz+1) + 3 (dy+1) + (dx+1);
   weights and inputs are bfloat16, sums are float32 on the GPU (float64 here);
@@ -115,11 +116,11 @@ def forward(p, x, round_bf16=True):
     wq = {n: r(p[n]) for n, *_ in LAYERS}
     c = {"x": r(x)}
 
-    def layer(name, inp, relu):
+    def layer(name, inp, relu, rnd=True):
         o = conv(inp, wq[name], p[name + "_b"])
         if relu:
             o = np.maximum(o, 0.0)
-        return r(o)
+        return r(o) if rnd else o
 
     c["a0"] = layer("W0a", c["x"], True)
     c["s0"] = layer("W0b", c["a0"], True)
@@ -134,7 +135,7 @@ def forward(p, x, round_bf16=True):
     c["u1"] = r(up(c["b2"]) + c["s1"])
     c["b1"] = layer("U1", c["u1"], True)
     c["u0"] = r(up(c["b1"]) + c["s0"])
-    c["y"] = layer("U0", c["u0"], False)
+    c["y"] = layer("U0", c["u0"], False, rnd=False)  # the output layer stays FP32
     c["wq"] = wq
     return c["y"], c
 
