@@ -13,8 +13,8 @@
 //  * pooling, upsampling + skip addition and their backward passes, ReLU masking, the
 //    masked mean-square loss and Adam.
 //
-// Layout: activations (D, H, W, C) with the channels innermost (BF16), gradients the same in
-// FP32; weights [tap][cout][cin], tap = 9 (dz+1) + 3 (dy+1) + (dx+1). D, H and W are
+// Layout: activations (D, H, W, C) with the channels innermost (BF16; the output layer FP32),
+// gradients the same in FP32; weights [tap][cout][cin], tap = 9 (dz+1) + 3 (dy+1) + (dx+1). D, H and W are
 // multiples of 8 (three 2x poolings).
 #include <cuda_bf16.h>
 
@@ -124,6 +124,100 @@ __global__ void __launch_bounds__(128) k_lp_conv(LpDims d, const bf16* __restric
             }
             if (ok0) store_pair<OutT>(out + r0 * COUT + co, c0, c1);
             if (ok1) store_pair<OutT>(out + r1 * COUT + co, c2, c3);
+        }
+    }
+}
+
+// The same convolution with the input tile staged in shared memory: a block computes a
+// 16 (x) x 4 (y) x 2 (z) tile of output voxels (8 rows of 16 along x, two per warp) from
+// an 18 x 6 x 4 halo tile loaded once with 16-byte loads (zeros outside the grid), and
+// every tap's A fragment is an ldmatrix.x4 of 16 rows gathered from the tile (lane l gives
+// the address of row l & 15, channel half l >> 4). A voxel occupies CIN + 8 BF16 in the
+// tile, so the eight 16-byte rows of one 8x8 matrix fall in distinct bank groups. The B
+// fragments (weights) come through L1 as before and serve both of a warp's rows.
+constexpr int kTX = 16, kTY = 4, kTZ = 2, kHX = kTX + 2, kHY = kTY + 2, kHZ = kTZ + 2;
+constexpr int kHalo = kHX * kHY * kHZ;
+
+__device__ __forceinline__ void ldmatrix_x4(uint32_t (&r)[4], uint32_t addr) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(addr));
+}
+
+template <int CIN, int COUT, bool RELU, typename OutT>
+__global__ void __launch_bounds__(128) k_lp_conv_tiled(LpDims d, const bf16* __restrict__ in,
+                                                       const bf16* __restrict__ w, const float* __restrict__ bias,
+                                                       OutT* __restrict__ out) {
+    static_assert(CIN % 16 == 0 && CIN <= 32 && COUT % 8 == 0, "channel counts");
+    constexpr int NT = COUT / 8, KC = CIN / 16, SC = CIN + 8, CH = CIN / 8;
+    __shared__ __align__(16) bf16 tile[kHalo * SC];
+    const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY, z0 = blockIdx.z * kTZ;
+    // halo tile: kHalo voxels x CH chunks of 8 channels (16 bytes)
+    for (int e = threadIdx.x; e < kHalo * CH; e += blockDim.x) {
+        const int hv = e / CH, q = e - hv * CH;
+        const int hx = hv % kHX, hy = (hv / kHX) % kHY, hz = hv / (kHX * kHY);
+        const int gx = x0 + hx - 1, gy = y0 + hy - 1, gz = z0 + hz - 1;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (gx >= 0 && gx < d.W && gy >= 0 && gy < d.H && gz >= 0 && gz < d.D)
+            v = __ldg(reinterpret_cast<const uint4*>(in + (((long long)gz * d.H + gy) * d.W + gx) * CIN) + q);
+        *reinterpret_cast<uint4*>(tile + hv * SC + q * 8) = v;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane >> 2, tg = lane & 3;
+    const int row = lane & 15, kofs = (lane >> 4) * 8;
+    const uint32_t tile_s = (uint32_t)__cvta_generic_to_shared(tile);
+    const uint32_t* __restrict__ w32 = reinterpret_cast<const uint32_t*>(w);
+    int yy[2], zz[2];
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+        const int mt = warp * 2 + m;  // 0..7
+        yy[m] = mt % kTY;
+        zz[m] = mt / kTY;
+    }
+    float acc[2][NT][4];
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int n = 0; n < NT; ++n) acc[m][n][0] = acc[m][n][1] = acc[m][n][2] = acc[m][n][3] = 0.f;
+    for (int t = 0; t < 27; ++t) {
+        const int dz = t / 9 - 1, dy = (t / 3) % 3 - 1, dx = t % 3 - 1;
+        uint32_t base[2];
+#pragma unroll
+        for (int m = 0; m < 2; ++m) {
+            const int hv = ((zz[m] + 1 + dz) * kHY + (yy[m] + 1 + dy)) * kHX + (row + 1 + dx);
+            base[m] = tile_s + (uint32_t)((hv * SC + kofs) * 2);
+        }
+#pragma unroll
+        for (int kc = 0; kc < KC; ++kc) {
+            uint32_t a[2][4];
+            ldmatrix_x4(a[0], base[0] + kc * 32);
+            ldmatrix_x4(a[1], base[1] + kc * 32);
+#pragma unroll
+            for (int n = 0; n < NT; ++n) {
+                const uint32_t* wp = w32 + ((size_t)t * COUT + n * 8 + g) * (CIN / 2);
+                const uint32_t b[2] = {__ldg(wp + kc * 8 + tg), __ldg(wp + kc * 8 + 4 + tg)};
+                mma_16816(acc[0][n], a[0], b);
+                mma_16816(acc[1][n], a[1], b);
+            }
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+        const int y = y0 + yy[m], z = z0 + zz[m];
+        if (y >= d.H || z >= d.D) continue;
+        const int xa = x0 + g, xb = x0 + g + 8;
+        const long long ra = ((long long)z * d.H + y) * d.W + xa, rb = ra + 8;
+#pragma unroll
+        for (int n = 0; n < NT; ++n) {
+            const int co = n * 8 + tg * 2;
+            const float b0 = bias ? bias[co] : 0.f, b1 = bias ? bias[co + 1] : 0.f;
+            float c0 = acc[m][n][0] + b0, c1 = acc[m][n][1] + b1, c2 = acc[m][n][2] + b0, c3 = acc[m][n][3] + b1;
+            if (RELU) {
+                c0 = fmaxf(c0, 0.f); c1 = fmaxf(c1, 0.f); c2 = fmaxf(c2, 0.f); c3 = fmaxf(c3, 0.f);
+            }
+            if (xa < d.W) store_pair<OutT>(out + ra * COUT + co, c0, c1);
+            if (xb < d.W) store_pair<OutT>(out + rb * COUT + co, c2, c3);
         }
     }
 }
@@ -294,13 +388,13 @@ __global__ void k_lp_mask(long long n, const float* __restrict__ d, const bf16* 
 
 // masked mean-square loss on output channel 0 and its gradient (16 channels, the others 0);
 // partial sums of the squared error per block
-__global__ void __launch_bounds__(kBlock) k_lp_loss(long long N, const bf16* __restrict__ y,
+__global__ void __launch_bounds__(kBlock) k_lp_loss(long long N, const float* __restrict__ y,
                                                     const float* __restrict__ target, const float* __restrict__ mask,
                                                     float inv_n, float* __restrict__ dy, double* __restrict__ partials) {
     double acc = 0.0;
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < N; v += (long long)gridDim.x * blockDim.x) {
         const float m = mask[v];
-        const float diff = (__bfloat162float(y[v * 16]) - target[v]) * m;
+        const float diff = (y[v * 16] - target[v]) * m;
         acc += (double)diff * diff;
         float4* o = reinterpret_cast<float4*>(dy + v * 16);
         o[0] = make_float4(2.f * diff * inv_n, 0.f, 0.f, 0.f);
@@ -311,9 +405,9 @@ __global__ void __launch_bounds__(kBlock) k_lp_loss(long long N, const bf16* __r
 }
 
 // output channel 0 to FP32
-__global__ void k_lp_out(long long N, const bf16* __restrict__ y, float* __restrict__ out) {
+__global__ void k_lp_out(long long N, const float* __restrict__ y, float* __restrict__ out) {
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < N; v += (long long)gridDim.x * blockDim.x)
-        out[v] = __bfloat162float(y[v * 16]);
+        out[v] = y[v * 16];
 }
 
 // Adam on the FP32 master parameters; the BF16 copy of every weight follows
@@ -381,7 +475,8 @@ struct ls_lpnet {
     bf16* wt;               // BF16 transposed, flipped weights (input gradients)
     int adam_t;
     // activations (BF16) per level
-    bf16 *x, *a0, *s0, *p1, *s1, *p2, *s2, *p3, *a3, *u2, *b2, *u1, *b1, *u0, *y;
+    bf16 *x, *a0, *s0, *p1, *s1, *p2, *s2, *p3, *a3, *u2, *b2, *u1, *b1, *u0;
+    float* y;               // FP32 output layer (16 channels, channel 0 used)
     // gradients (FP32)
     float *gy, *g0, *g0b, *g1, *g1b, *g2, *g2b, *g3, *g3b;
     bf16* q;                // BF16 masked gradient scratch
@@ -435,6 +530,17 @@ int lp_grid(const ls_lpnet* n, long long work, int block) {
 template <bool RELU, typename OutT>
 ls_status lp_conv(ls_lpnet* n, LpDims d, int cin, int cout, const bf16* in, const bf16* w, const float* bias,
                   OutT* out) {
+    if (cin <= 32) {
+        const dim3 tg((unsigned)((d.W + ls::kTX - 1) / ls::kTX), (unsigned)((d.H + ls::kTY - 1) / ls::kTY),
+                      (unsigned)((d.D + ls::kTZ - 1) / ls::kTZ));
+#define LP_TCASE(CI, CO)                                                                         \
+        if (cin == CI && cout == CO) {                                                           \
+            LP_LAUNCH(n, (ls::k_lp_conv_tiled<CI, CO, RELU, OutT>), tg, 128, d, in, w, bias, out); \
+            return LS_OK;                                                                        \
+        }
+        LP_TCASE(16, 16) LP_TCASE(16, 32) LP_TCASE(32, 64) LP_TCASE(32, 16)
+#undef LP_TCASE
+    }
     const int grid = lp_grid(n, (d.N + 15) / 16, 4);
 #define LP_CASE(CI, CO)                                                                        \
     if (cin == CI && cout == CO) {                                                             \
@@ -490,7 +596,7 @@ ls_status lp_forward(ls_lpnet* n, const float* c0, const float* c1, const float*
     LP_LAUNCH(n, ls::k_lp_up_add, lp_grid(n, d1.N * 32, 256), 256, d1, 32, (const bf16*)n->b2, (const bf16*)n->s1, n->u1);
     LS_TRY((lp_conv<true, bf16>(n, d1, 32, 16, n->u1, wb(6), bias(6), n->b1)));
     LP_LAUNCH(n, ls::k_lp_up_add, lp_grid(n, d0.N * 16, 256), 256, d0, 16, (const bf16*)n->b1, (const bf16*)n->s0, n->u0);
-    LS_TRY((lp_conv<false, bf16>(n, d0, 16, 16, n->u0, wb(7), bias(7), n->y)));
+    LS_TRY((lp_conv<false, float>(n, d0, 16, 16, n->u0, wb(7), bias(7), n->y)));
     return LS_OK;
 }
 
@@ -503,11 +609,28 @@ ls_status lp_layer_bwd(ls_lpnet* n, int l, LpDims d, const bf16* in, const bf16*
     return LS_OK;
 }
 
+// the gradient buffers, allocated by the first training step (inference needs none)
+ls_status lp_alloc_grads(ls_lpnet* n) {
+    if (n->gy) return LS_OK;
+    const long long v0 = (long long)n->D * n->H * n->W, v1 = v0 / 8, v2 = v0 / 64, v3 = v0 / 512;
+    LS_TRY(lp_alloc(n, &n->gy, v0 * 16));
+    LS_TRY(lp_alloc(n, &n->g0, v0 * 16));
+    LS_TRY(lp_alloc(n, &n->g0b, v0 * 16));
+    LS_TRY(lp_alloc(n, &n->g1, v1 * 32));
+    LS_TRY(lp_alloc(n, &n->g1b, v1 * 16));
+    LS_TRY(lp_alloc(n, &n->g2, v2 * 64));
+    LS_TRY(lp_alloc(n, &n->g2b, v2 * 32));
+    LS_TRY(lp_alloc(n, &n->g3, v3 * 64));
+    LS_TRY(lp_alloc(n, &n->g3b, v3 * 64));
+    LS_TRY(lp_alloc(n, &n->q, v0 * 16));
+    return LS_OK;
+}
+
 ls_status lp_backward(ls_lpnet* n) {
     const LpDims d0 = ls::lp_dims(n->D, n->H, n->W), d1 = ls::lp_dims(n->D / 2, n->H / 2, n->W / 2),
                  d2 = ls::lp_dims(n->D / 4, n->H / 4, n->W / 4), d3 = ls::lp_dims(n->D / 8, n->H / 8, n->W / 8);
     LP_CUDA(n, cudaMemsetAsync(n->g, 0, sizeof(float) * n->nparam, n->stream));
-    LS_TRY(lp_layer_bwd(n, 7, d0, n->u0, n->y, n->gy, n->g0));                     // d_u0 = d_s0 (partial)
+    LS_TRY(lp_layer_bwd(n, 7, d0, n->u0, nullptr, n->gy, n->g0));                  // d_u0 = d_s0 (partial)
     LP_LAUNCH(n, ls::k_lp_up_bwd, lp_grid(n, d1.N * 16, 256), 256, d1, 16, (const float*)n->g0, n->g1b);  // d_b1
     LS_TRY(lp_layer_bwd(n, 6, d1, n->u1, n->b1, n->g1b, n->g1));                    // d_u1
     LP_LAUNCH(n, ls::k_lp_up_bwd, lp_grid(n, d2.N * 32, 256), 256, d2, 32, (const float*)n->g1, n->g2b);  // d_b2
@@ -575,16 +698,6 @@ ls_status ls_lpnet_create(int D, int H, int W, int seed, ls_lpnet** out) {
         LS_TRY(lp_alloc(n, &n->b1, v1 * 16));
         LS_TRY(lp_alloc(n, &n->u0, v0 * 16));
         LS_TRY(lp_alloc(n, &n->y, v0 * 16));
-        LS_TRY(lp_alloc(n, &n->gy, v0 * 16));
-        LS_TRY(lp_alloc(n, &n->g0, v0 * 16));
-        LS_TRY(lp_alloc(n, &n->g0b, v0 * 16));
-        LS_TRY(lp_alloc(n, &n->g1, v1 * 32));
-        LS_TRY(lp_alloc(n, &n->g1b, v1 * 16));
-        LS_TRY(lp_alloc(n, &n->g2, v2 * 64));
-        LS_TRY(lp_alloc(n, &n->g2b, v2 * 32));
-        LS_TRY(lp_alloc(n, &n->g3, v3 * 64));
-        LS_TRY(lp_alloc(n, &n->g3b, v3 * 64));
-        LS_TRY(lp_alloc(n, &n->q, v0 * 16));
         LS_TRY(lp_alloc(n, &n->out, v0));
         LS_TRY(lp_alloc(n, &n->partials, (size_t)n->num_sms * 16));
         if (cudaMallocHost(&n->h_loss, sizeof(double)) != cudaSuccess) return LS_CUDA_ERROR;
@@ -671,7 +784,7 @@ ls_status ls_lpnet_forward(ls_lpnet* n, const float* c0, const float* c1, const 
     if (!n || !c0 || !c1 || !c2 || !out) return LS_BAD_ARG;
     LS_TRY(lp_forward(n, c0, c1, c2));
     const long long N = (long long)n->D * n->H * n->W;
-    LP_LAUNCH(n, ls::k_lp_out, lp_grid(n, N, 256), 256, N, (const bf16*)n->y, out);
+    LP_LAUNCH(n, ls::k_lp_out, lp_grid(n, N, 256), 256, N, (const float*)n->y, out);
     LP_CUDA(n, cudaStreamSynchronize(n->stream));
     return LS_OK;
 }
@@ -679,10 +792,11 @@ ls_status ls_lpnet_forward(ls_lpnet* n, const float* c0, const float* c1, const 
 ls_status ls_lpnet_train_step(ls_lpnet* n, const float* c0, const float* c1, const float* c2, const float* target,
                               const float* mask, long long mask_count, float lr, int update, double* loss) {
     if (!n || !c0 || !c1 || !c2 || !target || !mask || mask_count < 1 || !(lr >= 0.f)) return LS_BAD_ARG;
+    LS_TRY(lp_alloc_grads(n));
     LS_TRY(lp_forward(n, c0, c1, c2));
     const long long N = (long long)n->D * n->H * n->W;
     const int nb = lp_grid(n, N, ls::kBlock);
-    LP_LAUNCH(n, ls::k_lp_loss, nb, ls::kBlock, N, (const bf16*)n->y, target, mask, (float)(1.0 / (double)mask_count),
+    LP_LAUNCH(n, ls::k_lp_loss, nb, ls::kBlock, N, (const float*)n->y, target, mask, (float)(1.0 / (double)mask_count),
               n->gy, n->partials);
     LS_TRY(lp_backward(n));
     if (update) {

@@ -71,9 +71,11 @@ def test_parameter_layout_round_trip():
 
 
 @pytest.mark.gpu
-def test_gpu_forward_matches_oracle():
+@pytest.mark.parametrize("shape", [(16, 16, 24), (24, 40, 8), (8, 24, 56)])
+def test_gpu_forward_matches_oracle(shape):
+    """Grids whose extents are not multiples of the 16 x 4 x 2 convolution tile, down to
+    coarse levels of odd extent."""
     from leachingsim_gb300.runtime import LPNet, lpnet_flatten
-    shape = (16, 16, 24)
     p, mask, c1, c2, _ = _case(shape, 1)
     net = LPNet(shape)
     net.set_params(lpnet_flatten(p))
