@@ -283,6 +283,10 @@ ls_status ls_geom_clean(int I, int J, int K, int label_bytes, void* labels_host,
                         long long* changed);
 ls_status ls_geom_fracture(int I, int J, int K, int label_bytes, void* labels_host, long long* drilled,
                            long long* encapsulated);
+/* Euclidean distance of every voxel to the nearest site (sites[v] > 0.5; -1 where there is
+   no site), exact, through the same feature transform as ls_geom_fracture; DEVICE float32
+   arrays of I*J*K values, synchronous. */
+ls_status ls_geom_distance(int I, int J, int K, const float* sites, float* dist);
 ls_status ls_geom_classify(int I, int J, int K, const uint16_t* grey_host, int n_thresholds,
                            const uint16_t* thresholds, const int* labels, int label_bytes,
                            void* out_host);

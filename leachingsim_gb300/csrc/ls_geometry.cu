@@ -336,6 +336,30 @@ __global__ void k_ft_pass(Dims d, int* __restrict__ feat, int* __restrict__ st_s
     }
 }
 
+// sites of a float mask (> 0.5) for the distance transform
+__global__ void k_ft_init_mask(Dims d, const float* __restrict__ sites, int* __restrict__ feat) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < d.N;
+         r += (long long)gridDim.x * blockDim.x)
+        feat[r] = sites[r] > 0.5f ? (int)r : -1;
+}
+
+// Euclidean distance to the nearest site (-1 when there is none)
+__global__ void k_ft_distance(Dims d, const int* __restrict__ feat, float* __restrict__ dist) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < d.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        const int f = feat[r];
+        if (f < 0) {
+            dist[r] = -1.f;
+            continue;
+        }
+        int i, j, k, a, b, c;
+        gdecode(d, r, i, j, k);
+        gdecode(d, f, a, b, c);
+        const double di = a - i, dj = b - j, dk = c - k;
+        dist[r] = (float)sqrt(di * di + dj * dj + dk * dk);
+    }
+}
+
 // one coordinate of numpy.linspace(s, p, num)[t] rounded half to even: the step is
 // (p - s) / (num - 1), the point t * step + s (no fused multiply-add), the last point p
 __device__ __forceinline__ int lin_point(int s, int p, long long t, long long num) {
@@ -610,6 +634,29 @@ extern "C" ls_status ls_geom_fracture(int I, int J, int K, int label_bytes, void
     if (label_bytes == 1) return ls::fracture_t<uint8_t>(I, J, K, labels_host, drilled, encapsulated);
     if (label_bytes == 2) return ls::fracture_t<uint16_t>(I, J, K, labels_host, drilled, encapsulated);
     return LS_BAD_ARG;
+}
+
+extern "C" ls_status ls_geom_distance(int I, int J, int K, const float* sites, float* dist) {
+    if (!sites || !dist || !ls::dims_ok(I, J, K)) return LS_BAD_ARG;
+    ls::Dims d{I, J, K, (long long)J * K, (long long)I * J * K};
+    ls::Scratch s;
+    int *feat, *st_site, *st_pos;
+    long long* st_perp;
+    if (!s.get(&feat, d.N) || !s.get(&st_site, d.N) || !s.get(&st_pos, d.N) || !s.get(&st_perp, d.N))
+        return LS_CUDA_ERROR;
+    const int grid = ls::geo_grid(d.N);
+    ls::k_ft_init_mask<<<grid, 256>>>(d, sites, feat);
+    GEO_LAUNCH();
+    ls::k_ft_pass<0><<<ls::geo_grid(d.JK), 256>>>(d, feat, st_site, st_pos, st_perp);
+    GEO_LAUNCH();
+    ls::k_ft_pass<1><<<ls::geo_grid((long long)d.I * d.K), 256>>>(d, feat, st_site, st_pos, st_perp);
+    GEO_LAUNCH();
+    ls::k_ft_pass<2><<<ls::geo_grid((long long)d.I * d.J), 256>>>(d, feat, st_site, st_pos, st_perp);
+    GEO_LAUNCH();
+    ls::k_ft_distance<<<grid, 256>>>(d, feat, dist);
+    GEO_LAUNCH();
+    GEO_CHECK(cudaDeviceSynchronize());
+    return LS_OK;
 }
 
 extern "C" ls_status ls_geom_classify(int I, int J, int K, const uint16_t* grey_host, int n_thresholds,

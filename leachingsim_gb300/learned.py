@@ -6,7 +6,9 @@ pressure system to a start for the solve:
 
     mask  - 1 on the Pore rows (the unknowns), 0 elsewhere
     logk  - (log10 K + 15) / 3
-    bc    - the fixed values of the identity rows over the effective top pressure
+    dist  - the Euclidean distance to the nearest voxel that carries the top pressure
+            (ls_geom_distance), over 100: the pressure of the Pore space falls off with
+            it, on scales beyond the network's receptive field
 
 and predicts the deviation of the pressure from the top pressure, d = 100 (1 - P / p_top),
 on the Pore rows (the start is P / p_top = 1 - d / 100). The pressure of the Pore space
@@ -16,13 +18,15 @@ to the inlet only: elsewhere the system is singular or nearly so, the solver kee
 zero start's value, and what the network says there is discarded (the solver zeroes a
 supplied start on unanchored components). It is trained only on solutions of the plain
 solver (mixed-precision multigrid FCG with FP64 refinement) on seeded synthetic
-geometries, 96^3 patches with porosity 0.15-0.40, correlation length 2-10 and mineral
-fraction 0.05-0.30, Air inlet planes as in the workload. At use, the start goes through
+geometries with porosity 0.15-0.40, correlation length 2-10 and mineral fraction
+0.05-0.30, Air inlet planes as in the workload, as columns of the workload's depth
+(288 x 64 x 64): how far the pressure falls depends on the depth of the Pore space behind
+a voxel, which 96^3 patches do not show. At use, the start goes through
 ls_pressure_solve_start: the FP64 refinement rescales it once by its minimal-residual
 factor when that lowers the residual, judges it by the FP64 residual and finishes the
 solve with the plain solver, so a poor start costs iterations, never accuracy.
 
-    python -m leachingsim_gb300.learned train --samples 256 --epochs 16 --lr 2e-3 --seed 0
+    python -m leachingsim_gb300.learned train --samples 192 --epochs 16 --lr 2e-3 --seed 0
 
 writes lpnet_weights.npy beside this file (the weights shipped here were made so).
 """
@@ -38,8 +42,9 @@ import numpy as np
 from . import _abi
 from .geometry import grf_geometry
 
-PATCH = (96, 96, 96)
-DEV_SCALE = 100.0  # network output d = DEV_SCALE (1 - P / p_top)
+PATCH = (288, 64, 64)
+DEV_SCALE = 100.0   # network output d = DEV_SCALE (1 - P / p_top)
+DIST_SCALE = 100.0  # the distance input is dist / DIST_SCALE
 WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lpnet_weights.npy")
 RAMP = 3600.0  # the top-pressure ramp of src/Simulation.cpp:662-670
 
@@ -99,6 +104,7 @@ def make_sample(seed, shape=PATCH, t=RAMP, params=None):
         ctx.props()
         ctx.pressure_setup(t)
         m, k, b = ctx.pressure_learned_inputs()
+        dist = distance_input(b)
         ok, info = ctx.pressure_solve_start(torch.zeros(shape, dtype=torch.float32, device="cuda"), 0.0)
         if not ok:
             raise RuntimeError(f"plain solve failed on sample {seed}: {info}")
@@ -110,8 +116,16 @@ def make_sample(seed, shape=PATCH, t=RAMP, params=None):
         target = DEV_SCALE * (1.0 - tau) * anchored
     finally:
         ctx.close()
-    return (m, k, b, target, anchored), dict(meta, iterations=info["iterations"],
+    return (m, k, dist, target, anchored), dict(meta, iterations=info["iterations"],
                                              anchored=float(anchored.sum() / max(float(m.sum()), 1.0)))
+
+
+def distance_input(bc):
+    """The third input: distance to the voxels carrying the top pressure, over DIST_SCALE
+    (0 where no voxel carries it)."""
+    from .runtime import geom_distance
+    d = geom_distance((bc > 0.5).float())
+    return (d.clamp_min(0.0) / DIST_SCALE).contiguous()
 
 
 def _pad(t, shape):
@@ -137,7 +151,7 @@ class LearnedStart:
         ctx.pressure_setup(t) assembled."""
         m, k, b = ctx.pressure_learned_inputs()
         ps = self.net.shape
-        out = self.net.forward(_pad(m, ps), _pad(k, ps), _pad(b, ps))
+        out = self.net.forward(_pad(m, ps), _pad(k, ps), _pad(distance_input(b), ps))
         I, J, K = self.shape
         return ((1.0 - out[:I, :J, :K] / DEV_SCALE) * m).contiguous()
 
@@ -149,7 +163,7 @@ def load_weights(path=WEIGHTS):
     return np.load(path) if os.path.exists(path) else None
 
 
-def train(samples=256, epochs=16, lr=2e-3, seed=0, shape=PATCH, log=print):
+def train(samples=192, epochs=16, lr=2e-3, seed=0, shape=PATCH, log=print):
     """Generate samples with the plain solver and train a network on them; returns
     (flat parameters, history)."""
     from .runtime import LPNet
@@ -173,8 +187,8 @@ def train(samples=256, epochs=16, lr=2e-3, seed=0, shape=PATCH, log=print):
         for q, i in enumerate(order):
             step = ep * samples + q
             rate = lr * 0.5 * (1.0 + math.cos(math.pi * step / steps))  # cosine decay
-            m, k, b, tgt, anchored = data[i]
-            losses.append(net.train_step(m, k, b, tgt, anchored, lr=rate))
+            m, k, dist, tgt, anchored = data[i]
+            losses.append(net.train_step(m, k, dist, tgt, anchored, lr=rate))
         hist.append(float(np.mean(losses)))
         log(f"epoch {ep}: mean loss {hist[-1]:.3e}")
     train_s = time.time() - t1
@@ -188,7 +202,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     sub = ap.add_subparsers(dest="cmd", required=True)
     tr = sub.add_parser("train")
-    tr.add_argument("--samples", type=int, default=256)
+    tr.add_argument("--samples", type=int, default=192)
     tr.add_argument("--epochs", type=int, default=16)
     tr.add_argument("--lr", type=float, default=2e-3)
     tr.add_argument("--seed", type=int, default=0)

@@ -71,6 +71,7 @@ SYMBOLS = {
                                       C.c_longlong, C.c_float, C.c_int, C.POINTER(C.c_double)]),
     "ls_pressure_learned_inputs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ls_pressure_solve_start": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.POINTER(LsSolveInfo)]),
+    "ls_geom_distance": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     "ls_geom_fracture": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ls_geom_classify": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                    C.c_int, C.c_void_p]),
@@ -161,6 +162,18 @@ def geom_fracture(labels):
     _geom_check(load().ls_geom_fracture(*lab.shape, lab.itemsize, _p(lab), C.byref(n), C.byref(ne)),
                 "ls_geom_fracture")
     return lab, int(n.value), int(ne.value)
+
+
+def geom_distance(sites):
+    """Euclidean distance to the nearest site (sites > 0.5) of a torch CUDA float32 (I, J, K)
+    tensor; -1 where there is no site."""
+    import torch
+    t = sites.to(device="cuda", dtype=torch.float32).contiguous()
+    out = torch.empty_like(t)
+    torch.cuda.synchronize()
+    _geom_check(load().ls_geom_distance(*t.shape, C.c_void_p(t.data_ptr()), C.c_void_p(out.data_ptr())),
+                "ls_geom_distance")
+    return out
 
 
 def geom_classify(grey, thresholds, labels, label_bytes=1):

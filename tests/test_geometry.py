@@ -162,3 +162,18 @@ def test_gpu_fracture_edge_cases():
     # no Pore voxel at all: refused
     with pytest.raises(RuntimeError):
         geom_fracture(np.full((3, 4, 5), 4, np.uint8))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape,seed", [((20, 17, 33), 1), ((1, 40, 9), 2), ((12, 12, 12), 3)])
+def test_gpu_distance_matches_scipy(shape, seed):
+    import torch
+    from scipy import ndimage
+    from leachingsim_gb300.runtime import geom_distance
+    rng = np.random.default_rng(seed)
+    sites = (rng.random(shape) < 0.05).astype(np.float32)
+    sites.flat[0] = 1.0
+    d = geom_distance(torch.from_numpy(sites).cuda()).cpu().numpy()
+    ref = ndimage.distance_transform_edt(sites < 0.5)
+    np.testing.assert_allclose(d, ref, rtol=1e-6, atol=1e-6)
+    assert np.all(geom_distance(torch.zeros(shape).cuda()).cpu().numpy() == -1.0)
