@@ -201,6 +201,8 @@ def cold_pressure_solves(ctx, shape, solver, reps=2):
     variants = [("plain_fp64", PRESS_FP64, None), ("plain", PRESS_MIXED, None)]
     if ls is not None:
         variants.append(("learned", PRESS_MIXED, ls))
+    # context for the learned start: the untrained guess P = p_top on every Pore row
+    variants.append(("constant_start", PRESS_MIXED, "constant"))
     ctx.props()
     out = {}
     for name, s, start in variants:
@@ -213,7 +215,10 @@ def cold_pressure_solves(ctx, shape, solver, reps=2):
             w0 = time.perf_counter()
             ctx.pressure_setup(0.0)
             w1 = time.perf_counter()
-            x0 = start.start(ctx) if start is not None else zeros
+            if start == "constant":
+                x0 = ctx.pressure_learned_inputs()[0]
+            else:
+                x0 = start.start(ctx) if start is not None else zeros
             torch.cuda.synchronize()
             w2 = time.perf_counter()
             ok, info = ctx.pressure_solve_start(x0, 1.0 if start is not None else 0.0)
@@ -224,7 +229,7 @@ def cold_pressure_solves(ctx, shape, solver, reps=2):
                      "iterations": info["iterations"], "outer": info["outer_iterations"],
                      "scaled_rel_residual": info["rel_residual"], "converged": bool(ok)}
         if start is not None:
-            out[name]["inference_ms"] = round((w2 - w1) * 1e3, 3)
+            out[name]["start_ms"] = round((w2 - w1) * 1e3, 3)
     if ls is not None:
         ls.close()
     ctx.set_params(params(solver))
@@ -278,9 +283,10 @@ def gpu_arm(args, ws, rank, local):
                             "converged": bool(pinfo["converged"])}
     psolve.setdefault("learned", None)
     psolve["note"] = ("cold solves of the first step's pressure system: t = 0, zero start (learned: the "
-                      "network's start), rtol 1e-8 on the Jacobi-scaled FP64 residual; ms = assembly + "
-                      "[inference] + multigrid setup + solve; first_step = the run's own first step "
-                      "(device timers)")
+                      "network's start; constant_start: P = p_top on the Pore rows), rtol 1e-8 on the "
+                      "Jacobi-scaled FP64 residual; ms = assembly + [start: inputs, distance transform, "
+                      "network] + multigrid setup + solve; first_step = the run's own first step (device "
+                      "timers)")
     ctx.timing(False)
     t, n, _ = run_steps(ctx, t, n, max(args.warmup - 1, 0), DT)
     ctx.timing(True)

@@ -314,6 +314,13 @@ ls_status ls_lpnet_train_step(ls_lpnet* net, const float* c0, const float* c1, c
                               const float* target, const float* mask, long long mask_count, float lr,
                               int update, double* loss);
 
+/* Half-resolution transfers of a D x H x W float32 field (D, H, W even; DEVICE pointers,
+   synchronous): ls_field_pool2 writes the (weighted) mean of every 2x2x2 block, weight may
+   be null (plain mean; a block of zero weight gets 0); ls_field_up2 repeats each coarse
+   value over its block. The learned start runs the network at half resolution. */
+ls_status ls_field_pool2(int D, int H, int W, const float* fine, const float* weight, float* coarse);
+ls_status ls_field_up2(int D, int H, int W, const float* coarse, float* fine);
+
 /* Per-kernel-class device timing (CUDA events on the context stream). */
 typedef enum ls_timer {
     LS_T_PROPS = 0,

@@ -436,6 +436,37 @@ __global__ void k_lp_cast(long long n, const float* __restrict__ p, const int* _
     }
 }
 
+// coarse = sum(fine * wt) / sum(wt) over each 2x2x2 block (wt null: the mean; a block with
+// no weight: 0); coarse dims dc, fine dims 2 dc
+__global__ void k_lp_field_pool(LpDims dc, const float* __restrict__ fine, const float* __restrict__ wt,
+                                float* __restrict__ coarse) {
+    const int Wf = dc.W * 2, Hf = dc.H * 2;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < dc.N; v += (long long)gridDim.x * blockDim.x) {
+        int z, y, x;
+        lp_decode(dc, v, z, y, x);
+        float s = 0.f, sw = 0.f;
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b)
+                for (int q = 0; q < 2; ++q) {
+                    const long long f = (((long long)(2 * z + a) * Hf) + 2 * y + b) * Wf + 2 * x + q;
+                    const float w = wt ? wt[f] : 1.f;
+                    s += w * fine[f];
+                    sw += w;
+                }
+        coarse[v] = sw > 0.f ? s / sw : 0.f;
+    }
+}
+
+// fine = coarse(parent), fine dims df (even)
+__global__ void k_lp_field_up(LpDims df, const float* __restrict__ coarse, float* __restrict__ fine) {
+    const int Wc = df.W / 2, Hc = df.H / 2;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < df.N; v += (long long)gridDim.x * blockDim.x) {
+        int z, y, x;
+        lp_decode(df, v, z, y, x);
+        fine[v] = coarse[(((long long)(z / 2) * Hc) + y / 2) * Wc + x / 2];
+    }
+}
+
 }  // namespace
 }  // namespace ls
 
@@ -813,6 +844,26 @@ ls_status ls_lpnet_train_step(ls_lpnet* n, const float* c0, const float* c1, con
     double sum = 0.0;
     for (double v : part) sum += v;
     if (loss) *loss = sum / (double)mask_count;
+    return LS_OK;
+}
+
+ls_status ls_field_pool2(int D, int H, int W, const float* fine, const float* weight, float* coarse) {
+    if (!fine || !coarse || D < 2 || H < 2 || W < 2 || D % 2 || H % 2 || W % 2) return LS_BAD_ARG;
+    const LpDims dc = ls::lp_dims(D / 2, H / 2, W / 2);
+    long long b = (dc.N + 255) / 256;
+    if (b > 4096) b = 4096;
+    ls::k_lp_field_pool<<<(int)b, 256>>>(dc, fine, weight, coarse);
+    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return LS_CUDA_ERROR;
+    return LS_OK;
+}
+
+ls_status ls_field_up2(int D, int H, int W, const float* coarse, float* fine) {
+    if (!fine || !coarse || D < 2 || H < 2 || W < 2 || D % 2 || H % 2 || W % 2) return LS_BAD_ARG;
+    const LpDims df = ls::lp_dims(D, H, W);
+    long long b = (df.N + 255) / 256;
+    if (b > 4096) b = 4096;
+    ls::k_lp_field_up<<<(int)b, 256>>>(df, coarse, fine);
+    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return LS_CUDA_ERROR;
     return LS_OK;
 }
 

@@ -11,7 +11,11 @@ pressure system to a start for the solve:
             it, on scales beyond the network's receptive field
 
 and predicts the deviation of the pressure from the top pressure, d = 100 (1 - P / p_top),
-on the Pore rows (the start is P / p_top = 1 - d / 100). The pressure of the Pore space
+on the Pore rows (the start is P / p_top = 1 - d / 100). The network runs at half
+resolution: its inputs are the 2x2x2 block means of the three fields (ls_field_pool2), its
+output is repeated over each block (ls_field_up2); the deviation varies on the scale of
+the distance to the inlet, and the half-resolution network costs an eighth of the
+full-resolution one. The pressure of the Pore space
 that the Air inlet reaches sits within a few percent of p_top, so this scaling gives the
 network targets of order one. The loss covers the Pore voxels of the components anchored
 to the inlet only: elsewhere the system is singular or nearly so, the solver keeps the
@@ -26,7 +30,7 @@ ls_pressure_solve_start: the FP64 refinement rescales it once by its minimal-res
 factor when that lowers the residual, judges it by the FP64 residual and finishes the
 solve with the plain solver, so a poor start costs iterations, never accuracy.
 
-    python -m leachingsim_gb300.learned train --samples 192 --epochs 16 --lr 2e-3 --seed 0
+    python -m leachingsim_gb300.learned train --samples 256 --epochs 64 --lr 2e-3 --seed 0
 
 writes lpnet_weights.npy beside this file (the weights shipped here were made so).
 """
@@ -51,6 +55,18 @@ RAMP = 3600.0  # the top-pressure ramp of src/Simulation.cpp:662-670
 
 def pad8(shape):
     return tuple(((int(v) + 7) // 8) * 8 for v in shape)
+
+
+def pad16(shape):
+    """The fine grid of the learned start: multiples of 16, so that the half-resolution
+    network's grid is a multiple of 8."""
+    return tuple(((int(v) + 15) // 16) * 16 for v in shape)
+
+
+def coarse_inputs(m, k, dist):
+    """The network's inputs: 2x2x2 block means of the three fine fields (extents even)."""
+    from .runtime import field_pool2
+    return field_pool2(m), field_pool2(k), field_pool2(dist)
 
 
 def top_pressure(params, t):
@@ -91,8 +107,9 @@ def _solution(ctx):
 
 
 def make_sample(seed, shape=PATCH, t=RAMP, params=None):
-    """One training sample from the plain solver: the inputs (3 fields), the target
-    d = DEV_SCALE (1 - P / p_top) and the loss mask (the anchored Pore voxels)."""
+    """One training sample from the plain solver, at the network's half resolution: the
+    inputs (3 fields), the target d = DEV_SCALE (1 - P / p_top) averaged over the anchored
+    Pore voxels of each block, and the loss mask (the blocks holding any)."""
     import torch
     from .runtime import Context
     params = params or solver_params()
@@ -114,10 +131,16 @@ def make_sample(seed, shape=PATCH, t=RAMP, params=None):
         # start (the others keep 0)
         anchored = m * (tau > 0.5).float()
         target = DEV_SCALE * (1.0 - tau) * anchored
+        from .runtime import field_pool2
+        fs = pad16(shape)
+        m, k, dist, target, anchored = (_pad(v, fs) for v in (m, k, dist, target, anchored))
+        mc, kc, dc = coarse_inputs(m, k, dist)
+        tc = field_pool2(target, anchored)                   # mean over the anchored voxels
+        ac = (field_pool2(anchored) > 0.0).float()           # blocks holding any
     finally:
         ctx.close()
-    return (m, k, dist, target, anchored), dict(meta, iterations=info["iterations"],
-                                             anchored=float(anchored.sum() / max(float(m.sum()), 1.0)))
+    return (mc, kc, dc, tc, ac), dict(meta, iterations=info["iterations"],
+                                      anchored=float(anchored.sum() / max(float(m.sum()), 1.0)))
 
 
 def distance_input(bc):
@@ -138,22 +161,26 @@ def _pad(t, shape):
 
 
 class LearnedStart:
-    """A trained network sized for one grid (padded to multiples of 8)."""
+    """A trained network for one grid: the grid padded to multiples of 16, the network at
+    half of that."""
 
     def __init__(self, shape, params_flat):
         from .runtime import LPNet
         self.shape = tuple(shape)
-        self.net = LPNet(pad8(shape))
+        self.fine = pad16(shape)
+        self.net = LPNet(tuple(v // 2 for v in self.fine))
         self.net.set_params(params_flat)
 
     def start(self, ctx):
         """The start (a torch CUDA float32 tensor of ctx's shape) for the system that
         ctx.pressure_setup(t) assembled."""
+        from .runtime import field_up2
         m, k, b = ctx.pressure_learned_inputs()
-        ps = self.net.shape
-        out = self.net.forward(_pad(m, ps), _pad(k, ps), _pad(distance_input(b), ps))
+        fs = self.fine
+        mc, kc, dc = coarse_inputs(_pad(m, fs), _pad(k, fs), _pad(distance_input(b), fs))
+        d = field_up2(self.net.forward(mc, kc, dc))
         I, J, K = self.shape
-        return ((1.0 - out[:I, :J, :K] / DEV_SCALE) * m).contiguous()
+        return ((1.0 - d[:I, :J, :K] / DEV_SCALE) * m).contiguous()
 
     def close(self):
         self.net.close()
@@ -163,7 +190,7 @@ def load_weights(path=WEIGHTS):
     return np.load(path) if os.path.exists(path) else None
 
 
-def train(samples=192, epochs=16, lr=2e-3, seed=0, shape=PATCH, log=print):
+def train(samples=256, epochs=64, lr=2e-3, seed=0, shape=PATCH, log=print):
     """Generate samples with the plain solver and train a network on them; returns
     (flat parameters, history)."""
     from .runtime import LPNet
@@ -176,7 +203,7 @@ def train(samples=192, epochs=16, lr=2e-3, seed=0, shape=PATCH, log=print):
     gen_s = time.time() - t0
     log(f"generated {samples} samples in {gen_s:.1f}s "
         f"(mean plain iterations {np.mean([m['iterations'] for m in metas]):.1f})")
-    net = LPNet(shape, seed=seed)
+    net = LPNet(tuple(v // 2 for v in pad16(shape)), seed=seed)
     rng = np.random.default_rng(seed)
     hist = []
     t1 = time.time()
@@ -202,8 +229,8 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     sub = ap.add_subparsers(dest="cmd", required=True)
     tr = sub.add_parser("train")
-    tr.add_argument("--samples", type=int, default=192)
-    tr.add_argument("--epochs", type=int, default=16)
+    tr.add_argument("--samples", type=int, default=256)
+    tr.add_argument("--epochs", type=int, default=64)
     tr.add_argument("--lr", type=float, default=2e-3)
     tr.add_argument("--seed", type=int, default=0)
     tr.add_argument("--out", default=WEIGHTS)

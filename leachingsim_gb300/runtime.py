@@ -71,6 +71,8 @@ SYMBOLS = {
                                       C.c_longlong, C.c_float, C.c_int, C.POINTER(C.c_double)]),
     "ls_pressure_learned_inputs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ls_pressure_solve_start": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.POINTER(LsSolveInfo)]),
+    "ls_field_pool2": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ls_field_up2": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     "ls_geom_distance": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     "ls_geom_fracture": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ls_geom_classify": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
@@ -173,6 +175,32 @@ def geom_distance(sites):
     torch.cuda.synchronize()
     _geom_check(load().ls_geom_distance(*t.shape, C.c_void_p(t.data_ptr()), C.c_void_p(out.data_ptr())),
                 "ls_geom_distance")
+    return out
+
+
+def field_pool2(fine, weight=None):
+    """(Weighted) 2x2x2 block means of a torch CUDA float32 (D, H, W) field (even extents)."""
+    import torch
+    f = fine.contiguous()
+    w = weight.contiguous() if weight is not None else None
+    D, H, W = f.shape
+    out = torch.empty((D // 2, H // 2, W // 2), dtype=torch.float32, device=f.device)
+    torch.cuda.synchronize()
+    _geom_check(load().ls_field_pool2(D, H, W, C.c_void_p(f.data_ptr()),
+                                      C.c_void_p(w.data_ptr()) if w is not None else None,
+                                      C.c_void_p(out.data_ptr())), "ls_field_pool2")
+    return out
+
+
+def field_up2(coarse):
+    """Each value of a torch CUDA float32 (D, H, W) field repeated over a 2x2x2 block."""
+    import torch
+    c = coarse.contiguous()
+    D, H, W = (2 * v for v in c.shape)
+    out = torch.empty((D, H, W), dtype=torch.float32, device=c.device)
+    torch.cuda.synchronize()
+    _geom_check(load().ls_field_up2(D, H, W, C.c_void_p(c.data_ptr()), C.c_void_p(out.data_ptr())),
+                "ls_field_up2")
     return out
 
 

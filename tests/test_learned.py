@@ -68,7 +68,7 @@ def test_untrained_network_start_still_converges_to_the_same_solution():
     from leachingsim_gb300.runtime import LPNet
     ctx, _ = _ctx(3)
     x0, _ = _zero_solve(ctx)
-    net = LPNet(L.pad8(SHAPE), seed=9)
+    net = LPNet((8, 8, 8), seed=9)
     ls = L.LearnedStart(SHAPE, net.get_params())
     net.close()
     ok, info = ctx.pressure_solve_start(ls.start(ctx), 1.0)
@@ -114,3 +114,20 @@ def test_inner_precision_switch_within_one_context():
         assert _rel(x, xr) < 1e-7, solver
         assert _rel(x, xm) < 1e-6, solver
     ctx.close()
+
+
+def test_half_resolution_transfers():
+    import torch
+    from leachingsim_gb300.runtime import field_pool2, field_up2
+    rng = np.random.default_rng(5)
+    f = rng.standard_normal((6, 10, 4)).astype(np.float32)
+    w = (rng.random((6, 10, 4)) < 0.5).astype(np.float32)
+    blocks = lambda a: a.reshape(3, 2, 5, 2, 2, 2).transpose(0, 2, 4, 1, 3, 5).reshape(3, 5, 2, 8)
+    ft, wt = torch.from_numpy(f).cuda(), torch.from_numpy(w).cuda()
+    np.testing.assert_allclose(field_pool2(ft).cpu().numpy(), blocks(f).mean(-1), rtol=1e-6, atol=1e-6)
+    sw = blocks(w).sum(-1)
+    ref = np.where(sw > 0, (blocks(f) * blocks(w)).sum(-1) / np.maximum(sw, 1e-30), 0.0)
+    np.testing.assert_allclose(field_pool2(ft, wt).cpu().numpy(), ref, rtol=1e-6, atol=1e-6)
+    c = torch.from_numpy(rng.standard_normal((3, 5, 2)).astype(np.float32)).cuda()
+    up = field_up2(c).cpu().numpy()
+    np.testing.assert_array_equal(up, np.repeat(np.repeat(np.repeat(c.cpu().numpy(), 2, 0), 2, 1), 2, 2))
