@@ -234,7 +234,34 @@ def main(argv=None):
     tr.add_argument("--lr", type=float, default=2e-3)
     tr.add_argument("--seed", type=int, default=0)
     tr.add_argument("--out", default=WEIGHTS)
+    fw = sub.add_parser("forward", help="time the network's forward pass on random inputs")
+    fw.add_argument("--shape", default="144,176,176", help="network grid (multiples of 8)")
+    fw.add_argument("--reps", type=int, default=5)
     a = ap.parse_args(argv)
+    if a.cmd == "forward":
+        import torch
+        from .runtime import LPNet
+        shape = tuple(int(v) for v in a.shape.split(","))
+        net = LPNet(shape)
+        w = load_weights()
+        if w is not None:
+            net.set_params(w)
+        x = [torch.rand(shape, device="cuda") for _ in range(3)]
+        times = []
+        for _ in range(a.reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            net.forward(*x)
+            torch.cuda.synchronize()
+            times.append((time.perf_counter() - t0) * 1e3)
+        vox = shape[0] * shape[1] * shape[2]
+        # multiply-adds of the eight convolutions: full, 1/8, 1/64, 1/512 of the voxels
+        flops = 2 * 27 * vox * (16 * 16 * 2 + 16 * 16 + (16 * 32 + 32 * 16) / 8 + (32 * 64 + 64 * 32) / 64
+                                + 64 * 64 / 512)
+        best = min(times)
+        print(json.dumps({"shape": shape, "ms": round(best, 3), "tflops": round(flops / best / 1e9, 1),
+                          "times_ms": [round(t, 3) for t in times]}))
+        net.close()
     if a.cmd == "train":
         flat, hist = train(a.samples, a.epochs, a.lr, a.seed, log=lambda *x: print(*x, file=sys.stderr, flush=True))
         np.save(a.out, flat)
