@@ -23,9 +23,11 @@ zero start's value, and what the network says there is discarded (the solver zer
 supplied start on unanchored components). It is trained only on solutions of the plain
 solver (mixed-precision multigrid FCG with FP64 refinement) on seeded synthetic
 geometries with porosity 0.15-0.40, correlation length 2-10 and mineral fraction
-0.05-0.30, Air inlet planes as in the workload, as columns of the workload's depth
-(288 x 64 x 64): how far the pressure falls depends on the depth of the Pore space behind
-a voxel, which 96^3 patches do not show. At use, the start goes through
+0.05-0.30, Air inlet planes as in the workload: 16 solves of 288 x 256 x 256 (the
+workload's depth), each cut into 16 columns of 288 x 64 x 64. How far the pressure falls
+depends on the Pore space behind and beside a voxel, which small domains of their own do
+not show (96^3 patches, or narrow columns solved alone, train networks that help less at
+the workload's size). At use, the start goes through
 ls_pressure_solve_start: the FP64 refinement rescales it once by its minimal-residual
 factor when that lowers the residual, judges it by the FP64 residual and finishes the
 solve with the plain solver, so a poor start costs iterations, never accuracy.
@@ -46,7 +48,9 @@ import numpy as np
 from . import _abi
 from .geometry import grf_geometry
 
-PATCH = (288, 64, 64)
+PATCH = (288, 64, 64)   # training crops (fine voxels)
+WIDE = (288, 256, 256)   # the solves the crops are cut from
+CROPS = 16               # crops per solve
 DEV_SCALE = 100.0   # network output d = DEV_SCALE (1 - P / p_top)
 DIST_SCALE = 100.0  # the distance input is dist / DIST_SCALE
 WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lpnet_weights.npy")
@@ -143,6 +147,23 @@ def make_sample(seed, shape=PATCH, t=RAMP, params=None):
                                       anchored=float(anchored.sum() / max(float(m.sum()), 1.0)))
 
 
+def make_crops(seed, shape=WIDE, crop=PATCH, count=CROPS, t=RAMP, params=None):
+    """Training samples cut from one wide solve: the plain solver on a seeded geometry of
+    `shape`, the fields and target at half resolution, and `count` random crops of
+    half of `crop` (a crop of a wide domain carries the pressure drop of the wide domain,
+    which a narrow domain of its own would not)."""
+    full, meta = make_sample(seed, shape, t, params)
+    rng = np.random.default_rng(seed ^ 0x5EED)
+    cs = tuple(v // 2 for v in pad16(crop))
+    fs = full[0].shape
+    out = []
+    for _ in range(count):
+        o = [int(rng.integers(0, fs[a] - cs[a] + 1)) for a in range(3)]
+        sl = tuple(slice(o[a], o[a] + cs[a]) for a in range(3))
+        out.append(tuple(v[sl].contiguous() for v in full))
+    return out, meta
+
+
 def distance_input(bc):
     """The third input: distance to the voxels carrying the top pressure, over DIST_SCALE
     (0 where no voxel carries it)."""
@@ -190,18 +211,25 @@ def load_weights(path=WEIGHTS):
     return np.load(path) if os.path.exists(path) else None
 
 
-def train(samples=256, epochs=64, lr=2e-3, seed=0, shape=PATCH, log=print):
+def train(samples=256, epochs=64, lr=2e-3, seed=0, shape=PATCH, log=print, wide=None):
     """Generate samples with the plain solver and train a network on them; returns
     (flat parameters, history)."""
     from .runtime import LPNet
     t0 = time.time()
     data, metas = [], []
-    for s in range(samples):
-        d, meta = make_sample(seed * 100003 + s, shape)
-        data.append(d)
-        metas.append(meta)
+    if wide:
+        for s in range((samples + CROPS - 1) // CROPS):
+            d, meta = make_crops(seed * 100003 + s, wide, shape, CROPS)
+            data.extend(d)
+            metas.append(meta)
+        data = data[:samples]
+    else:
+        for s in range(samples):
+            d, meta = make_sample(seed * 100003 + s, shape)
+            data.append(d)
+            metas.append(meta)
     gen_s = time.time() - t0
-    log(f"generated {samples} samples in {gen_s:.1f}s "
+    log(f"generated {len(data)} samples from {len(metas)} solves in {gen_s:.1f}s "
         f"(mean plain iterations {np.mean([m['iterations'] for m in metas]):.1f})")
     net = LPNet(tuple(v // 2 for v in pad16(shape)), seed=seed)
     rng = np.random.default_rng(seed)
@@ -234,6 +262,8 @@ def main(argv=None):
     tr.add_argument("--lr", type=float, default=2e-3)
     tr.add_argument("--seed", type=int, default=0)
     tr.add_argument("--out", default=WEIGHTS)
+    tr.add_argument("--patches", action="store_true",
+                    help="solve each sample on its own (default: cut the samples from wide solves)")
     fw = sub.add_parser("forward", help="time the network's forward pass on random inputs")
     fw.add_argument("--shape", default="144,176,176", help="network grid (multiples of 8)")
     fw.add_argument("--reps", type=int, default=5)
@@ -263,7 +293,8 @@ def main(argv=None):
                           "times_ms": [round(t, 3) for t in times]}))
         net.close()
     if a.cmd == "train":
-        flat, hist = train(a.samples, a.epochs, a.lr, a.seed, log=lambda *x: print(*x, file=sys.stderr, flush=True))
+        flat, hist = train(a.samples, a.epochs, a.lr, a.seed, log=lambda *x: print(*x, file=sys.stderr, flush=True),
+                           wide=None if a.patches else WIDE)
         np.save(a.out, flat)
         print(json.dumps(hist))
 
