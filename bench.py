@@ -51,6 +51,22 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x, ws, device="cuda"):
+    """The largest of a per-rank value: the slowest replica sets the job's time."""
+    if ws <= 1:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(ws, steps_per_rank, seconds):
+    """Whole-job steps/s of ws independent replicas (no data-path collective), each running
+    steps_per_rank steps, over the slowest replica's time."""
+    return ws * steps_per_rank / seconds
+
+
 def make_geometry(shape):
     from leachingsim_gb300.geometry import grf_geometry
     lab, seed = grf_geometry(shape, air_inlet=True, **GEOM)
@@ -313,11 +329,7 @@ def gpu_arm(args, ws, rank, local):
     ctx.timing(False)
     mem = ctx.device_bytes()
     ctx.close()
-    t_max = dev_ms / 1e3
-    if ws > 1:
-        tt = torch.tensor([t_max], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(tt.item())
+    t_max = max_over_ranks(dev_ms / 1e3, ws)
 
     # ---- end to end: full configured run from a host image ---------------------------
     e2e = None
@@ -348,11 +360,8 @@ def gpu_arm(args, ws, rank, local):
         ctx.synchronize()
         e2e_wall = time.perf_counter() - w0
         ctx.close()
-        if ws > 1:
-            tt = torch.tensor([e2e_wall], device="cuda")
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            e2e_wall = float(tt.item())
-        e2e = {"value": round(ws * nsteps / e2e_wall, 4), "unit": UNIT,
+        e2e_wall = max_over_ranks(e2e_wall, ws)
+        e2e = {"value": round(replica_rate(ws, nsteps, e2e_wall), 4), "unit": UNIT,
                "h2d_bytes_per_step": int(h2d / nsteps), "d2h_bytes_per_step": int(d2h / nsteps),
                "steps": nsteps, "wall_s": round(e2e_wall, 3),
                "note": "fresh run from a pinned host label image, every nout-th step's fields read back to pinned host memory"}
@@ -362,7 +371,7 @@ def gpu_arm(args, ws, rank, local):
     cpu = None
     if ws == 1 and not args.no_cpu:
         cpu = cpu_sample(args.cpu_steps, 1, None)
-    value = ws * args.steps / t_max
+    value = replica_rate(ws, args.steps, t_max)
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3),
