@@ -439,6 +439,7 @@ static ls_status transfer(ls_ctx* c, ls_field f, void* host, size_t n, int padde
         if (f == LS_F_PERMEABILITY || f == LS_F_VISCOSITY || f == LS_F_CAP_PRESSURE || f == LS_F_REL_PERM)
             c->props_force = 1;
         if (f == LS_F_PRESSURE) c->p_eff_prev = 0.0;
+        if (f == LS_F_ACID) c->acid_zero = 0;
     } else {
         LS_CUDA(c, cudaMemcpyAsync(host, dev, n * esz, kind, c->stream));
     }
@@ -468,6 +469,7 @@ ls_status ls_init_fields(ls_ctx* c) {
     c->p_ready = 0;
     c->p_eff_prev = 0.0;
     c->props_force = 1;  // kr and Pc were cleared
+    c->acid_zero = 0;
     return LS_OK;
 }
 
@@ -485,6 +487,7 @@ ls_status ls_init_saturation(ls_ctx* c) {
 ls_status ls_init_acid(ls_ctx* c) {
     if (!c) return LS_BAD_ARG;
     LS_CUDA(c, cudaMemsetAsync(c->acid, 0, sizeof(double) * (size_t)c->g.N, c->stream));
+    c->acid_zero = 0;  // the plane beyond N keeps what it held
     return LS_OK;
 }
 
@@ -613,6 +616,7 @@ ls_status ls_rollback(ls_ctx* c) {
     }
     c->p_ready = 0;
     c->p_eff_prev = 0.0;
+    c->acid_zero = 0;
     return ls_props(c);
 }
 

@@ -290,6 +290,8 @@ struct ls_ctx {
     void* sht_label;      // transport-row inputs at the last evaluation (fully implicit rows)
     double *sht_fx, *sht_fy, *sht_fz;
     int t_valid;          // the stored transport rows are fully implicit rows for t_consts
+    int acid_zero;        // the acid field is identically 0: the last transport solve found
+                          // b = 0 and x = 0; cleared by every write from outside
     double t_consts[8];
     double *shq_P, *shq_C, *shq_K, *shq_V;  // flux inputs at the last evaluation
     double *shq_fx, *shq_fy, *shq_fz;       // the fluxes last computed

@@ -1029,7 +1029,8 @@ static ls_status inner_solve(ls_ctx* c, const TBuf& tb, const int lane_q[NQ], co
 // place), fields f0/f1 supplying the right-hand sides.
 template <typename L>
 static ls_status mixed_solve(ls_ctx* c, const Rows<L>& rows, int nrhs, const double* f0, const double* f1,
-                             double* x0, double* x1, double rtol, int max_it, ls_solve_info* info[2]) {
+                             double* x0, double* x1, double rtol, int max_it, ls_solve_info* info[2],
+                             int* zero_lanes = nullptr) {
     LS_TRY(t_alloc(c));
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
@@ -1075,6 +1076,11 @@ static ls_status mixed_solve(ls_ctx* c, const Rows<L>& rows, int nrhs, const dou
     // a system with b = 0 and x = 0 on every row is solved exactly: no residual pass
     for (int q = 0; q < nrhs; ++q)
         if (den[2 + q] == 0.0) { reason[q] = 2; mask &= ~(1 << q); }
+    if (zero_lanes) {
+        *zero_lanes = 0;
+        for (int q = 0; q < nrhs; ++q)
+            if (den[2 + q] == 0.0) *zero_lanes |= 1 << q;
+    }
     double rel[2] = {0.0, 0.0}, prev[2] = {INFINITY, INFINITY};
     int stagnant[2] = {0, 0};
     const int max_sweeps = 40;
@@ -1178,11 +1184,27 @@ static ls_status transport_t(ls_ctx* c, double dt, int which, ls_solve_info* ci,
     double* fields[2] = {c->conc, c->acid};
     double* f[2] = {nullptr, nullptr};
     ls_solve_info* inf[2] = {nullptr, nullptr};
-    int n = 0;
+    // An acid field that is identically 0 (the last solve found b = 0 and x = 0 on every row,
+    // and nothing has written the field since) gives b = 0 and x = 0 again: the solve would
+    // leave it as it is, so it is skipped with the info such a solve reports.
+    if ((which & 2) && c->acid_zero) {
+        which &= ~2;
+        if (ai) {
+            memset(ai, 0, sizeof(*ai));
+            ai->converged = 1;
+            ai->reason = 2;
+        }
+    }
+    int n = 0, acid_lane = -1;
     if (which & 1) { f[n] = fields[0]; inf[n] = ci; n++; }
-    if (which & 2) { f[n] = fields[1]; inf[n] = ai; n++; }
-    ls_status st = mixed_solve<L>(c, rows, n, f[0], f[1], f[0] + sh, n > 1 ? f[1] + sh : nullptr,
-                                  c->p.conc_rtol, c->p.conc_max_it, inf);
+    if (which & 2) { f[n] = fields[1]; inf[n] = ai; acid_lane = n; n++; }
+    ls_status st = LS_OK;
+    if (n > 0) {
+        int zero_lanes = 0;
+        st = mixed_solve<L>(c, rows, n, f[0], f[1], f[0] + sh, n > 1 ? f[1] + sh : nullptr, c->p.conc_rtol,
+                            c->p.conc_max_it, inf, &zero_lanes);
+        if (acid_lane >= 0) c->acid_zero = (st == LS_OK && ((zero_lanes >> acid_lane) & 1)) ? 1 : 0;
+    }
     if (st != LS_OK && st != LS_NOT_CONVERGED && st != LS_NONFINITE) return st;
     LS_LAUNCH(c, k_zero_solid_flux<L>, grid_for(c, c->g.N), kBlock, 0, c->g, (const L*)c->label,
               c->fx, c->fy, c->fz);

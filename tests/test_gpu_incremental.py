@@ -77,3 +77,28 @@ def test_uploaded_properties_are_overwritten_by_props():
     for f in PROPS:
         np.testing.assert_array_equal(g.download(f), ref[f], err_msg=f)
     g.close()
+
+
+def test_zero_acid_field_skips_its_solve_until_written():
+    """An identically zero acid field keeps b = 0 and x = 0: after one solve that finds so,
+    the acid solve is skipped (same info, same field) until the field is written again."""
+    from leachingsim_gb300.runtime import Context
+    lab = small_grf((16, 12, 14), seed=4)
+    p = params(conc_rtol=1e-12)
+    g = Context(lab.shape, params=p)
+    g.upload("label", lab)
+    g.init_all()
+    g.upload("acid", np.zeros(g.NP), padded=True)
+    for n in range(3):
+        ok, info = g.step(float(n), 1.0)
+        assert ok, info
+        okt, ci, ai = g.transport(1.0, 3)
+        assert okt and ai["iterations"] == 0 and ai["reason"] == 2
+        assert ai["max_value"] == 0.0 and ai["min_value"] == 0.0
+        assert not np.any(g.download("acid", padded=True))
+    acid = np.random.default_rng(1).uniform(0.0, 1.0, g.NP)
+    g.upload("acid", acid, padded=True)
+    okt, ci, ai = g.transport(1.0, 3)
+    assert okt and ai["iterations"] > 0
+    assert np.any(g.download("acid", padded=True))
+    g.close()
