@@ -14,6 +14,10 @@ image in pinned host memory, reading every output step's fields back into pinned
 host memory (file writing excluded).
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Separate lines: `--mixed` (the 512^3 uint16 fractured geometry, mixed precision against
+FP64 settings, per-field error and memory footprint) and `--geometry` (the geometry
+pre-processing pipeline at 512^3).
 """
 import argparse
 import json
@@ -209,7 +213,7 @@ def cold_pressure_solves(ctx, shape, solver, reps=2):
     run that follows starts from the same state."""
     import torch
     from leachingsim_gb300 import learned as L
-    from leachingsim_gb300._abi import PRESS_FP64, PRESS_MIXED
+    from leachingsim_gb300._abi import PRESS_FP64, PRESS_LEARNED, PRESS_MIXED
     zeros_p = np.zeros(ctx.NP)
     zeros = torch.zeros(shape, dtype=torch.float32, device="cuda")
     weights = L.load_weights()
@@ -217,13 +221,20 @@ def cold_pressure_solves(ctx, shape, solver, reps=2):
     variants = [("plain_fp64", PRESS_FP64, None), ("plain", PRESS_MIXED, None)]
     if ls is not None:
         variants.append(("learned", PRESS_MIXED, ls))
+    pw = L.load_precond_weights()
+    if pw is not None:
+        # the network as the coarse solver inside the flexible CG, the plain cycle as fallback
+        ctx.set_precond_weights(pw)
+        variants.append(("learned_precond", PRESS_LEARNED, None))
     # context for the learned start: the untrained guess P = p_top on every Pore row
     variants.append(("constant_start", PRESS_MIXED, "constant"))
     ctx.props()
     out = {}
     for name, s, start in variants:
         base = params("fp64" if s == PRESS_FP64 else "mixed")
+        base.press_solver = s
         ctx.set_params(base)
+        fb0 = ctx.pressure_fallbacks()
         for _ in range(reps):
             ctx.upload("pressure", zeros_p, padded=True)
             ctx.synchronize()
@@ -246,6 +257,8 @@ def cold_pressure_solves(ctx, shape, solver, reps=2):
                      "scaled_rel_residual": info["rel_residual"], "converged": bool(ok)}
         if start is not None:
             out[name]["start_ms"] = round((w2 - w1) * 1e3, 3)
+        if s == PRESS_LEARNED:
+            out[name]["fallbacks_per_solve"] = (ctx.pressure_fallbacks() - fb0) / reps
     if ls is not None:
         ls.close()
     ctx.set_params(params(solver))
@@ -299,7 +312,9 @@ def gpu_arm(args, ws, rank, local):
                             "converged": bool(pinfo["converged"])}
     psolve.setdefault("learned", None)
     psolve["note"] = ("cold solves of the first step's pressure system: t = 0, zero start (learned: the "
-                      "network's start; constant_start: P = p_top on the Pore rows), rtol 1e-8 on the "
+                      "network's start; constant_start: P = p_top on the Pore rows; learned_precond: the "
+                      "network as the multigrid's level-3 solver inside the flexible CG, with the plain "
+                      "cycle taking over on stagnation), rtol 1e-8 on the "
                       "Jacobi-scaled FP64 residual; ms = assembly + [start: inputs, distance transform, "
                       "network] + multigrid setup + solve; first_step = the run's own first step (device "
                       "timers)")
@@ -525,6 +540,119 @@ def geometry_arm(args):
     return line
 
 
+# ---------------------------------------------------------------------------
+# mixed precision at 512^3 (a separate line, --mixed): the uint16 grey-level geometry with
+# planar fractures, stepped with the FP32-inner solvers (FP64 refinement) and again with the
+# FP64 settings; per-field relative-L2 error of the first against the second
+
+MIX_SHAPE = (512, 512, 512)
+MIX_STEPS = 10
+
+
+def mixed_geometry(shape):
+    """uint16 labels of the mixed-precision workload: the grey-level random field (corr 6)
+    with 4 planar fractures of 1-3 voxel aperture (grey 0), classified on the GPU at the 20% /
+    88% grey quantiles into Pore / Rock / Sulphide (the fractures fall below the lowest
+    threshold: Pore), Air inlet planes i = 0, 1 as the pressure driver."""
+    from leachingsim_gb300 import runtime as rt
+    from leachingsim_gb300.geometry import grey_levels
+    grey = grey_levels(shape, corr_len=6.0, seed=0, n_fractures=4)
+    sub = grey[::4, ::4, ::4].ravel()
+    thr = [int(np.quantile(sub, 0.2)), int(np.quantile(sub, 0.88))]
+    lab = rt.geom_classify(grey, thr, [2, 3, 4], 2)
+    lab[0:2] = 1
+    return lab, thr
+
+
+MIX_FIELDS = ("pressure", "flux_x", "flux_y", "flux_z", "conc", "precipitate", "label")
+
+
+def mixed_run(lab, p, steps):
+    """steps accepted time steps from a fresh state; returns wall ms per step (first step
+    and the rest), the fields, the context's device bytes and the solver iterations."""
+    import torch
+    from leachingsim_gb300.runtime import Context
+    ctx = Context(lab.shape, label_bytes=2, params=p)
+    ctx.upload("label", lab)
+    ctx.init_all()
+    ctx.synchronize()
+    times, iters = [], []
+    t, n = 0.0, 0
+    first = None
+    for _ in range(steps):
+        w0 = time.perf_counter()
+        t, n, info = run_steps(ctx, t, n, 1, DT)
+        ctx.synchronize()
+        times.append((time.perf_counter() - w0) * 1e3)
+        iters.append((info[0]["pressure"]["iterations"], info[0]["conc"]["iterations"]))
+        if first is None:  # after the first (cold) step, outside the timed step
+            first = {f: ctx.download(f, padded=f != "label") for f in MIX_FIELDS}
+    out = {f: ctx.download(f, padded=f != "label") for f in MIX_FIELDS}
+    mem = ctx.device_bytes()
+    ctx.close()
+    torch.cuda.synchronize()
+    return times, (first, out), mem, iters
+
+
+def mixed_arm(args):
+    import torch
+    from leachingsim_gb300._abi import PRESS_FP64, PRESS_MIXED, default_params
+    shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else MIX_SHAPE
+    steps = max(args.steps, 2)
+    t0 = time.time()
+    lab, thr = mixed_geometry(shape)
+    log(f"mixed: geometry {shape} in {time.time() - t0:.1f}s, labels {np.bincount(lab.ravel()).tolist()}")
+    base = dict(c_sat=1.0, D=1.0, kreac=1.0)
+    pm = default_params(press_solver=PRESS_MIXED, press_rtol=PRESS_RTOL, conc_rtol=CONC_RTOL,
+                        sat_rtol=CONC_RTOL, **base)
+    pf = default_params(press_solver=PRESS_FP64, press_rtol=1e-12, conc_rtol=1e-12, sat_rtol=1e-12, **base)
+    with ClockSampler(0) as clk:
+        tm, fm, mem, im = mixed_run(lab, pm, steps)
+    tf, ff, _, iff = mixed_run(lab, pf, steps)
+
+    def rel(a, b):
+        a = np.asarray(a, np.float64).ravel()
+        b = np.asarray(b, np.float64).ravel()
+        d = np.linalg.norm(b)
+        return float(np.linalg.norm(a - b) / d) if d > 0 else float(np.linalg.norm(a - b))
+
+    vel = lambda f: np.concatenate([f[k].ravel() for k in ("flux_x", "flux_y", "flux_z")])  # noqa: E731
+
+    def errors(a, b):
+        return {"pressure": rel(a["pressure"], b["pressure"]), "velocity": rel(vel(a), vel(b)),
+                "conc": rel(a["conc"], b["conc"]), "precipitate": rel(a["precipitate"], b["precipitate"]),
+                "label_mismatches": int(np.count_nonzero(a["label"] != b["label"])),
+                "precipitated_voxels": int(np.count_nonzero(b["label"] == 5))}
+
+    err = {"first_step": errors(fm[0], ff[0]), "last_step": errors(fm[1], ff[1])}
+    warm_m = statistics.median(tm[1:])
+    warm_f = statistics.median(tf[1:])
+    vox = lab.size
+    total = torch.cuda.get_device_properties(0).total_memory
+    c5 = 1024 * 1024 * 768
+    return {"metric": f"time-steps/s at {shape[0]}x{shape[1]}x{shape[2]} uint16, mixed precision",
+            "value": round(1e3 / warm_m, 4), "unit": "time-steps/s", "n_gpus": 1, "steps": steps - 1,
+            "warmup": 1, "ms_per_step": round(warm_m, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic",
+            "config": {"workload": f"{shape[0]}x{shape[1]}x{shape[2]} uint16 grey-level random field "
+                                   "(corr 6) with 4 planar fractures of 1-3 voxel aperture, classified at the "
+                                   "20% / 88% grey quantiles -> Pore / Rock / Sulphide (fractures: Pore), Air "
+                                   "inlet planes, dt 1, D 1, kreac 1, csat 1; mixed: FP32 inner MG-FCG / "
+                                   "BiCGStab with FP64 refinement to pressure rtol 1e-8, transport 1e-6; "
+                                   "fp64: FP64 inner MG-PCG to pressure rtol 1e-12, transport 1e-12",
+                       "thresholds": thr, "l2": "working set > L2"},
+            "first_step_ms": {"mixed": round(tm[0], 3), "fp64": round(tf[0], 3)},
+            "fp64_ms_per_step": round(warm_f, 3),
+            "iterations": {"mixed": im, "fp64": iff},
+            "rel_l2_vs_fp64": err,
+            "memory": {"device_bytes": mem, "bytes_per_voxel": round(mem / vox, 1),
+                       "gpu_total_bytes": int(total),
+                       "projected_1024x1024x768_bytes": int(mem / vox * c5),
+                       "fits_1024x1024x768": bool(mem / vox * c5 < total)},
+            "clocks": clk.summary(),
+            "e2e": None}
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -542,9 +670,15 @@ def main():
                          "'timed' (for ncu --nvtx-include cold/ or timed/)")
     ap.add_argument("--geometry", action="store_true",
                     help="time the geometry pre-processing pipeline instead (a separate JSON line)")
+    ap.add_argument("--mixed", action="store_true",
+                    help="mixed precision against FP64 settings on the 512^3 uint16 fractured geometry "
+                         "(a separate JSON line)")
     args = ap.parse_args()
     if args.geometry:
         print(json.dumps(geometry_arm(args)), flush=True)
+        return
+    if args.mixed:
+        print(json.dumps(mixed_arm(args)), flush=True)
         return
     ws, rank, local = dist_env()
     if args.warmup < 3 and args.impl == "ours":

@@ -78,7 +78,10 @@ typedef enum ls_field {
 typedef enum ls_press_solver {
     LS_PRESS_MIXED = 0,    /* FP32 MG-PCG inner solves, FP64 iterative refinement outside */
     LS_PRESS_FP64 = 1,     /* FP64 MG-PCG inner solves (the plain path) */
-    LS_PRESS_JACOBI64 = 2  /* FP64 Jacobi-PCG inner solves (no multigrid; test path) */
+    LS_PRESS_JACOBI64 = 2, /* FP64 Jacobi-PCG inner solves (no multigrid; test path) */
+    LS_PRESS_LEARNED = 3   /* LS_PRESS_MIXED with the learned coarse solver in the multigrid cycle
+                              (ls_pressure_set_precond_weights); the plain cycle takes over when
+                              the flexible CG stagnates */
 } ls_press_solver;
 
 /*
@@ -203,6 +206,27 @@ ls_status ls_pressure_step(ls_ctx* ctx, double t, ls_solve_info* info);
    exactly as in ls_pressure_step. */
 ls_status ls_pressure_learned_inputs(ls_ctx* ctx, float* mask, float* logk, float* bc);
 ls_status ls_pressure_solve_start(ls_ctx* ctx, const float* start, double scale, ls_solve_info* info);
+/* Learned preconditioner of the pressure solve (no counterpart in the reference). With
+   press_solver = LS_PRESS_LEARNED the inner flexible CG (FP32, inside the FP64 refinement) is
+   preconditioned by the K-cycle whose coarse correction on multigrid level 3 (1/8 of the grid
+   along each axis) is the network of ls_lpnet_* applied to that level's residual, instead of
+   a V-cycle over the levels below. Network input channels on a grid holding the level at
+   its origin (extents rounded up to multiples of 8): the member mask, the anchoring fraction
+   e/d (the share of a cell's diagonal coupling to fixed values) and D^-1/2 b / s, s the
+   largest |D^-1/2 b| over the members; output D^1/2 x / (64 s). When the flexible CG
+   stagnates (a non-finite, negative or growing (r, z), (p, q) <= 0, or two iterations in a
+   row that reduce (r, z) by less than 0.64) the solve goes on with the plain K-cycle from its
+   current iterate and ls_pressure_fallbacks counts it; the FP64 residual judges every
+   accepted solve either way. Grids too small to have level 3 use the plain cycle.
+   params: count = ls_lpnet_param_count floats (host), copied. */
+ls_status ls_pressure_set_precond_weights(ls_ctx* ctx, const float* params, long long count);
+long long ls_pressure_fallbacks(const ls_ctx* ctx);
+/* Training hook: multigrid level `level` (1 = the first coarse level) of the hierarchy of the
+   last FP32-inner pressure solve: dims = its (I, J, K); for each non-null pointer, a host copy
+   of I*J*K values: owning strong component (-1: no unknown), excess e and the +i, +j, +k face
+   links (FP32, the sigma-scaled inner operator's Galerkin coarsening). */
+ls_status ls_pressure_mg_level(ls_ctx* ctx, int level, int* dims, int* comp, float* e, float* f0, float* f1,
+                               float* f2);
 /* Simulation::calculateFlux (src/Simulation.cpp:866-953). */
 ls_status ls_flux(ls_ctx* ctx);
 /* Simulation::updateSaturation(dt), explicit sub-stepping (src/Simulation.cpp:1672-1856). */

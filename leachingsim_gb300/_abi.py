@@ -32,7 +32,7 @@ FIELDS = {
 FIELD_DTYPES = {0: None, 1: "float32"}  # every other field is float64; labels per label_bytes
 
 # ls_press_solver
-PRESS_MIXED, PRESS_FP64, PRESS_JACOBI64 = 0, 1, 2
+PRESS_MIXED, PRESS_FP64, PRESS_JACOBI64, PRESS_LEARNED = 0, 1, 2, 3
 
 # ls_timer
 TIMERS = {

@@ -1,6 +1,7 @@
 // ls_api.cu - C-ABI entry points, context life cycle, transfers, snapshot, timing and
 // the time-step orchestration of src/main.cpp:303-432.
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -258,7 +259,7 @@ static ls_status validate_params(ls_ctx* c, const ls_params* p) {
     if (!(p->vg_n > 1.0)) return set_error(c, LS_BAD_ARG, "vg_n must be > 1");
     if (p->press_max_it < 1 || p->conc_max_it < 1 || p->sat_max_it < 1)
         return set_error(c, LS_BAD_ARG, "max_it must be >= 1");
-    if (p->press_solver < LS_PRESS_MIXED || p->press_solver > LS_PRESS_JACOBI64)
+    if (p->press_solver < LS_PRESS_MIXED || p->press_solver > LS_PRESS_LEARNED)
         return set_error(c, LS_BAD_ARG, "unknown press_solver");
     return LS_OK;
 }
@@ -281,6 +282,10 @@ ls_status ls_create(ls_ctx** out, int I, int J, int K, int label_bytes, const ls
     if (!c) return LS_BAD_ARG;
     c->inner_is64 = -1;
     c->mg_is64 = -1;
+    {
+        const char* gv = getenv("LS_MG_GRAPHS");
+        c->mg_graphs_off = (gv && gv[0] == '0') ? 1 : 0;
+    }
     c->g.I = I; c->g.J = J; c->g.K = K;
     c->g.JK = JK;
     c->g.N = (long long)I * JK;
@@ -373,6 +378,14 @@ ls_status ls_destroy(ls_ctx* c) {
     if (c->ti) cudaFree(c->ti);
     if (c->start_anchor) cudaFree(c->start_anchor);
     if (c->tcount) cudaFree(c->tcount);
+    {
+        void* lp[] = {c->lpc_c0, c->lpc_c1, c->lpc_c2, c->lpc_out, c->lpc_isd, c->lpc_anchor};
+        for (void* q : lp)
+            if (q) cudaFree(q);
+        if (c->lpc) ls_lpnet_destroy(c->lpc);
+    }
+    for (auto& gr : c->mg_graphs)
+        if (gr.exec) cudaGraphExecDestroy(gr.exec);
     for (auto& lv : c->mg) {
         void* lp[] = {lv.comp, lv.e, lv.face[0], lv.face[1], lv.face[2], lv.invd, lv.x, lv.b, lv.t};
         for (void* q : lp)
@@ -520,6 +533,38 @@ ls_status ls_pressure_learned_inputs(ls_ctx* c, float* mask, float* logk, float*
 ls_status ls_pressure_solve_start(ls_ctx* c, const float* start, double scale, ls_solve_info* info) {
     if (!c || !start || !(scale == scale)) return LS_BAD_ARG;
     return pressure_solve_run(c, info, start, scale);
+}
+
+ls_status ls_pressure_set_precond_weights(ls_ctx* c, const float* params, long long count) {
+    if (!c || count < 0 || (count > 0 && !params)) return LS_BAD_ARG;
+    c->lpc_params.assign(params, params + count);
+    if (c->lpc) {
+        if (ls_lpnet_param_count(c->lpc) != count)
+            return set_error(c, LS_BAD_ARG, "learned pressure solver: weight count does not match the network");
+        const ls_status st = ls_lpnet_set_params(c->lpc, c->lpc_params.data(), count);
+        if (st != LS_OK) return set_error(c, st, "learned pressure solver: loading the weights failed");
+    }
+    return LS_OK;
+}
+
+long long ls_pressure_fallbacks(const ls_ctx* c) { return c ? c->press_fallbacks : 0; }
+
+ls_status ls_pressure_mg_level(ls_ctx* c, int level, int* dims, int* comp, float* e, float* f0, float* f1,
+                               float* f2) {
+    if (!c || !dims || level < 1) return LS_BAD_ARG;
+    if (c->mg_is64 != 0 || (size_t)level > c->mg.size())
+        return set_error(c, LS_BAD_ARG, "no FP32 multigrid level of that number (run a mixed-precision solve first)");
+    const auto& lv = c->mg[level - 1];
+    dims[0] = lv.g.I;
+    dims[1] = lv.g.J;
+    dims[2] = lv.g.K;
+    const size_t n = (size_t)lv.g.N;
+    const void* src[5] = {lv.comp, lv.e, lv.face[0], lv.face[1], lv.face[2]};
+    void* dst[5] = {comp, e, f0, f1, f2};
+    for (int q = 0; q < 5; ++q)
+        if (dst[q]) LS_CUDA(c, cudaMemcpyAsync(dst[q], src[q], 4 * n, cudaMemcpyDeviceToHost, c->stream));
+    LS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return LS_OK;
 }
 
 ls_status ls_pressure_apply(ls_ctx* c, const double* x, double* y) {

@@ -216,6 +216,18 @@ struct TimedRegion {
     cudaEvent_t start, stop;
 };
 
+// One captured multigrid preconditioner application (mg_precondition): the launches of a
+// K-cycle depend only on these pointers, the output slot and the learned branch, and on the
+// hierarchy's buffers, which stay in place until mg_free.
+struct MGGraph {
+    const void* r;
+    void* z;
+    const void* dv2;
+    int slot, learned, is64;
+    cudaGraphExec_t exec;
+    long long launches;
+};
+
 // Device-side scalar slots (doubles) used by the solvers.
 enum Scalar {
     S_RED0 = 0,       // generic reduction outputs S_RED0..S_RED0+15
@@ -315,9 +327,22 @@ struct ls_ctx {
     void* mg0_x;
     void* mg0_t;
     int mg_is64;          // -1 = not allocated
+    std::vector<ls::MGGraph> mg_graphs;  // captured preconditioner applications
+    int mg_graphs_off;    // 1: launch the cycle kernel by kernel (LS_MG_GRAPHS=0)
     int* comp;            // fine-level strong-component ids (-1 = not an inner unknown)
     uint8_t* start_anchor; // per component root: anchored to fixed values (supplied starts)
     int* cc_flag;         // device flag for the labelling loop
+    // learned coarse solver of the multigrid (LS_PRESS_LEARNED): a network that stands in
+    // for the V-cycle below the K-cycle levels
+    ls_lpnet* lpc;                  // sized for the learned level's grid, or null
+    std::vector<float> lpc_params;  // weights from ls_pressure_set_precond_weights
+    int lpc_dims[3];                // the network's grid (the level's extents rounded up to 8)
+    int lpc_ready;                  // the network's fixed inputs match the current hierarchy
+    int lpc_active;                 // the learned cycle is in use in the current solve
+    float *lpc_c0, *lpc_c1, *lpc_c2, *lpc_out;  // network grid: inputs, output channel 0
+    float* lpc_isd;                 // learned level: 1/sqrt(diagonal) of served cells, else 0
+    uint8_t* lpc_anchor;            // per component id: anchored on the learned level
+    long long press_fallbacks;      // learned solves that fell back to the plain cycle
 
     // transport / implicit saturation (2 right-hand sides)
     double* tc[7];        // FP64 row coefficients: diagonal, then +i,-i,+j,-j,+k,-k

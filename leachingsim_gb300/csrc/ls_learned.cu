@@ -680,6 +680,29 @@ ls_status lp_backward(ls_lpnet* n) {
 
 }  // namespace
 
+namespace ls {
+
+// Forward pass on another stream (the pressure context's: the learned coarse solver of its
+// multigrid), channel 0 of the output into out (D*H*W floats); the network's own stream is
+// restored afterwards. Asynchronous: no synchronisation, no allocation.
+ls_status lpnet_forward_on(ls_lpnet* n, cudaStream_t s, const float* c0, const float* c1, const float* c2,
+                           float* out, std::string* err) {
+    cudaStream_t own = n->stream;
+    n->stream = s;
+    ls_status st = lp_forward(n, c0, c1, c2);
+    if (st == LS_OK) {
+        const long long N = (long long)n->D * n->H * n->W;
+        k_lp_out<<<lp_grid(n, N, 256), 256, 0, s>>>(N, (const float*)n->y, out);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) st = lp_fail(n, "k_lp_out", e);
+    }
+    n->stream = own;
+    if (st != LS_OK && err) *err = n->err;
+    return st;
+}
+
+}  // namespace ls
+
 extern "C" {
 
 ls_status ls_lpnet_create(int D, int H, int W, int seed, ls_lpnet** out) {

@@ -37,6 +37,11 @@ constexpr double kProlongScale = 1.8;
 constexpr int kKLevels = 2;   // levels 1..kKLevels take a K-cycle coarse correction
 constexpr int kKSlot0 = 32;   // device scalar slots of the K-cycle FCG (5 per level)
 constexpr int kUnionSpin = 1 << 20;  // bound on the union-find retry loop
+// learned coarse solver (LS_PRESS_LEARNED): the network solves level kLearnedLevel in place of
+// the V-cycle below the K-cycle levels
+constexpr int kLearnedLevel = kKLevels + 1;
+constexpr float kLpcOutScale = 64.f;  // network output x this x max|D^-1/2 b| = D^1/2 x
+constexpr int kLpcSlot = 48;          // device scalar: max |D^-1/2 b| over the level's members
 
 __device__ __forceinline__ long long lidx(const Grid& g, int i, int j, int k) {
     return (long long)k + (long long)g.K * ((long long)j + (long long)g.J * i);
@@ -516,6 +521,187 @@ __global__ void k_mg_coarsest(Grid g, const int* __restrict__ comp, const T* __r
 }
 
 // ---------------------------------------------------------------------------
+// learned coarse solver: the network maps (member mask, anchoring fraction e/d, D^-1/2 b / s)
+// on a D x H x W grid holding the level at its origin to D^1/2 x / (s kLpcOutScale), the
+// Jacobi-scaled correction, s = max |D^-1/2 b| over the members. The unit-diagonal scaling
+// makes the inputs and outputs independent of the level's coefficient magnitudes.
+
+__device__ __forceinline__ bool lpc_cell(const Grid& g, int W, int H, long long v, long long& r) {
+    const long long hw = (long long)W * H;
+    const int z = (int)(v / hw);
+    const long long rem = v - (long long)z * hw;
+    const int y = (int)(rem / W), x = (int)(rem - (long long)y * W);
+    if (z >= g.I || y >= g.J || x >= g.K) return false;
+    r = lidx(g, z, y, x);
+    return true;
+}
+
+// Components the network serves: those with a cell on the level whose excess is above
+// kLpcAnchor of its diagonal (coupled to fixed values). Elsewhere the level is singular or
+// nearly so; a correction there would excite near-null modes that only smoothing removes,
+// so those cells keep the zero correction. anchored is indexed by component id (N bytes).
+constexpr float kLpcAnchor = 1e-3f;
+
+template <typename T>
+__global__ void k_lpc_anchor(Grid g, const int* __restrict__ comp, const T* __restrict__ e,
+                             const T* __restrict__ invd, uint8_t* __restrict__ anchored) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N; r += (long long)gridDim.x * blockDim.x) {
+        const int id = comp[r];
+        if (id >= 0 && (float)e[r] * (float)invd[r] > kLpcAnchor) anchored[id] = 1;
+    }
+}
+
+// the fixed inputs of a hierarchy: mask, anchoring fraction e/d (the share of the diagonal
+// that couples to fixed values) and 1/sqrt(d) of the cells of anchored components (0 marks
+// the cells the network does not serve)
+template <typename T>
+__global__ void k_lpc_setup(Grid g, int D, int H, int W, const int* __restrict__ comp, const T* __restrict__ e,
+                            const T* __restrict__ invd, const uint8_t* __restrict__ anchored,
+                            float* __restrict__ c0, float* __restrict__ c1, float* __restrict__ isd) {
+    const long long n = (long long)D * H * W;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+        long long r = 0;
+        float m = 0.f, a = 0.f;
+        if (lpc_cell(g, W, H, v, r)) {
+            float q = 0.f;
+            if (comp[r] >= 0 && anchored[comp[r]]) {
+                m = 1.f;
+                a = (float)e[r] * (float)invd[r];
+                q = sqrtf((float)invd[r]);
+            }
+            isd[r] = q;
+        }
+        c0[v] = m;
+        c1[v] = a;
+    }
+}
+
+// s = max |b| / sqrt(d) over the served cells (one block; NaN entries are passed over here and
+// reach the network through k_lpc_pack, whose output then carries them to the caller)
+__global__ void __launch_bounds__(1024) k_lpc_scale(Grid g, const int* __restrict__ comp, const float* __restrict__ b,
+                                                    const float* __restrict__ isd, double* __restrict__ out) {
+    float m = 0.f;
+    for (long long r = threadIdx.x; r < g.N; r += blockDim.x)
+        if (comp[r] >= 0) m = fmaxf(m, fabsf(b[r] * isd[r]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ float sh[32];
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = (threadIdx.x < (blockDim.x >> 5)) ? sh[threadIdx.x] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) *out = (double)m;
+    }
+}
+
+__global__ void k_lpc_pack(Grid g, int D, int H, int W, const int* __restrict__ comp, const float* __restrict__ b,
+                           const float* __restrict__ isd, const double* __restrict__ s, float* __restrict__ c2) {
+    const float inv = (*s > 0.0) ? (float)(1.0 / *s) : 0.f;
+    const long long n = (long long)D * H * W;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+        long long r = 0;
+        float val = 0.f;
+        if (lpc_cell(g, W, H, v, r) && comp[r] >= 0) val = b[r] * isd[r] * inv;  // isd 0: not served
+        c2[v] = val;
+    }
+}
+
+// x = s kLpcOutScale D^-1/2 y on the served cells, 0 on the other members (non-members keep
+// their 0)
+__global__ void k_lpc_unpack(Grid g, int H, int W, const int* __restrict__ comp, const float* __restrict__ y,
+                             const float* __restrict__ isd, const double* __restrict__ s, float* __restrict__ x) {
+    const float sc = (float)(*s) * kLpcOutScale;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N; r += (long long)gridDim.x * blockDim.x) {
+        if (comp[r] < 0) continue;
+        if (isd[r] == 0.f) {
+            x[r] = 0.f;
+            continue;
+        }
+        const int i = (int)(r / g.JK);
+        const long long rem = r - (long long)i * g.JK;
+        const int j = (int)(rem / g.K), k = (int)(rem - (long long)j * g.K);
+        x[r] = sc * isd[r] * y[((long long)i * H + j) * W + k];
+    }
+}
+
+ls_status lpnet_forward_on(ls_lpnet* n, cudaStream_t s, const float* c0, const float* c1, const float* c2,
+                           float* out, std::string* err);
+
+static int round8(int v) { return ((v + 7) / 8) * 8; }
+
+void mg_graphs_clear(ls_ctx* c);
+
+// Build (or reuse) the network for the learned level of the current hierarchy and its fixed
+// inputs. Without weights the learned solver is an argument error; a hierarchy too shallow
+// to have the level leaves the plain cycle in use.
+static ls_status lpc_prepare(ls_ctx* c) {
+    c->lpc_ready = 0;
+    if (c->p.press_solver != LS_PRESS_LEARNED) return LS_OK;
+    if (c->lpc_params.empty())
+        return set_error(c, LS_BAD_ARG, "learned pressure solver: no weights (ls_pressure_set_precond_weights)");
+    if (c->mg.size() < (size_t)kLearnedLevel) return LS_OK;
+    const auto& lv = c->mg[kLearnedLevel - 1];
+    const Grid lg = lv.g;
+    const int dims[3] = {round8(lg.I), round8(lg.J), round8(lg.K)};
+    if (!c->lpc || dims[0] != c->lpc_dims[0] || dims[1] != c->lpc_dims[1] || dims[2] != c->lpc_dims[2]) {
+        mg_graphs_clear(c);  // captured cycles name the old network's buffers
+        if (c->lpc) {
+            ls_lpnet_destroy(c->lpc);
+            c->lpc = nullptr;
+        }
+        float** arrs[] = {&c->lpc_c0, &c->lpc_c1, &c->lpc_c2, &c->lpc_out, &c->lpc_isd};
+        for (float** q : arrs)
+            if (*q) {
+                cudaFree(*q);
+                *q = nullptr;
+            }
+        ls_lpnet* n = nullptr;
+        ls_status st = ls_lpnet_create(dims[0], dims[1], dims[2], 0, &n);
+        if (st != LS_OK) return set_error(c, st, "learned pressure solver: network creation failed");
+        c->lpc = n;
+        if (ls_lpnet_param_count(n) != (long long)c->lpc_params.size())
+            return set_error(c, LS_BAD_ARG, "learned pressure solver: weight count does not match the network");
+        st = ls_lpnet_set_params(n, c->lpc_params.data(), (long long)c->lpc_params.size());
+        if (st != LS_OK) return set_error(c, st, "learned pressure solver: loading the weights failed");
+        const size_t nn = (size_t)dims[0] * dims[1] * dims[2];
+        LS_TRY(dalloc_t(c, &c->lpc_c0, nn));
+        LS_TRY(dalloc_t(c, &c->lpc_c1, nn));
+        LS_TRY(dalloc_t(c, &c->lpc_c2, nn));
+        LS_TRY(dalloc_t(c, &c->lpc_out, nn));
+        LS_TRY(dalloc_t(c, &c->lpc_isd, (size_t)lg.N));
+        for (int q = 0; q < 3; ++q) c->lpc_dims[q] = dims[q];
+    }
+    if (!c->lpc_anchor) LS_TRY(dalloc_t(c, &c->lpc_anchor, (size_t)c->g.N));
+    LS_CUDA(c, cudaMemsetAsync(c->lpc_anchor, 0, (size_t)c->g.N, c->stream));
+    LS_LAUNCH(c, k_lpc_anchor<float>, grid_for(c, lg.N), kBlock, 0, lg, (const int*)lv.comp, (const float*)lv.e,
+              (const float*)lv.invd, c->lpc_anchor);
+    const long long nn = (long long)dims[0] * dims[1] * dims[2];
+    LS_LAUNCH(c, k_lpc_setup<float>, grid_for(c, nn), kBlock, 0, lg, dims[0], dims[1], dims[2],
+              (const int*)lv.comp, (const float*)lv.e, (const float*)lv.invd, (const uint8_t*)c->lpc_anchor,
+              c->lpc_c0, c->lpc_c1, c->lpc_isd);
+    c->lpc_ready = 1;
+    return LS_OK;
+}
+
+// x = the network's approximation of M_l^-1 b on the learned level
+static ls_status lpc_solve(ls_ctx* c, const Grid& lg, const int* comp, const float* b, float* x) {
+    const int* d = c->lpc_dims;
+    const long long nn = (long long)d[0] * d[1] * d[2];
+    LS_LAUNCH(c, k_lpc_scale, 1, 1024, 0, lg, comp, b, (const float*)c->lpc_isd, c->scal + kLpcSlot);
+    LS_LAUNCH(c, k_lpc_pack, grid_for(c, nn), kBlock, 0, lg, d[0], d[1], d[2], comp, b, (const float*)c->lpc_isd,
+              (const double*)(c->scal + kLpcSlot), c->lpc_c2);
+    std::string err;
+    const ls_status st = lpnet_forward_on(c->lpc, c->stream, c->lpc_c0, c->lpc_c1, c->lpc_c2, c->lpc_out, &err);
+    if (st != LS_OK) return set_error(c, st, "learned coarse solve: " + err);
+    c->launches += 16;  // the network's own launches: input pack, 8 convolutions, 3 poolings, 3 upsamplings, output
+    LS_LAUNCH(c, k_lpc_unpack, grid_for(c, lg.N), kBlock, 0, lg, d[1], d[2], comp, (const float*)c->lpc_out,
+              (const float*)c->lpc_isd, (const double*)(c->scal + kLpcSlot), x);
+    return LS_OK;
+}
+
+// ---------------------------------------------------------------------------
 
 static Grid coarse_of(const Grid& f) {
     Grid c;
@@ -529,7 +715,14 @@ static Grid coarse_of(const Grid& f) {
     return c;
 }
 
+void mg_graphs_clear(ls_ctx* c) {
+    for (auto& gr : c->mg_graphs)
+        if (gr.exec) cudaGraphExecDestroy(gr.exec);
+    c->mg_graphs.clear();
+}
+
 void mg_free(ls_ctx* c) {
+    mg_graphs_clear(c);
     for (auto& lv : c->mg) {
         void* lp[] = {lv.comp, lv.e, lv.face[0], lv.face[1], lv.face[2], lv.invd, lv.x, lv.b, lv.t};
         for (void* q : lp)
@@ -624,6 +817,8 @@ ls_status mg_setup(ls_ctx* c) {
     LS_CUDA(c, cudaMemcpyAsync(&flag, c->cc_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     LS_CUDA(c, cudaStreamSynchronize(c->stream));
     if (flag) return set_error(c, LS_TIMEOUT, "multigrid: component labelling gave up");
+    if (std::is_same<T, float>::value) return lpc_prepare(c);
+    c->lpc_ready = 0;
     return LS_OK;
 }
 
@@ -668,6 +863,7 @@ ls_status mg_apply(ls_ctx* c, const T* r, T* z, const T* dotv2, int* nblocks_out
     }
     // one damped-Jacobi sweep on level l (paired finest-level kernel for FP32 and even K)
     const bool pair0 = std::is_same<T, float>::value && (c->g.K % 2 == 0);
+    const bool learned = std::is_same<T, float>::value && c->lpc_active && c->lpc_ready && L >= (size_t)kLearnedLevel;
     auto smooth = [&](size_t l, const T* b, const T* x, T* xo, const T* dv, const T* dv2, int* nb) -> ls_status {
         Lv& a = lv[l];
         double* partials = dv ? c->partials : (double*)nullptr;
@@ -742,6 +938,10 @@ ls_status mg_apply(ls_ctx* c, const T* r, T* z, const T* dotv2, int* nblocks_out
             LS_TRY(kfcg(l + 1));
             corr = cl.kv[6];
             scale = (T)1;  // the FCG steps carry the optimal scaling
+        } else if (learned && l + 1 == (size_t)kLearnedLevel) {
+            LS_TRY(lpc_solve(c, cl.g, cl.comp, (const float*)cl.b, (float*)cl.x));
+            corr = cl.x;
+            scale = (T)1;
         } else {
             LS_TRY(cycle(l + 1, (const T*)cl.b, cl.x, nullptr, nullptr, nullptr));
             corr = cl.x;
@@ -755,6 +955,53 @@ ls_status mg_apply(ls_ctx* c, const T* r, T* z, const T* dotv2, int* nblocks_out
     return cycle(0, r, z, r, dotv2, nblocks_out);
 }
 
+// z = B r and the partials of (r, z), (dotv2, z) finalized into slot, slot + 1. The cycle's
+// ~150 launches (most on coarse levels, a few microseconds each) are captured into a CUDA graph
+// on first use and replayed from then on: one launch per application.
+template <typename T>
+ls_status mg_precondition(ls_ctx* c, const T* r, T* z, const T* dotv2, int slot) {
+    const int learned = (std::is_same<T, float>::value && c->lpc_active && c->lpc_ready) ? 1 : 0;
+    const int is64 = sizeof(T) == 8;
+    if (c->mg_graphs_off) {
+        int nb = 0;
+        LS_TRY(mg_apply<T>(c, r, z, dotv2, &nb));
+        return finalize_sum(c, nb, 2, slot);
+    }
+    for (const auto& gr : c->mg_graphs)
+        if (gr.r == r && gr.z == z && gr.dv2 == dotv2 && gr.slot == slot && gr.learned == learned &&
+            gr.is64 == is64) {
+            LS_CUDA(c, cudaGraphLaunch(gr.exec, c->stream));
+            c->launches += gr.launches;
+            return LS_OK;
+        }
+    const long long l0 = c->launches;
+    LS_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int nb = 0;
+    ls_status st = mg_apply<T>(c, r, z, dotv2, &nb);
+    if (st == LS_OK) st = finalize_sum(c, nb, 2, slot);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(c->stream, &graph);
+    const long long n = c->launches - l0;
+    c->launches = l0;
+    if (st != LS_OK || ec != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return st != LS_OK ? st : set_error(c, LS_CUDA_ERROR, std::string("multigrid graph capture: ") +
+                                                                  cudaGetErrorString(ec));
+    }
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess)
+        return set_error(c, LS_CUDA_ERROR, std::string("multigrid graph instantiation: ") + cudaGetErrorString(ei));
+    c->mg_graphs.push_back(MGGraph{r, z, dotv2, slot, learned, is64, exec, n});
+    LS_CUDA(c, cudaGraphLaunch(exec, c->stream));
+    c->launches += n;
+    return LS_OK;
+}
+
+template ls_status mg_precondition<float>(ls_ctx*, const float*, float*, const float*, int);
+template ls_status mg_precondition<double>(ls_ctx*, const double*, double*, const double*, int);
 template ls_status inner_invd<float>(ls_ctx*);
 template ls_status inner_invd<double>(ls_ctx*);
 template ls_status mg_setup<float>(ls_ctx*);

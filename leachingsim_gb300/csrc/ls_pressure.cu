@@ -36,6 +36,8 @@ ls_status mg_clear(ls_ctx* c);
 template <typename T>
 ls_status mg_apply(ls_ctx* c, const T* r, T* z, const T* dotv2, int* nblocks_out);
 template <typename T>
+ls_status mg_precondition(ls_ctx* c, const T* r, T* z, const T* dotv2, int slot);
+template <typename T>
 ls_status inner_invd(ls_ctx* c);
 
 // scalar slots
@@ -726,19 +728,31 @@ static ls_status inner_pcg(ls_ctx* c, bool use_mg, double tol, int max_it, int* 
     const int pgrid = grid_for(c, g.N / 2);
     // z = B r and (r, z) into slot; with the multigrid, also (qv, z) into slot + 1
     auto precondition = [&](int slot, const T* qv) -> ls_status {
-        if (use_mg) {
-            int nb = 0;
-            LS_TRY(mg_apply<T>(c, (const T*)r, z, qv, &nb));
-            return finalize_sum(c, nb, 2, slot);
-        }
+        if (use_mg) return mg_precondition<T>(c, (const T*)r, z, qv, slot);
         LS_LAUNCH(c, k_cg_jacobi<T>, grid, kBlock, 0, g, (const T*)c->iinvd, (const T*)r, z, c->partials);
         return finalize_sum(c, grid, 1, slot);
     };
+    // With the learned coarse solver (c->lpc_active) the cycle is checked as it goes: a
+    // non-finite, negative or growing (r, z), a direction with (p, q) <= 0, two iterations in
+    // a row that reduce (r, z) by less than kLpcSlow, or four that reduce it by less than
+    // kLpcSlow^4 end the learned inner solve without a correction and hand the rest of the
+    // solve to the plain cycle.
+    const double kLpcSlow = 0.64;
+    bool learned = use_mg && c->lpc_active;
+    int slow = 0;
+    double rz_hist[4] = {0.0, 0.0, 0.0, 0.0};  // (r, z) of the last four iterations
     *its = 0;
     *rel_out = 0.0;
     LS_TRY(precondition(SP_RZ, nullptr));
     double rz0 = 0.0;
     LS_TRY(read_scalars(c, SP_RZ, 1, &rz0));
+    if (learned && !(rz0 >= 0.0 && rz0 < INFINITY)) {
+        learned = false;
+        c->lpc_active = 0;
+        c->press_fallbacks++;
+        LS_TRY(precondition(SP_RZ, nullptr));
+        LS_TRY(read_scalars(c, SP_RZ, 1, &rz0));
+    }
     if (rz0 != rz0) return set_error(c, LS_NONFINITE, "pressure: NaN in the inner right-hand side");
     if (!(rz0 > 0.0)) {
         LS_CUDA(c, cudaMemsetAsync(x, 0, sizeof(T) * (size_t)g.N, c->stream));
@@ -768,7 +782,27 @@ static ls_status inner_pcg(ls_ctx* c, bool use_mg, double tol, int max_it, int* 
         double sc[3];
         LS_TRY(read_scalars(c, SP_PQ, 2, sc));  // (p, q) and the new (r, z)
         double pq = sc[0];
+        const double rz_prev = rz;
         rz = sc[1];
+        if (learned) {
+            const bool bad = !(rz >= 0.0 && rz < INFINITY) || !(pq > 0.0) || rz > rz_prev;
+            slow = (rz > kLpcSlow * rz_prev) ? slow + 1 : 0;
+            const double rz4 = rz_hist[it & 3];  // (r, z) four iterations back (rz0 at it = 3)
+            const bool slow4 = it >= 3 && rz > kLpcSlow * kLpcSlow * kLpcSlow * kLpcSlow * (it == 3 ? rz0 : rz4);
+            rz_hist[it & 3] = rz;
+            if (bad || slow >= 2 || slow4) {
+                // Drop the learned iterations' correction and return: the FP64 refinement
+                // then runs the plain cycle from the iterate this inner solve started from.
+                // (Continuing from the learned iterate is no good: its error carries modes
+                // the plain cycle reduces slowly -- measured, 560-610 plain iterations from
+                // it against 28 from zero at 338x338x283.)
+                c->lpc_active = 0;
+                c->press_fallbacks++;
+                LS_CUDA(c, cudaMemsetAsync(x, 0, sizeof(T) * (size_t)g.N, c->stream));
+                rz = rz0;
+                break;
+            }
+        }
         if (rz != rz) return set_error(c, LS_NONFINITE, "pressure: NaN in inner PCG");
         if (rz <= target || !(pq > 0.0) || rz < 0.0) break;
         LS_LAUNCH(c, k_cg_dir<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const double*)c->scal,
@@ -1024,7 +1058,13 @@ ls_status pressure_solve_run(ls_ctx* c, ls_solve_info* info, const float* start,
     if (!c->p_ready) return set_error(c, LS_BAD_ARG, "pressure system not assembled");
     // a supplied start is relative to the effective (ramped) top pressure
     const double sc = start ? start_scale * (c->p_eff > 0.0 ? c->p_eff : 1.0) : 0.0;
-    if (c->p.press_solver == LS_PRESS_MIXED) return pressure_solve_t<float>(c, info, start, sc);
+    if (c->p.press_solver == LS_PRESS_MIXED || c->p.press_solver == LS_PRESS_LEARNED) {
+        // the learned coarse solver is on for this solve until the flexible CG stagnates
+        c->lpc_active = (c->p.press_solver == LS_PRESS_LEARNED) ? 1 : 0;
+        const ls_status st = pressure_solve_t<float>(c, info, start, sc);
+        c->lpc_active = 0;
+        return st;
+    }
     return pressure_solve_t<double>(c, info, start, sc);
 }
 

@@ -69,6 +69,34 @@ void Simulation::setupPETSc(bool) {
     ls_params p = solver;
     check(ls_create(&ctx_, global_.i, global_.j, global_.k, label_bytes_, &p), "ls_create");
     sync_params();
+    if (!precond_weights.empty())
+        check(ls_pressure_set_precond_weights(ctx_, precond_weights.data(), (long long)precond_weights.size()),
+              "ls_pressure_set_precond_weights");
+}
+
+std::vector<float> Simulation::loadNpyFloat32(const std::string& path) {
+    std::ifstream fin(path, std::ios::binary);
+    if (!fin.is_open()) throw std::runtime_error("Cannot open file: " + path);
+    char magic[8];
+    fin.read(magic, 8);
+    if (!fin || std::string(magic + 1, 5) != "NUMPY") throw std::runtime_error(path + ": not a .npy file");
+    size_t hlen = 0;
+    unsigned char b[4] = {0, 0, 0, 0};
+    const int lenbytes = (unsigned char)magic[6] == 1 ? 2 : 4;  // format version 1: 2-byte length
+    fin.read(reinterpret_cast<char*>(b), lenbytes);
+    for (int q = lenbytes - 1; q >= 0; --q) hlen = (hlen << 8) | b[q];
+    std::string header(hlen, ' ');
+    fin.read(&header[0], (std::streamsize)hlen);
+    if (!fin || header.find("'<f4'") == std::string::npos || header.find("'fortran_order': False") == std::string::npos)
+        throw std::runtime_error(path + ": expected a C-order little-endian float32 array");
+    const std::streampos data = fin.tellg();
+    fin.seekg(0, std::ios::end);
+    const size_t n = (size_t)(fin.tellg() - data) / sizeof(float);
+    fin.seekg(data);
+    std::vector<float> out(n);
+    fin.read(reinterpret_cast<char*>(out.data()), (std::streamsize)(n * sizeof(float)));
+    if (!fin) throw std::runtime_error(path + ": short read");
+    return out;
 }
 
 // Simulation::readRAW (src/Simulation.cpp:68-74, src/MPIRawLoader.h:49-107): the file holds

@@ -102,6 +102,11 @@ public:
     unsigned long long total_leached_count = 0;
     // solver controls (mapped from -press_/-conc_/-acid_/-sat_ PETSc options)
     ls_params solver;
+    // weights of the learned coarse solver (press_solver = LS_PRESS_LEARNED), handed to the
+    // context when it is created
+    std::vector<float> precond_weights;
+    // Read a little-endian float32 .npy vector (the trained weights as saved by numpy).
+    static std::vector<float> loadNpyFloat32(const std::string& path);
 
     int rank() const { return 0; }
     int3 global_extent() const { return global_; }

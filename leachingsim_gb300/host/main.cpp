@@ -11,6 +11,7 @@
 // width), --solid_density (never set by the reference), --compat_shift, --press_solver
 // mixed|fp64|jacobi64, --dry-run (parse, print the resolved configuration, exit).
 #include <sys/stat.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <cmath>
@@ -114,7 +115,8 @@ int main(int argc, char* argv[]) {
         op.add("label_bits", "8", "Bits per voxel label of the RAW file (8 or 16)");
         op.add("solid_density", "1", "Density of the precipitate (unset in the original code)");
         op.add("compat_shift", "true", "Solve results land one i-plane up, as on the original's rank 0");
-        op.add("press_solver", "mixed", "Pressure solver: mixed, fp64 or jacobi64");
+        op.add("press_solver", "mixed", "Pressure solver: mixed, fp64, jacobi64 or learned");
+        op.add("precond_weights", "", "Weights (.npy) of the learned coarse solver (default: the shipped ones)");
         op.add("dry-run", "false", "Parse the options, print the configuration and exit");
 
         for (int a = 1; a < argc; ++a) {
@@ -183,7 +185,20 @@ int main(int argc, char* argv[]) {
             if (ps == "mixed") sim.solver.press_solver = LS_PRESS_MIXED;
             else if (ps == "fp64") sim.solver.press_solver = LS_PRESS_FP64;
             else if (ps == "jacobi64") sim.solver.press_solver = LS_PRESS_JACOBI64;
-            else throw runtime_error("--press_solver must be mixed, fp64 or jacobi64");
+            else if (ps == "learned") sim.solver.press_solver = LS_PRESS_LEARNED;
+            else throw runtime_error("--press_solver must be mixed, fp64, jacobi64 or learned");
+            if (ps == "learned") {
+                string wp = op.str("precond_weights");
+                if (wp.empty()) {
+                    // beside the executable, where the package ships them
+                    char buf[4096];
+                    const ssize_t len = readlink("/proc/self/exe", buf, sizeof(buf) - 1);
+                    string exe = len > 0 ? string(buf, (size_t)len) : string(argv[0]);
+                    const size_t slash = exe.rfind('/');
+                    wp = (slash == string::npos ? string(".") : exe.substr(0, slash)) + "/lpnet_precond_weights.npy";
+                }
+                sim.precond_weights = lsh::Simulation::loadNpyFloat32(wp);
+            }
         }
         // PETSc option passthrough onto this library's solvers
         for (size_t q = 0; q < op.unregistered.size(); ++q) {

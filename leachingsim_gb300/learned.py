@@ -253,6 +253,184 @@ def train(samples=256, epochs=64, lr=2e-3, seed=0, shape=PATCH, log=print, wide=
                   "train_s": round(train_s, 1), "loss": hist}
 
 
+# ---------------------------------------------------------------------------
+# The learned coarse solver of the pressure multigrid (press_solver = PRESS_LEARNED): the
+# same network, at 1/8 resolution, standing in for the V-cycle below the K-cycle levels.
+# Its inputs are the member mask of multigrid level 3, the anchoring fraction e/d of each
+# cell and the Jacobi-scaled residual D^-1/2 b / s (s = max |D^-1/2 b|); it predicts the
+# Jacobi-scaled correction D^1/2 x / (s LPC_OUT_SCALE) with x ~ M^-1 b. It is trained on the
+# level-3 operators of the plain solver's hierarchies for seeded geometries: for random
+# errors x (white noise and Gaussian-smoothed noise of several correlation lengths, on the
+# member cells) the input is b = M x and the target x itself, so no solve is needed.
+
+PRECOND_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lpnet_precond_weights.npy")
+LPC_LEVEL = 3
+LPC_OUT_SCALE = 64.0   # kLpcOutScale of csrc/ls_mg.cu
+LPC_SIGMAS = (0.0, 0.7, 1.5, 3.0, 6.0)
+
+
+def level_apply(op, x):
+    """M x of a multigrid level held as excess + links (float64): (M x)_i = e_i x_i +
+    sum_j c_ij (x_i - x_j), f0/f1/f2 the links of the +i/+j/+k faces."""
+    y = op["e"].astype(np.float64) * x
+    for ax, f in enumerate(("f0", "f1", "f2")):
+        c = np.asarray(op[f], np.float64)
+        lo = [slice(None)] * 3
+        hi = [slice(None)] * 3
+        lo[ax] = slice(0, -1)
+        hi[ax] = slice(1, None)
+        lo, hi = tuple(lo), tuple(hi)
+        d = c[lo] * (x[lo] - x[hi])
+        y[lo] += d
+        y[hi] -= d
+    return y
+
+
+def level_diag(op):
+    d = op["e"].astype(np.float64).copy()
+    for ax, f in enumerate(("f0", "f1", "f2")):
+        c = np.asarray(op[f], np.float64)
+        lo = [slice(None)] * 3
+        hi = [slice(None)] * 3
+        lo[ax] = slice(0, -1)
+        hi[ax] = slice(1, None)
+        d[tuple(lo)] += c[tuple(lo)]
+        d[tuple(hi)] += c[tuple(lo)]
+    return d
+
+
+LPC_ANCHOR = 1e-3     # kLpcAnchor of csrc/ls_mg.cu
+
+
+def precond_inputs(op):
+    """Mask of the cells the network serves (members of components with a cell whose excess
+    is above LPC_ANCHOR of its diagonal), anchoring fraction e/d and 1/sqrt(d) of those
+    cells (float64 arrays)."""
+    comp = op["comp"]
+    m = comp >= 0
+    d = level_diag(op)
+    frac = np.where(m & (d > 0), op["e"] / np.where(d > 0, d, 1.0), 0.0)
+    ids = np.unique(comp[m & (frac.astype(np.float32) > np.float32(LPC_ANCHOR))])
+    ok = m & (d > 0) & np.isin(comp, ids)
+    isd = np.where(ok, 1.0 / np.sqrt(np.where(ok, d, 1.0)), 0.0)
+    anchor = np.where(ok, frac, 0.0)
+    return ok, anchor, isd
+
+
+def precond_samples(op, count, rng, net_shape):
+    """count (mask, anchor, input, target) samples for one level operator, padded to the
+    network grid."""
+    from scipy.ndimage import gaussian_filter
+    m, anchor, isd = precond_inputs(op)
+    shape = m.shape
+
+    def pad(a):
+        out = np.zeros(net_shape, np.float32)
+        out[:shape[0], :shape[1], :shape[2]] = a
+        return out
+
+    out = []
+    while len(out) < count:
+        sigma = float(rng.choice(LPC_SIGMAS))
+        x = rng.standard_normal(shape)
+        if sigma > 0:
+            x = gaussian_filter(x, sigma, mode="nearest")
+        x = x * m
+        r = level_apply(op, x) * m
+        rh = r * isd
+        s = float(np.abs(rh).max())
+        if not (s > 0):
+            continue
+        tgt = np.where(m, x / np.where(m, isd, 1.0) / (s * LPC_OUT_SCALE), 0.0)
+        out.append((pad(m), pad(anchor), pad(rh / s), pad(tgt)))
+    return out
+
+
+def precond_level(seed, shape=WIDE, level=LPC_LEVEL, t=RAMP):
+    """The level-`level` operator of the plain solver's hierarchy for one seeded geometry."""
+    import torch
+    from .runtime import Context
+    lab, meta = patch_geometry(seed, shape)
+    ctx = Context(shape, params=solver_params())
+    try:
+        ctx.upload("label", lab)
+        ctx.init_all()
+        ctx.props()
+        ctx.pressure_setup(t)
+        ok, info = ctx.pressure_solve_start(torch.zeros(shape, dtype=torch.float32, device="cuda"), 0.0)
+        if not ok:
+            raise RuntimeError(f"plain solve failed on geometry {seed}: {info}")
+        op = ctx.mg_level(level)
+    finally:
+        ctx.close()
+    return op, dict(meta, iterations=info["iterations"])
+
+
+def train_precond(geometries=8, per_geometry=128, epochs=24, lr=2e-3, seed=0, shape=WIDE, log=print):
+    """Train the learned coarse solver; returns (flat parameters, history)."""
+    from .runtime import LPNet
+    rng = np.random.default_rng(seed)
+    t0 = time.time()
+    data, metas, net_shape = [], [], None
+    for g in range(geometries):
+        op, meta = precond_level(seed * 100003 + 7919 * (g + 1), shape)
+        ns = pad8(op["shape"])
+        if net_shape is None:
+            net_shape = ns
+        if ns != net_shape:
+            raise RuntimeError("training geometries must share the level grid")
+        data.extend(precond_samples(op, per_geometry, rng, net_shape))
+        metas.append(meta)
+    gen_s = time.time() - t0
+    log(f"generated {len(data)} samples from {len(metas)} level-{LPC_LEVEL} operators of {net_shape} "
+        f"in {gen_s:.1f}s")
+    import torch
+    dev = [tuple(torch.from_numpy(a).cuda() for a in d) for d in data]
+    net = LPNet(net_shape, seed=seed + 1)
+    hist = []
+    t1 = time.time()
+    n = len(dev)
+    steps = epochs * n
+    for ep in range(epochs):
+        order = rng.permutation(n)
+        losses = []
+        for q, i in enumerate(order):
+            rate = lr * 0.5 * (1.0 + math.cos(math.pi * (ep * n + q) / steps))
+            m, a, x, tgt = dev[i]
+            losses.append(net.train_step(m, a, x, tgt, m, lr=rate))
+        hist.append(float(np.mean(losses)))
+        log(f"epoch {ep}: mean loss {hist[-1]:.3e}")
+    train_s = time.time() - t1
+    flat = net.get_params()
+    net.close()
+    return flat, {"geometries": geometries, "samples": n, "epochs": epochs, "lr": lr,
+                  "net_shape": list(net_shape), "generate_s": round(gen_s, 1), "train_s": round(train_s, 1),
+                  "loss": hist}
+
+
+def precond_quality(flat, op, count=32, seed=1):
+    """Mean relative error ||x - x_net|| / ||x|| (Jacobi-scaled) of the network on random
+    samples of a level operator (random errors x as in training); flat None: the zero
+    correction (error 1)."""
+    from .runtime import LPNet
+    rng = np.random.default_rng(seed)
+    ns = pad8(op["shape"])
+    samples = precond_samples(op, count, rng, ns)
+    net = LPNet(ns)
+    if flat is not None:
+        net.set_params(flat)
+    errs = []
+    for m, a, x, tgt in samples:
+        y = net.forward(m, a, x).cpu().numpy() * m
+        errs.append(float(np.linalg.norm(y - tgt) / max(np.linalg.norm(tgt), 1e-30)))
+    net.close()
+    return float(np.mean(errs))
+
+
+def load_precond_weights(path=PRECOND_WEIGHTS):
+    return np.load(path) if os.path.exists(path) else None
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -264,6 +442,13 @@ def main(argv=None):
     tr.add_argument("--out", default=WEIGHTS)
     tr.add_argument("--patches", action="store_true",
                     help="solve each sample on its own (default: cut the samples from wide solves)")
+    tp = sub.add_parser("train-precond", help="train the learned coarse solver of the pressure multigrid")
+    tp.add_argument("--geometries", type=int, default=8)
+    tp.add_argument("--per-geometry", type=int, default=128)
+    tp.add_argument("--epochs", type=int, default=24)
+    tp.add_argument("--lr", type=float, default=2e-3)
+    tp.add_argument("--seed", type=int, default=0)
+    tp.add_argument("--out", default=PRECOND_WEIGHTS)
     fw = sub.add_parser("forward", help="time the network's forward pass on random inputs")
     fw.add_argument("--shape", default="144,176,176", help="network grid (multiples of 8)")
     fw.add_argument("--reps", type=int, default=5)
@@ -292,6 +477,11 @@ def main(argv=None):
         print(json.dumps({"shape": shape, "ms": round(best, 3), "tflops": round(flops / best / 1e9, 1),
                           "times_ms": [round(t, 3) for t in times]}))
         net.close()
+    if a.cmd == "train-precond":
+        flat, hist = train_precond(a.geometries, a.per_geometry, a.epochs, a.lr, a.seed,
+                                   log=lambda *x: print(*x, file=sys.stderr, flush=True))
+        np.save(a.out, flat)
+        print(json.dumps(hist))
     if a.cmd == "train":
         flat, hist = train(a.samples, a.epochs, a.lr, a.seed, log=lambda *x: print(*x, file=sys.stderr, flush=True),
                            wide=None if a.patches else WIDE)

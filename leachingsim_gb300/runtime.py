@@ -71,6 +71,10 @@ SYMBOLS = {
                                       C.c_longlong, C.c_float, C.c_int, C.POINTER(C.c_double)]),
     "ls_pressure_learned_inputs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ls_pressure_solve_start": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.POINTER(LsSolveInfo)]),
+    "ls_pressure_set_precond_weights": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
+    "ls_pressure_fallbacks": (C.c_longlong, [C.c_void_p]),
+    "ls_pressure_mg_level": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p]),
     "ls_field_pool2": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ls_field_up2": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     "ls_geom_distance": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
@@ -437,6 +441,29 @@ class Context:
         st = self._check(load().ls_pressure_solve_start(self.h, C.c_void_p(start.data_ptr()), float(scale),
                                                         C.byref(info)), (0, 1, 2, 3))
         return st in (0, 2), info.as_dict()
+
+    def set_precond_weights(self, flat):
+        """Weights of the learned coarse solver of the pressure multigrid (press_solver =
+        PRESS_LEARNED): the flat float32 parameter vector of an ls_lpnet."""
+        w = np.ascontiguousarray(flat, dtype=np.float32).ravel()
+        self._check(load().ls_pressure_set_precond_weights(self.h, _p(w), w.size))
+
+    def pressure_fallbacks(self):
+        """Learned pressure solves on this context that fell back to the plain cycle."""
+        return int(load().ls_pressure_fallbacks(self.h))
+
+    def mg_level(self, level):
+        """Multigrid level `level` of the last FP32-inner pressure solve: dict with its shape
+        and host copies of comp (int32), e, f0, f1, f2 (float32)."""
+        dims = np.zeros(3, dtype=np.int32)
+        self._check(load().ls_pressure_mg_level(self.h, int(level), _p(dims), None, None, None, None, None))
+        shape = tuple(int(v) for v in dims)
+        out = {"shape": shape, "comp": np.empty(shape, np.int32)}
+        for k in ("e", "f0", "f1", "f2"):
+            out[k] = np.empty(shape, np.float32)
+        self._check(load().ls_pressure_mg_level(self.h, int(level), _p(dims), _p(out["comp"]), _p(out["e"]),
+                                                _p(out["f0"]), _p(out["f1"]), _p(out["f2"])))
+        return out
 
     def flux(self):
         self._check(load().ls_flux(self.h))
