@@ -5,10 +5,16 @@
 // every start through the FP64 residual and finishes the solve.
 //
 // Kernels, all hand-written:
-//  * k_lp_conv: 3x3x3 convolution as an implicit GEMM on the tensor cores
-//    (mma.sync m16n8k16, BF16 x BF16 -> FP32): a warp computes 16 output voxels x all output
-//    channels; the K dimension runs over 27 taps x input channels in chunks of 16. The same
-//    kernel with flipped, transposed weights is the backward pass for the input gradient.
+//  * k_lp_conv_tc: 3x3x3 convolution as an implicit GEMM on the 5th-generation tensor cores
+//    (tcgen05.mma kind::f16, BF16 x BF16 -> FP32 accumulators in tensor memory): a CTA
+//    computes 16 x 8 x ZT output voxels (M = 128 per plane) x all output channels from
+//    shared-memory operands. Used where it is the faster kernel (32 -> 64 channels; every
+//    layer with up to 32 input channels under LS_LPNET_TC=2). With flipped, transposed
+//    weights it is also the input-gradient pass.
+//  * k_lp_conv / k_lp_conv_tiled: the same convolution with mma.sync m16n8k16 (BF16 x BF16
+//    -> FP32 in registers): a warp computes 16 output voxels x all output channels; the K
+//    dimension runs over 27 taps x input channels in chunks of 16. k_lp_conv serves the
+//    64-channel layers; k_lp_conv_tiled is the LS_LPNET_TC=0 path of the others.
 //  * k_lp_conv_dw: the weight / bias gradient, staged through shared memory, FP32 FMA.
 //  * pooling, upsampling + skip addition and their backward passes, ReLU masking, the
 //    masked mean-square loss and Adam.
@@ -19,6 +25,7 @@
 #include <cuda_bf16.h>
 
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -220,6 +227,191 @@ __global__ void __launch_bounds__(128) k_lp_conv_tiled(LpDims d, const bf16* __r
             if (xb < d.W) store_pair<OutT>(out + rb * COUT + co, c2, c3);
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// The same convolution on the 5th-generation tensor cores (tcgen05): a CTA computes a
+// 16 (x) x 8 (y) x ZT (z) block of output voxels as ZT implicit GEMMs of M = 128 (one per
+// plane), D_p[m][co] = sum over the 27 taps and CIN/16 K-steps of A_tap,p[m][k] B_tap[co][k],
+// accumulated in tensor memory (TMEM, FP32, COUT columns per plane) by 27 ZT CIN/16
+// tcgen05.mma instructions that one thread issues back to back; a tcgen05.commit on an
+// mbarrier signals completion and the eight warps read the TMEM lanes (rows) of their lane
+// quarter back for the bias / ReLU epilogue, two planes at a time. ZT planes share one
+// staging of the weights and of the input halo, which cp.async copies bring in (zero-filled
+// outside the grid) all in flight at once.
+//
+// Operands live in shared memory in the SWIZZLE_NONE K-major layout: 8 x 16-byte "core
+// matrices" (8 rows of 8 BF16), the descriptor's leading byte offset (LBO) stepping along K
+// and its stride byte offset (SBO) along M / N. The input halo is staged three times, once
+// per x-shift dx = -1, 0, +1, each as [8-channel chunk][ZT + 2 planes][10 rows][16 voxels] x
+// 16 B, so every tap's A operand is a plain descriptor: start = the (dx, plane + dz, dy) row,
+// SBO = 128 B (8 voxels), LBO = one chunk (all planes). The weights sit as [tap][K-step][k8]
+// [n8] core matrices (SBO = 128 B, LBO = COUT/8 x 128 B). Instruction descriptor: FP32
+// accumulator, BF16 A and B, both K-major, N = COUT, M = 128.
+constexpr int kTcX = 16, kTcY = 8, kTcRows = kTcY + 2;
+
+__device__ int g_lp_tc_timeouts;  // CTAs whose wait for the tensor cores gave up
+
+template <int CIN, int COUT, int ZT>
+struct TcShape {
+    static constexpr int KC = CIN / 16;
+    static constexpr int planes = ZT + 2;
+    static constexpr int chunk_bytes = planes * kTcRows * kTcX * 16;  // one 8-channel chunk of one copy
+    static constexpr int copy_bytes = (CIN / 8) * chunk_bytes;
+    static constexpr int a_bytes = 3 * copy_bytes;
+    static constexpr int w_bytes = 27 * CIN * COUT * 2;
+    static constexpr int smem = a_bytes + w_bytes;
+    static constexpr int cols = ZT * COUT;
+    static constexpr int tmem_cols = cols <= 32 ? 32 : cols <= 64 ? 64 : cols <= 128 ? 128 : cols <= 256 ? 256 : 512;
+};
+
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);  // version 1, SWIZZLE_NONE
+}
+
+constexpr int kTcThreads = 256;
+
+// 16-byte asynchronous global -> shared copy; valid == false fills the 16 bytes with zeros
+// (source size 0: nothing is read)
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool valid) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+
+template <int CIN, int COUT, int ZT, bool RELU, typename OutT>
+__global__ void __launch_bounds__(kTcThreads) k_lp_conv_tc(LpDims d, const bf16* __restrict__ in,
+                                                           const bf16* __restrict__ w, const float* __restrict__ bias,
+                                                           OutT* __restrict__ out) {
+    using S = TcShape<CIN, COUT, ZT>;
+    static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 64 && S::cols <= 256, "channel counts");
+    extern __shared__ __align__(1024) uint8_t tc_smem[];
+    __shared__ uint32_t tmem_slot;
+    __shared__ __align__(8) uint64_t mbar;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int x0 = blockIdx.x * kTcX, y0 = blockIdx.y * kTcY, z0 = blockIdx.z * ZT;
+    uint8_t* sA = tc_smem;
+    uint8_t* sW = tc_smem + S::a_bytes;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         (uint32_t)__cvta_generic_to_shared(&tmem_slot)),
+                     "r"(S::tmem_cols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    if (tid == 0)
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"((uint32_t)__cvta_generic_to_shared(&mbar)),
+                     "r"(1));
+    // input halo: three x-shifted copies, zeros outside the grid (asynchronous copies, all
+    // in flight at once)
+    constexpr int CH = CIN / 8;
+    const uint32_t sA_s = (uint32_t)__cvta_generic_to_shared(sA), sW_s = (uint32_t)__cvta_generic_to_shared(sW);
+    for (int e = tid; e < 3 * CH * S::planes * kTcRows * kTcX; e += kTcThreads) {
+        const int x = e % kTcX;
+        int r = e / kTcX;
+        const int ry = r % kTcRows;
+        r /= kTcRows;
+        const int pz = r % S::planes;
+        r /= S::planes;
+        const int q = r % CH, cp = r / CH;
+        const int gx = x0 + x + cp - 1, gy = y0 + ry - 1, gz = z0 + pz - 1;
+        const bool ok = gx >= 0 && gx < d.W && gy >= 0 && gy < d.H && gz >= 0 && gz < d.D;
+        const bf16* src = ok ? in + (((long long)gz * d.H + gy) * d.W + gx) * CIN + q * 8 : in;
+        cp_async16(sA_s + cp * S::copy_bytes + q * S::chunk_bytes + ((pz * kTcRows + ry) * kTcX + x) * 16, src, ok);
+    }
+    // weights [tap][co][ci] -> [tap][K-step][k8][n8] core matrices
+    for (int e = tid; e < 27 * COUT * CH; e += kTcThreads) {
+        const int q = e % CH;
+        const int co = (e / CH) % COUT, t = e / (CH * COUT);
+        const int kc = q >> 1, k8 = q & 1;
+        cp_async16(sW_s + ((((t * S::KC + kc) * 2 + k8) * (COUT / 8) + (co >> 3)) * 128) + (co & 7) * 16,
+                   w + ((size_t)t * COUT + co) * CIN + q * 8, true);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    const uint32_t mbar_s = (uint32_t)__cvta_generic_to_shared(&mbar);
+    if (tid == 0) {
+        // The start address sits in the descriptor's low 14 bits (address >> 4, < 256 KB), so
+        // each operand's descriptor is a base descriptor plus a compile-time offset: the tap and
+        // K-step loops unroll into bare MMA issues.
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(COUT >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+        const uint64_t da0 = tc_desc((uint32_t)__cvta_generic_to_shared(sA), S::chunk_bytes, 128);
+        const uint64_t db0 = tc_desc((uint32_t)__cvta_generic_to_shared(sW), (COUT / 8) * 128, 128);
+        for (int p = 0; p < ZT; ++p) {
+            const uint64_t dap = da0 + (uint64_t)((p * kTcRows * kTcX * 16) >> 4);
+            const uint32_t dtm = tmem + (uint32_t)(p * COUT);
+#pragma unroll
+            for (int t = 0; t < 27; ++t) {
+                const int dz = t / 9 - 1, dy = (t / 3) % 3 - 1, dx = t % 3 - 1;
+#pragma unroll
+                for (int kc = 0; kc < S::KC; ++kc) {
+                    const uint64_t da = dap + (uint64_t)(((dx + 1) * S::copy_bytes + 2 * kc * S::chunk_bytes +
+                                                          (((1 + dz) * kTcRows + (1 + dy)) * kTcX) * 16) >> 4);
+                    const uint64_t db = db0 + (uint64_t)(((t * S::KC + kc) * 2 * (COUT / 8) * 128) >> 4);
+                    const uint32_t acc = (t | kc) ? 1u : 0u;
+                    asm volatile(
+                        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtm),
+                        "l"(da), "l"(db), "r"(idesc), "r"(acc));
+                }
+            }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar_s));
+    }
+    // bounded wait for the MMAs (phase 0); warps other than the issuing one back off so that
+    // their polling does not take issue slots from it
+    uint32_t done = 0;
+    for (int it = 0; it < (1 << 22) && !done; ++it) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(mbar_s), "r"(0));
+        if (!done && warp != 0) __nanosleep(64);
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (done) {
+        // warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows m), of the planes p = w / 4 (mod 2)
+        const int m = (warp & 3) * 32 + lane;
+        const int x = x0 + (m % kTcX), y = y0 + m / kTcX;
+        const bool okxy = x < d.W && y < d.H;
+        for (int p = warp >> 2; p < ZT; p += kTcThreads / 128) {
+            const bool ok = okxy && z0 + p < d.D;
+            const long long v = ((long long)(z0 + p) * d.H + y) * d.W + x;
+#pragma unroll
+            for (int c0 = 0; c0 < COUT; c0 += 16) {
+                uint32_t r[16];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                    : "r"(tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(p * COUT + c0)));
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                if (ok) {
+#pragma unroll
+                    for (int q = 0; q < 16; q += 2) {
+                        const int co = c0 + q;
+                        float a = __uint_as_float(r[q]) + (bias ? bias[co] : 0.f);
+                        float b = __uint_as_float(r[q + 1]) + (bias ? bias[co + 1] : 0.f);
+                        if (RELU) {
+                            a = fmaxf(a, 0.f);
+                            b = fmaxf(b, 0.f);
+                        }
+                        store_pair<OutT>(out + v * COUT + co, a, b);
+                    }
+                }
+            }
+        }
+    } else if (tid == 0) {
+        atomicAdd(&g_lp_tc_timeouts, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(S::tmem_cols));
 }
 
 // dw[tap][co][ci] += sum_v dy[v, co] in[v + tap, ci]; db[co] += sum_v dy[v, co] (tap 13).
@@ -497,6 +689,8 @@ using ls::LpLayer;
 struct ls_lpnet {
     int D, H, W;
     int device, num_sms;
+    int use_tc;             // tcgen05 convolutions: 0 none, 1 where measured faster than mma.sync
+                            // (32 -> 64 channels), 2 every layer with CIN <= 32 (LS_LPNET_TC)
     cudaStream_t stream;
     LpLayer layer[kLpLayers];
     size_t nparam, nweight_bf;
@@ -558,9 +752,47 @@ int lp_grid(const ls_lpnet* n, long long work, int block) {
 }
 
 // conv forward / input-gradient dispatch over the channel pairs of the network
+// planes per CTA: for 16 input channels few enough that two CTAs share an SM (<= 113 KB of
+// shared memory each: one CTA stages while the other's MMAs run), for 32 as many as fit
+template <int CI, int CO>
+struct TcPlanes {
+    static constexpr int value = (CI == 16) ? (CO <= 16 ? 4 : 3) : (CO <= 16 ? 4 : 1);
+};
+
+template <int CI, int CO, bool RELU, typename OutT>
+ls_status lp_conv_tc(ls_lpnet* n, LpDims d, const bf16* in, const bf16* w, const float* bias, OutT* out) {
+    constexpr int ZT = TcPlanes<CI, CO>::value;
+    constexpr int smem = ls::TcShape<CI, CO, ZT>::smem;
+    static_assert(smem + 1024 <= 227 * 1024, "shared memory per CTA");
+    static bool attr = false;  // the dynamic shared-memory opt-in, once per instantiation
+    if (!attr) {
+        LP_CUDA(n, cudaFuncSetAttribute(ls::k_lp_conv_tc<CI, CO, ZT, RELU, OutT>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        attr = true;
+    }
+    const dim3 grid((unsigned)((d.W + ls::kTcX - 1) / ls::kTcX), (unsigned)((d.H + ls::kTcY - 1) / ls::kTcY),
+                    (unsigned)((d.D + ZT - 1) / ZT));
+    ls::k_lp_conv_tc<CI, CO, ZT, RELU, OutT><<<grid, ls::kTcThreads, smem, n->stream>>>(d, in, w, bias, out);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return lp_fail(n, "k_lp_conv_tc", e);
+    return LS_OK;
+}
+
 template <bool RELU, typename OutT>
 ls_status lp_conv(ls_lpnet* n, LpDims d, int cin, int cout, const bf16* in, const bf16* w, const float* bias,
                   OutT* out) {
+    // tcgen05 where it beats the mma.sync kernels: measured per layer of the 144x176x176
+    // network, the 32 -> 64 convolution (M = 128 x N = 64 MMAs) runs 62 us against 67; with
+    // N = 16 or 32 the MMAs are too narrow to pay for the operand staging (16 -> 16: 389
+    // against 308 us), so those layers stay on mma.sync unless LS_LPNET_TC=2
+    if (n->use_tc == 2) {
+#define LP_TC(CI, CO) \
+        if (cin == CI && cout == CO) return lp_conv_tc<CI, CO, RELU, OutT>(n, d, in, w, bias, out);
+        LP_TC(16, 16) LP_TC(16, 32) LP_TC(32, 64) LP_TC(32, 16)
+#undef LP_TC
+    } else if (n->use_tc == 1 && cin == 32 && cout == 64) {
+        return lp_conv_tc<32, 64, RELU, OutT>(n, d, in, w, bias, out);
+    }
     if (cin <= 32) {
         const dim3 tg((unsigned)((d.W + ls::kTX - 1) / ls::kTX), (unsigned)((d.H + ls::kTY - 1) / ls::kTY),
                       (unsigned)((d.D + ls::kTZ - 1) / ls::kTZ));
@@ -716,6 +948,10 @@ ls_status ls_lpnet_create(int D, int H, int W, int seed, ls_lpnet** out) {
     ls_status st = LS_OK;
     auto fail = [&](ls_status s) { ls_lpnet_destroy(n); return s; };
     if (cudaGetDevice(&n->device) != cudaSuccess) return fail(LS_CUDA_ERROR);
+    {
+        const char* tc = getenv("LS_LPNET_TC");
+        n->use_tc = (tc && (tc[0] == '0' || tc[0] == '2')) ? tc[0] - '0' : 1;
+    }
     cudaDeviceGetAttribute(&n->num_sms, cudaDevAttrMultiProcessorCount, n->device);
     if (cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(LS_CUDA_ERROR);
     size_t off = 0, boff = 0;

@@ -70,12 +70,24 @@ def test_parameter_layout_round_trip():
     assert lpnet_flatten(p).size == sum(27 * ci * co + co for _, ci, co, _ in lo.LAYERS)
 
 
+# convolution paths (LS_LPNET_TC, read when a network is created): "tc" = tcgen05 with TMEM
+# accumulators for every layer with up to 32 input channels (2), "auto" = tcgen05 where it is
+# the faster kernel, the 32 -> 64 layer (1, the default), "mma" = mma.sync only (0)
+PATHS = ["tc", "auto", "mma"]
+
+
+def _path(monkeypatch, path):
+    monkeypatch.setenv("LS_LPNET_TC", {"tc": "2", "auto": "1", "mma": "0"}[path])
+
+
 @pytest.mark.gpu
+@pytest.mark.parametrize("path", PATHS)
 @pytest.mark.parametrize("shape", [(16, 16, 24), (24, 40, 8), (8, 24, 56)])
-def test_gpu_forward_matches_oracle(shape):
-    """Grids whose extents are not multiples of the 16 x 4 x 2 convolution tile, down to
-    coarse levels of odd extent."""
+def test_gpu_forward_matches_oracle(shape, path, monkeypatch):
+    """Grids whose extents are not multiples of the convolution tiles (16 x 8 x 1 for
+    tcgen05, 16 x 4 x 2 for mma.sync), down to coarse levels of odd extent."""
     from leachingsim_gb300.runtime import LPNet, lpnet_flatten
+    _path(monkeypatch, path)
     p, mask, c1, c2, _ = _case(shape, 1)
     net = LPNet(shape)
     net.set_params(lpnet_flatten(p))
@@ -86,8 +98,10 @@ def test_gpu_forward_matches_oracle(shape):
 
 
 @pytest.mark.gpu
-def test_gpu_gradients_match_oracle():
+@pytest.mark.parametrize("path", PATHS)
+def test_gpu_gradients_match_oracle(path, monkeypatch):
     from leachingsim_gb300.runtime import LPNet, lpnet_flatten, lpnet_unflatten
+    _path(monkeypatch, path)
     shape = (16, 24, 16)
     p, mask, c1, c2, target = _case(shape, 2)
     net = LPNet(shape)
@@ -145,3 +159,21 @@ def test_gpu_training_reduces_loss():
         losses.append(net.train_step(mask, c1, np.zeros(shape, np.float32), target, mask, lr=2e-3))
     assert np.mean(losses[-10:]) < 0.3 * np.mean(losses[:10]), (losses[:10], losses[-10:])
     net.close()
+
+
+@pytest.mark.gpu
+def test_gpu_tcgen05_and_mma_sync_paths_agree(monkeypatch):
+    """Both convolution paths sum the same BF16 products in FP32, in different orders: the
+    outputs agree far inside the oracle tolerance, at a size with many tiles per level."""
+    from leachingsim_gb300.runtime import LPNet, lpnet_flatten
+    shape = (32, 48, 80)
+    p, mask, c1, c2, _ = _case(shape, 6)
+    outs = {}
+    for path in PATHS:
+        _path(monkeypatch, path)
+        net = LPNet(shape)
+        net.set_params(lpnet_flatten(p))
+        outs[path] = net.forward(mask, c1, c2).cpu().numpy()
+        net.close()
+    assert _rel(outs["tc"], outs["mma"]) < 5e-3
+    assert _rel(outs["auto"], outs["mma"]) < 5e-3
