@@ -272,10 +272,11 @@ __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32
 
 constexpr int kTcThreads = 256;
 
-// 16-byte asynchronous global -> shared copy; valid == false fills the 16 bytes with zeros
-// (source size 0: nothing is read)
+// 16-byte asynchronous global -> shared copy through L1 (the three x-shifted copies and the
+// two halves of a 32-byte voxel hit the same lines); valid == false fills the 16 bytes with
+// zeros (source size 0: nothing is read)
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool valid) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0)
                  : "memory");
 }
 
@@ -782,8 +783,8 @@ template <bool RELU, typename OutT>
 ls_status lp_conv(ls_lpnet* n, LpDims d, int cin, int cout, const bf16* in, const bf16* w, const float* bias,
                   OutT* out) {
     // tcgen05 where it beats the mma.sync kernels: measured per layer of the 144x176x176
-    // network, the 32 -> 64 convolution (M = 128 x N = 64 MMAs) runs 62 us against 67; with
-    // N = 16 or 32 the MMAs are too narrow to pay for the operand staging (16 -> 16: 389
+    // network, the 32 -> 64 convolution (M = 128 x N = 64 MMAs) runs 54 us against 67; with
+    // N = 16 or 32 the MMAs are too narrow to pay for the operand staging (16 -> 16: 360
     // against 308 us), so those layers stay on mma.sync unless LS_LPNET_TC=2
     if (n->use_tc == 2) {
 #define LP_TC(CI, CO) \
