@@ -8,9 +8,9 @@
 //  * k_lp_conv_tc: 3x3x3 convolution as an implicit GEMM on the 5th-generation tensor cores
 //    (tcgen05.mma kind::f16, BF16 x BF16 -> FP32 accumulators in tensor memory): a CTA
 //    computes 16 x 8 x ZT output voxels (M = 128 per plane) x all output channels from
-//    shared-memory operands. Used where it is the faster kernel (32 -> 64 channels; every
-//    layer with up to 32 input channels under LS_LPNET_TC=2). With flipped, transposed
-//    weights it is also the input-gradient pass.
+//    shared-memory operands. Used where it is at least as fast as mma.sync (32 -> 64 and
+//    16 -> 32 channels; every layer with up to 32 input channels under LS_LPNET_TC=2). With
+//    flipped, transposed weights it is also the input-gradient pass.
 //  * k_lp_conv / k_lp_conv_tiled: the same convolution with mma.sync m16n8k16 (BF16 x BF16
 //    -> FP32 in registers): a warp computes 16 output voxels x all output channels; the K
 //    dimension runs over 27 taps x input channels in chunks of 16. k_lp_conv serves the
@@ -690,8 +690,8 @@ using ls::LpLayer;
 struct ls_lpnet {
     int D, H, W;
     int device, num_sms;
-    int use_tc;             // tcgen05 convolutions: 0 none, 1 where measured faster than mma.sync
-                            // (32 -> 64 channels), 2 every layer with CIN <= 32 (LS_LPNET_TC)
+    int use_tc;             // tcgen05 convolutions: 0 none, 1 where measured at least as fast as
+                            // mma.sync (32 -> 64, 16 -> 32), 2 every layer with CIN <= 32 (LS_LPNET_TC)
     cudaStream_t stream;
     LpLayer layer[kLpLayers];
     size_t nparam, nweight_bf;
@@ -753,11 +753,12 @@ int lp_grid(const ls_lpnet* n, long long work, int block) {
 }
 
 // conv forward / input-gradient dispatch over the channel pairs of the network
-// planes per CTA: for 16 input channels few enough that two CTAs share an SM (<= 113 KB of
-// shared memory each: one CTA stages while the other's MMAs run), for 32 as many as fit
+// planes per CTA, measured at 144x176x176: for 16 input channels two (75-89 KB of shared
+// memory, two or three CTAs per SM, so that one CTA stages while another's MMAs run: 16 -> 16
+// in 347 us against 358 with four planes and 413 with one), for 32 as many as fit
 template <int CI, int CO>
 struct TcPlanes {
-    static constexpr int value = (CI == 16) ? (CO <= 16 ? 4 : 3) : (CO <= 16 ? 4 : 1);
+    static constexpr int value = (CI == 16) ? 2 : (CO <= 16 ? 4 : 1);
 };
 
 template <int CI, int CO, bool RELU, typename OutT>
@@ -782,17 +783,19 @@ ls_status lp_conv_tc(ls_lpnet* n, LpDims d, const bf16* in, const bf16* w, const
 template <bool RELU, typename OutT>
 ls_status lp_conv(ls_lpnet* n, LpDims d, int cin, int cout, const bf16* in, const bf16* w, const float* bias,
                   OutT* out) {
-    // tcgen05 where it beats the mma.sync kernels: measured per layer of the 144x176x176
-    // network, the 32 -> 64 convolution (M = 128 x N = 64 MMAs) runs 54 us against 67; with
-    // N = 16 or 32 the MMAs are too narrow to pay for the operand staging (16 -> 16: 360
-    // against 308 us), so those layers stay on mma.sync unless LS_LPNET_TC=2
+    // tcgen05 where it is at least as fast as the mma.sync kernels, measured per layer of the
+    // 144x176x176 network: 32 -> 64 (M = 128 x N = 64 MMAs) 54 us against 67, 16 -> 32 80 us
+    // against 80; where N = 16 the MMAs are too narrow to pay for the operand staging
+    // (16 -> 16: 347 against 308 us, 32 -> 16: 128 against 107), so those layers stay on
+    // mma.sync unless LS_LPNET_TC=2
     if (n->use_tc == 2) {
 #define LP_TC(CI, CO) \
         if (cin == CI && cout == CO) return lp_conv_tc<CI, CO, RELU, OutT>(n, d, in, w, bias, out);
         LP_TC(16, 16) LP_TC(16, 32) LP_TC(32, 64) LP_TC(32, 16)
 #undef LP_TC
-    } else if (n->use_tc == 1 && cin == 32 && cout == 64) {
-        return lp_conv_tc<32, 64, RELU, OutT>(n, d, in, w, bias, out);
+    } else if (n->use_tc == 1) {
+        if (cin == 32 && cout == 64) return lp_conv_tc<32, 64, RELU, OutT>(n, d, in, w, bias, out);
+        if (cin == 16 && cout == 32) return lp_conv_tc<16, 32, RELU, OutT>(n, d, in, w, bias, out);
     }
     if (cin <= 32) {
         const dim3 tg((unsigned)((d.W + ls::kTX - 1) / ls::kTX), (unsigned)((d.H + ls::kTY - 1) / ls::kTY),

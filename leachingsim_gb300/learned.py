@@ -7,13 +7,14 @@ pressure system to a start for the solve:
     mask  - 1 on the Pore rows (the unknowns), 0 elsewhere
     logk  - (log10 K + 15) / 3
     dist  - the Euclidean distance to the nearest voxel that carries the top pressure
-            (ls_geom_distance), over 100: the pressure of the Pore space falls off with
-            it, on scales beyond the network's receptive field
+            (ls_geom_distance on the half-resolution grid), over 100: the pressure of the
+            Pore space falls off with it, on scales beyond the network's receptive field
 
 and predicts the deviation of the pressure from the top pressure, d = 100 (1 - P / p_top),
 on the Pore rows (the start is P / p_top = 1 - d / 100). The network runs at half
-resolution: its inputs are the 2x2x2 block means of the three fields (ls_field_pool2), its
-output is repeated over each block (ls_field_up2); the deviation varies on the scale of
+resolution: its inputs are the 2x2x2 block means of the mask and the log-permeability
+(ls_field_pool2) and the distance computed on the half-resolution grid, its output is
+repeated over each block (ls_field_up2); the deviation varies on the scale of
 the distance to the inlet, and the half-resolution network costs an eighth of the
 full-resolution one. The pressure of the Pore space
 that the Air inlet reaches sits within a few percent of p_top, so this scaling gives the
@@ -67,10 +68,13 @@ def pad16(shape):
     return tuple(((int(v) + 15) // 16) * 16 for v in shape)
 
 
-def coarse_inputs(m, k, dist):
-    """The network's inputs: 2x2x2 block means of the three fine fields (extents even)."""
+def coarse_inputs(m, k, bc):
+    """The network's inputs from the fine fields (extents even): 2x2x2 block means of the
+    mask and the log-permeability, and the distance input computed on the half-resolution
+    grid itself (coarse_distance_input): an eighth of the work of a fine distance transform
+    and within a voxel of the block mean of the fine distances."""
     from .runtime import field_pool2
-    return field_pool2(m), field_pool2(k), field_pool2(dist)
+    return field_pool2(m), field_pool2(k), coarse_distance_input(bc)
 
 
 def top_pressure(params, t):
@@ -125,7 +129,6 @@ def make_sample(seed, shape=PATCH, t=RAMP, params=None):
         ctx.props()
         ctx.pressure_setup(t)
         m, k, b = ctx.pressure_learned_inputs()
-        dist = distance_input(b)
         ok, info = ctx.pressure_solve_start(torch.zeros(shape, dtype=torch.float32, device="cuda"), 0.0)
         if not ok:
             raise RuntimeError(f"plain solve failed on sample {seed}: {info}")
@@ -137,8 +140,8 @@ def make_sample(seed, shape=PATCH, t=RAMP, params=None):
         target = DEV_SCALE * (1.0 - tau) * anchored
         from .runtime import field_pool2
         fs = pad16(shape)
-        m, k, dist, target, anchored = (_pad(v, fs) for v in (m, k, dist, target, anchored))
-        mc, kc, dc = coarse_inputs(m, k, dist)
+        m, k, b, target, anchored = (_pad(v, fs) for v in (m, k, b, target, anchored))
+        mc, kc, dc = coarse_inputs(m, k, b)
         tc = field_pool2(target, anchored)                   # mean over the anchored voxels
         ac = (field_pool2(anchored) > 0.0).float()           # blocks holding any
     finally:
@@ -164,12 +167,15 @@ def make_crops(seed, shape=WIDE, crop=PATCH, count=CROPS, t=RAMP, params=None):
     return out, meta
 
 
-def distance_input(bc):
-    """The third input: distance to the voxels carrying the top pressure, over DIST_SCALE
-    (0 where no voxel carries it)."""
-    from .runtime import geom_distance
-    d = geom_distance((bc > 0.5).float())
-    return (d.clamp_min(0.0) / DIST_SCALE).contiguous()
+def coarse_distance_input(bc):
+    """The third input, on the half-resolution grid: the distance (in fine voxels) from each
+    2x2x2 block to the nearest block holding a voxel that carries the top pressure, over
+    DIST_SCALE (0 where no voxel carries it); bc is the fine identity-row field, extents
+    even."""
+    from .runtime import field_pool2, geom_distance
+    sites = (field_pool2(bc) > 0.0).float()
+    d = geom_distance(sites)
+    return (d.clamp_min(0.0) * (2.0 / DIST_SCALE)).contiguous()
 
 
 def _pad(t, shape):
@@ -198,7 +204,7 @@ class LearnedStart:
         from .runtime import field_up2
         m, k, b = ctx.pressure_learned_inputs()
         fs = self.fine
-        mc, kc, dc = coarse_inputs(_pad(m, fs), _pad(k, fs), _pad(distance_input(b), fs))
+        mc, kc, dc = coarse_inputs(_pad(m, fs), _pad(k, fs), _pad(b, fs))
         d = field_up2(self.net.forward(mc, kc, dc))
         I, J, K = self.shape
         return ((1.0 - d[:I, :J, :K] / DEV_SCALE) * m).contiguous()
