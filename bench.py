@@ -343,6 +343,24 @@ def gpu_arm(args, ws, rank, local):
     roof = roofline(ctx, shape, args.steps)
     ctx.timing(False)
     mem = ctx.device_bytes()
+    # the GPU plain path: the same number of steps on the same state with the FP64 inner
+    # multigrid-PCG for the pressure (the plain FP64 solver), right after the timed steps
+    plain = None
+    if not args.no_plain and args.solver != "fp64":
+        ctx.set_params(params("fp64"))
+        t, n, _ = run_steps(ctx, t, n, 1, DT)  # untimed: the switch allocates the FP64 buffers
+        barrier()
+        ev0.record(stream)
+        t, n, _ = run_steps(ctx, t, n, args.steps, DT)
+        ev1.record(stream)
+        ev1.synchronize()
+        barrier()
+        pms = max_over_ranks(ev0.elapsed_time(ev1) / 1e3, ws)
+        plain = {"value": round(replica_rate(ws, args.steps, pms), 4), "unit": UNIT,
+                 "ms_per_step": round(pms * 1e3 / args.steps, 3), "press_solver": "fp64",
+                 "note": "the same steps with the plain FP64 multigrid-PCG pressure solver, on the state "
+                         "the timed steps left (warm pressure starts, as in the timed steps)"}
+        ctx.set_params(p)
     ctx.close()
     t_max = max_over_ranks(dev_ms / 1e3, ws)
 
@@ -405,6 +423,7 @@ def gpu_arm(args, ws, rank, local):
         "cpu_baseline": cpu,
         "e2e": e2e,
         "pressure_solve": psolve,
+        "plain_path": plain,
         "clocks": clk.summary(),
     }
     return line
@@ -665,6 +684,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-cold", action="store_true", help="skip the separate cold pressure solves")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the steps with the plain FP64 pressure solver after the timed region")
     ap.add_argument("--nvtx", action="store_true",
                     help="wrap the first (cold) step in an NVTX range 'cold' and the timed steps in "
                          "'timed' (for ncu --nvtx-include cold/ or timed/)")

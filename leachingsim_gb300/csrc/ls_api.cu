@@ -537,13 +537,15 @@ ls_status ls_pressure_solve_start(ls_ctx* c, const float* start, double scale, l
 
 ls_status ls_pressure_set_precond_weights(ls_ctx* c, const float* params, long long count) {
     if (!c || count < 0 || (count > 0 && !params)) return LS_BAD_ARG;
-    c->lpc_params.assign(params, params + count);
-    if (c->lpc) {
+    if (c->lpc && count > 0) {
+        // the network exists already: check and load before keeping the copy, so that a
+        // rejected call leaves the weights in use unchanged
         if (ls_lpnet_param_count(c->lpc) != count)
             return set_error(c, LS_BAD_ARG, "learned pressure solver: weight count does not match the network");
-        const ls_status st = ls_lpnet_set_params(c->lpc, c->lpc_params.data(), count);
+        const ls_status st = ls_lpnet_set_params(c->lpc, params, count);
         if (st != LS_OK) return set_error(c, st, "learned pressure solver: loading the weights failed");
     }
+    c->lpc_params.assign(params, params + count);
     return LS_OK;
 }
 

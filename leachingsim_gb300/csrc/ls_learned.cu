@@ -918,6 +918,15 @@ ls_status lp_backward(ls_lpnet* n) {
 
 namespace ls {
 
+// CTAs of k_lp_conv_tc whose bounded wait for their MMAs gave up since the last call (the
+// counter is cleared); synchronous
+int lpnet_tc_timeouts() {
+    int v = 0, zero = 0;
+    if (cudaMemcpyFromSymbol(&v, g_lp_tc_timeouts, sizeof(int)) != cudaSuccess) return 0;
+    if (v) cudaMemcpyToSymbol(g_lp_tc_timeouts, &zero, sizeof(int));
+    return v;
+}
+
 // Forward pass on another stream (the pressure context's: the learned coarse solver of its
 // multigrid), channel 0 of the output into out (D*H*W floats); the network's own stream is
 // restored afterwards. Asynchronous: no synchronisation, no allocation.
@@ -1080,6 +1089,10 @@ ls_status ls_lpnet_forward(ls_lpnet* n, const float* c0, const float* c1, const 
     const long long N = (long long)n->D * n->H * n->W;
     LP_LAUNCH(n, ls::k_lp_out, lp_grid(n, N, 256), 256, N, (const float*)n->y, out);
     LP_CUDA(n, cudaStreamSynchronize(n->stream));
+    if (ls::lpnet_tc_timeouts()) {
+        n->err = "tensor-core convolution: a wait for the MMAs gave up";
+        return LS_TIMEOUT;
+    }
     return LS_OK;
 }
 
@@ -1104,6 +1117,10 @@ ls_status ls_lpnet_train_step(ls_lpnet* n, const float* c0, const float* c1, con
     std::vector<double> part(nb);
     LP_CUDA(n, cudaMemcpyAsync(part.data(), n->partials, sizeof(double) * nb, cudaMemcpyDeviceToHost, n->stream));
     LP_CUDA(n, cudaStreamSynchronize(n->stream));
+    if (ls::lpnet_tc_timeouts()) {
+        n->err = "tensor-core convolution: a wait for the MMAs gave up";
+        return LS_TIMEOUT;
+    }
     double sum = 0.0;
     for (double v : part) sum += v;
     if (loss) *loss = sum / (double)mask_count;

@@ -37,6 +37,7 @@ template <typename T>
 ls_status mg_apply(ls_ctx* c, const T* r, T* z, const T* dotv2, int* nblocks_out);
 template <typename T>
 ls_status mg_precondition(ls_ctx* c, const T* r, T* z, const T* dotv2, int slot);
+int lpnet_tc_timeouts();
 template <typename T>
 ls_status inner_invd(ls_ctx* c);
 
@@ -1061,8 +1062,11 @@ ls_status pressure_solve_run(ls_ctx* c, ls_solve_info* info, const float* start,
     if (c->p.press_solver == LS_PRESS_MIXED || c->p.press_solver == LS_PRESS_LEARNED) {
         // the learned coarse solver is on for this solve until the flexible CG stagnates
         c->lpc_active = (c->p.press_solver == LS_PRESS_LEARNED) ? 1 : 0;
-        const ls_status st = pressure_solve_t<float>(c, info, start, sc);
+        ls_status st = pressure_solve_t<float>(c, info, start, sc);
         c->lpc_active = 0;
+        // the solve has read its scalars back, so the network's convolutions have finished
+        if (c->p.press_solver == LS_PRESS_LEARNED && lpnet_tc_timeouts() && st == LS_OK)
+            st = set_error(c, LS_TIMEOUT, "learned coarse solve: a tensor-core wait gave up");
         return st;
     }
     return pressure_solve_t<double>(c, info, start, sc);
