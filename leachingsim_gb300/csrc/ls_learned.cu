@@ -8,9 +8,9 @@
 //  * k_lp_conv_tc: 3x3x3 convolution as an implicit GEMM on the 5th-generation tensor cores
 //    (tcgen05.mma kind::f16, BF16 x BF16 -> FP32 accumulators in tensor memory): a CTA
 //    computes 16 x 8 x ZT output voxels (M = 128 per plane) x all output channels from
-//    shared-memory operands. Used where it is at least as fast as mma.sync (32 -> 64 and
-//    16 -> 32 channels; every layer with up to 32 input channels under LS_LPNET_TC=2). With
-//    flipped, transposed weights it is also the input-gradient pass.
+//    shared-memory operands. Used where it is faster than mma.sync (32 -> 64 channels; every
+//    layer with up to 32 input channels under LS_LPNET_TC=2). With flipped, transposed
+//    weights it is also the input-gradient pass.
 //  * k_lp_conv / k_lp_conv_tiled: the same convolution with mma.sync m16n8k16 (BF16 x BF16
 //    -> FP32 in registers): a warp computes 16 output voxels x all output channels; the K
 //    dimension runs over 27 taps x input channels in chunks of 16. k_lp_conv serves the
@@ -280,19 +280,29 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool v
                  : "memory");
 }
 
-template <int CIN, int COUT, int ZT, bool RELU, typename OutT>
+// A CTA runs tiles blockIdx.x, blockIdx.x + gridDim.x, ... (one tile when the grid covers
+// them all; persistent CTAs otherwise). It stages the weights into shared memory once for all
+// its tiles and, with NBUF = 2 halo buffers, stages tile i + 1 (cp.async) while the tensor
+// cores run tile i, the epilogue of tile i overlapping the copies still in flight. One TMEM
+// accumulator set serves all tiles (the epilogue of tile i ends before the MMAs of tile i + 1
+// are issued); the mbarrier's phase flips once per tile.
+template <int CIN, int COUT, int ZT, int NBUF, bool RELU, typename OutT>
 __global__ void __launch_bounds__(kTcThreads) k_lp_conv_tc(LpDims d, const bf16* __restrict__ in,
                                                            const bf16* __restrict__ w, const float* __restrict__ bias,
                                                            OutT* __restrict__ out) {
     using S = TcShape<CIN, COUT, ZT>;
     static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 64 && S::cols <= 256, "channel counts");
+    static_assert(NBUF == 1 || NBUF == 2, "halo buffers");
     extern __shared__ __align__(1024) uint8_t tc_smem[];
     __shared__ uint32_t tmem_slot;
     __shared__ __align__(8) uint64_t mbar;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int x0 = blockIdx.x * kTcX, y0 = blockIdx.y * kTcY, z0 = blockIdx.z * ZT;
-    uint8_t* sA = tc_smem;
-    uint8_t* sW = tc_smem + S::a_bytes;
+    constexpr int CH = CIN / 8;
+    uint8_t* sW = tc_smem;
+    const uint32_t sW_s = (uint32_t)__cvta_generic_to_shared(sW);
+    const uint32_t sA_s = sW_s + S::w_bytes;  // buffer k at sA_s + k * a_bytes
+    const int tiles_x = (d.W + kTcX - 1) / kTcX, tiles_y = (d.H + kTcY - 1) / kTcY;
+    const int ntiles = tiles_x * tiles_y * ((d.D + ZT - 1) / ZT);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
                          (uint32_t)__cvta_generic_to_shared(&tmem_slot)),
@@ -302,24 +312,26 @@ __global__ void __launch_bounds__(kTcThreads) k_lp_conv_tc(LpDims d, const bf16*
     if (tid == 0)
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"((uint32_t)__cvta_generic_to_shared(&mbar)),
                      "r"(1));
-    // input halo: three x-shifted copies, zeros outside the grid (asynchronous copies, all
-    // in flight at once)
-    constexpr int CH = CIN / 8;
-    const uint32_t sA_s = (uint32_t)__cvta_generic_to_shared(sA), sW_s = (uint32_t)__cvta_generic_to_shared(sW);
-    for (int e = tid; e < 3 * CH * S::planes * kTcRows * kTcX; e += kTcThreads) {
-        const int x = e % kTcX;
-        int r = e / kTcX;
-        const int ry = r % kTcRows;
-        r /= kTcRows;
-        const int pz = r % S::planes;
-        r /= S::planes;
-        const int q = r % CH, cp = r / CH;
-        const int gx = x0 + x + cp - 1, gy = y0 + ry - 1, gz = z0 + pz - 1;
-        const bool ok = gx >= 0 && gx < d.W && gy >= 0 && gy < d.H && gz >= 0 && gz < d.D;
-        const bf16* src = ok ? in + (((long long)gz * d.H + gy) * d.W + gx) * CIN + q * 8 : in;
-        cp_async16(sA_s + cp * S::copy_bytes + q * S::chunk_bytes + ((pz * kTcRows + ry) * kTcX + x) * 16, src, ok);
-    }
-    // weights [tap][co][ci] -> [tap][K-step][k8][n8] core matrices
+    // input halo of tile t into buffer k: three x-shifted copies, zeros outside the grid
+    auto stage = [&](int t, int k) {
+        const int tx = t % tiles_x, ty = (t / tiles_x) % tiles_y, tz = t / (tiles_x * tiles_y);
+        const int x0 = tx * kTcX, y0 = ty * kTcY, z0 = tz * ZT;
+        const uint32_t base = sA_s + k * S::a_bytes;
+        for (int e = tid; e < 3 * CH * S::planes * kTcRows * kTcX; e += kTcThreads) {
+            const int x = e % kTcX;
+            int r = e / kTcX;
+            const int ry = r % kTcRows;
+            r /= kTcRows;
+            const int pz = r % S::planes;
+            r /= S::planes;
+            const int q = r % CH, cp = r / CH;
+            const int gx = x0 + x + cp - 1, gy = y0 + ry - 1, gz = z0 + pz - 1;
+            const bool ok = gx >= 0 && gx < d.W && gy >= 0 && gy < d.H && gz >= 0 && gz < d.D;
+            const bf16* src = ok ? in + (((long long)gz * d.H + gy) * d.W + gx) * CIN + q * 8 : in;
+            cp_async16(base + cp * S::copy_bytes + q * S::chunk_bytes + ((pz * kTcRows + ry) * kTcX + x) * 16, src, ok);
+        }
+    };
+    // weights [tap][co][ci] -> [tap][K-step][k8][n8] core matrices, once per CTA
     for (int e = tid; e < 27 * COUT * CH; e += kTcThreads) {
         const int q = e % CH;
         const int co = (e / CH) % COUT, t = e / (CH * COUT);
@@ -327,6 +339,7 @@ __global__ void __launch_bounds__(kTcThreads) k_lp_conv_tc(LpDims d, const bf16*
         cp_async16(sW_s + ((((t * S::KC + kc) * 2 + k8) * (COUT / 8) + (co >> 3)) * 128) + (co & 7) * 16,
                    w + ((size_t)t * COUT + co) * CIN + q * 8, true);
     }
+    if ((int)blockIdx.x < ntiles) stage(blockIdx.x, 0);
     asm volatile("cp.async.commit_group;\n" ::: "memory");
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
@@ -335,80 +348,103 @@ __global__ void __launch_bounds__(kTcThreads) k_lp_conv_tc(LpDims d, const bf16*
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t tmem = tmem_slot;
     const uint32_t mbar_s = (uint32_t)__cvta_generic_to_shared(&mbar);
-    if (tid == 0) {
-        // The start address sits in the descriptor's low 14 bits (address >> 4, < 256 KB), so
-        // each operand's descriptor is a base descriptor plus a compile-time offset: the tap and
-        // K-step loops unroll into bare MMA issues.
-        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(COUT >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
-        const uint64_t da0 = tc_desc((uint32_t)__cvta_generic_to_shared(sA), S::chunk_bytes, 128);
-        const uint64_t db0 = tc_desc((uint32_t)__cvta_generic_to_shared(sW), (COUT / 8) * 128, 128);
-        for (int p = 0; p < ZT; ++p) {
-            const uint64_t dap = da0 + (uint64_t)((p * kTcRows * kTcX * 16) >> 4);
-            const uint32_t dtm = tmem + (uint32_t)(p * COUT);
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(COUT >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+    int it = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+        const int buf = (NBUF == 2) ? (it & 1) : 0;
+        if (tid == 0) {
+            // the start address sits in the descriptor's low 14 bits (address >> 4, < 256 KB):
+            // each operand's descriptor is a base descriptor plus a compile-time offset
+            const uint64_t da0 = tc_desc(sA_s + buf * S::a_bytes, S::chunk_bytes, 128);
+            const uint64_t db0 = tc_desc(sW_s, (COUT / 8) * 128, 128);
+            for (int p = 0; p < ZT; ++p) {
+                const uint64_t dap = da0 + (uint64_t)((p * kTcRows * kTcX * 16) >> 4);
+                const uint32_t dtm = tmem + (uint32_t)(p * COUT);
 #pragma unroll
-            for (int t = 0; t < 27; ++t) {
-                const int dz = t / 9 - 1, dy = (t / 3) % 3 - 1, dx = t % 3 - 1;
+                for (int t = 0; t < 27; ++t) {
+                    const int dz = t / 9 - 1, dy = (t / 3) % 3 - 1, dx = t % 3 - 1;
 #pragma unroll
-                for (int kc = 0; kc < S::KC; ++kc) {
-                    const uint64_t da = dap + (uint64_t)(((dx + 1) * S::copy_bytes + 2 * kc * S::chunk_bytes +
-                                                          (((1 + dz) * kTcRows + (1 + dy)) * kTcX) * 16) >> 4);
-                    const uint64_t db = db0 + (uint64_t)(((t * S::KC + kc) * 2 * (COUT / 8) * 128) >> 4);
-                    const uint32_t acc = (t | kc) ? 1u : 0u;
-                    asm volatile(
-                        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtm),
-                        "l"(da), "l"(db), "r"(idesc), "r"(acc));
+                    for (int kc = 0; kc < S::KC; ++kc) {
+                        const uint64_t da = dap + (uint64_t)(((dx + 1) * S::copy_bytes + 2 * kc * S::chunk_bytes +
+                                                              (((1 + dz) * kTcRows + (1 + dy)) * kTcX) * 16) >> 4);
+                        const uint64_t db = db0 + (uint64_t)(((t * S::KC + kc) * 2 * (COUT / 8) * 128) >> 4);
+                        const uint32_t acc = (t | kc) ? 1u : 0u;
+                        asm volatile(
+                            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtm),
+                            "l"(da), "l"(db), "r"(idesc), "r"(acc));
+                    }
                 }
             }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar_s));
         }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar_s));
-    }
-    // bounded wait for the MMAs (phase 0); warps other than the issuing one back off so that
-    // their polling does not take issue slots from it
-    uint32_t done = 0;
-    for (int it = 0; it < (1 << 22) && !done; ++it) {
-        asm volatile(
-            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
-            : "=r"(done)
-            : "r"(mbar_s), "r"(0));
-        if (!done && warp != 0) __nanosleep(64);
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    if (done) {
-        // warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows m), of the planes p = w / 4 (mod 2)
-        const int m = (warp & 3) * 32 + lane;
-        const int x = x0 + (m % kTcX), y = y0 + m / kTcX;
-        const bool okxy = x < d.W && y < d.H;
-        for (int p = warp >> 2; p < ZT; p += kTcThreads / 128) {
-            const bool ok = okxy && z0 + p < d.D;
-            const long long v = ((long long)(z0 + p) * d.H + y) * d.W + x;
+        // the next tile's halo into the other buffer while the tensor cores run this one
+        const int next = tile + gridDim.x;
+        if (NBUF == 2 && next < ntiles) stage(next, buf ^ 1);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        // bounded wait for this tile's MMAs (phase it & 1); warps other than the issuing one
+        // back off so that their polling does not take issue slots from it
+        uint32_t done = 0;
+        for (int k = 0; k < (1 << 22) && !done; ++k) {
+            asm volatile(
+                "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+                : "=r"(done)
+                : "r"(mbar_s), "r"((uint32_t)(it & 1)));
+            if (!done && warp != 0) __nanosleep(64);
+        }
+        if (__syncthreads_or(!done)) {
+            // a wait gave up: stop here (no further MMAs or copies into buffers they may read)
+            if (tid == 0) atomicAdd(&g_lp_tc_timeouts, 1);
+            break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        {
+            const int tx = tile % tiles_x, ty = (tile / tiles_x) % tiles_y, tz = tile / (tiles_x * tiles_y);
+            const int x0 = tx * kTcX, y0 = ty * kTcY, z0 = tz * ZT;
+            // warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows m), of the planes p = w / 4 (mod 2)
+            const int m = (warp & 3) * 32 + lane;
+            const int x = x0 + (m % kTcX), y = y0 + m / kTcX;
+            const bool okxy = x < d.W && y < d.H;
+            for (int p = warp >> 2; p < ZT; p += kTcThreads / 128) {
+                const bool ok = okxy && z0 + p < d.D;
+                const long long v = ((long long)(z0 + p) * d.H + y) * d.W + x;
 #pragma unroll
-            for (int c0 = 0; c0 < COUT; c0 += 16) {
-                uint32_t r[16];
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-                    : "r"(tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(p * COUT + c0)));
-                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-                if (ok) {
+                for (int c0 = 0; c0 < COUT; c0 += 16) {
+                    uint32_t r[16];
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                        : "r"(tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(p * COUT + c0)));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                    if (ok) {
 #pragma unroll
-                    for (int q = 0; q < 16; q += 2) {
-                        const int co = c0 + q;
-                        float a = __uint_as_float(r[q]) + (bias ? bias[co] : 0.f);
-                        float b = __uint_as_float(r[q + 1]) + (bias ? bias[co + 1] : 0.f);
-                        if (RELU) {
-                            a = fmaxf(a, 0.f);
-                            b = fmaxf(b, 0.f);
+                        for (int q = 0; q < 16; q += 2) {
+                            const int co = c0 + q;
+                            float a = __uint_as_float(r[q]) + (bias ? bias[co] : 0.f);
+                            float b = __uint_as_float(r[q + 1]) + (bias ? bias[co + 1] : 0.f);
+                            if (RELU) {
+                                a = fmaxf(a, 0.f);
+                                b = fmaxf(b, 0.f);
+                            }
+                            store_pair<OutT>(out + v * COUT + co, a, b);
                         }
-                        store_pair<OutT>(out + v * COUT + co, a, b);
                     }
                 }
             }
         }
-    } else if (tid == 0) {
-        atomicAdd(&g_lp_tc_timeouts, 1);
+        // with one buffer the next tile is staged only now, after this tile's MMAs
+        if (NBUF == 1 && next < ntiles) {
+            stage(next, 0);
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+        }
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     if (warp == 0)
@@ -690,8 +726,8 @@ using ls::LpLayer;
 struct ls_lpnet {
     int D, H, W;
     int device, num_sms;
-    int use_tc;             // tcgen05 convolutions: 0 none, 1 where measured at least as fast as
-                            // mma.sync (32 -> 64, 16 -> 32), 2 every layer with CIN <= 32 (LS_LPNET_TC)
+    int use_tc;             // tcgen05 convolutions: 0 none, 1 where measured faster than mma.sync
+                            // (32 -> 64), 2 every layer with CIN <= 32 (LS_LPNET_TC)
     cudaStream_t stream;
     LpLayer layer[kLpLayers];
     size_t nparam, nweight_bf;
@@ -753,28 +789,44 @@ int lp_grid(const ls_lpnet* n, long long work, int block) {
 }
 
 // conv forward / input-gradient dispatch over the channel pairs of the network
-// planes per CTA, measured at 144x176x176: for 16 input channels two (75-89 KB of shared
-// memory, two or three CTAs per SM, so that one CTA stages while another's MMAs run: 16 -> 16
-// in 347 us against 358 with four planes and 413 with one), for 32 as many as fit
+// Planes per tile, halo buffers and persistence, measured per layer at 144x176x176 (the
+// weights plus NBUF halo buffers fit one CTA's shared memory, <= 227 KB). The layers with
+// 16 input or 16 output channels run one tile per CTA, two or three CTAs per SM overlapping
+// one another's staging and MMAs (16 -> 16: 420 us so, 479 as persistent CTAs three per SM
+// with the weights kept, 542 as one persistent CTA per SM with two halo buffers). 32 -> 64,
+// whose weights take 110 KB, runs persistent CTAs that stage them once: 47 us against 54
+// with one tile per CTA.
 template <int CI, int CO>
 struct TcPlanes {
-    static constexpr int value = (CI == 16) ? 2 : (CO <= 16 ? 4 : 1);
+    static constexpr int value = (CI == 16) ? 2 : (CO == 16 ? 4 : 1);
+    static constexpr int nbuf = 1;
+    static constexpr bool persist = (CI == 32 && CO == 64);
 };
 
 template <int CI, int CO, bool RELU, typename OutT>
 ls_status lp_conv_tc(ls_lpnet* n, LpDims d, const bf16* in, const bf16* w, const float* bias, OutT* out) {
-    constexpr int ZT = TcPlanes<CI, CO>::value;
-    constexpr int smem = ls::TcShape<CI, CO, ZT>::smem;
+    constexpr int ZT = TcPlanes<CI, CO>::value, NB = TcPlanes<CI, CO>::nbuf;
+    using S = ls::TcShape<CI, CO, ZT>;
+    constexpr int smem = S::w_bytes + NB * S::a_bytes;
     static_assert(smem + 1024 <= 227 * 1024, "shared memory per CTA");
     static bool attr = false;  // the dynamic shared-memory opt-in, once per instantiation
     if (!attr) {
-        LP_CUDA(n, cudaFuncSetAttribute(ls::k_lp_conv_tc<CI, CO, ZT, RELU, OutT>,
+        LP_CUDA(n, cudaFuncSetAttribute(ls::k_lp_conv_tc<CI, CO, ZT, NB, RELU, OutT>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         attr = true;
     }
-    const dim3 grid((unsigned)((d.W + ls::kTcX - 1) / ls::kTcX), (unsigned)((d.H + ls::kTcY - 1) / ls::kTcY),
-                    (unsigned)((d.D + ZT - 1) / ZT));
-    ls::k_lp_conv_tc<CI, CO, ZT, RELU, OutT><<<grid, ls::kTcThreads, smem, n->stream>>>(d, in, w, bias, out);
+    const long long ntiles = (long long)((d.W + ls::kTcX - 1) / ls::kTcX) * ((d.H + ls::kTcY - 1) / ls::kTcY) *
+                             ((d.D + ZT - 1) / ZT);
+    // persistent CTAs: as many as fit the SMs at once; otherwise one tile per CTA
+    static int per_sm = 0;
+    if (!per_sm) {
+        LP_CUDA(n, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ls::k_lp_conv_tc<CI, CO, ZT, NB, RELU, OutT>,
+                                                                 ls::kTcThreads, smem));
+        if (per_sm < 1) per_sm = 1;
+    }
+    const long long slots = TcPlanes<CI, CO>::persist ? (long long)per_sm * n->num_sms : ntiles;
+    const int grid = (int)(ntiles < slots ? ntiles : slots);
+    ls::k_lp_conv_tc<CI, CO, ZT, NB, RELU, OutT><<<grid, ls::kTcThreads, smem, n->stream>>>(d, in, w, bias, out);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return lp_fail(n, "k_lp_conv_tc", e);
     return LS_OK;
@@ -783,19 +835,18 @@ ls_status lp_conv_tc(ls_lpnet* n, LpDims d, const bf16* in, const bf16* w, const
 template <bool RELU, typename OutT>
 ls_status lp_conv(ls_lpnet* n, LpDims d, int cin, int cout, const bf16* in, const bf16* w, const float* bias,
                   OutT* out) {
-    // tcgen05 where it is at least as fast as the mma.sync kernels, measured per layer of the
-    // 144x176x176 network: 32 -> 64 (M = 128 x N = 64 MMAs) 54 us against 67, 16 -> 32 80 us
-    // against 80; where N = 16 the MMAs are too narrow to pay for the operand staging
-    // (16 -> 16: 347 against 308 us, 32 -> 16: 128 against 107), so those layers stay on
-    // mma.sync unless LS_LPNET_TC=2
+    // tcgen05 where it beats the mma.sync kernels, measured per layer of the 144x176x176
+    // network: 32 -> 64 (M = 128 x N = 64 MMAs, persistent CTAs that stage the 110 KB of
+    // weights once) 47 us against 67. Where N is 16 or 32 the MMAs are too narrow to pay for
+    // the operand staging (16 -> 16: 420 against 308 us, 16 -> 32: 86 against 80, 32 -> 16:
+    // 126 against 107), so those layers stay on mma.sync unless LS_LPNET_TC=2.
     if (n->use_tc == 2) {
 #define LP_TC(CI, CO) \
         if (cin == CI && cout == CO) return lp_conv_tc<CI, CO, RELU, OutT>(n, d, in, w, bias, out);
         LP_TC(16, 16) LP_TC(16, 32) LP_TC(32, 64) LP_TC(32, 16)
 #undef LP_TC
-    } else if (n->use_tc == 1) {
-        if (cin == 32 && cout == 64) return lp_conv_tc<32, 64, RELU, OutT>(n, d, in, w, bias, out);
-        if (cin == 16 && cout == 32) return lp_conv_tc<16, 32, RELU, OutT>(n, d, in, w, bias, out);
+    } else if (n->use_tc == 1 && cin == 32 && cout == 64) {
+        return lp_conv_tc<32, 64, RELU, OutT>(n, d, in, w, bias, out);
     }
     if (cin <= 32) {
         const dim3 tg((unsigned)((d.W + ls::kTX - 1) / ls::kTX), (unsigned)((d.H + ls::kTY - 1) / ls::kTY),
