@@ -313,7 +313,7 @@ def gpu_arm(args, ws, rank, local):
     psolve.setdefault("learned", None)
     psolve["note"] = ("cold solves of the first step's pressure system: t = 0, zero start (learned: the "
                       "network's start; constant_start: P = p_top on the Pore rows; learned_precond: the "
-                      "network as the multigrid's level-3 solver inside the flexible CG, with the plain "
+                      "network as the multigrid's level-4 solver inside the flexible CG, with the plain "
                       "cycle taking over on stagnation), rtol 1e-8 on the "
                       "Jacobi-scaled FP64 residual; ms = assembly + [start: inputs, distance transform, "
                       "network] + multigrid setup + solve; first_step = the run's own first step (device "

@@ -208,16 +208,16 @@ ls_status ls_pressure_learned_inputs(ls_ctx* ctx, float* mask, float* logk, floa
 ls_status ls_pressure_solve_start(ls_ctx* ctx, const float* start, double scale, ls_solve_info* info);
 /* Learned preconditioner of the pressure solve (no counterpart in the reference). With
    press_solver = LS_PRESS_LEARNED the inner flexible CG (FP32, inside the FP64 refinement) is
-   preconditioned by the K-cycle whose coarse correction on multigrid level 3 (1/8 of the grid
-   along each axis) is the network of ls_lpnet_* applied to that level's residual, instead of
-   a V-cycle over the levels below. Network input channels on a grid holding the level at
+   preconditioned by the K-cycle whose coarse correction on multigrid level 4 (1/16 of the grid
+   along each axis, the level below the three K-cycle levels) is the network of ls_lpnet_*
+   applied to that level's residual, instead of a V-cycle over the levels below. Network input channels on a grid holding the level at
    its origin (extents rounded up to multiples of 8): the member mask, the anchoring fraction
    e/d (the share of a cell's diagonal coupling to fixed values) and D^-1/2 b / s, s the
    largest |D^-1/2 b| over the members; output D^1/2 x / (64 s). When the flexible CG
    stagnates (a non-finite, negative or growing (r, z), (p, q) <= 0, or two iterations in a
    row that reduce (r, z) by less than 0.64) the solve goes on with the plain K-cycle from its
    current iterate and ls_pressure_fallbacks counts it; the FP64 residual judges every
-   accepted solve either way. Grids too small to have level 3 use the plain cycle.
+   accepted solve either way. Grids too small to have level 4 use the plain cycle.
    params: count = ls_lpnet_param_count floats (host), copied. */
 ls_status ls_pressure_set_precond_weights(ls_ctx* ctx, const float* params, long long count);
 long long ls_pressure_fallbacks(const ls_ctx* ctx);

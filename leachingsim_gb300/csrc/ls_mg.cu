@@ -34,14 +34,14 @@ constexpr double kOmega = 2.0 / 3.0;
 constexpr int kCoarsestCells = 512;
 constexpr int kCoarseSweeps = 48;
 constexpr double kProlongScale = 1.8;
-constexpr int kKLevels = 2;   // levels 1..kKLevels take a K-cycle coarse correction
+constexpr int kKLevels = 3;   // levels 1..kKLevels take a K-cycle coarse correction
 constexpr int kKSlot0 = 32;   // device scalar slots of the K-cycle FCG (5 per level)
 constexpr int kUnionSpin = 1 << 20;  // bound on the union-find retry loop
 // learned coarse solver (LS_PRESS_LEARNED): the network solves level kLearnedLevel in place of
 // the V-cycle below the K-cycle levels
-constexpr int kLearnedLevel = kKLevels + 1;
+constexpr int kLearnedLevel = kKLevels + 1;  // the level below the K-cycle levels
 constexpr float kLpcOutScale = 64.f;  // network output x this x max|D^-1/2 b| = D^1/2 x
-constexpr int kLpcSlot = 48;          // device scalar: max |D^-1/2 b| over the level's members
+constexpr int kLpcSlot = 60;          // device scalar: max |D^-1/2 b| over the level's members
 
 __device__ __forceinline__ long long lidx(const Grid& g, int i, int j, int k) {
     return (long long)k + (long long)g.K * ((long long)j + (long long)g.J * i);

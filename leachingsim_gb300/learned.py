@@ -262,15 +262,15 @@ def train(samples=256, epochs=64, lr=2e-3, seed=0, shape=PATCH, log=print, wide=
 # ---------------------------------------------------------------------------
 # The learned coarse solver of the pressure multigrid (press_solver = PRESS_LEARNED): the
 # same network, at 1/8 resolution, standing in for the V-cycle below the K-cycle levels.
-# Its inputs are the member mask of multigrid level 3, the anchoring fraction e/d of each
+# Its inputs are the member mask of multigrid level 4, the anchoring fraction e/d of each
 # cell and the Jacobi-scaled residual D^-1/2 b / s (s = max |D^-1/2 b|); it predicts the
 # Jacobi-scaled correction D^1/2 x / (s LPC_OUT_SCALE) with x ~ M^-1 b. It is trained on the
-# level-3 operators of the plain solver's hierarchies for seeded geometries: for random
+# level-4 operators of the plain solver's hierarchies for seeded geometries: for random
 # errors x (white noise and Gaussian-smoothed noise of several correlation lengths, on the
 # member cells) the input is b = M x and the target x itself, so no solve is needed.
 
 PRECOND_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lpnet_precond_weights.npy")
-LPC_LEVEL = 3
+LPC_LEVEL = 4
 LPC_OUT_SCALE = 64.0   # kLpcOutScale of csrc/ls_mg.cu
 LPC_SIGMAS = (0.0, 0.7, 1.5, 3.0, 6.0)
 

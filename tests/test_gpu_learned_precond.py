@@ -11,7 +11,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-SHAPE = (96, 96, 96)  # multigrid level 3 is 12^3, the network grid 16^3
+SHAPE = (96, 96, 96)  # multigrid level 4 (the learned one) is 6^3, the network grid 8^3
 
 
 def _ctx(seed=11):
@@ -109,7 +109,7 @@ def test_learned_weights_need_a_learned_solver():
 
 
 def test_trained_network_gains_over_no_network():
-    """The trained network's Jacobi-scaled error on random errors of a level-3 operator it
+    """The trained network's Jacobi-scaled error on random errors of a level-4 operator it
     was not trained on, against no correction (error 1) and the untrained network."""
     from leachingsim_gb300 import _abi
     from leachingsim_gb300 import learned as L
