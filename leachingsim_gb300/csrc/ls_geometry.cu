@@ -273,12 +273,18 @@ __global__ void k_ft_init(Dims d, const L* __restrict__ lab, int* __restrict__ f
 // remaining sequence that no later site beats strictly: the ties go to the earlier site,
 // which is the choice scipy.ndimage.distance_transform_edt makes. The line's stack of sites
 // lives in scratch at the line's own addresses.
-template <int AX>
+//
+// TR: the pass along the fastest axis (AX = 2) on the transposed array featT[k][i J + j]
+// (ft_transpose), whose lines run with stride I J, so that neighbouring threads (lines)
+// touch neighbouring addresses; on the original layout each thread would walk its own
+// contiguous line and a warp's loads would fall in 32 different sectors.
+template <int AX, bool TR = false>
 __global__ void k_ft_pass(Dims d, int* __restrict__ feat, int* __restrict__ st_site, int* __restrict__ st_pos,
                           long long* __restrict__ st_perp) {
+    static_assert(!TR || AX == 2, "only the fastest-axis pass runs transposed");
     const long long nlines = AX == 0 ? d.JK : AX == 1 ? (long long)d.I * d.K : (long long)d.I * d.J;
     const int n = AX == 0 ? d.I : AX == 1 ? d.J : d.K;
-    const long long stride = AX == 0 ? d.JK : AX == 1 ? (long long)d.K : 1LL;
+    const long long stride = AX == 0 ? d.JK : AX == 1 ? (long long)d.K : (TR ? (long long)d.I * d.J : 1LL);
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nlines;
          t += (long long)gridDim.x * blockDim.x) {
         long long base;
@@ -291,7 +297,7 @@ __global__ void k_ft_pass(Dims d, int* __restrict__ feat, int* __restrict__ st_s
         } else {
             li = (int)(t / d.J);
             lj = (int)(t - (long long)li * d.J);
-            base = t * d.K;
+            base = TR ? t : t * d.K;
         }
         // sweep 1: the sites whose cells on the line are not empty
         int ns = 0;
@@ -334,6 +340,47 @@ __global__ void k_ft_pass(Dims d, int* __restrict__ feat, int* __restrict__ st_s
             feat[base + q * stride] = st_site[base + l * stride];
         }
     }
+}
+
+// out[c R + r] = in[r C + c]: the transpose of an R x C int matrix through 32 x 33 shared
+// tiles (coalesced reads and writes)
+__global__ void k_ft_transpose(const int* __restrict__ in, int* __restrict__ out, long long R, int C) {
+    __shared__ int tile[32][33];
+    const long long nbr = (R + 31) / 32;
+    for (long long br = blockIdx.y; br < nbr; br += gridDim.y) {
+        const long long r0 = br * 32;
+        const int c0 = blockIdx.x * 32;
+        for (int q = threadIdx.y; q < 32; q += blockDim.y) {
+            const long long r = r0 + q;
+            const int c = c0 + threadIdx.x;
+            if (r < R && c < C) tile[q][threadIdx.x] = in[r * C + c];
+        }
+        __syncthreads();
+        for (int q = threadIdx.y; q < 32; q += blockDim.y) {
+            const int c = c0 + q;
+            const long long r = r0 + threadIdx.x;
+            if (r < R && c < C) out[(long long)c * R + r] = tile[threadIdx.x][q];
+        }
+        __syncthreads();
+    }
+}
+
+int geo_grid(long long n);
+
+// the three passes of the feature transform; the fastest-axis pass on the transposed
+// features (featT: N ints of scratch)
+static void ft_passes(const Dims& d, int* feat, int* featT, int* st_site, int* st_pos, long long* st_perp) {
+    k_ft_pass<0><<<geo_grid(d.JK), 256>>>(d, feat, st_site, st_pos, st_perp);
+    k_ft_pass<1><<<geo_grid((long long)d.I * d.K), 256>>>(d, feat, st_site, st_pos, st_perp);
+    const long long R = (long long)d.I * d.J;
+    const long long nbr = (R + 31) / 32;
+    const dim3 blk(32, 8);
+    const dim3 g1((unsigned)((d.K + 31) / 32), (unsigned)(nbr < 65535 ? nbr : 65535));
+    k_ft_transpose<<<g1, blk>>>(feat, featT, R, d.K);  // [i J + j][k] -> [k][i J + j]
+    k_ft_pass<2, true><<<geo_grid(R), 256>>>(d, featT, st_site, st_pos, st_perp);
+    const long long nbr2 = ((long long)d.K + 31) / 32;
+    const dim3 g2((unsigned)((R + 31) / 32), (unsigned)(nbr2 < 65535 ? nbr2 : 65535));
+    k_ft_transpose<<<g2, blk>>>(featT, feat, d.K, (int)R);  // back
 }
 
 // sites of a float mask (> 0.5) for the distance transform
@@ -541,11 +588,12 @@ ls_status fracture_t(int I, int J, int K, void* labels_host, long long* drilled,
     Scratch s;
     L* lab;
     uint8_t *enc, *frac;
-    int *feat, *st_site, *st_pos;
+    int *feat, *featT, *st_site, *st_pos;
     long long* st_perp;
     unsigned long long* counts;
     if (!s.get(&lab, d.N) || !s.get(&enc, d.N) || !s.get(&frac, d.N) || !s.get(&feat, d.N) ||
-        !s.get(&st_site, d.N) || !s.get(&st_pos, d.N) || !s.get(&st_perp, d.N) || !s.get(&counts, 3))
+        !s.get(&featT, d.N) || !s.get(&st_site, d.N) || !s.get(&st_pos, d.N) || !s.get(&st_perp, d.N) ||
+        !s.get(&counts, 3))
         return LS_CUDA_ERROR;
     GEO_CHECK(cudaMemcpy(lab, labels_host, sizeof(L) * d.N, cudaMemcpyHostToDevice));
     GEO_CHECK(cudaMemset(counts, 0, 3 * sizeof(unsigned long long)));
@@ -559,11 +607,7 @@ ls_status fracture_t(int I, int J, int K, void* labels_host, long long* drilled,
     if (h[0] == 0) return LS_OK;       // every Sulphide voxel is exposed already
     k_ft_init<L><<<grid, 256>>>(d, lab, feat);
     GEO_LAUNCH();
-    k_ft_pass<0><<<geo_grid(d.JK), 256>>>(d, feat, st_site, st_pos, st_perp);
-    GEO_LAUNCH();
-    k_ft_pass<1><<<geo_grid((long long)d.I * d.K), 256>>>(d, feat, st_site, st_pos, st_perp);
-    GEO_LAUNCH();
-    k_ft_pass<2><<<geo_grid((long long)d.I * d.J), 256>>>(d, feat, st_site, st_pos, st_perp);
+    ft_passes(d, feat, featT, st_site, st_pos, st_perp);
     GEO_LAUNCH();
     GEO_CHECK(cudaMemset(frac, 0, d.N));
     k_drill<L><<<grid, 256>>>(d, lab, enc, feat, frac);
@@ -640,18 +684,15 @@ extern "C" ls_status ls_geom_distance(int I, int J, int K, const float* sites, f
     if (!sites || !dist || !ls::dims_ok(I, J, K)) return LS_BAD_ARG;
     ls::Dims d{I, J, K, (long long)J * K, (long long)I * J * K};
     ls::Scratch s;
-    int *feat, *st_site, *st_pos;
+    int *feat, *featT, *st_site, *st_pos;
     long long* st_perp;
-    if (!s.get(&feat, d.N) || !s.get(&st_site, d.N) || !s.get(&st_pos, d.N) || !s.get(&st_perp, d.N))
+    if (!s.get(&feat, d.N) || !s.get(&featT, d.N) || !s.get(&st_site, d.N) || !s.get(&st_pos, d.N) ||
+        !s.get(&st_perp, d.N))
         return LS_CUDA_ERROR;
     const int grid = ls::geo_grid(d.N);
     ls::k_ft_init_mask<<<grid, 256>>>(d, sites, feat);
     GEO_LAUNCH();
-    ls::k_ft_pass<0><<<ls::geo_grid(d.JK), 256>>>(d, feat, st_site, st_pos, st_perp);
-    GEO_LAUNCH();
-    ls::k_ft_pass<1><<<ls::geo_grid((long long)d.I * d.K), 256>>>(d, feat, st_site, st_pos, st_perp);
-    GEO_LAUNCH();
-    ls::k_ft_pass<2><<<ls::geo_grid((long long)d.I * d.J), 256>>>(d, feat, st_site, st_pos, st_perp);
+    ls::ft_passes(d, feat, featT, st_site, st_pos, st_perp);
     GEO_LAUNCH();
     ls::k_ft_distance<<<grid, 256>>>(d, feat, dist);
     GEO_LAUNCH();
