@@ -125,3 +125,20 @@ def test_trained_network_gains_over_no_network():
     print({"trained": trained, "untrained": untrained})
     assert trained < 0.99
     assert trained < untrained
+
+
+def test_mg_level_hook_needs_an_fp32_hierarchy():
+    from leachingsim_gb300 import _abi
+    from leachingsim_gb300 import learned as L
+    from leachingsim_gb300.runtime import LsError
+    ctx = _ctx()
+    with pytest.raises(LsError):
+        ctx.mg_level(1)            # no solve yet
+    _solve(ctx, _abi.PRESS_MIXED)
+    op = ctx.mg_level(1)
+    assert op["shape"] == (48, 48, 48)
+    members = op["comp"] >= 0
+    assert members.any() and np.all(op["e"][members] >= 0) and np.all(op["f0"] >= 0)
+    with pytest.raises(LsError):
+        ctx.mg_level(99)
+    ctx.close()
