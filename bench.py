@@ -113,7 +113,7 @@ class ClockSampler:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={CLOCK_FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.fh,
                 stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -619,7 +619,7 @@ def mixed_arm(args):
     import torch
     from leachingsim_gb300._abi import PRESS_FP64, PRESS_MIXED, default_params
     shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else MIX_SHAPE
-    steps = max(args.steps, 2)
+    steps = MIX_STEPS  # ten steps per precision (the first a cold step)
     t0 = time.time()
     lab, thr = mixed_geometry(shape)
     log(f"mixed: geometry {shape} in {time.time() - t0:.1f}s, labels {np.bincount(lab.ravel()).tolist()}")
@@ -677,7 +677,7 @@ def mixed_arm(args):
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--solver", default="mixed", choices=["mixed", "fp64", "jacobi64"])
