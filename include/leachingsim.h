@@ -214,10 +214,12 @@ ls_status ls_pressure_solve_start(ls_ctx* ctx, const float* start, double scale,
    its origin (extents rounded up to multiples of 8): the member mask, the anchoring fraction
    e/d (the share of a cell's diagonal coupling to fixed values) and D^-1/2 b / s, s the
    largest |D^-1/2 b| over the members; output D^1/2 x / (64 s). When the flexible CG
-   stagnates (a non-finite, negative or growing (r, z), (p, q) <= 0, or two iterations in a
-   row that reduce (r, z) by less than 0.64) the solve goes on with the plain K-cycle from its
-   current iterate and ls_pressure_fallbacks counts it; the FP64 residual judges every
-   accepted solve either way. Grids too small to have level 4 use the plain cycle.
+   stagnates (a non-finite, negative or growing (r, z), (p, q) <= 0, two iterations in a row
+   that reduce (r, z) by less than 0.64, or four that reduce it by less than 0.64^4) the
+   learned iterations' correction is dropped, the solve goes on with the plain K-cycle from
+   the iterate the learned one started from, and ls_pressure_fallbacks counts it; the FP64
+   residual judges every accepted solve either way. Grids too small to have level 4 use the
+   plain cycle.
    params: count = ls_lpnet_param_count floats (host), copied. */
 ls_status ls_pressure_set_precond_weights(ls_ctx* ctx, const float* params, long long count);
 long long ls_pressure_fallbacks(const ls_ctx* ctx);
