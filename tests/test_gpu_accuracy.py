@@ -39,8 +39,6 @@ pytestmark = pytest.mark.gpu
 
 SHAPE = (32, 40, 40)
 TMAX, DT = 10.0, 1.0
-FIELDS = ("pressure", "velocity", "conc", "precipitate")
-
 
 SNAP = ("pressure", "flux_x", "flux_y", "flux_z", "conc", "precipitate", "label")
 
