@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define LS_ABI_VERSION 1
+#define LS_ABI_VERSION 2
 
 enum {
     LS_AIR = 1,
@@ -71,8 +71,27 @@ typedef enum ls_field {
     LS_F_CAP_PRESSURE = 11,
     LS_F_REL_PERM = 12,
     LS_F_PRECIPITATE = 13,
-    LS_F_COUNT = 14
+    LS_F_KMULT = 14,       /* float32 multiplier of the intrinsic permeability (1 = the reference's
+                              value); no counterpart in the reference, whose permeabilities are
+                              fixed per label (src/Simulation.cpp:190-191). Held only once
+                              uploaded; downloading it before then is LS_BAD_ARG. Not part of
+                              the snapshot (it does not change during a run). */
+    LS_F_COUNT = 15
 } ls_field;
+
+/* Boundary-condition models (ls_params.bc_mode). */
+typedef enum ls_bc_mode {
+    LS_BC_REFERENCE = 0,   /* the reference's: Air voxels touching non-Air hold the ramped
+                              top_pressure (src/Simulation.cpp:662-720), every other boundary is
+                              closed and no species flows in */
+    LS_BC_FLOW_I = 1       /* flow-through along i (Z), no counterpart in the reference: the Pore
+                              voxels of plane i = 0 hold p_inlet and those of plane i = I-1 hold
+                              p_outlet (identity rows of the pressure system), the sides stay
+                              closed; in the transport systems the Pore and Air voxels of plane
+                              i = 0 hold conc_inlet / acid_inlet (identity rows, like the inlet_bc
+                              rows of the reference's disabled block, src/Simulation.cpp:997-1004).
+                              Everything else follows the reference. */
+} ls_bc_mode;
 
 /* Pressure solver variants. */
 typedef enum ls_press_solver {
@@ -126,6 +145,15 @@ typedef struct ls_params {
     int conc_max_it;
     double sat_rtol;          /* implicit saturation solve */
     int sat_max_it;
+    /* Boundary model and permeability constants (ABI 2). */
+    int bc_mode;              /* ls_bc_mode; 0 = the reference's model */
+    double p_inlet;           /* LS_BC_FLOW_I: pressure of the Pore voxels of plane i = 0 (1.0) */
+    double p_outlet;          /* LS_BC_FLOW_I: pressure of the Pore voxels of plane i = I-1 (0.0) */
+    double conc_inlet;        /* LS_BC_FLOW_I: conc held on the fluid voxels of plane i = 0 (0.0) */
+    double acid_inlet;        /* LS_BC_FLOW_I: acid held on the fluid voxels of plane i = 0 (0.0) */
+    double pore_permeability; /* 1e-12: Air and clean Pore (src/Simulation.cpp:190) */
+    double rock_permeability; /* 1e-18: Rock, and the clogged / unleached end of the log blend
+                                 (src/Simulation.cpp:191) */
 } ls_params;
 
 /* Result of one linear solve (the reference's log line, src/Simulation.cpp:834-849). */
@@ -146,6 +174,23 @@ typedef struct ls_substep_info {
     double dt_sub;
 } ls_substep_info;
 
+/* FP64 species and mineral budget of one step (ABI 2). The reference keeps only the count of
+   leached voxels (src/main.cpp:414-431); these are sums over the I*J*K voxels of the values per
+   voxel (an amount in voxel volumes for a concentration), reduced in FP64 in a fixed order. */
+typedef struct ls_budget {
+    double conc;              /* sum of conc after the step */
+    double acid;              /* sum of acid after the step */
+    double mineral;           /* sum of frac after the step (unleached mineral) */
+    double precipitate;       /* sum of precipitate_inventory after the step */
+    double acid_consumed;     /* acid taken from the neighbours of the mineral by the dissolution
+                                 sweep during the step (src/Simulation.cpp:560-580) */
+    double mineral_dissolved; /* frac the mineral voxels lost during the step; equals
+                                 acid_consumed * time_scalar up to the FP32 rounding of frac, plus
+                                 the remainders (<= 1e-4 each) cleared at the leach threshold */
+    long long sulphide_voxels;     /* label == Sulphide after the step */
+    long long precipitate_voxels;  /* label == Precipitate after the step */
+} ls_budget;
+
 /* One full time step (src/main.cpp:303-432). */
 typedef struct ls_step_info {
     ls_solve_info pressure;
@@ -157,6 +202,7 @@ typedef struct ls_step_info {
     int leached;              /* voxels fully leached this step */
     int picard_iterations;
     int success;              /* 0 = the retry manager must roll back and halve dt */
+    ls_budget budget;         /* filled when success = 1 */
 } ls_step_info;
 
 typedef struct ls_ctx ls_ctx;

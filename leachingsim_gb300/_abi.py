@@ -28,8 +28,13 @@ FIELDS = {
     "label": 0, "frac": 1, "permeability": 2, "viscosity": 3, "pressure": 4,
     "conc": 5, "acid": 6, "flux_x": 7, "flux_y": 8, "flux_z": 9,
     "saturation": 10, "cap_pressure": 11, "rel_perm": 12, "precipitate": 13,
+    "kmult": 14,
 }
-FIELD_DTYPES = {0: None, 1: "float32"}  # every other field is float64; labels per label_bytes
+# every other field is float64; labels per label_bytes
+FIELD_DTYPES = {0: None, 1: "float32", 14: "float32"}
+
+# ls_bc_mode
+BC_REFERENCE, BC_FLOW_I = 0, 1
 
 # ls_press_solver
 PRESS_MIXED, PRESS_FP64, PRESS_JACOBI64, PRESS_LEARNED = 0, 1, 2, 3
@@ -58,6 +63,9 @@ class LsParams(C.Structure):
         ("press_rtol", C.c_double), ("press_max_it", C.c_int), ("press_solver", C.c_int),
         ("conc_rtol", C.c_double), ("conc_max_it", C.c_int),
         ("sat_rtol", C.c_double), ("sat_max_it", C.c_int),
+        ("bc_mode", C.c_int), ("p_inlet", C.c_double), ("p_outlet", C.c_double),
+        ("conc_inlet", C.c_double), ("acid_inlet", C.c_double),
+        ("pore_permeability", C.c_double), ("rock_permeability", C.c_double),
     ]
 
     def as_dict(self):
@@ -82,12 +90,24 @@ class LsSubstepInfo(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class LsBudget(C.Structure):
+    _fields_ = [
+        ("conc", C.c_double), ("acid", C.c_double), ("mineral", C.c_double),
+        ("precipitate", C.c_double), ("acid_consumed", C.c_double),
+        ("mineral_dissolved", C.c_double), ("sulphide_voxels", C.c_longlong),
+        ("precipitate_voxels", C.c_longlong),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class LsStepInfo(C.Structure):
     _fields_ = [
         ("pressure", LsSolveInfo), ("saturation", LsSubstepInfo),
         ("saturation_solve", LsSolveInfo), ("conc", LsSolveInfo), ("acid", LsSolveInfo),
         ("leaching", LsSubstepInfo), ("leached", C.c_int), ("picard_iterations", C.c_int),
-        ("success", C.c_int),
+        ("success", C.c_int), ("budget", LsBudget),
     ]
 
     def as_dict(self):
@@ -132,6 +152,13 @@ def default_params(**overrides):
     p.conc_max_it = 10000
     p.sat_rtol = 1e-10
     p.sat_max_it = 10000
+    p.bc_mode = BC_REFERENCE
+    p.p_inlet = 1.0
+    p.p_outlet = 0.0
+    p.conc_inlet = 0.0
+    p.acid_inlet = 0.0
+    p.pore_permeability = 1.0e-12
+    p.rock_permeability = 1.0e-18
     for k, v in overrides.items():
         if not hasattr(p, k):
             raise AttributeError(f"ls_params has no field {k!r}")

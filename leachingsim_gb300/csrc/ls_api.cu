@@ -1,5 +1,6 @@
 // ls_api.cu - C-ABI entry points, context life cycle, transfers, snapshot, timing and
 // the time-step orchestration of src/main.cpp:303-432.
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -211,8 +212,14 @@ static void* field_ptr(ls_ctx* c, ls_field f, size_t* esz) {
     case LS_F_CAP_PRESSURE: *esz = 8; return c->pc;
     case LS_F_REL_PERM: *esz = 8; return c->kr;
     case LS_F_PRECIPITATE: *esz = 8; return c->precip;
+    case LS_F_KMULT: *esz = 4; return c->kmult;
     default: return nullptr;
     }
+}
+
+__global__ void k_fill_f32(float* a, long long n, float v) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x)
+        a[r] = v;
 }
 
 extern "C" {
@@ -249,6 +256,14 @@ void ls_params_default(ls_params* p) {
     p->conc_max_it = 10000;
     p->sat_rtol = 1e-10;
     p->sat_max_it = 10000;
+    p->bc_mode = LS_BC_REFERENCE;
+    p->p_inlet = 1.0;
+    p->p_outlet = 0.0;
+    p->conc_inlet = 0.0;
+    p->acid_inlet = 0.0;
+    // src/Simulation.cpp:190-191
+    p->pore_permeability = 1.0e-12;
+    p->rock_permeability = 1.0e-18;
 }
 
 int ls_abi_version(void) { return LS_ABI_VERSION; }
@@ -261,6 +276,13 @@ static ls_status validate_params(ls_ctx* c, const ls_params* p) {
         return set_error(c, LS_BAD_ARG, "max_it must be >= 1");
     if (p->press_solver < LS_PRESS_MIXED || p->press_solver > LS_PRESS_LEARNED)
         return set_error(c, LS_BAD_ARG, "unknown press_solver");
+    if (p->bc_mode != LS_BC_REFERENCE && p->bc_mode != LS_BC_FLOW_I)
+        return set_error(c, LS_BAD_ARG, "unknown bc_mode");
+    if (!(p->pore_permeability > 0.0) || !(p->rock_permeability > 0.0))
+        return set_error(c, LS_BAD_ARG, "pore_permeability and rock_permeability must be > 0");
+    if (!std::isfinite(p->p_inlet) || !std::isfinite(p->p_outlet) || !std::isfinite(p->conc_inlet) ||
+        !std::isfinite(p->acid_inlet))
+        return set_error(c, LS_BAD_ARG, "inlet / outlet values must be finite");
     return LS_OK;
 }
 
@@ -362,7 +384,7 @@ ls_status ls_destroy(ls_ctx* c) {
                     c->sh_label, c->sh_sat, c->sh_precip, c->sh_frac, c->shf_label, c->shf_perm,
                     c->shf_visc, c->psb2, c->sat_q, c->dbits, c->sht_label, c->sht_fx, c->sht_fy, c->sht_fz,
                     c->shq_P, c->shq_C, c->shq_K, c->shq_V, c->shq_fx, c->shq_fy, c->shq_fz,
-                    c->wlist, c->wcount};
+                    c->wlist, c->wcount, c->kmult};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     for (void* q : c->l0base)
@@ -411,6 +433,10 @@ const char* ls_last_error(const ls_ctx* c) { return c ? c->err.c_str() : "null c
 ls_status ls_set_params(ls_ctx* c, const ls_params* p) {
     if (!c || !p) return LS_BAD_ARG;
     LS_TRY(validate_params(c, p));
+    // a new boundary model changes the pressure scale: no ratio rescaling of the warm start
+    if (p->bc_mode != c->p.bc_mode || p->p_inlet != c->p.p_inlet || p->p_outlet != c->p.p_outlet)
+        c->p_eff_prev = 0.0;
+    if (p->bc_mode != c->p.bc_mode || p->acid_inlet != c->p.acid_inlet) c->acid_zero = 0;
     c->p = *p;
     c->p_ready = 0;
     c->props_force = 1;  // the property constants may have changed
@@ -436,6 +462,12 @@ size_t ls_device_bytes(const ls_ctx* c) { return c ? c->device_bytes : 0; }
 static ls_status transfer(ls_ctx* c, ls_field f, void* host, size_t n, int padded, int up,
                           cudaMemcpyKind kind) {
     if (!c || !host) return LS_BAD_ARG;
+    if (f == LS_F_KMULT && !c->kmult) {
+        // held only once set: allocate with every voxel at 1 (the reference's permeabilities)
+        if (!up) return set_error(c, LS_BAD_ARG, "no permeability multiplier has been uploaded");
+        LS_TRY(dalloc_t(c, &c->kmult, (size_t)c->g.NP));
+        LS_LAUNCH(c, k_fill_f32, grid_for(c, c->g.NP), kBlock, 0, c->kmult, c->g.NP, 1.0f);
+    }
     size_t esz = 0;
     void* dev = field_ptr(c, f, &esz);
     if (!dev) return set_error(c, LS_BAD_ARG, "unknown field id");
@@ -449,7 +481,8 @@ static ls_status transfer(ls_ctx* c, ls_field f, void* host, size_t n, int padde
         LS_CUDA(c, cudaMemcpyAsync(dev, host, n * esz, kind, c->stream));
         if (f == LS_F_LABEL || f == LS_F_PERMEABILITY || f == LS_F_VISCOSITY) c->p_ready = 0;
         // outputs of the property kernel written from outside: re-evaluate every voxel
-        if (f == LS_F_PERMEABILITY || f == LS_F_VISCOSITY || f == LS_F_CAP_PRESSURE || f == LS_F_REL_PERM)
+        if (f == LS_F_PERMEABILITY || f == LS_F_VISCOSITY || f == LS_F_CAP_PRESSURE || f == LS_F_REL_PERM ||
+            f == LS_F_KMULT)
             c->props_force = 1;
         if (f == LS_F_PRESSURE) c->p_eff_prev = 0.0;
         if (f == LS_F_ACID) c->acid_zero = 0;
@@ -629,7 +662,7 @@ ls_status ls_precip(ls_ctx* c) {
 ls_status ls_dissolve(ls_ctx* c, double dt, int* leached, ls_substep_info* info) {
     if (!c || !(dt > 0.0)) return c ? set_error(c, LS_BAD_ARG, "dt must be > 0") : LS_BAD_ARG;
     Timed tm(c, LS_T_DISSOLVE);
-    return dissolve_run(c, dt, leached, info);
+    return dissolve_run(c, dt, leached, info, nullptr, nullptr);
 }
 
 // Simulation::saveState, src/Simulation.cpp:2312-2328.
@@ -704,7 +737,14 @@ ls_status ls_step(ls_ctx* c, double t, double dt, ls_step_info* info) {
     }
     if (ok) {
         LS_TRY(ls_precip(c));
-        LS_TRY(ls_dissolve(c, dt, &loc.leached, &loc.leaching));
+        {
+            // the sweep keeps the acid it starts from in the pressure residual buffer (free
+            // between pressure solves) for the budget's consumed acid
+            Timed tm(c, LS_T_DISSOLVE);
+            bool swept = false;
+            LS_TRY(dissolve_run(c, dt, &loc.leached, &loc.leaching, c->pr, &swept));
+            LS_TRY(budget_run(c, swept ? c->pr : nullptr, &loc.budget));
+        }
     }
     loc.success = ok ? 1 : 0;
     if (info) *info = loc;

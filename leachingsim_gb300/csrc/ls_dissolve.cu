@@ -157,7 +157,9 @@ __global__ void k_dz_level(Grid g, DzConst dc, const int* __restrict__ list, int
 }
 
 template <typename L>
-static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_info* info) {
+static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_info* info, double* acid_pre,
+                            bool* swept) {
+    if (swept) *swept = false;
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
     DzConst dc;
@@ -233,6 +235,10 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
               (const int*)c->dz_level_start, c->dz_count, c->dz_list);
     int* d_leached = c->d_int + 8;
     LS_CUDA(c, cudaMemsetAsync(d_leached, 0, sizeof(int), c->stream));
+    if (acid_pre)
+        LS_CUDA(c, cudaMemcpyAsync(acid_pre, c->acid, sizeof(double) * (size_t)g.N, cudaMemcpyDeviceToDevice,
+                                   c->stream));
+    if (swept) *swept = true;
     for (int step = 0; step < num_steps; ++step) {
         for (int w = 0; w < nlev; ++w) {
             int n = hist[w];
@@ -250,9 +256,10 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
     return LS_OK;
 }
 
-ls_status dissolve_run(ls_ctx* c, double dt, int* leached, ls_substep_info* info) {
-    if (c->label_bytes == 1) return dissolve_t<uint8_t>(c, dt, leached, info);
-    return dissolve_t<uint16_t>(c, dt, leached, info);
+ls_status dissolve_run(ls_ctx* c, double dt, int* leached, ls_substep_info* info, double* acid_pre,
+                       bool* swept) {
+    if (c->label_bytes == 1) return dissolve_t<uint8_t>(c, dt, leached, info, acid_pre, swept);
+    return dissolve_t<uint16_t>(c, dt, leached, info, acid_pre, swept);
 }
 
 }  // namespace ls

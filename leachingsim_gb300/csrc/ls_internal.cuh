@@ -248,6 +248,7 @@ struct ls_ctx {
     // fields, NP slots each
     void* label;
     float* frac;
+    float* kmult;         // intrinsic-permeability multiplier, allocated on first upload (else 1)
     double *perm, *visc, *P, *conc, *acid, *fx, *fy, *fz, *sat, *pc, *kr, *precip;
     // snapshot (src/Simulation.cpp:2312-2328)
     void* b_label;
@@ -293,6 +294,7 @@ struct ls_ctx {
     double* shf_visc;
     double* psb2;         // (b/diag)^2 of each pressure row, for the norm of the residual test
     double rows_evap_dx;  // evaporation constant the stored pressure rows were built with
+    double rows_bc[3];    // bc_mode, p_inlet, p_outlet the stored pressure rows were built with
     double* sat_q;        // div q + evaporative sink of each active voxel (saturation update)
     unsigned int* dbits;  // dirty bits of the change tests: two planes of dwords words
     long long dwords;     // ceil(N / 32)
@@ -304,7 +306,7 @@ struct ls_ctx {
     int t_valid;          // the stored transport rows are fully implicit rows for t_consts
     int acid_zero;        // the acid field is identically 0: the last transport solve found
                           // b = 0 and x = 0; cleared by every write from outside
-    double t_consts[8];
+    double t_consts[10];
     double *shq_P, *shq_C, *shq_K, *shq_V;  // flux inputs at the last evaluation
     double *shq_fx, *shq_fy, *shq_fz;       // the fluxes last computed
     int flux_valid;
@@ -515,7 +517,13 @@ ls_status pressure_learned_inputs_run(ls_ctx* c, float* mask, float* logk, float
 ls_status pressure_apply_run(ls_ctx* c, const double* x, double* y);
 ls_status transport_run(ls_ctx* c, double dt, int which, ls_solve_info* ci, ls_solve_info* ai);
 ls_status transport_apply_run(ls_ctx* c, double dt, const double* x, double* y);
-ls_status dissolve_run(ls_ctx* c, double dt, int* leached, ls_substep_info* info);
+// acid_pre (optional, N doubles): receives the acid the sweeps start from; *swept tells
+// whether they ran (otherwise nothing changed)
+ls_status dissolve_run(ls_ctx* c, double dt, int* leached, ls_substep_info* info, double* acid_pre,
+                       bool* swept);
+// FP64 budget of the fields after a step (acid_pre: the acid before the dissolution sweep, or
+// null when the sweep did not run)
+ls_status budget_run(ls_ctx* c, const double* acid_pre, ls_budget* b);
 ls_status init_frac_run(ls_ctx* c, unsigned long long* count);
 ls_status init_saturation_run(ls_ctx* c);
 

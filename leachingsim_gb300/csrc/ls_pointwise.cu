@@ -18,6 +18,7 @@ namespace ls {
 
 struct PropsConst {
     double m, s_res, vg_n, vg_alpha, inv_alpha;
+    double pore_permeability, rock_permeability;  // src/Simulation.cpp:190-191 (parameters here)
     double log_k_rock, log_k_pore;
     double k_clean_pore;     // pow(10, 0*log_k_rock + 1*log_k_pore), precipitate fraction 0
     double k_clogged_pore;   // pow(10, 1*log_k_rock + 0*log_k_pore), precipitate fraction 1
@@ -25,12 +26,13 @@ struct PropsConst {
 };
 
 // updateRelativePermeability / updateCapillaryPressure / initProperties for one voxel from
-// its label t, saturation s, precipitate fraction and mineral fraction.
+// its label t, saturation s, precipitate fraction, mineral fraction and intrinsic-permeability
+// multiplier km (1 where none is set: K * 1 is K exactly).
 __device__ __forceinline__ void props_eval(const PropsConst& pc, int t, double s, double precip_v,
-                                           float ff, double& krv, double& pcv, double& permv,
+                                           float ff, float km, double& krv, double& pcv, double& permv,
                                            double& viscv) {
-    const double pore_permeability = 1.0e-12;
-    const double rock_permeability = 1.0e-18;
+    const double pore_permeability = pc.pore_permeability;
+    const double rock_permeability = pc.rock_permeability;
     krv = 0.0;
     pcv = 0.0;
     if (t == kPore || t == kSulphide) {
@@ -72,6 +74,7 @@ __device__ __forceinline__ void props_eval(const PropsConst& pc, int t, double s
             K_intrinsic = pow(10.0, (f * pc.log_k_rock) + ((1.0 - f) * pc.log_k_pore));
         }
     }
+    if (km != 1.0f) K_intrinsic = K_intrinsic * (double)km;
     viscv = (t == kAir) ? 1.8e-5 : 1.0e-3;
     permv = K_intrinsic * smax(krv, 1e-15);
 }
@@ -115,6 +118,7 @@ __global__ void __launch_bounds__(kBlock) k_props(PropsConst pc, const L* __rest
                                                   const double* __restrict__ sat,
                                                   const double* __restrict__ precip,
                                                   const float* __restrict__ frac,
+                                                  const float* __restrict__ kmult,
                                                   double* __restrict__ kr, double* __restrict__ cap,
                                                   double* __restrict__ perm, double* __restrict__ visc,
                                                   const int* __restrict__ list,
@@ -123,7 +127,7 @@ __global__ void __launch_bounds__(kBlock) k_props(PropsConst pc, const L* __rest
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
         const int r = list[q];
         double krv, pcv, pv, vv;
-        props_eval(pc, (int)label[r], sat[r], precip[r], frac[r], krv, pcv, pv, vv);
+        props_eval(pc, (int)label[r], sat[r], precip[r], frac[r], kmult ? kmult[r] : 1.0f, krv, pcv, pv, vv);
         kr[r] = krv;
         cap[r] = pcv;
         perm[r] = pv;
@@ -138,8 +142,10 @@ ls_status props_run(ls_ctx* c) {
     pc.vg_n = c->p.vg_n;
     pc.vg_alpha = c->p.vg_alpha;
     pc.inv_alpha = 1.0 / c->p.vg_alpha;
-    pc.log_k_rock = std::log10(1.0e-18);
-    pc.log_k_pore = std::log10(1.0e-12);
+    pc.pore_permeability = c->p.pore_permeability;
+    pc.rock_permeability = c->p.rock_permeability;
+    pc.log_k_rock = std::log10(pc.rock_permeability);
+    pc.log_k_pore = std::log10(pc.pore_permeability);
     pc.k_clean_pore = std::pow(10.0, (0.0 * pc.log_k_rock) + ((1.0 - 0.0) * pc.log_k_pore));
     pc.k_clogged_pore = std::pow(10.0, (1.0 * pc.log_k_rock) + ((1.0 - 1.0) * pc.log_k_pore));
     pc.vg_n_is_2 = (c->p.vg_n == 2.0) ? 1 : 0;
@@ -159,13 +165,15 @@ ls_status props_run(ls_ctx* c) {
         LS_LAUNCH(c, k_props_scan<uint8_t>, grid, kBlock, 0, c->g, (const uint8_t*)c->label, c->sat, c->precip,
                   c->frac, (uint8_t*)c->sh_label, c->sh_sat, c->sh_precip, c->sh_frac, force, c->wlist, c->wcount);
         LS_LAUNCH(c, k_props<uint8_t>, grid, kBlock, 0, pc, (const uint8_t*)c->label, c->sat, c->precip,
-                  c->frac, c->kr, c->pc, c->perm, c->visc, (const int*)c->wlist, (const unsigned int*)c->wcount);
+                  c->frac, (const float*)c->kmult, c->kr, c->pc, c->perm, c->visc, (const int*)c->wlist,
+                  (const unsigned int*)c->wcount);
     } else {
         LS_LAUNCH(c, k_props_scan<uint16_t>, grid, kBlock, 0, c->g, (const uint16_t*)c->label, c->sat, c->precip,
                   c->frac, (uint16_t*)c->sh_label, c->sh_sat, c->sh_precip, c->sh_frac, force, c->wlist,
                   c->wcount);
         LS_LAUNCH(c, k_props<uint16_t>, grid, kBlock, 0, pc, (const uint16_t*)c->label, c->sat, c->precip,
-                  c->frac, c->kr, c->pc, c->perm, c->visc, (const int*)c->wlist, (const unsigned int*)c->wcount);
+                  c->frac, (const float*)c->kmult, c->kr, c->pc, c->perm, c->visc, (const int*)c->wlist,
+                  (const unsigned int*)c->wcount);
     }
     c->p_ready = 0;
     return LS_OK;
@@ -560,6 +568,61 @@ ls_status precip_run(ls_ctx* c) {
                   p.porosity, p.solid_density, p.time_scalar, (uint16_t*)c->label, c->conc, c->sat,
                   c->precip);
     c->p_ready = 0;
+    return LS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 budget of a step: the field sums, the acid the dissolution sweep took (per voxel the
+// acid before the sweep minus after, summed) and the mineral lost since the snapshot at the
+// start of the step (frac changes only in the sweep), in a fixed reduction order.
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_budget(Grid g, const L* __restrict__ label,
+                                                   const double* __restrict__ conc,
+                                                   const double* __restrict__ acid,
+                                                   const float* __restrict__ frac,
+                                                   const float* __restrict__ frac0,
+                                                   const double* __restrict__ precip,
+                                                   const double* __restrict__ acid_pre,
+                                                   double* __restrict__ partials) {
+    double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        const double a = acid[r];
+        const float f = frac[r];
+        acc[0] += conc[r];
+        acc[1] += a;
+        acc[2] += (double)f;
+        acc[3] += precip[r];
+        if (acid_pre) acc[4] += acid_pre[r] - a;
+        acc[5] += (double)frac0[r] - (double)f;
+        const int t = (int)label[r];
+        acc[6] += (t == kSulphide) ? 1.0 : 0.0;
+        acc[7] += (t == kPrecipitate) ? 1.0 : 0.0;
+    }
+    block_sum_store<8>(acc, partials);
+}
+
+ls_status budget_run(ls_ctx* c, const double* acid_pre, ls_budget* b) {
+    const int grid = grid_for(c, c->g.N);
+    if (c->label_bytes == 1)
+        LS_LAUNCH(c, k_budget<uint8_t>, grid, kBlock, 0, c->g, (const uint8_t*)c->label, (const double*)c->conc,
+                  (const double*)c->acid, (const float*)c->frac, (const float*)c->b_frac,
+                  (const double*)c->precip, acid_pre, c->partials);
+    else
+        LS_LAUNCH(c, k_budget<uint16_t>, grid, kBlock, 0, c->g, (const uint16_t*)c->label,
+                  (const double*)c->conc, (const double*)c->acid, (const float*)c->frac,
+                  (const float*)c->b_frac, (const double*)c->precip, acid_pre, c->partials);
+    LS_TRY(finalize_sum(c, grid, 8, S_RED0));
+    double v[8];
+    LS_TRY(read_scalars(c, S_RED0, 8, v));
+    b->conc = v[0];
+    b->acid = v[1];
+    b->mineral = v[2];
+    b->precipitate = v[3];
+    b->acid_consumed = v[4];
+    b->mineral_dissolved = v[5];
+    b->sulphide_voxels = (long long)v[6];
+    b->precipitate_voxels = (long long)v[7];
     return LS_OK;
 }
 

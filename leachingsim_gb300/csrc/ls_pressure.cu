@@ -59,6 +59,8 @@ enum {
 
 struct PressConst {
     double eff_top, evap_dx;
+    int bc_mode;             // ls_bc_mode
+    double p_inlet, p_outlet;
 };
 
 template <typename L>
@@ -165,7 +167,8 @@ __global__ void __launch_bounds__(kBlock) k_press_faces(Grid g, const L* __restr
 
 // One row of src/Simulation.cpp:674-792: kind, diagonal and right-hand side. The diagonal
 // subtracts the six link coefficients in the reference's order (+i, -i, +j, -j, +k, -k),
-// read from the stored faces.
+// read from the stored faces. With the flow-through model (LS_BC_FLOW_I, no counterpart in
+// the reference) the Pore voxels of planes i = 0 and i = I-1 are identity rows.
 template <typename L>
 __device__ __forceinline__ void press_row_eval(const Grid& g, const PressConst& pcst, const L* __restrict__ label,
                                                const double* __restrict__ f0, const double* __restrict__ f1,
@@ -187,6 +190,11 @@ __device__ __forceinline__ void press_row_eval(const Grid& g, const PressConst& 
                               (k > 0 && (int)label[r - 1] != kAir);
             bv = 0.0 + (is_surface ? pcst.eff_top : 0.0);
         }
+    } else if (t == kPore && pcst.bc_mode == LS_BC_FLOW_I && (i == 0 || i == g.I - 1)) {
+        // flow-through model: the Pore voxels of the end planes hold the inlet / outlet pressure
+        kd = 1;
+        dg = 1.0;
+        bv = 0.0 + (i == 0 ? pcst.p_inlet : pcst.p_outlet);
     } else if (t == kPore) {
         double diagonal_term = 0.0, source_term = 0.0;
         const long long nbs[6] = {r + g.JK, r - g.JK, r + g.K, r - g.K, r + 1, r - 1};
@@ -826,7 +834,13 @@ ls_status pressure_setup_run(ls_ctx* c, double t) {
     if (t < ramp_duration)
         effective_top_pressure = c->p.top_pressure * (t / ramp_duration) + 1e-6;
     pcst.eff_top = effective_top_pressure;
-    c->p_eff = effective_top_pressure;
+    pcst.bc_mode = c->p.bc_mode;
+    pcst.p_inlet = c->p.p_inlet;
+    pcst.p_outlet = c->p.p_outlet;
+    // the pressure scale of the system: the ramped Air pressure, or in the flow-through model
+    // the larger end pressure (fixed over time, so warm starts are not rescaled)
+    c->p_eff = (c->p.bc_mode == LS_BC_FLOW_I) ? std::max(std::fabs(c->p.p_inlet), std::fabs(c->p.p_outlet))
+                                              : effective_top_pressure;
     pcst.evap_dx = c->p.evaporative_flux * c->p.dx;
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
@@ -840,7 +854,9 @@ ls_status pressure_setup_run(ls_ctx* c, double t) {
     }
     const int faces_force = c->faces_force;
     c->faces_force = 0;
-    const int rows_force = (faces_force || c->rows_evap_dx != pcst.evap_dx) ? 1 : 0;
+    const double rows_bc[3] = {(double)pcst.bc_mode, pcst.p_inlet, pcst.p_outlet};
+    const int rows_force = (faces_force || c->rows_evap_dx != pcst.evap_dx ||
+                            memcmp(rows_bc, c->rows_bc, sizeof(rows_bc)) != 0) ? 1 : 0;
     LS_TRY(wlist_reset(c));
     if (c->label_bytes == 1)
         LS_LAUNCH(c, k_faces_dirty<uint8_t>, grid, kBlock, 0, g, (const uint8_t*)c->label, c->perm, c->visc,
@@ -873,6 +889,7 @@ ls_status pressure_setup_run(ls_ctx* c, double t) {
                   c->pdiag, c->pb, c->psb2, c->pisd, (const double*)c->pface[0], (const double*)c->pface[1],
                   (const double*)c->pface[2], (const int*)c->wlist, (const unsigned int*)c->wcount);
     c->rows_evap_dx = pcst.evap_dx;
+    memcpy(c->rows_bc, rows_bc, sizeof(rows_bc));
     LS_LAUNCH(c, k_press_den, grid, kBlock, 0, g, (const double*)c->psb2, c->partials);
     LS_TRY(finalize_sum(c, grid, 1, SP_DEN));
     c->p_t = t;

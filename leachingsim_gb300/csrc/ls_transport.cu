@@ -33,10 +33,20 @@ struct TransConst {
     double inv_dt, theta, alpha, D, Dpore, dx2, dx;
     double dc_pore, dc_other;  // -D_eff / dx^2 for a Pore neighbour / any other neighbour
     DxDiv dd;
+    int inlet;                 // flow-through model: plane i = 0 holds the inflow values
+    double in_val[2];          // inflow value of right-hand side 0 / 1
 };
 
+// Inflow row of the flow-through model (LS_BC_FLOW_I, no counterpart in the reference): the
+// Pore and Air voxels of plane i = 0 hold the inflow value, like the inlet_bc rows of the
+// reference's disabled block (src/Simulation.cpp:997-1004).
+__device__ __forceinline__ bool inflow_row(const TransConst& tc, int t, int i) {
+    return tc.inlet && i == 0 && (t == kPore || t == kAir);
+}
+
 // Coefficients of one transport row: diag, off[6] (+i,-i,+j,-j,+k,-k) and the explicit
-// right-hand-side part for field f (f may be null). kind: 1 identity, 2 coupled.
+// right-hand-side part for field f (f may be null). kind: 1 identity holding its old value,
+// 2 coupled, 3 identity holding the inflow value.
 // EXPL = false is the fully implicit case theta = 1: the theta factors are 1 and the
 // explicit part (1 - theta) * (...) adds zero to the right-hand side (for finite fields), so
 // both are left out, which takes most of the FP64 work out of the row.
@@ -51,6 +61,12 @@ __device__ __forceinline__ int trans_row(const Grid& g, const TransConst& tc,
     const int t = (int)label[r];
 #pragma unroll
     for (int d = 0; d < 6; ++d) off[d] = 0.0;
+    if (inflow_row(tc, t, i)) {
+        diag = 1.0;
+        if (f0) rhs[0] = 0.0 + tc.in_val[0];
+        if (f1) rhs[1] = 0.0 + tc.in_val[1];
+        return 3;
+    }
     if (t == kPrecipitate) {
         diag = 1.0;
         if (f0) rhs[0] = 0.0 + f0[r];
@@ -315,9 +331,10 @@ __global__ void __launch_bounds__(kBlock) k_t_rows(Rows<L> op, TBuf tb, const in
 
 // Also counts, per right-hand side, the rows where b or the solution after k_t_xid (b on
 // identity rows) is nonzero: a system with none has the exact solution x = 0 already.
-__global__ void __launch_bounds__(kBlock) k_t_rhs(Grid g, double inv_dt, TBuf tb, int nrhs, const double* f0,
-                                                  const double* f1, const double* __restrict__ x0,
-                                                  const double* __restrict__ x1, double* __restrict__ partials) {
+__global__ void __launch_bounds__(kBlock) k_t_rhs(Grid g, double inv_dt, double in0, double in1, TBuf tb,
+                                                  int nrhs, const double* f0, const double* f1,
+                                                  const double* __restrict__ x0, const double* __restrict__ x1,
+                                                  double* __restrict__ partials) {
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     unsigned int nz[2] = {0u, 0u};
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < (int)g.N; r += gridDim.x * blockDim.x) {
@@ -326,12 +343,12 @@ __global__ void __launch_bounds__(kBlock) k_t_rhs(Grid g, double inv_dt, TBuf tb
         for (int q = 0; q < nrhs; ++q) {
             const double fv = (q ? f1 : f0)[r];
             // trans_row's right-hand side at theta = 1: 0.0 + c_old on Precipitate rows,
-            // 0.0 + c_old * (1/dt) on every other row
-            const double rhs = (kind == 1) ? 0.0 + fv : 0.0 + fv * inv_dt;
+            // the inflow value on inflow rows, 0.0 + c_old * (1/dt) on every other row
+            const double rhs = (kind == 1) ? 0.0 + fv : (kind == 3) ? 0.0 + (q ? in1 : in0) : 0.0 + fv * inv_dt;
             tb.b[q][r] = rhs;
             double bt = rhs * inv;
             acc[q] += bt * bt;
-            const double xv = (kind == 1) ? rhs : (q ? x1 : x0)[r];
+            const double xv = (kind == 1 || kind == 3) ? rhs : (q ? x1 : x0)[r];
             const long long m = 0x7fffffffffffffffll;
             if ((__double_as_longlong(rhs) & m) != 0 || (__double_as_longlong(xv) & m) != 0) nz[q]++;
         }
@@ -347,7 +364,7 @@ __global__ void k_set_ones(double* v) { v[threadIdx.x] = 1.0; }
 __global__ void k_t_xid(Grid g, TBuf tb, double* x0, double* x1, int nrhs) {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
-        if (tb.kind[r] != 1) continue;
+        if (tb.kind[r] != 1 && tb.kind[r] != 3) continue;
         x0[r] = tb.b[0][r];
         if (nrhs > 1) x1[r] = tb.b[1][r];
     }
@@ -1038,8 +1055,9 @@ static ls_status mixed_solve(ls_ctx* c, const Rows<L>& rows, int nrhs, const dou
     if (rows.mode == 0 && rows.tc.theta == 1.0) {
         // fully implicit transport rows: recompute only the rows whose inputs changed
         const TransConst& tc = rows.tc;
-        const double consts[8] = {tc.inv_dt, tc.alpha, tc.D, tc.Dpore, tc.dx, tc.dc_pore, tc.dc_other,
-                                  (double)tc.dd.pow2};
+        // the inflow values enter the right-hand sides only (k_t_rhs), not the rows
+        const double consts[9] = {tc.inv_dt, tc.alpha, tc.D, tc.Dpore, tc.dx, tc.dc_pore, tc.dc_other,
+                                  (double)tc.dd.pow2, (double)tc.inlet};
         if (!c->sht_fx) {
             const size_t n = (size_t)g.N;
             LS_TRY(dalloc(c, &c->sht_label, n * c->label_bytes));
@@ -1054,8 +1072,8 @@ static ls_status mixed_solve(ls_ctx* c, const Rows<L>& rows, int nrhs, const dou
                   (L*)c->sht_label, c->sht_fx, c->sht_fy, c->sht_fz, c->dbits, force);
         LS_LAUNCH(c, k_t_scan, grid, kBlock, 0, g, (const unsigned int*)c->dbits, c->dwords, c->wlist, c->wcount);
         LS_LAUNCH(c, k_t_rows<L>, grid, kBlock, 0, rows, tb, (const int*)c->wlist, (const unsigned int*)c->wcount);
-        LS_LAUNCH(c, k_t_rhs, grid, kBlock, 0, g, rows.tc.inv_dt, tb, nrhs, f0, f1, (const double*)x0,
-                  (const double*)x1, c->partials);
+        LS_LAUNCH(c, k_t_rhs, grid, kBlock, 0, g, rows.tc.inv_dt, rows.tc.in_val[0], rows.tc.in_val[1], tb, nrhs,
+                  f0, f1, (const double*)x0, (const double*)x1, c->partials);
         LS_TRY(finalize_sum(c, grid, 4, S_RED0 + 4));
         memcpy(c->t_consts, consts, sizeof(consts));
         c->t_valid = 1;
@@ -1162,6 +1180,8 @@ static TransConst trans_const(const ls_ctx* c, double dt) {
     tc.dc_pore = -tc.Dpore / tc.dx2;
     tc.dc_other = -tc.D / tc.dx2;
     tc.dd = make_dxdiv(c->p.dx);
+    tc.inlet = (c->p.bc_mode == LS_BC_FLOW_I) ? 1 : 0;
+    tc.in_val[0] = tc.in_val[1] = 0.0;
     return tc;
 }
 
@@ -1186,8 +1206,10 @@ static ls_status transport_t(ls_ctx* c, double dt, int which, ls_solve_info* ci,
     ls_solve_info* inf[2] = {nullptr, nullptr};
     // An acid field that is identically 0 (the last solve found b = 0 and x = 0 on every row,
     // and nothing has written the field since) gives b = 0 and x = 0 again: the solve would
-    // leave it as it is, so it is skipped with the info such a solve reports.
-    if ((which & 2) && c->acid_zero) {
+    // leave it as it is, so it is skipped with the info such a solve reports. (A nonzero
+    // inflow of acid gives b != 0 on the inflow rows, so no skip then.)
+    const bool acid_inflow = rows.tc.inlet && c->p.acid_inlet != 0.0;
+    if ((which & 2) && c->acid_zero && !acid_inflow) {
         which &= ~2;
         if (ai) {
             memset(ai, 0, sizeof(*ai));
@@ -1196,8 +1218,8 @@ static ls_status transport_t(ls_ctx* c, double dt, int which, ls_solve_info* ci,
         }
     }
     int n = 0, acid_lane = -1;
-    if (which & 1) { f[n] = fields[0]; inf[n] = ci; n++; }
-    if (which & 2) { f[n] = fields[1]; inf[n] = ai; acid_lane = n; n++; }
+    if (which & 1) { f[n] = fields[0]; inf[n] = ci; rows.tc.in_val[n] = c->p.conc_inlet; n++; }
+    if (which & 2) { f[n] = fields[1]; inf[n] = ai; rows.tc.in_val[n] = c->p.acid_inlet; acid_lane = n; n++; }
     ls_status st = LS_OK;
     if (n > 0) {
         int zero_lanes = 0;

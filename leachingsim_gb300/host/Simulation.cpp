@@ -114,6 +114,18 @@ void Simulation::readRAW(const std::string& fname, size_t header) {
     props_valid_ = false;
 }
 
+void Simulation::readPermeabilityMultiplier(const std::string& fname) {
+    std::ifstream fin(fname, std::ios::binary);
+    if (!fin.is_open()) throw std::runtime_error("Cannot open file: " + fname);
+    size_t n = global_.size();
+    std::vector<float> buf(n);
+    fin.read(reinterpret_cast<char*>(buf.data()), (std::streamsize)(n * sizeof(float)));
+    if ((size_t)fin.gcount() != n * sizeof(float))
+        throw std::runtime_error("multiplier file " + fname + " is shorter than the domain");
+    check(ls_upload_field(ctx_, LS_F_KMULT, buf.data(), n, 0), "permeability multiplier upload");
+    props_valid_ = false;
+}
+
 void Simulation::initFields() { check(ls_init_fields(ctx_), "initFields"); props_valid_ = false; }
 
 void Simulation::initFrac() {

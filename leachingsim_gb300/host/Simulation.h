@@ -46,6 +46,9 @@ public:
     void setupDomain(int3 global_extent);
     void setupPETSc(bool zero_conc);
     void readRAW(const std::string& fname, size_t header);
+    // Per-voxel multiplier of the intrinsic permeability from a float32 RAW file (k fastest,
+    // no header); an extension with no counterpart in the reference.
+    void readPermeabilityMultiplier(const std::string& fname);
     void writeVTKFile(const std::string& fname_root, size_t tstep, size_t data_flags);
 
     // initialisation and time stepping

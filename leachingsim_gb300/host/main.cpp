@@ -117,6 +117,16 @@ int main(int argc, char* argv[]) {
         op.add("compat_shift", "true", "Solve results land one i-plane up, as on the original's rank 0");
         op.add("press_solver", "mixed", "Pressure solver: mixed, fp64, jacobi64 or learned");
         op.add("precond_weights", "", "Weights (.npy) of the learned coarse solver (default: the shipped ones)");
+        op.add("bc_mode", "reference",
+               "Boundary model: reference (Air surface at the ramped top pressure) or flow (Pore voxels of "
+               "z = 0 / z = max held at p_inlet / p_outlet, species inflow at z = 0)");
+        op.add("p_inlet", "1", "flow model: pressure of the Pore voxels of the z = 0 plane (Pa)");
+        op.add("p_outlet", "0", "flow model: pressure of the Pore voxels of the z = max plane (Pa)");
+        op.add("conc_inlet", "0", "flow model: dissolved-mineral concentration flowing in at z = 0");
+        op.add("acid_inlet", "0", "flow model: acid concentration flowing in at z = 0");
+        op.add("pore_perm", "1e-12", "Intrinsic permeability of Air and clean Pore voxels (m^2)");
+        op.add("rock_perm", "1e-18", "Intrinsic permeability of Rock voxels (m^2)");
+        op.add("kmult_file", "", "float32 RAW file (k fastest) multiplying each voxel's intrinsic permeability");
         op.add("dry-run", "false", "Parse the options, print the configuration and exit");
 
         for (int a = 1; a < argc; ++a) {
@@ -180,6 +190,18 @@ int main(int argc, char* argv[]) {
         sim.vg_alpha = 1.0;
         sim.s_res = 0.05;
         sim.solver.compat_shift = op.flag("compat_shift") ? 1 : 0;
+        {
+            string bm = op.str("bc_mode");
+            if (bm == "reference") sim.solver.bc_mode = LS_BC_REFERENCE;
+            else if (bm == "flow") sim.solver.bc_mode = LS_BC_FLOW_I;
+            else throw runtime_error("--bc_mode must be reference or flow");
+            sim.solver.p_inlet = op.num("p_inlet");
+            sim.solver.p_outlet = op.num("p_outlet");
+            sim.solver.conc_inlet = op.num("conc_inlet");
+            sim.solver.acid_inlet = op.num("acid_inlet");
+            sim.solver.pore_permeability = op.num("pore_perm");
+            sim.solver.rock_permeability = op.num("rock_perm");
+        }
         {
             string ps = op.str("press_solver");
             if (ps == "mixed") sim.solver.press_solver = LS_PRESS_MIXED;
@@ -253,6 +275,7 @@ int main(int argc, char* argv[]) {
         sim.setupDomain(global_extent);
         sim.setupPETSc(true);
         sim.readRAW(op.str("raw-file"), (size_t)op.integer("header_size"));
+        if (!op.str("kmult_file").empty()) sim.readPermeabilityMultiplier(op.str("kmult_file"));
 
         double t = 0.0;
         size_t n = 0;
@@ -376,6 +399,11 @@ int main(int argc, char* argv[]) {
                     if (sim.initial_sulphide_count > 0)
                         percentage = (double)sim.total_leached_count / sim.initial_sulphide_count * 100.0;
                     cout << "Done iteration. [" << info.leached << " voxels fully leached this step.]" << endl;
+                    const ls_budget& B = info.budget;
+                    cout << "    [Budget] conc: " << std::setprecision(15) << B.conc << " | acid: " << B.acid
+                         << " | mineral: " << B.mineral << " | precipitate: " << B.precipitate
+                         << " | acid consumed: " << B.acid_consumed << " | mineral dissolved: " << B.mineral_dissolved
+                         << " | sulphide voxels: " << B.sulphide_voxels << std::setprecision(6) << endl;
                     cout << "    [Leaching Progress] Total Leached: " << sim.total_leached_count << " / "
                          << sim.initial_sulphide_count << " (" << std::fixed << std::setprecision(4)
                          << percentage << "%)" << std::endl;

@@ -367,7 +367,7 @@ class Context:
     def _dtype(self, fid):
         if fid == 0:
             return np.uint8 if self.label_bytes == 1 else np.uint16
-        if fid == 1:
+        if fid in (1, 14):
             return np.float32
         return np.float64
 

@@ -49,6 +49,7 @@ struct lso_state {
     lso_solver_cfg cfg;
     uint16_t* label;
     float* frac;
+    float* kmult;       /* intrinsic-permeability multiplier (NULL: 1 everywhere) */
     double *perm, *visc, *P, *conc, *acid, *fx, *fy, *fz, *sat, *pc, *kr, *precip;
     uint16_t* b_label;
     float* b_frac;
@@ -138,7 +139,7 @@ lso_state* lso_create(int I, int J, int K, int label_bytes, const ls_params* p) 
 
 void lso_destroy(lso_state* s) {
     if (!s) return;
-    free(s->label); free(s->frac);
+    free(s->label); free(s->frac); free(s->kmult);
     double* f[] = {s->perm, s->visc, s->P, s->conc, s->acid, s->fx, s->fy, s->fz,
                    s->sat, s->pc, s->kr, s->precip, s->b_precip, s->b_sat, s->b_P,
                    s->b_conc, s->b_acid, s->b_fx, s->b_fy, s->b_fz};
@@ -179,6 +180,13 @@ void lso_params_default(ls_params* p) {
     p->conc_max_it = 10000;
     p->sat_rtol = 1e-6;
     p->sat_max_it = 10000;
+    p->bc_mode = LS_BC_REFERENCE;
+    p->p_inlet = 1.0;
+    p->p_outlet = 0.0;
+    p->conc_inlet = 0.0;
+    p->acid_inlet = 0.0;
+    p->pore_permeability = 1.0e-12;
+    p->rock_permeability = 1.0e-18;
 }
 void lso_set_solver(lso_state* s, const lso_solver_cfg* cfg) { s->cfg = *cfg; }
 unsigned long long lso_initial_sulphide_count(const lso_state* s) { return s->initial_sulphide_count; }
@@ -215,6 +223,13 @@ static void* field_ptr(lso_state* s, int f, size_t* esz) {
     case LS_F_CAP_PRESSURE: *esz = 8; return s->pc;
     case LS_F_REL_PERM: *esz = 8; return s->kr;
     case LS_F_PRECIPITATE: *esz = 8; return s->precip;
+    case LS_F_KMULT:
+        *esz = 4;
+        if (!s->kmult) {
+            s->kmult = (float*)xcalloc(s->NP, sizeof(float));
+            for (size_t r = 0; r < s->NP; ++r) s->kmult[r] = 1.0f;
+        }
+        return s->kmult;
     default: return NULL;
     }
 }
@@ -323,10 +338,14 @@ void lso_update_cap(lso_state* s) {
     }
 }
 
-/* Simulation::initProperties, S.cpp:187-248. */
+/* Simulation::initProperties, S.cpp:187-248. The two permeability constants of
+ * S.cpp:190-191 come from the parameters (the reference's values by default), and the
+ * intrinsic permeability is multiplied by the per-voxel factor when one was set (an
+ * extension: the reference has neither). */
 void lso_init_properties(lso_state* s) {
-    const double pore_permeability = 1.0e-12;
-    const double rock_permeability = 1.0e-18;
+    const double pore_permeability = s->p.pore_permeability;
+    const double rock_permeability = s->p.rock_permeability;
+    const float* kmult = s->kmult;
     const long N = (long)s->N;
 #pragma omp parallel for schedule(static)
     for (long r = 0; r < N; ++r) {
@@ -346,6 +365,7 @@ void lso_init_properties(lso_state* s) {
             double log_k_eff = (f * log_k_rock) + ((1.0 - f) * log_k_pore);
             K_intrinsic = pow(10.0, log_k_eff);
         }
+        if (kmult) K_intrinsic = K_intrinsic * (double)kmult[r];
         s->visc[r] = (type == AIR) ? 1.8e-5 : 1.0e-3;
         double K_rel = smax(s->kr[r], 1e-15);
         s->perm[r] = K_intrinsic * K_rel;
@@ -384,6 +404,8 @@ static double dot(const double* a, const double* b, long n) {
     for (long r = 0; r < n; ++r) acc += a[r] * b[r];
     return acc;
 }
+
+static double scaled_residual(lso_state* s, const ell_sys* e, const double* b, const double* x);
 
 /* Left-preconditioned restarted GMRES with classical Gram-Schmidt (PETSc's defaults for
    KSPGMRES) and the default convergence test: ||B r_k|| <= max(rtol*||B b||, abstol),
@@ -505,6 +527,411 @@ static int gmres(lso_state* s, const ell_sys* e, const double* b, double* x, int
     return reason;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Multigrid-preconditioned CG on the Pore block of the pressure system (test and baseline
+   infrastructure: the stand-in for the algebraic-multigrid preconditioner the reference's
+   production job scripts select for this system, -press_pc_type hypre -press_pc_hypre_type
+   boomeramg, hpc_cx3_test.pbs:44-51; hypre is not part of the reference and is not
+   restated). The unknowns S are the normal Pore rows (diagonal -sum of links < 0). With
+   them the operator is M = -A_SS in "excess + Laplacian" form, (M x)_r = e_r x_r +
+   sum over S neighbours of c (x_r - x_nb), c the row's link coefficient (the same seen from
+   both ends) and e_r the links of r to rows outside S. Levels coarsen 2x2x2 by aggregation
+   with Galerkin operators of the same form (sums of the children's excess and of the links
+   crossing a coarse face); a symmetric V-cycle (two damped Jacobi sweeps before and after,
+   a fixed number of sweeps on the coarsest level) preconditions CG. */
+
+typedef struct mg_level {
+    int I, J, K;
+    long n;
+    int8_t* mem;     /* member cell */
+    int8_t* owned;   /* member restricted into its coarse cell (of the block's majority component) */
+    int* comp;       /* strong component of a member (-1 otherwise) */
+    double* e;       /* excess */
+    double* c[3];    /* +i, +j, +k links */
+    double* invd;    /* 1 / (e + sum of links) */
+    double *x, *b, *t;
+} mg_level;
+
+typedef struct mg_hier {
+    int nlev;
+    mg_level L[24];
+} mg_hier;
+
+static void mg_level_alloc(mg_level* l, int I, int J, int K) {
+    l->I = I; l->J = J; l->K = K;
+    l->n = (long)I * J * K;
+    l->mem = (int8_t*)xcalloc(l->n, 1);
+    l->owned = (int8_t*)xcalloc(l->n, 1);
+    l->comp = (int*)xcalloc(l->n, sizeof(int));
+    l->e = (double*)xcalloc(l->n, sizeof(double));
+    for (int d = 0; d < 3; ++d) l->c[d] = (double*)xcalloc(l->n, sizeof(double));
+    l->invd = (double*)xcalloc(l->n, sizeof(double));
+    l->x = (double*)xcalloc(l->n, sizeof(double));
+    l->b = (double*)xcalloc(l->n, sizeof(double));
+    l->t = (double*)xcalloc(l->n, sizeof(double));
+}
+
+static void mg_free(mg_hier* h) {
+    for (int q = 0; q < h->nlev; ++q) {
+        mg_level* l = &h->L[q];
+        free(l->mem); free(l->owned); free(l->comp); free(l->e); free(l->invd); free(l->x); free(l->b); free(l->t);
+        for (int d = 0; d < 3; ++d) free(l->c[d]);
+    }
+    h->nlev = 0;
+}
+
+static void mg_invd(mg_level* l) {
+    const int I = l->I, J = l->J, K = l->K;
+    const long JK = (long)J * K;
+#pragma omp parallel for schedule(static)
+    for (long r = 0; r < l->n; ++r) {
+        if (!l->mem[r]) { l->invd[r] = 0.0; continue; }
+        int i = (int)(r / JK), j = (int)((r / K) % J), k = (int)(r % K);
+        double d = l->e[r] + l->c[0][r] + l->c[1][r] + l->c[2][r];
+        if (i > 0) d += l->c[0][r - JK];
+        if (j > 0) d += l->c[1][r - K];
+        if (k > 0) d += l->c[2][r - 1];
+        (void)I;
+        l->invd[r] = d > 0.0 ? 1.0 / d : 0.0;
+    }
+}
+
+/* y = M x on a level (members only; x is 0 off the members) */
+static void mg_apply(const mg_level* l, const double* x, double* y) {
+    const int J = l->J, K = l->K;
+    const long JK = (long)J * K;
+#pragma omp parallel for schedule(static)
+    for (long r = 0; r < l->n; ++r) {
+        if (!l->mem[r]) { y[r] = 0.0; continue; }
+        int i = (int)(r / JK), j = (int)((r / K) % J), k = (int)(r % K);
+        const double xr = x[r];
+        double a = l->e[r] * xr;
+        a += l->c[0][r] * (xr - x[r + (i + 1 < l->I ? JK : 0)]);
+        a += l->c[1][r] * (xr - x[r + (j + 1 < J ? K : 0)]);
+        a += l->c[2][r] * (xr - x[r + (k + 1 < K ? 1 : 0)]);
+        if (i > 0) a += l->c[0][r - JK] * (xr - x[r - JK]);
+        if (j > 0) a += l->c[1][r - K] * (xr - x[r - K]);
+        if (k > 0) a += l->c[2][r - 1] * (xr - x[r - 1]);
+        y[r] = a;
+    }
+}
+
+/* Strong components of a level's members: a link is strong when c > 1e-3 sqrt(d_i d_j), d the
+   cell's diagonal (e + its links). Union-find with path halving, roots = smallest index. */
+static int uf_find(int* p, int x) {
+    while (p[x] != x) {
+        p[x] = p[p[x]];
+        x = p[x];
+    }
+    return x;
+}
+
+static void mg_components(mg_level* l) {
+    const long JK = (long)l->J * l->K;
+    int* p = l->comp;
+    for (long r = 0; r < l->n; ++r) p[r] = l->mem[r] ? (int)r : -1;
+    for (long r = 0; r < l->n; ++r) {
+        if (!l->mem[r]) continue;
+        int i = (int)(r / JK), j = (int)((r / l->K) % l->J), k = (int)(r % l->K);
+        const long off[3] = {JK, l->K, 1};
+        const int ok[3] = {i + 1 < l->I, j + 1 < l->J, k + 1 < l->K};
+        for (int d = 0; d < 3; ++d) {
+            if (!ok[d]) continue;
+            long nb = r + off[d];
+            if (!l->mem[nb] || !(l->invd[r] > 0.0) || !(l->invd[nb] > 0.0)) continue;
+            /* c^2 > 1e-6 d_r d_nb  <=>  c^2 invd_r invd_nb > 1e-6 */
+            const double c = l->c[d][r];
+            if (c * c * l->invd[r] * l->invd[nb] > 1e-6) {
+                int a = uf_find(p, (int)r), b = uf_find(p, (int)nb);
+                if (a != b) {
+                    if (a < b) p[b] = a;
+                    else p[a] = b;
+                }
+            }
+        }
+    }
+    for (long r = 0; r < l->n; ++r)
+        if (l->mem[r]) p[r] = uf_find(p, (int)r);
+}
+
+/* Coarsening 2x2x2: each block is owned by the strong component holding most of its member
+   cells (ties: the smallest id); only those cells are restricted into the coarse cell and
+   corrected from it. Galerkin operator of that piecewise-constant prolongation in the same
+   form: coarse excess = the owned cells' excess plus their links to cells outside every
+   aggregate or in their own block but not owned; coarse links = the links between owned
+   cells of adjacent blocks. */
+static long mg_cell(const mg_level* l, int i, int j, int k) { return (long)k + (long)l->K * ((long)j + (long)l->J * i); }
+
+static void mg_coarsen(mg_level* f, mg_level* c) {
+    mg_level_alloc(c, (f->I + 1) / 2, (f->J + 1) / 2, (f->K + 1) / 2);
+    const long cJK = (long)c->J * c->K;
+    /* pass 1: owner component per block, owned flags on the fine level */
+#pragma omp parallel for schedule(static)
+    for (long C = 0; C < c->n; ++C) {
+        const int ci = (int)(C / cJK), cj = (int)((C / c->K) % c->J), ck = (int)(C % c->K);
+        int ids[8], cnt[8], nid = 0;
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b)
+                for (int g = 0; g < 2; ++g) {
+                    const int i = 2 * ci + a, j = 2 * cj + b, k = 2 * ck + g;
+                    if (i >= f->I || j >= f->J || k >= f->K) continue;
+                    const long r = mg_cell(f, i, j, k);
+                    if (!f->mem[r]) continue;
+                    int q = 0;
+                    while (q < nid && ids[q] != f->comp[r]) q++;
+                    if (q == nid) { ids[nid] = f->comp[r]; cnt[nid] = 0; nid++; }
+                    cnt[q]++;
+                }
+        int owner = -1, best = 0;
+        for (int q = 0; q < nid; ++q)
+            if (cnt[q] > best || (cnt[q] == best && ids[q] < owner)) { best = cnt[q]; owner = ids[q]; }
+        c->mem[C] = (int8_t)(nid > 0);
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b)
+                for (int g = 0; g < 2; ++g) {
+                    const int i = 2 * ci + a, j = 2 * cj + b, k = 2 * ck + g;
+                    if (i >= f->I || j >= f->J || k >= f->K) continue;
+                    const long r = mg_cell(f, i, j, k);
+                    f->owned[r] = (int8_t)(f->mem[r] && f->comp[r] == owner);
+                }
+    }
+    /* pass 2: coarse excess and links */
+    const long fJK = (long)f->J * f->K;
+#pragma omp parallel for schedule(static)
+    for (long C = 0; C < c->n; ++C) {
+        if (!c->mem[C]) continue;
+        const int ci = (int)(C / cJK), cj = (int)((C / c->K) % c->J), ck = (int)(C % c->K);
+        double ex = 0.0, cf[3] = {0.0, 0.0, 0.0};
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b)
+                for (int g = 0; g < 2; ++g) {
+                    const int i = 2 * ci + a, j = 2 * cj + b, k = 2 * ck + g;
+                    if (i >= f->I || j >= f->J || k >= f->K) continue;
+                    const long r = mg_cell(f, i, j, k);
+                    if (!f->owned[r]) continue;
+                    ex += f->e[r];
+                    const int pos[3] = {i, j, k}, lim[3] = {f->I, f->J, f->K}, side[3] = {a, b, g};
+                    const long off[3] = {fJK, f->K, 1};
+                    for (int d = 0; d < 3; ++d) {
+                        /* + neighbour */
+                        if (pos[d] + 1 < lim[d] && f->mem[r + off[d]] && f->c[d][r] != 0.0) {
+                            const long nb = r + off[d];
+                            if (side[d] == 1 && f->owned[nb]) cf[d] += f->c[d][r];  /* into the + block */
+                            else if (side[d] == 1 || !f->owned[nb]) ex += f->c[d][r]; /* out of every aggregate */
+                        }
+                        /* - neighbour */
+                        if (pos[d] > 0 && f->mem[r - off[d]] && f->c[d][r - off[d]] != 0.0) {
+                            const long nb = r - off[d];
+                            if (side[d] == 0 && f->owned[nb]) { /* the - block's link, counted there */ }
+                            else if (side[d] == 0 || !f->owned[nb]) ex += f->c[d][nb];
+                        }
+                    }
+                }
+        c->e[C] = ex;
+        for (int d = 0; d < 3; ++d) c->c[d][C] = cf[d];
+    }
+    mg_invd(c);
+}
+
+static void mg_build(mg_hier* h, const lso_state* s, const ell_sys* e, const int8_t* cls) {
+    mg_free(h);
+    mg_level* l0 = &h->L[0];
+    mg_level_alloc(l0, s->I, s->J, s->K);
+    const int I = s->I, J = s->J, K = s->K;
+    const long JK = (long)s->JK;
+#pragma omp parallel for schedule(static)
+    for (long r = 0; r < (long)s->N; ++r) {
+        if (cls[r] != 1) continue;
+        int i = (int)(r / JK), j = (int)((r / K) % J), k = (int)(r % K);
+        l0->mem[r] = 1;
+        double ex = -e->diag[r];
+        long nb[6] = {r + JK, r - JK, r + K, r - K, r + 1, r - 1};
+        int val[6] = {i + 1 < I, i > 0, j + 1 < J, j > 0, k + 1 < K, k > 0};
+        for (int d = 0; d < 6; ++d)
+            if (val[d] && cls[nb[d]] == 1) ex -= e->A[d][r];
+        l0->e[r] = ex > 0.0 ? ex : 0.0;
+        l0->c[0][r] = (val[0] && cls[nb[0]] == 1) ? e->A[0][r] : 0.0;
+        l0->c[1][r] = (val[2] && cls[nb[2]] == 1) ? e->A[2][r] : 0.0;
+        l0->c[2][r] = (val[4] && cls[nb[4]] == 1) ? e->A[4][r] : 0.0;
+    }
+    mg_invd(l0);
+    h->nlev = 1;
+    while (h->nlev < 24) {
+        mg_level* f = &h->L[h->nlev - 1];
+        if (f->n <= 512 || (f->I <= 2 && f->J <= 2 && f->K <= 2)) break;
+        mg_components(f);
+        mg_coarsen(f, &h->L[h->nlev]);
+        h->nlev++;
+    }
+}
+
+static void mg_jacobi(mg_level* l, const double* b, double* x, double* t, int sweeps, double w) {
+    for (int q = 0; q < sweeps; ++q) {
+        mg_apply(l, x, t);
+#pragma omp parallel for schedule(static)
+        for (long r = 0; r < l->n; ++r)
+            if (l->mem[r]) x[r] += w * l->invd[r] * (b[r] - t[r]);
+    }
+}
+
+/* z = V(r): one V-cycle from z = 0 (a fixed symmetric linear operator) */
+static void mg_vcycle(mg_hier* h, int q, const double* b, double* x) {
+    mg_level* l = &h->L[q];
+    memset(x, 0, sizeof(double) * l->n);
+    const double w = 0.6;
+    if (q == h->nlev - 1) {
+        mg_jacobi(l, b, x, l->t, 40, w);
+        return;
+    }
+    mg_jacobi(l, b, x, l->t, 2, w);
+    mg_apply(l, x, l->t);
+    mg_level* c = &h->L[q + 1];
+    const long fJK = (long)l->J * l->K, cJK = (long)c->J * c->K;
+#pragma omp parallel for schedule(static)
+    for (long C = 0; C < c->n; ++C) {
+        const int ci = (int)(C / cJK), cj = (int)((C / c->K) % c->J), ck = (int)(C % c->K);
+        double acc = 0.0;
+        for (int a = 0; a < 2; ++a)
+            for (int bb = 0; bb < 2; ++bb)
+                for (int g = 0; g < 2; ++g) {
+                    const int i = 2 * ci + a, j = 2 * cj + bb, k = 2 * ck + g;
+                    if (i >= l->I || j >= l->J || k >= l->K) continue;
+                    const long r = (long)k + (long)l->K * ((long)j + (long)l->J * i);
+                    if (l->owned[r]) acc += b[r] - l->t[r];
+                }
+        c->b[C] = acc;
+    }
+    mg_vcycle(h, q + 1, c->b, c->x);
+#pragma omp parallel for schedule(static)
+    for (long r = 0; r < l->n; ++r) {
+        if (!l->owned[r]) continue;
+        int i = (int)(r / fJK), j = (int)((r / l->K) % l->J), k = (int)(r % l->K);
+        long C = (long)(k / 2) + (long)c->K * ((long)(j / 2) + (long)c->J * (i / 2));
+        x[r] += 1.8 * c->x[C];
+    }
+    /* post-smoothing from the corrected iterate (symmetric with the pre-smoothing) */
+    mg_jacobi(l, b, x, l->t, 2, w);
+}
+
+/* Pressure solve on the Pore block (modes LSO_SOLVE_PCG and LSO_SOLVE_PRODUCTION). Identity
+   rows take their value; S solves M x_S = A_SQ x_Q - b_S by multigrid-preconditioned CG until
+   the Jacobi-scaled residual of the S rows is below rtol times the Jacobi-scaled norm of b
+   (the test the GPU solver and PETSc's Jacobi-preconditioned GMRES apply); the floored Pore
+   rows F (src/Simulation.cpp:783-786: diagonal +1e-16) are then evaluated from their own
+   row, and the pair is repeated until the floored values settle (their links are ~1e-22 or
+   smaller). */
+static int pressure_pcg(lso_state* s, const ell_sys* e, double* x, double rtol, int max_it, int* its_out,
+                        double* rel_out) {
+    const long n = (long)s->N;
+    const int I = s->I, J = s->J, K = s->K;
+    const long JK = (long)s->JK;
+    double* rhs = (double*)xcalloc(n, sizeof(double));
+    double* rr = (double*)xcalloc(n, sizeof(double));
+    double* z = (double*)xcalloc(n, sizeof(double));
+    double* pp = (double*)xcalloc(n, sizeof(double));
+    double* q = (double*)xcalloc(n, sizeof(double));
+    int8_t* cls = (int8_t*)xcalloc(n, 1); /* 0 fixed/empty, 1 normal Pore (S), 2 floored (F) */
+    double bden = 0.0;
+    for (long r = 0; r < n; ++r) {
+        if (e->kind[r] == 1) { x[r] = e->b[r]; cls[r] = 0; }
+        else if (e->kind[r] == 2) cls[r] = (e->diag[r] < 0.0) ? 1 : 2;
+        if (e->diag[r] != 0.0) {
+            double t = e->b[r] / e->diag[r];
+            bden += t * t;
+        }
+    }
+    mg_hier h;
+    memset(&h, 0, sizeof(h));
+    mg_build(&h, s, e, cls);
+    mg_level* l0 = &h.L[0];
+    int its = 0, reason = 2;
+    const double stop = rtol * rtol * (bden > 0.0 ? bden : 1.0);
+    for (int outer = 0; outer < 8; ++outer) {
+        /* rhs_S = -(b_S - sum over non-S neighbours of A x) */
+#pragma omp parallel for schedule(static)
+        for (long r = 0; r < n; ++r) {
+            if (cls[r] != 1) { rhs[r] = 0.0; x[r] = (cls[r] == 1) ? x[r] : x[r]; continue; }
+            int i = (int)(r / JK), j = (int)((r / K) % J), k = (int)(r % K);
+            double a = e->b[r];
+            long nb[6] = {r + JK, r - JK, r + K, r - K, r + 1, r - 1};
+            int val[6] = {i + 1 < I, i > 0, j + 1 < J, j > 0, k + 1 < K, k > 0};
+            for (int d = 0; d < 6; ++d)
+                if (val[d] && cls[nb[d]] != 1) a -= e->A[d][r] * x[nb[d]];
+            rhs[r] = -a;
+        }
+        /* the S part of x as a level-0 vector (zero elsewhere) */
+#pragma omp parallel for schedule(static)
+        for (long r = 0; r < n; ++r) q[r] = (cls[r] == 1) ? x[r] : 0.0;
+        mg_apply(l0, q, z);
+        double rz = 0.0, rn = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : rn)
+        for (long r = 0; r < n; ++r) {
+            rr[r] = (cls[r] == 1) ? rhs[r] - z[r] : 0.0;
+            const double t = rr[r] / e->diag[r];
+            if (cls[r] == 1) rn += t * t;
+        }
+        if (rn > stop) {
+            mg_vcycle(&h, 0, rr, z);
+#pragma omp parallel for schedule(static) reduction(+ : rz)
+            for (long r = 0; r < n; ++r) {
+                pp[r] = z[r];
+                rz += rr[r] * z[r];
+            }
+        }
+        while (rn > stop && its < max_it) {
+            mg_apply(l0, pp, q);
+            double pq = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : pq)
+            for (long r = 0; r < n; ++r) pq += pp[r] * q[r];
+            if (!(pq > 0.0)) { reason = (pq == pq) ? -3 : -4; break; }
+            const double alpha = rz / pq;
+            rn = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : rn)
+            for (long r = 0; r < n; ++r) {
+                if (cls[r] != 1) continue;
+                x[r] += alpha * pp[r];
+                rr[r] -= alpha * q[r];
+                const double t = rr[r] / e->diag[r];
+                rn += t * t;
+            }
+            its++;
+            if (!(rn == rn)) { reason = -4; break; }
+            if (rn <= stop) break;
+            mg_vcycle(&h, 0, rr, z);
+            double rzn = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : rzn)
+            for (long r = 0; r < n; ++r) rzn += rr[r] * z[r];
+            const double beta = rzn / rz;
+            rz = rzn;
+#pragma omp parallel for schedule(static)
+            for (long r = 0; r < n; ++r) pp[r] = z[r] + beta * pp[r];
+        }
+        if (reason < 0) break;
+        if (rn > stop) { reason = -3; break; }
+        /* floored rows from their own row */
+        double change = 0.0, mag = 0.0;
+        for (long r = 0; r < n; ++r) {
+            if (cls[r] != 2) continue;
+            int i = (int)(r / JK), j = (int)((r / K) % J), k = (int)(r % K);
+            double a = e->b[r];
+            long nb[6] = {r + JK, r - JK, r + K, r - K, r + 1, r - 1};
+            int val[6] = {i + 1 < I, i > 0, j + 1 < J, j > 0, k + 1 < K, k > 0};
+            for (int d = 0; d < 6; ++d)
+                if (val[d]) a -= e->A[d][r] * x[nb[d]];
+            double v = a / e->diag[r];
+            change = smax(change, fabs(v - x[r]));
+            mag = smax(mag, fabs(v));
+            x[r] = v;
+        }
+        if (change <= 1e-15 * smax(mag, 1e-300)) break;
+    }
+    mg_free(&h);
+    free(rhs); free(rr); free(z); free(pp); free(q); free(cls);
+    *its_out = its;
+    *rel_out = scaled_residual(s, e, e->b, x);
+    return reason;
+}
+
 /* Jacobi-scaled relative residual of the current x: ||B (b - A x)|| / ||B b||. */
 static double scaled_residual(lso_state* s, const ell_sys* e, const double* b, const double* x) {
     const long n = (long)s->N;
@@ -529,22 +956,28 @@ static double scaled_residual(lso_state* s, const ell_sys* e, const double* b, c
    TIGHT mode uses the config (default rtol 1e-13). The ls_params tolerances are used
    when the config gives none. */
 static int run_solve(lso_state* s, const ell_sys* e, double* x, double rtol_param,
-                     int maxit_param, int solves, ls_solve_info* info) {
+                     int maxit_param, int solves, ls_solve_info* info, int spd) {
     double rtol, max_it_d;
     if (s->cfg.mode == LSO_SOLVE_REFERENCE) {
         rtol = (s->cfg.rtol > 0.0) ? s->cfg.rtol : 1e-6;
         max_it_d = (s->cfg.max_it > 0) ? s->cfg.max_it : 10000;
+    } else if (s->cfg.mode == LSO_SOLVE_PRODUCTION) {
+        rtol = (s->cfg.rtol > 0.0) ? s->cfg.rtol : (rtol_param > 0.0 ? rtol_param : 1e-6);
+        max_it_d = (s->cfg.max_it > 0) ? s->cfg.max_it : (maxit_param > 0 ? maxit_param : 10000);
     } else {
         rtol = (s->cfg.rtol > 0.0) ? s->cfg.rtol : (rtol_param > 0.0 ? rtol_param : 1e-13);
         max_it_d = (s->cfg.max_it > 0) ? s->cfg.max_it : (maxit_param > 0 ? maxit_param : 100000);
     }
     int max_it = (int)max_it_d;
-    int restart = (s->cfg.mode == LSO_SOLVE_REFERENCE) ? 30 : (s->cfg.restart > 0 ? s->cfg.restart : 30);
+    int restart = (s->cfg.mode == LSO_SOLVE_REFERENCE || s->cfg.mode == LSO_SOLVE_PRODUCTION)
+                      ? 30 : (s->cfg.restart > 0 ? s->cfg.restart : 30);
     int its = 0, reason = 0;
     double rel = 0.0;
     int total = 0;
     for (int q = 0; q < solves; ++q) {
-        reason = gmres(s, e, e->b, x, restart, rtol, max_it, &its, &rel);
+        if (spd && (s->cfg.mode == LSO_SOLVE_PCG || s->cfg.mode == LSO_SOLVE_PRODUCTION))
+            reason = pressure_pcg(s, e, x, rtol, max_it, &its, &rel);
+        else reason = gmres(s, e, e->b, x, restart, rtol, max_it, &its, &rel);
         total += its;
     }
     if (info) {
@@ -566,7 +999,7 @@ static int run_solve(lso_state* s, const ell_sys* e, double* x, double rtol_para
 
 static int solves_per_call(const lso_state* s) {
     /* KSPSolve runs twice per pressure/conc/acid solve (S.cpp:823-825, 1262-1264, 2188-2190). */
-    return s->cfg.mode == LSO_SOLVE_REFERENCE ? 2 : 1;
+    return (s->cfg.mode == LSO_SOLVE_REFERENCE || s->cfg.mode == LSO_SOLVE_PRODUCTION) ? 2 : 1;
 }
 
 static double* solution_slots(lso_state* s, double* field) {
@@ -576,7 +1009,9 @@ static double* solution_slots(lso_state* s, double* field) {
 /* ------------------------------------------------------------------------ */
 /* pressure                                                                  */
 
-/* Simulation::setupPressureEqns, S.cpp:658-798. */
+/* Simulation::setupPressureEqns, S.cpp:658-798. With bc_mode LS_BC_FLOW_I (an extension)
+ * the Pore voxels of the planes i = 0 and i = I-1 are identity rows holding p_inlet and
+ * p_outlet; every other row is the reference's. */
 void lso_setup_pressure(lso_state* s, double current_time) {
     const double ramp_duration = 3600.0;
     double effective_top_pressure = s->p.top_pressure;
@@ -606,6 +1041,10 @@ void lso_setup_pressure(lso_state* s, double current_time) {
                         }
                         e->b[r] = 0.0 + (is_surface ? effective_top_pressure : 0.0);
                     }
+                } else if (t == PORE && s->p.bc_mode == LS_BC_FLOW_I && (i == 0 || i == I - 1)) {
+                    e->diag[r] = 1.0;
+                    e->b[r] = 0.0 + (i == 0 ? s->p.p_inlet : s->p.p_outlet);
+                    e->kind[r] = 1;
                 } else if (t == PORE) {
                     double diagonal_term = 0.0, source_term = 0.0;
                     for (int d = 0; d < 6; ++d) {
@@ -637,7 +1076,7 @@ void lso_setup_pressure(lso_state* s, double current_time) {
 /* Simulation::solvePressure, S.cpp:804-855. */
 int lso_solve_pressure(lso_state* s, ls_solve_info* info) {
     double* x = solution_slots(s, s->P);
-    return run_solve(s, &s->press, x, s->p.press_rtol, s->p.press_max_it, solves_per_call(s), info);
+    return run_solve(s, &s->press, x, s->p.press_rtol, s->p.press_max_it, solves_per_call(s), info, 1);
 }
 
 void lso_pressure_apply(const lso_state* s, const double* x, double* y) { ell_apply(s, &s->press, x, y); }
@@ -826,7 +1265,7 @@ void lso_setup_saturation(lso_state* s, double dt) {
 int lso_solve_saturation(lso_state* s, ls_solve_info* info, int* physics_valid) {
     double* x = solution_slots(s, s->sat);
     ls_solve_info loc;
-    int ok = run_solve(s, &s->satsys, x, s->p.sat_rtol, s->p.sat_max_it, 1, &loc);
+    int ok = run_solve(s, &s->satsys, x, s->p.sat_rtol, s->p.sat_max_it, 1, &loc, 0);
     int valid = 1;
     if (loc.max_value > 1.05 || loc.min_value < -0.05) valid = 0;
     if (valid) {
@@ -842,9 +1281,12 @@ int lso_solve_saturation(lso_state* s, ls_solve_info* info, int* physics_valid) 
 /* Simulation::handleSurfaceEffects, S.cpp:2063-2103. */
 void lso_handle_surface(lso_state* s) {
     const int I = s->I, J = s->J, K = s->K;
-    for (int k = 0; k < K; ++k)
+    /* order-independent: a voxel's test reads only whether its neighbours are Air, and the
+       flips it makes (Pore -> Precipitate) never create Air */
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < I; ++i)
         for (int j = 0; j < J; ++j)
-            for (int i = 0; i < I; ++i) {
+            for (int k = 0; k < K; ++k) {
                 size_t r = IDX(s, i, j, k), nb;
                 if (s->label[r] == PORE && s->sat[r] > 0.0) {
                     int is_surface_voxel = 0;
@@ -862,7 +1304,9 @@ void lso_handle_surface(lso_state* s) {
 /* transport                                                                 */
 
 /* Simulation::setupConcentrationEqns, active part S.cpp:1129-1232 (the block at
- * S.cpp:997-1128 is commented out). Links to neighbours outside the domain are
+ * S.cpp:997-1128 is commented out). With bc_mode LS_BC_FLOW_I (an extension, after the
+ * inlet_bc rows of that disabled block, S.cpp:997-1004) the Pore and Air voxels of plane
+ * i = 0 are identity rows holding conc_inlet / acid_inlet. Links to neighbours outside the domain are
  * skipped: the reference evaluates flux_x[Index(i-1,j,k)] before set_pore_link's own
  * validity test (S.cpp:1227,1229,1231), which throws at the low faces; the link it
  * would build is skipped either way. */
@@ -872,21 +1316,32 @@ void lso_setup_conc(lso_state* s, double dt, int which) {
     const double theta = s->p.theta, alpha = s->p.alpha_transfer, dx = s->p.dx;
     ell_sys* e = &s->trans;
     const int I = s->I, J = s->J, K = s->K;
-    for (int k = 0; k < K; ++k)
+    /* Each row depends only on labels, fluxes and field values of its voxel and neighbours.
+       The reference zeroes the fluxes of Rock and Precipitate voxels inside the same loop
+       (S.cpp:1133-1148); no row uses the flux of such a neighbour (a Rock neighbour takes the
+       exchange branch, a Precipitate neighbour's advection is zeroed), so the rows are built
+       first, in parallel, and the fluxes zeroed after. */
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < I; ++i)
         for (int j = 0; j < J; ++j)
-            for (int i = 0; i < I; ++i) {
+            for (int k = 0; k < K; ++k) {
                 size_t r = IDX(s, i, j, k), nb;
                 uint16_t t = s->label[r];
                 for (int d = 0; d < 6; ++d) e->A[d][r] = 0.0;
+                if (s->p.bc_mode == LS_BC_FLOW_I && i == 0 && (t == PORE || t == AIR)) {
+                    /* inlet plane (extension): the fluid voxels hold the inflow value */
+                    e->diag[r] = 1.0;
+                    e->b[r] = 0.0 + (which ? s->p.acid_inlet : s->p.conc_inlet);
+                    e->kind[r] = 1;
+                    continue;
+                }
                 if (t == PRECIPITATE) {
-                    s->fx[r] = 0.0; s->fy[r] = 0.0; s->fz[r] = 0.0;
                     e->diag[r] = 1.0;
                     e->b[r] = 0.0 + field[r];
                     e->kind[r] = 1;
                     continue;
                 }
                 if (t == ROCK) {
-                    s->fx[r] = 0.0; s->fy[r] = 0.0; s->fz[r] = 0.0;
                     double diag = inv_dt;
                     e->b[r] = 0.0 + field[r] * inv_dt;
                     for (int d = 0; d < 6; ++d) {
@@ -903,6 +1358,12 @@ void lso_setup_conc(lso_state* s, double dt, int which) {
                 double rhs = 0.0 + field[r] * inv_dt;
                 for (int d = 0; d < 6; ++d) {
                     if (!NB(s, i, j, k, d, &nb)) continue;
+                    uint16_t nt = s->label[nb];
+                    if (nt == ROCK) {
+                        diag += alpha;
+                        e->A[d][r] = -alpha;
+                        continue;
+                    }
                     double q_face;
                     switch (d) {
                     case 0: q_face = s->fx[r]; break;
@@ -911,12 +1372,6 @@ void lso_setup_conc(lso_state* s, double dt, int which) {
                     case 3: q_face = -s->fy[nb]; break;
                     case 4: q_face = s->fz[r]; break;
                     default: q_face = -s->fz[nb]; break;
-                    }
-                    uint16_t nt = s->label[nb];
-                    if (nt == ROCK) {
-                        diag += alpha;
-                        e->A[d][r] = -alpha;
-                        continue;
                     }
                     double actual_q_face = q_face;
                     if (nt == PRECIPITATE || nt == SULPHIDE) actual_q_face = 0.0;
@@ -936,12 +1391,18 @@ void lso_setup_conc(lso_state* s, double dt, int which) {
                 e->b[r] = rhs;
                 e->kind[r] = 2;
             }
+    const long N = (long)s->N;
+#pragma omp parallel for schedule(static)
+    for (long r = 0; r < N; ++r) {
+        uint16_t t = s->label[r];
+        if (t == PRECIPITATE || t == ROCK) { s->fx[r] = 0.0; s->fy[r] = 0.0; s->fz[r] = 0.0; }
+    }
 }
 
 /* Simulation::solveConc (S.cpp:1243-1295) / solveAcid (S.cpp:2167-2224). */
 int lso_solve_conc(lso_state* s, int which, ls_solve_info* info) {
     double* x = solution_slots(s, which ? s->acid : s->conc);
-    return run_solve(s, &s->trans, x, s->p.conc_rtol, s->p.conc_max_it, solves_per_call(s), info);
+    return run_solve(s, &s->trans, x, s->p.conc_rtol, s->p.conc_max_it, solves_per_call(s), info, 0);
 }
 
 void lso_transport_apply(const lso_state* s, const double* x, double* y) { ell_apply(s, &s->trans, x, y); }
@@ -950,7 +1411,9 @@ void lso_transport_rhs(const lso_state* s, double* b) { memcpy(b, s->trans.b, s-
 /* Simulation::handlePrecipitation, S.cpp:2114-2165. */
 void lso_handle_precip(lso_state* s) {
     const double c_sat = s->p.c_sat;
-    for (size_t r = 0; r < s->N; ++r) {
+    const long N = (long)s->N;
+#pragma omp parallel for schedule(static)
+    for (long r = 0; r < N; ++r) {
         if (s->label[r] == PORE && s->conc[r] > c_sat) {
             double excess_conc = s->conc[r] - c_sat;
             if (s->p.use_instant_precipitation) {
@@ -993,9 +1456,11 @@ int lso_update_frac(lso_state* s, double dt, ls_substep_info* info) {
     const double dx = s->p.dx;
     int leached_locally = 0;
     double max_rate = 0.0;
-    for (int k = 0; k < K; ++k)
+    /* the rate pass in parallel (a maximum does not depend on the order) */
+#pragma omp parallel for schedule(static) reduction(max : max_rate)
+    for (int i = 0; i < I; ++i)
         for (int j = 0; j < J; ++j)
-            for (int i = 0; i < I; ++i) {
+            for (int k = 0; k < K; ++k) {
                 size_t r = IDX(s, i, j, k);
                 if (s->label[r] == SULPHIDE) {
                     double flux_sum = 0.0;
@@ -1023,11 +1488,26 @@ int lso_update_frac(lso_state* s, double dt, ls_substep_info* info) {
     static const int di[6] = {1, -1, 0, 0, 0, 0};
     static const int dj[6] = {0, 0, 1, -1, 0, 0};
     static const int dk[6] = {0, 0, 0, 0, 1, -1};
-    for (int step = 0; step < num_steps; ++step) {
+    /* The sweeps visit, in the reference's loop order (k outer, i inner), only the voxels that
+       are active (label >= Sulphide, frac > 0) at the start: a sweep only ever lowers frac and
+       turns Sulphide into Pore, so no other voxel becomes active during the call. */
+    size_t nact = 0;
+    for (size_t r = 0; r < s->N; ++r)
+        if (s->label[r] >= SULPHIDE && s->frac[r] > 0.0) nact++;
+    size_t* act = (size_t*)xcalloc(nact ? nact : 1, sizeof(size_t));
+    {
+        size_t q = 0;
         for (int k = 0; k < K; ++k)
             for (int j = 0; j < J; ++j)
                 for (int i = 0; i < I; ++i) {
                     size_t r = IDX(s, i, j, k);
+                    if (s->label[r] >= SULPHIDE && s->frac[r] > 0.0) act[q++] = r;
+                }
+    }
+    for (int step = 0; step < num_steps; ++step) {
+        for (size_t q = 0; q < nact; ++q) {
+                    const size_t r = act[q];
+                    const int i = (int)(r / s->JK), j = (int)((r / (size_t)K) % (size_t)J), k = (int)(r % (size_t)K);
                     if (s->label[r] >= SULPHIDE && s->frac[r] > 0.0) {
                         double f[6];
                         for (int d = 0; d < 6; ++d) f[d] = surface_flux(s, i, j, k, d);
@@ -1054,43 +1534,73 @@ int lso_update_frac(lso_state* s, double dt, ls_substep_info* info) {
                             }
                         }
                     }
-                }
+        }
     }
+    free(act);
     return leached_locally;
 }
 
 /* ------------------------------------------------------------------------ */
 /* snapshot / rollback, S.cpp:2312-2353                                      */
 
+/* memcpy split over the threads */
+static void pcopy(void* dst, const void* src, size_t bytes) {
+    const long chunks = 64;
+#pragma omp parallel for schedule(static)
+    for (long c = 0; c < chunks; ++c) {
+        size_t a = bytes * (size_t)c / (size_t)chunks, b = bytes * (size_t)(c + 1) / (size_t)chunks;
+        memcpy((char*)dst + a, (const char*)src + a, b - a);
+    }
+}
+
 void lso_save_state(lso_state* s) {
     size_t n = s->NP;
-    memcpy(s->b_label, s->label, n * sizeof(uint16_t));
-    memcpy(s->b_frac, s->frac, n * sizeof(float));
-    memcpy(s->b_precip, s->precip, n * sizeof(double));
-    memcpy(s->b_sat, s->sat, n * sizeof(double));
-    memcpy(s->b_P, s->P, n * sizeof(double));
-    memcpy(s->b_conc, s->conc, n * sizeof(double));
-    memcpy(s->b_acid, s->acid, n * sizeof(double));
-    memcpy(s->b_fx, s->fx, n * sizeof(double));
-    memcpy(s->b_fy, s->fy, n * sizeof(double));
-    memcpy(s->b_fz, s->fz, n * sizeof(double));
+    pcopy(s->b_label, s->label, n * sizeof(uint16_t));
+    pcopy(s->b_frac, s->frac, n * sizeof(float));
+    pcopy(s->b_precip, s->precip, n * sizeof(double));
+    pcopy(s->b_sat, s->sat, n * sizeof(double));
+    pcopy(s->b_P, s->P, n * sizeof(double));
+    pcopy(s->b_conc, s->conc, n * sizeof(double));
+    pcopy(s->b_acid, s->acid, n * sizeof(double));
+    pcopy(s->b_fx, s->fx, n * sizeof(double));
+    pcopy(s->b_fy, s->fy, n * sizeof(double));
+    pcopy(s->b_fz, s->fz, n * sizeof(double));
 }
 
 void lso_restore_state(lso_state* s) {
     size_t n = s->NP;
-    memcpy(s->label, s->b_label, n * sizeof(uint16_t));
-    memcpy(s->frac, s->b_frac, n * sizeof(float));
-    memcpy(s->precip, s->b_precip, n * sizeof(double));
-    memcpy(s->sat, s->b_sat, n * sizeof(double));
-    memcpy(s->P, s->b_P, n * sizeof(double));
-    memcpy(s->conc, s->b_conc, n * sizeof(double));
-    memcpy(s->acid, s->b_acid, n * sizeof(double));
-    memcpy(s->fx, s->b_fx, n * sizeof(double));
-    memcpy(s->fy, s->b_fy, n * sizeof(double));
-    memcpy(s->fz, s->b_fz, n * sizeof(double));
+    pcopy(s->label, s->b_label, n * sizeof(uint16_t));
+    pcopy(s->frac, s->b_frac, n * sizeof(float));
+    pcopy(s->precip, s->b_precip, n * sizeof(double));
+    pcopy(s->sat, s->b_sat, n * sizeof(double));
+    pcopy(s->P, s->b_P, n * sizeof(double));
+    pcopy(s->conc, s->b_conc, n * sizeof(double));
+    pcopy(s->acid, s->b_acid, n * sizeof(double));
+    pcopy(s->fx, s->b_fx, n * sizeof(double));
+    pcopy(s->fy, s->b_fy, n * sizeof(double));
+    pcopy(s->fz, s->b_fz, n * sizeof(double));
     lso_update_relperm(s);
     lso_update_cap(s);
     lso_init_properties(s);
+}
+
+/* ------------------------------------------------------------------------ */
+/* FP64 budget of a step (an extension; the reference keeps only the leached count,
+ * main.cpp:414-431): sums over the N voxels in index order. acid_pre holds the acid
+ * before the dissolution sweep (NULL: the sweep did not run), b_frac the frac at the
+ * start of the step. */
+static void lso_budget(const lso_state* s, const double* acid_pre, ls_budget* b) {
+    memset(b, 0, sizeof(*b));
+    for (size_t r = 0; r < s->N; ++r) {
+        b->conc += s->conc[r];
+        b->acid += s->acid[r];
+        b->mineral += (double)s->frac[r];
+        b->precipitate += s->precip[r];
+        if (acid_pre) b->acid_consumed += acid_pre[r] - s->acid[r];
+        b->mineral_dissolved += (double)s->b_frac[r] - (double)s->frac[r];
+        if (s->label[r] == SULPHIDE) b->sulphide_voxels++;
+        if (s->label[r] == PRECIPITATE) b->precipitate_voxels++;
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1130,8 +1640,12 @@ int lso_step(lso_state* s, double t, double dt, ls_step_info* info) {
     }
     if (ok) {
         lso_handle_precip(s);
+        double* acid_pre = (double*)xcalloc(s->N, sizeof(double));
+        memcpy(acid_pre, s->acid, s->N * sizeof(double));
         loc.leached = lso_update_frac(s, dt, &loc.leaching);
         s->total_leached += (unsigned long long)loc.leached;
+        lso_budget(s, acid_pre, &loc.budget);
+        free(acid_pre);
     }
     loc.success = ok;
     if (info) *info = loc;

@@ -32,7 +32,14 @@ extern "C" {
 /* Linear solver modes. */
 enum {
     LSO_SOLVE_REFERENCE = 0, /* GMRES(30)+Jacobi, rtol/max_it from params, KSPSolve called twice */
-    LSO_SOLVE_TIGHT = 1      /* GMRES(restart)+Jacobi to a tight rtol, once */
+    LSO_SOLVE_TIGHT = 1,     /* GMRES(restart)+Jacobi to a tight rtol, once */
+    LSO_SOLVE_PCG = 2,       /* as TIGHT, but the pressure system by multigrid-preconditioned CG
+                                on its symmetric Pore block (faster at 64^3 and above) */
+    LSO_SOLVE_PRODUCTION = 3 /* the reference's production configuration (its job scripts'
+                                -press_pc_type hypre, an algebraic-multigrid preconditioner): the
+                                pressure by multigrid-preconditioned CG, the transport systems by
+                                GMRES(30)+Jacobi, tolerances from the parameters (the reference's
+                                1e-6 unless set), KSPSolve twice per solve; the timed CPU baseline */
 };
 
 typedef struct lso_solver_cfg {

@@ -18,13 +18,17 @@ LIB_PATH = os.path.join(_HERE, "liblsoracle.so")
 
 SOLVE_REFERENCE = 0
 SOLVE_TIGHT = 1
+SOLVE_PCG = 2
+SOLVE_PRODUCTION = 3
 
 
 def build(force=False):
     """Compile the oracle with the system C compiler (no FMA contraction, OpenMP)."""
     src = os.path.join(_HERE, "ls_oracle.c")
+    deps = [src, os.path.join(_HERE, "ls_oracle.h"),
+            os.path.join(os.path.dirname(_HERE), "include", "leachingsim.h")]
     if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= max(
-            os.path.getmtime(src), os.path.getmtime(os.path.join(_HERE, "ls_oracle.h"))):
+            os.path.getmtime(d) for d in deps):
         return LIB_PATH
     cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
            "-Wall", "-o", LIB_PATH + ".tmp", src, "-lm"]
@@ -139,7 +143,7 @@ class Oracle:
     def _dtype(self, fid):
         if fid == 0:
             return np.uint16
-        if fid == 1:
+        if fid in (1, 14):
             return np.float32
         return np.float64
 

@@ -33,7 +33,7 @@ def test_library_loads_and_exports_all_declared_symbols():
 
 
 def test_abi_version():
-    assert runtime.load().ls_abi_version() == 1
+    assert runtime.load().ls_abi_version() == 2
 
 
 def test_struct_layout_matches_header():
@@ -47,6 +47,8 @@ int main(void) {
   printf("%zu %zu %zu\n", offsetof(ls_params, compat_shift), offsetof(ls_params, press_solver),
          offsetof(ls_params, sat_max_it));
   printf("%zu %zu\n", offsetof(ls_step_info, leached), offsetof(ls_step_info, success));
+  printf("%zu %zu %zu %zu\n", offsetof(ls_params, bc_mode), offsetof(ls_params, rock_permeability),
+         offsetof(ls_step_info, budget), sizeof(ls_budget));
   return 0;
 }
 '''
@@ -66,6 +68,10 @@ int main(void) {
     assert vals[6] == _abi.LsParams.sat_max_it.offset
     assert vals[7] == _abi.LsStepInfo.leached.offset
     assert vals[8] == _abi.LsStepInfo.success.offset
+    assert vals[9] == _abi.LsParams.bc_mode.offset
+    assert vals[10] == _abi.LsParams.rock_permeability.offset
+    assert vals[11] == _abi.LsStepInfo.budget.offset
+    assert vals[12] == C.sizeof(_abi.LsBudget)
 
 
 def test_defaults_match_between_c_and_python():
