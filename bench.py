@@ -15,6 +15,19 @@ host memory (file writing excluded).
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 
+The CPU baseline (`cpu_baseline` and the `--impl reference` arm) runs the oracle's
+production mode on the same 338 x 338 x 283 grid, on all host cores, with no scaling:
+multigrid-preconditioned CG for the pressure (the stand-in for the algebraic multigrid the
+reference's job scripts select, -press_pc_type hypre) and GMRES(30)+Jacobi for the
+transport systems, each solve run twice like the reference's KSPSolve pair. The
+`cpu_baseline` leg times a few steps from the state the GPU run reached and compares the
+fields the two then produce; the reference arm runs the whole workload from the labels.
+
+`flow_mode` (inside the line, or alone with `--flow`): the same geometry without the Air
+planes, driven by the flow-through pressure boundary (P = 1 on the Pore voxels of z = 0,
+P = 0 on those of z = max, no-flow sides), so that every step solves a changed pressure
+system.
+
 Separate lines: `--mixed` (the 512^3 uint16 fractured geometry, mixed precision against
 FP64 settings, per-field error and memory footprint) and `--geometry` (the geometry
 pre-processing pipeline at 512^3).
@@ -38,7 +51,9 @@ UNIT = "time-steps/s"
 SHAPE = (283, 338, 338)  # (I, J, K) = (zext, yext, xext)
 GEOM = dict(porosity=0.25, corr_len=6.0, mineral_fraction=0.15, seed=0)
 DT, TMAX, NOUT = 1.0, 50.0, 10
-CPU_SAMPLE = (48, 96, 96)  # inlet block of the same geometry for the CPU baseline
+CPU_STEPS = 3  # steps of the cpu_baseline leg at the full grid
+PRECISION = ("FP64 fields, residuals, refinement and budgets; FP32 inner Krylov / multigrid "
+             "iterations of the pressure and transport solves")
 # output arrays of src/Simulation.cpp:1401-1485 (label, frac, 10 float64 fields)
 OUTPUT_FIELDS = ["label", "conc", "pressure", "frac", "flux_x", "flux_y", "flux_z", "saturation",
                  "cap_pressure", "rel_perm", "permeability", "acid"]
@@ -85,11 +100,20 @@ CONC_RTOL = 1e-6
 PRESS_RTOL = 1e-8
 
 
-def params(solver):
+def params(solver, **kw):
     from leachingsim_gb300._abi import PRESS_FP64, PRESS_JACOBI64, PRESS_MIXED, default_params
     s = {"mixed": PRESS_MIXED, "fp64": PRESS_FP64, "jacobi64": PRESS_JACOBI64}[solver]
     return default_params(c_sat=1.0, D=1.0, kreac=1.0, press_solver=s, conc_rtol=CONC_RTOL,
-                          sat_rtol=CONC_RTOL, press_rtol=PRESS_RTOL)
+                          sat_rtol=CONC_RTOL, press_rtol=PRESS_RTOL, **kw)
+
+
+def workload_config(shape, seed):
+    """The `config` object both arms print (identical, so the driver can pair them)."""
+    return {"workload": f"{shape[2]}x{shape[1]}x{shape[0]} uint8 GRF geometry (porosity 0.25, corr 6, 15% "
+                        "mineral, Air inlet), dt 1, tmax 50, nout 10, D 1, kreac 1, csat 1, transport rtol "
+                        "1e-6 (the reference's KSP default), pressure rtol 1e-8",
+            "shape_ijk": list(shape), "seed": seed,
+            "l2": "working set > L2" if shape[0] * shape[1] * shape[2] * 8 > 129e6 else "working set < L2"}
 
 
 # ---------------------------------------------------------------------------
@@ -191,10 +215,9 @@ def roofline(ctx, shape, nsteps):
     achieved = nbytes / (ms / 1e3) / 1e9
     peak, src = (peaks["hbm_gbs"], "measured") if peaks else (6800.0, "fallback")
     vox = shape[0] * shape[1] * shape[2]
-    # DRAM traffic per launch: dram__bytes_read.sum + dram__bytes_write.sum per voxel from ncu
-    # on the 160x256x256 case (inputs > L2), k_ti_v_pair 35.13 B and k_ti_st_pair 42.42 B
-    # (profiles/transport_apply_160x256x256.md), scaled by the voxel count; the timed launches
-    # alternate the two kernels
+    # DRAM traffic per launch: dram__bytes_read.sum + dram__bytes_write.sum per voxel from one
+    # ncu capture of the 160x256x256 case (inputs > L2), k_ti_v_pair 35.13 B and k_ti_st_pair
+    # 42.42 B, scaled by the voxel count; the timed launches alternate the two kernels
     traffic = 0.5 * (35.13 + 42.42) * vox
     return {"bound": "hbm", "kernel": "transport operator apply (k_ti_v_pair, k_ti_st_pair)",
             "achieved": round(achieved, 1), "peak": peak, "peak_source": src, "unit": "GB/s",
@@ -343,6 +366,12 @@ def gpu_arm(args, ws, rank, local):
     roof = roofline(ctx, shape, args.steps)
     ctx.timing(False)
     mem = ctx.device_bytes()
+    # the CPU baseline leg at the full grid, from this state (rank 0 of a 1-GPU run)
+    cpu = None
+    if ws == 1 and rank == 0 and not args.no_cpu:
+        cpu = cpu_leg(ctx, shape, p, t, n, args.cpu_steps)
+        t += args.cpu_steps * DT
+        n += args.cpu_steps
     # the GPU plain path: the same number of steps on the same state with the FP64 inner
     # multigrid-PCG for the pressure (the plain FP64 solver), right after the timed steps
     plain = None
@@ -399,24 +428,19 @@ def gpu_arm(args, ws, rank, local):
                "steps": nsteps, "wall_s": round(e2e_wall, 3),
                "note": "fresh run from a pinned host label image, every nout-th step's fields read back to pinned host memory"}
 
+    flow = None if args.no_flow else flow_run(args, shape, ws, barrier)
     if rank != 0:
         return None
-    cpu = None
-    if ws == 1 and not args.no_cpu:
-        cpu = cpu_sample(args.cpu_steps, 1, None)
     value = replica_rate(ws, args.steps, t_max)
     # the metric names the grid as the reference's CLI does: xext x yext x zext = K x J x I
     metric = METRIC if shape == SHAPE else f"time-steps/s at {shape[2]}x{shape[1]}x{shape[0]}"
     line = {
         "metric": metric, "value": round(value, 4), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic",
-        "config": {"workload": f"{shape[2]}x{shape[1]}x{shape[0]} uint8 GRF geometry (porosity 0.25, corr 6, 15% "
-                               "mineral, Air inlet), dt 1, tmax 50, nout 10, D 1, kreac 1, csat 1, transport rtol "
-                               "1e-6 (the reference's KSP default), pressure rtol 1e-8",
-                   "shape_ijk": list(shape), "seed": seed, "press_solver": args.solver,
-                   "parallelism": f"replicas{ws}", "l2": "working set > L2 (state %.1f GB)" % (mem / 1e9)},
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64/f32" if args.solver == "mixed" else "f64", "precision": PRECISION,
+        "data": "synthetic", "config": workload_config(shape, seed),
+        "press_solver": args.solver, "parallelism": f"replicas{ws}",
         "wall_ms_per_step": round(wall * 1e3 / args.steps, 3),
         "gpu_launches": launches,
         "device_bytes": mem,
@@ -426,62 +450,189 @@ def gpu_arm(args, ws, rank, local):
         "e2e": e2e,
         "pressure_solve": psolve,
         "plain_path": plain,
+        "flow_mode": flow,
         "clocks": clk.summary(),
     }
     return line
 
 
 # ---------------------------------------------------------------------------
-# CPU: the oracle's reference-algorithm mode (assembled operators, GMRES(30)+Jacobi,
-# rtol 1e-6, two KSPSolve calls per solve) on an inlet block of the same geometry
+# flow-through model: the workload's geometry without the Air planes, pressure held at 1 on
+# the Pore voxels of z = 0 and at 0 on those of z = max (no-flow sides), so every step solves
+# a changed pressure system (the relative permeabilities follow the saturation)
 
-def cpu_sample(steps, warmup, threads):
+FLOW_PIN, FLOW_POUT = 1.0, 0.0
+
+
+def flow_params(solver):
+    from leachingsim_gb300._abi import BC_FLOW_I
+    return params(solver, bc_mode=BC_FLOW_I, p_inlet=FLOW_PIN, p_outlet=FLOW_POUT)
+
+
+def flow_run(args, shape, ws, barrier):
+    """Steps/s of the flow-through model on the workload's grid: the first (cold) step, then
+    --warmup - 1 untimed and --steps timed steps with the mixed solver, then the same number
+    with the plain FP64 multigrid-PCG pressure solver on the state they left; per-step pressure
+    iterations and the pressure solve's share of the step from the library's timers."""
+    import torch
+    from leachingsim_gb300.geometry import grf_geometry
+    from leachingsim_gb300.runtime import Context
+    lab, seed = grf_geometry(shape, air_inlet=False, **GEOM)
+    ctx = Context(shape, label_bytes=1, params=flow_params(args.solver))
+    ctx.upload("label", lab)
+    ctx.init_all()
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.timing(True)
+    ctx.timing_reset()
+    t, n, first = run_steps(ctx, 0.0, 0, 1, DT)
+    cold = {k: round(ctx.timing_get(k)[0], 3) for k in ("press_setup", "press_inner", "press_outer")}
+    t, n, _ = run_steps(ctx, t, n, max(args.warmup - 1, 0), DT)
+
+    def timed(solver):
+        nonlocal t, n
+        ctx.set_params(flow_params(solver))
+        ctx.timing_reset()
+        barrier()
+        ev0.record(stream)
+        t, n, infos = run_steps(ctx, t, n, args.steps, DT)
+        ev1.record(stream)
+        ev1.synchronize()
+        barrier()
+        sec = max_over_ranks(ev0.elapsed_time(ev1) / 1e3, ws)
+        tm = {k: ctx.timing_get(k)[0] for k in ("press_setup", "press_inner", "press_outer")}
+        return {"value": round(replica_rate(ws, args.steps, sec), 4), "unit": UNIT,
+                "ms_per_step": round(sec * 1e3 / args.steps, 3),
+                "pressure_ms_per_step": round(sum(tm.values()) / args.steps, 3),
+                "press_inner_ms_per_step": round(tm["press_inner"] / args.steps, 3),
+                "pressure_iterations": [i["pressure"]["iterations"] for i in infos],
+                "pressure_rel_residual_max": max(i["pressure"]["rel_residual"] for i in infos)}
+
+    mixed = timed(args.solver)
+    plain = timed("fp64") if args.solver != "fp64" else None
+    ctx.timing(False)
+    ctx.close()
+    return {"metric": f"time-steps/s at {shape[2]}x{shape[1]}x{shape[0]}, flow-through pressure",
+            "workload": (f"the workload's geometry (seed {seed}) without Air planes; P = {FLOW_PIN:g} on the Pore "
+                         f"voxels of z = 0, P = {FLOW_POUT:g} on those of z = max, no-flow sides; dt 1, D 1, "
+                         "kreac 1, csat 1, pressure rtol 1e-8, transport rtol 1e-6"),
+            "steps": args.steps, "warmup": args.warmup, "mixed": mixed, "plain_fp64": plain,
+            "cold_step_pressure_ms": cold,
+            "cold_step_pressure_iterations": first[0]["pressure"]["iterations"]}
+
+
+# ---------------------------------------------------------------------------
+# CPU: the oracle's production mode (multigrid-preconditioned CG for the pressure, the
+# stand-in for the reference job scripts' -press_pc_type hypre; GMRES(30)+Jacobi for the
+# transport; two KSPSolve calls per solve; tolerances of the workload) on the full grid
+
+STATE_FIELDS = ["label", "frac", "precipitate", "saturation", "pressure", "conc", "acid", "flux_x", "flux_y",
+                "flux_z", "cap_pressure", "rel_perm", "permeability", "viscosity"]
+CMP_FIELDS = ["pressure", "flux_x", "flux_y", "flux_z", "conc", "precipitate", "saturation"]
+
+
+def cpu_threads():
+    return os.cpu_count() or 1
+
+
+def oracle_production(shape, p, threads):
     from oracle import oracle as om
-    full = SHAPE[0] * SHAPE[1] * SHAPE[2]
-    lab, _ = make_geometry(SHAPE)
-    sub = np.ascontiguousarray(lab[:CPU_SAMPLE[0], :CPU_SAMPLE[1], :CPU_SAMPLE[2]])
-    nthreads = threads or os.cpu_count() or 1
-    o = om.Oracle(sub.shape, params=params("fp64"), mode=om.SOLVE_REFERENCE, threads=nthreads)
-    o.set_solver(om.SOLVE_REFERENCE)
-    o.load_labels(sub)
-    o.init_all()
-    t = 0.0
-    for n in range(warmup):
-        o.step(t, DT)
-        t += DT
+    o = om.Oracle(shape, params=p, mode=om.SOLVE_PRODUCTION, threads=threads)
+    o.set_solver(om.SOLVE_PRODUCTION)
+    return o
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    d = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / d) if d > 0 else float(np.linalg.norm(a - b))
+
+
+def cpu_leg(ctx, shape, p, t, n, steps):
+    """The cpu_baseline leg: the state the GPU run has reached (every field, padded) goes to
+    the oracle, which runs `steps` steps on all host cores (timed); the GPU runs the same
+    steps from the same state (untimed), and the fields of both are compared."""
+    state = {f: ctx.download(f, padded=True).copy() for f in STATE_FIELDS}
+    for k in range(steps):
+        ok, _ = ctx.step(t + k * DT, DT)
+        if not ok:
+            raise RuntimeError("GPU step failed in the comparison leg")
+    gpu = {f: ctx.download(f, padded=True).copy() for f in CMP_FIELDS + ["label"]}
+    threads = cpu_threads()
+    o = oracle_production(shape, p, threads)
+    for f, v in state.items():
+        o.set(f, v.astype(np.uint16) if f == "label" else v, padded=True)
     w0 = time.perf_counter()
-    for n in range(steps):
+    iters = []
+    for k in range(steps):
+        ok, info = o.step(t + k * DT, DT)
+        if not ok:
+            raise RuntimeError("CPU reference step failed")
+        iters.append((info["pressure"]["iterations"], info["conc"]["iterations"]))
+    wall = time.perf_counter() - w0
+    cpu = {f: o.get(f, padded=True) for f in CMP_FIELDS + ["label"]}
+    o.close()
+    vel = lambda d: np.concatenate([d[k].ravel() for k in ("flux_x", "flux_y", "flux_z")])  # noqa: E731
+    cmp = {"pressure": rel_l2(gpu["pressure"], cpu["pressure"]), "velocity": rel_l2(vel(gpu), vel(cpu)),
+           "conc": rel_l2(gpu["conc"], cpu["conc"]), "saturation": rel_l2(gpu["saturation"], cpu["saturation"]),
+           "precipitate_abs": float(np.abs(gpu["precipitate"] - cpu["precipitate"]).max()),
+           "label_mismatches": int(np.count_nonzero(gpu["label"].astype(np.int64) != cpu["label"].astype(np.int64)))}
+    return {"value": round(steps / wall, 6), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": (f"{steps} steps of the full {shape[2]}x{shape[1]}x{shape[0]} grid (no scaling) from the "
+                       f"state the GPU run reached after its timed steps (t = {t:g} s), oracle production mode: "
+                       "multigrid-PCG pressure (for the job scripts' hypre AMG), GMRES(30)+Jacobi transport, "
+                       "KSPSolve twice, pressure rtol 1e-8, transport rtol 1e-6"),
+            "wall_s": round(wall, 3), "iterations": iters,
+            "gpu_vs_cpu_rel_l2": cmp,
+            "gpu_vs_cpu_note": ("the GPU's fields after the same steps from the same state, relative L2 per field "
+                                "(velocity = the three face fluxes together; precipitate as the largest absolute "
+                                "difference); both solve to the workload's tolerances")}
+
+
+def reference_arm(args, ws, rank):
+    """The reference's algorithm on the host cores, from the labels: the workload's own
+    geometry on the full grid, --warmup untimed steps (the first solves the cold pressure
+    system), then --steps timed steps. Rank 0 only."""
+    if rank != 0:
+        return None
+    shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else SHAPE
+    t0 = time.time()
+    lab, seed = make_geometry(shape)
+    threads = cpu_threads()
+    o = oracle_production(shape, params(args.solver), threads)
+    o.load_labels(lab)
+    o.init_all()
+    log(f"reference: geometry + init {time.time() - t0:.1f}s on {threads} threads")
+    t = 0.0
+    w0 = time.perf_counter()
+    for _ in range(args.warmup):
+        ok, _ = o.step(t, DT)
+        if not ok:
+            raise RuntimeError("CPU reference step failed")
+        t += DT
+    warm_wall = time.perf_counter() - w0
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
         ok, _ = o.step(t, DT)
         if not ok:
             raise RuntimeError("CPU reference step failed")
         t += DT
     wall = time.perf_counter() - w0
-    sample_rate = steps / wall
-    scale = sub.size / full
-    return {"value": round(sample_rate * scale, 6), "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": (f"{steps} warm steps (after {warmup} warm-up) of the {CPU_SAMPLE[0]}x{CPU_SAMPLE[1]}x"
-                       f"{CPU_SAMPLE[2]} inlet block (i,j,k) of the same geometry, oracle reference-"
-                       f"algorithm mode (GMRES(30)+Jacobi rtol 1e-6, KSPSolve twice); sample rate "
-                       f"{sample_rate:.3f} steps/s scaled by voxel count {sub.size}/{full}"),
-            "sample_steps_per_s": round(sample_rate, 4), "wall_s": round(wall, 3)}
-
-
-def reference_arm(args, ws, rank):
-    if rank != 0:
-        return None
-    cpu = cpu_sample(args.steps, args.warmup, None)
+    o.close()
+    value = args.steps / wall
+    metric = METRIC if shape == SHAPE else f"time-steps/s at {shape[2]}x{shape[1]}x{shape[0]}"
     return {
-        "impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(1e3 / cpu["value"], 3) if cpu["value"] else None,
+        "impl": "reference", "metric": metric, "value": round(value, 6), "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(wall * 1e3 / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic",
-        "config": {"workload": "338x338x283 uint8 GRF geometry (porosity 0.25, corr 6, 15% mineral, "
-                               "Air inlet), dt 1, tmax 50, nout 10, D 1, kreac 1, csat 1, transport rtol 1e-6 "
-                               "(the reference's KSP default), pressure rtol 1e-8",
-                   "shape_ijk": list(SHAPE), "parallelism": "host cores"},
-        "cpu_baseline": cpu,
-        "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "data": "synthetic", "config": workload_config(shape, seed),
+        "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": (f"the whole workload from the labels on the full grid: {args.warmup} untimed "
+                                    f"steps (the first a cold pressure solve, {warm_wall:.1f} s) then {args.steps} "
+                                    "timed steps; oracle production mode (multigrid-PCG pressure for the job "
+                                    "scripts' hypre AMG, GMRES(30)+Jacobi transport, KSPSolve twice)")},
+        "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
 
@@ -682,7 +833,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--solver", default="mixed", choices=["mixed", "fp64", "jacobi64"])
     ap.add_argument("--shape", default=None, help="override (I,J,K) for quick checks")
-    ap.add_argument("--cpu-steps", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=CPU_STEPS)
+    ap.add_argument("--no-flow", action="store_true", help="skip the flow-through model measurement")
+    ap.add_argument("--flow", action="store_true",
+                    help="only the flow-through model measurement, as its own JSON line")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-cold", action="store_true", help="skip the separate cold pressure solves")
@@ -702,6 +856,18 @@ def main():
         return
     if args.mixed:
         print(json.dumps(mixed_arm(args)), flush=True)
+        return
+    if args.flow:
+        import torch
+        torch.cuda.set_device(0)
+        shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else SHAPE
+        with ClockSampler(0) as clk:
+            fl = flow_run(args, shape, 1, torch.cuda.synchronize)
+        fl.update({"value": fl["mixed"]["value"], "unit": UNIT, "n_gpus": 1, "higher_is_better": True,
+                   "ms_per_step": fl["mixed"]["ms_per_step"], "scaling": "weak", "vs_baseline": None,
+                   "dtype": "f64/f32", "data": "synthetic", "config": {"workload": fl["workload"]},
+                   "clocks": clk.summary(), "e2e": None})
+        print(json.dumps(fl), flush=True)
         return
     ws, rank, local = dist_env()
     if args.warmup < 3 and args.impl == "ours":
