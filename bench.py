@@ -458,15 +458,16 @@ def gpu_arm(args, ws, rank, local):
 
 # ---------------------------------------------------------------------------
 # flow-through model: the workload's geometry without the Air planes, pressure held at 1 on
-# the Pore voxels of z = 0 and at 0 on those of z = max (no-flow sides), so every step solves
-# a changed pressure system (the relative permeabilities follow the saturation)
+# the Pore voxels of z = 0 and at 0 on those of z = max (no-flow sides), acid flowing in at
+# z = 0; the acid dissolves mineral, leached voxels open new pore space, and every step solves
+# a changed pressure system
 
-FLOW_PIN, FLOW_POUT = 1.0, 0.0
+FLOW_PIN, FLOW_POUT, FLOW_ACID = 1.0, 0.0, 1.0
 
 
 def flow_params(solver):
     from leachingsim_gb300._abi import BC_FLOW_I
-    return params(solver, bc_mode=BC_FLOW_I, p_inlet=FLOW_PIN, p_outlet=FLOW_POUT)
+    return params(solver, bc_mode=BC_FLOW_I, p_inlet=FLOW_PIN, p_outlet=FLOW_POUT, acid_inlet=FLOW_ACID)
 
 
 def flow_run(args, shape, ws, barrier):
@@ -506,7 +507,13 @@ def flow_run(args, shape, ws, barrier):
                 "pressure_ms_per_step": round(sum(tm.values()) / args.steps, 3),
                 "press_inner_ms_per_step": round(tm["press_inner"] / args.steps, 3),
                 "pressure_iterations": [i["pressure"]["iterations"] for i in infos],
-                "pressure_rel_residual_max": max(i["pressure"]["rel_residual"] for i in infos)}
+                "pressure_rel_residual_max": max(i["pressure"]["rel_residual"] for i in infos),
+                "dissolve_ms_per_step": round(ctx.timing_get("dissolve")[0] / args.steps, 3),
+                "transport_ms_per_step": round(ctx.timing_get("transport")[0] / args.steps, 3),
+                "leached_per_step": [i["leached"] for i in infos],
+                "leach_substeps": [i["leaching"]["num_steps"] for i in infos],
+                "mineral_budget_last": infos[-1]["budget"]["mineral"],
+                "dissolution_fallbacks": ctx.dissolve_fallbacks()}
 
     mixed = timed(args.solver)
     plain = timed("fp64") if args.solver != "fp64" else None
@@ -514,8 +521,9 @@ def flow_run(args, shape, ws, barrier):
     ctx.close()
     return {"metric": f"time-steps/s at {shape[2]}x{shape[1]}x{shape[0]}, flow-through pressure",
             "workload": (f"the workload's geometry (seed {seed}) without Air planes; P = {FLOW_PIN:g} on the Pore "
-                         f"voxels of z = 0, P = {FLOW_POUT:g} on those of z = max, no-flow sides; dt 1, D 1, "
-                         "kreac 1, csat 1, pressure rtol 1e-8, transport rtol 1e-6"),
+                         f"voxels of z = 0, P = {FLOW_POUT:g} on those of z = max, no-flow sides; acid "
+                         f"{FLOW_ACID:g} flowing in at z = 0; dt 1, D 1, kreac 1, csat 1, pressure rtol 1e-8, "
+                         "transport rtol 1e-6"),
             "steps": args.steps, "warmup": args.warmup, "mixed": mixed, "plain_fp64": plain,
             "cold_step_pressure_ms": cold,
             "cold_step_pressure_iterations": first[0]["pressure"]["iterations"]}

@@ -313,6 +313,10 @@ ls_status ls_transport(ls_ctx* ctx, double dt, int which, ls_solve_info* conc_in
 ls_status ls_precip(ls_ctx* ctx);
 /* Simulation::updateFrac(dt) (src/Simulation.cpp:315-617); *leached = voxels flipped. */
 ls_status ls_dissolve(ls_ctx* ctx, double dt, int* leached, ls_substep_info* info);
+/* Calls of ls_dissolve / ls_step whose sparse dissolution schedule (only the voxels that can
+   change, ordered by their dependencies) met a leach that could reach beyond it and were redone
+   with the full wavefront schedule (diagnostic; no counterpart in the reference). */
+long long ls_dissolve_fallbacks(const ls_ctx* ctx);
 /* Simulation::saveState / restoreState (src/Simulation.cpp:2312-2353); rollback also
    rebuilds the derived properties like the reference. */
 ls_status ls_snapshot(ls_ctx* ctx);
@@ -372,7 +376,10 @@ ls_status ls_geom_classify(int I, int J, int K, const uint16_t* grey_host, int n
    [27][cout][cin] (tap = 9 (dz+1) + 3 (dy+1) + (dx+1)) then the biases [cout].
    ls_lpnet_train_step runs forward, the masked mean-square loss of output vs target over
    the mask_count voxels with mask 1, backward and (update != 0) one Adam step with rate lr;
-   the gradients stay readable through ls_lpnet_get_grads. */
+   the gradients stay readable through ls_lpnet_get_grads. If a bounded wait of a tcgen05
+   convolution gives up, the network switches to its mma.sync kernels for good: ls_lpnet_forward
+   recomputes the pass with them and returns LS_STAGNATED_FALLBACK_USED (a valid output);
+   ls_lpnet_train_step returns LS_TIMEOUT (discard that step). */
 typedef struct ls_lpnet ls_lpnet;
 ls_status ls_lpnet_create(int D, int H, int W, int seed, ls_lpnet** net);
 ls_status ls_lpnet_destroy(ls_lpnet* net);

@@ -384,7 +384,8 @@ ls_status ls_destroy(ls_ctx* c) {
                     c->sh_label, c->sh_sat, c->sh_precip, c->sh_frac, c->shf_label, c->shf_perm,
                     c->shf_visc, c->psb2, c->sat_q, c->dbits, c->sht_label, c->sht_fx, c->sht_fy, c->sht_fz,
                     c->shq_P, c->shq_C, c->shq_K, c->shq_V, c->shq_fx, c->shq_fy, c->shq_fz,
-                    c->wlist, c->wcount, c->kmult};
+                    c->wlist, c->wcount, c->kmult, c->dz_sel, c->dz_flips, c->dz_save_frac,
+                    c->dz_save_precip, c->dz_save_conc, c->dz_save_label};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     for (void* q : c->l0base)
@@ -583,6 +584,8 @@ ls_status ls_pressure_set_precond_weights(ls_ctx* c, const float* params, long l
 }
 
 long long ls_pressure_fallbacks(const ls_ctx* c) { return c ? c->press_fallbacks : 0; }
+
+long long ls_dissolve_fallbacks(const ls_ctx* c) { return c ? c->dz_fallbacks : 0; }
 
 ls_status ls_pressure_mg_level(ls_ctx* c, int level, int* dims, int* comp, float* e, float* f0, float* f1,
                                float* f2) {

@@ -8,8 +8,10 @@
 // (w strictly increases along each of them), and two voxels with equal w are never within
 // distance 2, so processing the levels w = 0, 1, 2, ... in order, each level in parallel,
 // reproduces the sequential result exactly.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include "ls_internal.cuh"
@@ -120,7 +122,7 @@ template <typename L>
 __global__ void k_dz_level(Grid g, DzConst dc, const int* __restrict__ list, int count,
                            L* __restrict__ label, float* __restrict__ frac,
                            double* __restrict__ acid, double* __restrict__ precip,
-                           double* __restrict__ conc, int* __restrict__ leached) {
+                           double* __restrict__ conc, int* __restrict__ leached, int* __restrict__ flips) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= count) return;
     const long long r = list[t];
@@ -151,8 +153,163 @@ __global__ void k_dz_level(Grid g, DzConst dc, const int* __restrict__ list, int
             label[r] = (L)kPore;
             precip[r] = 0.0;
             conc[r] = dc.c_sat;
-            atomicAdd(leached, 1);
+            const int pos = atomicAdd(leached, 1);
+            if (flips) flips[pos] = (int)r;  // a voxel leaches at most once per call
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Sparse schedule. A voxel changes something in a sub-step only when a Pore or Rock neighbour
+// holds nonzero acid (flux_sum != 0) or its frac is at the threshold. During a call acid
+// changes only by consumption and a label only by a leach (Sulphide -> Pore), which can make
+// the leached voxel's own acid visible to its neighbours. The sweeps therefore visit S: the
+// voxels live at the start and the active voxels within two face steps of them, ordered by
+// their dependency level within S (level(v) = 1 + the largest level of the voxels of S within
+// Manhattan distance 2 that precede v in the reference's loop order, k outer, j, i inner), so
+// every pair that can interact runs in the sequential order; voxels of one level are
+// independent. If a voxel leached during the call has an active neighbour outside S, that
+// neighbour could have become live: the call is undone (acid from its copy; frac, label,
+// precip and conc of S from theirs) and redone with the full wavefront schedule, so the
+// result is always the sequential sweep's.
+//
+// Dense map M over the N voxels: -2 not active, -1 active outside S, >= 0 in S (its level);
+// during the selection -3 / -4 mark the voxels one / two face steps from a live one.
+
+template <typename L>
+__global__ void __launch_bounds__(kBlock) k_dz_seed(Grid g, DzConst dc, const L* __restrict__ label,
+                                                    const double* __restrict__ acid,
+                                                    const float* __restrict__ frac, int* __restrict__ M) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        const int t = (int)label[r];
+        const float f = frac[r];
+        if (!(t >= kSulphide && f > 0.0f)) {
+            M[r] = -2;
+            continue;
+        }
+        int i, j, k;
+        decode(g, r, i, j, k);
+        const long long nbs[6] = {r + g.JK, r - g.JK, r + g.K, r - g.K, r + 1, r - 1};
+        const bool val[6] = {i + 1 < g.I, i > 0, j + 1 < g.J, j > 0, k + 1 < g.K, k > 0};
+        double flux_sum = 0.0;
+#pragma unroll
+        for (int d = 0; d < 6; ++d) flux_sum += dz_surface_flux(g, dc, label, acid, val[d], nbs[d]);
+        M[r] = (flux_sum != 0.0 || (double)f <= 1e-4) ? 0 : -1;
+    }
+}
+
+// active voxels outside S with a face neighbour marked `from` get `to`
+__global__ void __launch_bounds__(kBlock) k_dz_grow(Grid g, int* __restrict__ M, int from, int to) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
+         r += (long long)gridDim.x * blockDim.x) {
+        if (M[r] != -1) continue;
+        int i, j, k;
+        decode(g, r, i, j, k);
+        const bool hit = (i + 1 < g.I && M[r + g.JK] == from) || (i > 0 && M[r - g.JK] == from) ||
+                         (j + 1 < g.J && M[r + g.K] == from) || (j > 0 && M[r - g.K] == from) ||
+                         (k + 1 < g.K && M[r + 1] == from) || (k > 0 && M[r - 1] == from);
+        if (hit) M[r] = to;
+    }
+}
+
+// S as a list (any order), every member at level 0
+__global__ void __launch_bounds__(kBlock) k_dz_collect(Grid g, int* __restrict__ M, int* __restrict__ list,
+                                                       unsigned int* __restrict__ count) {
+    // block-uniform trip count (block_append is called by every thread of the block)
+    for (long long b0 = (long long)blockIdx.x * blockDim.x; b0 < g.N; b0 += (long long)gridDim.x * blockDim.x) {
+        const long long r = b0 + threadIdx.x;
+        bool in = false;
+        if (r < g.N) {
+            const int m = M[r];
+            in = (m == 0 || m == -3 || m == -4);
+            if (in) M[r] = 0;
+        }
+        block_append(in, (int)r, list, count);
+    }
+}
+
+// One relaxation pass of the levels (values only grow and stay below the longest-path
+// level, so passes in place converge to it; *changed tells whether this pass moved any).
+__global__ void __launch_bounds__(kBlock) k_dz_relax(Grid g, int* __restrict__ M, const int* __restrict__ list,
+                                                     int n, int* __restrict__ changed) {
+    // the 12 offsets (di, dj, dk) within Manhattan distance 2 that precede in (k, j, i) order
+    const int od[12][3] = {{0, 0, -1}, {0, -1, 0}, {-1, 0, 0}, {0, 0, -2}, {0, -2, 0}, {-2, 0, 0},
+                           {1, 0, -1}, {-1, 0, -1}, {0, 1, -1}, {0, -1, -1}, {1, -1, 0}, {-1, -1, 0}};
+    bool moved = false;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const long long v = list[q];
+        int i, j, k;
+        decode(g, v, i, j, k);
+        int m = 0;
+#pragma unroll
+        for (int o = 0; o < 12; ++o) {
+            const int ni = i + od[o][0], nj = j + od[o][1], nk = k + od[o][2];
+            if (ni < 0 || ni >= g.I || nj < 0 || nj >= g.J || nk < 0 || nk >= g.K) continue;
+            const int lu = M[(long long)nk + (long long)g.K * ((long long)nj + (long long)g.J * ni)];
+            if (lu >= 0 && lu + 1 > m) m = lu + 1;
+        }
+        if (m > M[v]) {
+            M[v] = m;
+            moved = true;
+        }
+    }
+    if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) *changed = 1;
+}
+
+__global__ void k_dz_lhist(const int* __restrict__ list, int n, const int* __restrict__ M, int* __restrict__ hist) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+        atomicAdd(&hist[M[list[q]]], 1);
+}
+
+__global__ void k_dz_lscatter(const int* __restrict__ list, int n, const int* __restrict__ M,
+                              const int* __restrict__ start, int* __restrict__ cursor, int* __restrict__ out) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int v = list[q];
+        const int l = M[v];
+        out[start[l] + atomicAdd(&cursor[l], 1)] = v;
+    }
+}
+
+template <typename L>
+__global__ void k_dz_save(const int* __restrict__ list, int n, const L* __restrict__ label,
+                          const float* __restrict__ frac, const double* __restrict__ precip,
+                          const double* __restrict__ conc, L* __restrict__ sl, float* __restrict__ sf,
+                          double* __restrict__ sp, double* __restrict__ sc) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int v = list[q];
+        sl[q] = label[v];
+        sf[q] = frac[v];
+        sp[q] = precip[v];
+        sc[q] = conc[v];
+    }
+}
+
+template <typename L>
+__global__ void k_dz_restore(const int* __restrict__ list, int n, L* __restrict__ label, float* __restrict__ frac,
+                             double* __restrict__ precip, double* __restrict__ conc, const L* __restrict__ sl,
+                             const float* __restrict__ sf, const double* __restrict__ sp,
+                             const double* __restrict__ sc) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int v = list[q];
+        label[v] = sl[q];
+        frac[v] = sf[q];
+        precip[v] = sp[q];
+        conc[v] = sc[q];
+    }
+}
+
+// a voxel leached during the call with an active neighbour outside S
+__global__ void k_dz_check(Grid g, const int* __restrict__ flips, const int* __restrict__ nflips,
+                           const int* __restrict__ M, int* __restrict__ bad) {
+    const int n = *nflips;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const long long r = flips[q];
+        int i, j, k;
+        decode(g, r, i, j, k);
+        if ((i + 1 < g.I && M[r + g.JK] == -1) || (i > 0 && M[r - g.JK] == -1) || (j + 1 < g.J && M[r + g.K] == -1) ||
+            (j > 0 && M[r - g.K] == -1) || (k + 1 < g.K && M[r + 1] == -1) || (k > 0 && M[r - 1] == -1))
+            *bad = 1;
     }
 }
 
@@ -204,49 +361,145 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
     // every field unchanged (frac -= 0, nothing consumed, nothing flips).
     if (n_active == 0 || (n_flux == 0 && n_flip == 0)) return LS_OK;
 
-    // active list sorted by wavefront level
     const int nlev = (g.I - 1) + 2 * (g.J - 1) + 3 * (g.K - 1) + 1;
-    if (c->dz_cap < n_active || !c->dz_list) {
-        if (c->dz_list) { cudaFree(c->dz_list); c->device_bytes -= sizeof(int) * (size_t)c->dz_cap; }
-        c->dz_list = nullptr;
-        LS_TRY(dalloc_t(c, &c->dz_list, (size_t)n_active));
-        c->dz_cap = n_active;
-    }
+    auto grow_cap = [&](int need) -> ls_status {
+        if (c->dz_cap < need || !c->dz_list) {
+            if (c->dz_list) { cudaFree(c->dz_list); c->device_bytes -= sizeof(int) * (size_t)c->dz_cap; }
+            c->dz_list = nullptr;
+            LS_TRY(dalloc_t(c, &c->dz_list, (size_t)need));
+            c->dz_cap = need;
+        }
+        return LS_OK;
+    };
+    LS_TRY(grow_cap(n_active));
     if (!c->dz_level_start) {
         LS_TRY(dalloc_t(c, &c->dz_level_start, (size_t)nlev + 1));
         LS_TRY(dalloc_t(c, &c->dz_count, (size_t)nlev + 1));
     }
-    LS_CUDA(c, cudaMemsetAsync(c->dz_count, 0, sizeof(int) * (nlev + 1), c->stream));
-    LS_LAUNCH(c, k_dz_hist<L>, grid, kBlock, 0, g, label, (const float*)c->frac, c->dz_count);
-    std::vector<int> hist(nlev + 1), start(nlev + 1);
-    LS_CUDA(c, cudaMemcpyAsync(hist.data(), c->dz_count, sizeof(int) * (nlev + 1),
-                               cudaMemcpyDeviceToHost, c->stream));
-    LS_CUDA(c, cudaStreamSynchronize(c->stream));
-    int acc = 0;
-    for (int w = 0; w <= nlev; ++w) {
-        start[w] = acc;
-        acc += hist[w];
-    }
-    if (acc != n_active) return set_error(c, LS_CUDA_ERROR, "dissolution: active list count mismatch");
-    LS_CUDA(c, cudaMemcpyAsync(c->dz_level_start, start.data(), sizeof(int) * (nlev + 1),
-                               cudaMemcpyHostToDevice, c->stream));
-    LS_CUDA(c, cudaMemsetAsync(c->dz_count, 0, sizeof(int) * (nlev + 1), c->stream));
-    LS_LAUNCH(c, k_dz_scatter<L>, grid, kBlock, 0, g, label, (const float*)c->frac,
-              (const int*)c->dz_level_start, c->dz_count, c->dz_list);
     int* d_leached = c->d_int + 8;
-    LS_CUDA(c, cudaMemsetAsync(d_leached, 0, sizeof(int), c->stream));
-    if (acid_pre)
-        LS_CUDA(c, cudaMemcpyAsync(acid_pre, c->acid, sizeof(double) * (size_t)g.N, cudaMemcpyDeviceToDevice,
-                                   c->stream));
+    int* d_flag = c->d_int + 12;
+    // the acid the sweeps start from: for the budget, and for undoing a sparse call
+    double* acid0 = acid_pre ? acid_pre : c->pr;
+    LS_CUDA(c, cudaMemcpyAsync(acid0, c->acid, sizeof(double) * (size_t)g.N, cudaMemcpyDeviceToDevice, c->stream));
     if (swept) *swept = true;
-    for (int step = 0; step < num_steps; ++step) {
-        for (int w = 0; w < nlev; ++w) {
-            int n = hist[w];
-            if (n == 0) continue;
-            int blocks = (n + 127) / 128;
-            LS_LAUNCH(c, k_dz_level<L>, blocks, 128, 0, g, dc, (const int*)c->dz_list + start[w], n,
-                      (L*)c->label, c->frac, c->acid, c->precip, c->conc, d_leached);
+    std::vector<int> hist(nlev + 1), start(nlev + 1);
+
+    // sweeps over a level-sorted list: hist[w] voxels of level w from start[w]
+    auto run_sweeps = [&](int* flips) -> ls_status {
+        LS_CUDA(c, cudaMemsetAsync(d_leached, 0, sizeof(int), c->stream));
+        for (int step = 0; step < num_steps; ++step) {
+            for (int w = 0; w < nlev; ++w) {
+                int n = hist[w];
+                if (n == 0) continue;
+                int blocks = (n + 127) / 128;
+                LS_LAUNCH(c, k_dz_level<L>, blocks, 128, 0, g, dc, (const int*)c->dz_list + start[w], n,
+                          (L*)c->label, c->frac, c->acid, c->precip, c->conc, d_leached, flips);
+            }
         }
+        return LS_OK;
+    };
+    auto prefix = [&](int total) -> ls_status {
+        int acc = 0;
+        for (int w = 0; w <= nlev; ++w) {
+            start[w] = acc;
+            acc += hist[w];
+        }
+        if (acc != total) return set_error(c, LS_CUDA_ERROR, "dissolution: schedule count mismatch");
+        return LS_OK;
+    };
+
+    // ---- sparse schedule (see above); LS_DZ_SPARSE=0 keeps the full wavefront schedule
+    static const bool sparse_on = [] {
+        const char* e = getenv("LS_DZ_SPARSE");
+        return !(e && e[0] == '0');
+    }();
+    bool done = false;
+    if (sparse_on) {
+        LS_TRY(wlist_reset(c));
+        int* M = c->wlist;
+        LS_LAUNCH(c, k_dz_seed<L>, grid, kBlock, 0, g, dc, label, (const double*)c->acid, (const float*)c->frac, M);
+        LS_LAUNCH(c, k_dz_grow, grid, kBlock, 0, g, M, 0, -3);
+        LS_LAUNCH(c, k_dz_grow, grid, kBlock, 0, g, M, -3, -4);
+        if (c->dz_sel_cap < n_active) {
+            void* old[6] = {c->dz_sel, c->dz_flips, c->dz_save_frac, c->dz_save_precip, c->dz_save_conc,
+                            c->dz_save_label};
+            for (void* q : old)
+                if (q) cudaFree(q);
+            c->device_bytes -= (size_t)c->dz_sel_cap * (4 + 4 + 4 + 8 + 8 + c->label_bytes);
+            c->dz_sel_cap = 0;
+            LS_TRY(dalloc_t(c, &c->dz_sel, (size_t)n_active));
+            LS_TRY(dalloc_t(c, &c->dz_flips, (size_t)n_active));
+            LS_TRY(dalloc_t(c, &c->dz_save_frac, (size_t)n_active));
+            LS_TRY(dalloc_t(c, &c->dz_save_precip, (size_t)n_active));
+            LS_TRY(dalloc_t(c, &c->dz_save_conc, (size_t)n_active));
+            LS_TRY(dalloc(c, &c->dz_save_label, (size_t)n_active * c->label_bytes));
+            c->dz_sel_cap = n_active;
+        }
+        LS_LAUNCH(c, k_dz_collect, grid, kBlock, 0, g, M, c->dz_sel, c->wcount);
+        unsigned int nsel_u = 0;
+        LS_CUDA(c, cudaMemcpyAsync(&nsel_u, c->wcount, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
+        LS_CUDA(c, cudaStreamSynchronize(c->stream));
+        const int nsel = (int)nsel_u;
+        if (nsel < 1 || nsel > n_active) return set_error(c, LS_CUDA_ERROR, "dissolution: bad sparse selection");
+        const int sgrid = std::min(grid, (nsel + kBlock - 1) / kBlock);
+        // levels: relax until a pass moves none (at most the wavefront's level count + 1)
+        int passes = 0;
+        for (;;) {
+            LS_CUDA(c, cudaMemsetAsync(d_flag, 0, sizeof(int), c->stream));
+            LS_LAUNCH(c, k_dz_relax, sgrid, kBlock, 0, g, M, (const int*)c->dz_sel, nsel, d_flag);
+            int moved = 0;
+            LS_CUDA(c, cudaMemcpyAsync(&moved, d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+            LS_CUDA(c, cudaStreamSynchronize(c->stream));
+            if (!moved) break;
+            if (++passes > nlev + 1) return set_error(c, LS_CUDA_ERROR, "dissolution: levels did not settle");
+        }
+        LS_CUDA(c, cudaMemsetAsync(c->dz_count, 0, sizeof(int) * (nlev + 1), c->stream));
+        LS_LAUNCH(c, k_dz_lhist, sgrid, kBlock, 0, (const int*)c->dz_sel, nsel, (const int*)M, c->dz_count);
+        LS_CUDA(c, cudaMemcpyAsync(hist.data(), c->dz_count, sizeof(int) * (nlev + 1), cudaMemcpyDeviceToHost,
+                                   c->stream));
+        LS_CUDA(c, cudaStreamSynchronize(c->stream));
+        LS_TRY(prefix(nsel));
+        LS_CUDA(c, cudaMemcpyAsync(c->dz_level_start, start.data(), sizeof(int) * (nlev + 1), cudaMemcpyHostToDevice,
+                                   c->stream));
+        LS_CUDA(c, cudaMemsetAsync(c->dz_count, 0, sizeof(int) * (nlev + 1), c->stream));
+        LS_LAUNCH(c, k_dz_lscatter, sgrid, kBlock, 0, (const int*)c->dz_sel, nsel, (const int*)M,
+                  (const int*)c->dz_level_start, c->dz_count, c->dz_list);
+        LS_LAUNCH(c, k_dz_save<L>, sgrid, kBlock, 0, (const int*)c->dz_sel, nsel, label, (const float*)c->frac,
+                  (const double*)c->precip, (const double*)c->conc, (L*)c->dz_save_label, c->dz_save_frac,
+                  c->dz_save_precip, c->dz_save_conc);
+        LS_TRY(run_sweeps(c->dz_flips));
+        LS_CUDA(c, cudaMemsetAsync(d_flag, 0, sizeof(int), c->stream));
+        LS_LAUNCH(c, k_dz_check, sgrid, kBlock, 0, g, (const int*)c->dz_flips, (const int*)d_leached, (const int*)M,
+                  d_flag);
+        int bad = 0;
+        LS_CUDA(c, cudaMemcpyAsync(&bad, d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        LS_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (!bad) {
+            done = true;
+        } else {
+            // undo the call, then the full schedule below
+            LS_LAUNCH(c, k_dz_restore<L>, sgrid, kBlock, 0, (const int*)c->dz_sel, nsel, (L*)c->label, c->frac,
+                      c->precip, c->conc, (const L*)c->dz_save_label, (const float*)c->dz_save_frac,
+                      (const double*)c->dz_save_precip, (const double*)c->dz_save_conc);
+            LS_CUDA(c, cudaMemcpyAsync(c->acid, acid0, sizeof(double) * (size_t)g.N, cudaMemcpyDeviceToDevice,
+                                       c->stream));
+            c->dz_fallbacks++;
+        }
+    }
+    if (!done) {
+        // full schedule: every active voxel, sorted by wavefront level
+        LS_CUDA(c, cudaMemsetAsync(c->dz_count, 0, sizeof(int) * (nlev + 1), c->stream));
+        LS_LAUNCH(c, k_dz_hist<L>, grid, kBlock, 0, g, label, (const float*)c->frac, c->dz_count);
+        LS_CUDA(c, cudaMemcpyAsync(hist.data(), c->dz_count, sizeof(int) * (nlev + 1), cudaMemcpyDeviceToHost,
+                                   c->stream));
+        LS_CUDA(c, cudaStreamSynchronize(c->stream));
+        LS_TRY(prefix(n_active));
+        LS_CUDA(c, cudaMemcpyAsync(c->dz_level_start, start.data(), sizeof(int) * (nlev + 1), cudaMemcpyHostToDevice,
+                                   c->stream));
+        LS_CUDA(c, cudaMemsetAsync(c->dz_count, 0, sizeof(int) * (nlev + 1), c->stream));
+        LS_LAUNCH(c, k_dz_scatter<L>, grid, kBlock, 0, g, label, (const float*)c->frac,
+                  (const int*)c->dz_level_start, c->dz_count, c->dz_list);
+        LS_TRY(run_sweeps(nullptr));
     }
     int h = 0;
     LS_CUDA(c, cudaMemcpyAsync(&h, d_leached, sizeof(int), cudaMemcpyDeviceToHost, c->stream));

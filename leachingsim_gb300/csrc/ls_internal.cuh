@@ -358,10 +358,20 @@ struct ls_ctx {
     int8_t* tkind;        // 1 identity row, 2 coupled row
 
     // dissolution
-    int* dz_list;         // active mineral voxels sorted by wavefront
+    int* dz_list;         // active mineral voxels sorted by wavefront (or by dependency level)
     int* dz_count;
     int* dz_level_start;
     int dz_cap;
+    // sparse schedule of the dissolution sweep: the voxels that can change (in any order),
+    // the voxels fully leached during a call, and the pre-sweep state of the scheduled voxels
+    int* dz_sel;
+    int* dz_flips;
+    float* dz_save_frac;
+    double* dz_save_precip;
+    double* dz_save_conc;
+    void* dz_save_label;
+    int dz_sel_cap;
+    long long dz_fallbacks;  // calls that fell back to the full wavefront sweep
 
     // reductions
     double* partials;     // kMaxPartials * 8 doubles

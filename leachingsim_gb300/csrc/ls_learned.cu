@@ -27,6 +27,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "ls_internal.cuh"
@@ -751,6 +752,8 @@ struct ls_lpnet {
 
 namespace {
 
+constexpr int kLpMaxDevices = 64;
+
 ls_status lp_fail(ls_lpnet* n, const char* what, cudaError_t e) {
     if (n) {
         char buf[256];
@@ -809,21 +812,29 @@ ls_status lp_conv_tc(ls_lpnet* n, LpDims d, const bf16* in, const bf16* w, const
     using S = ls::TcShape<CI, CO, ZT>;
     constexpr int smem = S::w_bytes + NB * S::a_bytes;
     static_assert(smem + 1024 <= 227 * 1024, "shared memory per CTA");
-    static bool attr = false;  // the dynamic shared-memory opt-in, once per instantiation
-    if (!attr) {
-        LP_CUDA(n, cudaFuncSetAttribute(ls::k_lp_conv_tc<CI, CO, ZT, NB, RELU, OutT>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        attr = true;
+    // the dynamic shared-memory opt-in and the occupancy, once per instantiation and device
+    // (a function attribute belongs to the device's context, so each device sets its own)
+    static std::mutex mu;
+    static int per_sm_dev[kLpMaxDevices] = {0};
+    int dev = 0;
+    LP_CUDA(n, cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kLpMaxDevices) return lp_fail(n, "k_lp_conv_tc: device index", cudaErrorInvalidDevice);
+    int per_sm = 0;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!per_sm_dev[dev]) {
+            LP_CUDA(n, cudaFuncSetAttribute(ls::k_lp_conv_tc<CI, CO, ZT, NB, RELU, OutT>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+            int occ = 0;
+            LP_CUDA(n, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ls::k_lp_conv_tc<CI, CO, ZT, NB, RELU, OutT>,
+                                                                     ls::kTcThreads, smem));
+            per_sm_dev[dev] = occ < 1 ? 1 : occ;
+        }
+        per_sm = per_sm_dev[dev];
     }
     const long long ntiles = (long long)((d.W + ls::kTcX - 1) / ls::kTcX) * ((d.H + ls::kTcY - 1) / ls::kTcY) *
                              ((d.D + ZT - 1) / ZT);
     // persistent CTAs: as many as fit the SMs at once; otherwise one tile per CTA
-    static int per_sm = 0;
-    if (!per_sm) {
-        LP_CUDA(n, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ls::k_lp_conv_tc<CI, CO, ZT, NB, RELU, OutT>,
-                                                                 ls::kTcThreads, smem));
-        if (per_sm < 1) per_sm = 1;
-    }
     const long long slots = TcPlanes<CI, CO>::persist ? (long long)per_sm * n->num_sms : ntiles;
     const int grid = (int)(ntiles < slots ? ntiles : slots);
     ls::k_lp_conv_tc<CI, CO, ZT, NB, RELU, OutT><<<grid, ls::kTcThreads, smem, n->stream>>>(d, in, w, bias, out);
@@ -971,10 +982,14 @@ namespace ls {
 
 // CTAs of k_lp_conv_tc whose bounded wait for their MMAs gave up since the last call (the
 // counter is cleared); synchronous
+// (LS_LPNET_SIMULATE_TIMEOUT=1 makes it report one, for tests of the host's response; no
+// device wait is shortened or skipped)
 int lpnet_tc_timeouts() {
     int v = 0, zero = 0;
     if (cudaMemcpyFromSymbol(&v, g_lp_tc_timeouts, sizeof(int)) != cudaSuccess) return 0;
     if (v) cudaMemcpyToSymbol(g_lp_tc_timeouts, &zero, sizeof(int));
+    const char* sim = getenv("LS_LPNET_SIMULATE_TIMEOUT");
+    if (sim && sim[0] == '1') v += 1;
     return v;
 }
 
@@ -1141,8 +1156,15 @@ ls_status ls_lpnet_forward(ls_lpnet* n, const float* c0, const float* c1, const 
     LP_LAUNCH(n, ls::k_lp_out, lp_grid(n, N, 256), 256, N, (const float*)n->y, out);
     LP_CUDA(n, cudaStreamSynchronize(n->stream));
     if (ls::lpnet_tc_timeouts()) {
-        n->err = "tensor-core convolution: a wait for the MMAs gave up";
-        return LS_TIMEOUT;
+        // A tcgen05 wait gave up: the output is not valid, and the state a timed-out CTA left
+        // (tensor memory, shared memory, MMAs still in flight) is not trusted again. This network
+        // runs the mma.sync kernels from now on; the pass is recomputed with them.
+        n->use_tc = 0;
+        n->err = "tensor-core convolution: a wait for the MMAs gave up; recomputed with mma.sync";
+        LS_TRY(lp_forward(n, c0, c1, c2));
+        LP_LAUNCH(n, ls::k_lp_out, lp_grid(n, N, 256), 256, N, (const float*)n->y, out);
+        LP_CUDA(n, cudaStreamSynchronize(n->stream));
+        return LS_STAGNATED_FALLBACK_USED;
     }
     return LS_OK;
 }
@@ -1169,6 +1191,7 @@ ls_status ls_lpnet_train_step(ls_lpnet* n, const float* c0, const float* c1, con
     LP_CUDA(n, cudaMemcpyAsync(part.data(), n->partials, sizeof(double) * nb, cudaMemcpyDeviceToHost, n->stream));
     LP_CUDA(n, cudaStreamSynchronize(n->stream));
     if (ls::lpnet_tc_timeouts()) {
+        n->use_tc = 0;  // as in ls_lpnet_forward: no further tcgen05 launches on this network
         n->err = "tensor-core convolution: a wait for the MMAs gave up";
         return LS_TIMEOUT;
     }

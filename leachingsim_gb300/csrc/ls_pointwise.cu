@@ -639,7 +639,10 @@ ls_status budget_run(ls_ctx* c, const double* acid_pre, ls_budget* b) {
 // loaded with the library and held on every GPU that loads it until the process exits.
 // The first call on a device looks up the array's device address (cudaGetSymbolAddress,
 // with that device current) and caches it, so that first call should come before any
-// stream capture. Every call uses the same array: two calls that overlap on the GPU (on
+// stream capture; later calls check that the cached address is still device memory of that
+// device (it is not after a reset of the device's context) and look it up again if not.
+// Each call waits for its own result on the host (it reads the largest rate back to choose
+// the sub-step count). Every call uses the same array: two calls that overlap on the GPU (on
 // different streams or host threads) race on it. Each call writes every slot it later
 // reads (no accumulation), so nothing has to be cleared; the previous call's contents stay
 // until overwritten.
@@ -698,6 +701,17 @@ static double* noalloc_scratch_address(int device, cudaError_t* err) {
         return nullptr;
     }
     std::lock_guard<std::mutex> lock(mu);
+    if (addr[device]) {
+        // the address is cached per device; a reset of the device's context reloads the module,
+        // so check that the cached address is still device memory of this device, and look it
+        // up again otherwise
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, addr[device]) != cudaSuccess || at.type != cudaMemoryTypeDevice ||
+            at.device != device) {
+            cudaGetLastError();  // the failed query leaves its own error pending
+            addr[device] = nullptr;
+        }
+    }
     if (!addr[device]) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_sat_scratch);
@@ -761,10 +775,12 @@ extern "C" ls_status ls_saturation_noalloc(int I, int J, int K, int label_bytes,
         k_noalloc_sat_rate<uint16_t><<<nblocks, kBlock, 0, s>>>(g, dd, evaporative_flux, (const uint16_t*)label,
                                                                flux_x, flux_y, flux_z, scratch);
     k_noalloc_sat_final<<<1, kFinalizeThreads, 0, s>>>(nblocks, scratch);
+    // launch errors of these two launches, read without clearing anything else pending
+    ce = cudaPeekAtLastError();
+    if (ce != cudaSuccess) return noalloc_fail(LS_CUDA_ERROR, err, err_len, cudaGetErrorString(ce));
     double max_div_q = 0.0;
     ce = cudaMemcpyAsync(&max_div_q, scratch + kNoAllocSlots, sizeof(double), cudaMemcpyDeviceToHost, s);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
-    if (ce == cudaSuccess) ce = cudaGetLastError();
     if (ce != cudaSuccess) return noalloc_fail(LS_CUDA_ERROR, err, err_len, cudaGetErrorString(ce));
     // sub-step count, src/Simulation.cpp:1740-1767
     const double max_dsat = 0.1;
@@ -789,7 +805,7 @@ extern "C" ls_status ls_saturation_noalloc(int I, int J, int K, int label_bytes,
     else
         k_sat_update<uint16_t><<<grid2, kBlock, 0, s>>>(g, dd, evaporative_flux, dt_sub_over_phi, num_steps,
                                                         (const uint16_t*)label, flux_x, flux_y, flux_z, saturation);
-    ce = cudaGetLastError();
+    ce = cudaPeekAtLastError();
     if (ce != cudaSuccess) return noalloc_fail(LS_CUDA_ERROR, err, err_len, cudaGetErrorString(ce));
     return LS_OK;
 }

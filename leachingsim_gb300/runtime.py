@@ -73,6 +73,7 @@ SYMBOLS = {
     "ls_pressure_solve_start": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.POINTER(LsSolveInfo)]),
     "ls_pressure_set_precond_weights": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
     "ls_pressure_fallbacks": (C.c_longlong, [C.c_void_p]),
+    "ls_dissolve_fallbacks": (C.c_longlong, [C.c_void_p]),
     "ls_pressure_mg_level": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p]),
     "ls_field_pool2": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -274,9 +275,10 @@ class LPNet:
         except Exception:
             pass
 
-    def _check(self, st):
-        if st != 0:
+    def _check(self, st, allowed=(0,)):
+        if st not in allowed:
             raise LsError(st, (load().ls_lpnet_last_error(self.h) or b"").decode())
+        return st
 
     def _dev(self, a):
         import torch
@@ -309,8 +311,9 @@ class LPNet:
         t = [self._dev(c) for c in (c0, c1, c2)]
         out = torch.empty(self.shape, dtype=torch.float32, device="cuda")
         torch.cuda.synchronize()
-        self._check(load().ls_lpnet_forward(self.h, *[C.c_void_p(x.data_ptr()) for x in t],
-                                            C.c_void_p(out.data_ptr())))
+        # status 2: a tensor-core wait gave up and the pass was recomputed with mma.sync
+        self.last_status = self._check(load().ls_lpnet_forward(self.h, *[C.c_void_p(x.data_ptr()) for x in t],
+                                                               C.c_void_p(out.data_ptr())), (0, 2))
         return out
 
     def train_step(self, c0, c1, c2, target, mask, lr=1e-3, update=True):
@@ -451,6 +454,10 @@ class Context:
     def pressure_fallbacks(self):
         """Learned pressure solves on this context that fell back to the plain cycle."""
         return int(load().ls_pressure_fallbacks(self.h))
+
+    def dissolve_fallbacks(self):
+        """Dissolution calls on this context redone with the full wavefront schedule."""
+        return int(load().ls_dissolve_fallbacks(self.h))
 
     def mg_level(self, level):
         """Multigrid level `level` of the last FP32-inner pressure solve: dict with its shape

@@ -177,3 +177,32 @@ def test_gpu_tcgen05_and_mma_sync_paths_agree(monkeypatch):
         net.close()
     assert _rel(outs["tc"], outs["mma"]) < 5e-3
     assert _rel(outs["auto"], outs["mma"]) < 5e-3
+
+
+@pytest.mark.gpu
+def test_gpu_tcgen05_timeout_falls_back_to_mma_sync(monkeypatch):
+    """A tcgen05 wait that gives up (the library's timeout counter, here set by the host-side
+    LS_LPNET_SIMULATE_TIMEOUT switch; nothing on the GPU waits less or is skipped) makes the
+    network discard the pass, switch to its mma.sync kernels for good and recompute: the
+    forward returns the fallback status with the mma.sync result, and later passes (the
+    switch off again) still match it."""
+    from leachingsim_gb300.runtime import LPNet, lpnet_flatten
+    shape = (16, 24, 24)
+    p, mask, c1, c2, _ = _case(shape, 7)
+    _path(monkeypatch, "mma")
+    ref_net = LPNet(shape)
+    ref_net.set_params(lpnet_flatten(p))
+    ref = ref_net.forward(mask, c1, c2).cpu().numpy()
+    ref_net.close()
+    _path(monkeypatch, "tc")
+    net = LPNet(shape)
+    net.set_params(lpnet_flatten(p))
+    monkeypatch.setenv("LS_LPNET_SIMULATE_TIMEOUT", "1")
+    out = net.forward(mask, c1, c2).cpu().numpy()
+    assert net.last_status == 2
+    monkeypatch.delenv("LS_LPNET_SIMULATE_TIMEOUT")
+    again = net.forward(mask, c1, c2).cpu().numpy()
+    assert net.last_status == 0
+    net.close()
+    np.testing.assert_array_equal(out, ref)
+    np.testing.assert_array_equal(again, ref)
