@@ -117,15 +117,12 @@ __global__ void k_dz_scatter(Grid g, const L* __restrict__ label, const float* _
     }
 }
 
-// One wavefront level of one sub-step (the body of src/Simulation.cpp:475-603).
+// One voxel of one sub-step (the body of src/Simulation.cpp:475-603).
 template <typename L>
-__global__ void k_dz_level(Grid g, DzConst dc, const int* __restrict__ list, int count,
-                           L* __restrict__ label, float* __restrict__ frac,
-                           double* __restrict__ acid, double* __restrict__ precip,
-                           double* __restrict__ conc, int* __restrict__ leached, int* __restrict__ flips) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= count) return;
-    const long long r = list[t];
+__device__ __forceinline__ void dz_voxel(const Grid& g, const DzConst& dc, long long r, L* __restrict__ label,
+                                         float* __restrict__ frac, double* __restrict__ acid,
+                                         double* __restrict__ precip, double* __restrict__ conc,
+                                         int* __restrict__ leached, int* __restrict__ flips) {
     if (!((int)label[r] >= kSulphide && frac[r] > 0.0f)) return;
     int i, j, k;
     decode(g, r, i, j, k);
@@ -136,10 +133,8 @@ __global__ void k_dz_level(Grid g, DzConst dc, const int* __restrict__ list, int
     for (int d = 0; d < 6; ++d) f[d] = dz_surface_flux(g, dc, label, acid, val[d], nbs[d]);
     double flux_sum = f[0] + f[1] + f[2] + f[3] + f[4] + f[5];
     double area_per_face = dc.dx * dc.dx;
-    double voxel_volume = dc.dx * dc.dx * dc.dx;
     double mass_loss = flux_sum * area_per_face * dc.dt_sub;
     double fractional_loss = dc.vol.div(mass_loss);
-    (void)voxel_volume;
     float fr = (float)((double)frac[r] - (fractional_loss * dc.time_scalar));
     frac[r] = fr;
     if (flux_sum > 0.0) {
@@ -159,22 +154,46 @@ __global__ void k_dz_level(Grid g, DzConst dc, const int* __restrict__ list, int
     }
 }
 
+// Every sub-step of a call in one CTA: the wavefront levels in order, the voxels of a level
+// spread over the threads, a block barrier between levels (it makes a level's stores visible
+// to the next level's loads). The loop is bounded (sub-steps x levels) and waits on nothing
+// outside the CTA. hist[w] / start[w]: voxels of level w in list.
+constexpr int kDzThreads = 1024;
+template <typename L>
+__global__ void __launch_bounds__(kDzThreads) k_dz_sweep(Grid g, DzConst dc, int num_steps, int nlev,
+                                                          const int* __restrict__ list,
+                                                          const int* __restrict__ hist,
+                                                          const int* __restrict__ start, L* __restrict__ label,
+                                                          float* __restrict__ frac, double* __restrict__ acid,
+                                                          double* __restrict__ precip, double* __restrict__ conc,
+                                                          int* __restrict__ leached, int* __restrict__ flips) {
+    for (int step = 0; step < num_steps; ++step) {
+        for (int w = 0; w < nlev; ++w) {
+            const int n = __ldg(hist + w);
+            if (n == 0) continue;  // uniform across the block
+            const int* lw = list + __ldg(start + w);
+            for (int q = threadIdx.x; q < n; q += blockDim.x)
+                dz_voxel<L>(g, dc, (long long)__ldg(lw + q), label, frac, acid, precip, conc, leached, flips);
+            __syncthreads();
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Sparse schedule. A voxel changes something in a sub-step only when a Pore or Rock neighbour
 // holds nonzero acid (flux_sum != 0) or its frac is at the threshold. During a call acid
 // changes only by consumption and a label only by a leach (Sulphide -> Pore), which can make
 // the leached voxel's own acid visible to its neighbours. The sweeps therefore visit S: the
-// voxels live at the start and the active voxels within two face steps of them, ordered by
-// their dependency level within S (level(v) = 1 + the largest level of the voxels of S within
-// Manhattan distance 2 that precede v in the reference's loop order, k outer, j, i inner), so
-// every pair that can interact runs in the sequential order; voxels of one level are
-// independent. If a voxel leached during the call has an active neighbour outside S, that
+// voxels live at the start and the active voxels within two face steps of them, in the
+// wavefront order (a voxel outside S changes nothing, so dropping it leaves every other
+// voxel's inputs as in the full sweep). If a voxel leached during the call has an active
+// neighbour outside S, that
 // neighbour could have become live: the call is undone (acid from its copy; frac, label,
 // precip and conc of S from theirs) and redone with the full wavefront schedule, so the
 // result is always the sequential sweep's.
 //
-// Dense map M over the N voxels: -2 not active, -1 active outside S, >= 0 in S (its level);
-// during the selection -3 / -4 mark the voxels one / two face steps from a live one.
+// Dense map M over the N voxels: -2 not active, -1 active outside S, 0 in S; during the
+// selection -3 / -4 mark the voxels one / two face steps from a live one.
 
 template <typename L>
 __global__ void __launch_bounds__(kBlock) k_dz_seed(Grid g, DzConst dc, const L* __restrict__ label,
@@ -213,7 +232,7 @@ __global__ void __launch_bounds__(kBlock) k_dz_grow(Grid g, int* __restrict__ M,
     }
 }
 
-// S as a list (any order), every member at level 0
+// S as a list (any order), its members marked 0
 __global__ void __launch_bounds__(kBlock) k_dz_collect(Grid g, int* __restrict__ M, int* __restrict__ list,
                                                        unsigned int* __restrict__ count) {
     // block-uniform trip count (block_append is called by every thread of the block)
@@ -229,45 +248,23 @@ __global__ void __launch_bounds__(kBlock) k_dz_collect(Grid g, int* __restrict__
     }
 }
 
-// One relaxation pass of the levels (values only grow and stay below the longest-path
-// level, so passes in place converge to it; *changed tells whether this pass moved any).
-__global__ void __launch_bounds__(kBlock) k_dz_relax(Grid g, int* __restrict__ M, const int* __restrict__ list,
-                                                     int n, int* __restrict__ changed) {
-    // the 12 offsets (di, dj, dk) within Manhattan distance 2 that precede in (k, j, i) order
-    const int od[12][3] = {{0, 0, -1}, {0, -1, 0}, {-1, 0, 0}, {0, 0, -2}, {0, -2, 0}, {-2, 0, 0},
-                           {1, 0, -1}, {-1, 0, -1}, {0, 1, -1}, {0, -1, -1}, {1, -1, 0}, {-1, -1, 0}};
-    bool moved = false;
+// wavefront levels of the listed voxels: histogram, then the list sorted by level
+__global__ void k_dz_whist(Grid g, const int* __restrict__ list, int n, int* __restrict__ hist) {
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-        const long long v = list[q];
         int i, j, k;
-        decode(g, v, i, j, k);
-        int m = 0;
-#pragma unroll
-        for (int o = 0; o < 12; ++o) {
-            const int ni = i + od[o][0], nj = j + od[o][1], nk = k + od[o][2];
-            if (ni < 0 || ni >= g.I || nj < 0 || nj >= g.J || nk < 0 || nk >= g.K) continue;
-            const int lu = M[(long long)nk + (long long)g.K * ((long long)nj + (long long)g.J * ni)];
-            if (lu >= 0 && lu + 1 > m) m = lu + 1;
-        }
-        if (m > M[v]) {
-            M[v] = m;
-            moved = true;
-        }
+        decode(g, list[q], i, j, k);
+        atomicAdd(&hist[dz_level(i, j, k)], 1);
     }
-    if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) *changed = 1;
 }
 
-__global__ void k_dz_lhist(const int* __restrict__ list, int n, const int* __restrict__ M, int* __restrict__ hist) {
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
-        atomicAdd(&hist[M[list[q]]], 1);
-}
-
-__global__ void k_dz_lscatter(const int* __restrict__ list, int n, const int* __restrict__ M,
-                              const int* __restrict__ start, int* __restrict__ cursor, int* __restrict__ out) {
+__global__ void k_dz_wscatter(Grid g, const int* __restrict__ list, int n, const int* __restrict__ start,
+                              int* __restrict__ cursor, int* __restrict__ out) {
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
         const int v = list[q];
-        const int l = M[v];
-        out[start[l] + atomicAdd(&cursor[l], 1)] = v;
+        int i, j, k;
+        decode(g, v, i, j, k);
+        const int w = dz_level(i, j, k);
+        out[start[w] + atomicAdd(&cursor[w], 1)] = v;
     }
 }
 
@@ -384,18 +381,13 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
     if (swept) *swept = true;
     std::vector<int> hist(nlev + 1), start(nlev + 1);
 
-    // sweeps over a level-sorted list: hist[w] voxels of level w from start[w]
+    // every sub-step over the level-sorted list (hist[w] voxels of level w from start[w]; on
+    // the device: dz_count and dz_level_start) in one CTA
     auto run_sweeps = [&](int* flips) -> ls_status {
         LS_CUDA(c, cudaMemsetAsync(d_leached, 0, sizeof(int), c->stream));
-        for (int step = 0; step < num_steps; ++step) {
-            for (int w = 0; w < nlev; ++w) {
-                int n = hist[w];
-                if (n == 0) continue;
-                int blocks = (n + 127) / 128;
-                LS_LAUNCH(c, k_dz_level<L>, blocks, 128, 0, g, dc, (const int*)c->dz_list + start[w], n,
-                          (L*)c->label, c->frac, c->acid, c->precip, c->conc, d_leached, flips);
-            }
-        }
+        LS_LAUNCH(c, k_dz_sweep<L>, 1, kDzThreads, 0, g, dc, num_steps, nlev, (const int*)c->dz_list,
+                  (const int*)c->dz_count, (const int*)c->dz_level_start, (L*)c->label, c->frac, c->acid,
+                  c->precip, c->conc, d_leached, flips);
         return LS_OK;
     };
     auto prefix = [&](int total) -> ls_status {
@@ -442,19 +434,9 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
         const int nsel = (int)nsel_u;
         if (nsel < 1 || nsel > n_active) return set_error(c, LS_CUDA_ERROR, "dissolution: bad sparse selection");
         const int sgrid = std::min(grid, (nsel + kBlock - 1) / kBlock);
-        // levels: relax until a pass moves none (at most the wavefront's level count + 1)
-        int passes = 0;
-        for (;;) {
-            LS_CUDA(c, cudaMemsetAsync(d_flag, 0, sizeof(int), c->stream));
-            LS_LAUNCH(c, k_dz_relax, sgrid, kBlock, 0, g, M, (const int*)c->dz_sel, nsel, d_flag);
-            int moved = 0;
-            LS_CUDA(c, cudaMemcpyAsync(&moved, d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-            LS_CUDA(c, cudaStreamSynchronize(c->stream));
-            if (!moved) break;
-            if (++passes > nlev + 1) return set_error(c, LS_CUDA_ERROR, "dissolution: levels did not settle");
-        }
+        // S sorted by wavefront level
         LS_CUDA(c, cudaMemsetAsync(c->dz_count, 0, sizeof(int) * (nlev + 1), c->stream));
-        LS_LAUNCH(c, k_dz_lhist, sgrid, kBlock, 0, (const int*)c->dz_sel, nsel, (const int*)M, c->dz_count);
+        LS_LAUNCH(c, k_dz_whist, sgrid, kBlock, 0, g, (const int*)c->dz_sel, nsel, c->dz_count);
         LS_CUDA(c, cudaMemcpyAsync(hist.data(), c->dz_count, sizeof(int) * (nlev + 1), cudaMemcpyDeviceToHost,
                                    c->stream));
         LS_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -462,8 +444,8 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
         LS_CUDA(c, cudaMemcpyAsync(c->dz_level_start, start.data(), sizeof(int) * (nlev + 1), cudaMemcpyHostToDevice,
                                    c->stream));
         LS_CUDA(c, cudaMemsetAsync(c->dz_count, 0, sizeof(int) * (nlev + 1), c->stream));
-        LS_LAUNCH(c, k_dz_lscatter, sgrid, kBlock, 0, (const int*)c->dz_sel, nsel, (const int*)M,
-                  (const int*)c->dz_level_start, c->dz_count, c->dz_list);
+        LS_LAUNCH(c, k_dz_wscatter, sgrid, kBlock, 0, g, (const int*)c->dz_sel, nsel, (const int*)c->dz_level_start,
+                  c->dz_count, c->dz_list);
         LS_LAUNCH(c, k_dz_save<L>, sgrid, kBlock, 0, (const int*)c->dz_sel, nsel, label, (const float*)c->frac,
                   (const double*)c->precip, (const double*)c->conc, (L*)c->dz_save_label, c->dz_save_frac,
                   c->dz_save_precip, c->dz_save_conc);
