@@ -154,28 +154,51 @@ __device__ __forceinline__ void dz_voxel(const Grid& g, const DzConst& dc, long 
     }
 }
 
-// Every sub-step of a call in one CTA: the wavefront levels in order, the voxels of a level
-// spread over the threads, a block barrier between levels (it makes a level's stores visible
-// to the next level's loads). The loop is bounded (sub-steps x levels) and waits on nothing
-// outside the CTA. hist[w] / start[w]: voxels of level w in list.
-constexpr int kDzThreads = 1024;
+// Skewed wavefront over the sub-steps. A voxel's update reads and writes only itself and its
+// six face neighbours, so two updates can interact only within Manhattan distance 2, where
+// the wavefront index w = i + 2j + 3k differs by at most 6. Level l = w + kDzSkew * s (s the
+// sub-step) orders every interacting pair of updates as the sequential sweeps do: in one
+// sub-step by w; across sub-steps, (v, s) before (u, s + 1) for every u within distance 2,
+// and (u, s) before (v, s + 1) even when u comes after v. Updates of one level never
+// interact, so a level runs in parallel, and a call takes nlev + kDzSkew (num_steps - 1)
+// levels instead of nlev x num_steps.
+constexpr int kDzSkew = 7;
+
+// The (sub-step, voxel) updates of one level are spread over all threads: the level holds
+// the slices w = level - kDzSkew s of the sub-steps s it covers; one thread per update.
 template <typename L>
-__global__ void __launch_bounds__(kDzThreads) k_dz_sweep(Grid g, DzConst dc, int num_steps, int nlev,
-                                                          const int* __restrict__ list,
-                                                          const int* __restrict__ hist,
-                                                          const int* __restrict__ start, L* __restrict__ label,
-                                                          float* __restrict__ frac, double* __restrict__ acid,
-                                                          double* __restrict__ precip, double* __restrict__ conc,
-                                                          int* __restrict__ leached, int* __restrict__ flips) {
-    for (int step = 0; step < num_steps; ++step) {
-        for (int w = 0; w < nlev; ++w) {
-            const int n = __ldg(hist + w);
-            if (n == 0) continue;  // uniform across the block
-            const int* lw = list + __ldg(start + w);
-            for (int q = threadIdx.x; q < n; q += blockDim.x)
-                dz_voxel<L>(g, dc, (long long)__ldg(lw + q), label, frac, acid, precip, conc, leached, flips);
-            __syncthreads();
+__global__ void __launch_bounds__(kBlock) k_dz_skew(Grid g, DzConst dc, int level, int num_steps, int nlev,
+                                                    const int* __restrict__ list, const int* __restrict__ hist,
+                                                    const int* __restrict__ start, L* __restrict__ label,
+                                                    float* __restrict__ frac, double* __restrict__ acid,
+                                                    double* __restrict__ precip, double* __restrict__ conc,
+                                                    int* __restrict__ leached, int* __restrict__ flips) {
+    const int s_lo = level >= nlev ? (level - nlev) / kDzSkew + 1 : 0;
+    const int s_hi = min(num_steps - 1, level / kDzSkew);
+    const int ns = s_hi - s_lo + 1;  // slices of this level, <= ceil(nlev / kDzSkew)
+    // running totals of the slices' sizes, in shared memory (<= kDzSliceCap slices per pass)
+    constexpr int kDzSliceCap = 512;
+    __shared__ int cum[kDzSliceCap + 1];
+    for (int s0 = 0; s0 < ns; s0 += kDzSliceCap) {
+        const int m = min(kDzSliceCap, ns - s0);
+        if (threadIdx.x == 0) {
+            int acc = 0;
+            for (int t = 0; t < m; ++t) {
+                cum[t] = acc;
+                acc += __ldg(hist + level - kDzSkew * (s_lo + s0 + t));
+            }
+            cum[m] = acc;
         }
+        __syncthreads();
+        const int total = cum[m];
+        for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+            int t = 0;
+            while (cum[t + 1] <= idx) ++t;
+            const int w = level - kDzSkew * (s_lo + s0 + t);
+            const long long r = __ldg(list + __ldg(start + w) + (idx - cum[t]));
+            dz_voxel<L>(g, dc, r, label, frac, acid, precip, conc, leached, flips);
+        }
+        __syncthreads();
     }
 }
 
@@ -381,13 +404,24 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
     if (swept) *swept = true;
     std::vector<int> hist(nlev + 1), start(nlev + 1);
 
-    // every sub-step over the level-sorted list (hist[w] voxels of level w from start[w]; on
-    // the device: dz_count and dz_level_start) in one CTA
+    // every sub-step over the wavefront-sorted list (hist[w] voxels of level w from start[w];
+    // on the device: dz_count and dz_level_start) by the skewed levels
     auto run_sweeps = [&](int* flips) -> ls_status {
         LS_CUDA(c, cudaMemsetAsync(d_leached, 0, sizeof(int), c->stream));
-        LS_LAUNCH(c, k_dz_sweep<L>, 1, kDzThreads, 0, g, dc, num_steps, nlev, (const int*)c->dz_list,
-                  (const int*)c->dz_count, (const int*)c->dz_level_start, (L*)c->label, c->frac, c->acid,
-                  c->precip, c->conc, d_leached, flips);
+        const int nsk = nlev + kDzSkew * (num_steps - 1);
+        for (int l = 0; l < nsk; ++l) {
+            long long total = 0;
+            for (int s = 0; s < num_steps; ++s) {
+                const int w = l - kDzSkew * s;
+                if (w < 0) break;
+                if (w < nlev) total += hist[w];
+            }
+            if (total == 0) continue;
+            const int blocks = (int)std::min<long long>((total + kBlock - 1) / kBlock, (long long)c->num_sms * 8);
+            LS_LAUNCH(c, k_dz_skew<L>, blocks, kBlock, 0, g, dc, l, num_steps, nlev, (const int*)c->dz_list,
+                      (const int*)c->dz_count, (const int*)c->dz_level_start, (L*)c->label, c->frac, c->acid,
+                      c->precip, c->conc, d_leached, flips);
+        }
         return LS_OK;
     };
     auto prefix = [&](int total) -> ls_status {
