@@ -729,34 +729,50 @@ MIX_SHAPE = (512, 512, 512)
 MIX_STEPS = 10
 
 
+MIX_CONTRAST = 1e4  # permeability of the fracture voxels over that of the matrix's pores
+
+
 def mixed_geometry(shape):
     """uint16 labels of the mixed-precision workload: the grey-level random field (corr 6)
     with 4 planar fractures of 1-3 voxel aperture (grey 0), classified on the GPU at the 20% /
     88% grey quantiles into Pore / Rock / Sulphide (the fractures fall below the lowest
-    threshold: Pore), Air inlet planes i = 0, 1 as the pressure driver."""
+    threshold: Pore). The fracture voxels get the intrinsic-permeability multiplier 1e4
+    (fracture / matrix contrast 1e4); the flow-through boundary drives the pressure."""
     from leachingsim_gb300 import runtime as rt
     from leachingsim_gb300.geometry import grey_levels
     grey = grey_levels(shape, corr_len=6.0, seed=0, n_fractures=4)
     sub = grey[::4, ::4, ::4].ravel()
     thr = [int(np.quantile(sub, 0.2)), int(np.quantile(sub, 0.88))]
     lab = rt.geom_classify(grey, thr, [2, 3, 4], 2)
-    lab[0:2] = 1
-    return lab, thr
+    kmult = np.where(grey == 0, MIX_CONTRAST, 1.0).astype(np.float32)
+    return lab, kmult, thr
 
 
-MIX_FIELDS = ("pressure", "flux_x", "flux_y", "flux_z", "conc", "precipitate", "label")
+MIX_FIELDS = ("pressure", "flux_x", "flux_y", "flux_z", "conc", "acid", "precipitate", "label")
 
 
-def mixed_run(lab, p, steps):
-    """steps accepted time steps from a fresh state; returns wall ms per step (first step
-    and the rest), the fields, the context's device bytes and the solver iterations."""
+def mixed_params(fp64):
+    from leachingsim_gb300._abi import BC_FLOW_I, PRESS_FP64, PRESS_MIXED, default_params
+    base = dict(c_sat=1.0, D=1.0, kreac=1.0, bc_mode=BC_FLOW_I, p_inlet=FLOW_PIN, p_outlet=FLOW_POUT,
+                acid_inlet=FLOW_ACID)
+    if fp64:
+        return default_params(press_solver=PRESS_FP64, press_rtol=1e-12, conc_rtol=1e-12, sat_rtol=1e-12, **base)
+    return default_params(press_solver=PRESS_MIXED, press_rtol=PRESS_RTOL, conc_rtol=CONC_RTOL, sat_rtol=CONC_RTOL,
+                          **base)
+
+
+def mixed_run(lab, kmult, p, steps, keep=()):
+    """steps accepted time steps from a fresh state; returns wall ms per step, the fields
+    after the first step, after each step in `keep` and after the last, the context's device
+    bytes and the solver iterations."""
     import torch
     from leachingsim_gb300.runtime import Context
     ctx = Context(lab.shape, label_bytes=2, params=p)
     ctx.upload("label", lab)
+    ctx.upload("kmult", kmult)
     ctx.init_all()
     ctx.synchronize()
-    times, iters = [], []
+    times, iters, kept = [], [], {}
     t, n = 0.0, 0
     first = None
     for _ in range(steps):
@@ -764,47 +780,65 @@ def mixed_run(lab, p, steps):
         t, n, info = run_steps(ctx, t, n, 1, DT)
         ctx.synchronize()
         times.append((time.perf_counter() - w0) * 1e3)
-        iters.append((info[0]["pressure"]["iterations"], info[0]["conc"]["iterations"]))
+        iters.append((info[0]["pressure"]["iterations"], info[0]["conc"]["iterations"], info[0]["leached"]))
         if first is None:  # after the first (cold) step, outside the timed step
-            first = {f: ctx.download(f, padded=f != "label") for f in MIX_FIELDS}
-    out = {f: ctx.download(f, padded=f != "label") for f in MIX_FIELDS}
+            first = {f: ctx.download(f, padded=f != "label").copy() for f in MIX_FIELDS}
+        if n in keep:
+            kept[n] = {f: ctx.download(f, padded=f != "label").copy() for f in MIX_FIELDS}
+    out = {f: ctx.download(f, padded=f != "label").copy() for f in MIX_FIELDS}
     mem = ctx.device_bytes()
     ctx.close()
     torch.cuda.synchronize()
-    return times, (first, out), mem, iters
+    return times, (first, out), mem, iters, kept
 
 
 def mixed_arm(args):
     import torch
-    from leachingsim_gb300._abi import PRESS_FP64, PRESS_MIXED, default_params
     shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else MIX_SHAPE
     steps = MIX_STEPS  # ten steps per precision (the first a cold step)
     t0 = time.time()
-    lab, thr = mixed_geometry(shape)
-    log(f"mixed: geometry {shape} in {time.time() - t0:.1f}s, labels {np.bincount(lab.ravel()).tolist()}")
-    base = dict(c_sat=1.0, D=1.0, kreac=1.0)
-    pm = default_params(press_solver=PRESS_MIXED, press_rtol=PRESS_RTOL, conc_rtol=CONC_RTOL,
-                        sat_rtol=CONC_RTOL, **base)
-    pf = default_params(press_solver=PRESS_FP64, press_rtol=1e-12, conc_rtol=1e-12, sat_rtol=1e-12, **base)
+    lab, kmult, thr = mixed_geometry(shape)
+    log(f"mixed: geometry {shape} in {time.time() - t0:.1f}s, labels {np.bincount(lab.ravel()).tolist()}, "
+        f"fracture voxels {int((kmult > 1).sum())}")
+    cpu_steps = max(0, args.mixed_cpu_steps)
     with ClockSampler(0) as clk:
-        tm, fm, mem, im = mixed_run(lab, pm, steps)
-    tf, ff, _, iff = mixed_run(lab, pf, steps)
-
-    def rel(a, b):
-        a = np.asarray(a, np.float64).ravel()
-        b = np.asarray(b, np.float64).ravel()
-        d = np.linalg.norm(b)
-        return float(np.linalg.norm(a - b) / d) if d > 0 else float(np.linalg.norm(a - b))
+        tm, fm, mem, im, km = mixed_run(lab, kmult, mixed_params(False), steps, keep=(cpu_steps,))
+    tf, ff, _, iff, _ = mixed_run(lab, kmult, mixed_params(True), steps)
 
     vel = lambda f: np.concatenate([f[k].ravel() for k in ("flux_x", "flux_y", "flux_z")])  # noqa: E731
 
     def errors(a, b):
-        return {"pressure": rel(a["pressure"], b["pressure"]), "velocity": rel(vel(a), vel(b)),
-                "conc": rel(a["conc"], b["conc"]), "precipitate": rel(a["precipitate"], b["precipitate"]),
-                "label_mismatches": int(np.count_nonzero(a["label"] != b["label"])),
-                "precipitated_voxels": int(np.count_nonzero(b["label"] == 5))}
+        return {"pressure": rel_l2(a["pressure"], b["pressure"]), "velocity": rel_l2(vel(a), vel(b)),
+                "conc": rel_l2(a["conc"], b["conc"]), "acid": rel_l2(a["acid"], b["acid"]),
+                "precipitate_abs": float(np.abs(a["precipitate"] - b["precipitate"]).max()),
+                "label_mismatches": int(np.count_nonzero(a["label"] != b["label"]))}
 
     err = {"first_step": errors(fm[0], ff[0]), "last_step": errors(fm[1], ff[1])}
+    cpu = None
+    if cpu_steps > 0:
+        # the FP64 oracle (CPU, production mode at tight tolerances) from the same labels
+        from oracle import oracle as om
+        po = mixed_params(True)
+        threads = cpu_threads()
+        o = om.Oracle(shape, label_bytes=2, params=po, mode=om.SOLVE_PRODUCTION, threads=threads)
+        o.set_solver(om.SOLVE_PRODUCTION, rtol=1e-12)
+        o.load_labels(lab)
+        o.set("kmult", kmult)
+        o.init_all()
+        w0 = time.perf_counter()
+        t = 0.0
+        for _ in range(cpu_steps):
+            ok, _ = o.step(t, DT)
+            if not ok:
+                raise RuntimeError("oracle step failed")
+            t += DT
+        wall = time.perf_counter() - w0
+        of = {f: o.get(f, padded=f != "label") for f in MIX_FIELDS}
+        o.close()
+        cpu = {"steps": cpu_steps, "wall_s": round(wall, 1), "cores": threads,
+               "mixed_vs_oracle": errors(km[cpu_steps], of),
+               "note": ("the mixed-precision GPU fields after the first steps against the CPU oracle's (FP64, "
+                        "multigrid-PCG pressure and GMRES transport to rtol 1e-12) from the same labels")}
     warm_m = statistics.median(tm[1:])
     warm_f = statistics.median(tf[1:])
     vox = lab.size
@@ -813,18 +847,21 @@ def mixed_arm(args):
     return {"metric": f"time-steps/s at {shape[0]}x{shape[1]}x{shape[2]} uint16, mixed precision",
             "value": round(1e3 / warm_m, 4), "unit": "time-steps/s", "n_gpus": 1, "steps": steps - 1,
             "warmup": 1, "ms_per_step": round(warm_m, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f64/f32", "data": "synthetic",
             "config": {"workload": f"{shape[0]}x{shape[1]}x{shape[2]} uint16 grey-level random field "
                                    "(corr 6) with 4 planar fractures of 1-3 voxel aperture, classified at the "
-                                   "20% / 88% grey quantiles -> Pore / Rock / Sulphide (fractures: Pore), Air "
-                                   "inlet planes, dt 1, D 1, kreac 1, csat 1; mixed: FP32 inner MG-FCG / "
-                                   "BiCGStab with FP64 refinement to pressure rtol 1e-8, transport 1e-6; "
-                                   "fp64: FP64 inner MG-PCG to pressure rtol 1e-12, transport 1e-12",
+                                   "20% / 88% grey quantiles -> Pore / Rock / Sulphide (fractures: Pore with "
+                                   f"intrinsic permeability x{MIX_CONTRAST:g}, contrast {MIX_CONTRAST:g} to the "
+                                   "matrix), flow-through pressure (P = 1 at z = 0, 0 at z = max), acid 1 "
+                                   "flowing in, dt 1, D 1, kreac 1, csat 1; mixed: FP32 inner MG-FCG / BiCGStab "
+                                   "with FP64 refinement to pressure rtol 1e-8, transport 1e-6; fp64: FP64 "
+                                   "inner MG-PCG to pressure rtol 1e-12, transport 1e-12",
                        "thresholds": thr, "l2": "working set > L2"},
             "first_step_ms": {"mixed": round(tm[0], 3), "fp64": round(tf[0], 3)},
             "fp64_ms_per_step": round(warm_f, 3),
             "iterations": {"mixed": im, "fp64": iff},
             "rel_l2_vs_fp64": err,
+            "vs_cpu_oracle": cpu,
             "memory": {"device_bytes": mem, "bytes_per_voxel": round(mem / vox, 1),
                        "gpu_total_bytes": int(total),
                        "projected_1024x1024x768_bytes": int(mem / vox * c5),
@@ -843,6 +880,8 @@ def main():
     ap.add_argument("--shape", default=None, help="override (I,J,K) for quick checks")
     ap.add_argument("--cpu-steps", type=int, default=CPU_STEPS)
     ap.add_argument("--no-flow", action="store_true", help="skip the flow-through model measurement")
+    ap.add_argument("--mixed-cpu-steps", type=int, default=2,
+                    help="--mixed: steps of the CPU oracle comparison (0: none)")
     ap.add_argument("--flow", action="store_true",
                     help="only the flow-through model measurement, as its own JSON line")
     ap.add_argument("--no-e2e", action="store_true")

@@ -2,9 +2,9 @@
  * ls_oracle.c - CPU restatement of the LeachingSim per-time-step algorithm.
  *
  * TEST INFRASTRUCTURE ONLY (the checker and the timed CPU baseline); the
- * product library never links or calls it. PARITY UNPINNED: the reference
- * cannot be built or run here (MPI, PETSc, VTK, Boost absent) and ships no
- * tests or golden outputs; see ls_oracle.h.
+ * product library never links or calls it. Parity is pinned to the reference's
+ * own code compiled against single-rank MPI / PETSc / VTK stand-ins (oracle/_ref,
+ * tests/test_ref_pin.py); see ls_oracle.h.
  *
  * Citations "S.cpp:N" are to src/Simulation.cpp of the reference project,
  * "main.cpp:N" to src/main.cpp, "M.h:N" to src/MPIDomain.h.

@@ -6,12 +6,15 @@
  * times (--impl reference, cpu_baseline). The product library never links,
  * loads or calls it.
  *
- * PARITY UNPINNED: the reference (javalosp/LeachingSim) has no tests, no
- * golden outputs and needs MPI + PETSc + VTK + Boost, none of which exist
- * here, so it cannot be run to produce reference outputs. This restatement
- * follows its source line by line (citations are to files of the reference
- * project) and is cross-checked against an independent numpy restatement in
- * tests/twin.py.
+ * PARITY PINNED to the reference's own code: the reference (javalosp/LeachingSim)
+ * has no tests or golden outputs and needs MPI + PETSc + VTK + Boost, none of which
+ * exist here; its per-time-step sources are compiled unchanged against single-rank
+ * stand-ins for those libraries into oracle/_ref (oracle/build_ref.py), and
+ * tests/test_ref_pin.py checks this restatement against them function by function
+ * (bit for bit where no linear solve is involved) and over whole steps; two golden
+ * fixtures under tests/golden/ come from that library. The restatement follows the
+ * source line by line (citations are to files of the reference project) and is also
+ * cross-checked against an independent numpy restatement in tests/twin.py.
  *
  * Semantics restated are those of a single MPI rank (np=1), including the
  * one-plane write-back offset of every linear solve (compat_shift), the

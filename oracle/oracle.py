@@ -1,8 +1,8 @@
 """ctypes front end of the CPU oracle (oracle/ls_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
-bench.py's CPU-baseline leg, never by the product package. Parity unpinned:
-the reference cannot run here; see ls_oracle.h.
+bench.py's CPU-baseline leg, never by the product package. Its parity with the
+reference's own code is checked by tests/test_ref_pin.py; see ls_oracle.h.
 """
 import ctypes as C
 import os

@@ -5,7 +5,7 @@ images.
 The scripts keep their file names and shapes as module constants and do their work in
 main(); this runs each script's source with those constants replaced by a small seeded
 input, in a temporary directory, and stores input and output as tests/golden/geometry.npz.
-It needs the reference checkout (path in LEACHINGSIM_REF, default /root/reference) and
+It needs the reference checkout (its path in the environment variable LEACHINGSIM_REF) and
 scipy; the fixture it writes is what the tests use.
 
 Run:  python tests/golden/make_geometry_golden.py
@@ -20,7 +20,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
-REF = os.environ.get("LEACHINGSIM_REF", "/root/reference")
+REF = os.environ.get("LEACHINGSIM_REF")
+if not REF:
+    sys.exit("set LEACHINGSIM_REF to the reference checkout (its Python scripts are run from there)")
 
 from leachingsim_gb300.geometry import grf_geometry  # noqa: E402
 

@@ -1,11 +1,21 @@
-"""Generate the golden fixtures of tests/golden/ from the CPU oracle (tight solves).
+"""Generate the golden fixtures of tests/golden/.
 
-Cases: the reference's two generate_input.py recipes scaled to 20^3 (Air slabs at both
-ends) and a small seeded Gaussian-random-field geometry, each run from a fresh start for
-4 steps of dt = 1 (csat = 1, like the reference's job scripts), plus one restart-style
-case with acid present so the dissolution sweep is exercised. Saved per case: the inputs,
-the parameters, the per-step solver/sub-step summaries and the final fields (padded
-(I+1)*J*K arrays, the reference's np=1 layout).
+Oracle cases (the CPU oracle, tight solves): the reference's two generate_input.py recipes
+scaled to 20^3 (Air slabs at both ends) and a small seeded Gaussian-random-field geometry,
+each run from a fresh start for 4 steps of dt = 1 (csat = 1, like the reference's job
+scripts), plus one restart-style case with acid present so the dissolution sweep is
+exercised.
+
+Reference cases (source "reference"): produced by the reference's own code, the parity
+library oracle/_ref (src/Simulation.cpp compiled unchanged against single-rank MPI / PETSc /
+VTK stand-ins, tight GMRES solves), stepped in the order of src/main.cpp:303-432. The
+reference throws on non-solid voxels of a low face and on a domain without mineral, so these
+geometries have a Rock shell on the planes i, j, k = 0 and Air inlet planes i = 1, 2; one is
+uint8, one uint16 with acid present. They need the reference's sources (oracle/build_ref.py)
+and are skipped by this script where those are absent.
+
+Saved per case: the inputs, the parameters, the per-step summaries and the final fields
+(padded (I+1)*J*K arrays, the reference's np=1 layout).
 
 Run:  python tests/golden/make_golden.py
 """
@@ -36,6 +46,43 @@ def cases():
     yield "grf_acid_18x16x14", lab, dict(c_sat=1.0, kreac=5.0, time_scalar=100.0), acid
 
 
+def shelled(shape, seed, dtype):
+    """GRF geometry with Air inlet planes i = 1, 2 and Rock on the planes i, j, k = 0."""
+    lab, _ = grf_geometry(shape, porosity=0.35, corr_len=2.0, mineral_fraction=0.2, seed=seed, air_inlet=False,
+                          dtype=dtype)
+    lab[1:3] = 1
+    lab[0] = 3
+    lab[:, 0] = 3
+    lab[:, :, 0] = 3
+    return lab
+
+
+def reference_cases():
+    yield "ref_u8_16x14x12", shelled((16, 14, 12), 21, np.uint8), dict(c_sat=1.0), None
+    lab = shelled((14, 15, 12), 22, np.uint16)
+    acid = np.random.default_rng(23).uniform(0.0, 1.0, lab.shape)
+    yield "ref_u16_acid_14x15x12", lab, dict(c_sat=1.0, kreac=5.0, time_scalar=100.0), acid
+
+
+def run_reference(lab, pover, acid, steps=4):
+    from oracle import refsim
+    lb = 2 if lab.dtype == np.uint16 else 1
+    p = default_params(press_rtol=1e-13, conc_rtol=1e-13, **pover)
+    r = refsim.RefSim(lab.shape, label_bytes=lb, params=p, rtol=1e-14, restart=200, max_it=200000)
+    r.load_labels(lab)
+    r.init_all()
+    if acid is not None:
+        r.set("acid", acid)
+    infos = []
+    for n in range(steps):
+        ok, leached = r.step(float(n), 1.0)
+        assert ok
+        infos.append({"leached": int(leached)})
+    out = {f: r.get(f, padded=True) for f in FIELDS}
+    r.close()
+    return p, infos, out
+
+
 def run_case(lab, pover, acid, steps=4):
     p = default_params(press_rtol=1e-13, conc_rtol=1e-13, **pover)
     o = om.Oracle(lab.shape, params=p, mode=om.SOLVE_TIGHT, rtol=1e-14, restart=200, max_it=200000)
@@ -55,19 +102,34 @@ def run_case(lab, pover, acid, steps=4):
     return p, infos, out
 
 
+def save(manifest, name, lab, acid, p, infos, out, source):
+    arrays = {"in_label": lab}
+    if acid is not None:
+        arrays["in_acid"] = acid
+    for f, v in out.items():
+        arrays[f] = v
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrays)
+    manifest[name] = {"shape": list(lab.shape), "params": {k: v for k, v in p.as_dict().items()},
+                      "steps": len(infos), "infos": infos, "source": source,
+                      "label_bytes": 2 if lab.dtype == np.uint16 else 1}
+    print(name, source, lab.shape, [i["leached"] for i in infos])
+
+
 def main():
     manifest = {}
+    old = os.path.join(HERE, "manifest.json")
+    if os.path.exists(old):
+        manifest = json.load(open(old))
     for name, lab, pover, acid in cases():
         p, infos, out = run_case(lab, pover, acid)
-        arrays = {"in_label": lab}
-        if acid is not None:
-            arrays["in_acid"] = acid
-        for f, v in out.items():
-            arrays[f] = v
-        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrays)
-        manifest[name] = {"shape": list(lab.shape), "params": {k: v for k, v in p.as_dict().items()},
-                          "steps": len(infos), "infos": infos}
-        print(name, lab.shape, [i["leached"] for i in infos])
+        save(manifest, name, lab, acid, p, infos, out, "oracle")
+    from oracle import refsim
+    if refsim.available():
+        for name, lab, pover, acid in reference_cases():
+            p, infos, out = run_reference(lab, pover, acid)
+            save(manifest, name, lab, acid, p, infos, out, "reference")
+    else:
+        print("the reference's sources are not present: reference cases kept as they are")
     with open(os.path.join(HERE, "manifest.json"), "w") as fh:
         json.dump(manifest, fh, indent=1, sort_keys=True)
 

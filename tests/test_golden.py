@@ -1,8 +1,14 @@
-"""Golden fixtures (tests/golden/, made by tests/golden/make_golden.py from the oracle).
+"""Golden fixtures (tests/golden/, made by tests/golden/make_golden.py): four from the oracle
+and two ("source": "reference") from the reference's own code, the parity library oracle/_ref
+(src/Simulation.cpp compiled unchanged against single-rank MPI / PETSc / VTK stand-ins).
 
-CPU: the oracle still reproduces them. GPU: the CUDA path reproduces them through the C-ABI:
-labels exactly, fields within the stated tolerances (pressure per the conditioning note of
-test_gpu_parity.py)."""
+CPU: the oracle reproduces them (its own fixtures to 1e-9 / 1e-10; the reference's to the
+spread of two tight GMRES solves of the same systems: the rest 1e-10, precipitate by its
+largest absolute difference, pressure 1e-6: once clogging seals Pore clusters off from the
+inlet their pressure is held only by ~1e-22 links, and residual-converged solvers leave such
+near-null modes at different values). GPU: the CUDA path reproduces them through
+the C-ABI: labels exactly, fields within the stated tolerances (pressure per the
+conditioning note of test_gpu_parity.py)."""
 import json
 import os
 
@@ -34,16 +40,19 @@ def check(name, get, ptol, ftol):
     assert rel_l2(get("pressure"), d["pressure"]) < ptol
     for f in ("saturation", "flux_x", "flux_y", "flux_z"):
         assert rel_l2(get(f), d[f]) < ftol, f
-    for f in ("conc", "acid", "precipitate"):
+    for f in ("conc", "acid"):
         assert rel_l2(get(f) + 1.0, d[f] + 1.0) < ftol, f
+    # where conc sits at c_sat = 1 to within the solves' rounding, one side may precipitate
+    # ~1e-17 that the other does not
+    assert np.abs(get("precipitate") - d["precipitate"]).max() < 1e-12
 
 
 @pytest.mark.parametrize("name", NAMES)
 def test_oracle_reproduces_golden(oracle_mod, name):
     d, m, p = load(name)
     lab = d["in_label"]
-    o = oracle_mod.Oracle(lab.shape, params=p, mode=oracle_mod.SOLVE_TIGHT, rtol=1e-14, restart=200,
-                          max_it=200000)
+    o = oracle_mod.Oracle(lab.shape, label_bytes=m.get("label_bytes", 1), params=p, mode=oracle_mod.SOLVE_TIGHT,
+                          rtol=1e-14, restart=200, max_it=200000)
     o.load_labels(lab)
     o.init_all()
     if "in_acid" in d:
@@ -52,8 +61,10 @@ def test_oracle_reproduces_golden(oracle_mod, name):
         ok, info = o.step(float(n), 1.0)
         assert ok
         assert info["leached"] == m["infos"][n]["leached"]
-        assert info["saturation"]["num_steps"] == m["infos"][n]["sat_steps"]
-    check(name, lambda f: o.get(f, padded=True), 1e-9, 1e-10)
+        if "sat_steps" in m["infos"][n]:
+            assert info["saturation"]["num_steps"] == m["infos"][n]["sat_steps"]
+    ptol = 1e-6 if m.get("source") == "reference" else 1e-9
+    check(name, lambda f: o.get(f, padded=True), ptol, 1e-10)
 
 
 # Pressure: both solvers stop on the Jacobi-scaled residual (rtol 1e-11), which cannot see
@@ -69,8 +80,9 @@ def test_gpu_reproduces_golden(name, solver, ptol):
     p.press_solver = solver
     p.press_rtol = 1e-11
     p.conc_rtol = 1e-13
-    lab = d["in_label"].astype(np.uint8)
-    g = Context(lab.shape, params=p)
+    lb = m.get("label_bytes", 1)
+    lab = d["in_label"].astype(np.uint8 if lb == 1 else np.uint16)
+    g = Context(lab.shape, label_bytes=lb, params=p)
     g.upload("label", lab)
     g.init_all()
     if "in_acid" in d:
@@ -79,6 +91,7 @@ def test_gpu_reproduces_golden(name, solver, ptol):
         ok, info = g.step(float(n), 1.0)
         assert ok, info
         assert info["leached"] == m["infos"][n]["leached"]
-        assert info["saturation"]["num_steps"] == m["infos"][n]["sat_steps"]
+        if "sat_steps" in m["infos"][n]:
+            assert info["saturation"]["num_steps"] == m["infos"][n]["sat_steps"]
     check(name, lambda f: g.download(f, padded=True), ptol, 1e-8)
     g.close()
