@@ -487,6 +487,7 @@ static ls_status transfer(ls_ctx* c, ls_field f, void* host, size_t n, int padde
             c->props_force = 1;
         if (f == LS_F_PRESSURE) c->p_eff_prev = 0.0;
         if (f == LS_F_ACID) c->acid_zero = 0;
+        if (f == LS_F_LABEL || f == LS_F_FRAC) c->dz_no_threshold = 0;
     } else {
         LS_CUDA(c, cudaMemcpyAsync(host, dev, n * esz, kind, c->stream));
     }
@@ -522,6 +523,7 @@ ls_status ls_init_fields(ls_ctx* c) {
 
 ls_status ls_init_frac(ls_ctx* c, unsigned long long* count) {
     if (!c) return LS_BAD_ARG;
+    c->dz_no_threshold = 0;
     return init_frac_run(c, count);
 }
 
@@ -700,6 +702,7 @@ ls_status ls_rollback(ls_ctx* c) {
     c->p_ready = 0;
     c->p_eff_prev = 0.0;
     c->acid_zero = 0;
+    c->dz_no_threshold = 0;
     return ls_props(c);
 }
 

@@ -352,6 +352,18 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
         dc.vol = make_dxdiv(dc.dx * dc.dx * dc.dx);
     }
     const L* label = (const L*)c->label;
+    // With the acid field identically 0 (known from the transport solve that produced it) every
+    // flux sum is k_eff * 0 = 0, the largest rate 0 and the sub-step count 1; with no active
+    // voxel at the threshold either, the sweeps would change nothing: the rate pass is skipped.
+    if (c->acid_zero && c->dz_no_threshold) {
+        if (info) {
+            info->max_rate = 0.0;
+            info->num_steps = 1;
+            info->dt_sub = dt;
+        }
+        if (leached_out) *leached_out = 0;
+        return LS_OK;
+    }
     LS_CUDA(c, cudaMemsetAsync(c->d_int, 0, sizeof(int) * 4, c->stream));
     LS_LAUNCH(c, k_dz_rate<L>, grid, kBlock, 0, g, dc, label, (const double*)c->acid,
               (const float*)c->frac, c->d_int, c->partials);
@@ -379,7 +391,12 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
     if (leached_out) *leached_out = 0;
     // With no acid reaching any active voxel and none at the threshold, every sweep leaves
     // every field unchanged (frac -= 0, nothing consumed, nothing flips).
-    if (n_active == 0 || (n_flux == 0 && n_flip == 0)) return LS_OK;
+    if (n_active == 0 || (n_flux == 0 && n_flip == 0)) {
+        c->dz_no_threshold = 1;
+        return LS_OK;
+    }
+    // after the sweeps every active voxel is above the threshold or has been cleared to 0
+    c->dz_no_threshold = 1;
 
     const int nlev = (g.I - 1) + 2 * (g.J - 1) + 3 * (g.K - 1) + 1;
     auto grow_cap = [&](int need) -> ls_status {

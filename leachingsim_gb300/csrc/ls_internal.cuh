@@ -372,6 +372,8 @@ struct ls_ctx {
     void* dz_save_label;
     int dz_sel_cap;
     long long dz_fallbacks;  // calls that fell back to the full wavefront sweep
+    int dz_no_threshold;     // no active voxel has 0 < frac <= 1e-4 (known after a dissolution call;
+                             // cleared by every write of labels or frac from outside)
 
     // reductions
     double* partials;     // kMaxPartials * 8 doubles

@@ -172,4 +172,14 @@ int lsref_call(void* h, const char* method, double arg, int* result) {
     return rc;
 }
 
+// Simulation::writeCheckpoint / loadCheckpoint (src/Simulation.cpp:2235-2307) into / from
+// <dir>/checkpoint_rank0_<step>.bin
+int lsref_checkpoint(void* h, const char* dir, int step, int write) {
+    Simulation* s = static_cast<Simulation*>(h);
+    return guard([&] {
+        if (write) s->writeCheckpoint(dir, step);
+        else s->loadCheckpoint(dir, step);
+    });
+}
+
 }  // extern "C"

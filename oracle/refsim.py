@@ -37,7 +37,8 @@ def lib(label_bytes):
                               ("lsref_option", None, [C.c_char_p, C.c_char_p]),
                               ("lsref_field", vp, [vp, i, C.POINTER(C.c_int)]), ("lsref_init", i, [vp]),
                               ("lsref_initial_sulphide_count", C.c_ulonglong, [vp]),
-                              ("lsref_call", i, [vp, C.c_char_p, d, C.POINTER(C.c_int)])):
+                              ("lsref_call", i, [vp, C.c_char_p, d, C.POINTER(C.c_int)]),
+                              ("lsref_checkpoint", i, [vp, C.c_char_p, i, i])):
             f = getattr(L, fn)
             f.restype = res
             f.argtypes = args
@@ -99,6 +100,15 @@ class RefSim:
         if self.L.lsref_call(self.h, method.encode(), float(arg), C.byref(r)) != 0:
             raise RuntimeError(f"{method}: {self.L.lsref_last_error().decode()}")
         return r.value
+
+    def write_checkpoint(self, directory, step):
+        """Simulation::writeCheckpoint: <directory>/checkpoint_rank0_<step>.bin"""
+        if self.L.lsref_checkpoint(self.h, str(directory).encode(), int(step), 1) != 0:
+            raise RuntimeError(self.L.lsref_last_error().decode())
+
+    def load_checkpoint(self, directory, step):
+        if self.L.lsref_checkpoint(self.h, str(directory).encode(), int(step), 0) != 0:
+            raise RuntimeError(self.L.lsref_last_error().decode())
 
     def load_labels(self, labels):
         self.set("label", np.asarray(labels))
