@@ -870,6 +870,154 @@ def mixed_arm(args):
             "e2e": None}
 
 
+# ---------------------------------------------------------------------------
+# The large single domain: 1024x1024x768 uint16 (805 M voxels) with the lean device layout.
+
+LARGE_SHAPE = (768, 1024, 1024)  # (I, J, K) = (zext, yext, xext)
+LARGE_POROSITY = 0.20
+LARGE_FRACTURES = 8
+LARGE_DT = 0.5
+
+
+def large_geometry(shape, seed=0, porosity=LARGE_POROSITY, n_fractures=LARGE_FRACTURES, corr_len=6.0):
+    """uint16 labels and the permeability multiplier of the large fractured workload, made on
+    the GPU (a NumPy field of 805 M voxels takes minutes): a seeded Gaussian random field
+    (corr_len, periodic), scaled to grey levels 0..65535, n_fractures planar fractures of 1-3
+    voxel aperture at random orientations stamped in at grey 0, classified at the porosity /
+    88% grey quantiles (of a 1/64 subsample) into Pore / Rock / Sulphide as
+    ls_geom_classify does (label index = number of thresholds <= grey). Fracture voxels get
+    the multiplier MIX_CONTRAST. Returns host arrays (labels, kmult, thresholds)."""
+    import torch
+    import torch.nn.functional as F
+    dev = torch.device("cuda")
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    f = torch.randn(shape, generator=gen, device=dev, dtype=torch.float32)
+    half = int(3.0 * corr_len + 0.5)
+    x = torch.arange(-half, half + 1, device=dev, dtype=torch.float32)
+    w = torch.exp(-0.5 * (x / corr_len) ** 2)
+    w = (w / w.sum()).view(1, 1, -1)
+    for axis in range(3):
+        g = f.movedim(axis, 2).contiguous()
+        a, b, n = g.shape
+        g = F.pad(g.view(a * b, 1, n), (half, half), mode="circular")
+        g = F.conv1d(g, w).view(a, b, n)
+        f = g.movedim(2, axis).contiguous()
+        del g
+    lo, hi = f.min(), f.max()
+    grey = ((f - lo) / (hi - lo).clamp_min(1e-30) * 65535.0).to(torch.int32)
+    del f
+    rng = np.random.Generator(np.random.PCG64(seed))
+    I, J, K = shape
+    ii = torch.arange(I, device=dev, dtype=torch.float32).view(I, 1, 1) - I / 2.0
+    jj = torch.arange(J, device=dev, dtype=torch.float32).view(1, J, 1) - J / 2.0
+    kk = torch.arange(K, device=dev, dtype=torch.float32).view(1, 1, K) - K / 2.0
+    for _ in range(n_fractures):
+        nrm = rng.standard_normal(3)
+        nrm /= np.linalg.norm(nrm)
+        offset = rng.uniform(-0.3, 0.3) * min(shape)
+        ap = rng.integers(1, 4) / 2.0
+        dist = ii * float(nrm[0]) + jj * float(nrm[1]) + kk * float(nrm[2]) - float(offset)
+        grey.masked_fill_(dist.abs() <= ap, 0)
+        del dist
+    sub = grey[::4, ::4, ::4].flatten().float()
+    thr = [int(torch.quantile(sub, porosity).item()), int(torch.quantile(sub, 0.88).item())]
+    lab = (2 + (grey >= thr[0]).to(torch.int32) + (grey >= thr[1]).to(torch.int32)).to(torch.int16)
+    kmult = torch.where(grey == 0, MIX_CONTRAST, 1.0).to(torch.float32)
+    del grey
+    out = lab.cpu().numpy().view(np.uint16), kmult.cpu().numpy(), thr
+    del lab, kmult
+    torch.cuda.empty_cache()
+    return out
+
+
+def large_arm(args):
+    """Time steps of the large single domain with the lean layout (memory_mode MEM_LEAN): the
+    first (cold) step and args.warmup - 1 more untimed, args.steps timed with the mixed solver,
+    then args.steps with the plain FP64 multigrid-PCG pressure solver (same rtol) on the state
+    they left; the device footprint (the pool's reserved high-water mark) and the host snapshot."""
+    import torch
+    from leachingsim_gb300._abi import BC_FLOW_I, MEM_LEAN
+    from leachingsim_gb300.runtime import Context
+    torch.cuda.set_device(0)
+    shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else LARGE_SHAPE
+    t0 = time.time()
+    lab, kmult, thr = large_geometry(shape)
+    gen_s = time.time() - t0
+    counts = np.bincount(lab[::4, ::4, ::4].ravel(), minlength=5).tolist()
+    log(f"large: geometry {shape} in {gen_s:.1f}s, labels (1/64 sample) {counts}")
+
+    def lp(solver):
+        return params(solver, bc_mode=BC_FLOW_I, p_inlet=FLOW_PIN, p_outlet=FLOW_POUT, acid_inlet=FLOW_ACID,
+                      memory_mode=MEM_LEAN)
+
+    t1 = time.time()
+    ctx = Context(shape, label_bytes=2, params=lp("mixed"))
+    ctx.upload("label", lab)
+    ctx.upload("kmult", kmult)
+    del lab, kmult
+    ctx.init_all()
+    ctx.synchronize()
+    setup_s = time.time() - t1
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.timing(True)
+    ctx.timing_reset()
+    w0 = time.perf_counter()
+    t, n, first = run_steps(ctx, 0.0, 0, 1, LARGE_DT)
+    ctx.synchronize()
+    cold_ms = (time.perf_counter() - w0) * 1e3
+    t, n, _ = run_steps(ctx, t, n, max(args.warmup - 1, 0), LARGE_DT)
+
+    def timed(solver, steps):
+        nonlocal t, n
+        ctx.set_params(lp(solver))
+        ctx.timing_reset()
+        torch.cuda.synchronize()
+        ctx.synchronize()
+        ev0.record(stream)
+        t, n, infos = run_steps(ctx, t, n, steps, LARGE_DT)
+        ev1.record(stream)
+        ev1.synchronize()
+        sec = ev0.elapsed_time(ev1) / 1e3
+        tm = {k: round(ctx.timing_get(k)[0] / steps, 3)
+              for k in ("press_setup", "press_inner", "press_outer", "transport", "dissolve", "snapshot")}
+        return {"value": round(steps / sec, 4), "unit": UNIT, "ms_per_step": round(sec * 1e3 / steps, 3),
+                "ms_per_step_by_phase": tm,
+                "pressure_iterations": [i["pressure"]["iterations"] for i in infos],
+                "pressure_rel_residual_max": max(i["pressure"]["rel_residual"] for i in infos),
+                "leached_per_step": [i["leached"] for i in infos],
+                "mineral_budget_last": infos[-1]["budget"]["mineral"]}
+
+    with ClockSampler(0) as clk:
+        mixed = timed("mixed", args.steps)
+    plain = timed("fp64", max(1, min(args.steps, 2))) if not args.no_plain else None
+    ctx.timing(False)
+    vox = shape[0] * shape[1] * shape[2]
+    peak = ctx.device_peak_bytes()
+    host = ctx.host_bytes()
+    ctx.close()
+    total = torch.cuda.get_device_properties(0).total_memory
+    return {"metric": f"time-steps/s at {shape[2]}x{shape[1]}x{shape[0]} uint16, lean layout",
+            "value": mixed["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": mixed["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64/f32", "data": "synthetic",
+            "config": {"workload": f"{shape[2]}x{shape[1]}x{shape[0]} uint16 grey-level random field (corr 6, "
+                                   f"made on the GPU) with {LARGE_FRACTURES} planar fractures of 1-3 voxel "
+                                   f"aperture, classified at the {LARGE_POROSITY:g} / 0.88 grey quantiles -> "
+                                   f"Pore / Rock / Sulphide (fractures: Pore with intrinsic permeability "
+                                   f"x{MIX_CONTRAST:g}), flow-through pressure (P = {FLOW_PIN:g} at z = 0, "
+                                   f"{FLOW_POUT:g} at z = max), acid {FLOW_ACID:g} flowing in, dt {LARGE_DT:g}, D 1, "
+                                   "kreac 1, csat 1, pressure rtol 1e-8, transport rtol 1e-6; lean device layout",
+                       "thresholds": thr, "memory_mode": "lean", "l2": "working set > L2"},
+            "mixed": mixed, "plain_fp64": plain,
+            "first_step_ms": round(cold_ms, 1), "first_step_pressure_iterations": first[0]["pressure"]["iterations"],
+            "geometry_s": round(gen_s, 1), "setup_s": round(setup_s, 1),
+            "memory": {"device_peak_bytes": int(peak), "bytes_per_voxel": round(peak / vox, 1),
+                       "host_snapshot_bytes": int(host), "gpu_total_bytes": int(total)},
+            "clocks": clk.summary(), "e2e": None}
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -897,7 +1045,15 @@ def main():
     ap.add_argument("--mixed", action="store_true",
                     help="mixed precision against FP64 settings on the 512^3 uint16 fractured geometry "
                          "(a separate JSON line)")
+    ap.add_argument("--large", action="store_true",
+                    help="the 1024x1024x768 uint16 fractured domain with the lean device layout, mixed "
+                         "precision against the plain FP64 pressure solver (a separate JSON line)")
     args = ap.parse_args()
+    if args.large:
+        if args.steps == 40:
+            args.steps = 3  # the default count is for the 338x338x283 workload
+        print(json.dumps(large_arm(args)), flush=True)
+        return
     if args.geometry:
         print(json.dumps(geometry_arm(args)), flush=True)
         return

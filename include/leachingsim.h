@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define LS_ABI_VERSION 2
+#define LS_ABI_VERSION 3
 
 enum {
     LS_AIR = 1,
@@ -92,6 +92,23 @@ typedef enum ls_bc_mode {
                               rows of the reference's disabled block, src/Simulation.cpp:997-1004).
                               Everything else follows the reference. */
 } ls_bc_mode;
+
+/* Device memory layout of a context, fixed when it is created (ls_params.memory_mode). */
+typedef enum ls_memory_mode {
+    LS_MEM_RESIDENT = 0,   /* every work array stays allocated, the FP64 per-voxel kernels
+                              recompute only the voxels whose inputs changed (shadow copies of
+                              their inputs), the state snapshot is in device memory: ~620 bytes
+                              per voxel (uint16 labels, mixed precision) */
+    LS_MEM_LEAN = 1        /* for domains that do not fit that way: the pressure solve's and the
+                              transport solves' work arrays are cut from one device arena (the
+                              set of a phase is released when the other phase starts), every
+                              voxel is recomputed each step, the snapshot (but for the mineral
+                              fractions) is in pinned host memory and copied on a stream of its
+                              own while the step runs: ~285 bytes per voxel (mixed precision),
+                              ~310 (FP64). Results are bit-identical to LS_MEM_RESIDENT. The
+                              pressure system stays readable (ls_pressure_apply, ...) until the
+                              next transport solve. */
+} ls_memory_mode;
 
 /* Pressure solver variants. */
 typedef enum ls_press_solver {
@@ -154,6 +171,8 @@ typedef struct ls_params {
     double pore_permeability; /* 1e-12: Air and clean Pore (src/Simulation.cpp:190) */
     double rock_permeability; /* 1e-18: Rock, and the clogged / unleached end of the log blend
                                  (src/Simulation.cpp:191) */
+    /* ABI 3 */
+    int memory_mode;          /* ls_memory_mode; fixed at ls_create (ls_set_params rejects a change) */
 } ls_params;
 
 /* Result of one linear solve (the reference's log line, src/Simulation.cpp:834-849). */
@@ -222,6 +241,10 @@ void* ls_stream(ls_ctx* ctx);
 ls_status ls_synchronize(ls_ctx* ctx);
 /* Device bytes held by the context. */
 size_t ls_device_bytes(const ls_ctx* ctx);
+/* The most device bytes the context has held at once, and the host bytes it holds (the
+   snapshot of LS_MEM_LEAN). */
+size_t ls_device_peak_bytes(const ls_ctx* ctx);
+size_t ls_host_bytes(const ls_ctx* ctx);
 
 /* Host <-> device transfers. n_elems must be I*J*K (padded=0) or (I+1)*J*K (padded=1).
    The label upload replaces Simulation::readRAW's array (src/Simulation.cpp:68-74). */

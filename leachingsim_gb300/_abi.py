@@ -36,6 +36,9 @@ FIELD_DTYPES = {0: None, 1: "float32", 14: "float32"}
 # ls_bc_mode
 BC_REFERENCE, BC_FLOW_I = 0, 1
 
+# ls_memory_mode
+MEM_RESIDENT, MEM_LEAN = 0, 1
+
 # ls_press_solver
 PRESS_MIXED, PRESS_FP64, PRESS_JACOBI64, PRESS_LEARNED = 0, 1, 2, 3
 
@@ -66,6 +69,7 @@ class LsParams(C.Structure):
         ("bc_mode", C.c_int), ("p_inlet", C.c_double), ("p_outlet", C.c_double),
         ("conc_inlet", C.c_double), ("acid_inlet", C.c_double),
         ("pore_permeability", C.c_double), ("rock_permeability", C.c_double),
+        ("memory_mode", C.c_int),
     ]
 
     def as_dict(self):

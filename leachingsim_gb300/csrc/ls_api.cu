@@ -26,13 +26,51 @@ ls_status dalloc(ls_ctx* c, void** p, size_t bytes) {
     if (bytes == 0) bytes = 256;
     cudaError_t e = cudaMalloc(p, bytes);
     if (e != cudaSuccess) {
+        cudaGetLastError();
         *p = nullptr;
         char buf[160];
         snprintf(buf, sizeof(buf), "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
         return set_error(c, LS_CUDA_ERROR, buf);
     }
     c->device_bytes += bytes;
+    c->device_peak = std::max(c->device_peak, c->device_bytes);
+    static const bool trace = [] {
+        const char* e = getenv("LS_ALLOC_TRACE");
+        return e && e[0] == '1';
+    }();
+    if (trace)
+        fprintf(stderr, "[ls alloc] %zu bytes, held %zu, peak %zu, phase %d\n", bytes, c->device_bytes,
+                c->device_peak, c->arena_phase);
     return LS_OK;
+}
+
+static bool in_arena(const ls_ctx* c, const void* p) {
+    return c->arena && (const char*)p >= (const char*)c->arena && (const char*)p < (const char*)c->arena + c->arena_size;
+}
+
+ls_status walloc(ls_ctx* c, void** p, size_t bytes) {
+    if (!c->lean || c->arena_phase == kPhaseNone) return dalloc(c, p, bytes);
+    bytes = (std::max(bytes, (size_t)1) + 255) & ~(size_t)255;
+    if (c->arena && c->arena_used + bytes <= c->arena_size) {
+        *p = (char*)c->arena + c->arena_used;
+        c->arena_used += bytes;
+        return LS_OK;
+    }
+    // beyond the arena (the first steps): an array of its own, counted into the arena's next size
+    c->arena_overflow += bytes;
+    return dalloc(c, p, bytes);
+}
+
+void dfree(ls_ctx* c, void** p, size_t bytes) {
+    if (!*p) return;
+    if (in_arena(c, *p)) {  // the arena is reset as a whole
+        *p = nullptr;
+        return;
+    }
+    if (bytes == 0) bytes = 256;
+    cudaFree(*p);
+    c->device_bytes -= bytes;
+    *p = nullptr;
 }
 
 // ---------------------------------------------------------------------------
@@ -84,7 +122,7 @@ static void resolve_regions(ls_ctx* c) {
 ls_status l0_alloc(ls_ctx* c, int slot, size_t esize, void** out) {
     if (c->l0pad == 0) c->l0pad = ((c->g.JK + 31) / 32) * 32;
     const size_t bytes = esize * ((size_t)c->g.N + 2 * (size_t)c->l0pad);
-    LS_TRY(dalloc(c, &c->l0base[slot], bytes));
+    LS_TRY(walloc(c, &c->l0base[slot], bytes));
     c->l0bytes[slot] = bytes;
     LS_CUDA(c, cudaMemsetAsync(c->l0base[slot], 0, bytes, c->stream));
     *out = (char*)c->l0base[slot] + esize * (size_t)c->l0pad;
@@ -92,13 +130,80 @@ ls_status l0_alloc(ls_ctx* c, int slot, size_t esize, void** out) {
 }
 
 void l0_free(ls_ctx* c, int slot, void** p) {
-    if (c->l0base[slot]) {
-        cudaFree(c->l0base[slot]);
-        c->device_bytes -= c->l0bytes[slot];
-    }
-    c->l0base[slot] = nullptr;
+    dfree(c, &c->l0base[slot], c->l0bytes[slot]);
     c->l0bytes[slot] = 0;
     *p = nullptr;
+}
+
+__global__ void k_iota(long long n, int* __restrict__ list, unsigned int* __restrict__ count) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x)
+        list[r] = (int)r;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *count = (unsigned int)n;
+}
+
+ls_status wlist_all(ls_ctx* c) {
+    LS_TRY(wlist_reset(c));
+    LS_LAUNCH(c, k_iota, grid_for(c, c->g.N), kBlock, 0, c->g.N, c->wlist, c->wcount);
+    return LS_OK;
+}
+
+void snap_fence(ls_ctx* c, int groups) {
+    const int g = groups & c->snap_pending;
+    if (!g) return;
+    for (int q = 0; q < 4; ++q)
+        if (g & (1 << q)) cudaStreamWaitEvent(c->stream, c->snap_ev[q], 0);
+    c->snap_pending &= ~g;
+}
+
+static void lean_release_pressure(ls_ctx* c) {
+    const size_t n = (size_t)c->g.N;
+    double** rows[] = {&c->pdiag, &c->pb, &c->pface[0], &c->pface[1], &c->pface[2], &c->pisd, &c->pr,
+                       &c->pdelta, &c->psb2, &c->sat_q};
+    for (double** q : rows) dfree_t(c, q, n);
+    void** inner[] = {&c->ie, &c->iface[0], &c->iface[1], &c->iface[2], &c->iinvd, &c->inner[0],
+                      &c->inner[1], &c->inner[2], &c->inner[3], &c->inner[4]};
+    for (int q = 0; q < 10; ++q) l0_free(c, q, inner[q]);
+    c->inner_is64 = -1;
+    mg_free(c);
+    dfree_t(c, &c->comp, n);
+    dfree_t(c, &c->start_anchor, n);
+    c->p_ready = 0;
+}
+
+static void lean_release_transport(ls_ctx* c) {
+    const size_t n = (size_t)c->g.N;
+    for (double*& q : c->tc) dfree_t(c, &q, n);
+    for (double*& q : c->tb) dfree_t(c, &q, n);
+    for (float*& q : c->to) dfree_t(c, &q, n);
+    for (float*& q : c->trhs) dfree_t(c, &q, n);
+    dfree_t(c, &c->tinv, n);
+    dfree_t(c, &c->tkind, n);
+    dfree_t(c, &c->ti, (size_t)c->ti_stride * 7);
+    c->t_valid = 0;
+}
+
+ls_status lean_phase(ls_ctx* c, int phase) {
+    if (!c->lean || c->arena_phase == phase) return LS_OK;
+    lean_release_pressure(c);
+    lean_release_transport(c);
+    c->arena_need = std::max(c->arena_need, c->arena_used + c->arena_overflow);
+    c->arena_used = 0;
+    c->arena_overflow = 0;
+    if (c->arena_need > c->arena_size) {
+        // grow (the first switches): the released arrays and the old arena are back with the
+        // driver (cudaFree) before the new arena is mapped
+        if (c->arena) {
+            cudaFree(c->arena);
+            c->device_bytes -= c->arena_size;
+        }
+        c->arena = nullptr;
+        c->arena_size = 0;
+        c->arena_phase = kPhaseNone;  // the arena itself is not cut from the arena
+        LS_TRY(dalloc(c, &c->arena, c->arena_need));
+        c->arena_size = c->arena_need;
+    }
+    c->arena_phase = phase;
+    return LS_OK;
 }
 
 ls_status wlist_reset(ls_ctx* c) {
@@ -278,6 +383,8 @@ static ls_status validate_params(ls_ctx* c, const ls_params* p) {
         return set_error(c, LS_BAD_ARG, "unknown press_solver");
     if (p->bc_mode != LS_BC_REFERENCE && p->bc_mode != LS_BC_FLOW_I)
         return set_error(c, LS_BAD_ARG, "unknown bc_mode");
+    if (p->memory_mode != LS_MEM_RESIDENT && p->memory_mode != LS_MEM_LEAN)
+        return set_error(c, LS_BAD_ARG, "unknown memory_mode");
     if (!(p->pore_permeability > 0.0) || !(p->rock_permeability > 0.0))
         return set_error(c, LS_BAD_ARG, "pore_permeability and rock_permeability must be > 0");
     if (!std::isfinite(p->p_inlet) || !std::isfinite(p->p_outlet) || !std::isfinite(p->conc_inlet) ||
@@ -324,6 +431,21 @@ ls_status ls_create(ls_ctx** out, int I, int J, int K, int label_bytes, const ls
         delete c;
         return LS_CUDA_ERROR;
     }
+    if (c->p.memory_mode == LS_MEM_LEAN) {
+        c->lean = 1;
+        c->mg_graphs_off = 1;  // the hierarchy's arrays move between steps
+        if (cudaStreamCreateWithFlags(&c->snap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+            c->snap_stream = nullptr;
+            ls_destroy(c);
+            return LS_CUDA_ERROR;
+        }
+        for (cudaEvent_t& e : c->snap_ev)
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+                e = nullptr;
+                ls_destroy(c);
+                return LS_CUDA_ERROR;
+            }
+    }
     const size_t np = (size_t)NP, n = (size_t)c->g.N;
 #define ALLOC(ptr, count)                                                     \
     do {                                                                      \
@@ -338,23 +460,56 @@ ls_status ls_create(ls_ctx** out, int I, int J, int K, int label_bytes, const ls
         uint8_t* lb = nullptr;
         ALLOC(lb, np * label_bytes);
         c->label = lb;
-        uint8_t* blb = nullptr;
-        ALLOC(blb, np * label_bytes);
-        c->b_label = blb;
     }
     ALLOC(c->frac, np);
-    ALLOC(c->b_frac, np);
     double** f64[] = {&c->perm, &c->visc, &c->P, &c->conc, &c->acid, &c->fx, &c->fy, &c->fz,
-                      &c->sat, &c->pc, &c->kr, &c->precip, &c->b_precip, &c->b_sat, &c->b_P,
-                      &c->b_conc, &c->b_acid, &c->b_fx, &c->b_fy, &c->b_fz};
+                      &c->sat, &c->pc, &c->kr, &c->precip};
     for (double** q : f64) ALLOC(*q, np);
+    // the snapshot of src/Simulation.cpp:2312-2328: device arrays, or (lean) host arrays
+    void** snap[] = {&c->b_label, (void**)&c->b_frac, (void**)&c->b_precip, (void**)&c->b_sat, (void**)&c->b_P,
+                     (void**)&c->b_conc, (void**)&c->b_acid, (void**)&c->b_fx, (void**)&c->b_fy, (void**)&c->b_fz};
+    const size_t snap_bytes[] = {np * label_bytes, np * 4, np * 8, np * 8, np * 8, np * 8, np * 8, np * 8,
+                                 np * 8, np * 8};
+    // (the mineral fractions stay on the device in both layouts: the step's budget reads them)
+    const int kSnapFrac = 1;
+    if (c->lean) {
+        c->b_host_pinned = 1;
+        for (int q = 0; q < 10 && c->b_host_pinned; ++q)
+            if (q != kSnapFrac && cudaHostAlloc(snap[q], snap_bytes[q], cudaHostAllocDefault) != cudaSuccess)
+                c->b_host_pinned = 0;
+        if (!c->b_host_pinned) {
+            // not enough page-locked memory: pageable arrays (slower copies)
+            cudaGetLastError();
+            for (int q = 0; q < 10; ++q)
+                if (q != kSnapFrac && *snap[q]) cudaFreeHost(*snap[q]), *snap[q] = nullptr;
+            for (int q = 0; q < 10; ++q)
+                if (q != kSnapFrac && !(*snap[q] = std::calloc(1, snap_bytes[q]))) {
+                    ls_destroy(c);
+                    return LS_CUDA_ERROR;
+                }
+        }
+        for (int q = 0; q < 10; ++q)
+            if (q != kSnapFrac) c->host_bytes += snap_bytes[q];
+    }
+    for (int q = 0; q < 10; ++q) {
+        if (c->lean && q != kSnapFrac) continue;
+        st = dalloc(c, snap[q], snap_bytes[q]);
+        if (st != LS_OK) { ls_destroy(c); return st; }
+        if (cudaMemsetAsync(*snap[q], 0, snap_bytes[q], c->stream) != cudaSuccess) {
+            ls_destroy(c);
+            return LS_CUDA_ERROR;
+        }
+    }
     ALLOC(c->pkind, n);
-    ALLOC(c->pdiag, n);
-    ALLOC(c->pb, n);
-    for (int d = 0; d < 3; ++d) ALLOC(c->pface[d], n);
-    ALLOC(c->pisd, n);
-    ALLOC(c->pr, n);
-    ALLOC(c->pdelta, n);
+    if (!c->lean) {
+        // the pressure rows (lean: allocated by each assembly, released before the transport)
+        ALLOC(c->pdiag, n);
+        ALLOC(c->pb, n);
+        for (int d = 0; d < 3; ++d) ALLOC(c->pface[d], n);
+        ALLOC(c->pisd, n);
+        ALLOC(c->pr, n);
+        ALLOC(c->pdelta, n);
+    }
     ALLOC(c->partials, (size_t)kMaxPartials * 8);
     ALLOC(c->scal, (size_t)S_COUNT);
     ALLOC(c->d_int, (size_t)64);
@@ -375,10 +530,22 @@ ls_status ls_create(ls_ctx** out, int I, int J, int K, int label_bytes, const ls
 ls_status ls_destroy(ls_ctx* c) {
     if (!c) return LS_OK;
     if (c->stream) cudaStreamSynchronize(c->stream);
-    void* ptrs[] = {c->label, c->b_label, c->frac, c->b_frac, c->perm, c->visc, c->P, c->conc,
-                    c->acid, c->fx, c->fy, c->fz, c->sat, c->pc, c->kr, c->precip,
-                    c->b_precip, c->b_sat, c->b_P, c->b_conc, c->b_acid, c->b_fx, c->b_fy,
-                    c->b_fz, c->pkind, c->pdiag, c->pb, c->pface[0], c->pface[1], c->pface[2],
+    if (c->snap_stream) cudaStreamSynchronize(c->snap_stream);
+    // device arrays of dalloc
+    auto rel = [c](void* q) {
+        if (!q || in_arena(c, q)) return;  // arrays cut from the arena go with it
+        cudaFree(q);
+    };
+    void* snap[] = {c->b_label, c->b_frac, c->b_precip, c->b_sat, c->b_P, c->b_conc, c->b_acid, c->b_fx,
+                    c->b_fy, c->b_fz};
+    for (int q = 0; q < 10; ++q) {
+        if (!snap[q]) continue;
+        if (!c->lean || q == 1) rel(snap[q]);  // the mineral fractions: device memory in both layouts
+        else if (c->b_host_pinned) cudaFreeHost(snap[q]);
+        else std::free(snap[q]);
+    }
+    void* ptrs[] = {c->label, c->frac, c->perm, c->visc, c->P, c->conc,
+                    c->acid, c->fx, c->fy, c->fz, c->sat, c->pc, c->kr, c->precip, c->pkind, c->pdiag, c->pb, c->pface[0], c->pface[1], c->pface[2],
                     c->pisd, c->pr, c->pdelta, c->comp, c->cc_flag, c->tkind, c->tinv, c->dz_list,
                     c->dz_count, c->dz_level_start, c->partials, c->scal, c->d_int,
                     c->sh_label, c->sh_sat, c->sh_precip, c->sh_frac, c->shf_label, c->shf_perm,
@@ -386,35 +553,26 @@ ls_status ls_destroy(ls_ctx* c) {
                     c->shq_P, c->shq_C, c->shq_K, c->shq_V, c->shq_fx, c->shq_fy, c->shq_fz,
                     c->wlist, c->wcount, c->kmult, c->dz_sel, c->dz_flips, c->dz_save_frac,
                     c->dz_save_precip, c->dz_save_conc, c->dz_save_label};
-    for (void* q : ptrs)
-        if (q) cudaFree(q);
-    for (void* q : c->l0base)
-        if (q) cudaFree(q);
-    for (double* q : c->tc)
-        if (q) cudaFree(q);
-    for (double* q : c->tb)
-        if (q) cudaFree(q);
-    for (float* q : c->to)
-        if (q) cudaFree(q);
-    for (float* q : c->trhs)
-        if (q) cudaFree(q);
-    if (c->ti) cudaFree(c->ti);
-    if (c->start_anchor) cudaFree(c->start_anchor);
-    if (c->tcount) cudaFree(c->tcount);
+    for (void* q : ptrs) rel(q);
+    for (void* q : c->l0base) rel(q);
+    for (double* q : c->tc) rel(q);
+    for (double* q : c->tb) rel(q);
+    for (float* q : c->to) rel(q);
+    for (float* q : c->trhs) rel(q);
+    rel(c->ti);
+    rel(c->start_anchor);
+    rel(c->tcount);
     {
         void* lp[] = {c->lpc_c0, c->lpc_c1, c->lpc_c2, c->lpc_out, c->lpc_isd, c->lpc_anchor};
-        for (void* q : lp)
-            if (q) cudaFree(q);
+        for (void* q : lp) rel(q);
         if (c->lpc) ls_lpnet_destroy(c->lpc);
     }
     for (auto& gr : c->mg_graphs)
         if (gr.exec) cudaGraphExecDestroy(gr.exec);
     for (auto& lv : c->mg) {
         void* lp[] = {lv.comp, lv.e, lv.face[0], lv.face[1], lv.face[2], lv.invd, lv.x, lv.b, lv.t};
-        for (void* q : lp)
-            if (q) cudaFree(q);
-        for (void* q : lv.kv)
-            if (q) cudaFree(q);
+        for (void* q : lp) rel(q);
+        for (void* q : lv.kv) rel(q);
     }
     if (c->h_scal) cudaFreeHost(c->h_scal);
     if (c->h_int) cudaFreeHost(c->h_int);
@@ -423,6 +581,13 @@ ls_status ls_destroy(ls_ctx* c) {
         cudaEventDestroy(r.stop);
     }
     for (auto e : c->event_pool) cudaEventDestroy(e);
+    if (c->arena) cudaFree(c->arena);
+    if (c->snap_stream) {
+        cudaStreamSynchronize(c->snap_stream);
+        cudaStreamDestroy(c->snap_stream);
+    }
+    for (cudaEvent_t e : c->snap_ev)
+        if (e) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     cudaGetLastError();  // leave no error of the teardown pending for the next context
@@ -434,6 +599,8 @@ const char* ls_last_error(const ls_ctx* c) { return c ? c->err.c_str() : "null c
 ls_status ls_set_params(ls_ctx* c, const ls_params* p) {
     if (!c || !p) return LS_BAD_ARG;
     LS_TRY(validate_params(c, p));
+    if (p->memory_mode != c->p.memory_mode)
+        return set_error(c, LS_BAD_ARG, "memory_mode is fixed when the context is created");
     // a new boundary model changes the pressure scale: no ratio rescaling of the warm start
     if (p->bc_mode != c->p.bc_mode || p->p_inlet != c->p.p_inlet || p->p_outlet != c->p.p_outlet)
         c->p_eff_prev = 0.0;
@@ -455,10 +622,15 @@ void* ls_stream(ls_ctx* c) { return c ? (void*)c->stream : nullptr; }
 ls_status ls_synchronize(ls_ctx* c) {
     if (!c) return LS_BAD_ARG;
     LS_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (c->snap_stream) LS_CUDA(c, cudaStreamSynchronize(c->snap_stream));
     return LS_OK;
 }
 
 size_t ls_device_bytes(const ls_ctx* c) { return c ? c->device_bytes : 0; }
+
+size_t ls_device_peak_bytes(const ls_ctx* c) { return c ? c->device_peak : 0; }
+
+size_t ls_host_bytes(const ls_ctx* c) { return c ? c->host_bytes : 0; }
 
 static ls_status transfer(ls_ctx* c, ls_field f, void* host, size_t n, int padded, int up,
                           cudaMemcpyKind kind) {
@@ -479,6 +651,7 @@ static ls_status transfer(ls_ctx* c, ls_field f, void* host, size_t n, int padde
         return set_error(c, LS_BAD_ARG, buf);
     }
     if (up) {
+        snap_fence(c, kSnapAll);
         LS_CUDA(c, cudaMemcpyAsync(dev, host, n * esz, kind, c->stream));
         if (f == LS_F_LABEL || f == LS_F_PERMEABILITY || f == LS_F_VISCOSITY) c->p_ready = 0;
         // outputs of the property kernel written from outside: re-evaluate every voxel
@@ -511,6 +684,7 @@ ls_status ls_download_field_device(ls_ctx* c, ls_field f, void* dev, size_t n, i
 // Simulation::initFields, src/Simulation.cpp:165-180.
 ls_status ls_init_fields(ls_ctx* c) {
     if (!c) return LS_BAD_ARG;
+    snap_fence(c, kSnapAll);
     size_t bytes = sizeof(double) * (size_t)c->g.NP;
     double* f[] = {c->P, c->conc, c->fx, c->fy, c->fz, c->sat, c->pc, c->kr, c->precip};
     for (double* q : f) LS_CUDA(c, cudaMemsetAsync(q, 0, bytes, c->stream));
@@ -523,18 +697,21 @@ ls_status ls_init_fields(ls_ctx* c) {
 
 ls_status ls_init_frac(ls_ctx* c, unsigned long long* count) {
     if (!c) return LS_BAD_ARG;
+    snap_fence(c, kSnapAll);
     c->dz_no_threshold = 0;
     return init_frac_run(c, count);
 }
 
 ls_status ls_init_saturation(ls_ctx* c) {
     if (!c) return LS_BAD_ARG;
+    snap_fence(c, kSnapAll);
     return init_saturation_run(c);
 }
 
 // Simulation::initAcid, src/Simulation.cpp:285-310.
 ls_status ls_init_acid(ls_ctx* c) {
     if (!c) return LS_BAD_ARG;
+    snap_fence(c, kSnapAll);
     LS_CUDA(c, cudaMemsetAsync(c->acid, 0, sizeof(double) * (size_t)c->g.N, c->stream));
     c->acid_zero = 0;  // the plane beyond N keeps what it held
     return LS_OK;
@@ -676,8 +853,30 @@ ls_status ls_snapshot(ls_ctx* c) {
     Timed tm(c, LS_T_SNAPSHOT);
     size_t np = (size_t)c->g.NP, d8 = np * sizeof(double);
     cudaStream_t s = c->stream;
-    LS_CUDA(c, cudaMemcpyAsync(c->b_label, c->label, np * c->label_bytes, cudaMemcpyDeviceToDevice, s));
     LS_CUDA(c, cudaMemcpyAsync(c->b_frac, c->frac, np * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    if (c->lean) {
+        // to host memory on the snapshot stream, from the state the context's stream has
+        // reached here, in the order the step overwrites the fields (snap_fence)
+        snap_fence(c, kSnapAll);  // a previous snapshot's copies are done before these start
+        cudaStream_t ss = c->snap_stream;
+        LS_CUDA(c, cudaEventRecord(c->snap_ev[4], s));
+        LS_CUDA(c, cudaStreamWaitEvent(ss, c->snap_ev[4], 0));
+        LS_CUDA(c, cudaMemcpyAsync(c->b_P, c->P, d8, cudaMemcpyDefault, ss));
+        LS_CUDA(c, cudaEventRecord(c->snap_ev[0], ss));
+        for (auto pr : {std::make_pair(c->b_fx, c->fx), std::make_pair(c->b_fy, c->fy), std::make_pair(c->b_fz, c->fz)})
+            LS_CUDA(c, cudaMemcpyAsync(pr.first, pr.second, d8, cudaMemcpyDefault, ss));
+        LS_CUDA(c, cudaEventRecord(c->snap_ev[1], ss));
+        LS_CUDA(c, cudaMemcpyAsync(c->b_sat, c->sat, d8, cudaMemcpyDefault, ss));
+        LS_CUDA(c, cudaEventRecord(c->snap_ev[2], ss));
+        LS_CUDA(c, cudaMemcpyAsync(c->b_label, c->label, np * c->label_bytes, cudaMemcpyDefault, ss));
+        for (auto pr : {std::make_pair(c->b_conc, c->conc), std::make_pair(c->b_acid, c->acid),
+                        std::make_pair(c->b_precip, c->precip)})
+            LS_CUDA(c, cudaMemcpyAsync(pr.first, pr.second, d8, cudaMemcpyDefault, ss));
+        LS_CUDA(c, cudaEventRecord(c->snap_ev[3], ss));
+        c->snap_pending = kSnapAll;
+        return LS_OK;
+    }
+    LS_CUDA(c, cudaMemcpyAsync(c->b_label, c->label, np * c->label_bytes, cudaMemcpyDeviceToDevice, s));
     const std::pair<double*, double*> pairs[] = {
         {c->b_precip, c->precip}, {c->b_sat, c->sat}, {c->b_P, c->P}, {c->b_conc, c->conc},
         {c->b_acid, c->acid}, {c->b_fx, c->fx}, {c->b_fy, c->fy}, {c->b_fz, c->fz}};
@@ -692,12 +891,14 @@ ls_status ls_rollback(ls_ctx* c) {
         Timed tm(c, LS_T_SNAPSHOT);
         size_t np = (size_t)c->g.NP, d8 = np * sizeof(double);
         cudaStream_t s = c->stream;
-        LS_CUDA(c, cudaMemcpyAsync(c->label, c->b_label, np * c->label_bytes, cudaMemcpyDeviceToDevice, s));
-        LS_CUDA(c, cudaMemcpyAsync(c->frac, c->b_frac, np * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        snap_fence(c, kSnapAll);  // lean: the snapshot's copies to the host are done
+        const cudaMemcpyKind kind = c->lean ? cudaMemcpyDefault : cudaMemcpyDeviceToDevice;  // lean: from host
+        LS_CUDA(c, cudaMemcpyAsync(c->label, c->b_label, np * c->label_bytes, kind, s));
+        LS_CUDA(c, cudaMemcpyAsync(c->frac, c->b_frac, np * sizeof(float), kind, s));
         const std::pair<double*, double*> pairs[] = {
             {c->precip, c->b_precip}, {c->sat, c->b_sat}, {c->P, c->b_P}, {c->conc, c->b_conc},
             {c->acid, c->b_acid}, {c->fx, c->b_fx}, {c->fy, c->b_fy}, {c->fz, c->b_fz}};
-        for (auto& pr : pairs) LS_CUDA(c, cudaMemcpyAsync(pr.first, pr.second, d8, cudaMemcpyDeviceToDevice, s));
+        for (auto& pr : pairs) LS_CUDA(c, cudaMemcpyAsync(pr.first, pr.second, d8, kind, s));
     }
     c->p_ready = 0;
     c->p_eff_prev = 0.0;
@@ -745,11 +946,18 @@ ls_status ls_step(ls_ctx* c, double t, double dt, ls_step_info* info) {
         LS_TRY(ls_precip(c));
         {
             // the sweep keeps the acid it starts from in the pressure residual buffer (free
-            // between pressure solves) for the budget's consumed acid
+            // between pressure solves) for the budget's consumed acid; lean: the pressure
+            // arrays are released by now, and the first transport right-hand side is free
             Timed tm(c, LS_T_DISSOLVE);
+            double* acid_pre = c->pr;
+            if (c->lean) {
+                LS_TRY(lean_phase(c, kPhaseTransport));
+                if (!c->tb[0]) LS_TRY(walloc_t(c, &c->tb[0], (size_t)c->g.N));
+                acid_pre = c->tb[0];
+            }
             bool swept = false;
-            LS_TRY(dissolve_run(c, dt, &loc.leached, &loc.leaching, c->pr, &swept));
-            LS_TRY(budget_run(c, swept ? c->pr : nullptr, &loc.budget));
+            LS_TRY(dissolve_run(c, dt, &loc.leached, &loc.leaching, acid_pre, &swept));
+            LS_TRY(budget_run(c, swept ? acid_pre : nullptr, &loc.budget));
         }
     }
     loc.success = ok ? 1 : 0;

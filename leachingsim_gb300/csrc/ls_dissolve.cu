@@ -401,8 +401,7 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
     const int nlev = (g.I - 1) + 2 * (g.J - 1) + 3 * (g.K - 1) + 1;
     auto grow_cap = [&](int need) -> ls_status {
         if (c->dz_cap < need || !c->dz_list) {
-            if (c->dz_list) { cudaFree(c->dz_list); c->device_bytes -= sizeof(int) * (size_t)c->dz_cap; }
-            c->dz_list = nullptr;
+            dfree_t(c, &c->dz_list, (size_t)c->dz_cap);
             LS_TRY(dalloc_t(c, &c->dz_list, (size_t)need));
             c->dz_cap = need;
         }
@@ -464,11 +463,13 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
         LS_LAUNCH(c, k_dz_grow, grid, kBlock, 0, g, M, 0, -3);
         LS_LAUNCH(c, k_dz_grow, grid, kBlock, 0, g, M, -3, -4);
         if (c->dz_sel_cap < n_active) {
-            void* old[6] = {c->dz_sel, c->dz_flips, c->dz_save_frac, c->dz_save_precip, c->dz_save_conc,
-                            c->dz_save_label};
-            for (void* q : old)
-                if (q) cudaFree(q);
-            c->device_bytes -= (size_t)c->dz_sel_cap * (4 + 4 + 4 + 8 + 8 + c->label_bytes);
+            const size_t cap = (size_t)c->dz_sel_cap;
+            dfree_t(c, &c->dz_sel, cap);
+            dfree_t(c, &c->dz_flips, cap);
+            dfree_t(c, &c->dz_save_frac, cap);
+            dfree_t(c, &c->dz_save_precip, cap);
+            dfree_t(c, &c->dz_save_conc, cap);
+            dfree(c, &c->dz_save_label, cap * c->label_bytes);
             c->dz_sel_cap = 0;
             LS_TRY(dalloc_t(c, &c->dz_sel, (size_t)n_active));
             LS_TRY(dalloc_t(c, &c->dz_flips, (size_t)n_active));
@@ -544,6 +545,7 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
 
 ls_status dissolve_run(ls_ctx* c, double dt, int* leached, ls_substep_info* info, double* acid_pre,
                        bool* swept) {
+    snap_fence(c, kSnapRest);
     if (c->label_bytes == 1) return dissolve_t<uint8_t>(c, dt, leached, info, acid_pre, swept);
     return dissolve_t<uint16_t>(c, dt, leached, info, acid_pre, swept);
 }

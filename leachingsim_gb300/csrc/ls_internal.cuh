@@ -324,6 +324,7 @@ struct ls_ctx {
         void* b;            // T
         void* t;            // T
         void* kv[7];        // K-cycle vectors on this level (rr, za, zb, pd, q0, q1, e), T, or null
+        int esize;          // sizeof(T)
     };
     std::vector<MGLevel> mg;
     void* mg0_x;
@@ -343,6 +344,7 @@ struct ls_ctx {
     int lpc_active;                 // the learned cycle is in use in the current solve
     float *lpc_c0, *lpc_c1, *lpc_c2, *lpc_out;  // network grid: inputs, output channel 0
     float* lpc_isd;                 // learned level: 1/sqrt(diagonal) of served cells, else 0
+    long long lpc_isd_n;            // its length
     uint8_t* lpc_anchor;            // per component id: anchored on the learned level
     long long press_fallbacks;      // learned solves that fell back to the plain cycle
 
@@ -392,6 +394,20 @@ struct ls_ctx {
     double timer_bytes[LS_T_COUNT];
     unsigned long long initial_sulphide_count;
     size_t device_bytes;
+    size_t device_peak;   // most device_bytes held at once
+    size_t host_bytes;    // pinned (or pageable) host memory of the lean snapshot
+    int lean;             // LS_MEM_LEAN
+    // lean: the work arrays of the current phase (pressure or transport) are cut from one
+    // arena, reset at every phase switch and sized to the larger phase's need
+    void* arena;
+    size_t arena_size, arena_used, arena_overflow, arena_need;
+    int arena_phase;      // kPhase*
+    int b_host_pinned;    // lean: the snapshot arrays came from cudaHostAlloc (else malloc)
+    // lean: the snapshot's device-to-host copies run on their own stream, in the order the
+    // step first overwrites the fields; a phase that writes a field waits for its copy
+    cudaStream_t snap_stream;
+    cudaEvent_t snap_ev[5];  // [0..3] copies of the groups kSnap*, [4] the snapshot's start
+    int snap_pending;        // groups whose copies the main stream has not waited for
 };
 
 namespace ls {
@@ -541,6 +557,33 @@ ls_status init_saturation_run(ls_ctx* c);
 
 // allocation helper tracking device bytes
 ls_status dalloc(ls_ctx* c, void** p, size_t bytes);
+// releases an array of `bytes` bytes from dalloc (null: nothing); *p becomes null
+void dfree(ls_ctx* c, void** p, size_t bytes);
+template <typename T>
+void dfree_t(ls_ctx* c, T** p, size_t n) {
+    dfree(c, reinterpret_cast<void**>(p), n * sizeof(T));
+}
+// the work list holding every voxel 0 .. N-1 (the change-tracked kernels without change
+// tracking, LS_MEM_LEAN)
+ls_status wlist_all(ls_ctx* c);
+// Groups of snapshot fields (LS_MEM_LEAN), in the order a step first writes them: the
+// pressure, the fluxes, the saturation, then labels, conc, acid and precipitate.
+constexpr int kSnapP = 1, kSnapFlux = 2, kSnapSat = 4, kSnapRest = 8, kSnapAll = 15;
+// make the context's stream wait until the snapshot copies of `groups` are done (no-op when
+// none are pending)
+void snap_fence(ls_ctx* c, int groups);
+// Work arrays of one phase of the step (the pressure solve's or the transport solves'): in
+// LS_MEM_LEAN cut from the context's arena, which lean_phase resets; otherwise dalloc.
+ls_status walloc(ls_ctx* c, void** p, size_t bytes);
+template <typename T>
+ls_status walloc_t(ls_ctx* c, T** p, size_t n) {
+    return walloc(c, reinterpret_cast<void**>(p), n * sizeof(T));
+}
+// LS_MEM_LEAN: enter a phase; on a switch every work array of either phase is released and
+// the arena is reset (and grown to the largest need seen). No-op otherwise.
+constexpr int kPhaseNone = 0, kPhasePressure = 1, kPhaseTransport = 2;
+ls_status lean_phase(ls_ctx* c, int phase);
+void mg_free(ls_ctx* c);
 // the work list, its counter and the dirty flags, allocated on first use; resets the counter
 ls_status wlist_reset(ls_ctx* c);
 // finest-level array in slot `slot`: N elements of `esize` bytes with l0pad zero elements on

@@ -651,12 +651,12 @@ static ls_status lpc_prepare(ls_ctx* c) {
             ls_lpnet_destroy(c->lpc);
             c->lpc = nullptr;
         }
-        float** arrs[] = {&c->lpc_c0, &c->lpc_c1, &c->lpc_c2, &c->lpc_out, &c->lpc_isd};
-        for (float** q : arrs)
-            if (*q) {
-                cudaFree(*q);
-                *q = nullptr;
-            }
+        const size_t old_nn = (size_t)c->lpc_dims[0] * c->lpc_dims[1] * c->lpc_dims[2];
+        dfree_t(c, &c->lpc_c0, old_nn);
+        dfree_t(c, &c->lpc_c1, old_nn);
+        dfree_t(c, &c->lpc_c2, old_nn);
+        dfree_t(c, &c->lpc_out, old_nn);
+        dfree_t(c, &c->lpc_isd, (size_t)c->lpc_isd_n);
         ls_lpnet* n = nullptr;
         ls_status st = ls_lpnet_create(dims[0], dims[1], dims[2], 0, &n);
         if (st != LS_OK) return set_error(c, st, "learned pressure solver: network creation failed");
@@ -671,6 +671,7 @@ static ls_status lpc_prepare(ls_ctx* c) {
         LS_TRY(dalloc_t(c, &c->lpc_c2, nn));
         LS_TRY(dalloc_t(c, &c->lpc_out, nn));
         LS_TRY(dalloc_t(c, &c->lpc_isd, (size_t)lg.N));
+        c->lpc_isd_n = lg.N;
         for (int q = 0; q < 3; ++q) c->lpc_dims[q] = dims[q];
     }
     if (!c->lpc_anchor) LS_TRY(dalloc_t(c, &c->lpc_anchor, (size_t)c->g.N));
@@ -723,12 +724,13 @@ void mg_graphs_clear(ls_ctx* c) {
 
 void mg_free(ls_ctx* c) {
     mg_graphs_clear(c);
-    for (auto& lv : c->mg) {
-        void* lp[] = {lv.comp, lv.e, lv.face[0], lv.face[1], lv.face[2], lv.invd, lv.x, lv.b, lv.t};
-        for (void* q : lp)
-            if (q) cudaFree(q);
-        for (void* q : lv.kv)
-            if (q) cudaFree(q);
+    for (size_t m = 0; m < c->mg.size(); ++m) {
+        auto& lv = c->mg[m];
+        const size_t n = (size_t)lv.g.N, es = (size_t)lv.esize;
+        dfree_t(c, &lv.comp, n);
+        void** lp[] = {&lv.e, &lv.face[0], &lv.face[1], &lv.face[2], &lv.invd, &lv.x, &lv.b, &lv.t};
+        for (void** q : lp) dfree(c, q, es * n);
+        for (void*& q : lv.kv) dfree(c, &q, es * n);
     }
     c->mg.clear();
     l0_free(c, 10, &c->mg0_x);
@@ -741,7 +743,7 @@ static ls_status mg_alloc(ls_ctx* c) {
     const int is64 = sizeof(T) == 8;
     if (c->mg_is64 == is64) return LS_OK;
     mg_free(c);
-    if (!c->comp) LS_TRY(dalloc_t(c, &c->comp, (size_t)c->g.N));
+    if (!c->comp) LS_TRY(walloc_t(c, &c->comp, (size_t)c->g.N));
     if (!c->cc_flag) LS_TRY(dalloc_t(c, &c->cc_flag, (size_t)4));
     LS_TRY(l0_alloc(c, 10, sizeof(T), &c->mg0_x));
     LS_TRY(l0_alloc(c, 11, sizeof(T), &c->mg0_t));
@@ -751,10 +753,11 @@ static ls_status mg_alloc(ls_ctx* c) {
         Grid cg = coarse_of(g);
         ls_ctx::MGLevel lv = {};
         lv.g = cg;
-        LS_TRY(dalloc_t(c, &lv.comp, (size_t)cg.N));
+        lv.esize = (int)sizeof(T);
+        LS_TRY(walloc_t(c, &lv.comp, (size_t)cg.N));
         void** arrs[] = {&lv.e, &lv.face[0], &lv.face[1], &lv.face[2], &lv.invd, &lv.x, &lv.b, &lv.t};
         for (void** q : arrs) {
-            LS_TRY(dalloc(c, q, sizeof(T) * (size_t)cg.N));
+            LS_TRY(walloc(c, q, sizeof(T) * (size_t)cg.N));
             LS_CUDA(c, cudaMemsetAsync(*q, 0, sizeof(T) * (size_t)cg.N, c->stream));
         }
         c->mg.push_back(lv);
@@ -764,7 +767,7 @@ static ls_status mg_alloc(ls_ctx* c) {
     for (size_t m = 1; m <= (size_t)kKLevels && m < c->mg.size(); ++m) {
         auto& lv = c->mg[m - 1];
         for (void*& q : lv.kv) {
-            LS_TRY(dalloc(c, &q, sizeof(T) * (size_t)lv.g.N));
+            LS_TRY(walloc(c, &q, sizeof(T) * (size_t)lv.g.N));
             LS_CUDA(c, cudaMemsetAsync(q, 0, sizeof(T) * (size_t)lv.g.N, c->stream));
         }
     }

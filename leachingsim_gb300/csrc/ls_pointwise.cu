@@ -150,6 +150,22 @@ ls_status props_run(ls_ctx* c) {
     pc.k_clogged_pore = std::pow(10.0, (1.0 * pc.log_k_rock) + ((1.0 - 1.0) * pc.log_k_pore));
     pc.vg_n_is_2 = (c->p.vg_n == 2.0) ? 1 : 0;
     const size_t n = (size_t)c->g.N;
+    int grid = grid_for(c, c->g.N);
+    if (c->lean) {
+        // no change tracking: every voxel
+        c->props_force = 0;
+        LS_TRY(wlist_all(c));
+        if (c->label_bytes == 1)
+            LS_LAUNCH(c, k_props<uint8_t>, grid, kBlock, 0, pc, (const uint8_t*)c->label, c->sat, c->precip,
+                      c->frac, (const float*)c->kmult, c->kr, c->pc, c->perm, c->visc, (const int*)c->wlist,
+                      (const unsigned int*)c->wcount);
+        else
+            LS_LAUNCH(c, k_props<uint16_t>, grid, kBlock, 0, pc, (const uint16_t*)c->label, c->sat, c->precip,
+                      c->frac, (const float*)c->kmult, c->kr, c->pc, c->perm, c->visc, (const int*)c->wlist,
+                      (const unsigned int*)c->wcount);
+        c->p_ready = 0;
+        return LS_OK;
+    }
     if (!c->sh_sat) {
         LS_TRY(dalloc(c, &c->sh_label, n * c->label_bytes));
         LS_TRY(dalloc_t(c, &c->sh_sat, n));
@@ -159,7 +175,6 @@ ls_status props_run(ls_ctx* c) {
     }
     const int force = c->props_force;
     c->props_force = 0;
-    int grid = grid_for(c, c->g.N);
     LS_TRY(wlist_reset(c));
     if (c->label_bytes == 1) {
         LS_LAUNCH(c, k_props_scan<uint8_t>, grid, kBlock, 0, c->g, (const uint8_t*)c->label, c->sat, c->precip,
@@ -292,13 +307,24 @@ __global__ void __launch_bounds__(kBlock) k_flux(Grid g, DxDiv dd, double mcg, c
         const double qy = -transmissivity * (gPy - gCy);
         const double qz = -transmissivity * (gPz - gCz);
         fx[r] = qx; fy[r] = qy; fz[r] = qz;
-        sfx[r] = qx; sfy[r] = qy; sfz[r] = qz;
+        if (sfx) {  // null: no change tracking
+            sfx[r] = qx; sfy[r] = qy; sfz[r] = qz;
+        }
     }
 }
 
 ls_status flux_run(ls_ctx* c) {
+    snap_fence(c, kSnapFlux);
     int grid = grid_for(c, c->g.N);
     const size_t n = (size_t)c->g.N;
+    if (c->lean) {
+        // no change tracking: every voxel, no shadow copies
+        LS_TRY(wlist_all(c));
+        LS_LAUNCH(c, k_flux, grid, kBlock, 0, c->g, make_dxdiv(c->p.dx), c->p.max_cap_grad, c->P, c->pc,
+                  c->perm, c->visc, c->fx, c->fy, c->fz, (double*)nullptr, (double*)nullptr, (double*)nullptr,
+                  (const int*)c->wlist, (const unsigned int*)c->wcount);
+        return LS_OK;
+    }
     if (!c->shq_P) {
         double** arrs[] = {&c->shq_P, &c->shq_C, &c->shq_K, &c->shq_V, &c->shq_fx, &c->shq_fy, &c->shq_fz};
         for (double** q : arrs) LS_TRY(dalloc_t(c, q, n));
@@ -452,10 +478,11 @@ __global__ void __launch_bounds__(kBlock) k_sat_update_st(Grid g, double dt_sub_
 }
 
 ls_status saturation_run(ls_ctx* c, double dt, ls_substep_info* info) {
+    snap_fence(c, kSnapSat);
     const DxDiv dx = make_dxdiv(c->p.dx);
     const double evap = c->p.evaporative_flux;
     int grid = grid_for(c, c->g.N);
-    if (!c->sat_q) LS_TRY(dalloc_t(c, &c->sat_q, (size_t)c->g.N));
+    if (!c->sat_q) LS_TRY(walloc_t(c, &c->sat_q, (size_t)c->g.N));
     if (c->label_bytes == 1)
         LS_LAUNCH(c, k_sat_rate_st<uint8_t>, grid, kBlock, 0, c->g, dx, evap, (const uint8_t*)c->label,
                   c->fx, c->fy, c->fz, c->sat_q, c->partials);
@@ -518,6 +545,7 @@ __global__ void __launch_bounds__(kBlock) k_surface(Grid g, L* __restrict__ labe
 }
 
 ls_status surface_run(ls_ctx* c) {
+    snap_fence(c, kSnapRest);
     int grid = grid_for(c, c->g.N);
     if (c->label_bytes == 1)
         LS_LAUNCH(c, k_surface<uint8_t>, grid, kBlock, 0, c->g, (uint8_t*)c->label, c->sat, c->conc);
@@ -557,6 +585,7 @@ __global__ void __launch_bounds__(kBlock) k_precip(Grid g, double c_sat, int ins
 }
 
 ls_status precip_run(ls_ctx* c) {
+    snap_fence(c, kSnapRest);
     int grid = grid_for(c, c->g.N);
     const ls_params& p = c->p;
     if (c->label_bytes == 1)

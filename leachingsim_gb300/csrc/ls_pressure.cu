@@ -845,7 +845,23 @@ ls_status pressure_setup_run(ls_ctx* c, double t) {
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
     const size_t n = (size_t)g.N;
-    if (!c->shf_perm) {
+    if (c->lean) {
+        // every face and row afresh, in arrays that share memory with the transport's
+        LS_TRY(lean_phase(c, kPhasePressure));
+        double** rows[] = {&c->pdiag, &c->pb, &c->pface[0], &c->pface[1], &c->pface[2], &c->pisd, &c->pr,
+                           &c->pdelta, &c->psb2};
+        for (double** q : rows)
+            if (!*q) LS_TRY(walloc_t(c, q, n));
+        LS_TRY(wlist_all(c));
+        if (c->label_bytes == 1)
+            LS_LAUNCH(c, k_press_faces<uint8_t>, grid, kBlock, 0, g, (const uint8_t*)c->label, c->perm,
+                      c->visc, c->pface[0], c->pface[1], c->pface[2], (const int*)c->wlist,
+                      (const unsigned int*)c->wcount);
+        else
+            LS_LAUNCH(c, k_press_faces<uint16_t>, grid, kBlock, 0, g, (const uint16_t*)c->label, c->perm,
+                      c->visc, c->pface[0], c->pface[1], c->pface[2], (const int*)c->wlist,
+                      (const unsigned int*)c->wcount);
+    } else if (!c->shf_perm) {
         LS_TRY(dalloc(c, &c->shf_label, n * c->label_bytes));
         LS_TRY(dalloc_t(c, &c->shf_perm, n));
         LS_TRY(dalloc_t(c, &c->shf_visc, n));
@@ -857,29 +873,31 @@ ls_status pressure_setup_run(ls_ctx* c, double t) {
     const double rows_bc[3] = {(double)pcst.bc_mode, pcst.p_inlet, pcst.p_outlet};
     const int rows_force = (faces_force || c->rows_evap_dx != pcst.evap_dx ||
                             memcmp(rows_bc, c->rows_bc, sizeof(rows_bc)) != 0) ? 1 : 0;
-    LS_TRY(wlist_reset(c));
-    if (c->label_bytes == 1)
-        LS_LAUNCH(c, k_faces_dirty<uint8_t>, grid, kBlock, 0, g, (const uint8_t*)c->label, c->perm, c->visc,
-                  (uint8_t*)c->shf_label, c->shf_perm, c->shf_visc, c->dbits, faces_force);
-    else
-        LS_LAUNCH(c, k_faces_dirty<uint16_t>, grid, kBlock, 0, g, (const uint16_t*)c->label, c->perm, c->visc,
-                  (uint16_t*)c->shf_label, c->shf_perm, c->shf_visc, c->dbits, faces_force);
-    LS_LAUNCH(c, k_faces_scan, grid, kBlock, 0, g, (const unsigned int*)c->dbits, c->dwords, c->wlist,
-              c->wcount);
-    if (c->label_bytes == 1)
-        LS_LAUNCH(c, k_press_faces<uint8_t>, grid, kBlock, 0, g, (const uint8_t*)c->label, c->perm,
-                  c->visc, c->pface[0], c->pface[1], c->pface[2], (const int*)c->wlist,
-                  (const unsigned int*)c->wcount);
-    else
-        LS_LAUNCH(c, k_press_faces<uint16_t>, grid, kBlock, 0, g, (const uint16_t*)c->label, c->perm,
-                  c->visc, c->pface[0], c->pface[1], c->pface[2], (const int*)c->wlist,
-                  (const unsigned int*)c->wcount);
-    // rows: the same change bits (labels, faces), plus every Air row (boundary pressure)
-    LS_CUDA(c, cudaMemsetAsync(c->wcount, 0, sizeof(unsigned int), c->stream));
-    LS_LAUNCH(c, k_rows_scan, grid, kBlock, 0, g, (const unsigned int*)c->dbits, c->dwords,
-              c->label_bytes == 1 ? (const uint8_t*)c->label : (const uint8_t*)nullptr,
-              c->label_bytes == 2 ? (const uint16_t*)c->label : (const uint16_t*)nullptr, rows_force, c->wlist,
-              c->wcount);
+    if (!c->lean) {
+        LS_TRY(wlist_reset(c));
+        if (c->label_bytes == 1)
+            LS_LAUNCH(c, k_faces_dirty<uint8_t>, grid, kBlock, 0, g, (const uint8_t*)c->label, c->perm, c->visc,
+                      (uint8_t*)c->shf_label, c->shf_perm, c->shf_visc, c->dbits, faces_force);
+        else
+            LS_LAUNCH(c, k_faces_dirty<uint16_t>, grid, kBlock, 0, g, (const uint16_t*)c->label, c->perm, c->visc,
+                      (uint16_t*)c->shf_label, c->shf_perm, c->shf_visc, c->dbits, faces_force);
+        LS_LAUNCH(c, k_faces_scan, grid, kBlock, 0, g, (const unsigned int*)c->dbits, c->dwords, c->wlist,
+                  c->wcount);
+        if (c->label_bytes == 1)
+            LS_LAUNCH(c, k_press_faces<uint8_t>, grid, kBlock, 0, g, (const uint8_t*)c->label, c->perm,
+                      c->visc, c->pface[0], c->pface[1], c->pface[2], (const int*)c->wlist,
+                      (const unsigned int*)c->wcount);
+        else
+            LS_LAUNCH(c, k_press_faces<uint16_t>, grid, kBlock, 0, g, (const uint16_t*)c->label, c->perm,
+                      c->visc, c->pface[0], c->pface[1], c->pface[2], (const int*)c->wlist,
+                      (const unsigned int*)c->wcount);
+        // rows: the same change bits (labels, faces), plus every Air row (boundary pressure)
+        LS_CUDA(c, cudaMemsetAsync(c->wcount, 0, sizeof(unsigned int), c->stream));
+        LS_LAUNCH(c, k_rows_scan, grid, kBlock, 0, g, (const unsigned int*)c->dbits, c->dwords,
+                  c->label_bytes == 1 ? (const uint8_t*)c->label : (const uint8_t*)nullptr,
+                  c->label_bytes == 2 ? (const uint16_t*)c->label : (const uint16_t*)nullptr, rows_force, c->wlist,
+                  c->wcount);
+    }  // lean: the work list still holds every voxel
     if (c->label_bytes == 1)
         LS_LAUNCH(c, k_press_setup<uint8_t>, grid, kBlock, 0, g, pcst, (const uint8_t*)c->label, c->pkind,
                   c->pdiag, c->pb, c->psb2, c->pisd, (const double*)c->pface[0], (const double*)c->pface[1],
@@ -956,7 +974,7 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info, const float* s
         // anchored components
         LS_TRY(build_inner());
         inner_ready = true;
-        if (!c->start_anchor) LS_TRY(dalloc_t(c, &c->start_anchor, (size_t)g.N));
+        if (!c->start_anchor) LS_TRY(walloc_t(c, &c->start_anchor, (size_t)g.N));
         LS_CUDA(c, cudaMemsetAsync(c->start_anchor, 0, (size_t)g.N, c->stream));
         LS_LAUNCH(c, k_start_anchor<T>, grid, kBlock, 0, g, (const int*)c->comp, (const T*)c->ie,
                   (const T*)c->iface[0], (const T*)c->iface[1], (const T*)c->iface[2], c->start_anchor);
@@ -1077,6 +1095,7 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info, const float* s
 
 ls_status pressure_solve_run(ls_ctx* c, ls_solve_info* info, const float* start, double start_scale) {
     if (!c->p_ready) return set_error(c, LS_BAD_ARG, "pressure system not assembled");
+    snap_fence(c, kSnapP);
     // a supplied start is relative to the effective (ramped) top pressure
     const double sc = start ? start_scale * (c->p_eff > 0.0 ? c->p_eff : 1.0) : 0.0;
     if (c->p.press_solver == LS_PRESS_MIXED || c->p.press_solver == LS_PRESS_LEARNED) {

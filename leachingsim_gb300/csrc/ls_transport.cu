@@ -917,23 +917,25 @@ __global__ void k_zero_solid_flux(Grid g, const L* __restrict__ label, double* _
 
 static ls_status t_alloc(ls_ctx* c) {
     const size_t n = (size_t)c->g.N;
-    for (int q = 0; q < 7; ++q)
-        if (!c->tc[q]) LS_TRY(dalloc_t(c, &c->tc[q], n));
-    for (int q = 0; q < 2; ++q)
-        if (!c->tb[q]) LS_TRY(dalloc_t(c, &c->tb[q], n));
-    for (int q = 0; q < 6; ++q)
-        if (!c->to[q]) LS_TRY(dalloc_t(c, &c->to[q], n));
-    for (int q = 0; q < 2; ++q)
-        if (!c->trhs[q]) LS_TRY(dalloc_t(c, &c->trhs[q], n));
-    if (!c->tkind) LS_TRY(dalloc_t(c, &c->tkind, n));
-    if (!c->tinv) LS_TRY(dalloc_t(c, &c->tinv, n));
+    LS_TRY(lean_phase(c, kPhaseTransport));  // lean: the transport arrays take the pressure solve's memory
+    // largest first (lean: an arena sized for the other phase then wastes the least)
     if (!c->ti) {
         // 7 inner vectors of up to N float2 each, with `pad` elements on both sides
         c->ti_pad = ((c->g.JK + 31) / 32) * 32;
         c->ti_stride = ((2 * (c->g.N + 2 * c->ti_pad) + 63) / 64) * 64;
-        LS_TRY(dalloc_t(c, &c->ti, (size_t)c->ti_stride * 7));
+        LS_TRY(walloc_t(c, &c->ti, (size_t)c->ti_stride * 7));
         LS_CUDA(c, cudaMemsetAsync(c->ti, 0, sizeof(float) * (size_t)c->ti_stride * 7, c->stream));
     }
+    for (int q = 0; q < 7; ++q)
+        if (!c->tc[q]) LS_TRY(walloc_t(c, &c->tc[q], n));
+    for (int q = 0; q < 2; ++q)
+        if (!c->tb[q]) LS_TRY(walloc_t(c, &c->tb[q], n));
+    if (!c->tinv) LS_TRY(walloc_t(c, &c->tinv, n));
+    for (int q = 0; q < 6; ++q)
+        if (!c->to[q]) LS_TRY(walloc_t(c, &c->to[q], n));
+    for (int q = 0; q < 2; ++q)
+        if (!c->trhs[q]) LS_TRY(walloc_t(c, &c->trhs[q], n));
+    if (!c->tkind) LS_TRY(walloc_t(c, &c->tkind, n));
     if (!c->tcount) {
         LS_TRY(dalloc_t(c, &c->tcount, 1));
         LS_CUDA(c, cudaMemsetAsync(c->tcount, 0, sizeof(unsigned int), c->stream));
@@ -1052,7 +1054,7 @@ static ls_status mixed_solve(ls_ctx* c, const Rows<L>& rows, int nrhs, const dou
     const Grid g = c->g;
     const int grid = grid_for(c, g.N);
     TBuf tb = make_tbuf(c);
-    if (rows.mode == 0 && rows.tc.theta == 1.0) {
+    if (rows.mode == 0 && rows.tc.theta == 1.0 && !c->lean) {
         // fully implicit transport rows: recompute only the rows whose inputs changed
         const TransConst& tc = rows.tc;
         // the inflow values enter the right-hand sides only (k_t_rhs), not the rows
@@ -1234,6 +1236,7 @@ static ls_status transport_t(ls_ctx* c, double dt, int which, ls_solve_info* ci,
 }
 
 ls_status transport_run(ls_ctx* c, double dt, int which, ls_solve_info* ci, ls_solve_info* ai) {
+    snap_fence(c, kSnapRest | kSnapFlux);  // conc, acid; the fluxes of Rock and Precipitate are zeroed
     if (c->label_bytes == 1) return transport_t<uint8_t>(c, dt, which, ci, ai);
     return transport_t<uint16_t>(c, dt, which, ci, ai);
 }
@@ -1317,6 +1320,7 @@ static ls_status sat_implicit_t(ls_ctx* c, double dt, ls_solve_info* info) {
 }
 
 ls_status saturation_implicit_run(ls_ctx* c, double dt, ls_solve_info* info) {
+    snap_fence(c, kSnapSat);
     if (c->label_bytes == 1) return sat_implicit_t<uint8_t>(c, dt, info);
     return sat_implicit_t<uint16_t>(c, dt, info);
 }

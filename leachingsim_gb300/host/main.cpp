@@ -127,6 +127,9 @@ int main(int argc, char* argv[]) {
         op.add("pore_perm", "1e-12", "Intrinsic permeability of Air and clean Pore voxels (m^2)");
         op.add("rock_perm", "1e-18", "Intrinsic permeability of Rock voxels (m^2)");
         op.add("kmult_file", "", "float32 RAW file (k fastest) multiplying each voxel's intrinsic permeability");
+        op.add("lean", "false",
+               "Lean device layout for domains that do not fit otherwise: the pressure and transport solves "
+               "share work memory, no change tracking, the retry snapshot in host memory");
         op.add("dry-run", "false", "Parse the options, print the configuration and exit");
 
         for (int a = 1; a < argc; ++a) {
@@ -201,6 +204,7 @@ int main(int argc, char* argv[]) {
             sim.solver.acid_inlet = op.num("acid_inlet");
             sim.solver.pore_permeability = op.num("pore_perm");
             sim.solver.rock_permeability = op.num("rock_perm");
+            sim.solver.memory_mode = op.flag("lean") ? LS_MEM_LEAN : LS_MEM_RESIDENT;
         }
         {
             string ps = op.str("press_solver");

@@ -27,6 +27,8 @@ SYMBOLS = {
     "ls_stream": (C.c_void_p, [C.c_void_p]),
     "ls_synchronize": (C.c_int, [C.c_void_p]),
     "ls_device_bytes": (C.c_size_t, [C.c_void_p]),
+    "ls_device_peak_bytes": (C.c_size_t, [C.c_void_p]),
+    "ls_host_bytes": (C.c_size_t, [C.c_void_p]),
     "ls_upload_field": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_int]),
     "ls_download_field": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_int]),
     "ls_upload_field_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_int]),
@@ -523,6 +525,14 @@ class Context:
 
     def device_bytes(self):
         return int(load().ls_device_bytes(self.h))
+
+    def device_peak_bytes(self):
+        """The most device bytes held at once (memory_mode MEM_LEAN: reserved by its pool)."""
+        return int(load().ls_device_peak_bytes(self.h))
+
+    def host_bytes(self):
+        """Host bytes of the context (the snapshot of memory_mode MEM_LEAN)."""
+        return int(load().ls_host_bytes(self.h))
 
     # test hooks -------------------------------------------------------------
     def pressure_setup(self, t):

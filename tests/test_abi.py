@@ -33,7 +33,7 @@ def test_library_loads_and_exports_all_declared_symbols():
 
 
 def test_abi_version():
-    assert runtime.load().ls_abi_version() == 2
+    assert runtime.load().ls_abi_version() == 3
 
 
 def test_struct_layout_matches_header():
@@ -49,6 +49,7 @@ int main(void) {
   printf("%zu %zu\n", offsetof(ls_step_info, leached), offsetof(ls_step_info, success));
   printf("%zu %zu %zu %zu\n", offsetof(ls_params, bc_mode), offsetof(ls_params, rock_permeability),
          offsetof(ls_step_info, budget), sizeof(ls_budget));
+  printf("%zu %d %d\n", offsetof(ls_params, memory_mode), (int)LS_MEM_RESIDENT, (int)LS_MEM_LEAN);
   return 0;
 }
 '''
@@ -72,6 +73,8 @@ int main(void) {
     assert vals[10] == _abi.LsParams.rock_permeability.offset
     assert vals[11] == _abi.LsStepInfo.budget.offset
     assert vals[12] == C.sizeof(_abi.LsBudget)
+    assert vals[13] == _abi.LsParams.memory_mode.offset
+    assert (vals[14], vals[15]) == (_abi.MEM_RESIDENT, _abi.MEM_LEAN)
 
 
 def test_defaults_match_between_c_and_python():
