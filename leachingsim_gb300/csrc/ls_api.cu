@@ -141,6 +141,97 @@ __global__ void k_iota(long long n, int* __restrict__ list, unsigned int* __rest
     if (blockIdx.x == 0 && threadIdx.x == 0) *count = (unsigned int)n;
 }
 
+// Ordered compaction: block b takes the rows of chunk b (kOlistChunk consecutive rows), so the
+// list is the chunks' rows in ascending order: count per chunk, one-block exclusive scan,
+// then each block writes its chunk's rows tile by tile at its offset.
+constexpr int kOlistChunk = 8192;
+
+__device__ __forceinline__ int block_excl_scan(int v, int* total) {
+    __shared__ int ws[kBlock / 32];
+    const int lane = (int)(threadIdx.x & 31u), warp = (int)(threadIdx.x >> 5);
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < kBlock / 32 ? ws[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < kBlock / 32) ws[lane] = w;
+    }
+    __syncthreads();
+    const int before = (warp > 0 ? ws[warp - 1] : 0) + x - v;
+    *total = ws[kBlock / 32 - 1];
+    __syncthreads();
+    return before;
+}
+
+__global__ void __launch_bounds__(kBlock) k_olist_count(long long n, const int8_t* __restrict__ kind, int min_kind,
+                                                        int* __restrict__ counts) {
+    const long long lo = (long long)blockIdx.x * kOlistChunk;
+    const long long hi = lo + kOlistChunk < n ? lo + kOlistChunk : n;
+    int cnt = 0;
+    for (long long r = lo + threadIdx.x; r < hi; r += kBlock) cnt += (int)kind[r] >= min_kind ? 1 : 0;
+    int total = 0;
+    block_excl_scan(cnt, &total);
+    if (threadIdx.x == 0) counts[blockIdx.x] = total;
+}
+
+// counts[0 .. nb) -> exclusive offsets in place, counts[nb] = the total; one block
+__global__ void __launch_bounds__(kBlock) k_olist_scan(long long nb, int* __restrict__ counts,
+                                                       unsigned int* __restrict__ total_out) {
+    const long long per = (nb + kBlock - 1) / kBlock;
+    const long long lo = threadIdx.x * per, hi = lo + per < nb ? lo + per : nb;
+    int sum = 0;
+    for (long long q = lo; q < hi; ++q) sum += counts[q];
+    int total = 0;
+    int run = block_excl_scan(sum, &total);
+    for (long long q = lo; q < hi; ++q) {
+        const int v = counts[q];
+        counts[q] = run;
+        run += v;
+    }
+    if (threadIdx.x == 0) {
+        counts[nb] = total;
+        *total_out = (unsigned int)total;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_olist_fill(long long n, const int8_t* __restrict__ kind, int min_kind,
+                                                       const int* __restrict__ offsets, int* __restrict__ list) {
+    const long long lo = (long long)blockIdx.x * kOlistChunk;
+    const long long hi = lo + kOlistChunk < n ? lo + kOlistChunk : n;
+    int run = offsets[blockIdx.x];
+    for (long long base = lo; base < hi; base += kBlock) {  // block-uniform trip count
+        const long long r = base + threadIdx.x;
+        const int pred = (r < hi && (int)kind[r] >= min_kind) ? 1 : 0;
+        int total = 0;
+        const int at = block_excl_scan(pred, &total);
+        if (pred) list[run + at] = (int)r;
+        run += total;
+    }
+}
+
+ls_status ordered_list(ls_ctx* c, const int8_t* kind, int min_kind) {
+    LS_TRY(wlist_reset(c));
+    const long long nb = (c->g.N + kOlistChunk - 1) / kOlistChunk;
+    if (!c->olist_counts) {
+        LS_TRY(dalloc_t(c, &c->olist_counts, (size_t)nb + 1));
+        c->olist_nb = nb;
+    }
+    LS_LAUNCH(c, k_olist_count, (int)nb, kBlock, 0, c->g.N, kind, min_kind, c->olist_counts);
+    LS_LAUNCH(c, k_olist_scan, 1, kBlock, 0, nb, c->olist_counts, c->wcount);
+    LS_LAUNCH(c, k_olist_fill, (int)nb, kBlock, 0, c->g.N, kind, min_kind, (const int*)c->olist_counts, c->wlist);
+    return LS_OK;
+}
+
 ls_status wlist_all(ls_ctx* c) {
     LS_TRY(wlist_reset(c));
     LS_LAUNCH(c, k_iota, grid_for(c, c->g.N), kBlock, 0, c->g.N, c->wlist, c->wcount);
@@ -208,6 +299,7 @@ ls_status lean_phase(ls_ctx* c, int phase) {
 
 ls_status wlist_reset(ls_ctx* c) {
     const size_t n = (size_t)c->g.N;
+    c->plist_valid = 0;
     if (!c->wlist) LS_TRY(dalloc_t(c, &c->wlist, n));
     if (!c->wcount) LS_TRY(dalloc_t(c, &c->wcount, 4));
     if (!c->dbits) {
@@ -551,7 +643,7 @@ ls_status ls_destroy(ls_ctx* c) {
                     c->sh_label, c->sh_sat, c->sh_precip, c->sh_frac, c->shf_label, c->shf_perm,
                     c->shf_visc, c->psb2, c->sat_q, c->dbits, c->sht_label, c->sht_fx, c->sht_fy, c->sht_fz,
                     c->shq_P, c->shq_C, c->shq_K, c->shq_V, c->shq_fx, c->shq_fy, c->shq_fz,
-                    c->wlist, c->wcount, c->kmult, c->dz_sel, c->dz_flips, c->dz_save_frac,
+                    c->wlist, c->wcount, c->olist_counts, c->kmult, c->dz_sel, c->dz_flips, c->dz_save_frac,
                     c->dz_save_precip, c->dz_save_conc, c->dz_save_label};
     for (void* q : ptrs) rel(q);
     for (void* q : c->l0base) rel(q);

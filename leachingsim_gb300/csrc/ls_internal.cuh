@@ -105,6 +105,37 @@ __device__ __forceinline__ bool dpos(double x) {  // x > 0
     return b > 0 && b <= 0x7ff0000000000000ll;
 }
 
+// Maxima of doubles on the integer pipe: an order-preserving map of the bit pattern to a
+// signed 64-bit key (x < y iff key(x) < key(y); -0.0 and +0.0 both map to the key of +0.0;
+// NaN is the caller's to skip). kKeyNegInf is the key of -Inf, the start of a maximum.
+constexpr long long kKeyNegInf = -1ll - 0x7ff0000000000000ll;
+__device__ __forceinline__ long long dkey_bits(long long b) {
+    if (b == (long long)0x8000000000000000ull) b = 0;
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffll);
+}
+__device__ __forceinline__ long long dkey(double x) { return dkey_bits(__double_as_longlong(x)); }
+__device__ __forceinline__ long long dkey_neg(double x) {  // key(-x)
+    return dkey_bits(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+}
+__device__ __forceinline__ double dunkey(long long k) {
+    return __longlong_as_double(k >= 0 ? k : (k ^ 0x7fffffffffffffffll));
+}
+
+// float -> double, exact, on the integer pipe for normal, zero, infinite and NaN values
+// (subnormal floats take the FP64 conversion)
+__device__ __forceinline__ double f2d_exact(float f) {
+    const unsigned int u = __float_as_uint(f);
+    const unsigned int e = (u >> 23) & 0xffu;
+    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+    const unsigned long long man = (unsigned long long)(u & 0x7fffffu) << 29;
+    if (e == 0) {
+        if ((u & 0x7fffffu) == 0) return __longlong_as_double((long long)sign);
+        return (double)f;
+    }
+    if (e == 0xffu) return __longlong_as_double((long long)(sign | 0x7ff0000000000000ull | man));
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 896u) << 52) | man));
+}
+
 // double -> float rounded toward zero (|x| < 2^-126 -> +-0, |x| >= 2^128 -> +-Inf, NaN ->
 // NaN); for FP32 copies whose rounding does not matter.
 __device__ __forceinline__ float d2f_rz(double x) {
@@ -299,6 +330,9 @@ struct ls_ctx {
     unsigned int* dbits;  // dirty bits of the change tests: two planes of dwords words
     long long dwords;     // ceil(N / 32)
     int* wlist;           // voxel work list of the change-tracked kernels (N entries)
+    int* olist_counts;    // per-chunk counts / offsets of ordered_list (olist_nb + 1 ints)
+    long long olist_nb;
+    int plist_valid;      // wlist holds the ascending list of the pressure unknowns (kind >= 2)
     unsigned int* wcount; // its length
     int props_force, faces_force;  // recompute every voxel on the next call
     void* sht_label;      // transport-row inputs at the last evaluation (fully implicit rows)
@@ -563,6 +597,9 @@ template <typename T>
 void dfree_t(ls_ctx* c, T** p, size_t n) {
     dfree(c, reinterpret_cast<void**>(p), n * sizeof(T));
 }
+// The ascending list of the rows r < N with kind[r] >= min_kind into wlist / wcount (a
+// deterministic order, so that reductions over it are reproducible).
+ls_status ordered_list(ls_ctx* c, const int8_t* kind, int min_kind);
 // the work list holding every voxel 0 .. N-1 (the change-tracked kernels without change
 // tracking, LS_MEM_LEAN)
 ls_status wlist_all(ls_ctx* c);

@@ -424,29 +424,68 @@ __global__ void __launch_bounds__(kBlock) k_sat_update(Grid g, DxDiv dd, double 
 
 // The context path of the update: the rate pass stores div q + evaporative sink of every
 // active voxel (the update applies that same sum in every sub-step), so the update pass does
-// no flux arithmetic.
+// no flux arithmetic. The rate pass runs over the list of the active (Pore) voxels: warps
+// of active voxels only. div q in fewer FP64 operations, with the same value: the six face
+// means are (f + f_nb) * 0.5 and every sum and difference of them is exact up to rounding
+// that commutes with the exact halving (no result is subnormal: fluxes are far above
+// 2^-1022), so ((A+ - A-) + (B+ - B-)) + (C+ - C-), halved once, equals the sum of the halved
+// differences bit for bit; with dx a power of two the halving and 1/dx are one exact scaling.
 template <typename L>
-__global__ void __launch_bounds__(kBlock) k_sat_rate_st(Grid g, DxDiv dd, double evap,
-                                                        const L* __restrict__ label,
-                                                        const double* __restrict__ fx,
-                                                        const double* __restrict__ fy,
-                                                        const double* __restrict__ fz,
-                                                        double* __restrict__ qsum,
-                                                        double* __restrict__ partials) {
+__global__ void __launch_bounds__(kBlock) k_sat_rate_list(Grid g, DxDiv dd, double evap,
+                                                          const L* __restrict__ label,
+                                                          const double* __restrict__ fx,
+                                                          const double* __restrict__ fy,
+                                                          const double* __restrict__ fz,
+                                                          const int* __restrict__ list,
+                                                          const unsigned int* __restrict__ count,
+                                                          double* __restrict__ qsum,
+                                                          double* __restrict__ partials) {
     double v[1] = {0.0};
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
-         r += (long long)gridDim.x * blockDim.x) {
-        int t = (int)label[r];
-        if (sat_inactive(t)) continue;
+    const long long n = (long long)*count;
+    const double half_scale = dd.pow2 ? 0.5 * dd.inv_dx : 0.5;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+         q += (long long)gridDim.x * blockDim.x) {
+        const long long r = list[q];
+        const int t = (int)label[r];
         int i, j, k;
         decode(g, r, i, j, k);
-        double div_q, evap_sink;
-        sat_rates(g, label, fx, fy, fz, r, i, j, k, t, dd, evap, div_q, evap_sink);
+        const double fxr = fx[r], fyr = fy[r], fzr = fz[r];
+        const double ap = (i + 1 < g.I) ? fxr + fx[r + g.JK] : 0.0;
+        const double am = (i > 0) ? fxr + fx[r - g.JK] : 0.0;
+        const double bp = (j + 1 < g.J) ? fyr + fy[r + g.K] : 0.0;
+        const double bm = (j > 0) ? fyr + fy[r - g.K] : 0.0;
+        const double cp = (k + 1 < g.K) ? fzr + fz[r + 1] : 0.0;
+        const double cm = (k > 0) ? fzr + fz[r - 1] : 0.0;
+        const double sum = ((ap - am) + (bp - bm)) + (cp - cm);
+        const double div_q = dd.pow2 ? sum * half_scale : (sum * 0.5) / dd.dx;
+        double evap_sink = 0.0;
+        if (t == kPore && __double_as_longlong(evap) != 0) {
+            int air_faces = 0;
+            if (i + 1 < g.I && (int)label[r + g.JK] == kAir) air_faces++;
+            if (i > 0 && (int)label[r - g.JK] == kAir) air_faces++;
+            if (j + 1 < g.J && (int)label[r + g.K] == kAir) air_faces++;
+            if (j > 0 && (int)label[r - g.K] == kAir) air_faces++;
+            if (k + 1 < g.K && (int)label[r + 1] == kAir) air_faces++;
+            if (k > 0 && (int)label[r - 1] == kAir) air_faces++;
+            evap_sink = dd.div(air_faces * evap);
+        }
         qsum[r] = div_q + evap_sink;
-        double total_rate = fabs(div_q) + evap_sink;
+        const double total_rate = fabs(div_q) + evap_sink;
         if (total_rate > v[0]) v[0] = total_rate;
     }
     block_max_store<1>(v, partials);
+}
+
+__global__ void __launch_bounds__(kBlock) k_active_list_sat(Grid g, const uint8_t* __restrict__ l8,
+                                                            const uint16_t* __restrict__ l16,
+                                                            int* __restrict__ list, unsigned int* __restrict__ count) {
+    // block-uniform trip count (block_append is called by every thread of the block)
+    for (long long b0 = (long long)blockIdx.x * blockDim.x; b0 < g.N; b0 += (long long)gridDim.x * blockDim.x) {
+        const long long r = b0 + threadIdx.x;
+        bool act = false;
+        if (r < g.N) act = !sat_inactive(l8 ? (int)l8[r] : (int)l16[r]);
+        block_append(act, (int)r, list, count);
+    }
 }
 
 template <typename L>
@@ -483,12 +522,17 @@ ls_status saturation_run(ls_ctx* c, double dt, ls_substep_info* info) {
     const double evap = c->p.evaporative_flux;
     int grid = grid_for(c, c->g.N);
     if (!c->sat_q) LS_TRY(walloc_t(c, &c->sat_q, (size_t)c->g.N));
+    // the active voxels (any order: the pass writes per voxel and takes a maximum)
+    LS_TRY(wlist_reset(c));
+    LS_LAUNCH(c, k_active_list_sat, grid, kBlock, 0, c->g,
+              c->label_bytes == 1 ? (const uint8_t*)c->label : (const uint8_t*)nullptr,
+              c->label_bytes == 2 ? (const uint16_t*)c->label : (const uint16_t*)nullptr, c->wlist, c->wcount);
     if (c->label_bytes == 1)
-        LS_LAUNCH(c, k_sat_rate_st<uint8_t>, grid, kBlock, 0, c->g, dx, evap, (const uint8_t*)c->label,
-                  c->fx, c->fy, c->fz, c->sat_q, c->partials);
+        LS_LAUNCH(c, k_sat_rate_list<uint8_t>, grid, kBlock, 0, c->g, dx, evap, (const uint8_t*)c->label,
+                  c->fx, c->fy, c->fz, (const int*)c->wlist, (const unsigned int*)c->wcount, c->sat_q, c->partials);
     else
-        LS_LAUNCH(c, k_sat_rate_st<uint16_t>, grid, kBlock, 0, c->g, dx, evap, (const uint16_t*)c->label,
-                  c->fx, c->fy, c->fz, c->sat_q, c->partials);
+        LS_LAUNCH(c, k_sat_rate_list<uint16_t>, grid, kBlock, 0, c->g, dx, evap, (const uint16_t*)c->label,
+                  c->fx, c->fy, c->fz, (const int*)c->wlist, (const unsigned int*)c->wcount, c->sat_q, c->partials);
     LS_TRY(finalize_max(c, grid, 1, S_RED0));
     double max_div_q = 0.0;
     LS_TRY(read_scalars(c, S_RED0, 1, &max_div_q));
@@ -613,21 +657,34 @@ __global__ void __launch_bounds__(kBlock) k_budget(Grid g, const L* __restrict__
                                                    const double* __restrict__ precip,
                                                    const double* __restrict__ acid_pre,
                                                    double* __restrict__ partials) {
+    // FP64 issue is what bounds this pass, so terms that add nothing are skipped on the integer
+    // side: a sum that starts at +0.0 never becomes -0.0, so adding +-0.0 leaves it as it is,
+    // and x - x = +0.0 (an unchanged voxel's consumed acid or lost mineral). The counts are
+    // integers and the FP32 fractions widen exactly on the integer pipe.
     double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    long long n_sul = 0, n_pre = 0;
+    const long long kMag = 0x7fffffffffffffffll;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
         const double a = acid[r];
-        const float f = frac[r];
-        acc[0] += conc[r];
-        acc[1] += a;
-        acc[2] += (double)f;
-        acc[3] += precip[r];
-        if (acid_pre) acc[4] += acid_pre[r] - a;
-        acc[5] += (double)frac0[r] - (double)f;
+        const double cv = conc[r], pv = precip[r];
+        const float f = frac[r], f0 = frac0[r];
+        const double fd = f2d_exact(f);
+        if (__double_as_longlong(cv) & kMag) acc[0] += cv;
+        if (__double_as_longlong(a) & kMag) acc[1] += a;
+        if (__float_as_uint(f) & 0x7fffffffu) acc[2] += fd;
+        if (__double_as_longlong(pv) & kMag) acc[3] += pv;
+        if (acid_pre) {
+            const double ap = acid_pre[r];
+            if (__double_as_longlong(ap) != __double_as_longlong(a)) acc[4] += ap - a;
+        }
+        if (__float_as_uint(f0) != __float_as_uint(f)) acc[5] += f2d_exact(f0) - fd;
         const int t = (int)label[r];
-        acc[6] += (t == kSulphide) ? 1.0 : 0.0;
-        acc[7] += (t == kPrecipitate) ? 1.0 : 0.0;
+        n_sul += (t == kSulphide) ? 1 : 0;
+        n_pre += (t == kPrecipitate) ? 1 : 0;
     }
+    acc[6] = (double)n_sul;
+    acc[7] = (double)n_pre;
     block_sum_store<8>(acc, partials);
 }
 

@@ -497,47 +497,67 @@ __global__ void k_press_apply_full(Grid g, const int8_t* __restrict__ kind,
     }
 }
 
-// Outer residual r = b - A x on Pore rows (0 elsewhere) with the scaled norm, NaN count
-// and the max / -min of x.
-__global__ void __launch_bounds__(kBlock) k_press_residual(Grid g, const int8_t* __restrict__ kind,
-                                                           const double* __restrict__ diag,
-                                                           const double* __restrict__ isd,
-                                                           const double* __restrict__ b,
-                                                           const double* __restrict__ f0,
-                                                           const double* __restrict__ f1,
-                                                           const double* __restrict__ f2,
-                                                           const double* __restrict__ x,
-                                                           double* __restrict__ res,
-                                                           double* __restrict__ partials,
-                                                           double* __restrict__ partials_max,
-                                                           int nblk) {
+// The residual pass in two parts. k_press_xstat, over all rows: the block maxima of x and -x
+// (the log line's min / max), the NaN count of x, and res = 0 on the rows that are not
+// unknowns. k_press_resid_list, over the ascending list of the unknowns (kind >= 2, about a
+// quarter of the rows): res, (r / diag)^2 and its NaN count. The FP64 row work thus runs in
+// warps of unknowns only (a grid-stride pass over all rows issues it for every warp holding
+// one unknown). Both write per-block partials (norm, NaN count) into their own halves of one
+// array, summed in a fixed order.
+__global__ void __launch_bounds__(kBlock) k_press_xstat(Grid g, const int8_t* __restrict__ kind,
+                                                        const double* __restrict__ x, double* __restrict__ res,
+                                                        double* __restrict__ partials,
+                                                        double* __restrict__ partials_max) {
     double acc[2] = {0.0, 0.0};
-    double mx[2] = {-INFINITY, -INFINITY};
+    long long k0 = kKeyNegInf, k1 = kKeyNegInf;  // maxima of x and -x, as integer keys
+    int nans = 0;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
-        int kd = kind[r];
-        double xv = x[r];
-        mx[0] = smax(mx[0], xv);
-        mx[1] = smax(mx[1], -xv);
-        if (disnan(xv)) acc[1] += 1.0;
-        double rv = 0.0;
-        if (kd >= 2) {
-            int i, j, k;
-            decode(g, r, i, j, k);
-            double dg = diag[r];
-            rv = b[r] - press_row_apply_fma(g, r, i, j, k, dg, x, f0, f1, f2);
-            // (r / diag)^2 without an FP64 division: 1/diag^2 = isd^4 for normal rows
-            double id2 = (kd == 2) ? isd[r] : 1e16;  // 1/|diag|; floored rows: diag = 1e-16
-            const double wr = rv * id2;
-            acc[0] = __fma_rn(wr, wr, acc[0]);
-            if (disnan(rv)) acc[1] += 1.0;
+        const double xv = x[r];
+        if (disnan(xv)) {
+            ++nans;
+        } else {
+            k0 = max(k0, dkey(xv));
+            k1 = max(k1, dkey_neg(xv));
         }
-        res[r] = rv;
+        if (kind[r] < 2) res[r] = 0.0;
     }
+    acc[1] = (double)nans;
+    double mx[2] = {dunkey(k0), dunkey(k1)};
     block_sum_store<2>(acc, partials);
     __syncthreads();
     block_max_store<2>(mx, partials_max);
-    (void)nblk;
+}
+
+__global__ void __launch_bounds__(kBlock) k_press_resid_list(Grid g, const int8_t* __restrict__ kind,
+                                                             const double* __restrict__ diag,
+                                                             const double* __restrict__ isd,
+                                                             const double* __restrict__ b,
+                                                             const double* __restrict__ f0,
+                                                             const double* __restrict__ f1,
+                                                             const double* __restrict__ f2,
+                                                             const double* __restrict__ x,
+                                                             const int* __restrict__ list,
+                                                             const unsigned int* __restrict__ count,
+                                                             double* __restrict__ res,
+                                                             double* __restrict__ partials) {
+    double acc[2] = {0.0, 0.0};
+    const long long n = (long long)*count;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+         q += (long long)gridDim.x * blockDim.x) {
+        const long long r = list[q];
+        const int kd = kind[r];
+        int i, j, k;
+        decode(g, r, i, j, k);
+        const double rv = b[r] - press_row_apply_fma(g, r, i, j, k, diag[r], x, f0, f1, f2);
+        // (r / diag)^2 without an FP64 division: 1/|diag| = isd for normal rows
+        const double id2 = (kd == 2) ? isd[r] : 1e16;  // floored rows: diag = 1e-16
+        const double wr = rv * id2;
+        acc[0] = __fma_rn(wr, wr, acc[0]);
+        if (disnan(rv)) acc[1] += 1.0;
+        res[r] = rv;
+    }
+    block_sum_store<2>(acc, partials);
 }
 
 // Correction for floored rows and the inner right-hand side
@@ -910,6 +930,9 @@ ls_status pressure_setup_run(ls_ctx* c, double t) {
     memcpy(c->rows_bc, rows_bc, sizeof(rows_bc));
     LS_LAUNCH(c, k_press_den, grid, kBlock, 0, g, (const double*)c->psb2, c->partials);
     LS_TRY(finalize_sum(c, grid, 1, SP_DEN));
+    // the unknowns, for the residual passes of the solve
+    LS_TRY(ordered_list(c, (const int8_t*)c->pkind, 2));
+    c->plist_valid = 1;
     c->p_t = t;
     c->p_ready = 1;
     return LS_OK;
@@ -1002,11 +1025,17 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info, const float* s
         double sc[2] = {0.0, 0.0};
         {
             Timed tm(c, LS_T_PRESS_OUTER);
-            LS_LAUNCH(c, k_press_residual, grid, kBlock, 0, g, (const int8_t*)c->pkind,
-                      (const double*)c->pdiag, (const double*)c->pisd, (const double*)c->pb, (const double*)c->pface[0],
+            if (!c->plist_valid) {
+                LS_TRY(ordered_list(c, (const int8_t*)c->pkind, 2));
+                c->plist_valid = 1;
+            }
+            LS_LAUNCH(c, k_press_xstat, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const double*)x, c->pr,
+                      c->partials, pmax);
+            LS_LAUNCH(c, k_press_resid_list, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const double*)c->pdiag,
+                      (const double*)c->pisd, (const double*)c->pb, (const double*)c->pface[0],
                       (const double*)c->pface[1], (const double*)c->pface[2], (const double*)x,
-                      c->pr, c->partials, pmax, grid);
-            LS_TRY(finalize_sum(c, grid, 2, SP_NUM));
+                      (const int*)c->wlist, (const unsigned int*)c->wcount, c->pr, c->partials + 2 * grid);
+            LS_TRY(finalize_sum(c, 2 * grid, 2, SP_NUM));
         }
         LS_TRY(read_scalars(c, SP_NUM, 2, sc));
         if (sc[1] > 0.0 || sc[0] != sc[0]) {
@@ -1071,7 +1100,7 @@ static ls_status pressure_solve_t(ls_ctx* c, ls_solve_info* info, const float* s
     }
     // min / max of the solution vector for the log line
     double mm[2] = {0.0, 0.0};
-    // k_press_residual left the block maxima of x and -x in pmax
+    // k_press_xstat left the block maxima of x and -x in pmax
     LS_LAUNCH(c, k_finalize<true>, 2, kFinalizeThreads, 0, pmax, grid, 2, c->scal + SP_XMAX);
     LS_TRY(read_scalars(c, SP_XMAX, 2, mm));
     if (result == LS_OK) c->p_eff_prev = c->p_eff;

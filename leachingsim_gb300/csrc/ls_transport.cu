@@ -394,15 +394,17 @@ __global__ void __launch_bounds__(kBlock) k_t_resid(Grid g, TBuf tb, double* x0,
         int i, j, k;
         decode(g, r, i, j, k);
         const double inv = tb.inv[r];
+        // the inner right-hand side in FP32 rounded toward zero on the integer pipe (its
+        // rounding is the inner solve's business; the FP64 pipe bounds this pass)
         if (mask & 1) {
             double rv = (tb.b[0][r] - t_row_apply(g, tb, r, i, j, k, x0)) * inv;
-            r0[r] = (float)rv;
+            r0[r] = d2f_rz(rv);
             acc[0] = __fma_rn(rv, rv, acc[0]);
             if (disnan(rv)) acc[2] += 1.0;
         }
         if (mask & 2) {
             double rv = (tb.b[1][r] - t_row_apply(g, tb, r, i, j, k, x1)) * inv;
-            r1[r] = (float)rv;
+            r1[r] = d2f_rz(rv);
             acc[1] = __fma_rn(rv, rv, acc[1]);
             if (disnan(rv)) acc[3] += 1.0;
         }
@@ -893,13 +895,15 @@ __global__ void __launch_bounds__(kFinalizeThreads) k_ti_fin(const double* __res
 // min / max of x over the rows
 __global__ void __launch_bounds__(kBlock) k_minmax(Grid g, const double* __restrict__ x,
                                                    double* __restrict__ partials) {
-    double m[2] = {-INFINITY, -INFINITY};
+    long long k0 = kKeyNegInf, k1 = kKeyNegInf;  // maxima of x and -x (NaN skipped), as integer keys
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
-        double v = x[r];
-        m[0] = smax(m[0], v);
-        m[1] = smax(m[1], -v);
+        const double v = x[r];
+        if (disnan(v)) continue;
+        k0 = max(k0, dkey(v));
+        k1 = max(k1, dkey_neg(v));
     }
+    double m[2] = {dunkey(k0), dunkey(k1)};
     block_max_store<2>(m, partials);
 }
 
