@@ -412,13 +412,18 @@ def gpu_arm(args, ws, rank, local):
         h2d = N
         d2h = 0
         te, ne = 0.0, 0
+        pending = None
         for _ in range(nsteps):
             te, ne, _ = run_steps(ctx, te, ne, 1, DT)
             if (ne - 1) % NOUT == 0:
                 ctx.props()   # property sync before output (src/main.cpp:491-494)
-                for f in OUTPUT_FIELDS:
-                    ctx.download(f, out=out_bufs[f])
-                    d2h += out_bufs[f].nbytes
+                if pending is not None:
+                    pending.wait()  # the previous output's copies (long done) before reusing its buffers
+                # the copies drain on the context's copy stream while the next steps run
+                pending = ctx.download_async(OUTPUT_FIELDS, [out_bufs[f] for f in OUTPUT_FIELDS])
+                d2h += sum(out_bufs[f].nbytes for f in OUTPUT_FIELDS)
+        if pending is not None:
+            pending.wait()
         ctx.synchronize()
         e2e_wall = time.perf_counter() - w0
         ctx.close()
@@ -426,7 +431,9 @@ def gpu_arm(args, ws, rank, local):
         e2e = {"value": round(replica_rate(ws, nsteps, e2e_wall), 4), "unit": UNIT,
                "h2d_bytes_per_step": int(h2d / nsteps), "d2h_bytes_per_step": int(d2h / nsteps),
                "steps": nsteps, "wall_s": round(e2e_wall, 3),
-               "note": "fresh run from a pinned host label image, every nout-th step's fields read back to pinned host memory"}
+               "note": ("fresh run from a pinned host label image, every nout-th step's fields read back to "
+                        "pinned host memory (copies on the context's copy stream, overlapping the next "
+                        "steps; all landed before the clock stops)")}
 
     flow = None if args.no_flow else flow_run(args, shape, ws, barrier)
     if rank != 0:
@@ -871,6 +878,80 @@ def mixed_arm(args):
 
 
 # ---------------------------------------------------------------------------
+# The learned preconditioner over a long run: the flow-through model on the workload's grid,
+# acid flowing in so that dissolution changes the permeability every step.
+
+C4_STEPS = 200
+
+
+def c4_arm(args):
+    """tmax = 200 steps (dt 1) of the flow-through model at 338x338x283 from the same fresh
+    state, once per pressure solver: the learned coarse solver inside the flexible CG with the
+    plain cycle as fallback (press_solver LEARNED), the plain mixed-precision K-cycle FCG, and
+    the plain FP64 multigrid-PCG; per arm the pressure solve's device time per step (assembly,
+    setup, inner and refinement timers), its iterations, the fallbacks and the whole run's
+    steps/s."""
+    import torch
+    from leachingsim_gb300 import learned as L
+    from leachingsim_gb300._abi import PRESS_FP64, PRESS_LEARNED, PRESS_MIXED
+    from leachingsim_gb300.geometry import grf_geometry
+    from leachingsim_gb300.runtime import Context
+    torch.cuda.set_device(0)
+    shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else SHAPE
+    steps = args.steps if args.steps != 40 else C4_STEPS
+    lab, seed = grf_geometry(shape, air_inlet=False, **GEOM)
+    pw = L.load_precond_weights()
+    arms = {}
+    for name, solver in (("learned_precond", PRESS_LEARNED), ("plain_mixed", PRESS_MIXED), ("plain_fp64", PRESS_FP64)):
+        if solver == PRESS_LEARNED and pw is None:
+            arms[name] = None
+            continue
+        p = flow_params("fp64" if solver == PRESS_FP64 else "mixed")
+        p.press_solver = solver
+        ctx = Context(shape, label_bytes=1, params=p)
+        if solver == PRESS_LEARNED:
+            ctx.set_precond_weights(pw)
+        ctx.upload("label", lab)
+        ctx.init_all()
+        ctx.timing(True)
+        per_step, its = [], []
+        t, n = 0.0, 0
+        ctx.synchronize()
+        w0 = time.perf_counter()
+        for _ in range(steps):
+            ctx.timing_reset()
+            t, n, info = run_steps(ctx, t, n, 1, DT)
+            per_step.append(sum(ctx.timing_get(k)[0] for k in ("press_setup", "press_inner", "press_outer")))
+            its.append(info[0]["pressure"]["iterations"])
+        ctx.synchronize()
+        wall = time.perf_counter() - w0
+        fb = ctx.pressure_fallbacks()
+        mineral = info[0]["budget"]["mineral"]
+        ctx.timing(False)
+        ctx.close()
+        arms[name] = {"pressure_ms_per_step_mean": round(statistics.mean(per_step), 3),
+                      "pressure_ms_per_step_median": round(statistics.median(per_step), 3),
+                      "pressure_ms_first_step": round(per_step[0], 3),
+                      "pressure_ms_total": round(sum(per_step), 1),
+                      "iterations_mean": round(statistics.mean(its), 2), "iterations_first": its[0],
+                      "fallbacks": fb, "steps_per_s": round(steps / wall, 3), "wall_s": round(wall, 1),
+                      "mineral_after": mineral}
+        log(f"c4 {name}: {arms[name]}")
+    base = arms["plain_mixed"]["pressure_ms_total"]
+    return {"metric": f"pressure solve ms per step over {steps} steps at {shape[2]}x{shape[1]}x{shape[0]}, "
+                      "flow-through model with evolving porosity",
+            "value": arms["learned_precond"]["pressure_ms_per_step_mean"] if arms["learned_precond"] else None,
+            "unit": "ms/step", "higher_is_better": False, "n_gpus": 1, "steps": steps, "data": "synthetic",
+            "config": {"workload": f"the workload's geometry (seed {seed}) without Air planes, P = {FLOW_PIN:g} / "
+                                   f"{FLOW_POUT:g} on the Pore voxels of z = 0 / z = max, acid {FLOW_ACID:g} "
+                                   f"flowing in, dt {DT:g}, {steps} steps from a fresh state per arm, pressure rtol "
+                                   "1e-8"},
+            "arms": arms,
+            "learned_vs_plain_mixed": (round(arms["learned_precond"]["pressure_ms_total"] / base, 3)
+                                       if arms["learned_precond"] else None)}
+
+
+# ---------------------------------------------------------------------------
 # The large single domain: 1024x1024x768 uint16 (805 M voxels) with the lean device layout.
 
 LARGE_SHAPE = (768, 1024, 1024)  # (I, J, K) = (zext, yext, xext)
@@ -1048,7 +1129,13 @@ def main():
     ap.add_argument("--large", action="store_true",
                     help="the 1024x1024x768 uint16 fractured domain with the lean device layout, mixed "
                          "precision against the plain FP64 pressure solver (a separate JSON line)")
+    ap.add_argument("--c4", action="store_true",
+                    help="200 steps of the flow-through model with the learned preconditioner against the "
+                         "plain solvers (a separate JSON line)")
     args = ap.parse_args()
+    if args.c4:
+        print(json.dumps(c4_arm(args)), flush=True)
+        return
     if args.large:
         if args.steps == 40:
             args.steps = 3  # the default count is for the 338x338x283 workload

@@ -254,6 +254,27 @@ ls_status ls_download_field(ls_ctx* ctx, ls_field f, void* host, size_t n_elems,
 ls_status ls_upload_field_device(ls_ctx* ctx, ls_field f, const void* dev, size_t n_elems, int padded);
 ls_status ls_download_field_device(ls_ctx* ctx, ls_field f, void* dev, size_t n_elems, int padded);
 
+/* Output without stalling the time loop (the reference's writeVTKFile downloads, src/
+   Simulation.cpp:1306-1566, made asynchronous; ABI 3). Copies `count` fields (ls_field ids,
+   I*J*K or (I+1)*J*K elements each) as they are now into host buffers, on a stream of the
+   context's own, and returns at once; *done receives an event handle that ls_event_wait
+   blocks on until every copy has landed (from any thread) and ls_event_release frees. The
+   steps that follow run while the copies drain: in the resident layout the fields are first
+   copied into a device staging buffer the context keeps (the size of the fields copied), so
+   nothing waits for the host; in the lean layout the copies read the fields themselves and a
+   later call that overwrites one waits on the device for its copy. The buffers should be
+   page-locked (ls_host_alloc) for the copies to run asynchronously. */
+ls_status ls_download_fields_async(ls_ctx* ctx, int count, const int* fields, void* const* host_buffers,
+                                   int padded, void** done);
+ls_status ls_event_wait(void* done);
+void ls_event_release(void* done);
+/* Page-locked host memory (null on failure) and its release. */
+void* ls_host_alloc(size_t bytes);
+void ls_host_free(void* p);
+/* The number of NaN or infinite values of an FP64 field over the I*J*K voxels (the output
+   writer's NaN scrub of src/Simulation.cpp:1487-1517 is needed only when it is nonzero). */
+ls_status ls_count_nonfinite(ls_ctx* ctx, ls_field f, long long* count);
+
 /* Initialisation (src/Simulation.cpp:165-180, 254-278, 285-310, 1573-1590, 109-125). */
 ls_status ls_init_fields(ls_ctx* ctx);
 ls_status ls_init_frac(ls_ctx* ctx, unsigned long long* initial_sulphide_count);

@@ -71,7 +71,7 @@ def build_cli():
     srcs = [os.path.join(HOST, s) for s in HOST_SOURCES]
     tmp = CLI + ".tmp"
     cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I" + os.path.join(ROOT, "include"), "-I" + HOST,
-           *srcs, "-o", tmp, "-L" + HERE, "-lleachingsim_gb300", "-Wl,-rpath,$ORIGIN"]
+           *srcs, "-o", tmp, "-L" + HERE, "-lleachingsim_gb300", "-Wl,-rpath,$ORIGIN", "-pthread"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"host build failed:\n{res.stdout}\n{res.stderr}")

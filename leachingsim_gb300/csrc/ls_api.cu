@@ -241,7 +241,7 @@ ls_status wlist_all(ls_ctx* c) {
 void snap_fence(ls_ctx* c, int groups) {
     const int g = groups & c->snap_pending;
     if (!g) return;
-    for (int q = 0; q < 4; ++q)
+    for (int q = 0; q < 5; ++q)
         if (g & (1 << q)) cudaStreamWaitEvent(c->stream, c->snap_ev[q], 0);
     c->snap_pending &= ~g;
 }
@@ -526,18 +526,18 @@ ls_status ls_create(ls_ctx** out, int I, int J, int K, int label_bytes, const ls
     if (c->p.memory_mode == LS_MEM_LEAN) {
         c->lean = 1;
         c->mg_graphs_off = 1;  // the hierarchy's arrays move between steps
-        if (cudaStreamCreateWithFlags(&c->snap_stream, cudaStreamNonBlocking) != cudaSuccess) {
-            c->snap_stream = nullptr;
+    }
+    if (cudaStreamCreateWithFlags(&c->snap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        c->snap_stream = nullptr;
+        ls_destroy(c);
+        return LS_CUDA_ERROR;
+    }
+    for (cudaEvent_t& e : c->snap_ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            e = nullptr;
             ls_destroy(c);
             return LS_CUDA_ERROR;
         }
-        for (cudaEvent_t& e : c->snap_ev)
-            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
-                e = nullptr;
-                ls_destroy(c);
-                return LS_CUDA_ERROR;
-            }
-    }
     const size_t np = (size_t)NP, n = (size_t)c->g.N;
 #define ALLOC(ptr, count)                                                     \
     do {                                                                      \
@@ -674,6 +674,8 @@ ls_status ls_destroy(ls_ctx* c) {
     }
     for (auto e : c->event_pool) cudaEventDestroy(e);
     if (c->arena) cudaFree(c->arena);
+    if (c->stage) cudaFree(c->stage);
+    if (c->stage_free) cudaEventDestroy(c->stage_free);
     if (c->snap_stream) {
         cudaStreamSynchronize(c->snap_stream);
         cudaStreamDestroy(c->snap_stream);
@@ -757,6 +759,130 @@ static ls_status transfer(ls_ctx* c, ls_field f, void* host, size_t n, int padde
         LS_CUDA(c, cudaMemcpyAsync(host, dev, n * esz, kind, c->stream));
     }
     LS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return LS_OK;
+}
+
+static int field_group(int f) {
+    switch (f) {
+    case LS_F_PRESSURE: return kSnapP;
+    case LS_F_FLUX_X: case LS_F_FLUX_Y: case LS_F_FLUX_Z: return kSnapFlux;
+    case LS_F_SATURATION: return kSnapSat;
+    case LS_F_PERMEABILITY: case LS_F_VISCOSITY: case LS_F_CAP_PRESSURE: case LS_F_REL_PERM: return kSnapProps;
+    default: return kSnapRest;
+    }
+}
+
+ls_status ls_download_fields_async(ls_ctx* c, int count, const int* fields, void* const* hosts, int padded,
+                                   void** done) {
+    if (!c || count < 1 || !fields || !hosts || !done) return c ? set_error(c, LS_BAD_ARG, "bad arguments") : LS_BAD_ARG;
+    *done = nullptr;
+    const size_t n = padded ? (size_t)c->g.NP : (size_t)c->g.N;
+    struct Item { void* dev; void* host; size_t bytes; int group; };
+    std::vector<Item> items;
+    for (int q = 0; q < count; ++q) {
+        size_t esz = 0;
+        void* dev = field_ptr(c, (ls_field)fields[q], &esz);
+        if (!dev || !hosts[q]) return set_error(c, LS_BAD_ARG, "ls_download_fields_async: unknown field or null buffer");
+        items.push_back({dev, hosts[q], n * esz, field_group(fields[q])});
+    }
+    cudaEvent_t ev = nullptr;
+    LS_CUDA(c, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaStream_t ss = c->snap_stream;
+    size_t total = 0;
+    for (const Item& it : items) total += (it.bytes + 255) & ~(size_t)255;
+    if (!c->lean) {
+        // resident layout: device copies into the staging buffer on the context's stream (the
+        // fields are free to change right after), then the copies to the host from there
+        if (c->stage_bytes < total) {
+            if (c->stage) {
+                LS_CUDA(c, cudaStreamSynchronize(ss));
+                dfree(c, &c->stage, c->stage_bytes);
+                c->stage_bytes = 0;
+            }
+            LS_TRY(dalloc(c, &c->stage, total));
+            c->stage_bytes = total;
+        } else if (c->stage_free) {
+            LS_CUDA(c, cudaStreamWaitEvent(c->stream, c->stage_free, 0));  // the last batch is out of it
+        }
+        if (!c->stage_free) LS_CUDA(c, cudaEventCreateWithFlags(&c->stage_free, cudaEventDisableTiming));
+        size_t off = 0;
+        for (Item& it : items) {
+            void* dst = (char*)c->stage + off;
+            LS_CUDA(c, cudaMemcpyAsync(dst, it.dev, it.bytes, cudaMemcpyDeviceToDevice, c->stream));
+            it.dev = dst;
+            off += (it.bytes + 255) & ~(size_t)255;
+        }
+        LS_CUDA(c, cudaEventRecord(c->snap_ev[5], c->stream));
+        LS_CUDA(c, cudaStreamWaitEvent(ss, c->snap_ev[5], 0));
+        for (const Item& it : items) LS_CUDA(c, cudaMemcpyAsync(it.host, it.dev, it.bytes, cudaMemcpyDefault, ss));
+        LS_CUDA(c, cudaEventRecord(c->stage_free, ss));
+        LS_CUDA(c, cudaEventRecord(ev, ss));
+        *done = ev;
+        return LS_OK;
+    }
+    // lean layout (no room for a staging buffer): straight from the fields, and the kernels
+    // that overwrite one wait for its copy
+    LS_CUDA(c, cudaEventRecord(c->snap_ev[5], c->stream));
+    LS_CUDA(c, cudaStreamWaitEvent(ss, c->snap_ev[5], 0));
+    // in the order the next step overwrites the groups
+    for (int q : {4, 0, 1, 2, 3}) {
+        const int g = 1 << q;
+        bool any = false;
+        for (const Item& it : items)
+            if (it.group == g) {
+                LS_CUDA(c, cudaMemcpyAsync(it.host, it.dev, it.bytes, cudaMemcpyDefault, ss));
+                any = true;
+            }
+        if (any) {
+            LS_CUDA(c, cudaEventRecord(c->snap_ev[q], ss));
+            c->snap_pending |= g;
+        }
+    }
+    LS_CUDA(c, cudaEventRecord(ev, ss));
+    *done = ev;
+    return LS_OK;
+}
+
+ls_status ls_event_wait(void* done) {
+    if (!done) return LS_BAD_ARG;
+    return cudaEventSynchronize((cudaEvent_t)done) == cudaSuccess ? LS_OK : LS_CUDA_ERROR;
+}
+
+void ls_event_release(void* done) {
+    if (done) cudaEventDestroy((cudaEvent_t)done);
+}
+
+void* ls_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, bytes ? bytes : 1, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void ls_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+__global__ void k_count_nonfinite(long long n, const double* __restrict__ v, double* __restrict__ partials) {
+    double acc[1] = {0.0};
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x)
+        if ((__double_as_longlong(v[r]) & 0x7ff0000000000000ll) == 0x7ff0000000000000ll) acc[0] += 1.0;
+    block_sum_store<1>(acc, partials);
+}
+
+ls_status ls_count_nonfinite(ls_ctx* c, ls_field f, long long* count) {
+    if (!c || !count) return c ? set_error(c, LS_BAD_ARG, "null count") : LS_BAD_ARG;
+    size_t esz = 0;
+    void* dev = field_ptr(c, f, &esz);
+    if (!dev || esz != 8) return set_error(c, LS_BAD_ARG, "ls_count_nonfinite: an FP64 field is needed");
+    const int grid = grid_for(c, c->g.N);
+    LS_LAUNCH(c, k_count_nonfinite, grid, kBlock, 0, c->g.N, (const double*)dev, c->partials);
+    LS_TRY(finalize_sum(c, grid, 1, S_RED0));
+    double v = 0.0;
+    LS_TRY(read_scalars(c, S_RED0, 1, &v));
+    *count = (long long)v;
     return LS_OK;
 }
 
@@ -951,8 +1077,8 @@ ls_status ls_snapshot(ls_ctx* c) {
         // reached here, in the order the step overwrites the fields (snap_fence)
         snap_fence(c, kSnapAll);  // a previous snapshot's copies are done before these start
         cudaStream_t ss = c->snap_stream;
-        LS_CUDA(c, cudaEventRecord(c->snap_ev[4], s));
-        LS_CUDA(c, cudaStreamWaitEvent(ss, c->snap_ev[4], 0));
+        LS_CUDA(c, cudaEventRecord(c->snap_ev[5], s));
+        LS_CUDA(c, cudaStreamWaitEvent(ss, c->snap_ev[5], 0));
         LS_CUDA(c, cudaMemcpyAsync(c->b_P, c->P, d8, cudaMemcpyDefault, ss));
         LS_CUDA(c, cudaEventRecord(c->snap_ev[0], ss));
         for (auto pr : {std::make_pair(c->b_fx, c->fx), std::make_pair(c->b_fy, c->fy), std::make_pair(c->b_fz, c->fz)})
@@ -965,7 +1091,7 @@ ls_status ls_snapshot(ls_ctx* c) {
                         std::make_pair(c->b_precip, c->precip)})
             LS_CUDA(c, cudaMemcpyAsync(pr.first, pr.second, d8, cudaMemcpyDefault, ss));
         LS_CUDA(c, cudaEventRecord(c->snap_ev[3], ss));
-        c->snap_pending = kSnapAll;
+        c->snap_pending = kSnapP | kSnapFlux | kSnapSat | kSnapRest;
         return LS_OK;
     }
     LS_CUDA(c, cudaMemcpyAsync(c->b_label, c->label, np * c->label_bytes, cudaMemcpyDeviceToDevice, s));

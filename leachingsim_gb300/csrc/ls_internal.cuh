@@ -437,11 +437,18 @@ struct ls_ctx {
     size_t arena_size, arena_used, arena_overflow, arena_need;
     int arena_phase;      // kPhase*
     int b_host_pinned;    // lean: the snapshot arrays came from cudaHostAlloc (else malloc)
-    // lean: the snapshot's device-to-host copies run on their own stream, in the order the
-    // step first overwrites the fields; a phase that writes a field waits for its copy
+    // Copies of fields to host memory (the lean snapshot, ls_download_fields_async) run on a
+    // stream of their own, from the state the context's stream had reached; a kernel family
+    // that writes a field waits for the pending copies of its group (snap_fence)
     cudaStream_t snap_stream;
-    cudaEvent_t snap_ev[5];  // [0..3] copies of the groups kSnap*, [4] the snapshot's start
+    cudaEvent_t snap_ev[6];  // [0..4] copies of the groups kSnap*, [5] the start of a batch
     int snap_pending;        // groups whose copies the main stream has not waited for
+    // resident layout: ls_download_fields_async copies the fields into this device staging
+    // buffer first (a fast device copy), so that the steps that follow never wait for the
+    // copies to the host; stage_free is recorded after the last copy out of it
+    void* stage;
+    size_t stage_bytes;
+    cudaEvent_t stage_free;
 };
 
 namespace ls {
@@ -603,9 +610,10 @@ ls_status ordered_list(ls_ctx* c, const int8_t* kind, int min_kind);
 // the work list holding every voxel 0 .. N-1 (the change-tracked kernels without change
 // tracking, LS_MEM_LEAN)
 ls_status wlist_all(ls_ctx* c);
-// Groups of snapshot fields (LS_MEM_LEAN), in the order a step first writes them: the
-// pressure, the fluxes, the saturation, then labels, conc, acid and precipitate.
-constexpr int kSnapP = 1, kSnapFlux = 2, kSnapSat = 4, kSnapRest = 8, kSnapAll = 15;
+// Groups of fields copied to the host, in the order a step first writes them: the pressure,
+// the fluxes, the saturation, then labels, frac, conc, acid and precipitate; the properties
+// (K, viscosity, Pc, kr) are written by the props pass at the start of a step.
+constexpr int kSnapP = 1, kSnapFlux = 2, kSnapSat = 4, kSnapRest = 8, kSnapProps = 16, kSnapAll = 31;
 // make the context's stream wait until the snapshot copies of `groups` are done (no-op when
 // none are pending)
 void snap_fence(ls_ctx* c, int groups);

@@ -15,7 +15,8 @@
 //    -> FP32 in registers): a warp computes 16 output voxels x all output channels; the K
 //    dimension runs over 27 taps x input channels in chunks of 16. k_lp_conv serves the
 //    64-channel layers; k_lp_conv_tiled is the LS_LPNET_TC=0 path of the others.
-//  * k_lp_conv_dw: the weight / bias gradient, staged through shared memory, FP32 FMA.
+//  * k_lp_conv_dw_mma: the weight / bias gradient, staged transposed through shared memory,
+//    mma.sync m16n8k16 (k_lp_conv_dw: the same with FP32 FMA, LS_LPNET_DW=0).
 //  * pooling, upsampling + skip addition and their backward passes, ReLU masking, the
 //    masked mean-square loss and Adam.
 //
@@ -520,6 +521,103 @@ __global__ void __launch_bounds__(256) k_lp_conv_dw(LpDims d, const bf16* __rest
     if (t == 13 && threadIdx.x < COUT) atomicAdd(&db[threadIdx.x], bacc);
 }
 
+// The weight gradient on the tensor cores: for tap t, dW_t (COUT x CIN) = dY^T X_t, a GEMM
+// whose K runs over the voxels (X_t: the input at the voxel shifted by the tap, 0 outside).
+// A block takes one tap and a chunk of voxels, stages 64 voxels at a time transposed in
+// shared memory (dY as A rows = output channels, X_t as B columns = input channels, K
+// contiguous so that every fragment register is one 32-bit load) and issues mma.sync
+// m16n8k16 (BF16 x BF16 -> FP32). The (COUT/16) x (CIN/8) output tiles are spread over the 8
+// warps; with fewer tiles than warps the warps also split the 4 K-steps of a stage. Partial
+// results go to dw with FP32 atomics, as the FMA kernel above does; the bias gradient (the
+// centre tap's blocks) is summed in FP32.
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(256) k_lp_conv_dw_mma(LpDims d, const bf16* __restrict__ in,
+                                                        const bf16* __restrict__ dy, float* __restrict__ dw,
+                                                        float* __restrict__ db, int chunk) {
+    constexpr int KS = 66;                       // row stride in bf16 (64 voxels + 2: 32-bit aligned)
+    constexpr int TILES = (COUT / 16) * (CIN / 8);
+    constexpr int KGROUPS = TILES >= 8 ? 1 : 8 / TILES;  // warps sharing the tiles split K
+    constexpr int TW = 8 / KGROUPS;              // warps per K-group
+    constexpr int PERW = (TILES + TW - 1) / TW;  // tiles per warp
+    static_assert(COUT % 16 == 0 && CIN % 8 == 0 && 8 % KGROUPS == 0, "channel counts");
+    __shared__ __align__(16) bf16 sD[COUT][KS];  // sD[co][v]
+    __shared__ __align__(16) bf16 sX[CIN][KS];   // sX[ci][v]
+    __shared__ long long sN[64];
+    const int t = blockIdx.y;
+    const int dz = t / 9 - 1, dyy = (t / 3) % 3 - 1, dx = t % 3 - 1;
+    const long long v0 = (long long)blockIdx.x * chunk;
+    const long long vend = (v0 + chunk < d.N) ? v0 + chunk : d.N;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3;
+    const int kgroup = warp / TW, wt = warp - kgroup * TW;
+    float acc[PERW][4];
+#pragma unroll
+    for (int q = 0; q < PERW; ++q)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[q][e] = 0.f;
+    float bacc = 0.f;
+    for (long long vb = v0; vb < vend; vb += 64) {
+        if (threadIdx.x < 64) {
+            const long long v = vb + threadIdx.x;
+            long long nb = -1;
+            if (v < vend) {
+                int z, y, x;
+                lp_decode(d, v, z, y, x);
+                z += dz; y += dyy; x += dx;
+                if (z >= 0 && z < d.D && y >= 0 && y < d.H && x >= 0 && x < d.W)
+                    nb = ((long long)z * d.H + y) * d.W + x;
+            }
+            sN[threadIdx.x] = nb;
+        }
+        for (int e = threadIdx.x; e < 64 * COUT; e += 256) {
+            const int vv = e / COUT, co = e - vv * COUT;
+            const long long v = vb + vv;
+            sD[co][vv] = (v < vend) ? dy[v * COUT + co] : __float2bfloat16(0.f);
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < 64 * CIN; e += 256) {
+            const int vv = e / CIN, ci = e - vv * CIN;
+            const long long nb = sN[vv];
+            sX[ci][vv] = (nb >= 0) ? in[nb * CIN + ci] : __float2bfloat16(0.f);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int ks = kgroup; ks < 4; ks += KGROUPS) {
+            const int k0 = ks * 16 + tig * 2;
+#pragma unroll
+            for (int q = 0; q < PERW; ++q) {
+                const int tile = wt + q * TW;
+                if (tile < TILES) {
+                    const int m0 = (tile / (CIN / 8)) * 16, n0 = (tile % (CIN / 8)) * 8;
+                    uint32_t a[4], b[2];
+                    a[0] = *reinterpret_cast<const uint32_t*>(&sD[m0 + gid][k0]);
+                    a[1] = *reinterpret_cast<const uint32_t*>(&sD[m0 + gid + 8][k0]);
+                    a[2] = *reinterpret_cast<const uint32_t*>(&sD[m0 + gid][k0 + 8]);
+                    a[3] = *reinterpret_cast<const uint32_t*>(&sD[m0 + gid + 8][k0 + 8]);
+                    b[0] = *reinterpret_cast<const uint32_t*>(&sX[n0 + gid][k0]);
+                    b[1] = *reinterpret_cast<const uint32_t*>(&sX[n0 + gid][k0 + 8]);
+                    mma_16816(acc[q], a, b);
+                }
+            }
+        }
+        if (t == 13 && threadIdx.x < COUT)
+            for (int vv = 0; vv < 64; ++vv) bacc += __bfloat162float(sD[threadIdx.x][vv]);
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < PERW; ++q) {
+        const int tile = wt + q * TW;
+        if (tile < TILES) {
+            const int m0 = (tile / (CIN / 8)) * 16, n0 = (tile % (CIN / 8)) * 8;
+            float* base = dw + (size_t)t * COUT * CIN;
+            atomicAdd(&base[(size_t)(m0 + gid) * CIN + n0 + tig * 2], acc[q][0]);
+            atomicAdd(&base[(size_t)(m0 + gid) * CIN + n0 + tig * 2 + 1], acc[q][1]);
+            atomicAdd(&base[(size_t)(m0 + gid + 8) * CIN + n0 + tig * 2], acc[q][2]);
+            atomicAdd(&base[(size_t)(m0 + gid + 8) * CIN + n0 + tig * 2 + 1], acc[q][3]);
+        }
+    }
+    if (t == 13 && threadIdx.x < COUT) atomicAdd(&db[threadIdx.x], bacc);
+}
+
 // wt[26 - tap][ci][co] = w[tap][co][ci] (the input-gradient convolution)
 __global__ void k_lp_wt(const bf16* __restrict__ w, bf16* __restrict__ wt, int cin, int cout) {
     const int n = 27 * cin * cout;
@@ -885,10 +983,18 @@ ls_status lp_conv(ls_lpnet* n, LpDims d, int cin, int cout, const bf16* in, cons
 ls_status lp_conv_dw(ls_lpnet* n, LpDims d, int cin, int cout, const bf16* in, const bf16* dy, float* dw, float* db) {
     const int chunk = 2048;
     const dim3 grid((unsigned)((d.N + chunk - 1) / chunk), 27);
-#define LP_CASE(CI, CO)                                                                   \
-    if (cin == CI && cout == CO) {                                                        \
-        LP_LAUNCH(n, (ls::k_lp_conv_dw<CI, CO>), grid, 256, d, in, dy, dw, db, chunk);    \
-        return LS_OK;                                                                     \
+    // tensor cores (mma.sync); LS_LPNET_DW=0 keeps the FP32 FMA kernel (for comparison)
+    static const bool fma_only = [] {
+        const char* e = getenv("LS_LPNET_DW");
+        return e && e[0] == '0';
+    }();
+#define LP_CASE(CI, CO)                                                                          \
+    if (cin == CI && cout == CO) {                                                               \
+        if (fma_only)                                                                            \
+            LP_LAUNCH(n, (ls::k_lp_conv_dw<CI, CO>), grid, 256, d, in, dy, dw, db, chunk);       \
+        else                                                                                     \
+            LP_LAUNCH(n, (ls::k_lp_conv_dw_mma<CI, CO>), grid, 256, d, in, dy, dw, db, chunk);   \
+        return LS_OK;                                                                            \
     }
     LP_CASE(16, 16) LP_CASE(16, 32) LP_CASE(32, 64) LP_CASE(64, 64) LP_CASE(64, 32) LP_CASE(32, 16)
 #undef LP_CASE

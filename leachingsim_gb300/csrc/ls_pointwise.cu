@@ -136,6 +136,7 @@ __global__ void __launch_bounds__(kBlock) k_props(PropsConst pc, const L* __rest
 }
 
 ls_status props_run(ls_ctx* c) {
+    snap_fence(c, kSnapProps);
     PropsConst pc;
     pc.m = 1.0 - (1.0 / c->p.vg_n);
     pc.s_res = c->p.s_res;

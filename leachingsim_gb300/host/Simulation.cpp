@@ -23,7 +23,22 @@ Simulation::Simulation(size_t seed, int label_bytes) : seed_(seed), label_bytes_
 }
 
 Simulation::~Simulation() {
+    try {
+        finishOutput();
+    } catch (const std::exception& e) {
+        std::cerr << "VTK output: " << e.what() << std::endl;
+    }
+    for (void* p : out_bufs_) ls_host_free(p);
     if (ctx_) ls_destroy(ctx_);
+}
+
+void Simulation::finishOutput() {
+    if (writer_.joinable()) writer_.join();
+    if (!writer_error_.empty()) {
+        std::string e = writer_error_;
+        writer_error_.clear();
+        throw std::runtime_error(e);
+    }
 }
 
 void Simulation::check(ls_status st, const char* what) {
@@ -301,48 +316,119 @@ template std::vector<float> Simulation::download<float>(ls_field);
 template std::vector<uint8_t> Simulation::download<uint8_t>(ls_field);
 template std::vector<uint16_t> Simulation::download<uint16_t>(ls_field);
 
-// Simulation::writeVTKFile (src/Simulation.cpp:1306-1566), one piece (np=1).
+// Simulation::writeVTKFile (src/Simulation.cpp:1306-1566), one piece (np=1). The fields are
+// copied to page-locked buffers on the context's copy stream and the piece is written from
+// them on a background thread, so the time loop goes on while the copies drain and the file
+// is encoded (the next steps' kernels wait on the device only for the copies of the fields
+// they overwrite). The reference scrubs NaNs of Pressure and CapillaryPressure in place
+// (src/Simulation.cpp:1487-1517): when the device counts any, this output takes the
+// synchronous path that does the same.
 void Simulation::writeVTKFile(const std::string& fname_root, size_t tstep, size_t data_flags) {
-    VtkFields fields;
+    finishOutput();  // the previous piece is written and its buffers are free
     const size_t n = global_.size();
-    if (data_flags & Type) {
-        fields.label.resize(n * label_bytes_);
-        check(ls_download_field(ctx_, LS_F_LABEL, fields.label.data(), n, 0), "download label");
+    struct Want { size_t flag; ls_field f; size_t esz; };
+    const Want wants[] = {{Type, LS_F_LABEL, (size_t)label_bytes_}, {Conc, LS_F_CONC, 8}, {Pressure, LS_F_PRESSURE, 8},
+                          {Frac, LS_F_FRAC, 4}, {Flux_Vec, LS_F_FLUX_X, 8}, {Flux_Vec, LS_F_FLUX_Y, 8},
+                          {Flux_Vec, LS_F_FLUX_Z, 8}, {Saturation, LS_F_SATURATION, 8},
+                          {CapPressure, LS_F_CAP_PRESSURE, 8}, {RelPermeability, LS_F_REL_PERM, 8},
+                          {Permeability, LS_F_PERMEABILITY, 8}, {AcidConc, LS_F_ACID, 8}};
+    const int nw = (int)(sizeof(wants) / sizeof(wants[0]));
+    long long nan_p = 0, nan_c = 0;
+    if (data_flags & Pressure) check(ls_count_nonfinite(ctx_, LS_F_PRESSURE, &nan_p), "count NaN");
+    if (data_flags & CapPressure) check(ls_count_nonfinite(ctx_, LS_F_CAP_PRESSURE, &nan_c), "count NaN");
+    if (out_bufs_.empty() && nan_p == 0 && nan_c == 0) {
+        out_bufs_.assign(nw, nullptr);
+        for (int q = 0; q < nw; ++q) {
+            out_bufs_[q] = ls_host_alloc(n * wants[q].esz);
+            if (!out_bufs_[q]) {  // no page-locked memory: synchronous output from now on
+                for (void*& p : out_bufs_) ls_host_free(p), p = nullptr;
+                out_bufs_.assign(1, nullptr);
+                break;
+            }
+        }
+    }
+    const bool async = nan_p == 0 && nan_c == 0 && out_bufs_.size() == (size_t)nw;
+    std::vector<std::vector<char>> sync_bufs;
+    void* ptr[12] = {};
+    if (async) {
+        int ids[12];
+        void* hosts[12];
+        int cnt = 0;
+        for (int q = 0; q < nw; ++q)
+            if (data_flags & wants[q].flag) {
+                ids[cnt] = (int)wants[q].f;
+                hosts[cnt++] = out_bufs_[q];
+                ptr[q] = out_bufs_[q];
+            }
+        void* done = nullptr;
+        check(ls_download_fields_async(ctx_, cnt, ids, hosts, 0, &done), "download fields");
+        write_pvti(fname_root, tstep, global_.i, global_.j, global_.k, data_flags, label_bytes_);
+        VtkFields fields;
         fields.label_bytes = label_bytes_;
+        fields.label = ptr[0];
+        fields.conc = (const double*)ptr[1];
+        fields.pressure = (const double*)ptr[2];
+        fields.frac = (const float*)ptr[3];
+        fields.fx = (const double*)ptr[4];
+        fields.fy = (const double*)ptr[5];
+        fields.fz = (const double*)ptr[6];
+        fields.sat = (const double*)ptr[7];
+        fields.pc = (const double*)ptr[8];
+        fields.kr = (const double*)ptr[9];
+        fields.perm = (const double*)ptr[10];
+        fields.acid = (const double*)ptr[11];
+        std::stringstream piece;
+        piece << fname_root << "_0_" << setw(6) << setfill('0') << tstep << ".vti";
+        const int3 g = global_;
+        std::string path = piece.str();
+        writer_ = std::thread([this, done, path, g, data_flags, fields]() {
+            try {
+                if (ls_event_wait(done) != LS_OK) throw std::runtime_error("field copies failed");
+                write_vti(path, g.i, g.j, g.k, data_flags, fields);
+            } catch (const std::exception& e) {
+                writer_error_ = std::string("writing ") + path + ": " + e.what();
+            }
+            ls_event_release(done);
+        });
+        return;
     }
-    auto get64 = [&](ls_field f, std::vector<double>& v) {
-        v.resize(n);
-        check(ls_download_field(ctx_, f, v.data(), n, 0), "download");
+    // synchronous path (NaN scrub, or no page-locked memory)
+    sync_bufs.resize(nw);
+    for (int q = 0; q < nw; ++q)
+        if (data_flags & wants[q].flag) {
+            sync_bufs[q].resize(n * wants[q].esz);
+            check(ls_download_field(ctx_, wants[q].f, sync_bufs[q].data(), n, 0), "download");
+            ptr[q] = sync_bufs[q].data();
+        }
+    int scrub_p = 0, scrub_c = 0;
+    auto scrub = [&](int q, int& cnt) {
+        if (!ptr[q]) return;
+        double* v = (double*)ptr[q];
+        for (size_t r = 0; r < n; ++r)
+            if (std::isnan(v[r]) || std::isinf(v[r])) { v[r] = 0.0; cnt++; }
     };
-    if (data_flags & Conc) get64(LS_F_CONC, fields.conc);
-    if (data_flags & Pressure) get64(LS_F_PRESSURE, fields.pressure);
-    if (data_flags & Frac) {
-        fields.frac.resize(n);
-        check(ls_download_field(ctx_, LS_F_FRAC, fields.frac.data(), n, 0), "download frac");
-    }
-    if (data_flags & Flux_Vec) {
-        get64(LS_F_FLUX_X, fields.fx);
-        get64(LS_F_FLUX_Y, fields.fy);
-        get64(LS_F_FLUX_Z, fields.fz);
-    }
-    if (data_flags & Saturation) get64(LS_F_SATURATION, fields.sat);
-    if (data_flags & CapPressure) get64(LS_F_CAP_PRESSURE, fields.pc);
-    if (data_flags & RelPermeability) get64(LS_F_REL_PERM, fields.kr);
-    if (data_flags & Permeability) get64(LS_F_PERMEABILITY, fields.perm);
-    if (data_flags & AcidConc) get64(LS_F_ACID, fields.acid);
-    // NaN scrub of pressure and capillary pressure, in place like the reference
-    // (src/Simulation.cpp:1487-1517)
-    int nan_p = 0, nan_c = 0;
-    for (double& v : fields.pressure)
-        if (std::isnan(v) || std::isinf(v)) { v = 0.0; nan_p++; }
-    for (double& v : fields.pc)
-        if (std::isnan(v) || std::isinf(v)) { v = 0.0; nan_c++; }
-    if (nan_p > 0) check(ls_upload_field(ctx_, LS_F_PRESSURE, fields.pressure.data(), n, 0), "upload P");
-    if (nan_c > 0) check(ls_upload_field(ctx_, LS_F_CAP_PRESSURE, fields.pc.data(), n, 0), "upload Pc");
-    if (nan_p > 0 || nan_c > 0)
-        cout << "    [VTK Writer Rank 0] checked " << nan_p << " Pressure NaNs and " << nan_c
+    scrub(2, scrub_p);
+    scrub(8, scrub_c);
+    if (scrub_p > 0) check(ls_upload_field(ctx_, LS_F_PRESSURE, ptr[2], n, 0), "upload P");
+    if (scrub_c > 0) check(ls_upload_field(ctx_, LS_F_CAP_PRESSURE, ptr[8], n, 0), "upload Pc");
+    if (scrub_p > 0 || scrub_c > 0)
+        cout << "    [VTK Writer Rank 0] checked " << scrub_p << " Pressure NaNs and " << scrub_c
              << " CapPressure NaNs from boundary padding." << endl;
     write_pvti(fname_root, tstep, global_.i, global_.j, global_.k, data_flags, label_bytes_);
+    VtkFields fields;
+    fields.label_bytes = label_bytes_;
+    fields.label = ptr[0];
+    fields.conc = (const double*)ptr[1];
+    fields.pressure = (const double*)ptr[2];
+    fields.frac = (const float*)ptr[3];
+    fields.fx = (const double*)ptr[4];
+    fields.fy = (const double*)ptr[5];
+    fields.fz = (const double*)ptr[6];
+    fields.sat = (const double*)ptr[7];
+    fields.pc = (const double*)ptr[8];
+    fields.kr = (const double*)ptr[9];
+    fields.perm = (const double*)ptr[10];
+    fields.acid = (const double*)ptr[11];
     std::stringstream piece;
     piece << fname_root << "_0_" << setw(6) << setfill('0') << tstep << ".vti";
     write_vti(piece.str(), global_.i, global_.j, global_.k, data_flags, fields);
@@ -351,6 +437,7 @@ void Simulation::writeVTKFile(const std::string& fname_root, size_t tstep, size_
 // Simulation::writeCheckpoint / loadCheckpoint (src/Simulation.cpp:2235-2307): the padded
 // (I+1)*J*K arrays in the order img, frac, precipitate, saturation, pressure, conc, acid.
 void Simulation::writeCheckpoint(const std::string& out_dir, int step) {
+    finishOutput();  // the output written before a checkpoint is complete on disk with it
     std::stringstream fname;
     fname << out_dir << "/checkpoint_rank0_" << setw(6) << setfill('0') << step << ".bin";
     std::ofstream fout(fname.str(), std::ios::out | std::ios::binary);

@@ -8,6 +8,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "leachingsim.h"
@@ -50,6 +51,10 @@ public:
     // no header); an extension with no counterpart in the reference.
     void readPermeabilityMultiplier(const std::string& fname);
     void writeVTKFile(const std::string& fname_root, size_t tstep, size_t data_flags);
+    // Waits for the piece file of the last writeVTKFile (written on a background thread while
+    // the time loop goes on); rethrows its error. Called by the next writeVTKFile, by
+    // writeCheckpoint and by the destructor.
+    void finishOutput();
 
     // initialisation and time stepping
     void initProperties();
@@ -135,6 +140,11 @@ private:
     int conc_pending_ = 0;  // bit 0 conc, bit 1 acid set up and not yet solved
     size_t num_grains_ = 0;
     std::vector<double> ks_;
+    // asynchronous output: page-locked copies of the fields (ls_download_fields_async) and the
+    // thread that writes the .vti piece from them once they have landed
+    std::vector<void*> out_bufs_;
+    std::thread writer_;
+    std::string writer_error_;
 };
 
 }  // namespace lsh

@@ -463,6 +463,7 @@ int main(int argc, char* argv[]) {
                 }
             }
         } while (t < tmax);
+        sim.finishOutput();
 
         cout << "\n*** Simulation Finished ***" << endl;
     } catch (const std::exception& e) {

@@ -67,8 +67,8 @@ void write_pvti(const std::string& fname_root, size_t tstep, int I, int J, int K
 
 // gather a field into VTK point order (i fastest)
 template <typename T>
-static std::vector<T> to_vtk(const std::vector<T>& a, int I, int J, int K, int ncomp = 1,
-                             const std::vector<T>* b = nullptr, const std::vector<T>* c = nullptr) {
+static std::vector<T> to_vtk(const T* a, int I, int J, int K, int ncomp = 1, const T* b = nullptr,
+                             const T* c = nullptr) {
     std::vector<T> out((size_t)I * J * K * ncomp);
     size_t cnt = 0;
     for (int k = 0; k < K; ++k)
@@ -77,8 +77,8 @@ static std::vector<T> to_vtk(const std::vector<T>& a, int I, int J, int K, int n
                 size_t r = (size_t)k + (size_t)K * ((size_t)j + (size_t)J * i);
                 out[cnt * ncomp] = a[r];
                 if (ncomp == 3) {
-                    out[cnt * 3 + 1] = (*b)[r];
-                    out[cnt * 3 + 2] = (*c)[r];
+                    out[cnt * 3 + 1] = b[r];
+                    out[cnt * 3 + 2] = c[r];
                 }
                 cnt++;
             }
@@ -96,19 +96,17 @@ void write_vti(const std::string& path, int I, int J, int K, size_t flags, const
         switch (s.flag) {
         case Type:
             if (f.label_bytes == 2) {
-                std::vector<uint16_t> a(f.label.size() / 2);
-                std::memcpy(a.data(), f.label.data(), f.label.size());
-                auto o = to_vtk(a, I, J, K);
+                auto o = to_vtk((const uint16_t*)f.label, I, J, K);
                 add(s, o.data(), o.size() * 2);
             } else {
-                auto o = to_vtk(f.label, I, J, K);
+                auto o = to_vtk((const uint8_t*)f.label, I, J, K);
                 add(s, o.data(), o.size());
             }
             break;
         case Conc: { auto o = to_vtk(f.conc, I, J, K); add(s, o.data(), o.size() * 8); } break;
         case Pressure: { auto o = to_vtk(f.pressure, I, J, K); add(s, o.data(), o.size() * 8); } break;
         case Frac: { auto o = to_vtk(f.frac, I, J, K); add(s, o.data(), o.size() * 4); } break;
-        case Flux_Vec: { auto o = to_vtk(f.fx, I, J, K, 3, &f.fy, &f.fz); add(s, o.data(), o.size() * 8); } break;
+        case Flux_Vec: { auto o = to_vtk(f.fx, I, J, K, 3, f.fy, f.fz); add(s, o.data(), o.size() * 8); } break;
         case Saturation: { auto o = to_vtk(f.sat, I, J, K); add(s, o.data(), o.size() * 8); } break;
         case CapPressure: { auto o = to_vtk(f.pc, I, J, K); add(s, o.data(), o.size() * 8); } break;
         case RelPermeability: { auto o = to_vtk(f.kr, I, J, K); add(s, o.data(), o.size() * 8); } break;

@@ -10,11 +10,14 @@
 
 namespace lsh {
 
+// The arrays of one output (null: not written), each I*J*K values in the solver's order;
+// the memory belongs to the caller.
 struct VtkFields {
-    std::vector<uint8_t> label;  // label_bytes per voxel
+    const void* label = nullptr;  // label_bytes per voxel
     int label_bytes = 1;
-    std::vector<double> conc, pressure, fx, fy, fz, sat, pc, kr, perm, acid;
-    std::vector<float> frac;
+    const double *conc = nullptr, *pressure = nullptr, *fx = nullptr, *fy = nullptr, *fz = nullptr,
+                 *sat = nullptr, *pc = nullptr, *kr = nullptr, *perm = nullptr, *acid = nullptr;
+    const float* frac = nullptr;
 };
 
 // Voxel (i,j,k) of an I x J x K domain is stored at k + K*(j + J*i); VTK's x axis is i.

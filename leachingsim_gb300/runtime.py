@@ -33,6 +33,13 @@ SYMBOLS = {
     "ls_download_field": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_int]),
     "ls_upload_field_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_int]),
     "ls_download_field_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_int]),
+    "ls_download_fields_async": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                           C.POINTER(C.c_void_p)]),
+    "ls_event_wait": (C.c_int, [C.c_void_p]),
+    "ls_event_release": (None, [C.c_void_p]),
+    "ls_host_alloc": (C.c_void_p, [C.c_size_t]),
+    "ls_host_free": (None, [C.c_void_p]),
+    "ls_count_nonfinite": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_longlong)]),
     "ls_init_fields": (C.c_int, [C.c_void_p]),
     "ls_init_frac": (C.c_int, [C.c_void_p, C.POINTER(C.c_ulonglong)]),
     "ls_init_saturation": (C.c_int, [C.c_void_p]),
@@ -252,6 +259,29 @@ def lpnet_unflatten(flat):
     return out
 
 
+class PendingDownload:
+    """Copies started by Context.download_async: wait() blocks until all have landed."""
+
+    def __init__(self, ev, outs):
+        self._ev = ev
+        self.outs = outs  # keeps the buffers alive while the copies run
+
+    def wait(self):
+        if self._ev:
+            st = load().ls_event_wait(self._ev)
+            load().ls_event_release(self._ev)
+            self._ev = None
+            if st != 0:
+                raise LsError(st, "ls_event_wait")
+        return self.outs
+
+    def __del__(self):
+        try:
+            self.wait()
+        except Exception:
+            pass
+
+
 class LPNet:
     """The learned pressure network on the GPU (owns an ls_lpnet). Fields are torch CUDA
     float32 tensors of shape (D, H, W) or numpy arrays (copied to the device)."""
@@ -380,6 +410,28 @@ class Context:
         fid = FIELDS[name]
         a = np.ascontiguousarray(np.asarray(arr).reshape(-1), dtype=self._dtype(fid))
         self._check(load().ls_upload_field(self.h, fid, _p(a), a.size, int(padded)))
+
+    def download_async(self, names, outs, padded=False):
+        """Start copying the fields `names` into the host arrays `outs` (contiguous, of the
+        fields' dtypes and sizes; page-locked for the copies to overlap) and return a
+        PendingDownload; the context's later steps wait on the device only for the copies of
+        the fields they overwrite."""
+        fids = (C.c_int * len(names))(*[FIELDS[nm] for nm in names])
+        n = self.NP if padded else self.N
+        ptrs = (C.c_void_p * len(names))()
+        for q, (nm, o) in enumerate(zip(names, outs)):
+            if not (isinstance(o, np.ndarray) and o.flags.c_contiguous and o.size == n
+                    and o.dtype == self._dtype(FIELDS[nm])):
+                raise ValueError(f"buffer for {nm} must be a contiguous {self._dtype(FIELDS[nm])} array of {n}")
+            ptrs[q] = o.ctypes.data
+        ev = C.c_void_p()
+        self._check(load().ls_download_fields_async(self.h, len(names), fids, ptrs, int(padded), C.byref(ev)))
+        return PendingDownload(ev, list(outs))
+
+    def count_nonfinite(self, name):
+        c = C.c_longlong(0)
+        self._check(load().ls_count_nonfinite(self.h, FIELDS[name], C.byref(c)))
+        return int(c.value)
 
     def download(self, name, padded=False, out=None):
         fid = FIELDS[name]
