@@ -506,6 +506,9 @@ ls_status ls_create(ls_ctx** out, int I, int J, int K, int label_bytes, const ls
     {
         const char* gv = getenv("LS_MG_GRAPHS");
         c->mg_graphs_off = (gv && gv[0] == '0') ? 1 : 0;
+        const char* tv = getenv("LS_MG_TAIL_CELLS");
+        c->mg_tail_cells = tv ? atoll(tv) : 4096;
+        if (c->mg_tail_cells < 0) c->mg_tail_cells = 0;
     }
     c->g.I = I; c->g.J = J; c->g.K = K;
     c->g.JK = JK;

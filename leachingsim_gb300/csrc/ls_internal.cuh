@@ -366,6 +366,7 @@ struct ls_ctx {
     int mg_is64;          // -1 = not allocated
     std::vector<ls::MGGraph> mg_graphs;  // captured preconditioner applications
     int mg_graphs_off;    // 1: launch the cycle kernel by kernel (LS_MG_GRAPHS=0)
+    long long mg_tail_cells;  // coarse levels up to this many cells run as one block (LS_MG_TAIL_CELLS; 0: off)
     int* comp;            // fine-level strong-component ids (-1 = not an inner unknown)
     uint8_t* start_anchor; // per component root: anchored to fixed values (supplied starts)
     int* cc_flag;         // device flag for the labelling loop

@@ -262,6 +262,22 @@ __global__ void k_mg_coarse_op(Grid f, Grid cg, const int* __restrict__ fcomp, c
 // ---------------------------------------------------------------------------
 // V-cycle kernels
 
+// One damped-Jacobi update of cell r (shared by the level kernels and the one-block tail)
+template <typename T>
+__device__ __forceinline__ T smooth_cell(const Grid& g, long long r, const T* __restrict__ e,
+                                         const T* __restrict__ f0, const T* __restrict__ f1,
+                                         const T* __restrict__ f2, const T* __restrict__ invd,
+                                         const T* __restrict__ b, const T* __restrict__ x) {
+    const T bv = b[r];
+    if (x) {
+        int i, j, k;
+        decode(g, r, i, j, k);
+        const T res = bv - m_apply(g, r, i, j, k, e, f0, f1, f2, x);
+        return x[r] + (T)kOmega * invd[r] * res;
+    }
+    return (T)kOmega * invd[r] * bv;
+}
+
 // x_out = x + omega invd (b - M x); x == nullptr means x = 0. With dotv, the per-block
 // partial of (dotv, x_out) is stored (the (r, z) of the PCG).
 // Cells that are not members keep 0 in every level vector: the buffers are cleared when
@@ -280,16 +296,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth(Grid g, const int* __restr
          r += (long long)gridDim.x * blockDim.x) {
         const bool live = kind0 ? kind0[r] == 2 : comp[r] >= 0;
         if (!live) continue;
-        T out;
-        T bv = b[r];
-        if (x) {
-            int i, j, k;
-            decode(g, r, i, j, k);
-            T res = bv - m_apply(g, r, i, j, k, e, f0, f1, f2, x);
-            out = x[r] + (T)kOmega * invd[r] * res;
-        } else {
-            out = (T)kOmega * invd[r] * bv;
-        }
+        const T out = smooth_cell(g, r, e, f0, f1, f2, invd, b, x);
         xo[r] = out;
         if (dotv) acc += dotv[r] * out;
         if (dotv2) acc2 += dotv2[r] * out;
@@ -389,6 +396,31 @@ __global__ void k_mg_restrict_gather(Grid f, Grid cg, const int* __restrict__ fc
     }
 }
 
+// b_c(R) = sum over the owned members of (b - M x)
+template <typename T>
+__device__ __forceinline__ T restrict_cell(const Grid& f, const Grid& cg, long long R, const int* __restrict__ fcomp,
+                                           const int* __restrict__ ccomp, const T* __restrict__ e,
+                                           const T* __restrict__ f0, const T* __restrict__ f1,
+                                           const T* __restrict__ f2, const T* __restrict__ fb,
+                                           const T* __restrict__ fx) {
+    int I, J, K;
+    decode(cg, R, I, J, K);
+    const int own = ccomp[R];
+    T acc = (T)0;
+    if (own >= 0) {
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b)
+                for (int c = 0; c < 2; ++c) {
+                    int i = 2 * I + a, j = 2 * J + b, k = 2 * K + c;
+                    if (i >= f.I || j >= f.J || k >= f.K) continue;
+                    long long fr = lidx(f, i, j, k);
+                    if (fcomp[fr] != own) continue;
+                    acc += fb[fr] - m_apply(f, fr, i, j, k, e, f0, f1, f2, fx);
+                }
+    }
+    return acc;
+}
+
 // coarse right-hand side: b_c(R) = sum over owned members of (b - M x)
 template <typename T>
 __global__ void k_mg_restrict(Grid f, Grid cg, const int* __restrict__ fcomp, const int* __restrict__ ccomp,
@@ -396,24 +428,20 @@ __global__ void k_mg_restrict(Grid f, Grid cg, const int* __restrict__ fcomp, co
                               const T* __restrict__ f2, const T* __restrict__ fb, const T* __restrict__ fx,
                               T* __restrict__ cb) {
     for (long long R = blockIdx.x * (long long)blockDim.x + threadIdx.x; R < cg.N;
-         R += (long long)gridDim.x * blockDim.x) {
-        int I, J, K;
-        decode(cg, R, I, J, K);
-        const int own = ccomp[R];
-        T acc = (T)0;
-        if (own >= 0) {
-            for (int a = 0; a < 2; ++a)
-                for (int b = 0; b < 2; ++b)
-                    for (int c = 0; c < 2; ++c) {
-                        int i = 2 * I + a, j = 2 * J + b, k = 2 * K + c;
-                        if (i >= f.I || j >= f.J || k >= f.K) continue;
-                        long long fr = lidx(f, i, j, k);
-                        if (fcomp[fr] != own) continue;
-                        acc += fb[fr] - m_apply(f, fr, i, j, k, e, f0, f1, f2, fx);
-                    }
-        }
-        cb[R] = acc;
-    }
+         R += (long long)gridDim.x * blockDim.x)
+        cb[R] = restrict_cell(f, cg, R, fcomp, ccomp, e, f0, f1, f2, fb, fx);
+}
+
+template <typename T>
+__device__ __forceinline__ void prolong_cell(const Grid& f, const Grid& cg, long long r, const int* __restrict__ fcomp,
+                                             const int* __restrict__ ccomp, const T* __restrict__ cx,
+                                             T* __restrict__ fx, T scale) {
+    const int id = fcomp[r];
+    if (id < 0) return;
+    int i, j, k;
+    decode(f, r, i, j, k);
+    const long long R = lidx(cg, i >> 1, j >> 1, k >> 1);
+    if (ccomp[R] == id) fx[r] += scale * cx[R];
 }
 
 // x_f += kProlongScale * x_c(block) for owned members. Piecewise-constant prolongation
@@ -423,14 +451,8 @@ template <typename T>
 __global__ void k_mg_prolong(Grid f, Grid cg, const int* __restrict__ fcomp, const int* __restrict__ ccomp,
                              const T* __restrict__ cx, T* __restrict__ fx, T scale) {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < f.N;
-         r += (long long)gridDim.x * blockDim.x) {
-        int id = fcomp[r];
-        if (id < 0) continue;
-        int i, j, k;
-        decode(f, r, i, j, k);
-        long long R = lidx(cg, i >> 1, j >> 1, k >> 1);
-        if (ccomp[R] == id) fx[r] += scale * cx[R];
-    }
+         r += (long long)gridDim.x * blockDim.x)
+        prolong_cell(f, cg, r, fcomp, ccomp, cx, fx, scale);
 }
 
 // ---------------------------------------------------------------------------
@@ -497,9 +519,10 @@ __global__ void k_kc_second(Grid g, const int* __restrict__ comp, const double* 
 
 // coarsest level: a fixed number of damped Jacobi sweeps from zero by one CTA
 template <typename T>
-__global__ void k_mg_coarsest(Grid g, const int* __restrict__ comp, const T* __restrict__ e,
-                              const T* __restrict__ f0, const T* __restrict__ f1, const T* __restrict__ f2,
-                              const T* __restrict__ invd, const T* __restrict__ b, T* x, T* t, int sweeps) {
+__device__ __forceinline__ void coarsest_block(const Grid& g, const int* __restrict__ comp, const T* __restrict__ e,
+                                               const T* __restrict__ f0, const T* __restrict__ f1,
+                                               const T* __restrict__ f2, const T* __restrict__ invd,
+                                               const T* __restrict__ b, T* x, T* t, int sweeps) {
     for (long long r = threadIdx.x; r < g.N; r += blockDim.x)
         x[r] = (comp[r] >= 0) ? (T)kOmega * invd[r] * b[r] : (T)0;
     __syncthreads();
@@ -516,6 +539,70 @@ __global__ void k_mg_coarsest(Grid g, const int* __restrict__ comp, const T* __r
         }
         __syncthreads();
         for (long long r = threadIdx.x; r < g.N; r += blockDim.x) x[r] = t[r];
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void k_mg_coarsest(Grid g, const int* __restrict__ comp, const T* __restrict__ e,
+                              const T* __restrict__ f0, const T* __restrict__ f1, const T* __restrict__ f2,
+                              const T* __restrict__ invd, const T* __restrict__ b, T* x, T* t, int sweeps) {
+    coarsest_block(g, comp, e, f0, f1, f2, invd, b, x, t, sweeps);
+}
+
+// The V-cycle over the small coarse levels in one block. The levels from `first` down hold
+// a few thousand cells at most, where a kernel per sweep costs more in launch than in work
+// (the cycle over levels 5-6 of the 338x338x283 workload: 7 launches of ~7 us); one block
+// of 1024 threads runs the same cycle -- the same per-cell updates in the same order, so
+// the same results bit for bit -- with a barrier between sweeps. Level q of the tail reads
+// its right-hand side from b[q] and leaves its correction in x[q] (t[q]: scratch), as the
+// kernels of cycle() do.
+constexpr int kMaxTail = 8;
+template <typename T>
+struct TailLevels {
+    Grid g[kMaxTail];
+    const int* comp[kMaxTail];
+    const T *e[kMaxTail], *f0[kMaxTail], *f1[kMaxTail], *f2[kMaxTail], *invd[kMaxTail];
+    T *x[kMaxTail], *b[kMaxTail], *t[kMaxTail];
+    int n;  // levels in the tail; the last is the coarsest
+};
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_mg_tail(TailLevels<T> L, T scale, int sweeps) {
+    const int n = L.n;
+    // down: two smoothing sweeps from zero, then the restricted residual
+    for (int q = 0; q + 1 < n; ++q) {
+        const Grid& g = L.g[q];
+        for (long long r = threadIdx.x; r < g.N; r += blockDim.x)
+            if (L.comp[q][r] >= 0) L.t[q][r] = smooth_cell(g, r, L.e[q], L.f0[q], L.f1[q], L.f2[q], L.invd[q],
+                                                          (const T*)L.b[q], (const T*)nullptr);
+        __syncthreads();
+        for (long long r = threadIdx.x; r < g.N; r += blockDim.x)
+            if (L.comp[q][r] >= 0) L.x[q][r] = smooth_cell(g, r, L.e[q], L.f0[q], L.f1[q], L.f2[q], L.invd[q],
+                                                          (const T*)L.b[q], (const T*)L.t[q]);
+        __syncthreads();
+        const Grid& cg = L.g[q + 1];
+        for (long long R = threadIdx.x; R < cg.N; R += blockDim.x)
+            L.b[q + 1][R] = restrict_cell(g, cg, R, L.comp[q], L.comp[q + 1], L.e[q], L.f0[q], L.f1[q], L.f2[q],
+                                          (const T*)L.b[q], (const T*)L.x[q]);
+        __syncthreads();
+    }
+    const int c = n - 1;
+    coarsest_block(L.g[c], L.comp[c], L.e[c], L.f0[c], L.f1[c], L.f2[c], L.invd[c], (const T*)L.b[c], L.x[c],
+                   L.t[c], sweeps);
+    // up: the scaled coarse correction, then two smoothing sweeps
+    for (int q = n - 2; q >= 0; --q) {
+        const Grid& g = L.g[q];
+        for (long long r = threadIdx.x; r < g.N; r += blockDim.x)
+            prolong_cell(g, L.g[q + 1], r, L.comp[q], L.comp[q + 1], (const T*)L.x[q + 1], L.x[q], scale);
+        __syncthreads();
+        for (long long r = threadIdx.x; r < g.N; r += blockDim.x)
+            if (L.comp[q][r] >= 0) L.t[q][r] = smooth_cell(g, r, L.e[q], L.f0[q], L.f1[q], L.f2[q], L.invd[q],
+                                                          (const T*)L.b[q], (const T*)L.x[q]);
+        __syncthreads();
+        for (long long r = threadIdx.x; r < g.N; r += blockDim.x)
+            if (L.comp[q][r] >= 0) L.x[q][r] = smooth_cell(g, r, L.e[q], L.f0[q], L.f1[q], L.f2[q], L.invd[q],
+                                                          (const T*)L.b[q], (const T*)L.t[q]);
         __syncthreads();
     }
 }
@@ -913,8 +1000,32 @@ ls_status mg_apply(ls_ctx* c, const T* r, T* z, const T* dotv2, int* nblocks_out
         LS_LAUNCH(c, k_kc_second<T>, gd, kBlock, 0, a.g, a.comp, s, (const T*)pd, e);
         return LS_OK;
     };
+    // the small coarse levels below the K-cycle run as one block (k_mg_tail)
+    size_t tail_start = L + 1;
+    if (c->mg_tail_cells > 0)
+        for (size_t l = L; l > (size_t)kKLevels && l >= 1 && lv[l].g.N <= c->mg_tail_cells; --l) tail_start = l;
+    if (tail_start <= L && L - tail_start + 1 > (size_t)kMaxTail) tail_start = L + 1 - kMaxTail;
     cycle = [&](size_t l, const T* b, T* out, const T* dv, const T* dv2, int* nb) -> ls_status {
         Lv& a = lv[l];
+        if (l >= tail_start && !dv && b == a.b && out == a.x) {
+            TailLevels<T> tl = {};
+            tl.n = (int)(L - l + 1);
+            for (int q = 0; q < tl.n; ++q) {
+                const Lv& m = lv[l + q];
+                tl.g[q] = m.g;
+                tl.comp[q] = m.comp;
+                tl.e[q] = m.e;
+                tl.f0[q] = m.f0;
+                tl.f1[q] = m.f1;
+                tl.f2[q] = m.f2;
+                tl.invd[q] = m.invd;
+                tl.x[q] = m.x;
+                tl.b[q] = m.b;
+                tl.t[q] = m.t;
+            }
+            LS_LAUNCH(c, k_mg_tail<T>, 1, 1024, 0, tl, (T)kProlongScale, kCoarseSweeps);
+            return LS_OK;
+        }
         if (l == L) {
             LS_LAUNCH(c, k_mg_coarsest<T>, 1, 1024, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, a.invd, b, out, a.t,
                       kCoarseSweeps);

@@ -93,3 +93,17 @@ def test_create_rejects_bad_arguments_without_touching_a_gpu():
     assert L.ls_create(None, 8, 8, 8, 1, None) == _abi.LS_BAD_ARG
     assert L.ls_last_error(None) == b"null context"
     assert L.ls_destroy(None) == _abi.LS_OK
+
+
+def test_create_rejects_grids_beyond_32_bit_indices():
+    """Voxel ids and row indices are 32-bit: (I+1)*J*K plus a plane and a grid stride of
+    headroom must stay below 2^31; larger grids are refused before any device work (the
+    large single domain, 768 x 1024 x 1024, is inside the limit)."""
+    L = runtime.load()
+    h = C.c_void_p()
+    p = _abi.default_params()
+    assert L.ls_create(C.byref(h), 1300, 1300, 1300, 1, C.byref(p)) == _abi.LS_BAD_ARG
+    assert not h.value
+    assert L.ls_create(C.byref(h), 1, 8, 8, 1, C.byref(p)) == _abi.LS_BAD_ARG
+    assert L.ls_create(C.byref(h), 8, 8, 8, 3, C.byref(p)) == _abi.LS_BAD_ARG
+    assert (768 + 1) * 1024 * 1024 + 1024 * 1024 + (1 << 22) < (1 << 31)

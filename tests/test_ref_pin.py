@@ -149,7 +149,9 @@ def test_solves_and_the_write_back_offset(oracle_mod, name, dtype, lb, shape, se
     Po, Pr = o.get("pressure", padded=True), r.get("pressure", padded=True)
     same(Po[0], P0[0], "pressure plane 0 (oracle)")
     same(Pr[0], P0[0], "pressure plane 0 (reference)")
-    assert rel_l2(Po, Pr) < 1e-7  # near-null modes of the floored Pore clusters, as in test_gpu_parity.py
+    # near-null modes of the floored Pore clusters: two solves to rtol 1e-13 differ there by up
+    # to ~1.3e-7 (the oracle's OpenMP reductions make its own runs differ by as much)
+    assert rel_l2(Po, Pr) < 1e-6
     for f in ("flux_x", "flux_y", "flux_z", "conc", "acid"):
         v = rng.normal(0, 1.0, (shape[0] + 1,) + shape[1:])
         for a in (o, r):
