@@ -646,7 +646,7 @@ ls_status ls_destroy(ls_ctx* c) {
                     c->sh_label, c->sh_sat, c->sh_precip, c->sh_frac, c->shf_label, c->shf_perm,
                     c->shf_visc, c->psb2, c->sat_q, c->dbits, c->sht_label, c->sht_fx, c->sht_fy, c->sht_fz,
                     c->shq_P, c->shq_C, c->shq_K, c->shq_V, c->shq_fx, c->shq_fy, c->shq_fz,
-                    c->wlist, c->wcount, c->olist_counts, c->kmult, c->dz_sel, c->dz_flips, c->dz_save_frac,
+                    c->wlist, c->wcount, c->olist_counts, c->dz_tab, c->kmult, c->dz_sel, c->dz_flips, c->dz_save_frac,
                     c->dz_save_precip, c->dz_save_conc, c->dz_save_label};
     for (void* q : ptrs) rel(q);
     for (void* q : c->l0base) rel(q);

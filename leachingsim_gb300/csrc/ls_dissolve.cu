@@ -168,27 +168,24 @@ constexpr int kDzSkew = 7;
 // the slices w = level - kDzSkew s of the sub-steps s it covers; one thread per update.
 template <typename L>
 __global__ void __launch_bounds__(kBlock) k_dz_skew(Grid g, DzConst dc, int level, int num_steps, int nlev,
-                                                    const int* __restrict__ list, const int* __restrict__ hist,
-                                                    const int* __restrict__ start, L* __restrict__ label,
+                                                    const int* __restrict__ list, const int* __restrict__ tab,
+                                                    int nsk, const int* __restrict__ start, L* __restrict__ label,
                                                     float* __restrict__ frac, double* __restrict__ acid,
                                                     double* __restrict__ precip, double* __restrict__ conc,
                                                     int* __restrict__ leached, int* __restrict__ flips) {
     const int s_lo = level >= nlev ? (level - nlev) / kDzSkew + 1 : 0;
     const int s_hi = min(num_steps - 1, level / kDzSkew);
     const int ns = s_hi - s_lo + 1;  // slices of this level, <= ceil(nlev / kDzSkew)
-    // running totals of the slices' sizes, in shared memory (<= kDzSliceCap slices per pass)
+    // running totals of the slices' sizes from the level table the host built (tab: nsk + 1
+    // offsets, then per level ns + 1 running totals), into shared memory <= kDzSliceCap slices
+    // per pass
+    const int* __restrict__ cumg = tab + (nsk + 1) + __ldg(tab + level);
     constexpr int kDzSliceCap = 512;
     __shared__ int cum[kDzSliceCap + 1];
     for (int s0 = 0; s0 < ns; s0 += kDzSliceCap) {
         const int m = min(kDzSliceCap, ns - s0);
-        if (threadIdx.x == 0) {
-            int acc = 0;
-            for (int t = 0; t < m; ++t) {
-                cum[t] = acc;
-                acc += __ldg(hist + level - kDzSkew * (s_lo + s0 + t));
-            }
-            cum[m] = acc;
-        }
+        const int base = __ldg(cumg + s0);
+        for (int t = threadIdx.x; t <= m; t += blockDim.x) cum[t] = __ldg(cumg + s0 + t) - base;
         __syncthreads();
         const int total = cum[m];
         for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
@@ -425,19 +422,42 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
     auto run_sweeps = [&](int* flips) -> ls_status {
         LS_CUDA(c, cudaMemsetAsync(d_leached, 0, sizeof(int), c->stream));
         const int nsk = nlev + kDzSkew * (num_steps - 1);
+        // the level table: per level the running totals of its slices' sizes (slice t of level
+        // l: w = l - kDzSkew (s_lo + t)), so that no block sums them serially
+        std::vector<int>& tab = c->dz_tab_host;
+        tab.assign((size_t)nsk + 1, 0);
+        std::vector<long long> totals((size_t)nsk, 0);
         for (int l = 0; l < nsk; ++l) {
-            long long total = 0;
-            for (int s = 0; s < num_steps; ++s) {
+            tab[l] = (int)(tab.size() - (size_t)(nsk + 1));
+            const int s_lo = l >= nlev ? (l - nlev) / kDzSkew + 1 : 0;
+            const int s_hi = std::min(num_steps - 1, l / kDzSkew);
+            long long acc = 0;
+            tab.push_back(0);
+            for (int s = s_lo; s <= s_hi; ++s) {
                 const int w = l - kDzSkew * s;
-                if (w < 0) break;
-                if (w < nlev) total += hist[w];
+                acc += (w >= 0 && w < nlev) ? hist[w] : 0;
+                tab.push_back((int)acc);
             }
+            totals[l] = acc;
+        }
+        tab[nsk] = (int)(tab.size() - (size_t)(nsk + 1));
+        if ((long long)tab.size() > c->dz_tab_cap) {
+            dfree_t(c, &c->dz_tab, (size_t)c->dz_tab_cap);
+            c->dz_tab_cap = 0;
+            LS_TRY(dalloc_t(c, &c->dz_tab, tab.size()));
+            c->dz_tab_cap = (long long)tab.size();
+        }
+        LS_CUDA(c, cudaMemcpyAsync(c->dz_tab, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, c->stream));
+        for (int l = 0; l < nsk; ++l) {
+            const long long total = totals[l];
             if (total == 0) continue;
             const int blocks = (int)std::min<long long>((total + kBlock - 1) / kBlock, (long long)c->num_sms * 8);
             LS_LAUNCH(c, k_dz_skew<L>, blocks, kBlock, 0, g, dc, l, num_steps, nlev, (const int*)c->dz_list,
-                      (const int*)c->dz_count, (const int*)c->dz_level_start, (L*)c->label, c->frac, c->acid,
+                      (const int*)c->dz_tab, nsk, (const int*)c->dz_level_start, (L*)c->label, c->frac, c->acid,
                       c->precip, c->conc, d_leached, flips);
         }
+        // the host table must outlive the asynchronous copy: the call ends with a synchronisation
+        LS_CUDA(c, cudaStreamSynchronize(c->stream));
         return LS_OK;
     };
     auto prefix = [&](int total) -> ls_status {

@@ -398,6 +398,9 @@ struct ls_ctx {
     int* dz_list;         // active mineral voxels sorted by wavefront (or by dependency level)
     int* dz_count;
     int* dz_level_start;
+    int* dz_tab;                    // per-level running totals of the skewed schedule's slices
+    long long dz_tab_cap;
+    std::vector<int> dz_tab_host;
     int dz_cap;
     // sparse schedule of the dissolution sweep: the voxels that can change (in any order),
     // the voxels fully leached during a call, and the pre-sweep state of the scheduled voxels
