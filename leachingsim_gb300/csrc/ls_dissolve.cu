@@ -419,6 +419,14 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
 
     // every sub-step over the wavefront-sorted list (hist[w] voxels of level w from start[w];
     // on the device: dz_count and dz_level_start) by the skewed levels
+    // threads per block of the level launches (LS_DZ_THREADS: 32 .. 256)
+    static const int dz_threads = [] {
+        const char* e = getenv("LS_DZ_THREADS");
+        int v = e ? atoi(e) : 64;
+        if (v < 32) v = 32;
+        if (v > kBlock) v = kBlock;
+        return (v / 32) * 32;
+    }();
     auto run_sweeps = [&](int* flips) -> ls_status {
         LS_CUDA(c, cudaMemsetAsync(d_leached, 0, sizeof(int), c->stream));
         const int nsk = nlev + kDzSkew * (num_steps - 1);
@@ -448,11 +456,15 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
             c->dz_tab_cap = (long long)tab.size();
         }
         LS_CUDA(c, cudaMemcpyAsync(c->dz_tab, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, c->stream));
+        // small blocks: a level holds tens to thousands of updates of ~100 FP64 operations
+        // each (six correctly rounded divisions among them), so its time is the FP64 issue of
+        // the busiest SM; blocks of one or two warps put every warp on its own SM
         for (int l = 0; l < nsk; ++l) {
             const long long total = totals[l];
             if (total == 0) continue;
-            const int blocks = (int)std::min<long long>((total + kBlock - 1) / kBlock, (long long)c->num_sms * 8);
-            LS_LAUNCH(c, k_dz_skew<L>, blocks, kBlock, 0, g, dc, l, num_steps, nlev, (const int*)c->dz_list,
+            const int bt = dz_threads;
+            const int blocks = (int)std::min<long long>((total + bt - 1) / bt, (long long)c->num_sms * (kBlock / bt) * 8);
+            LS_LAUNCH(c, k_dz_skew<L>, blocks, bt, 0, g, dc, l, num_steps, nlev, (const int*)c->dz_list,
                       (const int*)c->dz_tab, nsk, (const int*)c->dz_level_start, (L*)c->label, c->frac, c->acid,
                       c->precip, c->conc, d_leached, flips);
         }
