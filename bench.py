@@ -226,6 +226,18 @@ def roofline(ctx, shape, nsteps):
             "launches": cnt, "us_per_launch": round(ms * 1e3 / cnt, 2)}
 
 
+def true_rel_residual(ctx):
+    """||b - A x||_2 / ||b||_2 in FP64 for the assembled pressure system and its last solution
+    (outside the timed solves: A x through the library's FP64 operator on the host arrays)."""
+    Pp = ctx.download("pressure", padded=True).ravel()
+    sh = ctx.J * ctx.K if ctx.params.compat_shift else 0
+    x = Pp[sh:sh + ctx.N]
+    b = ctx.pressure_rhs()
+    r = b - ctx.pressure_apply(x)
+    nb = float(np.linalg.norm(b))
+    return float(np.linalg.norm(r) / nb) if nb > 0 else float(np.linalg.norm(r))
+
+
 def cold_pressure_solves(ctx, shape, solver, reps=2):
     """The second metric: cold solves of the first step's pressure system (t = 0, zero
     start, rtol 1e-8 on the Jacobi-scaled FP64 residual) with the plain FP64 multigrid-PCG,
@@ -277,7 +289,8 @@ def cold_pressure_solves(ctx, shape, solver, reps=2):
         out[name] = {"solver": "fp64" if s == PRESS_FP64 else "mixed", "ms": round((w3 - w0) * 1e3, 3),
                      "setup_ms": round((w1 - w0) * 1e3, 3), "solve_ms": round((w3 - w2) * 1e3, 3),
                      "iterations": info["iterations"], "outer": info["outer_iterations"],
-                     "scaled_rel_residual": info["rel_residual"], "converged": bool(ok)}
+                     "scaled_rel_residual": info["rel_residual"],
+                     "true_rel_residual": true_rel_residual(ctx), "converged": bool(ok)}
         if start is not None:
             out[name]["start_ms"] = round((w2 - w1) * 1e3, 3)
         if s == PRESS_LEARNED:
@@ -334,7 +347,9 @@ def gpu_arm(args, ws, rank, local):
                             "outer": pinfo["outer_iterations"], "scaled_rel_residual": pinfo["rel_residual"],
                             "converged": bool(pinfo["converged"])}
     psolve.setdefault("learned", None)
-    psolve["note"] = ("cold solves of the first step's pressure system: t = 0, zero start (learned: the "
+    psolve["note"] = ("cold solves of the first step's pressure system (true_rel_residual: ||b - A x||_2 / "
+                      "||b||_2 of the result in FP64, the solves stop on the Jacobi-scaled one): t = 0, zero "
+                      "start (learned: the "
                       "network's start; constant_start: P = p_top on the Pore rows; learned_precond: the "
                       "network as the multigrid's level-4 solver inside the flexible CG, with the plain "
                       "cycle taking over on stagnation), rtol 1e-8 on the "

@@ -523,25 +523,37 @@ __global__ void __launch_bounds__(256) k_lp_conv_dw(LpDims d, const bf16* __rest
 
 // The weight gradient on the tensor cores: for tap t, dW_t (COUT x CIN) = dY^T X_t, a GEMM
 // whose K runs over the voxels (X_t: the input at the voxel shifted by the tap, 0 outside).
-// A block takes one tap and a chunk of voxels, stages 64 voxels at a time transposed in
-// shared memory (dY as A rows = output channels, X_t as B columns = input channels, K
-// contiguous so that every fragment register is one 32-bit load) and issues mma.sync
-// m16n8k16 (BF16 x BF16 -> FP32). The (COUT/16) x (CIN/8) output tiles are spread over the 8
-// warps; with fewer tiles than warps the warps also split the 4 K-steps of a stage. Partial
-// results go to dw with FP32 atomics, as the FMA kernel above does; the bias gradient (the
-// centre tap's blocks) is summed in FP32.
+// A block takes one tap and a chunk of voxels and stages 64 voxels at a time in shared
+// memory in their natural layout (a voxel's channels contiguous: 16-byte copies, rows padded
+// by 16 bytes so that the eight rows of an 8x8 matrix fall in distinct bank groups); the
+// fragments come from ldmatrix.trans (A = dY^T: rows = output channels; B = X_t: columns =
+// input channels) and feed mma.sync m16n8k16 (BF16 x BF16 -> FP32). The (COUT/16) x (CIN/8)
+// output tiles are spread over the 8 warps; with fewer tiles than warps the warps also split
+// the 4 K-steps of a stage. Partial results go to dw with FP32 atomics; the bias gradient
+// (the centre tap's blocks) is summed in FP32.
+__device__ __forceinline__ void ldmatrix_x4_trans(uint32_t (&r)[4], uint32_t addr) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(addr));
+}
+__device__ __forceinline__ void ldmatrix_x2_trans(uint32_t (&r)[2], uint32_t addr) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];\n"
+                 : "=r"(r[0]), "=r"(r[1])
+                 : "r"(addr));
+}
+
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(256) k_lp_conv_dw_mma(LpDims d, const bf16* __restrict__ in,
                                                         const bf16* __restrict__ dy, float* __restrict__ dw,
                                                         float* __restrict__ db, int chunk) {
-    constexpr int KS = 66;                       // row stride in bf16 (64 voxels + 2: 32-bit aligned)
+    constexpr int SD = COUT + 8, SX = CIN + 8;   // row strides in bf16 (16-byte multiples)
     constexpr int TILES = (COUT / 16) * (CIN / 8);
     constexpr int KGROUPS = TILES >= 8 ? 1 : 8 / TILES;  // warps sharing the tiles split K
     constexpr int TW = 8 / KGROUPS;              // warps per K-group
     constexpr int PERW = (TILES + TW - 1) / TW;  // tiles per warp
     static_assert(COUT % 16 == 0 && CIN % 8 == 0 && 8 % KGROUPS == 0, "channel counts");
-    __shared__ __align__(16) bf16 sD[COUT][KS];  // sD[co][v]
-    __shared__ __align__(16) bf16 sX[CIN][KS];   // sX[ci][v]
+    __shared__ __align__(16) bf16 sD[64 * SD];   // sD[v][co]
+    __shared__ __align__(16) bf16 sX[64 * SX];   // sX[v][ci]
     __shared__ long long sN[64];
     const int t = blockIdx.y;
     const int dz = t / 9 - 1, dyy = (t / 3) % 3 - 1, dx = t % 3 - 1;
@@ -549,6 +561,10 @@ __global__ void __launch_bounds__(256) k_lp_conv_dw_mma(LpDims d, const bf16* __
     const long long vend = (v0 + chunk < d.N) ? v0 + chunk : d.N;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3;
     const int kgroup = warp / TW, wt = warp - kgroup * TW;
+    const uint32_t sD_s = (uint32_t)__cvta_generic_to_shared(sD);
+    const uint32_t sX_s = (uint32_t)__cvta_generic_to_shared(sX);
+    // ldmatrix row of this lane: matrix q = lane / 8, row lane % 8
+    const int lq = lane >> 3, lr = lane & 7;
     float acc[PERW][4];
 #pragma unroll
     for (int q = 0; q < PERW; ++q)
@@ -568,39 +584,42 @@ __global__ void __launch_bounds__(256) k_lp_conv_dw_mma(LpDims d, const bf16* __
             }
             sN[threadIdx.x] = nb;
         }
-        for (int e = threadIdx.x; e < 64 * COUT; e += 256) {
-            const int vv = e / COUT, co = e - vv * COUT;
+        // dY rows: 64 voxels x COUT / 8 chunks of 16 bytes
+        for (int e = threadIdx.x; e < 64 * (COUT / 8); e += 256) {
+            const int vv = e / (COUT / 8), c8 = e - vv * (COUT / 8);
             const long long v = vb + vv;
-            sD[co][vv] = (v < vend) ? dy[v * COUT + co] : __float2bfloat16(0.f);
+            uint4 val = make_uint4(0u, 0u, 0u, 0u);
+            if (v < vend) val = *reinterpret_cast<const uint4*>(dy + v * COUT + c8 * 8);
+            *reinterpret_cast<uint4*>(sD + vv * SD + c8 * 8) = val;
         }
         __syncthreads();
-        for (int e = threadIdx.x; e < 64 * CIN; e += 256) {
-            const int vv = e / CIN, ci = e - vv * CIN;
+        for (int e = threadIdx.x; e < 64 * (CIN / 8); e += 256) {
+            const int vv = e / (CIN / 8), c8 = e - vv * (CIN / 8);
             const long long nb = sN[vv];
-            sX[ci][vv] = (nb >= 0) ? in[nb * CIN + ci] : __float2bfloat16(0.f);
+            uint4 val = make_uint4(0u, 0u, 0u, 0u);
+            if (nb >= 0) val = *reinterpret_cast<const uint4*>(in + nb * CIN + c8 * 8);
+            *reinterpret_cast<uint4*>(sX + vv * SX + c8 * 8) = val;
         }
         __syncthreads();
 #pragma unroll
         for (int ks = kgroup; ks < 4; ks += KGROUPS) {
-            const int k0 = ks * 16 + tig * 2;
+            const int k0 = ks * 16;
 #pragma unroll
             for (int q = 0; q < PERW; ++q) {
                 const int tile = wt + q * TW;
                 if (tile < TILES) {
                     const int m0 = (tile / (CIN / 8)) * 16, n0 = (tile % (CIN / 8)) * 8;
                     uint32_t a[4], b[2];
-                    a[0] = *reinterpret_cast<const uint32_t*>(&sD[m0 + gid][k0]);
-                    a[1] = *reinterpret_cast<const uint32_t*>(&sD[m0 + gid + 8][k0]);
-                    a[2] = *reinterpret_cast<const uint32_t*>(&sD[m0 + gid][k0 + 8]);
-                    a[3] = *reinterpret_cast<const uint32_t*>(&sD[m0 + gid + 8][k0 + 8]);
-                    b[0] = *reinterpret_cast<const uint32_t*>(&sX[n0 + gid][k0]);
-                    b[1] = *reinterpret_cast<const uint32_t*>(&sX[n0 + gid][k0 + 8]);
+                    // A (16 x 16, m = co, k = v) from sD[v][co]: matrix q = (m half q & 1, k half q >> 1)
+                    ldmatrix_x4_trans(a, sD_s + 2u * (uint32_t)((k0 + (lq >> 1) * 8 + lr) * SD + m0 + (lq & 1) * 8));
+                    // B (16 x 8, k = v, n = ci) from sX[v][ci]: matrix q = k half (lanes 0-15)
+                    ldmatrix_x2_trans(b, sX_s + 2u * (uint32_t)((k0 + (lq & 1) * 8 + lr) * SX + n0));
                     mma_16816(acc[q], a, b);
                 }
             }
         }
         if (t == 13 && threadIdx.x < COUT)
-            for (int vv = 0; vv < 64; ++vv) bacc += __bfloat162float(sD[threadIdx.x][vv]);
+            for (int vv = 0; vv < 64; ++vv) bacc += __bfloat162float(sD[vv * SD + threadIdx.x]);
         __syncthreads();
     }
 #pragma unroll
@@ -981,7 +1000,11 @@ ls_status lp_conv(ls_lpnet* n, LpDims d, int cin, int cout, const bf16* in, cons
 }
 
 ls_status lp_conv_dw(ls_lpnet* n, LpDims d, int cin, int cout, const bf16* in, const bf16* dy, float* dw, float* db) {
-    const int chunk = 2048;
+    // voxels per block: up to 2048, fewer on the coarse levels so that the 27 taps' blocks
+    // still cover the SMs a few times over (multiples of the 64-voxel stage)
+    long long ch = d.N / ((long long)n->num_sms * 2);
+    ch = std::max(256ll, std::min(2048ll, (ch + 63) / 64 * 64));
+    const int chunk = (int)ch;
     const dim3 grid((unsigned)((d.N + chunk - 1) / chunk), 27);
     // tensor cores (mma.sync); LS_LPNET_DW=0 keeps the FP32 FMA kernel (for comparison)
     static const bool fma_only = [] {

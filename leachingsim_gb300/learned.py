@@ -458,7 +458,29 @@ def main(argv=None):
     fw = sub.add_parser("forward", help="time the network's forward pass on random inputs")
     fw.add_argument("--shape", default="144,176,176", help="network grid (multiples of 8)")
     fw.add_argument("--reps", type=int, default=5)
+    ts = sub.add_parser("train-step", help="time the network's training step (forward, backward, Adam) on random inputs")
+    ts.add_argument("--shape", default="144,32,32", help="network grid (multiples of 8)")
+    ts.add_argument("--steps", type=int, default=20)
     a = ap.parse_args(argv)
+    if a.cmd == "train-step":
+        import torch
+        from .runtime import LPNet
+        shape = tuple(int(v) for v in a.shape.split(","))
+        net = LPNet(shape, seed=1)
+        g = torch.Generator(device="cuda")
+        g.manual_seed(0)
+        x = [torch.randn(shape, device="cuda", generator=g) for _ in range(4)]
+        mask = torch.ones(shape, device="cuda")
+        for _ in range(3):
+            net.train_step(x[0], x[1], x[2], x[3], mask, lr=1e-4)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            net.train_step(x[0], x[1], x[2], x[3], mask, lr=1e-4)
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3 / a.steps
+        net.close()
+        print(json.dumps({"shape": shape, "train_step_ms": round(ms, 3), "steps": a.steps}))
     if a.cmd == "forward":
         import torch
         from .runtime import LPNet
