@@ -141,8 +141,9 @@ __global__ void k_cc_hook(Grid g, const T* __restrict__ f0, const T* __restrict_
             T c = fs[d][r];
             if (!(c > (T)0)) continue;  // c > 0 only between two unknowns
             long long nb = r + offs[d];
-            double w = (double)c * sqrt((double)invd[r] * (double)invd[nb]);
-            if (!(w > kStrong)) continue;
+            // c / sqrt(d_r d_nb) > kStrong, squared: no square root on the FP64 pipe
+            const T w2 = c * c * invd[r] * invd[nb];
+            if (!(w2 > (T)(kStrong * kStrong))) continue;
             int a = (int)r, b = (int)nb;
             int spins = 0;
             while (true) {
