@@ -5,16 +5,20 @@
 // every start through the FP64 residual and finishes the solve.
 //
 // Kernels, all hand-written:
-//  * k_lp_conv_tc: 3x3x3 convolution as an implicit GEMM on the 5th-generation tensor cores
-//    (tcgen05.mma kind::f16, BF16 x BF16 -> FP32 accumulators in tensor memory): a CTA
-//    computes 16 x 8 x ZT output voxels (M = 128 per plane) x all output channels from
-//    shared-memory operands. Used where it is faster than mma.sync (32 -> 64 channels; every
-//    layer with up to 32 input channels under LS_LPNET_TC=2). With flipped, transposed
-//    weights it is also the input-gradient pass.
+//  * k_lp_conv_tma: 3x3x3 convolution as an implicit GEMM on the 5th-generation tensor cores
+//    (tcgen05.mma kind::f16, BF16 x BF16 -> FP32 accumulators in tensor memory), its input
+//    halo brought into shared memory by TMA (cp.async.bulk.tensor), streamed through z with
+//    the three dz taps stacked along N, warp-specialised (TMA / MMA / epilogue warps) on
+//    persistent CTAs. Every layer (64 output channels from 64 inputs as two launches); with
+//    flipped, transposed weights also the input-gradient pass. The default (LS_LPNET_TC=3).
+//  * k_lp_conv_tc: the first tcgen05 form, a CTA per 16 x 8 x ZT output tile with its halo
+//    staged three times by cp.async (LS_LPNET_TC=2: layers with up to 32 input channels;
+//    1: the 32 -> 64 layer alone, mma.sync elsewhere).
 //  * k_lp_conv / k_lp_conv_tiled: the same convolution with mma.sync m16n8k16 (BF16 x BF16
 //    -> FP32 in registers): a warp computes 16 output voxels x all output channels; the K
 //    dimension runs over 27 taps x input channels in chunks of 16. k_lp_conv serves the
-//    64-channel layers; k_lp_conv_tiled is the LS_LPNET_TC=0 path of the others.
+//    64-channel layers outside LS_LPNET_TC=3; k_lp_conv_tiled is the LS_LPNET_TC=0 path of
+//    the others.
 //  * k_lp_conv_dw_mma: the weight / bias gradient, staged transposed through shared memory,
 //    mma.sync m16n8k16 (k_lp_conv_dw: the same with FP32 FMA, LS_LPNET_DW=0).
 //  * pooling, upsampling + skip addition and their backward passes, ReLU masking, the
@@ -23,6 +27,7 @@
 // Layout: activations (D, H, W, C) with the channels innermost (BF16; the output layer FP32),
 // gradients the same in FP32; weights [tap][cout][cin], tap = 9 (dz+1) + 3 (dy+1) + (dx+1). D, H and W are
 // multiples of 8 (three 2x poolings).
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <cstdio>
@@ -453,6 +458,351 @@ __global__ void __launch_bounds__(kTcThreads) k_lp_conv_tc(LpDims d, const bf16*
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(S::tmem_cols));
 }
 
+// ---------------------------------------------------------------------------
+// The convolution streamed through z on the tensor cores, its input brought in by the tensor
+// memory accelerator (TMA). A persistent CTA (one per SM) runs tiles of 8 (x) x 16 (y) output
+// voxels x ZT planes. For each input plane p of a tile (z0 - 1 .. z0 + ZT) one TMA load per
+// 8-channel chunk brings the plane's 10 x 18 halo into a stage of a ring of shared-memory
+// buffers (zeros outside the grid: the tensor map's out-of-bounds fill), and nine (dy, dx) x
+// CIN/16 tcgen05.mma instructions apply the plane to the three output planes it feeds at once:
+// B stacks the dz = +1, 0, -1 weights along N (N = 3 COUT), so D is the consecutive
+// COUT-column blocks of output planes p - 1, p, p + 1 in a tensor-memory region of ZT planes
+// (at a tile's first and last planes the MMA takes only the part of N that lands inside it).
+// Every (dy, dx) tap is a plain descriptor on the one halo copy: an output row of 8 voxels is
+// one 8 x 16-byte core matrix, rows y are 160 bytes (10 voxels) apart (SBO), the two
+// 8-channel halves of a K-step a chunk apart (LBO).
+//
+// Roles, synchronised by mbarriers: warp 0 issues the TMA loads (stage full / empty), warp 1
+// the MMAs (a tcgen05.commit frees a stage once its MMAs have read it, another marks a region
+// full after a tile's last plane), warps 2-5 read a full region back (tcgen05.ld; warp w owns
+// the TMEM lanes of quarter w % 4), add the bias, apply ReLU, store the outputs and write
+// zeros back, so that every MMA accumulates. Two regions alternate: a tile's epilogue
+// overlaps the next tile's loads and MMAs. Every wait is bounded (kTmWaitCycles): one that gives
+// up raises the CTA's abort flag, the CTA drains the copies and MMAs it issued (bounded
+// waits too), frees its tensor memory, counts a timeout and returns.
+constexpr int kTmX = 8, kTmY = 16, kTmHX = kTmX + 2, kTmHY = kTmY + 2;
+constexpr int kTmBox = kTmHX * kTmHY * 16;                // bytes of one box: 8 channels x 10 x 18
+constexpr int kTmChunk = (kTmBox + 127) / 128 * 128;      // its slot in a stage (128-byte aligned)
+constexpr int kTmThreads = 192;
+
+// COUT = the output channels of one launch (a 64-channel output runs as two launches of 32)
+template <int CIN, int COUT>
+struct TmShape {
+    static constexpr int CH = CIN / 8, KC = CIN / 16;
+    static constexpr int ZT = 256 / COUT;                 // two regions of ZT x COUT = 256 columns
+    static constexpr int region = ZT * COUT;
+    static constexpr int stage_bytes = CH * kTmChunk;
+    static constexpr int NB = 3 * COUT / 8;               // n8 groups of the stacked B
+    static constexpr int w_bytes = 27 * CIN * COUT * 2;
+    // as many halo stages as fit beside the weights in 200 KB (4 to 32)
+    static constexpr int fit = (200 * 1024 - w_bytes) / stage_bytes;
+    static constexpr int stages = fit < 4 ? 4 : fit > 32 ? 32 : fit;
+    static constexpr int smem = w_bytes + stages * stage_bytes + 1024;  // + alignment of the base
+};
+
+// bounded wait for the completion of the mbarrier phase of the given parity; false when it
+// gave up (raising the abort flag) or another role raised it (abort null: drain waits). The
+// bound is counted in SM clock cycles (kTmWaitCycles, about 2 s), read only once a first poll
+// has failed.
+constexpr long long kTmWaitCycles = 4000000000ll;
+
+__device__ __forceinline__ bool tm_poll(uint32_t bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+__device__ __forceinline__ bool tm_wait(uint32_t bar, uint32_t parity, volatile int* abort, bool backoff) {
+    if (tm_poll(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (true) {
+        if (tm_poll(bar, parity)) return true;
+        if (abort && *abort) return false;
+        if (clock64() - t0 > kTmWaitCycles) {
+            if (abort) *abort = 1;
+            return false;
+        }
+        if (backoff) __nanosleep(32);
+    }
+}
+
+__device__ __forceinline__ void tm_bar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void tm_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tm_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// 4-D tiled TMA load (coordinates innermost first) into shared memory, completing on bar
+__device__ __forceinline__ void tm_load4(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                         uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];\n" ::"r"(dst),
+        "l"((unsigned long long)map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void tm_mma(uint32_t dtm, uint64_t da, uint64_t db, uint32_t idesc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtm),
+        "l"(da), "l"(db), "r"(idesc), "r"(1u));
+}
+
+__device__ __forceinline__ void tm_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tm_ld16(uint32_t (&r)[16], uint32_t ta) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(ta));
+}
+
+__device__ __forceinline__ void tm_st16_zero(uint32_t ta) {
+    const uint32_t z = 0u;
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};\n" ::"r"(ta),
+        "r"(z), "r"(z), "r"(z), "r"(z), "r"(z), "r"(z), "r"(z), "r"(z), "r"(z), "r"(z), "r"(z), "r"(z), "r"(z), "r"(z),
+        "r"(z), "r"(z)
+        : "memory");
+}
+
+template <typename T>
+__device__ __forceinline__ void store16(T* p, const float (&f)[16]);
+template <>
+__device__ __forceinline__ void store16<bf16>(bf16* p, const float (&f)[16]) {
+    uint32_t u[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(f[2 * q], f[2 * q + 1]);
+        u[q] = *reinterpret_cast<const uint32_t*>(&h);
+    }
+    reinterpret_cast<uint4*>(p)[0] = make_uint4(u[0], u[1], u[2], u[3]);
+    reinterpret_cast<uint4*>(p)[1] = make_uint4(u[4], u[5], u[6], u[7]);
+}
+template <>
+__device__ __forceinline__ void store16<float>(float* p, const float (&f)[16]) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        reinterpret_cast<float4*>(p)[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+}
+
+// Output channels co0 .. co0 + COUT - 1 of a layer with cout_total (the weights' and the
+// bias's row count); out holds ostride values per voxel (only0: channel co0 alone, the
+// network's output channel); zt <= TmShape::ZT output planes per tile
+template <int CIN, int COUT, bool RELU, typename OutT>
+__global__ void __launch_bounds__(kTmThreads, 1) k_lp_conv_tma(const __grid_constant__ CUtensorMap tmap, LpDims d,
+                                                               const bf16* __restrict__ w,
+                                                               const float* __restrict__ bias,
+                                                               OutT* __restrict__ out, int cout_total, int co0,
+                                                               int ostride, int only0, int zt) {
+    using S = TmShape<CIN, COUT>;
+    constexpr int kTmStages = S::stages;
+    static_assert(CIN % 16 == 0 && CIN <= 64 && COUT % 16 == 0 && COUT <= 64, "channel counts");
+    extern __shared__ uint8_t tm_smem_raw[];
+    __shared__ __align__(8) uint64_t bar_full[kTmStages], bar_empty[kTmStages], bar_tfull[2], bar_tempty[2], bar_drain;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int s_abort;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t sW = ((uint32_t)__cvta_generic_to_shared(tm_smem_raw) + 1023u) & ~1023u;  // weights, then stages
+    const uint32_t sA = sW + S::w_bytes;
+    const int tiles_x = (d.W + kTmX - 1) / kTmX, tiles_y = (d.H + kTmY - 1) / kTmY;
+    const int ntiles = tiles_x * tiles_y * ((d.D + zt - 1) / zt);
+    auto sbar = [](uint64_t* b) { return (uint32_t)__cvta_generic_to_shared(b); };
+    volatile int* abort = &s_abort;
+
+    // the stacked weights: B[tap9][K-step][k8][n8 group] core matrices, row n = j COUT + co
+    // holding the weights of dz = 1 - j (output plane p - 1 + j from input plane p)
+    for (int e = tid; e < 27 * COUT * S::CH; e += kTmThreads) {
+        const int q = e % S::CH;
+        const int nn = (e / S::CH) % (3 * COUT), t9 = e / (S::CH * 3 * COUT);
+        const int j = nn / COUT, co = nn % COUT;
+        const uint4 v =
+            __ldg(reinterpret_cast<const uint4*>(w + ((size_t)(9 * (2 - j) + t9) * cout_total + co0 + co) * CIN + q * 8));
+        const uint32_t dst = sW + (uint32_t)((((t9 * S::KC + (q >> 1)) * 2 + (q & 1)) * S::NB + (nn >> 3)) * 128 +
+                                             (nn & 7) * 16);
+        asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};\n" ::"r"(dst), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
+                     : "memory");
+    }
+    if (tid == 0) {
+        s_abort = 0;
+        for (int s = 0; s < kTmStages; ++s) {
+            tm_bar_init(sbar(&bar_full[s]), 1);
+            tm_bar_init(sbar(&bar_empty[s]), 1);
+        }
+        for (int r = 0; r < 2; ++r) {
+            tm_bar_init(sbar(&bar_tfull[r]), 1);
+            tm_bar_init(sbar(&bar_tempty[r]), 4);
+        }
+        tm_bar_init(sbar(&bar_drain), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(
+                         (uint32_t)__cvta_generic_to_shared(&tmem_slot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    if (warp >= 2) {  // every MMA accumulates: tensor memory starts at zero
+        const uint32_t lanes = (uint32_t)((warp & 3) * 32) << 16;
+        for (int c = 0; c < 512; c += 16) tm_st16_zero(tmem + lanes + (uint32_t)c);
+        asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the weights, for the MMAs
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+
+    uint32_t loaded = 0;   // warp 0: planes whose loads were issued
+    bool issued = false;   // warp 1: any MMA issued
+    if (warp == 0) {
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+            const int tx = tile % tiles_x, ty = (tile / tiles_x) % tiles_y, tz = tile / (tiles_x * tiles_y);
+            const int x0 = tx * kTmX, y0 = ty * kTmY, z0 = tz * zt;
+            bool ok = true;
+            for (int li = 0; li < zt + 2 && ok; ++li) {
+                const int p = z0 - 1 + li;
+                if (p < 0 || p >= d.D) continue;
+                const int s = (int)(loaded % kTmStages);
+                const uint32_t ph = (loaded / kTmStages) & 1u;
+                if (lane == 0) {
+                    ok = tm_wait(sbar(&bar_empty[s]), ph ^ 1u, abort, false);
+                    if (ok) {
+                        tm_expect_tx(sbar(&bar_full[s]), (uint32_t)(S::CH * kTmBox));
+                        for (int q = 0; q < S::CH; ++q)
+                            tm_load4(sA + (uint32_t)(s * S::stage_bytes + q * kTmChunk), &tmap, q * 8, x0 - 1, y0 - 1, p,
+                                     sbar(&bar_full[s]));
+                    }
+                }
+                ok = __shfl_sync(0xffffffffu, ok, 0);
+                if (ok) ++loaded;
+            }
+            if (!ok) break;
+        }
+    } else if (warp == 1) {
+        const uint32_t idesc0 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(128 >> 4) << 24);
+        const uint64_t db0 = tc_desc(sW, S::NB * 128, 128);
+        uint32_t used = 0;
+        int it = 0;
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+            const int tz = tile / (tiles_x * tiles_y), z0 = tz * zt;
+            const int r = it & 1;
+            bool ok = true;
+            if (lane == 0) ok = tm_wait(sbar(&bar_tempty[r]), (((uint32_t)it >> 1) & 1u) ^ 1u, abort, false);
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            for (int li = 0; li < zt + 2 && ok; ++li) {
+                const int p = z0 - 1 + li;
+                if (p < 0 || p >= d.D) continue;
+                const int s = (int)(used % kTmStages);
+                const uint32_t ph = (used / kTmStages) & 1u;
+                if (lane == 0) {
+                    ok = tm_wait(sbar(&bar_full[s]), ph, abort, false);
+                    if (ok) {
+                        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                        const int j0 = li < 2 ? 2 - li : 0;
+                        const int j1 = zt + 2 - li < 3 ? zt + 2 - li : 3;
+                        const uint32_t idesc = idesc0 | ((uint32_t)(((j1 - j0) * COUT) >> 3) << 17);
+                        const uint32_t dtm = tmem + (uint32_t)(r * S::region + (li + j0 - 2) * COUT);
+                        const uint64_t da0 = tc_desc(sA + (uint32_t)(s * S::stage_bytes), kTmChunk, kTmHX * 16);
+                        const uint64_t dbj = db0 + (uint64_t)((j0 * (COUT / 8) * 128) >> 4);
+#pragma unroll
+                        for (int t9 = 0; t9 < 9; ++t9) {
+                            const int dy = t9 / 3 - 1, dx = t9 % 3 - 1;
+#pragma unroll
+                            for (int kc = 0; kc < S::KC; ++kc) {
+                                const uint64_t da =
+                                    da0 + (uint64_t)((2 * kc * kTmChunk + ((dy + 1) * kTmHX + (dx + 1)) * 16) >> 4);
+                                const uint64_t db = dbj + (uint64_t)(((t9 * S::KC + kc) * 2 * S::NB * 128) >> 4);
+                                tm_mma(dtm, da, db, idesc);
+                            }
+                        }
+                        tm_commit(sbar(&bar_empty[s]));  // the stage is free once these MMAs have read it
+                        issued = true;
+                    }
+                }
+                ok = __shfl_sync(0xffffffffu, ok, 0);
+                if (ok) ++used;
+            }
+            if (!ok) break;
+            if (lane == 0) tm_commit(sbar(&bar_tfull[r]));
+        }
+    } else {
+        const int quarter = warp & 3;
+        const uint32_t lanes = (uint32_t)(quarter * 32) << 16;
+        const int m = quarter * 32 + lane;
+        int it = 0;
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+            const int tx = tile % tiles_x, ty = (tile / tiles_x) % tiles_y, tz = tile / (tiles_x * tiles_y);
+            const int x = tx * kTmX + (m & 7), y = ty * kTmY + (m >> 3), z0 = tz * zt;
+            const int r = it & 1;
+            if (!__all_sync(0xffffffffu, tm_wait(sbar(&bar_tfull[r]), ((uint32_t)it >> 1) & 1u, abort, true))) break;
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const bool okxy = x < d.W && y < d.H;
+            for (int s = 0; s < zt; ++s) {
+                const int z = z0 + s;
+                const bool ok = okxy && z < d.D;
+                OutT* dst =
+                    out + (((long long)(ok ? z : 0) * d.H + (ok ? y : 0)) * d.W + (ok ? x : 0)) * ostride + co0;
+#pragma unroll
+                for (int c0 = 0; c0 < COUT; c0 += 16) {
+                    uint32_t v[16];
+                    const uint32_t ta = tmem + lanes + (uint32_t)(r * S::region + s * COUT + c0);
+                    tm_ld16(v, ta);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                    tm_st16_zero(ta);
+                    if (ok && !only0) {
+                        float f[16];
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) {
+                            float a = __uint_as_float(v[q]) + (bias ? __ldg(bias + co0 + c0 + q) : 0.f);
+                            f[q] = RELU ? fmaxf(a, 0.f) : a;
+                        }
+                        store16<OutT>(dst + c0, f);
+                    } else if (ok && c0 == 0) {
+                        const float a = __uint_as_float(v[0]) + (bias ? __ldg(bias + co0) : 0.f);
+                        dst[0] = (OutT)(RELU ? fmaxf(a, 0.f) : a);
+                    }
+                }
+            }
+            asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) tm_arrive(sbar(&bar_tempty[r]));
+        }
+    }
+    // drain: no copy or MMA of this CTA may be in flight when it frees its memory
+    if (warp == 0 && lane == 0)
+        for (uint32_t k = loaded > (uint32_t)kTmStages ? loaded - kTmStages : 0u; k < loaded; ++k)
+            tm_wait(sbar(&bar_full[k % kTmStages]), (k / kTmStages) & 1u, nullptr, false);
+    if (warp == 1 && lane == 0 && issued) {
+        tm_commit(sbar(&bar_drain));
+        tm_wait(sbar(&bar_drain), 0u, nullptr, false);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (tid == 0 && s_abort) atomicAdd(&g_lp_tc_timeouts, 1);
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem));
+}
+
 // dw[tap][co][ci] += sum_v dy[v, co] in[v + tap, ci]; db[co] += sum_v dy[v, co] (tap 13).
 // Block (chunk of voxels, tap): 64-voxel slices of dy and of the shifted input staged in
 // shared memory, each thread accumulating its (co, ci) pairs, one atomic add per pair.
@@ -637,6 +987,107 @@ __global__ void __launch_bounds__(256) k_lp_conv_dw_mma(LpDims d, const bf16* __
     if (t == 13 && threadIdx.x < COUT) atomicAdd(&db[threadIdx.x], bacc);
 }
 
+// The weight / bias gradient of the layers with 16 or 32 input and output channels (16 -> 16,
+// 16 -> 32, 32 -> 16), tiled like k_lp_conv_tiled: a persistent
+// block walks tiles of 16 (x) x 4 (y) x 2 (z) voxels; per tile it stages the input halo
+// (18 x 6 x 4 voxels, zeros outside the grid) and the tile's output gradient (zeros outside)
+// once, and each of its 8 warps runs the GEMMs dW_t += dY^T X_t of its taps (t = warp,
+// warp + 8, ...) over the tile's 128 voxels on mma.sync m16n8k16: per row of 16 voxels one
+// A fragment (dY^T, ldmatrix.trans from [voxel][co]) serves all the warp's taps, each tap's B
+// fragment (X shifted by the tap, ldmatrix.trans from the halo) is a plain row offset. The
+// sums stay in registers across all the block's tiles; one atomic add per weight and block.
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(256, (CIN * COUT > 256) ? 1 : 2)
+    k_lp_conv_dw_tiled(LpDims d, const bf16* __restrict__ in, const bf16* __restrict__ dy, float* __restrict__ dw,
+                       float* __restrict__ db) {
+    static_assert((CIN == 16 || CIN == 32) && (COUT == 16 || COUT == 32) && CIN * COUT <= 512, "channel counts");
+    constexpr int SX = CIN + 8, SD = COUT + 8, CH = CIN / 8, NT = CIN / 8, MT = COUT / 16, TPW = 4;
+    constexpr int kTile = kTX * kTY * kTZ;
+    __shared__ __align__(16) bf16 sX[kHalo * SX];
+    __shared__ __align__(16) bf16 sD[kTile * SD];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3;
+    const int lq = lane >> 3, lr = lane & 7;
+    const uint32_t sX_s = (uint32_t)__cvta_generic_to_shared(sX);
+    const uint32_t sD_s = (uint32_t)__cvta_generic_to_shared(sD);
+    const int tiles_x = (d.W + kTX - 1) / kTX, tiles_y = (d.H + kTY - 1) / kTY;
+    const long long ntiles = (long long)tiles_x * tiles_y * ((d.D + kTZ - 1) / kTZ);
+    float acc[TPW][MT][NT][4];
+#pragma unroll
+    for (int q = 0; q < TPW; ++q)
+#pragma unroll
+        for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+            for (int nt = 0; nt < NT; ++nt)
+                acc[q][mt][nt][0] = acc[q][mt][nt][1] = acc[q][mt][nt][2] = acc[q][mt][nt][3] = 0.f;
+    float bacc = 0.f;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int tx = (int)(tile % tiles_x), ty = (int)((tile / tiles_x) % tiles_y), tz = (int)(tile / ((long long)tiles_x * tiles_y));
+        const int x0 = tx * kTX, y0 = ty * kTY, z0 = tz * kTZ;
+        for (int e = threadIdx.x; e < kHalo * CH; e += blockDim.x) {
+            const int hv = e / CH, q = e - hv * CH;
+            const int hx = hv % kHX, hy = (hv / kHX) % kHY, hz = hv / (kHX * kHY);
+            const int gx = x0 + hx - 1, gy = y0 + hy - 1, gz = z0 + hz - 1;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (gx >= 0 && gx < d.W && gy >= 0 && gy < d.H && gz >= 0 && gz < d.D)
+                v = __ldg(reinterpret_cast<const uint4*>(in + (((long long)gz * d.H + gy) * d.W + gx) * CIN) + q);
+            *reinterpret_cast<uint4*>(sX + hv * SX + q * 8) = v;
+        }
+        for (int e = threadIdx.x; e < kTile * (COUT / 8); e += blockDim.x) {
+            const int vv = e / (COUT / 8), c8 = e - vv * (COUT / 8);
+            const int gx = x0 + vv % kTX, gy = y0 + (vv / kTX) % kTY, gz = z0 + vv / (kTX * kTY);
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (gx < d.W && gy < d.H && gz < d.D)
+                v = __ldg(reinterpret_cast<const uint4*>(dy + (((long long)gz * d.H + gy) * d.W + gx) * COUT) + c8);
+            *reinterpret_cast<uint4*>(sD + vv * SD + c8 * 8) = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < COUT)
+            for (int vv = 0; vv < kTile; ++vv) bacc += __bfloat162float(sD[vv * SD + threadIdx.x]);
+#pragma unroll 1
+        for (int r = 0; r < kTY * kTZ; ++r) {  // rows of 16 voxels: the K steps
+            const int ry = r % kTY, rz = r / kTY;
+            uint32_t a[MT][4];
+#pragma unroll
+            for (int mt = 0; mt < MT; ++mt)
+                ldmatrix_x4_trans(a[mt], sD_s + 2u * (uint32_t)((r * kTX + (lq >> 1) * 8 + lr) * SD + mt * 16 + (lq & 1) * 8));
+#pragma unroll
+            for (int q = 0; q < TPW; ++q) {
+                const int t = warp + 8 * q;
+                if (t < 27) {
+                    const int tdz = t / 9 - 1, tdy = (t / 3) % 3 - 1, tdx = t % 3 - 1;
+                    const int hrow = ((rz + 1 + tdz) * kHY + (ry + 1 + tdy)) * kHX + 1 + tdx;
+#pragma unroll
+                    for (int nt = 0; nt < NT; ++nt) {
+                        uint32_t b[2];
+                        ldmatrix_x2_trans(b, sX_s + 2u * (uint32_t)((hrow + (lq & 1) * 8 + lr) * SX + nt * 8));
+#pragma unroll
+                        for (int mt = 0; mt < MT; ++mt) mma_16816(acc[q][mt][nt], a[mt], b);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < TPW; ++q) {
+        const int t = warp + 8 * q;
+        if (t < 27) {
+            float* base = dw + (size_t)t * COUT * CIN;
+#pragma unroll
+            for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+                for (int nt = 0; nt < NT; ++nt) {
+                    const size_t r0 = (size_t)(mt * 16 + gid) * CIN + nt * 8 + tig * 2, r1 = r0 + 8 * CIN;
+                    atomicAdd(&base[r0], acc[q][mt][nt][0]);
+                    atomicAdd(&base[r0 + 1], acc[q][mt][nt][1]);
+                    atomicAdd(&base[r1], acc[q][mt][nt][2]);
+                    atomicAdd(&base[r1 + 1], acc[q][mt][nt][3]);
+                }
+        }
+    }
+    if (threadIdx.x < COUT) atomicAdd(&db[threadIdx.x], bacc);
+}
+
 // wt[26 - tap][ci][co] = w[tap][co][ci] (the input-gradient convolution)
 __global__ void k_lp_wt(const bf16* __restrict__ w, bf16* __restrict__ wt, int cin, int cout) {
     const int n = 27 * cin * cout;
@@ -648,100 +1099,152 @@ __global__ void k_lp_wt(const bf16* __restrict__ w, bf16* __restrict__ wt, int c
 }
 
 // the 16-channel input: channels 0..2 from three FP32 fields, the rest 0
+// Elementwise kernels: one thread per voxel and 16-byte group of channels (8 BF16 or 4 FP32),
+// so that each decodes its voxel once and moves whole 16-byte words; the arithmetic (order of
+// the sums included) is per channel as written.
+__device__ __forceinline__ void bf8_to_f(const uint4& u, float (&f)[8]) {
+    const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        f[2 * q] = __uint_as_float(w[q] << 16);
+        f[2 * q + 1] = __uint_as_float(w[q] & 0xffff0000u);
+    }
+}
+
+__device__ __forceinline__ uint32_t bf2_bits(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+__device__ __forceinline__ uint4 f_to_bf8(const float (&f)[8]) {
+    return make_uint4(bf2_bits(f[0], f[1]), bf2_bits(f[2], f[3]), bf2_bits(f[4], f[5]), bf2_bits(f[6], f[7]));
+}
+
+// the 16 input channels: the three fields, then zeros
 __global__ void k_lp_pack(LpDims d, const float* __restrict__ c0, const float* __restrict__ c1,
                           const float* __restrict__ c2, bf16* __restrict__ x) {
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < d.N; v += (long long)gridDim.x * blockDim.x) {
-        __nv_bfloat162* o = reinterpret_cast<__nv_bfloat162*>(x + v * 16);
-        o[0] = __floats2bfloat162_rn(c0[v], c1[v]);
-        o[1] = __floats2bfloat162_rn(c2[v], 0.f);
-        const __nv_bfloat162 z = __floats2bfloat162_rn(0.f, 0.f);
-        for (int q = 2; q < 8; ++q) o[q] = z;
+        uint4* o = reinterpret_cast<uint4*>(x + v * 16);
+        o[0] = make_uint4(bf2_bits(c0[v], c1[v]), bf2_bits(c2[v], 0.f), 0u, 0u);
+        o[1] = make_uint4(0u, 0u, 0u, 0u);
     }
 }
 
-// coarse = mean of the 2x2x2 children (fine dims df, coarse dims dc)
+// coarse = mean of the 2x2x2 children (fine dims 2 dc), C a multiple of 8
 __global__ void k_lp_pool(LpDims dc, int C, const bf16* __restrict__ fine, bf16* __restrict__ coarse) {
-    const int Wf = dc.W * 2, Hf = dc.H * 2;
-    const long long n = dc.N * C;
+    const int Wf = dc.W * 2, Hf = dc.H * 2, CH = C / 8, sh = __ffs(CH) - 1;
+    const long long n = dc.N * CH;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const long long v = e / C;
-        const int c = (int)(e - v * C);
+        const long long v = e >> sh;
+        const int q = (int)(e - (v << sh));
         int z, y, x;
         lp_decode(dc, v, z, y, x);
-        float s = 0.f;
+        float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         for (int a = 0; a < 2; ++a)
             for (int b = 0; b < 2; ++b)
-                for (int q = 0; q < 2; ++q)
-                    s += __bfloat162float(fine[((((long long)(2 * z + a) * Hf) + 2 * y + b) * Wf + 2 * x + q) * C + c]);
-        coarse[e] = __float2bfloat16_rn(s * 0.125f);
+                for (int c = 0; c < 2; ++c) {
+                    float f[8];
+                    bf8_to_f(__ldg(reinterpret_cast<const uint4*>(
+                                 fine + ((((long long)(2 * z + a) * Hf) + 2 * y + b) * Wf + 2 * x + c) * C) + q),
+                             f);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) s[k] += f[k];
+                }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) s[k] *= 0.125f;
+        reinterpret_cast<uint4*>(coarse + v * C)[q] = f_to_bf8(s);
     }
 }
 
-// out(fine) = coarse(parent) + skip
+// out(fine) = coarse(parent) + skip, C a multiple of 8
 __global__ void k_lp_up_add(LpDims df, int C, const bf16* __restrict__ coarse, const bf16* __restrict__ skip,
                             bf16* __restrict__ out) {
-    const int Wc = df.W / 2, Hc = df.H / 2;
-    const long long n = df.N * C;
+    const int Wc = df.W / 2, Hc = df.H / 2, CH = C / 8, sh = __ffs(CH) - 1;
+    const long long n = df.N * CH;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const long long v = e / C;
-        const int c = (int)(e - v * C);
+        const long long v = e >> sh;
+        const int q = (int)(e - (v << sh));
         int z, y, x;
         lp_decode(df, v, z, y, x);
         const long long p = (((long long)(z / 2) * Hc) + y / 2) * Wc + x / 2;
-        out[e] = __float2bfloat16_rn(__bfloat162float(coarse[p * C + c]) + __bfloat162float(skip[e]));
+        float a[8], b[8];
+        bf8_to_f(__ldg(reinterpret_cast<const uint4*>(coarse + p * C) + q), a);
+        bf8_to_f(__ldg(reinterpret_cast<const uint4*>(skip + v * C) + q), b);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] += b[k];
+        reinterpret_cast<uint4*>(out + v * C)[q] = f_to_bf8(a);
     }
 }
 
-// coarse gradient = sum of the 8 children's gradients (backward of the upsampling)
+// coarse gradient = sum of the 8 children's gradients (backward of the upsampling), C a
+// multiple of 4
 __global__ void k_lp_up_bwd(LpDims dc, int C, const float* __restrict__ fine, float* __restrict__ coarse) {
-    const int Wf = dc.W * 2, Hf = dc.H * 2;
-    const long long n = dc.N * C;
+    const int Wf = dc.W * 2, Hf = dc.H * 2, CH = C / 4, sh = __ffs(CH) - 1;
+    const long long n = dc.N * CH;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const long long v = e / C;
-        const int c = (int)(e - v * C);
+        const long long v = e >> sh;
+        const int q = (int)(e - (v << sh));
         int z, y, x;
         lp_decode(dc, v, z, y, x);
-        float s = 0.f;
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int a = 0; a < 2; ++a)
             for (int b = 0; b < 2; ++b)
-                for (int q = 0; q < 2; ++q)
-                    s += fine[((((long long)(2 * z + a) * Hf) + 2 * y + b) * Wf + 2 * x + q) * C + c];
-        coarse[e] = s;
+                for (int c = 0; c < 2; ++c) {
+                    const float4 f = __ldg(reinterpret_cast<const float4*>(
+                                               fine + ((((long long)(2 * z + a) * Hf) + 2 * y + b) * Wf + 2 * x + c) * C) +
+                                           q);
+                    s.x += f.x; s.y += f.y; s.z += f.z; s.w += f.w;
+                }
+        reinterpret_cast<float4*>(coarse + v * C)[q] = s;
     }
 }
 
-// fine gradient += coarse gradient (parent) / 8 (backward of the pooling)
+// fine gradient += coarse gradient (parent) / 8 (backward of the pooling), C a multiple of 4
 __global__ void k_lp_pool_bwd_add(LpDims df, int C, const float* __restrict__ coarse, float* __restrict__ fine) {
-    const int Wc = df.W / 2, Hc = df.H / 2;
-    const long long n = df.N * C;
+    const int Wc = df.W / 2, Hc = df.H / 2, CH = C / 4, sh = __ffs(CH) - 1;
+    const long long n = df.N * CH;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const long long v = e / C;
-        const int c = (int)(e - v * C);
+        const long long v = e >> sh;
+        const int q = (int)(e - (v << sh));
         int z, y, x;
         lp_decode(df, v, z, y, x);
         const long long p = (((long long)(z / 2) * Hc) + y / 2) * Wc + x / 2;
-        fine[e] += coarse[p * C + c] * 0.125f;
+        const float4 c = __ldg(reinterpret_cast<const float4*>(coarse + p * C) + q);
+        float4* f = reinterpret_cast<float4*>(fine + v * C) + q;
+        float4 o = *f;
+        o.x += c.x * 0.125f; o.y += c.y * 0.125f; o.z += c.z * 0.125f; o.w += c.w * 0.125f;
+        *f = o;
     }
 }
 
-// BF16 gradient at a layer output: d masked by the ReLU (out > 0) when relu is set
+// BF16 gradient at a layer output: d masked by the ReLU (out > 0) when relu is set; n a
+// multiple of 8
 __global__ void k_lp_mask(long long n, const float* __restrict__ d, const bf16* __restrict__ out, int relu,
                           bf16* __restrict__ q) {
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const float v = (!relu || __bfloat162float(out[e]) > 0.f) ? d[e] : 0.f;
-        q[e] = __float2bfloat16_rn(v);
+    const long long n8 = n / 8;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n8; e += (long long)gridDim.x * blockDim.x) {
+        const float4 d0 = __ldg(reinterpret_cast<const float4*>(d) + 2 * e);
+        const float4 d1 = __ldg(reinterpret_cast<const float4*>(d) + 2 * e + 1);
+        float v[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
+        if (relu) {
+            float o[8];
+            bf8_to_f(__ldg(reinterpret_cast<const uint4*>(out) + e), o);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) v[k] = o[k] > 0.f ? v[k] : 0.f;
+        }
+        reinterpret_cast<uint4*>(q)[e] = f_to_bf8(v);
     }
 }
 
 // masked mean-square loss on output channel 0 and its gradient (16 channels, the others 0);
 // partial sums of the squared error per block
-__global__ void __launch_bounds__(kBlock) k_lp_loss(long long N, const float* __restrict__ y,
+__global__ void __launch_bounds__(kBlock) k_lp_loss(long long N, const float* __restrict__ y, int ys,
                                                     const float* __restrict__ target, const float* __restrict__ mask,
                                                     float inv_n, float* __restrict__ dy, double* __restrict__ partials) {
     double acc = 0.0;
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < N; v += (long long)gridDim.x * blockDim.x) {
         const float m = mask[v];
-        const float diff = (y[v * 16] - target[v]) * m;
+        const float diff = (y[v * ys] - target[v]) * m;
         acc += (double)diff * diff;
         float4* o = reinterpret_cast<float4*>(dy + v * 16);
         o[0] = make_float4(2.f * diff * inv_n, 0.f, 0.f, 0.f);
@@ -752,9 +1255,9 @@ __global__ void __launch_bounds__(kBlock) k_lp_loss(long long N, const float* __
 }
 
 // output channel 0 to FP32
-__global__ void k_lp_out(long long N, const float* __restrict__ y, float* __restrict__ out) {
+__global__ void k_lp_out(long long N, const float* __restrict__ y, int ys, float* __restrict__ out) {
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < N; v += (long long)gridDim.x * blockDim.x)
-        out[v] = y[v * 16];
+        out[v] = y[v * ys];
 }
 
 // Adam on the FP32 master parameters; the BF16 copy of every weight follows
@@ -844,7 +1347,8 @@ using ls::LpLayer;
 struct ls_lpnet {
     int D, H, W;
     int device, num_sms;
-    int use_tc;             // tcgen05 convolutions: 0 none, 1 where measured faster than mma.sync
+    int use_tc;             // convolutions: 3 the TMA-fed tcgen05 kernel (default), 0 mma.sync only, 1 the
+                            // first tcgen05 kernel where it beat mma.sync
                             // (32 -> 64), 2 every layer with CIN <= 32 (LS_LPNET_TC)
     cudaStream_t stream;
     LpLayer layer[kLpLayers];
@@ -856,7 +1360,8 @@ struct ls_lpnet {
     int adam_t;
     // activations (BF16) per level
     bf16 *x, *a0, *s0, *p1, *s1, *p2, *s2, *p3, *a3, *u2, *b2, *u1, *b1, *u0;
-    float* y;               // FP32 output layer (16 channels, channel 0 used)
+    float* y;               // FP32 output layer (channel 0 used): y_stride values per voxel
+    int y_stride;           // 16, or 1 where the layer stores channel 0 alone
     // gradients (FP32)
     float *gy, *g0, *g0b, *g1, *g1b, *g2, *g2b, *g3, *g3b;
     bf16* q;                // BF16 masked gradient scratch
@@ -909,7 +1414,8 @@ int lp_grid(const ls_lpnet* n, long long work, int block) {
 }
 
 // conv forward / input-gradient dispatch over the channel pairs of the network
-// Planes per tile, halo buffers and persistence, measured per layer at 144x176x176 (the
+// The first tcgen05 kernel (k_lp_conv_tc): planes per tile, halo buffers and persistence,
+// measured per layer at 144x176x176 (the
 // weights plus NBUF halo buffers fit one CTA's shared memory, <= 227 KB). The layers with
 // 16 input or 16 output channels run one tile per CTA, two or three CTAs per SM overlapping
 // one another's staging and MMAs (16 -> 16: 420 us so, 479 as persistent CTAs three per SM
@@ -960,14 +1466,93 @@ ls_status lp_conv_tc(ls_lpnet* n, LpDims d, const bf16* in, const bf16* w, const
     return LS_OK;
 }
 
+// cuTensorMapEncodeTiled, from the driver through the runtime's entry-point query (no link
+// against the driver library); resolved when a network is created, never during a capture
+typedef CUresult (*LpEncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+LpEncodeTiled lp_encode_tiled() {
+    static const LpEncodeTiled fn = []() -> LpEncodeTiled {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return (LpEncodeTiled)p;
+    }();
+    return fn;
+}
+
+// The TMA-fed convolution (k_lp_conv_tma): a tensor map over the input (channels, x, y, z),
+// 8-channel x 10 x 18 x 1 boxes, zeros outside; one persistent CTA per SM (it takes all 512
+// TMEM columns: the shared memory asked for keeps a second CTA off the SM).
+template <int CI, int CO, bool RELU, typename OutT>
+ls_status lp_conv_tma(ls_lpnet* n, LpDims d, const bf16* in, const bf16* w, const float* bias, OutT* out,
+                      int cout_total = CO, int co0 = 0, int ostride = CO, int only0 = 0) {
+    using S = ls::TmShape<CI, CO>;
+    constexpr int smem = S::smem < 116 * 1024 ? 116 * 1024 : S::smem;
+    static_assert(smem <= 227 * 1024, "shared memory per CTA");
+    const LpEncodeTiled enc = lp_encode_tiled();
+    if (!enc) return lp_fail(n, "cuTensorMapEncodeTiled: not available", cudaErrorNotSupported);
+    if (((uintptr_t)in & 15u) != 0) return lp_fail(n, "k_lp_conv_tma: input not 16-byte aligned", cudaErrorInvalidValue);
+    alignas(64) CUtensorMap map;
+    const cuuint64_t dims[4] = {(cuuint64_t)CI, (cuuint64_t)d.W, (cuuint64_t)d.H, (cuuint64_t)d.D};
+    const cuuint64_t strides[3] = {(cuuint64_t)CI * 2, (cuuint64_t)d.W * CI * 2, (cuuint64_t)d.H * d.W * CI * 2};
+    const cuuint32_t box[4] = {8, (cuuint32_t)ls::kTmHX, (cuuint32_t)ls::kTmHY, 1};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    const CUresult cr = enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)in, dims, strides, box, es,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (cr != CUDA_SUCCESS) return lp_fail(n, "cuTensorMapEncodeTiled", cudaErrorInvalidValue);
+    static std::mutex mu;
+    static bool set_dev[kLpMaxDevices] = {false};
+    int dev = 0;
+    LP_CUDA(n, cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kLpMaxDevices) return lp_fail(n, "k_lp_conv_tma: device index", cudaErrorInvalidDevice);
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!set_dev[dev]) {
+            LP_CUDA(n, cudaFuncSetAttribute(ls::k_lp_conv_tma<CI, CO, RELU, OutT>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+            set_dev[dev] = true;
+        }
+    }
+    // planes per tile: the most the tensor memory holds, fewer where the tiles would not
+    // cover the SMs (the coarse levels)
+    const long long txy = (long long)((d.W + ls::kTmX - 1) / ls::kTmX) * ((d.H + ls::kTmY - 1) / ls::kTmY);
+    int zt = S::ZT;
+    while (zt > 1 && txy * ((d.D + zt - 1) / zt) < n->num_sms) zt /= 2;
+    const long long ntiles = txy * ((d.D + zt - 1) / zt);
+    const int grid = (int)(ntiles < n->num_sms ? ntiles : n->num_sms);
+    ls::k_lp_conv_tma<CI, CO, RELU, OutT><<<grid, ls::kTmThreads, smem, n->stream>>>(map, d, w, bias, out, cout_total,
+                                                                                      co0, ostride, only0, zt);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return lp_fail(n, "k_lp_conv_tma", e);
+    return LS_OK;
+}
+
 template <bool RELU, typename OutT>
 ls_status lp_conv(ls_lpnet* n, LpDims d, int cin, int cout, const bf16* in, const bf16* w, const float* bias,
                   OutT* out) {
-    // tcgen05 where it beats the mma.sync kernels, measured per layer of the 144x176x176
-    // network: 32 -> 64 (M = 128 x N = 64 MMAs, persistent CTAs that stage the 110 KB of
-    // weights once) 47 us against 67. Where N is 16 or 32 the MMAs are too narrow to pay for
-    // the operand staging (16 -> 16: 420 against 308 us, 16 -> 32: 86 against 80, 32 -> 16:
-    // 126 against 107), so those layers stay on mma.sync unless LS_LPNET_TC=2.
+    // Measured per layer of the 144x176x176 network (ncu launch list): the TMA-fed kernel
+    // 16 -> 16 in 160 us (mma.sync 308, the first tcgen05 kernel 420), 16 -> 32 in 37 (80 / 86),
+    // 32 -> 64 in 28 (67 / 47), 32 -> 16 in 49 (107 / 126), 64 -> 32 in 29 (mma.sync 175).
+    // LS_LPNET_TC=1: the first tcgen05 kernel on the 32 -> 64 layer alone, where it beat
+    // mma.sync; 2: on every layer with up to 32 input channels; 0: mma.sync only.
+    if (n->use_tc == 3) {
+#define LP_TMA(CI, CO) \
+        if (cin == CI && cout == CO) return lp_conv_tma<CI, CO, RELU, OutT>(n, d, in, w, bias, out);
+        LP_TMA(16, 16) LP_TMA(16, 32) LP_TMA(32, 64) LP_TMA(32, 16) LP_TMA(64, 32)
+#undef LP_TMA
+        if (cin == 64 && cout == 64) {  // 221 KB of weights: two launches of 32 output channels
+            LS_TRY((lp_conv_tma<64, 32, RELU, OutT>(n, d, in, w, bias, out, 64, 0, 64)));
+            return lp_conv_tma<64, 32, RELU, OutT>(n, d, in, w, bias, out, 64, 32, 64);
+        }
+    }
     if (n->use_tc == 2) {
 #define LP_TC(CI, CO) \
         if (cin == CI && cout == CO) return lp_conv_tc<CI, CO, RELU, OutT>(n, d, in, w, bias, out);
@@ -1011,6 +1596,18 @@ ls_status lp_conv_dw(ls_lpnet* n, LpDims d, int cin, int cout, const bf16* in, c
         const char* e = getenv("LS_LPNET_DW");
         return e && e[0] == '0';
     }();
+    if (!fma_only && cin <= 32 && cout <= 32 && cin * cout <= 512) {
+        // the halo staged once per tile for all 27 taps; persistent blocks, two per SM (one
+        // where the accumulators of 16 x 32 weights per tap take the registers)
+        const long long ntiles = (long long)((d.W + ls::kTX - 1) / ls::kTX) * ((d.H + ls::kTY - 1) / ls::kTY) *
+                                 ((d.D + ls::kTZ - 1) / ls::kTZ);
+        const long long cap = (cin * cout > 256 ? 1LL : 2LL) * n->num_sms;
+        const int grid = (int)(ntiles < cap ? ntiles : cap);
+        if (cin == 16 && cout == 16) LP_LAUNCH(n, (ls::k_lp_conv_dw_tiled<16, 16>), grid, 256, d, in, dy, dw, db);
+        else if (cin == 16) LP_LAUNCH(n, (ls::k_lp_conv_dw_tiled<16, 32>), grid, 256, d, in, dy, dw, db);
+        else LP_LAUNCH(n, (ls::k_lp_conv_dw_tiled<32, 16>), grid, 256, d, in, dy, dw, db);
+        return LS_OK;
+    }
 #define LP_CASE(CI, CO)                                                                          \
     if (cin == CI && cout == CO) {                                                               \
         if (fma_only)                                                                            \
@@ -1043,25 +1640,32 @@ ls_status lp_forward(ls_lpnet* n, const float* c0, const float* c1, const float*
     LP_LAUNCH(n, ls::k_lp_pack, lp_grid(n, d0.N, 256), 256, d0, c0, c1, c2, n->x);
     LS_TRY((lp_conv<true, bf16>(n, d0, 16, 16, n->x, wb(0), bias(0), n->a0)));
     LS_TRY((lp_conv<true, bf16>(n, d0, 16, 16, n->a0, wb(1), bias(1), n->s0)));
-    LP_LAUNCH(n, ls::k_lp_pool, lp_grid(n, d1.N * 16, 256), 256, d1, 16, (const bf16*)n->s0, n->p1);
+    LP_LAUNCH(n, ls::k_lp_pool, lp_grid(n, d1.N * 2, 256), 256, d1, 16, (const bf16*)n->s0, n->p1);
     LS_TRY((lp_conv<true, bf16>(n, d1, 16, 32, n->p1, wb(2), bias(2), n->s1)));
-    LP_LAUNCH(n, ls::k_lp_pool, lp_grid(n, d2.N * 32, 256), 256, d2, 32, (const bf16*)n->s1, n->p2);
+    LP_LAUNCH(n, ls::k_lp_pool, lp_grid(n, d2.N * 4, 256), 256, d2, 32, (const bf16*)n->s1, n->p2);
     LS_TRY((lp_conv<true, bf16>(n, d2, 32, 64, n->p2, wb(3), bias(3), n->s2)));
-    LP_LAUNCH(n, ls::k_lp_pool, lp_grid(n, d3.N * 64, 256), 256, d3, 64, (const bf16*)n->s2, n->p3);
+    LP_LAUNCH(n, ls::k_lp_pool, lp_grid(n, d3.N * 8, 256), 256, d3, 64, (const bf16*)n->s2, n->p3);
     LS_TRY((lp_conv<true, bf16>(n, d3, 64, 64, n->p3, wb(4), bias(4), n->a3)));
-    LP_LAUNCH(n, ls::k_lp_up_add, lp_grid(n, d2.N * 64, 256), 256, d2, 64, (const bf16*)n->a3, (const bf16*)n->s2, n->u2);
+    LP_LAUNCH(n, ls::k_lp_up_add, lp_grid(n, d2.N * 8, 256), 256, d2, 64, (const bf16*)n->a3, (const bf16*)n->s2, n->u2);
     LS_TRY((lp_conv<true, bf16>(n, d2, 64, 32, n->u2, wb(5), bias(5), n->b2)));
-    LP_LAUNCH(n, ls::k_lp_up_add, lp_grid(n, d1.N * 32, 256), 256, d1, 32, (const bf16*)n->b2, (const bf16*)n->s1, n->u1);
+    LP_LAUNCH(n, ls::k_lp_up_add, lp_grid(n, d1.N * 4, 256), 256, d1, 32, (const bf16*)n->b2, (const bf16*)n->s1, n->u1);
     LS_TRY((lp_conv<true, bf16>(n, d1, 32, 16, n->u1, wb(6), bias(6), n->b1)));
-    LP_LAUNCH(n, ls::k_lp_up_add, lp_grid(n, d0.N * 16, 256), 256, d0, 16, (const bf16*)n->b1, (const bf16*)n->s0, n->u0);
-    LS_TRY((lp_conv<false, float>(n, d0, 16, 16, n->u0, wb(7), bias(7), n->y)));
+    LP_LAUNCH(n, ls::k_lp_up_add, lp_grid(n, d0.N * 2, 256), 256, d0, 16, (const bf16*)n->b1, (const bf16*)n->s0, n->u0);
+    if (n->use_tc == 3) {
+        // only output channel 0 is read (inference and loss): the layer stores it alone
+        LS_TRY((lp_conv_tma<16, 16, false, float>(n, d0, n->u0, wb(7), bias(7), n->y, 16, 0, 1, 1)));
+        n->y_stride = 1;
+    } else {
+        LS_TRY((lp_conv<false, float>(n, d0, 16, 16, n->u0, wb(7), bias(7), n->y)));
+        n->y_stride = 16;
+    }
     return LS_OK;
 }
 
 // backward of one layer: q = mask(d), dW += in^T q, dIn = conv(q, W^T) (dIn null: skipped)
 ls_status lp_layer_bwd(ls_lpnet* n, int l, LpDims d, const bf16* in, const bf16* out, const float* dout, float* din) {
     const LpLayer& L = n->layer[l];
-    LP_LAUNCH(n, ls::k_lp_mask, lp_grid(n, d.N * L.cout, 256), 256, d.N * L.cout, dout, out, L.relu, n->q);
+    LP_LAUNCH(n, ls::k_lp_mask, lp_grid(n, d.N * L.cout / 8, 256), 256, d.N * L.cout, dout, out, L.relu, n->q);
     LS_TRY(lp_conv_dw(n, d, L.cin, L.cout, in, (const bf16*)n->q, n->g + L.w_off, n->g + L.b_off));
     if (din) LS_TRY((lp_conv<false, float>(n, d, L.cout, L.cin, (const bf16*)n->q, n->wt + L.wb_off, nullptr, din)));
     return LS_OK;
@@ -1089,17 +1693,17 @@ ls_status lp_backward(ls_lpnet* n) {
                  d2 = ls::lp_dims(n->D / 4, n->H / 4, n->W / 4), d3 = ls::lp_dims(n->D / 8, n->H / 8, n->W / 8);
     LP_CUDA(n, cudaMemsetAsync(n->g, 0, sizeof(float) * n->nparam, n->stream));
     LS_TRY(lp_layer_bwd(n, 7, d0, n->u0, nullptr, n->gy, n->g0));                  // d_u0 = d_s0 (partial)
-    LP_LAUNCH(n, ls::k_lp_up_bwd, lp_grid(n, d1.N * 16, 256), 256, d1, 16, (const float*)n->g0, n->g1b);  // d_b1
+    LP_LAUNCH(n, ls::k_lp_up_bwd, lp_grid(n, d1.N * 4, 256), 256, d1, 16, (const float*)n->g0, n->g1b);  // d_b1
     LS_TRY(lp_layer_bwd(n, 6, d1, n->u1, n->b1, n->g1b, n->g1));                    // d_u1
-    LP_LAUNCH(n, ls::k_lp_up_bwd, lp_grid(n, d2.N * 32, 256), 256, d2, 32, (const float*)n->g1, n->g2b);  // d_b2
+    LP_LAUNCH(n, ls::k_lp_up_bwd, lp_grid(n, d2.N * 8, 256), 256, d2, 32, (const float*)n->g1, n->g2b);  // d_b2
     LS_TRY(lp_layer_bwd(n, 5, d2, n->u2, n->b2, n->g2b, n->g2));                    // d_u2
-    LP_LAUNCH(n, ls::k_lp_up_bwd, lp_grid(n, d3.N * 64, 256), 256, d3, 64, (const float*)n->g2, n->g3);   // d_a3
+    LP_LAUNCH(n, ls::k_lp_up_bwd, lp_grid(n, d3.N * 16, 256), 256, d3, 64, (const float*)n->g2, n->g3);   // d_a3
     LS_TRY(lp_layer_bwd(n, 4, d3, n->p3, n->a3, n->g3, n->g3b));                    // d_p3
-    LP_LAUNCH(n, ls::k_lp_pool_bwd_add, lp_grid(n, d2.N * 64, 256), 256, d2, 64, (const float*)n->g3b, n->g2);  // d_s2
+    LP_LAUNCH(n, ls::k_lp_pool_bwd_add, lp_grid(n, d2.N * 16, 256), 256, d2, 64, (const float*)n->g3b, n->g2);  // d_s2
     LS_TRY(lp_layer_bwd(n, 3, d2, n->p2, n->s2, n->g2, n->g2b));                    // d_p2
-    LP_LAUNCH(n, ls::k_lp_pool_bwd_add, lp_grid(n, d1.N * 32, 256), 256, d1, 32, (const float*)n->g2b, n->g1);  // d_s1
+    LP_LAUNCH(n, ls::k_lp_pool_bwd_add, lp_grid(n, d1.N * 8, 256), 256, d1, 32, (const float*)n->g2b, n->g1);  // d_s1
     LS_TRY(lp_layer_bwd(n, 2, d1, n->p1, n->s1, n->g1, n->g1b));                    // d_p1
-    LP_LAUNCH(n, ls::k_lp_pool_bwd_add, lp_grid(n, d0.N * 16, 256), 256, d0, 16, (const float*)n->g1b, n->g0);  // d_s0
+    LP_LAUNCH(n, ls::k_lp_pool_bwd_add, lp_grid(n, d0.N * 4, 256), 256, d0, 16, (const float*)n->g1b, n->g0);  // d_s0
     LS_TRY(lp_layer_bwd(n, 1, d0, n->a0, n->s0, n->g0, n->g0b));                    // d_a0
     LS_TRY(lp_layer_bwd(n, 0, d0, n->x, n->a0, n->g0b, nullptr));
     return LS_OK;
@@ -1132,7 +1736,7 @@ ls_status lpnet_forward_on(ls_lpnet* n, cudaStream_t s, const float* c0, const f
     ls_status st = lp_forward(n, c0, c1, c2);
     if (st == LS_OK) {
         const long long N = (long long)n->D * n->H * n->W;
-        k_lp_out<<<lp_grid(n, N, 256), 256, 0, s>>>(N, (const float*)n->y, out);
+        k_lp_out<<<lp_grid(n, N, 256), 256, 0, s>>>(N, (const float*)n->y, n->y_stride, out);
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) st = lp_fail(n, "k_lp_out", e);
     }
@@ -1153,12 +1757,14 @@ ls_status ls_lpnet_create(int D, int H, int W, int seed, ls_lpnet** out) {
     ls_lpnet* n = new (std::nothrow) ls_lpnet();
     if (!n) return LS_CUDA_ERROR;
     n->D = D; n->H = H; n->W = W;
+    n->y_stride = 16;
     ls_status st = LS_OK;
     auto fail = [&](ls_status s) { ls_lpnet_destroy(n); return s; };
     if (cudaGetDevice(&n->device) != cudaSuccess) return fail(LS_CUDA_ERROR);
     {
         const char* tc = getenv("LS_LPNET_TC");
-        n->use_tc = (tc && (tc[0] == '0' || tc[0] == '2')) ? tc[0] - '0' : 1;
+        n->use_tc = (tc && tc[0] >= '0' && tc[0] <= '3') ? tc[0] - '0' : 3;
+        if (n->use_tc == 3 && !lp_encode_tiled()) n->use_tc = 1;  // no tensor maps from this driver
     }
     cudaDeviceGetAttribute(&n->num_sms, cudaDevAttrMultiProcessorCount, n->device);
     if (cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(LS_CUDA_ERROR);
@@ -1282,7 +1888,7 @@ ls_status ls_lpnet_forward(ls_lpnet* n, const float* c0, const float* c1, const 
     if (!n || !c0 || !c1 || !c2 || !out) return LS_BAD_ARG;
     LS_TRY(lp_forward(n, c0, c1, c2));
     const long long N = (long long)n->D * n->H * n->W;
-    LP_LAUNCH(n, ls::k_lp_out, lp_grid(n, N, 256), 256, N, (const float*)n->y, out);
+    LP_LAUNCH(n, ls::k_lp_out, lp_grid(n, N, 256), 256, N, (const float*)n->y, n->y_stride, out);
     LP_CUDA(n, cudaStreamSynchronize(n->stream));
     if (ls::lpnet_tc_timeouts()) {
         // A tcgen05 wait gave up: the output is not valid, and the state a timed-out CTA left
@@ -1291,7 +1897,7 @@ ls_status ls_lpnet_forward(ls_lpnet* n, const float* c0, const float* c1, const 
         n->use_tc = 0;
         n->err = "tensor-core convolution: a wait for the MMAs gave up; recomputed with mma.sync";
         LS_TRY(lp_forward(n, c0, c1, c2));
-        LP_LAUNCH(n, ls::k_lp_out, lp_grid(n, N, 256), 256, N, (const float*)n->y, out);
+        LP_LAUNCH(n, ls::k_lp_out, lp_grid(n, N, 256), 256, N, (const float*)n->y, n->y_stride, out);
         LP_CUDA(n, cudaStreamSynchronize(n->stream));
         return LS_STAGNATED_FALLBACK_USED;
     }
@@ -1305,7 +1911,7 @@ ls_status ls_lpnet_train_step(ls_lpnet* n, const float* c0, const float* c1, con
     LS_TRY(lp_forward(n, c0, c1, c2));
     const long long N = (long long)n->D * n->H * n->W;
     const int nb = lp_grid(n, N, ls::kBlock);
-    LP_LAUNCH(n, ls::k_lp_loss, nb, ls::kBlock, N, (const float*)n->y, target, mask, (float)(1.0 / (double)mask_count),
+    LP_LAUNCH(n, ls::k_lp_loss, nb, ls::kBlock, N, (const float*)n->y, n->y_stride, target, mask, (float)(1.0 / (double)mask_count),
               n->gy, n->partials);
     LS_TRY(lp_backward(n));
     if (update) {

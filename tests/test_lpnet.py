@@ -70,14 +70,15 @@ def test_parameter_layout_round_trip():
     assert lpnet_flatten(p).size == sum(27 * ci * co + co for _, ci, co, _ in lo.LAYERS)
 
 
-# convolution paths (LS_LPNET_TC, read when a network is created): "tc" = tcgen05 with TMEM
-# accumulators for every layer with up to 32 input channels (2), "auto" = tcgen05 where it is
-# the faster kernel, the 32 -> 64 layer (1, the default), "mma" = mma.sync only (0)
-PATHS = ["tc", "auto", "mma"]
+# convolution paths (LS_LPNET_TC, read when a network is created): "tma" = the TMA-fed
+# tcgen05 kernel streaming through z with the dz taps stacked along N, every layer (3, the
+# default); "tc" = the first tcgen05 kernel for every layer with up to 32 input channels (2),
+# "tc64" = that kernel on the 32 -> 64 layer alone (1), "mma" = mma.sync only (0)
+PATHS = ["tma", "tc", "tc64", "mma"]
 
 
 def _path(monkeypatch, path):
-    monkeypatch.setenv("LS_LPNET_TC", {"tc": "2", "auto": "1", "mma": "0"}[path])
+    monkeypatch.setenv("LS_LPNET_TC", {"tc": "2", "tma": "3", "tc64": "1", "mma": "0"}[path])
 
 
 @pytest.mark.gpu
@@ -163,7 +164,7 @@ def test_gpu_training_reduces_loss():
 
 @pytest.mark.gpu
 def test_gpu_tcgen05_and_mma_sync_paths_agree(monkeypatch):
-    """Both convolution paths sum the same BF16 products in FP32, in different orders: the
+    """The convolution paths sum the same BF16 products in FP32, in different orders: the
     outputs agree far inside the oracle tolerance, at a size with many tiles per level."""
     from leachingsim_gb300.runtime import LPNet, lpnet_flatten
     shape = (32, 48, 80)
@@ -175,12 +176,13 @@ def test_gpu_tcgen05_and_mma_sync_paths_agree(monkeypatch):
         net.set_params(lpnet_flatten(p))
         outs[path] = net.forward(mask, c1, c2).cpu().numpy()
         net.close()
-    assert _rel(outs["tc"], outs["mma"]) < 5e-3
-    assert _rel(outs["auto"], outs["mma"]) < 5e-3
+    for path in ("tma", "tc", "tc64"):
+        assert _rel(outs[path], outs["mma"]) < 5e-3, path
 
 
 @pytest.mark.gpu
-def test_gpu_tcgen05_timeout_falls_back_to_mma_sync(monkeypatch):
+@pytest.mark.parametrize("path", ["tma", "tc"])
+def test_gpu_tcgen05_timeout_falls_back_to_mma_sync(path, monkeypatch):
     """A tcgen05 wait that gives up (the library's timeout counter, here set by the host-side
     LS_LPNET_SIMULATE_TIMEOUT switch; nothing on the GPU waits less or is skipped) makes the
     network discard the pass, switch to its mma.sync kernels for good and recompute: the
@@ -194,7 +196,7 @@ def test_gpu_tcgen05_timeout_falls_back_to_mma_sync(monkeypatch):
     ref_net.set_params(lpnet_flatten(p))
     ref = ref_net.forward(mask, c1, c2).cpu().numpy()
     ref_net.close()
-    _path(monkeypatch, "tc")
+    _path(monkeypatch, path)
     net = LPNet(shape)
     net.set_params(lpnet_flatten(p))
     monkeypatch.setenv("LS_LPNET_SIMULATE_TIMEOUT", "1")
