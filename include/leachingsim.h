@@ -333,8 +333,10 @@ ls_status ls_saturation_implicit(ls_ctx* ctx, double dt, ls_solve_info* info);
    take the device-wide synchronisation an allocation may imply. Its reduction scratch is a
    fixed device array (LS_NOALLOC_SAT_SCRATCH_BYTES) held by every GPU that loads the
    library until the process exits; the first call on a device looks up that array's
-   address, so it should come before any stream capture. All calls share the array: calls
-   that overlap on the GPU race. Domains above LS_NOALLOC_SAT_MAX_VOXELS (512^3) are
+   address. The call reads the largest rate back to the host and waits for it on the given
+   stream before it picks the sub-step count, so it returns with its work done. All calls
+   share the array: calls that overlap on the GPU race. Domains above
+   LS_NOALLOC_SAT_MAX_VOXELS (512^3) are
    rejected with LS_BAD_ARG and a message in err (if given).
    Device pointers: label (I*J*K, uint8 or uint16 per label_bytes), flux_x/y/z (I*J*K
    float64), saturation ((I+1)*J*K float64, updated in place like the context's field).
