@@ -311,7 +311,7 @@ ls_status wlist_reset(ls_ctx* c) {
 }
 
 ls_status finalize_sum(ls_ctx* c, int nblocks, int nvals, int out_slot) {
-    LS_LAUNCH(c, k_finalize<false>, nvals, kFinalizeThreads, 0, c->partials, nblocks, nvals,
+    LS_LAUNCH_PDL(c, k_finalize<false>, nvals, kFinalizeThreads, 0, c->partials, nblocks, nvals,
               c->scal + out_slot);
     return LS_OK;
 }
@@ -509,6 +509,8 @@ ls_status ls_create(ls_ctx** out, int I, int J, int K, int label_bytes, const ls
         const char* tv = getenv("LS_MG_TAIL_CELLS");
         c->mg_tail_cells = tv ? atoll(tv) : 4096;
         if (c->mg_tail_cells < 0) c->mg_tail_cells = 0;
+        const char* pv = getenv("LS_PDL");
+        c->pdl = (pv && pv[0] == '0') ? 0 : 1;
     }
     c->g.I = I; c->g.J = J; c->g.K = K;
     c->g.JK = JK;

@@ -367,6 +367,7 @@ struct ls_ctx {
     std::vector<ls::MGGraph> mg_graphs;  // captured preconditioner applications
     int mg_graphs_off;    // 1: launch the cycle kernel by kernel (LS_MG_GRAPHS=0)
     long long mg_tail_cells;  // coarse levels up to this many cells run as one block (LS_MG_TAIL_CELLS; 0: off)
+    int pdl;                  // programmatic dependent launch in the multigrid cycle (LS_PDL; 0: off)
     int* comp;            // fine-level strong-component ids (-1 = not an inner unknown)
     uint8_t* start_anchor; // per component root: anchored to fixed values (supplied starts)
     int* cc_flag;         // device flag for the labelling loop
@@ -479,6 +480,29 @@ ls_status check_cuda(ls_ctx* c, cudaError_t e, const char* what);
         if (e__ != cudaSuccess) return ls::check_cuda((ctx), e__, #kernel);         \
     } while (0)
 
+// Programmatic dependent launch, for the chains of small kernels of the multigrid cycle: the
+// kernel may be scheduled while its predecessor in the stream still runs (once every block of
+// the predecessor has passed its pdl_enter), so its launch overlaps the predecessor's work.
+// Only kernels that begin with pdl_enter() are launched this way (ctx->pdl = 0: LS_PDL=0,
+// ordinary launches).
+#define LS_LAUNCH_PDL(ctx, kernel, grid, block, smem, ...)                          \
+    do {                                                                            \
+        cudaLaunchConfig_t cfg__ = {};                                              \
+        cfg__.gridDim = dim3(grid);                                                 \
+        cfg__.blockDim = dim3(block);                                               \
+        cfg__.dynamicSmemBytes = (smem);                                            \
+        cfg__.stream = (ctx)->stream;                                               \
+        cudaLaunchAttribute at__[1];                                                \
+        at__[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;            \
+        at__[0].val.programmaticStreamSerializationAllowed = (ctx)->pdl ? 1 : 0;    \
+        cfg__.attrs = at__;                                                         \
+        cfg__.numAttrs = 1;                                                         \
+        cudaError_t e__ = cudaLaunchKernelEx(&cfg__, kernel, __VA_ARGS__);          \
+        (ctx)->launches++;                                                          \
+        if (e__ == cudaSuccess) e__ = cudaGetLastError();                           \
+        if (e__ != cudaSuccess) return ls::check_cuda((ctx), e__, #kernel);         \
+    } while (0)
+
 inline int grid_for(const ls_ctx* c, long long n) {
     long long want = (n + kBlock - 1) / kBlock;
     long long cap = (long long)c->num_sms * 8;
@@ -546,6 +570,14 @@ __device__ __forceinline__ void block_max_store(double (&v)[NV], double* partial
     }
 }
 
+// The first statement of a kernel launched with LS_LAUNCH_PDL: wait until the grid before it
+// in the stream has completed and its memory operations are visible, then let the next
+// kernel be scheduled. In a kernel launched the ordinary way the wait returns at once.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // One block per value: a fixed-order tree reduction of the per-block partials (the
 // result does not depend on timing).
 constexpr int kFinalizeThreads = 256;
@@ -553,6 +585,7 @@ template <bool MAX>
 __global__ void __launch_bounds__(kFinalizeThreads) k_finalize(const double* __restrict__ partials,
                                                                int nblocks, int nvals,
                                                                double* __restrict__ out) {
+    pdl_enter();
     __shared__ double sh[kFinalizeThreads];
     const int v = blockIdx.x;
     double acc = MAX ? -INFINITY : 0.0;

@@ -292,6 +292,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth(Grid g, const int* __restr
                                                       const T* __restrict__ b, const T* __restrict__ x,
                                                       T* __restrict__ xo, const T* __restrict__ dotv,
                                                       const T* __restrict__ dotv2, double* __restrict__ partials) {
+    pdl_enter();
     T acc = (T)0, acc2 = (T)0;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
@@ -319,6 +320,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth0_pair(int N2, int JK2, int
                                                             const float* __restrict__ dotv,
                                                             const float* __restrict__ dotv2,
                                                             double* __restrict__ partials) {
+    pdl_enter();
     float acc = 0.f, acc2 = 0.f;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N2; t += gridDim.x * blockDim.x) {
         const char2 kd = reinterpret_cast<const char2*>(kind)[t];
@@ -360,6 +362,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_resid0_pair(int N2, int JK2, int 
                                                            const float* __restrict__ f1, const float* __restrict__ f2,
                                                            const float* __restrict__ b, const float* __restrict__ x,
                                                            float* __restrict__ res) {
+    pdl_enter();
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N2; t += gridDim.x * blockDim.x) {
         const char2 kd = reinterpret_cast<const char2*>(kind)[t];
         const bool l0 = kd.x == 2, l1 = kd.y == 2;
@@ -376,6 +379,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_resid0_pair(int N2, int JK2, int 
 template <typename T>
 __global__ void k_mg_restrict_gather(Grid f, Grid cg, const int* __restrict__ fcomp, const int* __restrict__ ccomp,
                                      const T* __restrict__ res, T* __restrict__ cb) {
+    pdl_enter();
     for (long long R = blockIdx.x * (long long)blockDim.x + threadIdx.x; R < cg.N;
          R += (long long)gridDim.x * blockDim.x) {
         int I, J, K;
@@ -428,6 +432,7 @@ __global__ void k_mg_restrict(Grid f, Grid cg, const int* __restrict__ fcomp, co
                               const T* __restrict__ e, const T* __restrict__ f0, const T* __restrict__ f1,
                               const T* __restrict__ f2, const T* __restrict__ fb, const T* __restrict__ fx,
                               T* __restrict__ cb) {
+    pdl_enter();
     for (long long R = blockIdx.x * (long long)blockDim.x + threadIdx.x; R < cg.N;
          R += (long long)gridDim.x * blockDim.x)
         cb[R] = restrict_cell(f, cg, R, fcomp, ccomp, e, f0, f1, f2, fb, fx);
@@ -451,6 +456,7 @@ __device__ __forceinline__ void prolong_cell(const Grid& f, const Grid& cg, long
 template <typename T>
 __global__ void k_mg_prolong(Grid f, Grid cg, const int* __restrict__ fcomp, const int* __restrict__ ccomp,
                              const T* __restrict__ cx, T* __restrict__ fx, T scale) {
+    pdl_enter();
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < f.N;
          r += (long long)gridDim.x * blockDim.x)
         prolong_cell(f, cg, r, fcomp, ccomp, cx, fx, scale);
@@ -469,6 +475,7 @@ __global__ void __launch_bounds__(kBlock) k_kc_apply(Grid g, const int* __restri
                                                      const T* __restrict__ f2, const T* __restrict__ pd,
                                                      const T* __restrict__ rr, T* __restrict__ q,
                                                      double* __restrict__ partials) {
+    pdl_enter();
     T a0 = (T)0, a1 = (T)0;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
@@ -489,6 +496,7 @@ template <typename T>
 __global__ void k_kc_first(Grid g, const int* __restrict__ comp, const double* __restrict__ s,
                            const T* __restrict__ pd, const T* __restrict__ q, T* __restrict__ e,
                            T* __restrict__ rr) {
+    pdl_enter();
     const T a = (T)((s[0] > 0.0) ? s[1] / s[0] : 0.0);
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
@@ -502,6 +510,7 @@ __global__ void k_kc_first(Grid g, const int* __restrict__ comp, const double* _
 template <typename T>
 __global__ void k_kc_dir(Grid g, const int* __restrict__ comp, const double* __restrict__ s,
                          const T* __restrict__ z, const T* __restrict__ pd0, T* __restrict__ pd1) {
+    pdl_enter();
     const T b = (T)((s[0] > 0.0) ? -s[2] / s[0] : 0.0);
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x)
@@ -512,6 +521,7 @@ __global__ void k_kc_dir(Grid g, const int* __restrict__ comp, const double* __r
 template <typename T>
 __global__ void k_kc_second(Grid g, const int* __restrict__ comp, const double* __restrict__ s,
                             const T* __restrict__ pd1, T* __restrict__ e) {
+    pdl_enter();
     const T a = (T)((s[3] > 0.0) ? s[4] / s[3] : 0.0);
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x)
@@ -548,6 +558,7 @@ template <typename T>
 __global__ void k_mg_coarsest(Grid g, const int* __restrict__ comp, const T* __restrict__ e,
                               const T* __restrict__ f0, const T* __restrict__ f1, const T* __restrict__ f2,
                               const T* __restrict__ invd, const T* __restrict__ b, T* x, T* t, int sweeps) {
+    pdl_enter();
     coarsest_block(g, comp, e, f0, f1, f2, invd, b, x, t, sweeps);
 }
 
@@ -570,6 +581,7 @@ struct TailLevels {
 
 template <typename T>
 __global__ void __launch_bounds__(1024) k_mg_tail(TailLevels<T> L, T scale, int sweeps) {
+    pdl_enter();
     const int n = L.n;
     // down: two smoothing sweeps from zero, then the restricted residual
     for (int q = 0; q + 1 < n; ++q) {
@@ -961,7 +973,7 @@ ls_status mg_apply(ls_ctx* c, const T* r, T* z, const T* dotv2, int* nblocks_out
         if (l == 0 && pair0) {
             const int N2 = (int)(a.g.N / 2);
             const int gd = grid_for(c, N2);
-            LS_LAUNCH(c, k_mg_smooth0_pair, gd, kBlock, 0, N2, (int)(a.g.JK / 2), a.g.K / 2,
+            LS_LAUNCH_PDL(c, k_mg_smooth0_pair, gd, kBlock, 0, N2, (int)(a.g.JK / 2), a.g.K / 2,
                       (const int8_t*)c->pkind, (const float*)a.e, (const float*)a.f0, (const float*)a.f1,
                       (const float*)a.f2, (const float*)a.invd, (const float*)b, (const float*)x, (float*)xo,
                       (const float*)dv, (const float*)dv2, partials);
@@ -969,7 +981,7 @@ ls_status mg_apply(ls_ctx* c, const T* r, T* z, const T* dotv2, int* nblocks_out
             return LS_OK;
         }
         const int gd = grid_for(c, a.g.N);
-        LS_LAUNCH(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp,
+        LS_LAUNCH_PDL(c, k_mg_smooth<T>, gd, kBlock, 0, a.g, a.comp,
                   l == 0 ? (const int8_t*)c->pkind : (const int8_t*)nullptr, a.e, a.f0, a.f1, a.f2, a.invd, b, x,
                   xo, dv, dv2, partials);
         if (nb) *nb = gd;
@@ -987,18 +999,18 @@ ls_status mg_apply(ls_ctx* c, const T* r, T* z, const T* dotv2, int* nblocks_out
         const int gd = grid_for(c, a.g.N);
         LS_CUDA(c, cudaMemcpyAsync(rr, a.b, sizeof(T) * (size_t)a.g.N, cudaMemcpyDeviceToDevice, c->stream));
         LS_TRY(cycle(m, (const T*)rr, za, nullptr, nullptr, nullptr));
-        LS_LAUNCH(c, k_kc_apply<T>, gd, kBlock, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, (const T*)za,
+        LS_LAUNCH_PDL(c, k_kc_apply<T>, gd, kBlock, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, (const T*)za,
                   (const T*)rr, q0, c->partials);
         LS_TRY(finalize_sum(c, gd, 2, slot));  // (za, q0), (za, rr)
-        LS_LAUNCH(c, k_kc_first<T>, gd, kBlock, 0, a.g, a.comp, s, (const T*)za, (const T*)q0, e, rr);
+        LS_LAUNCH_PDL(c, k_kc_first<T>, gd, kBlock, 0, a.g, a.comp, s, (const T*)za, (const T*)q0, e, rr);
         int nb = 0;
         LS_TRY(cycle(m, (const T*)rr, zb, (const T*)q0, nullptr, &nb));
         LS_TRY(finalize_sum(c, nb, 2, slot + 2));  // (zb, q0)
-        LS_LAUNCH(c, k_kc_dir<T>, gd, kBlock, 0, a.g, a.comp, s, (const T*)zb, (const T*)za, pd);
-        LS_LAUNCH(c, k_kc_apply<T>, gd, kBlock, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, (const T*)pd,
+        LS_LAUNCH_PDL(c, k_kc_dir<T>, gd, kBlock, 0, a.g, a.comp, s, (const T*)zb, (const T*)za, pd);
+        LS_LAUNCH_PDL(c, k_kc_apply<T>, gd, kBlock, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, (const T*)pd,
                   (const T*)rr, q1, c->partials);
         LS_TRY(finalize_sum(c, gd, 2, slot + 3));  // (pd, q1), (pd, rr)
-        LS_LAUNCH(c, k_kc_second<T>, gd, kBlock, 0, a.g, a.comp, s, (const T*)pd, e);
+        LS_LAUNCH_PDL(c, k_kc_second<T>, gd, kBlock, 0, a.g, a.comp, s, (const T*)pd, e);
         return LS_OK;
     };
     // the small coarse levels below the K-cycle run as one block (k_mg_tail)
@@ -1024,11 +1036,11 @@ ls_status mg_apply(ls_ctx* c, const T* r, T* z, const T* dotv2, int* nblocks_out
                 tl.b[q] = m.b;
                 tl.t[q] = m.t;
             }
-            LS_LAUNCH(c, k_mg_tail<T>, 1, 1024, 0, tl, (T)kProlongScale, kCoarseSweeps);
+            LS_LAUNCH_PDL(c, k_mg_tail<T>, 1, 1024, 0, tl, (T)kProlongScale, kCoarseSweeps);
             return LS_OK;
         }
         if (l == L) {
-            LS_LAUNCH(c, k_mg_coarsest<T>, 1, 1024, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, a.invd, b, out, a.t,
+            LS_LAUNCH_PDL(c, k_mg_coarsest<T>, 1, 1024, 0, a.g, a.comp, a.e, a.f0, a.f1, a.f2, a.invd, b, out, a.t,
                       kCoarseSweeps);
             return LS_OK;
         }
@@ -1038,13 +1050,13 @@ ls_status mg_apply(ls_ctx* c, const T* r, T* z, const T* dotv2, int* nblocks_out
         if (l == 0 && pair0) {
             // residual into the free ping-pong buffer, then the per-block sums
             const int N2 = (int)(a.g.N / 2);
-            LS_LAUNCH(c, k_mg_resid0_pair, grid_for(c, N2), kBlock, 0, N2, (int)(a.g.JK / 2), a.g.K / 2,
+            LS_LAUNCH_PDL(c, k_mg_resid0_pair, grid_for(c, N2), kBlock, 0, N2, (int)(a.g.JK / 2), a.g.K / 2,
                       (const int8_t*)c->pkind, (const float*)a.e, (const float*)a.f0, (const float*)a.f1,
                       (const float*)a.f2, (const float*)b, (const float*)a.x, (float*)a.t);
-            LS_LAUNCH(c, k_mg_restrict_gather<T>, grid_for(c, cl.g.N), kBlock, 0, a.g, cl.g, a.comp, cl.comp,
+            LS_LAUNCH_PDL(c, k_mg_restrict_gather<T>, grid_for(c, cl.g.N), kBlock, 0, a.g, cl.g, a.comp, cl.comp,
                       (const T*)a.t, cl.b);
         } else {
-            LS_LAUNCH(c, k_mg_restrict<T>, grid_for(c, cl.g.N), kBlock, 0, a.g, cl.g, a.comp, cl.comp, a.e, a.f0,
+            LS_LAUNCH_PDL(c, k_mg_restrict<T>, grid_for(c, cl.g.N), kBlock, 0, a.g, cl.g, a.comp, cl.comp, a.e, a.f0,
                       a.f1, a.f2, b, (const T*)a.x, cl.b);
         }
         const T* corr;
@@ -1062,7 +1074,7 @@ ls_status mg_apply(ls_ctx* c, const T* r, T* z, const T* dotv2, int* nblocks_out
             corr = cl.x;
             scale = (T)kProlongScale;
         }
-        LS_LAUNCH(c, k_mg_prolong<T>, grid_for(c, a.g.N), kBlock, 0, a.g, cl.g, a.comp, cl.comp, corr, a.x,
+        LS_LAUNCH_PDL(c, k_mg_prolong<T>, grid_for(c, a.g.N), kBlock, 0, a.g, cl.g, a.comp, cl.comp, corr, a.x,
                   scale);
         LS_TRY(smooth(l, b, (const T*)a.x, a.t, nullptr, nullptr, nullptr));
         return smooth(l, b, (const T*)a.t, out, dv, dv2, nb);

@@ -636,6 +636,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_apply(Grid g, const int8_t* __res
                                                      const T* __restrict__ w1,
                                                      const T* __restrict__ w2, T* __restrict__ q,
                                                      double* __restrict__ partials) {
+    pdl_enter();
     T a = (T)0;  // per-thread partial in the inner precision
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
@@ -656,6 +657,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_apply0_pair(int N2, int JK2, int 
                                                            const float* __restrict__ w0, const float* __restrict__ w1,
                                                            const float* __restrict__ w2, float* __restrict__ q,
                                                            double* __restrict__ partials) {
+    pdl_enter();
     float a = 0.f;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N2; t += gridDim.x * blockDim.x) {
         const char2 kd = reinterpret_cast<const char2*>(kind)[t];
@@ -675,6 +677,7 @@ template <typename T>
 __global__ void k_cg_update(Grid g, const int8_t* __restrict__ kind, const double* __restrict__ scal,
                             const T* __restrict__ p, const T* __restrict__ q, T* __restrict__ x,
                             T* __restrict__ r_) {
+    pdl_enter();
     const double pq = scal[SP_PQ];
     const T a = (T)((pq > 0.0) ? scal[SP_RZ] / pq : 0.0);
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
@@ -690,6 +693,7 @@ template <typename T>
 __global__ void __launch_bounds__(kBlock) k_cg_jacobi(Grid g, const T* __restrict__ invd,
                                                       const T* __restrict__ r_, T* __restrict__ z,
                                                       double* __restrict__ partials) {
+    pdl_enter();
     T a = (T)0;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
@@ -707,6 +711,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_jacobi(Grid g, const T* __restric
 template <typename T>
 __global__ void k_cg_dir(Grid g, const int8_t* __restrict__ kind, const double* __restrict__ scal,
                          const T* __restrict__ z, T* __restrict__ p, int flexible) {
+    pdl_enter();
     const T beta = (T)(flexible ? ((scal[SP_PQ] > 0.0) ? -scal[SP_ZQ] / scal[SP_PQ] : 0.0)
                                 : scal[SP_RZN] / scal[SP_RZ]);
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
@@ -717,6 +722,7 @@ __global__ void k_cg_dir(Grid g, const int8_t* __restrict__ kind, const double* 
 // p = z, x = 0
 template <typename T>
 __global__ void k_copy_zero(Grid g, const T* __restrict__ a, T* __restrict__ b, T* __restrict__ z) {
+    pdl_enter();
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
         b[r] = a[r];
@@ -724,7 +730,10 @@ __global__ void k_copy_zero(Grid g, const T* __restrict__ a, T* __restrict__ b, 
     }
 }
 
-__global__ void k_set_scalar(double* scal, int dst, int src) { scal[dst] = scal[src]; }
+__global__ void k_set_scalar(double* scal, int dst, int src) {
+    pdl_enter();
+    scal[dst] = scal[src];
+}
 
 template <typename T>
 static ls_status inner_alloc(ls_ctx* c) {
@@ -761,7 +770,7 @@ static ls_status inner_pcg(ls_ctx* c, bool use_mg, double tol, int max_it, int* 
     // z = B r and (r, z) into slot; with the multigrid, also (qv, z) into slot + 1
     auto precondition = [&](int slot, const T* qv) -> ls_status {
         if (use_mg) return mg_precondition<T>(c, (const T*)r, z, qv, slot);
-        LS_LAUNCH(c, k_cg_jacobi<T>, grid, kBlock, 0, g, (const T*)c->iinvd, (const T*)r, z, c->partials);
+        LS_LAUNCH_PDL(c, k_cg_jacobi<T>, grid, kBlock, 0, g, (const T*)c->iinvd, (const T*)r, z, c->partials);
         return finalize_sum(c, grid, 1, slot);
     };
     // With the learned coarse solver (c->lpc_active) the cycle is checked as it goes: a
@@ -790,24 +799,24 @@ static ls_status inner_pcg(ls_ctx* c, bool use_mg, double tol, int max_it, int* 
         LS_CUDA(c, cudaMemsetAsync(x, 0, sizeof(T) * (size_t)g.N, c->stream));
         return LS_OK;
     }
-    LS_LAUNCH(c, k_copy_zero<T>, grid, kBlock, 0, g, (const T*)z, p, x);
+    LS_LAUNCH_PDL(c, k_copy_zero<T>, grid, kBlock, 0, g, (const T*)z, p, x);
     const double target = tol * tol * rz0;
     double rz = rz0;
     for (int it = 0; it < max_it; ++it) {
         {
             Timed tm(c, LS_T_CG_APPLY);
             if (std::is_same<T, float>::value && g.K % 2 == 0)
-                LS_LAUNCH(c, k_cg_apply0_pair, pgrid, kBlock, 0, (int)(g.N / 2), (int)(g.JK / 2), g.K / 2,
+                LS_LAUNCH_PDL(c, k_cg_apply0_pair, pgrid, kBlock, 0, (int)(g.N / 2), (int)(g.JK / 2), g.K / 2,
                           (const int8_t*)c->pkind, (const float*)p, (const float*)e, (const float*)w0,
                           (const float*)w1, (const float*)w2, (float*)q, c->partials);
             else
-                LS_LAUNCH(c, k_cg_apply<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const T*)p, e, w0, w1,
+                LS_LAUNCH_PDL(c, k_cg_apply<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const T*)p, e, w0, w1,
                           w2, q, c->partials);
             // p in, excess and three own face links, q out
             if (c->timing) c->timer_bytes[LS_T_CG_APPLY] += (double)g.N * 6.0 * sizeof(T);
         }
         LS_TRY(finalize_sum(c, (std::is_same<T, float>::value && g.K % 2 == 0) ? pgrid : grid, 1, SP_PQ));
-        LS_LAUNCH(c, k_cg_update<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const double*)c->scal,
+        LS_LAUNCH_PDL(c, k_cg_update<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const double*)c->scal,
                   (const T*)p, (const T*)q, x, r);
         LS_TRY(precondition(SP_RZN, (const T*)q));
         *its = it + 1;
@@ -837,9 +846,9 @@ static ls_status inner_pcg(ls_ctx* c, bool use_mg, double tol, int max_it, int* 
         }
         if (rz != rz) return set_error(c, LS_NONFINITE, "pressure: NaN in inner PCG");
         if (rz <= target || !(pq > 0.0) || rz < 0.0) break;
-        LS_LAUNCH(c, k_cg_dir<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const double*)c->scal,
+        LS_LAUNCH_PDL(c, k_cg_dir<T>, grid, kBlock, 0, g, (const int8_t*)c->pkind, (const double*)c->scal,
                   (const T*)z, p, use_mg ? 1 : 0);
-        LS_LAUNCH(c, k_set_scalar, 1, 1, 0, c->scal, SP_RZ, SP_RZN);
+        LS_LAUNCH_PDL(c, k_set_scalar, 1, 1, 0, c->scal, SP_RZ, SP_RZN);
     }
     *rel_out = sqrt(std::max(rz, 0.0) / rz0);
     return LS_OK;

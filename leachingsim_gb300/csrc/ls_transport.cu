@@ -548,6 +548,7 @@ template <int NQ, bool FIRST>
 __global__ void __launch_bounds__(kBlock) k_ti_v(int N, int JK, int K, TOff op, TIVec iv,
                                                  const double* __restrict__ scal,
                                                  double* __restrict__ partials) {
+    pdl_enter();
     if (scal[TI_ANY] == 0.0) return;
     using L = Lanes<NQ>;
     using V = typename L::V;
@@ -578,6 +579,7 @@ template <int NQ>
 __global__ void __launch_bounds__(kBlock) k_ti_st(int N, int JK, int K, TOff op, TIVec iv,
                                                   const double* __restrict__ scal,
                                                   double* __restrict__ partials) {
+    pdl_enter();
     if (scal[TI_ANY] == 0.0) return;
     using L = Lanes<NQ>;
     using V = typename L::V;
@@ -621,6 +623,7 @@ __global__ void __launch_bounds__(kBlock) k_ti_st(int N, int JK, int K, TOff op,
 // r = s - w t; d += a p + w s; p = r + b (p - w v)
 template <int NQ>
 __global__ void __launch_bounds__(kBlock) k_ti_xp(int N, TIVec iv, const double* __restrict__ scal) {
+    pdl_enter();
     if (scal[TI_ANY] == 0.0) return;
     using L = Lanes<NQ>;
     using V = typename L::V;
@@ -674,6 +677,7 @@ template <bool FIRST>
 __global__ void __launch_bounds__(kBlock) k_ti_v_pair(int N2, int JK2, int K2, TOff op, TIVec iv,
                                                       const double* __restrict__ scal,
                                                       double* __restrict__ partials) {
+    pdl_enter();
     if (scal[TI_ANY] == 0.0) return;
     const float* __restrict__ X = FIRST ? iv.r : iv.p;
     const float2* __restrict__ RH = reinterpret_cast<const float2*>(iv.rh);
@@ -695,6 +699,7 @@ __global__ void __launch_bounds__(kBlock) k_ti_v_pair(int N2, int JK2, int K2, T
 __global__ void __launch_bounds__(kBlock) k_ti_st_pair(int N2, int JK2, int K2, TOff op, TIVec iv,
                                                        const double* __restrict__ scal,
                                                        double* __restrict__ partials) {
+    pdl_enter();
     if (scal[TI_ANY] == 0.0) return;
     const float* __restrict__ R = iv.r;
     const float* __restrict__ VV = iv.v;
@@ -742,6 +747,7 @@ __global__ void __launch_bounds__(kBlock) k_ti_st_pair(int N2, int JK2, int K2, 
 
 // k_ti_xp on pairs of rows (8-byte loads and stores)
 __global__ void __launch_bounds__(kBlock) k_ti_xp_pair(int N2, TIVec iv, const double* __restrict__ scal) {
+    pdl_enter();
     if (scal[TI_ANY] == 0.0) return;
     const float2* __restrict__ S = reinterpret_cast<const float2*>(iv.s);
     const float2* __restrict__ T = reinterpret_cast<const float2*>(iv.t);
@@ -863,6 +869,7 @@ template <int PH, int NQ>
 __global__ void __launch_bounds__(kFinalizeThreads) k_ti_fin(const double* __restrict__ partials, int nblocks,
                                                              double* scal, unsigned int* counter,
                                                              double tol2_0, double tol2_1) {
+    pdl_enter();
     if (PH != PH_INIT && scal[TI_ANY] == 0.0) return;
     constexpr int NV = (PH == PH_ST) ? 5 * NQ : NQ;
     __shared__ double sh[kFinalizeThreads];
@@ -991,40 +998,40 @@ static ls_status inner_solve(ls_ctx* c, const TBuf& tb, const int lane_q[NQ], co
         const int nb = std::min(batch, max_it - it);
         for (int b = 0; b < nb; ++b, ++it) {
             if (it > 0) {
-                if (pair) LS_LAUNCH(c, k_ti_xp_pair, kgrid, kBlock, 0, N2, iv, (const double*)c->scal);
-                else LS_LAUNCH(c, k_ti_xp<NQ>, grid, kBlock, 0, N, iv, (const double*)c->scal);
+                if (pair) LS_LAUNCH_PDL(c, k_ti_xp_pair, kgrid, kBlock, 0, N2, iv, (const double*)c->scal);
+                else LS_LAUNCH_PDL(c, k_ti_xp<NQ>, grid, kBlock, 0, N, iv, (const double*)c->scal);
             }
             {
                 Timed tm(c, LS_T_KRY_APPLY);
                 if (pair) {
                     if (it == 0)
-                        LS_LAUNCH(c, k_ti_v_pair<true>, kgrid, kBlock, 0, N2, JK2, K2, op, iv,
+                        LS_LAUNCH_PDL(c, k_ti_v_pair<true>, kgrid, kBlock, 0, N2, JK2, K2, op, iv,
                                   (const double*)c->scal, c->partials);
                     else
-                        LS_LAUNCH(c, k_ti_v_pair<false>, kgrid, kBlock, 0, N2, JK2, K2, op, iv,
+                        LS_LAUNCH_PDL(c, k_ti_v_pair<false>, kgrid, kBlock, 0, N2, JK2, K2, op, iv,
                                   (const double*)c->scal, c->partials);
                 } else if (it == 0) {
-                    LS_LAUNCH(c, (k_ti_v<NQ, true>), grid, kBlock, 0, N, JK, K, op, iv, (const double*)c->scal,
+                    LS_LAUNCH_PDL(c, (k_ti_v<NQ, true>), grid, kBlock, 0, N, JK, K, op, iv, (const double*)c->scal,
                               c->partials);
                 } else {
-                    LS_LAUNCH(c, (k_ti_v<NQ, false>), grid, kBlock, 0, N, JK, K, op, iv, (const double*)c->scal,
+                    LS_LAUNCH_PDL(c, (k_ti_v<NQ, false>), grid, kBlock, 0, N, JK, K, op, iv, (const double*)c->scal,
                               c->partials);
                 }
                 if (c->timing) c->timer_bytes[LS_T_KRY_APPLY] += v_bytes + (it == 0 ? 4.0 * NQ * g.N : 0.0);
             }
-            LS_LAUNCH(c, (k_ti_fin<PH_V, NQ>), NQ, kFinalizeThreads, 0, (const double*)c->partials, kgrid,
+            LS_LAUNCH_PDL(c, (k_ti_fin<PH_V, NQ>), NQ, kFinalizeThreads, 0, (const double*)c->partials, kgrid,
                       c->scal, c->tcount, 0.0, 0.0);
             {
                 Timed tm(c, LS_T_KRY_APPLY);
                 if (pair)
-                    LS_LAUNCH(c, k_ti_st_pair, kgrid, kBlock, 0, N2, JK2, K2, op, iv, (const double*)c->scal,
+                    LS_LAUNCH_PDL(c, k_ti_st_pair, kgrid, kBlock, 0, N2, JK2, K2, op, iv, (const double*)c->scal,
                               c->partials);
                 else
-                    LS_LAUNCH(c, k_ti_st<NQ>, grid, kBlock, 0, N, JK, K, op, iv, (const double*)c->scal,
+                    LS_LAUNCH_PDL(c, k_ti_st<NQ>, grid, kBlock, 0, N, JK, K, op, iv, (const double*)c->scal,
                               c->partials);
                 if (c->timing) c->timer_bytes[LS_T_KRY_APPLY] += st_bytes;
             }
-            LS_LAUNCH(c, (k_ti_fin<PH_ST, NQ>), 5 * NQ, kFinalizeThreads, 0, (const double*)c->partials, kgrid,
+            LS_LAUNCH_PDL(c, (k_ti_fin<PH_ST, NQ>), 5 * NQ, kFinalizeThreads, 0, (const double*)c->partials, kgrid,
                       c->scal, c->tcount, 0.0, 0.0);
         }
         LS_TRY(read_scalars(c, TI_BASE, TI_ANY - TI_BASE + 1, sc));
