@@ -424,12 +424,15 @@ def gpu_arm(args, ws, rank, local):
         ctx = Context(shape, label_bytes=1, params=p)
         ctx.upload("label", pinned_lab.numpy())
         ctx.init_all()
+        w1 = time.perf_counter()
         h2d = N
         d2h = 0
         te, ne = 0.0, 0
         pending = None
+        step_s, out_s = [], []
         for _ in range(nsteps):
-            te, ne, _ = run_steps(ctx, te, ne, 1, DT)
+            s0 = time.perf_counter()
+            te, ne, _ = run_steps(ctx, te, ne, 1, DT)   # returns after the step's scalars are read
             if (ne - 1) % NOUT == 0:
                 ctx.props()   # property sync before output (src/main.cpp:491-494)
                 if pending is not None:
@@ -437,15 +440,24 @@ def gpu_arm(args, ws, rank, local):
                 # the copies drain on the context's copy stream while the next steps run
                 pending = ctx.download_async(OUTPUT_FIELDS, [out_bufs[f] for f in OUTPUT_FIELDS])
                 d2h += sum(out_bufs[f].nbytes for f in OUTPUT_FIELDS)
+                out_s.append(time.perf_counter() - s0)
+            else:
+                step_s.append(time.perf_counter() - s0)
+        w2 = time.perf_counter()
         if pending is not None:
             pending.wait()
         ctx.synchronize()
         e2e_wall = time.perf_counter() - w0
+        e2e_parts = {"create_upload_init_ms": round((w1 - w0) * 1e3, 2),
+                     "first_step_ms": round(out_s[0] * 1e3, 2) if out_s else None,
+                     "step_ms_median": round(statistics.median(step_s) * 1e3, 2) if step_s else None,
+                     "output_step_ms_mean": round(statistics.mean(out_s[1:]) * 1e3, 2) if len(out_s) > 1 else None,
+                     "final_drain_ms": round((time.perf_counter() - w2) * 1e3, 2)}
         ctx.close()
         e2e_wall = max_over_ranks(e2e_wall, ws)
         e2e = {"value": round(replica_rate(ws, nsteps, e2e_wall), 4), "unit": UNIT,
                "h2d_bytes_per_step": int(h2d / nsteps), "d2h_bytes_per_step": int(d2h / nsteps),
-               "steps": nsteps, "wall_s": round(e2e_wall, 3),
+               "steps": nsteps, "wall_s": round(e2e_wall, 3), "parts": e2e_parts,
                "note": ("fresh run from a pinned host label image, every nout-th step's fields read back to "
                         "pinned host memory (copies on the context's copy stream, overlapping the next "
                         "steps; all landed before the clock stops)")}
