@@ -451,6 +451,8 @@ def gpu_arm(args, ws, rank, local):
         e2e_parts = {"create_upload_init_ms": round((w1 - w0) * 1e3, 2),
                      "first_step_ms": round(out_s[0] * 1e3, 2) if out_s else None,
                      "step_ms_median": round(statistics.median(step_s) * 1e3, 2) if step_s else None,
+                     "step_ms_mean": round(statistics.mean(step_s) * 1e3, 2) if step_s else None,
+                     "step_ms_max": round(max(step_s) * 1e3, 2) if step_s else None,
                      "output_step_ms_mean": round(statistics.mean(out_s[1:]) * 1e3, 2) if len(out_s) > 1 else None,
                      "final_drain_ms": round((time.perf_counter() - w2) * 1e3, 2)}
         ctx.close()

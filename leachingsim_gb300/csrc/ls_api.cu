@@ -743,6 +743,8 @@ static ls_status transfer(ls_ctx* c, ls_field f, void* host, size_t n, int padde
     size_t esz = 0;
     void* dev = field_ptr(c, f, &esz);
     if (!dev) return set_error(c, LS_BAD_ARG, "unknown field id");
+    const bool flux = f == LS_F_FLUX_X || f == LS_F_FLUX_Y || f == LS_F_FLUX_Z;
+    if (flux) LS_TRY(flux_zero_now(c));
     size_t want = padded ? (size_t)c->g.NP : (size_t)c->g.N;
     if (n != want) {
         char buf[128];
@@ -758,6 +760,7 @@ static ls_status transfer(ls_ctx* c, ls_field f, void* host, size_t n, int padde
             f == LS_F_KMULT)
             c->props_force = 1;
         if (f == LS_F_PRESSURE) c->p_eff_prev = 0.0;
+        if (flux) c->fx_is_shadow = 0;
         if (f == LS_F_ACID) c->acid_zero = 0;
         if (f == LS_F_LABEL || f == LS_F_FRAC) c->dz_no_threshold = 0;
     } else {
@@ -788,6 +791,8 @@ ls_status ls_download_fields_async(ls_ctx* c, int count, const int* fields, void
         size_t esz = 0;
         void* dev = field_ptr(c, (ls_field)fields[q], &esz);
         if (!dev || !hosts[q]) return set_error(c, LS_BAD_ARG, "ls_download_fields_async: unknown field or null buffer");
+        if (fields[q] == LS_F_FLUX_X || fields[q] == LS_F_FLUX_Y || fields[q] == LS_F_FLUX_Z)
+            LS_TRY(flux_zero_now(c));
         items.push_back({dev, hosts[q], n * esz, field_group(fields[q])});
     }
     cudaEvent_t ev = nullptr;
@@ -882,6 +887,7 @@ ls_status ls_count_nonfinite(ls_ctx* c, ls_field f, long long* count) {
     size_t esz = 0;
     void* dev = field_ptr(c, f, &esz);
     if (!dev || esz != 8) return set_error(c, LS_BAD_ARG, "ls_count_nonfinite: an FP64 field is needed");
+    if (f == LS_F_FLUX_X || f == LS_F_FLUX_Y || f == LS_F_FLUX_Z) LS_TRY(flux_zero_now(c));
     const int grid = grid_for(c, c->g.N);
     LS_LAUNCH(c, k_count_nonfinite, grid, kBlock, 0, c->g.N, (const double*)dev, c->partials);
     LS_TRY(finalize_sum(c, grid, 1, S_RED0));
@@ -911,6 +917,8 @@ ls_status ls_init_fields(ls_ctx* c) {
     size_t bytes = sizeof(double) * (size_t)c->g.NP;
     double* f[] = {c->P, c->conc, c->fx, c->fy, c->fz, c->sat, c->pc, c->kr, c->precip};
     for (double* q : f) LS_CUDA(c, cudaMemsetAsync(q, 0, bytes, c->stream));
+    c->flux_zero_pending = 0;
+    c->fx_is_shadow = 0;
     c->p_ready = 0;
     c->p_eff_prev = 0.0;
     c->props_force = 1;  // kr and Pc were cleared
@@ -1074,6 +1082,7 @@ ls_status ls_dissolve(ls_ctx* c, double dt, int* leached, ls_substep_info* info)
 ls_status ls_snapshot(ls_ctx* c) {
     if (!c) return LS_BAD_ARG;
     Timed tm(c, LS_T_SNAPSHOT);
+    c->flux_zero_pending_b = c->flux_zero_pending;  // the fluxes are copied as they are
     size_t np = (size_t)c->g.NP, d8 = np * sizeof(double);
     cudaStream_t s = c->stream;
     LS_CUDA(c, cudaMemcpyAsync(c->b_frac, c->frac, np * sizeof(float), cudaMemcpyDeviceToDevice, s));
@@ -1123,6 +1132,8 @@ ls_status ls_rollback(ls_ctx* c) {
             {c->acid, c->b_acid}, {c->fx, c->b_fx}, {c->fy, c->b_fy}, {c->fz, c->b_fz}};
         for (auto& pr : pairs) LS_CUDA(c, cudaMemcpyAsync(pr.first, pr.second, d8, kind, s));
     }
+    c->flux_zero_pending = c->flux_zero_pending_b;
+    c->fx_is_shadow = 0;
     c->p_ready = 0;
     c->p_eff_prev = 0.0;
     c->acid_zero = 0;

@@ -344,6 +344,9 @@ struct ls_ctx {
     double *shq_P, *shq_C, *shq_K, *shq_V;  // flux inputs at the last evaluation
     double *shq_fx, *shq_fy, *shq_fz;       // the fluxes last computed
     int flux_valid;
+    int flux_zero_pending;    // the Rock / Precipitate fluxes are still to be zeroed (flux_zero_now)
+    int flux_zero_pending_b;  // the same at the last snapshot
+    int fx_is_shadow;         // fx / fy / fz equal the change-tracking shadows at every voxel
     double flux_consts[2];
 
     // multigrid: the finest level is the inner system above (vectors mg0_x, mg0_t);
@@ -622,6 +625,7 @@ ls_status pressure_solve_run(ls_ctx* c, ls_solve_info* info, const float* start 
 ls_status pressure_learned_inputs_run(ls_ctx* c, float* mask, float* logk, float* bc);
 ls_status pressure_apply_run(ls_ctx* c, const double* x, double* y);
 ls_status transport_run(ls_ctx* c, double dt, int which, ls_solve_info* ci, ls_solve_info* ai);
+ls_status flux_zero_now(ls_ctx* c);
 ls_status transport_apply_run(ls_ctx* c, double dt, const double* x, double* y);
 // acid_pre (optional, N doubles): receives the acid the sweeps start from; *swept tells
 // whether they ran (otherwise nothing changed)

@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(kBlock) k_flux_scan(Grid g, const unsigned int
             d = dbit(own, lane) || (i > 0 && dbit(im, lane)) || (i + 1 < g.I && dbit(ip, lane)) ||
                 (j > 0 && dbit(jm, lane)) || (j + 1 < g.J && dbit(jp, lane)) || (k > 0 && dbit(km, lane)) ||
                 (k + 1 < g.K && dbit(kp, lane));
-            if (!d) {
+            if (!d && sfx) {  // null: the fluxes already equal the shadows
                 fx[r] = sfx[r];
                 fy[r] = sfy[r];
                 fz[r] = sfz[r];
@@ -324,6 +324,7 @@ ls_status flux_run(ls_ctx* c) {
         LS_LAUNCH(c, k_flux, grid, kBlock, 0, c->g, make_dxdiv(c->p.dx), c->p.max_cap_grad, c->P, c->pc,
                   c->perm, c->visc, c->fx, c->fy, c->fz, (double*)nullptr, (double*)nullptr, (double*)nullptr,
                   (const int*)c->wlist, (const unsigned int*)c->wcount);
+        c->flux_zero_pending = 0;  // every voxel written
         return LS_OK;
     }
     if (!c->shq_P) {
@@ -336,14 +337,20 @@ ls_status flux_run(ls_ctx* c) {
     LS_TRY(wlist_reset(c));
     LS_LAUNCH(c, k_flux_dirty, grid, kBlock, 0, c->g, c->P, c->pc, c->perm, c->visc, c->shq_P, c->shq_C,
               c->shq_K, c->shq_V, c->dbits, c->dwords, force);
+    // unchanged voxels get their last computed flux back, unless the fluxes still hold it
+    const bool restore = !c->fx_is_shadow || force;
     LS_LAUNCH(c, k_flux_scan, grid, kBlock, 0, c->g, (const unsigned int*)c->dbits, c->dwords, c->fx, c->fy, c->fz,
-              (const double*)c->shq_fx, (const double*)c->shq_fy, (const double*)c->shq_fz, c->wlist, c->wcount);
+              restore ? (const double*)c->shq_fx : (const double*)nullptr,
+              restore ? (const double*)c->shq_fy : (const double*)nullptr,
+              restore ? (const double*)c->shq_fz : (const double*)nullptr, c->wlist, c->wcount);
     LS_LAUNCH(c, k_flux, grid, kBlock, 0, c->g, make_dxdiv(c->p.dx), c->p.max_cap_grad, c->P, c->pc,
               c->perm, c->visc, c->fx, c->fy, c->fz, c->shq_fx, c->shq_fy, c->shq_fz, (const int*)c->wlist,
               (const unsigned int*)c->wcount);
     c->flux_consts[0] = c->p.dx;
     c->flux_consts[1] = c->p.max_cap_grad;
     c->flux_valid = 1;
+    c->flux_zero_pending = 0;  // every voxel holds its fresh flux, equal to its shadow
+    c->fx_is_shadow = 1;
     return LS_OK;
 }
 
@@ -518,6 +525,7 @@ __global__ void __launch_bounds__(kBlock) k_sat_update_st(Grid g, double dt_sub_
 }
 
 ls_status saturation_run(ls_ctx* c, double dt, ls_substep_info* info) {
+    LS_TRY(flux_zero_now(c));  // after a transport without a flux evaluation since
     snap_fence(c, kSnapSat);
     const DxDiv dx = make_dxdiv(c->p.dx);
     const double evap = c->p.evaporative_flux;

@@ -1241,13 +1241,33 @@ static ls_status transport_t(ls_ctx* c, double dt, int which, ls_solve_info* ci,
         if (acid_lane >= 0) c->acid_zero = (st == LS_OK && ((zero_lanes >> acid_lane) & 1)) ? 1 : 0;
     }
     if (st != LS_OK && st != LS_NOT_CONVERGED && st != LS_NONFINITE) return st;
-    LS_LAUNCH(c, k_zero_solid_flux<L>, grid_for(c, c->g.N), kBlock, 0, c->g, (const L*)c->label,
-              c->fx, c->fy, c->fz);
+    c->flux_zero_pending = 1;  // the Rock / Precipitate fluxes are zeroed when next looked at
     return st;
 }
 
+// The reference zeroes the flux of Rock and Precipitate voxels after the transport solve
+// (src/Simulation.cpp:1134-1149). Nothing in a time step reads those fluxes again before the
+// next step's flux evaluation overwrites them, so the zeroing waits until something looks:
+// the field transfers, counts and asynchronous downloads and the saturation updates call
+// this first (a snapshot keeps the pending state with the fields it copies). Until then the
+// fluxes keep equal to the change-tracking shadows, and the next flux evaluation need not
+// restore them.
+ls_status flux_zero_now(ls_ctx* c) {
+    if (!c->flux_zero_pending) return LS_OK;
+    snap_fence(c, kSnapFlux);
+    if (c->label_bytes == 1)
+        LS_LAUNCH(c, k_zero_solid_flux<uint8_t>, grid_for(c, c->g.N), kBlock, 0, c->g, (const uint8_t*)c->label,
+                  c->fx, c->fy, c->fz);
+    else
+        LS_LAUNCH(c, k_zero_solid_flux<uint16_t>, grid_for(c, c->g.N), kBlock, 0, c->g,
+                  (const uint16_t*)c->label, c->fx, c->fy, c->fz);
+    c->flux_zero_pending = 0;
+    c->fx_is_shadow = 0;
+    return LS_OK;
+}
+
 ls_status transport_run(ls_ctx* c, double dt, int which, ls_solve_info* ci, ls_solve_info* ai) {
-    snap_fence(c, kSnapRest | kSnapFlux);  // conc, acid; the fluxes of Rock and Precipitate are zeroed
+    snap_fence(c, kSnapRest);  // conc, acid
     if (c->label_bytes == 1) return transport_t<uint8_t>(c, dt, which, ci, ai);
     return transport_t<uint16_t>(c, dt, which, ci, ai);
 }
@@ -1331,6 +1351,7 @@ static ls_status sat_implicit_t(ls_ctx* c, double dt, ls_solve_info* info) {
 }
 
 ls_status saturation_implicit_run(ls_ctx* c, double dt, ls_solve_info* info) {
+    LS_TRY(flux_zero_now(c));  // after a transport without a flux evaluation since
     snap_fence(c, kSnapSat);
     if (c->label_bytes == 1) return sat_implicit_t<uint8_t>(c, dt, info);
     return sat_implicit_t<uint16_t>(c, dt, info);
