@@ -322,12 +322,43 @@ ls_status finalize_max(ls_ctx* c, int nblocks, int nvals, int out_slot) {
     return LS_OK;
 }
 
-ls_status read_scalars(ls_ctx* c, int first, int count, double* out) {
-    LS_CUDA(c, cudaMemcpyAsync(c->h_scal + first, c->scal + first, sizeof(double) * count,
-                               cudaMemcpyDeviceToHost, c->stream));
+// Small device-to-host reads (scalars, counters, histograms) go through a kernel that
+// writes mapped host memory, not through cudaMemcpyAsync: the copy engines may be carrying
+// an output download to the host, and a step's readback queued behind it would wait for it.
+__global__ void k_to_host(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, size_t bytes) {
+    if (((((uintptr_t)src) | ((uintptr_t)dst) | bytes) & 7u) == 0) {
+        for (size_t q = threadIdx.x; q < bytes / 8; q += blockDim.x)
+            reinterpret_cast<unsigned long long*>(dst)[q] = reinterpret_cast<const unsigned long long*>(src)[q];
+    } else {
+        for (size_t b = threadIdx.x; b < bytes; b += blockDim.x) dst[b] = src[b];
+    }
+}
+
+static ls_status small_host_buffer(ls_ctx* c, size_t bytes) {
+    if (bytes <= c->h_small_bytes) return LS_OK;
     LS_CUDA(c, cudaStreamSynchronize(c->stream));
-    for (int q = 0; q < count; ++q) out[q] = c->h_scal[first + q];
+    if (c->h_small) cudaFreeHost(c->h_small);
+    c->h_small = nullptr;
+    c->hd_small = nullptr;
+    c->h_small_bytes = 0;
+    const size_t want = std::max(bytes, (size_t)65536);
+    LS_CUDA(c, cudaHostAlloc(&c->h_small, want, cudaHostAllocMapped));
+    LS_CUDA(c, cudaHostGetDevicePointer(&c->hd_small, c->h_small, 0));
+    c->h_small_bytes = want;
     return LS_OK;
+}
+
+ls_status read_device(ls_ctx* c, const void* dev, void* out, size_t bytes) {
+    if (bytes == 0) return LS_OK;
+    LS_TRY(small_host_buffer(c, bytes));
+    LS_LAUNCH(c, k_to_host, 1, 256, 0, (const uint8_t*)dev, (uint8_t*)c->hd_small, bytes);
+    LS_CUDA(c, cudaStreamSynchronize(c->stream));
+    std::memcpy(out, c->h_small, bytes);
+    return LS_OK;
+}
+
+ls_status read_scalars(ls_ctx* c, int first, int count, double* out) {
+    return read_device(c, c->scal + first, out, sizeof(double) * (size_t)count);
 }
 
 // ---------------------------------------------------------------------------
@@ -612,7 +643,7 @@ ls_status ls_create(ls_ctx** out, int I, int J, int K, int label_bytes, const ls
     ALLOC(c->d_int, (size_t)64);
 #undef ALLOC
     if (cudaMallocHost(&c->h_scal, sizeof(double) * S_COUNT) != cudaSuccess ||
-        cudaMallocHost(&c->h_int, sizeof(int) * 64) != cudaSuccess) {
+        cudaMallocHost(&c->h_int, sizeof(int) * 64) != cudaSuccess || small_host_buffer(c, 65536) != LS_OK) {
         ls_destroy(c);
         return LS_CUDA_ERROR;
     }
@@ -673,6 +704,7 @@ ls_status ls_destroy(ls_ctx* c) {
     }
     if (c->h_scal) cudaFreeHost(c->h_scal);
     if (c->h_int) cudaFreeHost(c->h_int);
+    if (c->h_small) cudaFreeHost(c->h_small);
     for (auto& r : c->regions) {
         cudaEventDestroy(r.start);
         cudaEventDestroy(r.stop);
@@ -780,6 +812,30 @@ static int field_group(int f) {
     }
 }
 
+// Device-to-device copy of `bytes` bytes on the SMs: 16-byte words, then the bytes after the
+// last whole word (the snapshot's and the staging buffers are 256-byte aligned).
+__global__ void k_dcopy(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, size_t bytes) {
+    const size_t n16 = bytes / 16;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n16; q += stride)
+        reinterpret_cast<uint4*>(dst)[q] = __ldg(reinterpret_cast<const uint4*>(src) + q);
+    for (size_t b = n16 * 16 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; b < bytes; b += stride) dst[b] = src[b];
+}
+
+// The snapshot, the rollback and the output staging copy on the SMs rather than with
+// cudaMemcpyAsync: the copy engines carry the output downloads to the host, and a step's
+// snapshot queued behind one of those would wait for it.
+static ls_status dcopy(ls_ctx* c, void* dst, const void* src, size_t bytes) {
+    if (bytes == 0) return LS_OK;
+    if ((((uintptr_t)dst) | ((uintptr_t)src)) & 15u) {
+        LS_CUDA(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, c->stream));
+        return LS_OK;
+    }
+    LS_LAUNCH(c, k_dcopy, grid_for(c, (long long)(bytes / 16 + 1)), kBlock, 0, (const uint8_t*)src, (uint8_t*)dst,
+              bytes);
+    return LS_OK;
+}
+
 ls_status ls_download_fields_async(ls_ctx* c, int count, const int* fields, void* const* hosts, int padded,
                                    void** done) {
     if (!c || count < 1 || !fields || !hosts || !done) return c ? set_error(c, LS_BAD_ARG, "bad arguments") : LS_BAD_ARG;
@@ -818,7 +874,7 @@ ls_status ls_download_fields_async(ls_ctx* c, int count, const int* fields, void
         size_t off = 0;
         for (Item& it : items) {
             void* dst = (char*)c->stage + off;
-            LS_CUDA(c, cudaMemcpyAsync(dst, it.dev, it.bytes, cudaMemcpyDeviceToDevice, c->stream));
+            LS_TRY(dcopy(c, dst, it.dev, it.bytes));
             it.dev = dst;
             off += (it.bytes + 255) & ~(size_t)255;
         }
@@ -1085,7 +1141,7 @@ ls_status ls_snapshot(ls_ctx* c) {
     c->flux_zero_pending_b = c->flux_zero_pending;  // the fluxes are copied as they are
     size_t np = (size_t)c->g.NP, d8 = np * sizeof(double);
     cudaStream_t s = c->stream;
-    LS_CUDA(c, cudaMemcpyAsync(c->b_frac, c->frac, np * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    LS_TRY(dcopy(c, c->b_frac, c->frac, np * sizeof(float)));
     if (c->lean) {
         // to host memory on the snapshot stream, from the state the context's stream has
         // reached here, in the order the step overwrites the fields (snap_fence)
@@ -1108,11 +1164,11 @@ ls_status ls_snapshot(ls_ctx* c) {
         c->snap_pending = kSnapP | kSnapFlux | kSnapSat | kSnapRest;
         return LS_OK;
     }
-    LS_CUDA(c, cudaMemcpyAsync(c->b_label, c->label, np * c->label_bytes, cudaMemcpyDeviceToDevice, s));
+    LS_TRY(dcopy(c, c->b_label, c->label, np * c->label_bytes));
     const std::pair<double*, double*> pairs[] = {
         {c->b_precip, c->precip}, {c->b_sat, c->sat}, {c->b_P, c->P}, {c->b_conc, c->conc},
         {c->b_acid, c->acid}, {c->b_fx, c->fx}, {c->b_fy, c->fy}, {c->b_fz, c->fz}};
-    for (auto& pr : pairs) LS_CUDA(c, cudaMemcpyAsync(pr.first, pr.second, d8, cudaMemcpyDeviceToDevice, s));
+    for (auto& pr : pairs) LS_TRY(dcopy(c, pr.first, pr.second, d8));
     return LS_OK;
 }
 

@@ -367,8 +367,7 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
     LS_TRY(finalize_max(c, grid, 1, S_RED0));
     double global_max_rate = 0.0;
     LS_TRY(read_scalars(c, S_RED0, 1, &global_max_rate));
-    LS_CUDA(c, cudaMemcpyAsync(c->h_int, c->d_int, sizeof(int) * 4, cudaMemcpyDeviceToHost, c->stream));
-    LS_CUDA(c, cudaStreamSynchronize(c->stream));
+    LS_TRY(read_device(c, c->d_int, c->h_int, sizeof(int) * 4));
     const int n_active = c->h_int[0], n_flux = c->h_int[1], n_flip = c->h_int[2];
     // sub-step count, src/Simulation.cpp:423-452
     double effective_fractional_rate = global_max_rate * c->p.time_scalar;
@@ -513,17 +512,14 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
         }
         LS_LAUNCH(c, k_dz_collect, grid, kBlock, 0, g, M, c->dz_sel, c->wcount);
         unsigned int nsel_u = 0;
-        LS_CUDA(c, cudaMemcpyAsync(&nsel_u, c->wcount, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
-        LS_CUDA(c, cudaStreamSynchronize(c->stream));
+        LS_TRY(read_device(c, c->wcount, &nsel_u, sizeof(unsigned int)));
         const int nsel = (int)nsel_u;
         if (nsel < 1 || nsel > n_active) return set_error(c, LS_CUDA_ERROR, "dissolution: bad sparse selection");
         const int sgrid = std::min(grid, (nsel + kBlock - 1) / kBlock);
         // S sorted by wavefront level
         LS_CUDA(c, cudaMemsetAsync(c->dz_count, 0, sizeof(int) * (nlev + 1), c->stream));
         LS_LAUNCH(c, k_dz_whist, sgrid, kBlock, 0, g, (const int*)c->dz_sel, nsel, c->dz_count);
-        LS_CUDA(c, cudaMemcpyAsync(hist.data(), c->dz_count, sizeof(int) * (nlev + 1), cudaMemcpyDeviceToHost,
-                                   c->stream));
-        LS_CUDA(c, cudaStreamSynchronize(c->stream));
+        LS_TRY(read_device(c, c->dz_count, hist.data(), sizeof(int) * (nlev + 1)));
         LS_TRY(prefix(nsel));
         LS_CUDA(c, cudaMemcpyAsync(c->dz_level_start, start.data(), sizeof(int) * (nlev + 1), cudaMemcpyHostToDevice,
                                    c->stream));
@@ -538,8 +534,7 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
         LS_LAUNCH(c, k_dz_check, sgrid, kBlock, 0, g, (const int*)c->dz_flips, (const int*)d_leached, (const int*)M,
                   d_flag);
         int bad = 0;
-        LS_CUDA(c, cudaMemcpyAsync(&bad, d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-        LS_CUDA(c, cudaStreamSynchronize(c->stream));
+        LS_TRY(read_device(c, d_flag, &bad, sizeof(int)));
         if (!bad) {
             done = true;
         } else {
@@ -556,9 +551,7 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
         // full schedule: every active voxel, sorted by wavefront level
         LS_CUDA(c, cudaMemsetAsync(c->dz_count, 0, sizeof(int) * (nlev + 1), c->stream));
         LS_LAUNCH(c, k_dz_hist<L>, grid, kBlock, 0, g, label, (const float*)c->frac, c->dz_count);
-        LS_CUDA(c, cudaMemcpyAsync(hist.data(), c->dz_count, sizeof(int) * (nlev + 1), cudaMemcpyDeviceToHost,
-                                   c->stream));
-        LS_CUDA(c, cudaStreamSynchronize(c->stream));
+        LS_TRY(read_device(c, c->dz_count, hist.data(), sizeof(int) * (nlev + 1)));
         LS_TRY(prefix(n_active));
         LS_CUDA(c, cudaMemcpyAsync(c->dz_level_start, start.data(), sizeof(int) * (nlev + 1), cudaMemcpyHostToDevice,
                                    c->stream));
@@ -568,8 +561,7 @@ static ls_status dissolve_t(ls_ctx* c, double dt, int* leached_out, ls_substep_i
         LS_TRY(run_sweeps(nullptr));
     }
     int h = 0;
-    LS_CUDA(c, cudaMemcpyAsync(&h, d_leached, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    LS_CUDA(c, cudaStreamSynchronize(c->stream));
+    LS_TRY(read_device(c, d_leached, &h, sizeof(int)));
     if (leached_out) *leached_out = h;
     c->p_ready = 0;
     return LS_OK;

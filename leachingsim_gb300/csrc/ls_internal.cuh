@@ -425,6 +425,9 @@ struct ls_ctx {
     double* h_scal;       // pinned host mirror
     int* d_int;           // device ints (counters, flags)
     int* h_int;           // pinned host mirror
+    void* h_small;        // mapped pinned host memory for small readbacks (read_device)
+    void* hd_small;       // its device address
+    size_t h_small_bytes;
 
     // accounting
     long long launches;
@@ -529,6 +532,7 @@ struct Timed {
 ls_status finalize_sum(ls_ctx* c, int nblocks, int nvals, int out_slot);
 ls_status finalize_max(ls_ctx* c, int nblocks, int nvals, int out_slot);
 ls_status read_scalars(ls_ctx* c, int first, int count, double* out);
+ls_status read_device(ls_ctx* c, const void* dev, void* out, size_t bytes);
 
 // device block reduction of nvals doubles per thread into partials[blockIdx.x*nvals + v]
 template <int NV>
