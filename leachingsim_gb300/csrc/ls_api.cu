@@ -679,6 +679,7 @@ ls_status ls_destroy(ls_ctx* c) {
                     c->sh_label, c->sh_sat, c->sh_precip, c->sh_frac, c->shf_label, c->shf_perm,
                     c->shf_visc, c->psb2, c->sat_q, c->dbits, c->sht_label, c->sht_fx, c->sht_fy, c->sht_fz,
                     c->shq_P, c->shq_C, c->shq_K, c->shq_V, c->shq_fx, c->shq_fy, c->shq_fz,
+                    c->solid_bits, c->solid_bits_b,
                     c->wlist, c->wcount, c->olist_counts, c->dz_tab, c->kmult, c->dz_sel, c->dz_flips, c->dz_save_frac,
                     c->dz_save_precip, c->dz_save_conc, c->dz_save_label};
     for (void* q : ptrs) rel(q);
@@ -1138,7 +1139,10 @@ ls_status ls_dissolve(ls_ctx* c, double dt, int* leached, ls_substep_info* info)
 ls_status ls_snapshot(ls_ctx* c) {
     if (!c) return LS_BAD_ARG;
     Timed tm(c, LS_T_SNAPSHOT);
-    c->flux_zero_pending_b = c->flux_zero_pending;  // the fluxes are copied as they are
+    // the fluxes are copied as they are, with the zeroing still owed and the voxels it covers
+    c->flux_zero_pending_b = c->flux_zero_pending;
+    if (c->flux_zero_pending)
+        LS_TRY(dcopy(c, c->solid_bits_b, c->solid_bits, sizeof(unsigned int) * (size_t)((c->g.N + 31) / 32)));
     size_t np = (size_t)c->g.NP, d8 = np * sizeof(double);
     cudaStream_t s = c->stream;
     LS_TRY(dcopy(c, c->b_frac, c->frac, np * sizeof(float)));
@@ -1189,6 +1193,8 @@ ls_status ls_rollback(ls_ctx* c) {
         for (auto& pr : pairs) LS_CUDA(c, cudaMemcpyAsync(pr.first, pr.second, d8, kind, s));
     }
     c->flux_zero_pending = c->flux_zero_pending_b;
+    if (c->flux_zero_pending)
+        LS_TRY(dcopy(c, c->solid_bits, c->solid_bits_b, sizeof(unsigned int) * (size_t)((c->g.N + 31) / 32)));
     c->fx_is_shadow = 0;
     c->p_ready = 0;
     c->p_eff_prev = 0.0;

@@ -346,6 +346,8 @@ struct ls_ctx {
     int flux_valid;
     int flux_zero_pending;    // the Rock / Precipitate fluxes are still to be zeroed (flux_zero_now)
     int flux_zero_pending_b;  // the same at the last snapshot
+    unsigned int* solid_bits;    // the voxels that were Rock or Precipitate at the last transport
+    unsigned int* solid_bits_b;  // the same at the last snapshot
     int fx_is_shadow;         // fx / fy / fz equal the change-tracking shadows at every voxel
     double flux_consts[2];
 

@@ -914,15 +914,30 @@ __global__ void __launch_bounds__(kBlock) k_minmax(Grid g, const double* __restr
     block_max_store<2>(m, partials);
 }
 
-// zero the flux of Rock and Precipitate voxels (src/Simulation.cpp:1134-1149), after the
-// solve; no transport row uses the flux of such a voxel
+// The Rock and Precipitate voxels at the end of a transport solve, one bit each: the voxels
+// whose flux the reference zeroes then (src/Simulation.cpp:1134-1149; no transport row uses
+// the flux of such a voxel). Labels change after the solve (precipitation makes Pore voxels
+// Precipitate), so the deferred zeroing works from these bits, not from the labels it finds.
 template <typename L>
-__global__ void k_zero_solid_flux(Grid g, const L* __restrict__ label, double* __restrict__ fx,
+__global__ void k_solid_bits(Grid g, const L* __restrict__ label, unsigned int* __restrict__ bits) {
+    for (long long r0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); r0 < g.N;
+         r0 += (long long)gridDim.x * blockDim.x) {
+        const long long r = r0 + (threadIdx.x & 31u);
+        bool s = false;
+        if (r < g.N) {
+            const int t = (int)label[r];
+            s = t == kRock || t == kPrecipitate;
+        }
+        const unsigned int w = __ballot_sync(0xffffffffu, s);
+        if ((threadIdx.x & 31u) == 0u) bits[r0 >> 5] = w;
+    }
+}
+
+__global__ void k_zero_solid_flux(Grid g, const unsigned int* __restrict__ bits, double* __restrict__ fx,
                                   double* __restrict__ fy, double* __restrict__ fz) {
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.N;
          r += (long long)gridDim.x * blockDim.x) {
-        int t = (int)label[r];
-        if (t == kRock || t == kPrecipitate) { fx[r] = 0.0; fy[r] = 0.0; fz[r] = 0.0; }
+        if ((bits[r >> 5] >> (r & 31)) & 1u) { fx[r] = 0.0; fy[r] = 0.0; fz[r] = 0.0; }
     }
 }
 
@@ -1241,7 +1256,14 @@ static ls_status transport_t(ls_ctx* c, double dt, int which, ls_solve_info* ci,
         if (acid_lane >= 0) c->acid_zero = (st == LS_OK && ((zero_lanes >> acid_lane) & 1)) ? 1 : 0;
     }
     if (st != LS_OK && st != LS_NOT_CONVERGED && st != LS_NONFINITE) return st;
-    c->flux_zero_pending = 1;  // the Rock / Precipitate fluxes are zeroed when next looked at
+    // the Rock / Precipitate fluxes are zeroed when next looked at: record which they are
+    if (!c->solid_bits) {
+        const size_t words = (size_t)((c->g.N + 31) / 32);
+        LS_TRY(dalloc_t(c, &c->solid_bits, words));
+        LS_TRY(dalloc_t(c, &c->solid_bits_b, words));
+    }
+    LS_LAUNCH(c, k_solid_bits<L>, grid_for(c, c->g.N), kBlock, 0, c->g, (const L*)c->label, c->solid_bits);
+    c->flux_zero_pending = 1;
     return st;
 }
 
@@ -1249,18 +1271,15 @@ static ls_status transport_t(ls_ctx* c, double dt, int which, ls_solve_info* ci,
 // (src/Simulation.cpp:1134-1149). Nothing in a time step reads those fluxes again before the
 // next step's flux evaluation overwrites them, so the zeroing waits until something looks:
 // the field transfers, counts and asynchronous downloads and the saturation updates call
-// this first (a snapshot keeps the pending state with the fields it copies). Until then the
-// fluxes keep equal to the change-tracking shadows, and the next flux evaluation need not
-// restore them.
+// this first. It zeroes the voxels recorded at the solve (k_solid_bits), whatever their
+// labels have become since; a snapshot keeps the pending state and those bits with the
+// fields it copies. Until then the fluxes keep equal to the change-tracking shadows, and the
+// next flux evaluation need not restore them.
 ls_status flux_zero_now(ls_ctx* c) {
     if (!c->flux_zero_pending) return LS_OK;
     snap_fence(c, kSnapFlux);
-    if (c->label_bytes == 1)
-        LS_LAUNCH(c, k_zero_solid_flux<uint8_t>, grid_for(c, c->g.N), kBlock, 0, c->g, (const uint8_t*)c->label,
-                  c->fx, c->fy, c->fz);
-    else
-        LS_LAUNCH(c, k_zero_solid_flux<uint16_t>, grid_for(c, c->g.N), kBlock, 0, c->g,
-                  (const uint16_t*)c->label, c->fx, c->fy, c->fz);
+    LS_LAUNCH(c, k_zero_solid_flux, grid_for(c, c->g.N), kBlock, 0, c->g, (const unsigned int*)c->solid_bits, c->fx,
+              c->fy, c->fz);
     c->flux_zero_pending = 0;
     c->fx_is_shadow = 0;
     return LS_OK;
