@@ -461,7 +461,8 @@ __global__ void __launch_bounds__(kTcThreads) k_lp_conv_tc(LpDims d, const bf16*
 // ---------------------------------------------------------------------------
 // The convolution streamed through z on the tensor cores, its input brought in by the tensor
 // memory accelerator (TMA). A persistent CTA (one per SM) runs tiles of 8 (x) x 16 (y) output
-// voxels x ZT planes. For each input plane p of a tile (z0 - 1 .. z0 + ZT) one TMA load per
+// voxels x zt planes (TmShape::ZT, fewer on coarse grids, so that the tiles cover the SMs).
+// For each input plane p of a tile (z0 - 1 .. z0 + zt) one TMA load per
 // 8-channel chunk brings the plane's 10 x 18 halo into a stage of a ring of shared-memory
 // buffers (zeros outside the grid: the tensor map's out-of-bounds fill), and nine (dy, dx) x
 // CIN/16 tcgen05.mma instructions apply the plane to the three output planes it feeds at once:
