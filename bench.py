@@ -11,7 +11,9 @@ saturation, surface clogging, conc + acid transport, precipitation, dissolution,
 snapshot). `value` times --steps steps after --warmup steps with the state resident
 in HBM; `e2e` runs the whole configured simulation (tmax / dt steps) from a label
 image in pinned host memory, reading every output step's fields back into pinned
-host memory (file writing excluded).
+host memory (file writing excluded); `e2e.parts` splits its wall time (context
+creation and upload, the cold first step, the other steps' median / mean / maximum,
+the output steps, the final drain of the copies).
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 
